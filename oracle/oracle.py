@@ -1,0 +1,267 @@
+"""ORACLE - test infrastructure only.
+
+ctypes front-ends for
+  * ``libgz_oracle.so``  - the CPU restatement of the reference hash Splitter
+    (oracle/split_oracle.cc); travels everywhere, built by ``build()``;
+  * ``_ref/libgzref_splitter.so`` - the reference Splitter itself compiled from the
+    reference tree (oracle/ref/Makefile); exists only where the reference sources and
+    pyarrow are present, and is used to pin the restatement and to make golden fixtures.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg import this.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import tempfile
+from dataclasses import dataclass
+from typing import List, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "libgz_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libgzref_splitter.so")
+REF_HASH_SO = os.path.join(HERE, "_ref", "libgzref_hash.so")
+
+_I64P = ctypes.POINTER(ctypes.c_int64)
+
+
+def build_oracle(force: bool = False) -> str:
+    src = os.path.join(HERE, "split_oracle.cc")
+    if force or not os.path.exists(ORACLE_SO) or os.path.getmtime(ORACLE_SO) < max(
+            os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "spark_hash.h"))):
+        subprocess.check_call(["g++", "-std=c++17", "-O3", "-fPIC", "-shared", src,
+                               "-o", ORACLE_SO])
+    return ORACLE_SO
+
+
+def build_ref(ref_root: str = "/root/reference") -> bool:
+    """Compile the reference Splitter (x86_64 + pyarrow + reference tree only)."""
+    if not os.path.isdir(os.path.join(ref_root, "native-sql-engine")):
+        return False
+    subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "ref"), f"REF={ref_root}"])
+    return os.path.exists(REF_SO)
+
+
+@dataclass
+class SplitOutput:
+    partition_lengths: np.ndarray
+    raw_partition_lengths: np.ndarray
+    bytes_written: int
+    bytes_spilled: int
+    data: bytes
+
+    def partition_bytes(self, pid: int) -> bytes:
+        start = int(self.partition_lengths[:pid].sum())
+        return self.data[start:start + int(self.partition_lengths[pid])]
+
+
+class OracleSplitter:
+    """Restated reference Splitter (hash partitioning, compression off, write_schema off)."""
+
+    _lib = None
+
+    @classmethod
+    def lib(cls):
+        if cls._lib is None:
+            lib = ctypes.CDLL(build_oracle())
+            lib.gzo_make.restype = ctypes.c_void_p
+            lib.gzo_make.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                                     ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64,
+                                     ctypes.c_int32, ctypes.c_int32, ctypes.c_char_p,
+                                     ctypes.c_int]
+            lib.gzo_split.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
+                                      ctypes.c_void_p, ctypes.c_int32, ctypes.c_char_p,
+                                      ctypes.c_int]
+            lib.gzo_stop.restype = ctypes.c_int64
+            lib.gzo_stop.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p,
+                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p,
+                                     ctypes.c_int]
+            lib.gzo_file_bytes.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+            lib.gzo_last_pids.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+            lib.gzo_spill.restype = ctypes.c_int64
+            lib.gzo_spill.argtypes = [ctypes.c_void_p, ctypes.c_int64]
+            lib.gzo_close.argtypes = [ctypes.c_void_p]
+            lib.gzo_hash_int.restype = ctypes.c_int32
+            lib.gzo_hash_int.argtypes = [ctypes.c_int32, ctypes.c_int32]
+            lib.gzo_hash_long.restype = ctypes.c_int32
+            lib.gzo_hash_long.argtypes = [ctypes.c_int64, ctypes.c_int32]
+            lib.gzo_murmur3_bytes.restype = ctypes.c_uint32
+            lib.gzo_murmur3_bytes.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32]
+            lib.gzo_pmod.restype = ctypes.c_int32
+            lib.gzo_pmod.argtypes = [ctypes.c_int32, ctypes.c_int32]
+            cls._lib = lib
+        return cls._lib
+
+    def __init__(self, schema, num_partitions: int, key_cols: Sequence[int],
+                 offheap_per_task: int = 0, buffer_size: int = 4096, prefer_spill: bool = True):
+        self.P = num_partitions
+        types = np.array([f.code for f in schema], np.int32)
+        keys = np.array(key_cols, np.int32)
+        err = ctypes.create_string_buffer(512)
+        self.h = self.lib().gzo_make(types.ctypes.data, len(types), num_partitions,
+                                     keys.ctypes.data, len(keys), offheap_per_task,
+                                     buffer_size, int(prefer_spill), err, 512)
+        if not self.h:
+            raise ValueError(err.value.decode())
+
+    def split(self, batch) -> None:
+        addrs, sizes = batch.addrs_sizes()
+        err = ctypes.create_string_buffer(512)
+        if self.lib().gzo_split(self.h, batch.num_rows, addrs.ctypes.data, sizes.ctypes.data,
+                                len(addrs), err, 512):
+            raise ValueError(err.value.decode())
+
+    def last_pids(self, num_rows: int) -> np.ndarray:
+        out = np.zeros(num_rows, np.uint16)
+        self.lib().gzo_last_pids(self.h, out.ctypes.data)
+        return out
+
+    def spill(self, size: int) -> int:
+        return self.lib().gzo_spill(self.h, size)
+
+    def stop(self) -> SplitOutput:
+        lengths = np.zeros(self.P, np.int64)
+        raw = np.zeros(self.P, np.int64)
+        metrics = np.zeros(3, np.int64)
+        err = ctypes.create_string_buffer(512)
+        n = self.lib().gzo_stop(self.h, None, lengths.ctypes.data, raw.ctypes.data,
+                                metrics.ctypes.data, err, 512)
+        if n < 0:
+            raise ValueError(err.value.decode())
+        data = np.zeros(n, np.uint8)
+        if n:
+            self.lib().gzo_file_bytes(self.h, data.ctypes.data)
+        return SplitOutput(lengths, raw, int(metrics[0]), int(metrics[1]), data.tobytes())
+
+    def close(self):
+        if self.h:
+            self.lib().gzo_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def run_oracle(schema, batches, num_partitions, key_cols, **opts) -> SplitOutput:
+    s = OracleSplitter(schema, num_partitions, key_cols, **opts)
+    for b in batches:
+        s.split(b)
+    out = s.stop()
+    s.close()
+    return out
+
+
+# ---------------------------------------------------------------------------------------
+# the reference itself (this container only)
+def to_pyarrow_schema(schema):
+    import pyarrow as pa
+    m = {"null": pa.null(), "bool": pa.bool_(), "int8": pa.int8(), "uint8": pa.uint8(),
+         "int16": pa.int16(), "uint16": pa.uint16(), "float16": pa.float16(),
+         "int32": pa.int32(), "uint32": pa.uint32(), "float32": pa.float32(),
+         "date32": pa.date32(), "time32": pa.time32("ms"), "int64": pa.int64(),
+         "uint64": pa.uint64(), "float64": pa.float64(), "date64": pa.date64(),
+         "time64": pa.time64("us"), "timestamp": pa.timestamp("us"),
+         "decimal128": pa.decimal128(30, 2), "utf8": pa.string(), "binary": pa.binary()}
+    return pa.schema([pa.field(f.name, m[f.type], f.nullable) for f in schema])
+
+
+class RefSplitter:
+    """The reference Splitter compiled from the reference tree (oracle/_ref)."""
+
+    _lib = None
+
+    @classmethod
+    def available(cls) -> bool:
+        return os.path.exists(REF_SO)
+
+    @classmethod
+    def lib(cls):
+        if cls._lib is None:
+            lib = ctypes.CDLL(REF_SO)
+            lib.gzref_make.restype = ctypes.c_void_p
+            lib.gzref_make.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32,
+                                       ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64,
+                                       ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                       ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
+                                       ctypes.c_int]
+            lib.gzref_split.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_int32, ctypes.c_char_p,
+                                        ctypes.c_int]
+            lib.gzref_stop.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]
+            lib.gzref_compressed_size.restype = ctypes.c_int64
+            lib.gzref_compressed_size.argtypes = [ctypes.c_void_p, ctypes.c_int32,
+                                                  ctypes.c_void_p, ctypes.c_void_p,
+                                                  ctypes.c_int32]
+            lib.gzref_spill.argtypes = [ctypes.c_void_p, ctypes.c_int64, _I64P]
+            lib.gzref_close.argtypes = [ctypes.c_void_p]
+            cls._lib = lib
+        return cls._lib
+
+    def __init__(self, schema, num_partitions: int, key_cols: Sequence[int],
+                 offheap_per_task: int = 0, buffer_size: int = 4096, prefer_spill: bool = True,
+                 write_schema: bool = False):
+        self.P = num_partitions
+        self.tmp = tempfile.TemporaryDirectory(prefix="gzref-")
+        self.data_file = os.path.join(self.tmp.name, "data")
+        sbytes = to_pyarrow_schema(schema).serialize().to_pybytes()
+        self._sbuf = ctypes.create_string_buffer(sbytes, len(sbytes))
+        keys = np.array(key_cols, np.int32)
+        err = ctypes.create_string_buffer(512)
+        self.h = self.lib().gzref_make(self._sbuf, len(sbytes), num_partitions,
+                                       keys.ctypes.data, len(keys), offheap_per_task,
+                                       buffer_size, int(prefer_spill), int(write_schema),
+                                       self.data_file.encode(),
+                                       os.path.join(self.tmp.name, "local").encode(), err, 512)
+        if not self.h:
+            raise ValueError(err.value.decode())
+
+    def split(self, batch) -> None:
+        addrs, sizes = batch.addrs_sizes()
+        err = ctypes.create_string_buffer(512)
+        if self.lib().gzref_split(self.h, batch.num_rows, addrs.ctypes.data, sizes.ctypes.data,
+                                  len(addrs), err, 512):
+            raise ValueError(err.value.decode())
+
+    def compressed_size(self, batch) -> int:
+        addrs, sizes = batch.addrs_sizes()
+        return self.lib().gzref_compressed_size(self.h, batch.num_rows, addrs.ctypes.data,
+                                                sizes.ctypes.data, len(addrs))
+
+    def spill(self, size: int) -> int:
+        actual = ctypes.c_int64(0)
+        self.lib().gzref_spill(self.h, size, ctypes.byref(actual))
+        return actual.value
+
+    def stop(self) -> SplitOutput:
+        lengths = np.zeros(self.P, np.int64)
+        raw = np.zeros(self.P, np.int64)
+        metrics = np.zeros(2, np.int64)
+        err = ctypes.create_string_buffer(512)
+        if self.lib().gzref_stop(self.h, lengths.ctypes.data, raw.ctypes.data,
+                                 metrics.ctypes.data, err, 512):
+            raise ValueError(err.value.decode())
+        with open(self.data_file, "rb") as f:
+            data = f.read()
+        return SplitOutput(lengths, raw, int(metrics[0]), int(metrics[1]), data)
+
+    def close(self):
+        if self.h:
+            self.lib().gzref_close(self.h)
+            self.h = None
+        self.tmp.cleanup()
+
+
+def run_ref(schema, batches, num_partitions, key_cols, **opts) -> SplitOutput:
+    s = RefSplitter(schema, num_partitions, key_cols, **opts)
+    for b in batches:
+        s.split(b)
+    out = s.stop()
+    s.close()
+    return out

@@ -1,0 +1,2 @@
+#pragma once
+#include "gandiva_stub.h"

@@ -1,0 +1,742 @@
+/*
+ * ORACLE — test infrastructure only.  A plain, row-at-a-time CPU restatement of the
+ * reference hash Splitter (native-sql-engine/cpp/src/shuffle/splitter.{h,cc}), used by
+ * tests/, the smoke check and bench.py's CPU-baseline leg to check the CUDA product.
+ * It is never linked into, loaded by or called from the product library.
+ *
+ * What it restates (reference file:line in native-sql-engine/cpp/src/shuffle/):
+ *   Init: column classification fixed-then-binary, P <= 64K, buffer_size <= 32K  splitter.cc:216-335
+ *   hash chain (seed 42, Spark Murmur3, nulls pass the seed) + pmod + histogram  splitter.cc:1402-1470
+ *   DoSplit: sticky input_has_null_ quirk, per-pid prepare/emit/spill policy     splitter.cc:855-938
+ *   CalculateSplitBatchSize (empirical binary sizes, offheap rule)               splitter.cc:800-853
+ *   AllocatePartitionBuffers (validity iff input_has_null_, 0xff fill)           splitter.cc:610-713
+ *   Split{FixedWidthValue,Validity,Binary}Buffer / SplitBoolType                 splitter.cc:939-1303
+ *   CacheRecordBatch (slice, raw size, IPC payload)                              splitter.cc:438-608
+ *   SpillPartition / SpillLargestPartition / SpillFixedSize                      splitter.cc:741-799
+ *   Stop / WriteCachedRecordBatchAndClose / EOS                                  splitter.cc:84-172,395-437
+ * Arrow IPC framing restates the Arrow C++ writer (continuation token, int32 metadata
+ * length padded to 8, flatbuffer Message{RecordBatch}, 8-byte padded body; a validity
+ * buffer is written only when the slice has nulls) with a small FlatBufferBuilder that
+ * follows the published flatbuffers build algorithm (back-to-front, vtable dedup).
+ *
+ * Spilled payloads are kept in host memory ("spill files" are byte vectors); the bytes of a
+ * partition do not depend on when it was spilled (splitter.cc:75-143).
+ */
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <memory>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "spark_hash.h"
+
+namespace {
+
+using namespace gzoracle;
+
+// Type codes shared with include/gz_split.h (GZ_TYPE_*).
+enum TypeCode {
+  T_NULL = 0, T_BOOL = 1, T_INT8 = 2, T_UINT8 = 3, T_INT16 = 4, T_UINT16 = 5,
+  T_HALF_FLOAT = 6, T_INT32 = 7, T_UINT32 = 8, T_FLOAT32 = 9, T_DATE32 = 10,
+  T_TIME32 = 11, T_INT64 = 12, T_UINT64 = 13, T_FLOAT64 = 14, T_DATE64 = 15,
+  T_TIME64 = 16, T_TIMESTAMP = 17, T_DECIMAL128 = 18, T_STRING = 19, T_BINARY = 20,
+};
+
+int ByteWidth(int t) {
+  switch (t) {
+    case T_INT8: case T_UINT8: return 1;
+    case T_INT16: case T_UINT16: case T_HALF_FLOAT: return 2;
+    case T_INT32: case T_UINT32: case T_FLOAT32: case T_DATE32: case T_TIME32: return 4;
+    case T_INT64: case T_UINT64: case T_FLOAT64: case T_DATE64: case T_TIME64:
+    case T_TIMESTAMP: return 8;
+    case T_DECIMAL128: return 16;
+    default: return 0;
+  }
+}
+bool IsBinary(int t) { return t == T_STRING || t == T_BINARY; }
+
+int64_t BytesForBits(int64_t n) { return (n + 7) / 8; }
+int64_t Pad8(int64_t n) { return (n + 7) & ~int64_t(7); }
+bool GetBit(const uint8_t* b, int64_t i) { return (b[i >> 3] >> (i & 7)) & 1; }
+void ClearBit(uint8_t* b, int64_t i) { b[i >> 3] &= (uint8_t)~(1u << (i & 7)); }
+
+// ---------------------------------------------------------------------------------------
+// Minimal FlatBufferBuilder: the published flatbuffers algorithm (buffer grows toward the
+// front; offsets are distances from the end; tables end with a vtable that is shared when an
+// identical one was written before).
+class FlatBuilder {
+ public:
+  uint32_t Size() const { return (uint32_t)buf_.size(); }
+  void Pad(size_t n) { buf_.insert(buf_.begin(), n, 0); }
+  void Align(size_t a) {
+    minalign_ = std::max(minalign_, a);
+    Pad((~buf_.size() + 1) & (a - 1));
+  }
+  void PreAlign(size_t len, size_t a) {
+    if (len == 0) return;
+    minalign_ = std::max(minalign_, a);
+    Pad((~(buf_.size() + len) + 1) & (a - 1));
+  }
+  template <typename T>
+  uint32_t Push(T v) {
+    Align(sizeof(T));
+    uint8_t tmp[sizeof(T)];
+    memcpy(tmp, &v, sizeof(T));
+    buf_.insert(buf_.begin(), tmp, tmp + sizeof(T));
+    return Size();
+  }
+  void PushBytes(const uint8_t* p, size_t n) { buf_.insert(buf_.begin(), p, p + n); }
+  uint32_t ReferTo(uint32_t off) {
+    Align(4);
+    return Size() - off + 4;
+  }
+  // vector of 16-byte structs made of two int64 (FieldNode / Buffer)
+  uint32_t StructVector16(const std::vector<std::pair<int64_t, int64_t>>& v) {
+    PreAlign(v.size() * 16, 4);
+    PreAlign(v.size() * 16, 8);
+    std::vector<uint8_t> raw(v.size() * 16);
+    for (size_t i = 0; i < v.size(); i++) {
+      memcpy(&raw[i * 16], &v[i].first, 8);
+      memcpy(&raw[i * 16 + 8], &v[i].second, 8);
+    }
+    PushBytes(raw.data(), raw.size());
+    return Push<uint32_t>((uint32_t)v.size());
+  }
+  void StartTable() {
+    fields_.clear();
+    table_start_ = Size();
+  }
+  template <typename T>
+  void AddScalar(uint16_t voff, T v, T def) {
+    if (v == def) return;
+    fields_.push_back({voff, Push<T>(v)});
+  }
+  void AddOffset(uint16_t voff, uint32_t off) {
+    if (off == 0) return;
+    fields_.push_back({voff, Push<uint32_t>(ReferTo(off))});
+  }
+  uint32_t EndTable() {
+    uint32_t loc = Push<int32_t>(0);
+    uint16_t maxv = 4;
+    for (auto& f : fields_) maxv = std::max<uint16_t>(maxv, f.first + 2);
+    std::vector<uint16_t> vt(maxv / 2, 0);
+    vt[0] = maxv;
+    vt[1] = (uint16_t)(loc - table_start_);
+    for (auto& f : fields_) vt[f.first / 2] = (uint16_t)(loc - f.second);
+    std::vector<uint8_t> vtb(maxv);
+    memcpy(vtb.data(), vt.data(), maxv);
+    uint32_t use = 0;
+    for (uint32_t prev : vtables_) {
+      const uint8_t* p = &buf_[buf_.size() - prev];
+      uint16_t sz;
+      memcpy(&sz, p, 2);
+      if (sz == maxv && memcmp(p, vtb.data(), maxv) == 0) {
+        use = prev;
+        break;
+      }
+    }
+    if (use == 0) {
+      PushBytes(vtb.data(), vtb.size());
+      use = Size();
+      vtables_.push_back(use);
+    }
+    int32_t soff = (int32_t)use - (int32_t)loc;
+    memcpy(&buf_[buf_.size() - loc], &soff, 4);
+    return loc;
+  }
+  std::vector<uint8_t> Finish(uint32_t root) {
+    PreAlign(4, minalign_);
+    Push<uint32_t>(ReferTo(root));
+    return buf_;
+  }
+
+ private:
+  std::vector<uint8_t> buf_;
+  size_t minalign_ = 1;
+  uint32_t table_start_ = 0;
+  std::vector<std::pair<uint16_t, uint32_t>> fields_;
+  std::vector<uint32_t> vtables_;
+};
+
+// A body buffer of an IPC record batch; `len == 0` is an empty (placeholder) buffer.
+struct BodyBuf {
+  const uint8_t* data;
+  int64_t len;
+};
+
+// Arrow IPC encapsulated message for one record batch (MetadataVersion V5, no codec).
+std::vector<uint8_t> EncodeRecordBatch(int64_t length,
+                                       const std::vector<std::pair<int64_t, int64_t>>& nodes,
+                                       const std::vector<BodyBuf>& body, int64_t* body_len) {
+  std::vector<std::pair<int64_t, int64_t>> bufmeta;
+  int64_t off = 0;
+  for (auto& b : body) {
+    bufmeta.push_back({off, b.len});
+    off += Pad8(b.len);
+  }
+  *body_len = off;
+  FlatBuilder fb;
+  uint32_t fnodes = fb.StructVector16(nodes);
+  uint32_t fbufs = fb.StructVector16(bufmeta);
+  fb.StartTable();  // RecordBatch: length(0) nodes(1) buffers(2) compression(3) variadic(4)
+  fb.AddScalar<int64_t>(4, length, 0);
+  fb.AddOffset(8, fbufs);
+  fb.AddOffset(6, fnodes);
+  uint32_t rb = fb.EndTable();
+  fb.StartTable();  // Message: version(0) header_type(1) header(2) bodyLength(3) custom_metadata(4)
+  fb.AddScalar<int64_t>(10, off, 0);
+  fb.AddOffset(8, rb);
+  fb.AddScalar<int16_t>(4, 4 /*V5*/, 0);
+  fb.AddScalar<uint8_t>(6, 3 /*RecordBatch*/, 0);
+  uint32_t msg = fb.EndTable();
+  std::vector<uint8_t> meta = fb.Finish(msg);
+  int64_t padded = Pad8(meta.size() + 8);
+  std::vector<uint8_t> out;
+  out.reserve(padded + off);
+  uint32_t cont = 0xFFFFFFFFu;
+  int32_t mlen = (int32_t)(padded - 8);
+  out.insert(out.end(), (uint8_t*)&cont, (uint8_t*)&cont + 4);
+  out.insert(out.end(), (uint8_t*)&mlen, (uint8_t*)&mlen + 4);
+  out.insert(out.end(), meta.begin(), meta.end());
+  out.resize(padded, 0);
+  for (auto& b : body) {
+    if (b.len > 0) out.insert(out.end(), b.data, b.data + b.len);
+    out.resize(out.size() + (Pad8(b.len) - b.len), 0);
+  }
+  return out;
+}
+
+struct Field {
+  int type;
+  std::string name;
+};
+
+struct InCol {
+  const uint8_t* validity = nullptr;  // nullptr when the validity buffer is empty
+  const uint8_t* offsets = nullptr;
+  const uint8_t* values = nullptr;
+  int64_t null_count = 0;
+};
+
+struct Options {
+  int64_t offheap_per_task = 0;
+  int32_t buffer_size = 4096;
+  int32_t batch_compress_threshold = 256;
+  bool prefer_spill = true;
+  bool write_schema = false;
+};
+
+// Per (array column, partition) buffers, mirroring partition_buffers_ (splitter.h:242-244).
+struct PartBufs {
+  bool has_validity = false;
+  std::vector<uint8_t> validity;  // capacity bytes, 0xff filled
+  std::vector<uint8_t> values;    // fixed: cap * width; bool: bitmap
+  std::vector<int32_t> offsets;   // binary: cap + 1
+  std::vector<uint8_t> chars;     // binary values (grows)
+  int64_t chars_used = 0;
+};
+
+class OracleSplitter {
+ public:
+  OracleSplitter(std::vector<Field> fields, int P, std::vector<int> keys, Options o)
+      : fields_(std::move(fields)), P_(P), keys_(std::move(keys)), opt_(o) {}
+
+  std::string Init() {
+    if (P_ <= 0 || P_ > 65536) return "num_partitions must be in [1, 65536]";
+    if (opt_.buffer_size > 32768) return "buffer_size must be <= 32768";
+    std::vector<int> bin;
+    for (int i = 0; i < (int)fields_.size(); i++) {
+      int t = fields_[i].type;
+      if (IsBinary(t)) bin.push_back(i);
+      else if (t == T_NULL) continue;
+      else if (t == T_BOOL || ByteWidth(t) > 0) array_idx_.push_back(i);
+      else return "unsupported field type";
+    }
+    fixed_cnt_ = (int)array_idx_.size();
+    array_idx_.insert(array_idx_.end(), bin.begin(), bin.end());
+    for (int k : keys_) {
+      if (k < 0 || k >= (int)fields_.size()) return "key column out of range";
+      int t = fields_[k].type;
+      if (!(t == T_BOOL || t == T_INT8 || t == T_INT16 || t == T_INT32 || t == T_DATE32 ||
+            t == T_FLOAT32 || t == T_INT64 || t == T_FLOAT64 || t == T_STRING))
+        return "key type has no Spark hash";
+    }
+    int A = (int)array_idx_.size();
+    bufs_.assign(A, std::vector<PartBufs>(P_));
+    input_has_null_.assign(A, false);
+    empirical_.assign(A - fixed_cnt_, 0);
+    cap_.assign(P_, 0);
+    base_.assign(P_, 0);
+    cached_.assign(P_, {});
+    cached_size_.assign(P_, 0);
+    spilled_.assign(P_, {});
+    writer_.assign(P_, false);
+    spill_opened_.assign(P_, false);
+    partition_lengths_.assign(P_, 0);
+    raw_lengths_.assign(P_, 0);
+    return "";
+  }
+
+  // buffers: flat list in schema order [validity, (offsets), values] per non-null field
+  std::string Split(int32_t n, const int64_t* addrs, const int64_t* sizes, int nbuf) {
+    std::vector<InCol> cols(fields_.size());
+    int idx = 0;
+    for (size_t f = 0; f < fields_.size(); f++) {
+      if (fields_[f].type == T_NULL) continue;
+      if (idx >= nbuf) return "insufficient number of buffers";
+      InCol c;
+      if (sizes[idx] > 0 && addrs[idx] != 0) c.validity = (const uint8_t*)addrs[idx];
+      idx++;
+      if (IsBinary(fields_[f].type)) {
+        if (idx >= nbuf) return "insufficient number of buffers";
+        c.offsets = (const uint8_t*)addrs[idx++];
+      }
+      if (idx >= nbuf) return "insufficient number of buffers";
+      c.values = (const uint8_t*)addrs[idx++];
+      if (c.validity) {
+        int64_t valid = 0;
+        for (int64_t i = 0; i < n; i++) valid += GetBit(c.validity, i);
+        c.null_count = n - valid;
+      }
+      cols[f] = c;
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    ComputePid(n, cols);
+    compute_pid_ns_ += std::chrono::duration_cast<std::chrono::nanoseconds>(
+                           std::chrono::steady_clock::now() - t0).count();
+    return DoSplit(n, cols);
+  }
+
+  // SpillFixedSize (splitter.cc:741-756)
+  int64_t SpillFixedSize(int64_t size) {
+    int64_t cur = 0;
+    int tries = 0;
+    while (cur < size && tries < 5) {
+      tries++;
+      int64_t got;
+      if (SpillLargest(&got) < 0) break;
+      cur += got;
+    }
+    return cur;
+  }
+
+  std::string Stop(const char* data_file, std::vector<uint8_t>* file_bytes) {
+    std::vector<uint8_t> out;
+    for (int p = 0; p < P_; p++) {
+      CacheRecordBatch(p, true);
+      if (cached_size_[p] > 0) writer_[p] = true;
+      if (writer_[p]) {
+        size_t before = out.size();
+        if (!spill_opened_[p] && cached_size_[p] == 0) return "Partition writer got empty partition";
+        if (spill_opened_[p]) {
+          out.insert(out.end(), spilled_[p].begin(), spilled_[p].end());
+          bytes_spilled_ += (int64_t)spilled_[p].size();
+          spilled_[p].clear();
+        }
+        for (auto& m : cached_[p]) out.insert(out.end(), m.begin(), m.end());
+        cached_[p].clear();
+        cached_size_[p] = 0;
+        uint32_t eos[2] = {0xFFFFFFFFu, 0};
+        out.insert(out.end(), (uint8_t*)eos, (uint8_t*)eos + 8);
+        partition_lengths_[p] = (int64_t)(out.size() - before);
+        bytes_written_ += partition_lengths_[p];
+      } else {
+        partition_lengths_[p] = 0;
+      }
+    }
+    if (data_file && data_file[0]) {
+      FILE* f = fopen(data_file, "wb");
+      if (!f) return std::string("cannot open data file ") + data_file;
+      if (!out.empty() && fwrite(out.data(), 1, out.size(), f) != out.size()) {
+        fclose(f);
+        return "short write";
+      }
+      fclose(f);
+    }
+    if (file_bytes) *file_bytes = std::move(out);
+    return "";
+  }
+
+  const std::vector<int64_t>& partition_lengths() const { return partition_lengths_; }
+  const std::vector<int64_t>& raw_lengths() const { return raw_lengths_; }
+  int64_t bytes_written() const { return bytes_written_; }
+  int64_t bytes_spilled() const { return bytes_spilled_; }
+  int64_t compute_pid_ns() const { return compute_pid_ns_; }
+  const std::vector<uint16_t>& last_pids() const { return pid_; }
+
+ private:
+  // HashSplitter::ComputeAndCountPartitionId (splitter.cc:1440-1470)
+  void ComputePid(int32_t n, const std::vector<InCol>& cols) {
+    pid_.assign(n, 0);
+    cnt_.assign(P_, 0);
+    for (int32_t r = 0; r < n; r++) {
+      int32_t h = 42;
+      for (int k : keys_) {
+        const InCol& c = cols[k];
+        if (c.validity && !GetBit(c.validity, r)) continue;  // null: seed passes through
+        switch (fields_[k].type) {
+          case T_BOOL: h = spark_hash_int(GetBit(c.values, r) ? 1 : 0, h); break;
+          case T_INT8: h = spark_hash_int(((const int8_t*)c.values)[r], h); break;
+          case T_INT16: h = spark_hash_int(((const int16_t*)c.values)[r], h); break;
+          case T_INT32: case T_DATE32: case T_FLOAT32:
+            h = spark_hash_int(((const int32_t*)c.values)[r], h);
+            break;
+          case T_INT64: case T_FLOAT64:
+            h = spark_hash_long(((const int64_t*)c.values)[r], h);
+            break;
+          case T_STRING: {
+            const int32_t* off = (const int32_t*)c.offsets;
+            h = SparkHashBytes(c.values + off[r], off[r + 1] - off[r], h);
+            break;
+          }
+        }
+      }
+      int32_t p = spark_pmod(h, P_);
+      pid_[r] = (uint16_t)p;
+      cnt_[p]++;
+    }
+  }
+
+  static int32_t SparkHashBytes(const uint8_t* p, int32_t len, int32_t seed) {
+    uint32_t h1 = (uint32_t)seed;
+    int32_t aligned = len - len % 4;
+    for (int32_t i = 0; i < aligned; i += 4) {
+      uint32_t k;
+      memcpy(&k, p + i, 4);
+      h1 = mix_h1(h1, mix_k1(k));
+    }
+    for (int32_t i = aligned; i < len; i++) h1 = mix_h1(h1, mix_k1((uint32_t)(int32_t)(int8_t)p[i]));
+    return (int32_t)fmix32(h1, (uint32_t)len);
+  }
+
+  // CalculateSplitBatchSize (splitter.cc:800-853)
+  uint32_t SplitBatchSize(int32_t n, const std::vector<InCol>& cols) {
+    int A = (int)array_idx_.size();
+    for (int a = fixed_cnt_; a < A; a++) {
+      uint64_t& e = empirical_[a - fixed_cnt_];
+      if (e == 0) {
+        const InCol& c = cols[array_idx_[a]];
+        if (c.offsets) {
+          const int32_t* off = (const int32_t*)c.offsets;
+          uint64_t len = (uint64_t)(uint32_t)(off[n] - off[0]);
+          e = len % n == 0 ? len / n : len / n + 1;
+        }
+      }
+    }
+    uint32_t size_per_row = 0;
+    for (auto e : empirical_) size_per_row += (uint32_t)e;
+    for (int a = 0; a < A; a++) {
+      int ci = array_idx_[a];
+      if (ci < fixed_cnt_) {
+        int t = fields_[ci].type;
+        size_per_row += t == T_BOOL ? 0 : ByteWidth(t);
+      }
+    }
+    int64_t rows = opt_.offheap_per_task > 0 && size_per_row > 0
+                       ? (opt_.offheap_per_task / size_per_row / P_) >> 2
+                       : opt_.buffer_size;
+    rows = std::min<int64_t>(rows, opt_.buffer_size);
+    return (uint32_t)rows;
+  }
+
+  // AllocatePartitionBuffers (splitter.cc:610-713); capacities are logical.
+  void Allocate(int p, uint32_t new_size) {
+    int A = (int)array_idx_.size();
+    for (int a = 0; a < A; a++) {
+      PartBufs& b = bufs_[a][p];
+      int t = fields_[array_idx_[a]].type;
+      b = PartBufs();
+      if (IsBinary(t)) {
+        b.offsets.assign(new_size + 1, 0);
+      } else if (t == T_BOOL) {
+        b.values.assign(BytesForBits(new_size), 0xff);
+      } else {
+        b.values.assign((size_t)new_size * ByteWidth(t), 0);
+      }
+      if (input_has_null_[a]) {
+        b.has_validity = true;
+        b.validity.assign(BytesForBits(new_size), 0xff);
+      }
+    }
+    cap_[p] = new_size;
+  }
+
+  // CacheRecordBatch (splitter.cc:462-608)
+  void CacheRecordBatch(int p, bool reset) {
+    uint32_t n = base_[p];
+    if (n == 0) return;
+    std::vector<std::pair<int64_t, int64_t>> nodes;
+    std::vector<BodyBuf> body;
+    std::vector<std::vector<uint8_t>> keep;
+    int64_t raw = 0;
+    int fixed_i = 0, bin_i = 0;
+    for (size_t f = 0; f < fields_.size(); f++) {
+      int t = fields_[f].type;
+      if (t == T_NULL) {
+        nodes.push_back({n, n});
+        continue;
+      }
+      int a = IsBinary(t) ? fixed_cnt_ + bin_i++ : fixed_i++;
+      PartBufs& b = bufs_[a][p];
+      int64_t nulls = 0;
+      if (b.has_validity) {
+        for (uint32_t i = 0; i < n; i++) nulls += !GetBit(b.validity.data(), i);
+        raw += BytesForBits(n);
+      }
+      nodes.push_back({n, nulls});
+      body.push_back(nulls > 0 ? BodyBuf{b.validity.data(), BytesForBits(n)} : BodyBuf{nullptr, 0});
+      if (IsBinary(t)) {
+        int64_t vlen = b.offsets[n];
+        body.push_back({(const uint8_t*)b.offsets.data(), (int64_t)(n + 1) * 4});
+        body.push_back({b.chars.data(), vlen});
+        raw += (int64_t)(n + 1) * 4 + vlen;
+      } else {
+        int64_t vlen = t == T_BOOL ? BytesForBits(n) : (int64_t)n * ByteWidth(t);
+        body.push_back({b.values.data(), vlen});
+        raw += vlen;
+      }
+    }
+    int64_t body_len;
+    auto msg = EncodeRecordBatch(n, nodes, body, &body_len);
+    raw_lengths_[p] += raw;
+    cached_size_[p] += body_len;
+    cached_[p].push_back(std::move(msg));
+    base_[p] = 0;
+    int A = (int)array_idx_.size();
+    for (int a = 0; a < A; a++) {
+      PartBufs& b = bufs_[a][p];
+      if (reset) {
+        b = PartBufs();
+      } else if (IsBinary(fields_[array_idx_[a]].type)) {
+        b.chars_used = 0;
+      }
+    }
+  }
+
+  // SpillPartition (splitter.cc:758-776): payloads to the partition's spill bytes, then
+  // every present validity buffer of the partition is refilled with 0xff.
+  void SpillPartition(int p) {
+    writer_[p] = true;
+    spill_opened_[p] = true;
+    for (auto& m : cached_[p]) spilled_[p].insert(spilled_[p].end(), m.begin(), m.end());
+    cached_[p].clear();
+    cached_size_[p] = 0;
+    for (auto& col : bufs_) {
+      if (col[p].has_validity) std::fill(col[p].validity.begin(), col[p].validity.end(), 0xff);
+    }
+  }
+
+  int SpillLargest(int64_t* size) {
+    int64_t max_size = 0;
+    int pick = -1;
+    for (int p = 0; p < P_; p++) {
+      if (cached_size_[p] > max_size) {
+        max_size = cached_size_[p];
+        pick = p;
+      }
+    }
+    *size = 0;
+    if (pick >= 0) {
+      SpillPartition(pick);
+      *size = max_size;
+    }
+    return pick;
+  }
+
+  // DoSplit (splitter.cc:855-938)
+  std::string DoSplit(int32_t n, const std::vector<InCol>& cols) {
+    int A = (int)array_idx_.size();
+    for (int a = 0; a < A; a++) {
+      int ci = array_idx_[a];
+      if (ci < fixed_cnt_ && !input_has_null_[a] && cols[ci].null_count != 0)
+        input_has_null_[a] = true;
+    }
+    for (int p = 0; p < P_; p++) {
+      uint32_t c = cnt_[p];
+      if (c == 0) continue;
+      if (cap_[p] == 0) {
+        Allocate(p, std::max(SplitBatchSize(n, cols), c));
+      } else if (base_[p] + c > cap_[p]) {
+        uint32_t ns = std::max(SplitBatchSize(n, cols), c);
+        if (opt_.prefer_spill) {
+          if (ns > cap_[p]) {
+            CacheRecordBatch(p, true);
+            SpillPartition(p);
+            Allocate(p, ns);
+          } else {
+            CacheRecordBatch(p, false);
+            SpillPartition(p);
+          }
+        } else {
+          CacheRecordBatch(p, true);
+          Allocate(p, ns);
+        }
+      }
+    }
+    // stable scatter: rows in input order land at base + running rank
+    std::vector<uint32_t> pos(base_.begin(), base_.end());
+    std::vector<uint32_t> run(P_, 0);
+    for (int a = 0; a < A; a++) {
+      int ci = array_idx_[a];
+      int t = fields_[ci].type;
+      const InCol& c = cols[ci];
+      // lazy validity (SplitValidityBuffer, splitter.cc:1179-1207)
+      if (c.null_count > 0) {
+        for (int p = 0; p < P_; p++) {
+          if (cnt_[p] > 0 && !bufs_[a][p].has_validity) {
+            bufs_[a][p].has_validity = true;
+            uint32_t bits = std::max<uint32_t>(cnt_[p], (uint32_t)opt_.buffer_size);
+            bufs_[a][p].validity.assign(BytesForBits(std::max<uint32_t>(bits, cap_[p])), 0xff);
+          }
+        }
+      }
+      std::fill(run.begin(), run.end(), 0);
+      for (int32_t r = 0; r < n; r++) {
+        int p = pid_[r];
+        uint32_t d = pos[p] + run[p]++;
+        PartBufs& b = bufs_[a][p];
+        if (c.null_count > 0 && !GetBit(c.validity, r)) ClearBit(b.validity.data(), d);
+        if (IsBinary(t)) {
+          const int32_t* off = (const int32_t*)c.offsets;
+          int32_t len = off[r + 1] - off[r];
+          if ((int64_t)b.chars.size() < b.chars_used + len)
+            b.chars.resize(std::max<int64_t>(b.chars_used + len, b.chars.size() * 3 / 2 + 64));
+          memcpy(b.chars.data() + b.chars_used, c.values + off[r], len);
+          b.chars_used += len;
+          b.offsets[d + 1] = (int32_t)b.chars_used;
+        } else if (t == T_BOOL) {
+          if (!GetBit(c.values, r)) ClearBit(b.values.data(), d);
+          else b.values[d >> 3] |= (uint8_t)(1u << (d & 7));
+        } else {
+          int w = ByteWidth(t);
+          memcpy(b.values.data() + (size_t)d * w, c.values + (size_t)r * w, w);
+        }
+      }
+      if (t == T_BOOL) {
+        // SplitBoolType writes the last touched byte as 0xff & bits (splitter.cc:1162-1173):
+        // bits above a partition's last row in that byte are 1.
+        for (int p = 0; p < P_; p++) {
+          if (cnt_[p] == 0) continue;
+          uint32_t end = pos[p] + cnt_[p];
+          for (uint32_t d = end; d & 7; d++) bufs_[a][p].values[d >> 3] |= (uint8_t)(1u << (d & 7));
+        }
+      }
+    }
+    for (int p = 0; p < P_; p++) base_[p] += cnt_[p];
+    return "";
+  }
+
+  std::vector<Field> fields_;
+  int P_;
+  std::vector<int> keys_;
+  Options opt_;
+  std::vector<int> array_idx_;
+  int fixed_cnt_ = 0;
+  std::vector<std::vector<PartBufs>> bufs_;
+  std::vector<bool> input_has_null_;
+  std::vector<uint64_t> empirical_;
+  std::vector<uint32_t> cap_, base_;
+  std::vector<std::vector<std::vector<uint8_t>>> cached_;
+  std::vector<int64_t> cached_size_;
+  std::vector<std::vector<uint8_t>> spilled_;
+  std::vector<bool> writer_, spill_opened_;
+  std::vector<int64_t> partition_lengths_, raw_lengths_;
+  std::vector<uint16_t> pid_;
+  std::vector<uint32_t> cnt_;
+  int64_t bytes_written_ = 0, bytes_spilled_ = 0, compute_pid_ns_ = 0;
+};
+
+struct Handle {
+  std::unique_ptr<OracleSplitter> s;
+  std::string err;
+  std::vector<uint8_t> file;
+};
+
+}  // namespace
+
+extern "C" {
+
+/* fields: types[nf] (GZ_TYPE_* codes); keys: column indices; opts: see Options. */
+void* gzo_make(const int32_t* types, int32_t nf, int32_t num_partitions, const int32_t* keys,
+               int32_t n_keys, int64_t offheap_per_task, int32_t buffer_size,
+               int32_t prefer_spill, char* err, int errlen) {
+  std::vector<Field> fields;
+  for (int i = 0; i < nf; i++) fields.push_back({types[i], "f" + std::to_string(i)});
+  Options o;
+  o.offheap_per_task = offheap_per_task;
+  if (buffer_size > 0) o.buffer_size = buffer_size;
+  o.prefer_spill = prefer_spill != 0;
+  auto h = new Handle;
+  h->s.reset(new OracleSplitter(fields, num_partitions, std::vector<int>(keys, keys + n_keys), o));
+  std::string e = h->s->Init();
+  if (!e.empty()) {
+    if (err) snprintf(err, errlen, "%s", e.c_str());
+    delete h;
+    return nullptr;
+  }
+  return h;
+}
+
+int gzo_split(void* hp, int32_t num_rows, const int64_t* addrs, const int64_t* sizes,
+              int32_t n, char* err, int errlen) {
+  auto* h = (Handle*)hp;
+  std::string e = h->s->Split(num_rows, addrs, sizes, n);
+  if (!e.empty()) {
+    if (err) snprintf(err, errlen, "%s", e.c_str());
+    return 1;
+  }
+  return 0;
+}
+
+/* partition ids of the last Split call (uint16 per row) */
+void gzo_last_pids(void* hp, uint16_t* out) {
+  auto* h = (Handle*)hp;
+  auto& v = h->s->last_pids();
+  memcpy(out, v.data(), v.size() * 2);
+}
+
+int64_t gzo_spill(void* hp, int64_t size) { return ((Handle*)hp)->s->SpillFixedSize(size); }
+
+/* metrics: [bytes_written, bytes_spilled, compute_pid_ns]; returns data size or -1 */
+int64_t gzo_stop(void* hp, const char* data_file, int64_t* lengths, int64_t* raw_lengths,
+                 int64_t* metrics, char* err, int errlen) {
+  auto* h = (Handle*)hp;
+  std::string e = h->s->Stop(data_file, &h->file);
+  if (!e.empty()) {
+    if (err) snprintf(err, errlen, "%s", e.c_str());
+    return -1;
+  }
+  auto& pl = h->s->partition_lengths();
+  auto& rl = h->s->raw_lengths();
+  for (size_t i = 0; i < pl.size(); i++) {
+    lengths[i] = pl[i];
+    raw_lengths[i] = rl[i];
+  }
+  metrics[0] = h->s->bytes_written();
+  metrics[1] = h->s->bytes_spilled();
+  metrics[2] = h->s->compute_pid_ns();
+  return (int64_t)h->file.size();
+}
+
+/* copies the data-file bytes produced by the last gzo_stop */
+void gzo_file_bytes(void* hp, uint8_t* out) {
+  auto* h = (Handle*)hp;
+  memcpy(out, h->file.data(), h->file.size());
+}
+
+void gzo_close(void* hp) { delete (Handle*)hp; }
+
+/* hash pins */
+int32_t gzo_hash_int(int32_t v, int32_t seed) { return spark_hash_int(v, seed); }
+int32_t gzo_hash_long(int64_t v, int32_t seed) { return spark_hash_long(v, seed); }
+uint32_t gzo_murmur3_bytes(const uint8_t* p, int32_t len, uint32_t seed) {
+  return murmur3_x86_32(p, len, seed);
+}
+int32_t gzo_pmod(int32_t h, int32_t p) { return spark_pmod(h, p); }
+
+}  // extern "C"

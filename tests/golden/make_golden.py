@@ -1,0 +1,238 @@
+"""Generate the golden fixtures in this directory from the reference Splitter itself.
+
+Run in a checkout where the reference sources and pyarrow are present:
+
+    python tests/golden/make_golden.py [/path/to/gazelle_plugin]
+
+It compiles the reference Splitter (oracle/ref/Makefile -> oracle/_ref/) and runs it on
+seeded inputs from gazelle_plugin_gb300.workloads, recording for every case the SHA-256 of
+the input buffers, of the whole shuffle data file and of every partition's bytes, plus
+partition_lengths, raw_partition_lengths and bytes spilled.  The reference's own unit-test
+batches (native-sql-engine/cpp/src/tests/shuffle_split_test.cc:186-208) are materialised
+into ref_fixture.npz together with the expected data-file bytes.
+
+The reference hashes through gandiva, which is absent; oracle/ref/stub supplies the same
+Spark Murmur3 chain (oracle/spark_hash.h), so what these fixtures pin is everything after
+the hash: pmod, histogram, stable scatter, buffer/emit policy, validity, IPC and file bytes.
+Configurations on which the reference has undefined behaviour are excluded: with
+prefer_spill, a reallocation (new size > capacity) reads partition_buffers_ after
+CacheRecordBatch cleared it (splitter.cc:907-909, 766-773), which happens whenever a
+partition receives more rows in one batch than its buffer holds or offheap_per_task > 0.
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from gazelle_plugin_gb300 import workloads as W  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def sha(b) -> str:
+    return hashlib.sha256(b).hexdigest()
+
+
+def input_digest(batches) -> str:
+    h = hashlib.sha256()
+    for b in batches:
+        h.update(np.int64(b.num_rows).tobytes())
+        for buf in b.buffers:
+            h.update(np.int64(buf.nbytes).tobytes())
+            h.update(buf.tobytes())
+    return h.hexdigest()
+
+
+def record(name, schema, batches, P, keys, opts, gen):
+    out = O.run_ref(schema, batches, P, keys, **opts)
+    return {
+        "name": name,
+        "gen": gen,
+        "schema": [[f.name, f.type, f.nullable] for f in schema],
+        "num_partitions": P,
+        "keys": [int(k) for k in keys],
+        "options": opts,
+        "input_sha256": input_digest(batches),
+        "data_sha256": sha(out.data),
+        "partition_sha256": ([sha(out.partition_bytes(p)) for p in range(P)] if P <= 256
+                             else None),
+        "partition_lengths": out.partition_lengths.tolist(),
+        "raw_partition_lengths": out.raw_partition_lengths.tolist(),
+        "bytes_spilled": out.bytes_spilled,
+        "bytes_written": out.bytes_written,
+    }
+
+
+def cases():
+    """(name, schema, batches, P, keys, options, generator description)"""
+    yield ("c1", W.C1_SCHEMA, W.c1_batches(0, 10, 4096), 8, W.C1_KEYS, {},
+           {"workload": "c1", "seed": 0, "num_batches": 10, "rows": 4096})
+    yield ("c1_buf512_nospill", W.C1_SCHEMA, W.c1_batches(0, 10, 512), 8, W.C1_KEYS,
+           {"buffer_size": 512, "prefer_spill": False},
+           {"workload": "c1", "seed": 0, "num_batches": 10, "rows": 512})
+    yield ("c2_16x4096", W.C2_SCHEMA, W.c2_batches(1, 16, 4096), 200, W.C2_KEYS, {},
+           {"workload": "c2", "seed": 1, "num_batches": 16, "rows": 4096})
+    yield ("c3_p16_nulls", W.C3_SCHEMA, W.c3_batches(2, 6, 4096, 0.2, 0.05), 16, W.C3_KEYS, {},
+           {"workload": "c3", "seed": 2, "num_batches": 6, "rows": 4096, "null_frac": 0.2,
+            "key_nulls": 0.05})
+    yield ("c3_p2000", W.C3_SCHEMA, W.c3_batches(2, 3, 4096, 0.0, 0.0), 2000, W.C3_KEYS,
+           {"buffer_size": 8},
+           {"workload": "c3", "seed": 2, "num_batches": 3, "rows": 4096, "null_frac": 0.0,
+            "key_nulls": 0.0})
+    for seed in range(24):
+        rng = np.random.default_rng(1000 + seed)
+        schema = W.random_schema(rng, int(rng.integers(1, 9)))
+        keys = [i for i, f in enumerate(schema) if f.type in W.KEY_TYPES]
+        keys = [int(k) for k in rng.choice(keys, size=int(rng.integers(1, len(keys) + 1)),
+                                           replace=False)]
+        P = int(rng.choice([1, 2, 3, 7, 16, 64, 200]))
+        bsz = int(rng.choice([16, 64, 100, 4096]))
+        nb = int(rng.integers(1, 10))
+        ps = bool(rng.random() < 0.6)
+        opts = {"buffer_size": bsz, "prefer_spill": ps,
+                "offheap_per_task": 0 if ps else int(rng.choice([0, 1 << 16, 1 << 20]))}
+        nullf = float(rng.choice([0.0, 0.01, 0.3, 0.9]))
+        batches = [W.random_batch(rng, schema, int(rng.integers(1, bsz + 1)), nullf)
+                   for _ in range(nb)]
+        yield (f"random_{seed}", schema, batches, P, keys, opts,
+               {"workload": "random", "seed": 1000 + seed})
+
+
+def random_case(seed):
+    """Re-create the inputs of a `random_<n>` case (same draw order as cases())."""
+    rng = np.random.default_rng(seed)
+    schema = W.random_schema(rng, int(rng.integers(1, 9)))
+    keys = [i for i, f in enumerate(schema) if f.type in W.KEY_TYPES]
+    keys = [int(k) for k in rng.choice(keys, size=int(rng.integers(1, len(keys) + 1)),
+                                       replace=False)]
+    P = int(rng.choice([1, 2, 3, 7, 16, 64, 200]))
+    bsz = int(rng.choice([16, 64, 100, 4096]))
+    nb = int(rng.integers(1, 10))
+    ps = bool(rng.random() < 0.6)
+    opts = {"buffer_size": bsz, "prefer_spill": ps,
+            "offheap_per_task": 0 if ps else int(rng.choice([0, 1 << 16, 1 << 20]))}
+    nullf = float(rng.choice([0.0, 0.01, 0.3, 0.9]))
+    batches = [W.random_batch(rng, schema, int(rng.integers(1, bsz + 1)), nullf)
+               for _ in range(nb)]
+    return schema, batches, P, keys, opts
+
+
+def regenerate(case):
+    """Inputs of a recorded case, rebuilt from its generator description."""
+    g = case["gen"]
+    if g["workload"] == "c1":
+        return W.c1_batches(g["seed"], g["num_batches"], g["rows"])
+    if g["workload"] == "c2":
+        return W.c2_batches(g["seed"], g["num_batches"], g["rows"])
+    if g["workload"] == "c3":
+        return W.c3_batches(g["seed"], g["num_batches"], g["rows"], g["null_frac"],
+                            g["key_nulls"])
+    if g["workload"] == "random":
+        return random_case(g["seed"])[1]
+    raise KeyError(g["workload"])
+
+
+# ---------------------------------------------------------------------------------------
+# the reference unit-test batches (shuffle_split_test.cc:99-127, 186-208)
+REF_FIXTURE_SCHEMA = [
+    W.Field("f_na", "null"), W.Field("f_int8_a", "int8"), W.Field("f_int8_b", "int8"),
+    W.Field("f_int32", "int32"), W.Field("f_uint64", "uint64"), W.Field("f_double", "float64"),
+    W.Field("f_bool", "bool"), W.Field("f_string", "utf8"),
+    W.Field("f_nullable_string", "utf8"), W.Field("f_decimal128", "decimal128"),
+]
+
+
+def ref_fixture_batches():
+    import pyarrow as pa
+    from decimal import Decimal
+    d1 = [
+        [None] * 10,
+        [1, 2, 3, None, 4, None, 5, 6, None, 7],
+        [1, -1, None, None, -2, 2, None, None, 3, -3],
+        [1, 2, 3, 4, None, 5, 6, 7, 8, None],
+        [None] * 10,
+        [-0.1234567, None, 0.1234567, None, -0.142857, None, 0.142857, 0.285714, 0.428617,
+         None],
+        [None, True, False, None, True, True, False, True, None, None],
+        ["alice0", "bob1", "alice2", "bob3", "Alice4", "Bob5", "AlicE6", "boB7", "ALICE8",
+         "BOB9"],
+        ["alice", "bob", None, None, "Alice", "Bob", None, "alicE", None, "boB"],
+        ["-1.01", "2.01", "-3.01", None, "0.11", "3.14", "2.27", None, "-3.14", None],
+    ]
+    d2 = [
+        [None, None], [None, None], [1, -1], [100, None], [1, 1], [0.142857, -0.142857],
+        [True, False], ["bob", "alice" * 40], [None, None], [None, None],
+    ]
+    pschema = O.to_pyarrow_schema(REF_FIXTURE_SCHEMA)
+    pschema = pa.schema([f.with_type(pa.decimal128(10, 2)) if f.name == "f_decimal128" else f
+                         for f in pschema])
+    out = []
+    for data in (d1, d2):
+        cols = []
+        for f, vals in zip(pschema, data):
+            if f.name == "f_decimal128":
+                vals = [None if v is None else Decimal(v) for v in vals]
+            cols.append(pa.array(vals, f.type))
+        out.append(pa.record_batch(cols, schema=pschema))
+    return out
+
+
+def to_batch(rb) -> W.Batch:
+    bufs = []
+    for col in rb.columns:
+        if col.type.id == 0 or str(col.type) == "null":
+            continue
+        arr_bufs = col.buffers()
+        v = arr_bufs[0]
+        bufs.append(np.frombuffer(v, np.uint8).copy() if (v is not None and col.null_count)
+                    else np.zeros(0, np.uint8))
+        for b in arr_bufs[1:]:
+            bufs.append(np.frombuffer(b, np.uint8).copy() if b is not None
+                        else np.zeros(0, np.uint8))
+    return W.Batch(rb.num_rows, bufs)
+
+
+def main():
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if not O.build_ref(ref_root):
+        raise SystemExit("reference tree not found")
+    recs = []
+    for name, schema, batches, P, keys, opts, gen in cases():
+        recs.append(record(name, schema, batches, P, keys, opts, gen))
+        print(name, recs[-1]["data_sha256"][:16])
+    with open(os.path.join(HERE, "splits.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py", "cases": recs}, f, indent=1)
+
+    # the reference's own unit-test batches, sequence [b1, b2, b1] as in TestHashSplitter
+    b1, b2 = [to_batch(rb) for rb in ref_fixture_batches()]
+    seq = [b1, b2, b1]
+    arrays = {}
+    for i, b in enumerate((b1, b2)):
+        arrays[f"b{i}_rows"] = np.array([b.num_rows])
+        for j, buf in enumerate(b.buffers):
+            arrays[f"b{i}_buf{j}"] = buf
+    meta = []
+    for P, bsz, keys in [(2, 4, [1, 2, 3]), (3, 4096, [3, 5]), (5, 2, [6, 1])]:
+        out = O.run_ref(REF_FIXTURE_SCHEMA, seq, P, keys, buffer_size=bsz)
+        tag = f"p{P}_b{bsz}"
+        arrays[f"{tag}_data"] = np.frombuffer(out.data, np.uint8)
+        arrays[f"{tag}_lengths"] = out.partition_lengths
+        arrays[f"{tag}_raw"] = out.raw_partition_lengths
+        meta.append({"tag": tag, "num_partitions": P, "buffer_size": bsz, "keys": keys})
+    np.savez_compressed(os.path.join(HERE, "ref_fixture.npz"), **arrays)
+    with open(os.path.join(HERE, "ref_fixture.json"), "w") as f:
+        json.dump({"schema": [[x.name, x.type, x.nullable] for x in REF_FIXTURE_SCHEMA],
+                   "sequence": [0, 1, 0], "runs": meta}, f, indent=1)
+    print("ref fixture", [m["tag"] for m in meta])
+
+
+if __name__ == "__main__":
+    main()
