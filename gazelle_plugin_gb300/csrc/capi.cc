@@ -1,0 +1,266 @@
+// C ABI of the GB300 hash split (include/gz_split.h).
+//
+// Handles live in a mutex-guarded table with ids starting at 4, like the JNI layer's
+// ConcurrentMap (native-sql-engine/cpp/src/jni/concurrent_map.h:35-80).  A call on one handle
+// is not synchronised against another call on the same handle: one splitter per task thread,
+// as in the reference.
+#include <stdio.h>
+#include <string.h>
+
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+
+#include "../../include/gz_split.h"
+#include "schema_ipc.h"
+#include "splitter.h"
+
+namespace {
+
+struct Entry {
+  std::unique_ptr<gz::Splitter> splitter;
+  std::string last_error;
+};
+
+std::mutex g_mu;
+std::map<int64_t, std::shared_ptr<Entry>> g_table;
+int64_t g_next_id = 4;
+thread_local std::string t_make_error;
+
+std::shared_ptr<Entry> Lookup(int64_t id) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_table.find(id);
+  return it == g_table.end() ? nullptr : it->second;
+}
+
+GzStatus Report(Entry* e, const gz::Status& st) {
+  if (!st.ok() && e) e->last_error = st.msg;
+  return st.code;
+}
+
+GzStatus MakeCommon(const char* short_name, int32_t num_partitions, std::vector<gz::Field> fields,
+                    const int32_t* key_cols, int32_t n_keys, const GzSplitOptions* opts,
+                    int64_t* out_handle) {
+  if (out_handle == nullptr || short_name == nullptr) {
+    t_make_error = "null argument";
+    return GZ_INVALID;
+  }
+  GzSplitOptions o;
+  if (opts) o = *opts;
+  else gz_split_default_options(&o);
+  std::vector<int32_t> keys(key_cols, key_cols + (n_keys > 0 ? n_keys : 0));
+  std::unique_ptr<gz::Splitter> s;
+  gz::Status st = gz::Splitter::Make(short_name, std::move(fields), num_partitions, keys, o, &s);
+  if (!st.ok()) {
+    t_make_error = "Failed create native shuffle splitter: " + st.msg;
+    return st.code;
+  }
+  auto e = std::make_shared<Entry>();
+  e->splitter = std::move(s);
+  std::lock_guard<std::mutex> lk(g_mu);
+  *out_handle = g_next_id++;
+  g_table[*out_handle] = e;
+  return GZ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void gz_split_default_options(GzSplitOptions* o) {
+  if (!o) return;
+  memset(o, 0, sizeof(*o));
+  o->offheap_per_task = 0;
+  o->buffer_size = 4096;
+  o->num_sub_dirs = 64;
+  o->batch_compress_threshold = 256;
+  o->compression = 0;
+  o->prefer_spill = 1;
+  o->write_schema = 1;
+  o->buffered_write = 0;
+  o->input_kind = GZ_INPUT_HOST;
+  o->device = 0;
+  o->keep_output_on_device = 1;
+  o->flush_bytes = 512ll << 20;
+  o->device_budget = 64ll << 30;
+  o->data_file = nullptr;
+  o->local_dirs = nullptr;
+}
+
+GzStatus gz_split_make(const char* short_name, int32_t num_partitions, const uint8_t* schema_ipc,
+                       int64_t schema_len, const int32_t* key_cols, int32_t n_keys,
+                       const GzSplitOptions* opts, int64_t* out_handle) {
+  std::vector<gz::Field> fields;
+  std::string err;
+  if (!gz::ParseSchemaIpc(schema_ipc, schema_len, &fields, &err)) {
+    t_make_error = "Make splitter schema: " + err;
+    return err.find("not implemented") != std::string::npos ? GZ_NOT_IMPLEMENTED : GZ_INVALID;
+  }
+  return MakeCommon(short_name, num_partitions, std::move(fields), key_cols, n_keys, opts, out_handle);
+}
+
+GzStatus gz_split_make_fields(const char* short_name, int32_t num_partitions,
+                              const GzField* fields, int32_t n_fields, const int32_t* key_cols,
+                              int32_t n_keys, const GzSplitOptions* opts, int64_t* out_handle) {
+  if (fields == nullptr && n_fields > 0) {
+    t_make_error = "Make splitter schema can't be null";
+    return GZ_INVALID;
+  }
+  std::vector<gz::Field> fs;
+  for (int i = 0; i < n_fields; i++) {
+    gz::Field f;
+    f.type = fields[i].type;
+    f.nullable = fields[i].nullable != 0;
+    f.precision = fields[i].precision;
+    f.scale = fields[i].scale;
+    f.unit = fields[i].unit;
+    f.name = fields[i].name ? fields[i].name : "";
+    fs.push_back(f);
+  }
+  return MakeCommon(short_name, num_partitions, std::move(fs), key_cols, n_keys, opts, out_handle);
+}
+
+GzStatus gz_split_split(int64_t handle, int32_t num_rows, const int64_t* buf_addrs,
+                        const int64_t* buf_sizes, int32_t n_bufs, int32_t first_batch,
+                        int64_t* out_compressed_size) {
+  auto e = Lookup(handle);
+  if (!e) {
+    t_make_error = "Invalid splitter id " + std::to_string(handle);
+    return GZ_INVALID;
+  }
+  if (buf_addrs == nullptr || buf_sizes == nullptr) {
+    e->last_error = "Native split: buf_addrs can't be null";
+    return GZ_INVALID;
+  }
+  if (first_batch) {
+    int64_t cs = -1;
+    GzStatus s = Report(e.get(), e->splitter->CompressedSize(num_rows, buf_addrs, buf_sizes, n_bufs, &cs));
+    if (out_compressed_size) *out_compressed_size = cs;
+    return s;
+  }
+  if (out_compressed_size) *out_compressed_size = -1;
+  return Report(e.get(), e->splitter->Split(num_rows, buf_addrs, buf_sizes, n_bufs));
+}
+
+GzStatus gz_split_stop(int64_t handle, GzSplitResult* out) {
+  auto e = Lookup(handle);
+  if (!e) {
+    t_make_error = "Invalid splitter id " + std::to_string(handle);
+    return GZ_INVALID;
+  }
+  GzStatus s = Report(e.get(), e->splitter->Stop());
+  if (s != GZ_OK || out == nullptr) return s;
+  gz::Splitter& sp = *e->splitter;
+  out->total_compute_pid_time = sp.TotalComputePidTime();
+  out->total_write_time = sp.TotalWriteTime();
+  out->total_spill_time = sp.TotalSpillTime();
+  out->total_compress_time = sp.TotalCompressTime();
+  out->total_bytes_written = sp.TotalBytesWritten();
+  out->total_bytes_spilled = sp.TotalBytesSpilled();
+  const auto& pl = sp.PartitionLengths();
+  const auto& rl = sp.RawPartitionLengths();
+  if (out->partition_lengths) memcpy(out->partition_lengths, pl.data(), pl.size() * sizeof(int64_t));
+  if (out->raw_partition_lengths) memcpy(out->raw_partition_lengths, rl.data(), rl.size() * sizeof(int64_t));
+  return GZ_OK;
+}
+
+GzStatus gz_split_data(int64_t handle, uint8_t* dst, int64_t* out_size) {
+  auto e = Lookup(handle);
+  if (!e) return GZ_INVALID;
+  const auto& d = e->splitter->DataBytes();
+  if (out_size) *out_size = (int64_t)d.size();
+  if (dst && !d.empty()) memcpy(dst, d.data(), d.size());
+  return GZ_OK;
+}
+
+GzStatus gz_split_spill(int64_t handle, int64_t size, int64_t* actual) {
+  auto e = Lookup(handle);
+  if (!e) return GZ_INVALID;
+  int64_t a = 0;
+  GzStatus s = Report(e.get(), e->splitter->SpillFixedSize(size, &a));
+  if (actual) *actual = a;
+  return s;
+}
+
+GzStatus gz_split_set_compress(int64_t handle, int32_t codec) {
+  auto e = Lookup(handle);
+  if (!e) return GZ_INVALID;
+  return Report(e.get(), e->splitter->SetCompressType(codec));
+}
+
+GzStatus gz_split_close(int64_t handle) {
+  std::shared_ptr<Entry> e;
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_table.find(handle);
+    if (it == g_table.end()) return GZ_OK;  // closing twice is harmless, as in the JNI layer
+    e = it->second;
+    g_table.erase(it);
+  }
+  return GZ_OK;
+}
+
+GzStatus gz_split_last_pids(int64_t handle, uint16_t* out, int32_t num_rows) {
+  auto e = Lookup(handle);
+  if (!e) return GZ_INVALID;
+  return Report(e.get(), e->splitter->LastPids(out, num_rows));
+}
+
+GzStatus gz_last_error(int64_t handle, char* buf, size_t len) {
+  if (!buf || len == 0) return GZ_INVALID;
+  std::string msg;
+  if (handle == 0) {
+    msg = t_make_error;
+  } else {
+    auto e = Lookup(handle);
+    msg = e ? e->last_error : t_make_error;
+  }
+  snprintf(buf, len, "%s", msg.c_str());
+  return GZ_OK;
+}
+
+GzStatus gz_split_kernel_times(int64_t handle, double* out4) {
+  auto e = Lookup(handle);
+  if (!e || !out4) return GZ_INVALID;
+  return Report(e.get(), e->splitter->KernelTimes(out4));
+}
+
+GzStatus gz_debug_encode_record_batch(int64_t length, const int64_t* nodes, int32_t n_nodes,
+                                      const uint8_t* const* bufs, const int64_t* buf_lens,
+                                      int32_t n_bufs, uint8_t* out, int64_t out_cap,
+                                      int64_t* out_len) {
+  std::vector<gz::FieldNodeMeta> nm;
+  for (int i = 0; i < n_nodes; i++) nm.push_back(gz::FieldNodeMeta{nodes[2 * i], nodes[2 * i + 1]});
+  std::vector<gz::ChunkedBuffer> bb;
+  for (int i = 0; i < n_bufs; i++) {
+    gz::ChunkedBuffer c;
+    if (buf_lens[i] > 0) c.push_back(gz::Chunk{bufs[i], buf_lens[i]});
+    bb.push_back(c);
+  }
+  gz::MemorySink sink;
+  int64_t body = 0;
+  if (gz::WriteRecordBatchMessage(&sink, length, nm, bb, &body) < 0) return GZ_IO;
+  *out_len = (int64_t)sink.buffer().size();
+  if (*out_len > out_cap) return GZ_INVALID;
+  memcpy(out, sink.buffer().data(), sink.buffer().size());
+  return GZ_OK;
+}
+
+GzStatus gz_debug_parse_schema(const uint8_t* schema_ipc, int64_t len, int32_t* types,
+                               int32_t* nullable, int32_t cap, int32_t* n_fields) {
+  std::vector<gz::Field> fields;
+  std::string err;
+  if (!gz::ParseSchemaIpc(schema_ipc, len, &fields, &err)) {
+    t_make_error = err;
+    return GZ_INVALID;
+  }
+  *n_fields = (int32_t)fields.size();
+  for (int i = 0; i < (int)fields.size() && i < cap; i++) {
+    types[i] = fields[i].type;
+    nullable[i] = fields[i].nullable ? 1 : 0;
+  }
+  return GZ_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,126 @@
+// Shared host/device definitions of the GB300 hash-split engine.
+//
+// One "flush" is a device pass over a group of consecutive input batches:
+//   k_hash_count : Spark Murmur3 chain + pmod per row, per-tile partition histograms
+//                  (rows, and bytes of every utf8 column), per-batch null counts
+//   k_plan       : per-partition walk over the flush's batches that restates the reference
+//                  buffer policy (allocate / emit / reuse, validity presence) and turns the
+//                  histograms into destination offsets; then scans over partitions
+//   k_scatter    : per-tile stable counting sort by partition id in shared memory, then a
+//                  coalesced scatter of every column into partition-contiguous output
+// Output of a flush, per array column, is partition-major: all rows of partition 0 in input
+// order, then partition 1, ...  An emitted record batch (reference CacheRecordBatch) is a
+// contiguous row range of one partition, possibly continued from the previous flush.
+#pragma once
+#include <stdint.h>
+
+namespace gz {
+
+constexpr int kMaxKeys = 8;
+constexpr int kMaxCols = 64;    // array columns (fixed + bool + binary)
+constexpr int kMaxSchemaCols = 256;
+constexpr int kTileRows = 4096; // rows per k_hash_count / k_scatter CTA
+constexpr int kScatterThreads = 512;
+constexpr int kPlanThreads = 1024;
+constexpr int kMaxBatchesPerFlush = 4096;
+
+enum KeyKind : int32_t { KEY_I32 = 0, KEY_I64 = 1, KEY_I8 = 2, KEY_I16 = 3, KEY_BOOL = 4 };
+enum ColKind : int32_t { COL_FIXED = 0, COL_BOOL = 1, COL_BINARY = 2 };
+
+// Static description of the split, copied to the device once at make.
+struct SchemaDesc {
+  int32_t P;
+  int32_t n_cols;      // schema fields, including null-type fields
+  int32_t n_array;     // array columns: fixed (incl. bool) first, then binary (splitter.cc:246-269)
+  int32_t n_fixed;     // fixed_width_col_cnt_
+  int32_t n_str;       // binary columns
+  int32_t n_keys;
+  int32_t prefer_spill;
+  int32_t pad0;
+  uint64_t quirk_mask;  // array columns a with array_idx_[a] < fixed_width_col_cnt_ (splitter.cc:878-886)
+  int32_t key_col[kMaxKeys];
+  int32_t key_kind[kMaxKeys];
+  int32_t arr_col[kMaxCols];    // schema index of array column a
+  int32_t arr_kind[kMaxCols];   // ColKind
+  int32_t arr_width[kMaxCols];  // value bytes of a fixed column
+  int32_t arr_str[kMaxCols];    // binary ordinal k of a binary column, -1 otherwise
+};
+
+// Device addresses of one input column of one batch.  offsets only for binary columns;
+// validity == nullptr means an empty validity buffer (no nulls).
+struct ColPtr {
+  const uint8_t* validity;
+  const int32_t* offsets;
+  const uint8_t* values;
+  uint64_t values_bytes;  // readable bytes at `values` (binary columns: offsets are checked)
+};
+
+// bits of FlushDesc::err
+constexpr int32_t kErrEmitOverflow = 1;
+constexpr int32_t kErrBadOffsets = 2;
+
+struct BatchDesc {
+  uint32_t nrows;
+  uint32_t tile0;
+  uint32_t ntiles;
+  uint32_t split_size;  // CalculateSplitBatchSize for this batch (splitter.cc:800-853)
+};
+
+struct TileDesc {
+  uint32_t batch;
+  uint32_t row0;   // first row inside the batch
+  uint32_t nrows;
+  uint32_t frow0;  // first row inside the flush (index into pids)
+};
+
+// Emission record written by k_plan: [p, frow_end, rows, hv_lo, hv_hi, fb_end[n_str]]
+constexpr int kEmitFixedWords = 5;
+
+struct FlushDesc {
+  uint32_t n_batches;
+  uint32_t n_tiles;
+  uint32_t n_rows;
+  uint32_t hist_in_smem;  // 1: k_hash_count histograms in shared memory
+
+  const BatchDesc* batches;  // [n_batches]
+  const TileDesc* tiles;     // [n_tiles]
+  const ColPtr* cols;        // [n_batches][n_cols]
+
+  // scratch (reused across flushes)
+  uint16_t* pids;     // [n_rows]
+  uint32_t* cnt;      // [n_tiles][P] rows; rewritten by k_plan to the flush-local row offset
+  uint32_t* bcnt;     // [n_tiles][n_str][P] bytes; rewritten to the flush-local byte offset
+  uint32_t* vpos;     // [n_tiles][P] validity bit offset (pieces start on 64-bit boundaries)
+  uint32_t* sbyte;    // [n_tiles][n_str][P] byte offset inside the partition's segment
+  uint32_t* nullcnt;  // [n_batches][n_array]
+
+  // per-partition results of this flush
+  uint32_t* rows_f;   // [P]
+  uint32_t* vbits_f;  // [P]
+  uint32_t* bytes_f;  // [n_str][P]
+  uint32_t* pstart;   // [P]   exclusive scans over partitions
+  uint32_t* vstart;   // [P]
+  uint32_t* cstart;   // [n_str][P]
+
+  uint32_t* emit;        // [emit_cap][kEmitFixedWords + n_str]
+  uint32_t* emit_count;  // [1]
+  uint32_t emit_cap;
+  uint32_t pad1;
+  uint32_t* call_flags;  // [n_batches] 1 when some partition ran CalculateSplitBatchSize
+
+  // outputs of this flush, indexed by array column
+  uint8_t* out_values[kMaxCols];   // fixed: n_rows * width; binary: n_rows int32 end offsets
+  uint32_t* out_bits[kMaxCols];    // bool values, same bit layout as validity
+  uint32_t* out_valid[kMaxCols];   // validity words, 0xff-filled; nullptr: no nulls in flush
+  uint8_t* out_chars[kMaxCols];    // binary bytes
+
+  // persistent partition state (the reference's per-pid buffer bookkeeping)
+  uint32_t* st_cap;               // partition_buffer_size_
+  uint32_t* st_base;              // partition_buffer_idx_base_
+  unsigned long long* st_hv;      // validity buffer present, per array column
+  uint32_t* st_sb;                // [n_str][P] bytes in the open segment
+  unsigned long long* st_ihn;     // [1] input_has_null_ (sticky)
+  int32_t* err;                   // device error word
+};
+
+}  // namespace gz

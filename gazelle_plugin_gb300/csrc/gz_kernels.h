@@ -1,0 +1,15 @@
+// Launch wrappers of the hash-split kernels (kernels.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "gz_engine.cuh"
+
+namespace gz {
+
+cudaError_t launch_hash_count(const SchemaDesc& sd, const FlushDesc& fd, cudaStream_t st);
+cudaError_t launch_plan(const SchemaDesc& sd, const FlushDesc& fd, cudaStream_t st);
+cudaError_t launch_scatter(const SchemaDesc& sd, const FlushDesc& fd, cudaStream_t st);
+size_t scatter_smem_bytes();
+int max_str_columns();
+
+}  // namespace gz

@@ -1,0 +1,1156 @@
+// Host engine of the GB300 hash split (see splitter.h).
+#include "splitter.h"
+
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <numeric>
+
+#include "gz_kernels.h"
+
+namespace gz {
+
+namespace {
+
+inline int64_t BytesForBits(int64_t n) { return (n + 7) >> 3; }
+inline size_t AlignUp(size_t x, size_t a) { return (x + a - 1) / a * a; }
+inline int64_t NowNs() {
+  return std::chrono::duration_cast<std::chrono::nanoseconds>(
+             std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+int ByteWidth(int t) {
+  switch (t) {
+    case GZ_TYPE_INT8: case GZ_TYPE_UINT8: return 1;
+    case GZ_TYPE_INT16: case GZ_TYPE_UINT16: case GZ_TYPE_HALF_FLOAT: return 2;
+    case GZ_TYPE_INT32: case GZ_TYPE_UINT32: case GZ_TYPE_FLOAT32: case GZ_TYPE_DATE32:
+    case GZ_TYPE_TIME32: return 4;
+    case GZ_TYPE_INT64: case GZ_TYPE_UINT64: case GZ_TYPE_FLOAT64: case GZ_TYPE_DATE64:
+    case GZ_TYPE_TIME64: case GZ_TYPE_TIMESTAMP: return 8;
+    case GZ_TYPE_DECIMAL128: return 16;
+    default: return 0;
+  }
+}
+inline bool IsBinary(int t) { return t == GZ_TYPE_STRING || t == GZ_TYPE_BINARY; }
+
+// Copies `nbits` bits from src (starting at bit `sbit`) to dst (starting at bit `dbit`);
+// dst bits outside the range are left as they are.
+void CopyBits(const uint8_t* src, uint64_t sbit, uint8_t* dst, uint64_t dbit, uint64_t nbits) {
+  for (uint64_t i = 0; i < nbits; i++) {
+    const uint64_t s = sbit + i, d = dbit + i;
+    const uint8_t b = (src[s >> 3] >> (s & 7)) & 1;
+    if (b) dst[d >> 3] |= (uint8_t)(1u << (d & 7));
+    else dst[d >> 3] &= (uint8_t)~(1u << (d & 7));
+  }
+}
+
+int64_t CountZeros(const uint8_t* bits, int64_t n) {
+  int64_t ones = 0;
+  int64_t full = n >> 3;
+  for (int64_t i = 0; i < full; i++) ones += __builtin_popcount(bits[i]);
+  for (int64_t i = full * 8; i < n; i++) ones += (bits[i >> 3] >> (i & 7)) & 1;
+  return n - ones;
+}
+
+}  // namespace
+
+Status Splitter::Cuda(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return Status::OK();
+  cudaGetLastError();
+  return Status::Error(e == cudaErrorMemoryAllocation ? GZ_OOM : GZ_CUDA,
+                       std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+Status Splitter::Make(const std::string& short_name, std::vector<Field> fields, int32_t P,
+                      std::vector<int32_t> keys, const GzSplitOptions& opts,
+                      std::unique_ptr<Splitter>* out) {
+  std::unique_ptr<Splitter> s(new Splitter());
+  Status st = s->Init(short_name, std::move(fields), P, std::move(keys), opts);
+  if (!st.ok()) return st;
+  *out = std::move(s);
+  return Status::OK();
+}
+
+Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, int32_t P,
+                      std::vector<int32_t> keys, const GzSplitOptions& opts) {
+  if (short_name != "hash") {
+    if (short_name == "rr" || short_name == "range" || short_name == "single")
+      return Status::Error(GZ_NOT_IMPLEMENTED,
+                           "Partitioning " + short_name + " is not implemented by the GPU splitter");
+    return Status::Error(GZ_NOT_IMPLEMENTED, "Partitioning " + short_name + " not supported yet.");
+  }
+  if (P <= 0 || P > 64 * 1024) return Status::Error(GZ_INVALID, "num_partitions must be in [1, 65536]");
+  opts_ = opts;
+  if (opts_.buffer_size <= 0) opts_.buffer_size = 4096;
+  if (opts_.buffer_size > 32 * 1024) return Status::Error(GZ_INVALID, "buffer_size must be <= 32768");
+  if (opts_.compression != 0)
+    return Status::Error(GZ_NOT_IMPLEMENTED, "only uncompressed shuffle output is implemented");
+  if (opts_.flush_bytes <= 0) opts_.flush_bytes = 512ll << 20;
+  if (opts_.flush_bytes > (1ll << 30)) opts_.flush_bytes = 1ll << 30;
+  data_file_ = opts.data_file ? opts.data_file : "";
+  opts_.data_file = nullptr;
+  opts_.local_dirs = nullptr;
+  if ((int)fields.size() > kMaxSchemaCols) return Status::Error(GZ_NOT_IMPLEMENTED, "too many fields");
+  fields_ = std::move(fields);
+  P_ = P;
+  keys_ = std::move(keys);
+
+  // Splitter::Init column classification (splitter.cc:246-269)
+  std::vector<int32_t> bin;
+  field_array_.assign(fields_.size(), -1);
+  for (size_t i = 0; i < fields_.size(); i++) {
+    const int t = fields_[i].type;
+    if (IsBinary(t)) bin.push_back((int32_t)i);
+    else if (t == GZ_TYPE_NULL) continue;
+    else if (t == GZ_TYPE_BOOL || ByteWidth(t) > 0) array_idx_.push_back((int32_t)i);
+    else return Status::Error(GZ_NOT_IMPLEMENTED, "field type not implemented in ColumnarShuffle");
+  }
+  fixed_cnt_ = (int32_t)array_idx_.size();
+  array_idx_.insert(array_idx_.end(), bin.begin(), bin.end());
+  n_array_ = (int32_t)array_idx_.size();
+  n_str_ = (int32_t)bin.size();
+  if (n_array_ == 0) return Status::Error(GZ_NOT_IMPLEMENTED, "schema without data columns");
+  if (n_array_ > kMaxCols) return Status::Error(GZ_NOT_IMPLEMENTED, "more than 64 data columns");
+  if (n_str_ > max_str_columns()) return Status::Error(GZ_NOT_IMPLEMENTED, "more than 32 binary columns");
+  if ((int)keys_.size() > kMaxKeys) return Status::Error(GZ_NOT_IMPLEMENTED, "more than 8 hash keys");
+
+  memset(&sd_, 0, sizeof(sd_));
+  sd_.P = P_;
+  sd_.n_cols = (int32_t)fields_.size();
+  sd_.n_array = n_array_;
+  sd_.n_fixed = fixed_cnt_;
+  sd_.n_str = n_str_;
+  sd_.n_keys = (int32_t)keys_.size();
+  sd_.prefer_spill = opts_.prefer_spill ? 1 : 0;
+  for (int a = 0; a < n_array_; a++) {
+    const int ci = array_idx_[a];
+    field_array_[ci] = a;
+    const int t = fields_[ci].type;
+    sd_.arr_col[a] = ci;
+    sd_.arr_kind[a] = IsBinary(t) ? COL_BINARY : t == GZ_TYPE_BOOL ? COL_BOOL : COL_FIXED;
+    sd_.arr_width[a] = ByteWidth(t);
+    sd_.arr_str[a] = a >= fixed_cnt_ ? a - fixed_cnt_ : -1;
+    if (ci < fixed_cnt_) sd_.quirk_mask |= 1ull << a;
+  }
+  // hash chain (HashSplitter::CreateProjector, splitter.cc:1402-1438)
+  for (size_t k = 0; k < keys_.size(); k++) {
+    const int ci = keys_[k];
+    if (ci < 0 || ci >= (int)fields_.size()) return Status::Error(GZ_INVALID, "key column out of range");
+    int kind;
+    switch (fields_[ci].type) {
+      case GZ_TYPE_BOOL: kind = KEY_BOOL; break;
+      case GZ_TYPE_INT8: kind = KEY_I8; break;
+      case GZ_TYPE_INT16: kind = KEY_I16; break;
+      case GZ_TYPE_INT32: case GZ_TYPE_FLOAT32: case GZ_TYPE_DATE32: kind = KEY_I32; break;
+      case GZ_TYPE_INT64: case GZ_TYPE_FLOAT64: kind = KEY_I64; break;
+      default:
+        return Status::Error(GZ_NOT_IMPLEMENTED,
+                             "hash key type has no Spark-compatible hash in the GPU splitter");
+    }
+    sd_.key_col[k] = ci;
+    sd_.key_kind[k] = kind;
+  }
+  // JNI buffer layout (jni_common.h:308-382): [validity, (offsets), values] per field
+  field_buf0_.resize(fields_.size());
+  int nb = 0;
+  for (size_t i = 0; i < fields_.size(); i++) {
+    field_buf0_[i] = nb;
+    nb += IsBinary(fields_[i].type) ? 3 : 2;
+  }
+  n_bufs_expected_ = nb;
+  empirical_.assign(n_str_, 0);
+
+  device_ = opts_.device;
+  GzStatus dummy;
+  (void)dummy;
+  Status st = Cuda(cudaSetDevice(device_), "cudaSetDevice");
+  if (!st.ok()) return st;
+  st = Cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+  if (!st.ok()) return st;
+  {
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device_) == cudaSuccess) {
+      uint64_t thr = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+  }
+  // persistent partition state
+  const size_t state_bytes = AlignUp(sizeof(uint32_t) * P_, 256) * 2 +
+                             AlignUp(sizeof(unsigned long long) * P_, 256) +
+                             AlignUp(sizeof(uint32_t) * (size_t)std::max(n_str_, 1) * P_, 256) +
+                             256 * 3;
+  st = Cuda(cudaMalloc(&d_state_, state_bytes), "cudaMalloc(state)");
+  if (!st.ok()) return st;
+  st = Cuda(cudaMemsetAsync(d_state_, 0, state_bytes, stream_), "cudaMemset(state)");
+  if (!st.ok()) return st;
+  uint8_t* q = d_state_;
+  st_cap_ = reinterpret_cast<uint32_t*>(q); q += AlignUp(sizeof(uint32_t) * P_, 256);
+  st_base_ = reinterpret_cast<uint32_t*>(q); q += AlignUp(sizeof(uint32_t) * P_, 256);
+  st_hv_ = reinterpret_cast<unsigned long long*>(q); q += AlignUp(sizeof(unsigned long long) * P_, 256);
+  st_sb_ = reinterpret_cast<uint32_t*>(q); q += AlignUp(sizeof(uint32_t) * (size_t)std::max(n_str_, 1) * P_, 256);
+  st_ihn_ = reinterpret_cast<unsigned long long*>(q); q += 256;
+  d_err_ = reinterpret_cast<int32_t*>(q); q += 256;
+  d_call_ = reinterpret_cast<uint32_t*>(q);
+  for (int i = 0; i < 2; i++) {
+    st = Cuda(cudaEventCreateWithFlags(&stage_ev_[i], cudaEventDisableTiming), "cudaEventCreate");
+    if (!st.ok()) return st;
+    st = Cuda(cudaEventCreateWithFlags(&tab_ev_[i], cudaEventDisableTiming), "cudaEventCreate");
+    if (!st.ok()) return st;
+  }
+  dev_off_.resize(n_str_);
+  partition_lengths_.assign(P_, 0);
+  raw_partition_lengths_.assign(P_, 0);
+  segments_.assign(P_, {});
+  open_.assign(P_, Segment());
+  return Status::OK();
+}
+
+Splitter::~Splitter() {
+  if (stream_) cudaStreamSynchronize(stream_);
+  for (auto& f : flushes_) {
+    if (f.d_out) cudaFree(f.d_out);
+    for (auto& e : f.ev)
+      if (e) cudaEventDestroy(e);
+  }
+  for (auto& c : meta_chunks_) cudaFreeHost(c);
+  for (int i = 0; i < 2; i++) {
+    if (h_tables_[i]) cudaFreeHost(h_tables_[i]);
+    if (tab_ev_[i]) cudaEventDestroy(tab_ev_[i]);
+  }
+  for (int i = 0; i < 2; i++) {
+    if (h_stage_[i]) cudaFreeHost(h_stage_[i]);
+    if (d_stage_[i]) cudaFree(d_stage_[i]);
+    if (stage_ev_[i]) cudaEventDestroy(stage_ev_[i]);
+  }
+  if (d_scratch_) cudaFree(d_scratch_);
+  if (d_state_) cudaFree(d_state_);
+  if (stream_) cudaStreamDestroy(stream_);
+}
+
+// CalculateSplitBatchSize (splitter.cc:800-853).  `host_offsets` (may hold nullptr) are the
+// batch's offset buffers per binary column, readable on the host.
+uint32_t Splitter::SplitBatchSize(int32_t num_rows, const std::vector<const int32_t*>& host_offsets,
+                                  bool* complete) {
+  for (int k = 0; k < n_str_; k++) {
+    if (empirical_[k] == 0 && host_offsets[k] != nullptr && num_rows > 0) {
+      const uint64_t len = (uint64_t)(uint32_t)(host_offsets[k][num_rows] - host_offsets[k][0]);
+      empirical_[k] = len % num_rows == 0 ? len / num_rows : len / num_rows + 1;
+    }
+  }
+  *complete = true;
+  for (int k = 0; k < n_str_; k++)
+    if (empirical_[k] == 0) *complete = false;
+  uint32_t size_per_row = 0;
+  for (int k = 0; k < n_str_; k++) size_per_row += (uint32_t)empirical_[k];
+  for (int a = 0; a < n_array_; a++) {
+    const int ci = array_idx_[a];
+    if (ci < fixed_cnt_) {
+      const int t = fields_[ci].type;
+      size_per_row += t == GZ_TYPE_BOOL ? 0 : ByteWidth(t);
+    }
+  }
+  int64_t rows = opts_.offheap_per_task > 0 && size_per_row > 0
+                     ? (opts_.offheap_per_task / size_per_row / P_) >> 2
+                     : opts_.buffer_size;
+  rows = std::min<int64_t>(rows, opts_.buffer_size);
+  return (uint32_t)rows;
+}
+
+Status Splitter::EnsureStaging(size_t bytes) {
+  if (bytes <= stage_cap_) return Status::OK();
+  Status st = Cuda(cudaStreamSynchronize(stream_), "sync");
+  if (!st.ok()) return st;
+  size_t cap = AlignUp(std::max<size_t>(bytes, (size_t)opts_.flush_bytes + (8u << 20)), 1 << 20);
+  for (int i = 0; i < 2; i++) {
+    if (h_stage_[i]) cudaFreeHost(h_stage_[i]);
+    if (d_stage_[i]) cudaFree(d_stage_[i]);
+    h_stage_[i] = nullptr;
+    d_stage_[i] = nullptr;
+    st = Cuda(cudaHostAlloc(&h_stage_[i], cap, cudaHostAllocDefault), "cudaHostAlloc(stage)");
+    if (!st.ok()) return st;
+    st = Cuda(cudaMalloc(&d_stage_[i], cap), "cudaMalloc(stage)");
+    if (!st.ok()) return st;
+    stage_busy_[i] = false;
+  }
+  stage_cap_ = cap;
+  return Status::OK();
+}
+
+Status Splitter::Split(int32_t num_rows, const int64_t* addrs, const int64_t* sizes, int32_t n) {
+  if (stopped_) return Status::Error(GZ_INVALID, "split after stop");
+  Status st = Cuda(cudaSetDevice(device_), "cudaSetDevice");
+  if (!st.ok()) return st;
+  if (n < n_bufs_expected_) return Status::Error(GZ_INVALID, "insufficient number of in_buf_addrs");
+  if (num_rows < 0) return Status::Error(GZ_INVALID, "negative num_rows");
+  if (num_rows == 0) return Status::OK();  // an empty batch changes no splitter state
+  last_batch_rows_ = (uint32_t)num_rows;
+  const bool host_in = opts_.input_kind == GZ_INPUT_HOST;
+  const uint32_t nr = (uint32_t)num_rows;
+
+  // validate and size every buffer that is read
+  struct Need {
+    const uint8_t* src;
+    size_t bytes;
+  };
+  std::vector<Need> need(n_bufs_expected_, Need{nullptr, 0});
+  std::vector<const int32_t*> host_off(n_str_, nullptr);
+  PendingBatch pb;
+  pb.nrows = nr;
+  pb.validity_mask = 0;
+  pb.char_bytes.assign(n_str_, 0);
+  pb.cols.assign(fields_.size(), ColPtr{nullptr, nullptr, nullptr, 0});
+  size_t batch_bytes = 0;
+  for (size_t f = 0; f < fields_.size(); f++) {
+    const int a = field_array_[f];
+    if (a < 0) continue;  // null type: buffers ignored
+    const int t = fields_[f].type;
+    const int b0 = field_buf0_[f];
+    // validity
+    if (addrs[b0] != 0 && sizes[b0] > 0) {
+      const size_t vb = (size_t)BytesForBits(nr);
+      if ((size_t)sizes[b0] < vb) return Status::Error(GZ_INVALID, "validity buffer too small");
+      need[b0] = Need{reinterpret_cast<const uint8_t*>(addrs[b0]), vb};
+      pb.validity_mask |= 1ull << a;
+    }
+    const int vi = IsBinary(t) ? b0 + 2 : b0 + 1;
+    if (IsBinary(t)) {
+      const size_t ob = (size_t)(nr + 1) * 4;
+      if (addrs[b0 + 1] == 0 || (size_t)sizes[b0 + 1] < ob)
+        return Status::Error(GZ_INVALID, "offsets buffer too small");
+      need[b0 + 1] = Need{reinterpret_cast<const uint8_t*>(addrs[b0 + 1]), ob};
+      size_t cb = (size_t)std::max<int64_t>(sizes[vi], 0);
+      if (host_in) {
+        const int32_t* off = reinterpret_cast<const int32_t*>(addrs[b0 + 1]);
+        host_off[a - fixed_cnt_] = off;
+        if (off[nr] < off[0] || off[0] < 0 || (int64_t)off[nr] > sizes[vi])
+          return Status::Error(GZ_INVALID, "offsets exceed the value buffer");
+        cb = (size_t)off[nr];
+        pb.char_bytes[a - fixed_cnt_] = (uint64_t)(off[nr] - off[0]);
+      } else {
+        pb.char_bytes[a - fixed_cnt_] = (uint64_t)cb;
+      }
+      if (cb > 0) need[vi] = Need{reinterpret_cast<const uint8_t*>(addrs[vi]), cb};
+    } else {
+      const size_t vbytes = t == GZ_TYPE_BOOL ? (size_t)BytesForBits(nr) : (size_t)nr * ByteWidth(t);
+      if (addrs[vi] == 0 || (size_t)sizes[vi] < vbytes)
+        return Status::Error(GZ_INVALID, "value buffer too small");
+      need[vi] = Need{reinterpret_cast<const uint8_t*>(addrs[vi]), vbytes};
+    }
+  }
+  for (auto& nd : need) batch_bytes += AlignUp(nd.bytes, 64);
+
+  // CalculateSplitBatchSize.  Its row count depends on the empirical binary sizes only when
+  // offheap_per_task > 0; those sizes are learned from the first batch with rows (where every
+  // partition allocates, so the reference always computes them) and, while one is still 0,
+  // from each later batch in which some partition reaches the function (splitter.cc:804-835).
+  std::vector<uint64_t> empirical_before = empirical_;
+  bool probe_call = false;
+  if (opts_.offheap_per_task > 0 && n_str_ > 0) {
+    bool missing = false;
+    for (int k = 0; k < n_str_; k++) missing |= empirical_[k] == 0;
+    if (missing && !host_in) {
+      st = Cuda(cudaStreamSynchronize(stream_), "sync");
+      if (!st.ok()) return st;
+      for (int k = 0; k < n_str_; k++) {
+        const int f = array_idx_[fixed_cnt_ + k];
+        const int32_t* doff = reinterpret_cast<const int32_t*>(addrs[field_buf0_[f] + 1]);
+        dev_off_[k].assign(nr + 1, 0);
+        st = Cuda(cudaMemcpy(&dev_off_[k][0], doff, 4, cudaMemcpyDeviceToHost), "read offsets");
+        if (!st.ok()) return st;
+        st = Cuda(cudaMemcpy(&dev_off_[k][nr], doff + nr, 4, cudaMemcpyDeviceToHost), "read offsets");
+        if (!st.ok()) return st;
+        host_off[k] = dev_off_[k].data();
+      }
+    }
+    probe_call = missing && seen_rows_;
+  }
+  bool complete = true;
+  pb.split_size = SplitBatchSize(num_rows, host_off, &complete);
+  seen_rows_ = true;
+  const uint32_t ntiles = (nr + kTileRows - 1) / kTileRows;
+  pb.last_tile_rows = nr - (ntiles - 1) * kTileRows;
+
+  // make room in the current flush group
+  const size_t tables_extra = sizeof(BatchDesc) + sizeof(TileDesc) * ntiles +
+                              sizeof(ColPtr) * fields_.size() + 1024;
+  auto group_tables = [&](size_t nb_, size_t nt_) {
+    return AlignUp(sizeof(BatchDesc) * nb_, 256) + AlignUp(sizeof(TileDesc) * nt_, 256) +
+           AlignUp(sizeof(ColPtr) * nb_ * fields_.size(), 256);
+  };
+  size_t cur_tiles = 0;
+  for (auto& b : pending_) cur_tiles += (b.nrows + kTileRows - 1) / kTileRows;
+  if (!pending_.empty() &&
+      (pending_bytes_ + batch_bytes > (uint64_t)opts_.flush_bytes ||
+       pending_.size() + 1 > (size_t)kMaxBatchesPerFlush ||
+       (host_in && used_ + batch_bytes + group_tables(pending_.size() + 1, cur_tiles + ntiles) +
+                       tables_extra > stage_cap_))) {
+    st = Flush();
+    if (!st.ok()) return st;
+  }
+  if (host_in) {
+    st = EnsureStaging(batch_bytes + group_tables(1, ntiles) + tables_extra);
+    if (!st.ok()) return st;
+    if (pending_.empty() && stage_busy_[cur_]) {
+      st = Cuda(cudaEventSynchronize(stage_ev_[cur_]), "stage wait");
+      if (!st.ok()) return st;
+      stage_busy_[cur_] = false;
+    }
+    // copy the batch into pinned staging; device addresses point into the device twin
+    for (size_t f = 0; f < fields_.size(); f++) {
+      const int a = field_array_[f];
+      if (a < 0) continue;
+      const int t = fields_[f].type;
+      const int b0 = field_buf0_[f];
+      ColPtr cp{nullptr, nullptr, nullptr, 0};
+      const int nbuf = IsBinary(t) ? 3 : 2;
+      for (int j = 0; j < nbuf; j++) {
+        const Need& nd = need[b0 + j];
+        if (nd.bytes == 0) continue;
+        memcpy(h_stage_[cur_] + used_, nd.src, nd.bytes);
+        const uint8_t* dptr = d_stage_[cur_] + used_;
+        used_ += AlignUp(nd.bytes, 64);
+        if (j == 0) cp.validity = dptr;
+        else if (IsBinary(t) && j == 1) cp.offsets = reinterpret_cast<const int32_t*>(dptr);
+        else {
+          cp.values = dptr;
+          cp.values_bytes = nd.bytes;
+        }
+      }
+      if (IsBinary(t) && cp.values == nullptr) cp.values = d_stage_[cur_];  // all strings empty
+      pb.cols[f] = cp;
+    }
+  } else {
+    for (size_t f = 0; f < fields_.size(); f++) {
+      const int a = field_array_[f];
+      if (a < 0) continue;
+      const int t = fields_[f].type;
+      const int b0 = field_buf0_[f];
+      ColPtr cp{nullptr, nullptr, nullptr, 0};
+      if (need[b0].bytes) cp.validity = need[b0].src;
+      if (IsBinary(t)) {
+        cp.offsets = reinterpret_cast<const int32_t*>(addrs[b0 + 1]);
+        cp.values = reinterpret_cast<const uint8_t*>(addrs[b0 + 2]);
+        cp.values_bytes = (uint64_t)std::max<int64_t>(sizes[b0 + 2], 0);
+        if (reinterpret_cast<uintptr_t>(cp.offsets) % 4)
+          return Status::Error(GZ_INVALID, "device offsets buffer must be 4-byte aligned");
+      } else {
+        cp.values = need[b0 + 1].src;
+        const int w = t == GZ_TYPE_BOOL ? 1 : ByteWidth(t);
+        if (reinterpret_cast<uintptr_t>(cp.values) % (uintptr_t)w)
+          return Status::Error(GZ_INVALID, "device value buffer is not aligned to its width");
+      }
+      pb.cols[f] = cp;
+    }
+  }
+  if (probe_call && !pending_.empty()) {
+    // this batch has to be alone in its device pass so its call flag can be read back
+    st = Flush();
+    if (!st.ok()) return st;
+  }
+  pending_bytes_ += batch_bytes;
+  pending_.push_back(std::move(pb));
+  if (probe_call) {
+    st = Flush();
+    if (!st.ok()) return st;
+    uint32_t called = 0;
+    st = Cuda(cudaMemcpyAsync(&called, d_call_, 4, cudaMemcpyDeviceToHost, stream_), "read call flag");
+    if (!st.ok()) return st;
+    st = Cuda(cudaStreamSynchronize(stream_), "sync");
+    if (!st.ok()) return st;
+    if (!called) empirical_ = empirical_before;  // nobody recomputed the sizes in this batch
+  }
+  return Status::OK();
+}
+
+// Small pinned blocks for per-flush metadata, carved from 4 MiB chunks kept until destruction.
+Status Splitter::PinnedMeta(size_t bytes, uint32_t** out) {
+  bytes = AlignUp(bytes, 256);
+  if (meta_chunks_.empty() || meta_used_ + bytes > meta_chunk_cap_) {
+    const size_t cap = std::max<size_t>(bytes, 4u << 20);
+    void* c = nullptr;
+    Status st = Cuda(cudaHostAlloc(&c, cap, cudaHostAllocDefault), "cudaHostAlloc(meta)");
+    if (!st.ok()) return st;
+    meta_chunks_.push_back(c);
+    meta_chunk_cap_ = cap;
+    meta_used_ = 0;
+  }
+  *out = reinterpret_cast<uint32_t*>(static_cast<uint8_t*>(meta_chunks_.back()) + meta_used_);
+  meta_used_ += bytes;
+  return Status::OK();
+}
+
+Status Splitter::EnsureScratch(size_t bytes) {
+  if (bytes <= scratch_cap_) return Status::OK();
+  if (d_scratch_) {
+    Status st = Cuda(cudaStreamSynchronize(stream_), "sync");
+    if (!st.ok()) return st;
+    cudaFree(d_scratch_);
+    d_scratch_ = nullptr;
+  }
+  size_t cap = AlignUp(bytes + bytes / 4, 1 << 20);
+  Status st = Cuda(cudaMalloc(&d_scratch_, cap), "cudaMalloc(scratch)");
+  if (!st.ok()) return st;
+  scratch_cap_ = cap;
+  return Status::OK();
+}
+
+Status Splitter::Flush() {
+  if (pending_.empty()) return Status::OK();
+  const bool host_in = opts_.input_kind == GZ_INPUT_HOST;
+  const uint32_t NB = (uint32_t)pending_.size();
+  const size_t C = fields_.size();
+  const int P = P_;
+  const int nstr = n_str_;
+  const int A = n_array_;
+
+  // tables
+  std::vector<BatchDesc> batches(NB);
+  std::vector<TileDesc> tiles;
+  uint64_t R = 0;
+  uint64_t emit_bound_a = 0;
+  uint32_t smin = UINT32_MAX, capmax = (uint32_t)opts_.buffer_size;
+  for (uint32_t b = 0; b < NB; b++) {
+    const PendingBatch& pb = pending_[b];
+    const uint32_t nt = (pb.nrows + kTileRows - 1) / kTileRows;
+    batches[b] = BatchDesc{pb.nrows, (uint32_t)tiles.size(), nt, pb.split_size};
+    for (uint32_t t = 0; t < nt; t++) {
+      const uint32_t r0 = t * kTileRows;
+      tiles.push_back(TileDesc{b, r0, std::min<uint32_t>(kTileRows, pb.nrows - r0), (uint32_t)(R + r0)});
+    }
+    R += pb.nrows;
+    emit_bound_a += std::min<uint64_t>((uint64_t)P, pb.nrows);
+    smin = std::min(smin, pb.split_size);
+    capmax = std::max(capmax, pb.nrows);
+  }
+  if (R >= (1ull << 31)) return Status::Error(GZ_INVALID, "flush too large");
+  const uint32_t T = (uint32_t)tiles.size();
+  const uint64_t emit_bound_b =
+      2 * (R + (uint64_t)P * capmax) / std::max<uint32_t>(smin, 1) + 2 * (uint64_t)P + 16;
+  const uint32_t emit_cap = (uint32_t)std::min(emit_bound_a, emit_bound_b) + 1;
+  const uint64_t pieces_max = (uint64_t)P + emit_cap;
+  const uint64_t vbits_max = R + 64 * pieces_max;
+  const size_t vwords_bytes = AlignUp((size_t)((vbits_max + 31) / 32) * 4, 256);
+
+  // output layout
+  FlushRec fr;
+  fr.n_rows = (uint32_t)R;
+  fr.n_batches = NB;
+  fr.emit_cap = emit_cap;
+  fr.off_values.assign(A, SIZE_MAX);
+  fr.off_bits.assign(A, SIZE_MAX);
+  fr.off_valid.assign(A, SIZE_MAX);
+  fr.off_chars.assign(A, SIZE_MAX);
+  uint64_t any_valid = 0;
+  for (auto& pb : pending_) any_valid |= pb.validity_mask;
+  size_t o = 0;
+  for (int a = 0; a < A; a++) {
+    const int kind = sd_.arr_kind[a];
+    if (kind == COL_FIXED) {
+      fr.off_values[a] = o;
+      o += AlignUp((size_t)R * sd_.arr_width[a], 256);
+    } else if (kind == COL_BINARY) {
+      fr.off_values[a] = o;
+      o += AlignUp((size_t)R * 4, 256);
+      uint64_t cb = 0;
+      for (auto& pb : pending_) cb += pb.char_bytes[sd_.arr_str[a]];
+      fr.off_chars[a] = o;
+      o += AlignUp((size_t)cb + 16, 256);
+    }
+  }
+  const size_t bits_begin = o;
+  for (int a = 0; a < A; a++) {
+    if (sd_.arr_kind[a] == COL_BOOL) {
+      fr.off_bits[a] = o;
+      o += vwords_bytes;
+    }
+    if (any_valid & (1ull << a)) {
+      fr.off_valid[a] = o;
+      o += vwords_bytes;
+    }
+  }
+  const size_t bits_end = o;
+  fr.out_bytes = std::max<size_t>(o, 256);
+  Status st = Cuda(cudaMallocAsync(reinterpret_cast<void**>(&fr.d_out), fr.out_bytes, stream_),
+                   "cudaMallocAsync(flush output)");
+  if (!st.ok()) return st;
+  if (bits_end > bits_begin) {
+    st = Cuda(cudaMemsetAsync(fr.d_out + bits_begin, 0xff, bits_end - bits_begin, stream_), "memset bits");
+    if (!st.ok()) return st;
+  }
+
+  // scratch layout
+  const size_t TP = (size_t)T * P;
+  size_t so = 0;
+  auto take = [&](size_t bytes) {
+    size_t at = so;
+    so += AlignUp(bytes, 256);
+    return at;
+  };
+  const size_t s_pids = take(R * 2);
+  const size_t s_cnt = take(TP * 4);
+  const size_t s_vpos = take(TP * 4);
+  const size_t s_bcnt = take(TP * nstr * 4 + 4);
+  const size_t s_sbyte = take(TP * nstr * 4 + 4);
+  const size_t s_null = take((size_t)NB * A * 4);
+  const size_t s_call = take((size_t)NB * 4);
+  const size_t s_vbits = take((size_t)P * 4);
+  const size_t meta_words = (3 + 2 * (size_t)nstr) * P + 1 + (size_t)emit_cap * (kEmitFixedWords + nstr);
+  const size_t s_meta = take(meta_words * 4);  // rows_f, pstart, vstart, bytes_f, cstart, count, emits
+  const size_t tb_batches = AlignUp(sizeof(BatchDesc) * NB, 256);
+  const size_t tb_tiles = AlignUp(sizeof(TileDesc) * T, 256);
+  const size_t tb_cols = AlignUp(sizeof(ColPtr) * NB * C, 256);
+  const size_t tb_total = tb_batches + tb_tiles + tb_cols;
+  const size_t s_tab = host_in ? 0 : take(tb_total);
+  st = EnsureScratch(so);
+  if (!st.ok()) return st;
+  uint8_t* S = d_scratch_;
+
+  FlushDesc fd;
+  memset(&fd, 0, sizeof(fd));
+  fd.n_batches = NB;
+  fd.n_tiles = T;
+  fd.n_rows = (uint32_t)R;
+  fd.hist_in_smem = (size_t)P * (1 + nstr) * 4 <= 96 * 1024 ? 1 : 0;
+  fd.pids = reinterpret_cast<uint16_t*>(S + s_pids);
+  fd.cnt = reinterpret_cast<uint32_t*>(S + s_cnt);
+  fd.vpos = reinterpret_cast<uint32_t*>(S + s_vpos);
+  fd.bcnt = reinterpret_cast<uint32_t*>(S + s_bcnt);
+  fd.sbyte = reinterpret_cast<uint32_t*>(S + s_sbyte);
+  fd.nullcnt = reinterpret_cast<uint32_t*>(S + s_null);
+  fd.call_flags = reinterpret_cast<uint32_t*>(S + s_call);
+  fd.vbits_f = reinterpret_cast<uint32_t*>(S + s_vbits);
+  uint32_t* meta = reinterpret_cast<uint32_t*>(S + s_meta);
+  fd.rows_f = meta;
+  fd.pstart = meta + P;
+  fd.vstart = meta + 2 * (size_t)P;
+  fd.bytes_f = meta + 3 * (size_t)P;
+  fd.cstart = meta + (3 + (size_t)nstr) * P;
+  fd.emit_count = meta + (3 + 2 * (size_t)nstr) * P;
+  fd.emit = fd.emit_count + 1;
+  fd.emit_cap = emit_cap;
+  for (int a = 0; a < A; a++) {
+    if (fr.off_values[a] != SIZE_MAX) fd.out_values[a] = fr.d_out + fr.off_values[a];
+    if (fr.off_bits[a] != SIZE_MAX) fd.out_bits[a] = reinterpret_cast<uint32_t*>(fr.d_out + fr.off_bits[a]);
+    if (fr.off_valid[a] != SIZE_MAX) fd.out_valid[a] = reinterpret_cast<uint32_t*>(fr.d_out + fr.off_valid[a]);
+    if (fr.off_chars[a] != SIZE_MAX) fd.out_chars[a] = fr.d_out + fr.off_chars[a];
+  }
+  fd.st_cap = st_cap_;
+  fd.st_base = st_base_;
+  fd.st_hv = st_hv_;
+  fd.st_sb = st_sb_;
+  fd.st_ihn = st_ihn_;
+  fd.err = d_err_;
+
+  // tables into staging (host inputs) or a pinned table buffer
+  uint8_t* htab;
+  uint8_t* dtab;
+  if (host_in) {
+    used_ = AlignUp(used_, 256);
+    if (used_ + tb_total > stage_cap_) return Status::Error(GZ_INVALID, "staging overflow");
+    htab = h_stage_[cur_] + used_;
+    dtab = d_stage_[cur_] + used_;
+    used_ += tb_total;
+  } else {
+    // two pinned table buffers; wait only for the copy that last used this one
+    const int ti = tab_cur_;
+    if (tab_busy_[ti]) {
+      st = Cuda(cudaEventSynchronize(tab_ev_[ti]), "table wait");
+      if (!st.ok()) return st;
+      tab_busy_[ti] = false;
+    }
+    if (tb_total > tables_cap_[ti]) {
+      if (h_tables_[ti]) cudaFreeHost(h_tables_[ti]);
+      h_tables_[ti] = nullptr;
+      tables_cap_[ti] = AlignUp(tb_total * 2, 1 << 16);
+      st = Cuda(cudaHostAlloc(&h_tables_[ti], tables_cap_[ti], cudaHostAllocDefault), "cudaHostAlloc(tables)");
+      if (!st.ok()) return st;
+    }
+    htab = h_tables_[ti];
+    dtab = nullptr;
+  }
+  memcpy(htab, batches.data(), sizeof(BatchDesc) * NB);
+  memcpy(htab + tb_batches, tiles.data(), sizeof(TileDesc) * T);
+  ColPtr* hc = reinterpret_cast<ColPtr*>(htab + tb_batches + tb_tiles);
+  for (uint32_t b = 0; b < NB; b++)
+    for (size_t c = 0; c < C; c++) hc[b * C + c] = pending_[b].cols[c];
+  if (host_in) {
+    st = Cuda(cudaMemcpyAsync(d_stage_[cur_], h_stage_[cur_], used_, cudaMemcpyHostToDevice, stream_), "H2D");
+    if (!st.ok()) return st;
+    st = Cuda(cudaEventRecord(stage_ev_[cur_], stream_), "event");
+    if (!st.ok()) return st;
+    stage_busy_[cur_] = true;
+  } else {
+    dtab = S + s_tab;
+    st = Cuda(cudaMemcpyAsync(dtab, htab, tb_total, cudaMemcpyHostToDevice, stream_), "H2D tables");
+    if (!st.ok()) return st;
+    st = Cuda(cudaEventRecord(tab_ev_[tab_cur_], stream_), "event");
+    if (!st.ok()) return st;
+    tab_busy_[tab_cur_] = true;
+    tab_cur_ ^= 1;
+  }
+  fd.batches = reinterpret_cast<const BatchDesc*>(dtab);
+  fd.tiles = reinterpret_cast<const TileDesc*>(dtab + tb_batches);
+  fd.cols = reinterpret_cast<const ColPtr*>(dtab + tb_batches + tb_tiles);
+
+  st = Cuda(cudaMemsetAsync(S + s_null, 0, (size_t)NB * A * 4, stream_), "memset");
+  if (!st.ok()) return st;
+  st = Cuda(cudaMemsetAsync(S + s_call, 0, (size_t)NB * 4, stream_), "memset");
+  if (!st.ok()) return st;
+  st = Cuda(cudaMemsetAsync(fd.emit_count, 0, 4, stream_), "memset");
+  if (!st.ok()) return st;
+  if (!fd.hist_in_smem) {
+    st = Cuda(cudaMemsetAsync(S + s_cnt, 0, TP * 4, stream_), "memset");
+    if (!st.ok()) return st;
+    if (nstr) {
+      st = Cuda(cudaMemsetAsync(S + s_bcnt, 0, TP * nstr * 4, stream_), "memset");
+      if (!st.ok()) return st;
+    }
+  }
+  for (auto& e : fr.ev) {
+    st = Cuda(cudaEventCreate(&e), "cudaEventCreate");
+    if (!st.ok()) return st;
+  }
+  cudaEventRecord(fr.ev[0], stream_);
+  st = Cuda(launch_hash_count(sd_, fd, stream_), "k_hash_count");
+  if (!st.ok()) return st;
+  cudaEventRecord(fr.ev[1], stream_);
+  st = Cuda(launch_plan(sd_, fd, stream_), "k_plan");
+  if (!st.ok()) return st;
+  cudaEventRecord(fr.ev[2], stream_);
+  st = Cuda(launch_scatter(sd_, fd, stream_), "k_scatter");
+  if (!st.ok()) return st;
+  cudaEventRecord(fr.ev[3], stream_);
+  // the last batch's call flag, for the empirical-size bookkeeping
+  st = Cuda(cudaMemcpyAsync(d_call_, fd.call_flags + (NB - 1), 4, cudaMemcpyDeviceToDevice, stream_), "D2D");
+  if (!st.ok()) return st;
+
+  // flush metadata to pinned host memory
+  fr.meta_words = meta_words;
+  st = PinnedMeta(meta_words * 4, &fr.h_meta);
+  if (!st.ok()) return st;
+  st = Cuda(cudaMemcpyAsync(fr.h_meta, meta, meta_words * 4, cudaMemcpyDeviceToHost, stream_), "D2H meta");
+  if (!st.ok()) return st;
+
+  resident_bytes_ += fr.out_bytes;
+  flushes_.push_back(std::move(fr));
+  pending_.clear();
+  pending_bytes_ = 0;
+  if (host_in) {
+    cur_ ^= 1;
+    used_ = 0;
+  }
+  // keep HBM use under the budget (or move every flush out when asked to)
+  const size_t budget = opts_.device_budget > 0 ? (size_t)opts_.device_budget : (64ull << 30);
+  for (auto& f : flushes_) {
+    if (!(opts_.keep_output_on_device == 0 || resident_bytes_ > budget)) break;
+    if (!f.on_host) {
+      st = MoveFlushToHost(f);
+      if (!st.ok()) return st;
+    }
+  }
+  return Status::OK();
+}
+
+Status Splitter::MoveFlushToHost(FlushRec& f) {
+  if (f.on_host) return Status::OK();
+  const int64_t t0 = NowNs();
+  f.h_out.resize(f.out_bytes);
+  Status st = Cuda(cudaMemcpyAsync(f.h_out.data(), f.d_out, f.out_bytes, cudaMemcpyDeviceToHost, stream_), "D2H out");
+  if (!st.ok()) return st;
+  st = Cuda(cudaFreeAsync(f.d_out, stream_), "cudaFreeAsync");
+  if (!st.ok()) return st;
+  st = Cuda(cudaStreamSynchronize(stream_), "sync");
+  if (!st.ok()) return st;
+  f.d_out = nullptr;
+  f.on_host = true;
+  resident_bytes_ -= f.out_bytes;
+  total_spill_time_ += NowNs() - t0;
+  return Status::OK();
+}
+
+Status Splitter::SyncAndCheck() {
+  Status st = Cuda(cudaStreamSynchronize(stream_), "device work");
+  if (!st.ok()) return st;
+  int32_t err = 0;
+  st = Cuda(cudaMemcpy(&err, d_err_, 4, cudaMemcpyDeviceToHost), "read error word");
+  if (!st.ok()) return st;
+  if (err & kErrBadOffsets)
+    return Status::Error(GZ_INVALID, "binary offsets are decreasing or exceed the value buffer");
+  if (err) return Status::Error(GZ_CUDA, "device emission list overflow");
+  for (; timed_flushes_ < flushes_.size(); timed_flushes_++) {
+    FlushRec& f = flushes_[timed_flushes_];
+    float ms[3] = {0, 0, 0};
+    for (int i = 0; i < 3; i++) cudaEventElapsedTime(&ms[i], f.ev[i], f.ev[i + 1]);
+    kernel_ms_[0] += ms[0];
+    kernel_ms_[1] += ms[1];
+    kernel_ms_[2] += ms[2];
+    kernel_ms_[3] += ms[0] + ms[1] + ms[2];
+    total_compute_pid_time_ += (int64_t)(ms[0] * 1e6);
+  }
+  return Status::OK();
+}
+
+// Turns the emission records of finished flushes into per-partition segments.
+Status Splitter::ProcessFlushes() {
+  const int P = P_;
+  const int nstr = n_str_;
+  const int words = kEmitFixedWords + nstr;
+  for (; processed_flushes_ < flushes_.size(); processed_flushes_++) {
+    const int32_t fi = (int32_t)processed_flushes_;
+    const FlushRec& f = flushes_[fi];
+    const uint32_t ne = f.emit_count(P, nstr);
+    if (ne > f.emit_cap) return Status::Error(GZ_CUDA, "emission list overflow");
+    const uint32_t* recs = f.emits(P, nstr);
+    std::vector<std::vector<const uint32_t*>> by_p(P);
+    for (uint32_t i = 0; i < ne; i++) {
+      const uint32_t* r = recs + (size_t)i * words;
+      if (r[0] >= (uint32_t)P) return Status::Error(GZ_CUDA, "bad emission record");
+      by_p[r[0]].push_back(r);
+    }
+    const uint32_t* rows_f = f.rows_f();
+    const uint32_t* bytes_f = f.bytes_f(P);
+    for (int p = 0; p < P; p++) {
+      auto& v = by_p[p];
+      std::sort(v.begin(), v.end(), [](const uint32_t* x, const uint32_t* y) { return x[1] < y[1]; });
+      uint32_t frow0 = 0, vpos0 = 0;
+      std::vector<uint32_t> fb0(nstr, 0);
+      Segment& open = open_[p];
+      for (const uint32_t* r : v) {
+        const uint32_t frow1 = r[1];
+        std::vector<uint32_t> fb1(r + kEmitFixedWords, r + kEmitFixedWords + nstr);
+        if (frow1 > frow0) open.pieces.push_back(Piece{fi, frow0, frow1, vpos0, fb0, fb1});
+        vpos0 += (frow1 - frow0 + 63u) & ~63u;
+        frow0 = frow1;
+        fb0 = fb1;
+        open.rows = r[2];
+        open.hv = (uint64_t)r[3] | ((uint64_t)r[4] << 32);
+        open.at_stop = false;
+        open.spilled = opts_.prefer_spill != 0;
+        uint32_t got = 0;
+        for (auto& pc : open.pieces) got += pc.frow1 - pc.frow0;
+        if (got != open.rows) return Status::Error(GZ_CUDA, "segment rows do not add up");
+        segments_[p].push_back(std::move(open));
+        open = Segment();
+      }
+      if (rows_f[p] > frow0) {
+        std::vector<uint32_t> fb1(nstr);
+        for (int k = 0; k < nstr; k++) fb1[k] = bytes_f[(size_t)k * P + p];
+        open.pieces.push_back(Piece{fi, frow0, rows_f[p], vpos0, fb0, fb1});
+      }
+    }
+  }
+  return Status::OK();
+}
+
+// Assembles the record batch of segment `s` of partition `p` from the host copies of the
+// flush outputs and writes it as one IPC message (CacheRecordBatch + WriteIpcPayload).
+Status Splitter::AssembleAndWrite(int p, Segment& s, ByteSink* sink, bool count_only, int64_t* raw) {
+  const int P = P_;
+  const int nstr = n_str_;
+  const uint32_t n = s.rows;
+  std::vector<FieldNodeMeta> nodes;
+  std::vector<ChunkedBuffer> bufs;
+  std::vector<std::vector<uint8_t>> temps;
+  temps.reserve(2 * fields_.size());
+  static const uint8_t kZero4[4] = {0, 0, 0, 0};
+  int64_t rawb = 0;
+
+  // bits of a per-flush bit region (validity or bool values) for this segment
+  auto gather_bits = [&](const std::vector<size_t> FlushRec::*offs, int a, bool* all_ones) -> const uint8_t* {
+    const int64_t nb = BytesForBits(n);
+    if (s.pieces.size() == 1) {
+      const Piece& pc = s.pieces[0];
+      const FlushRec& f = flushes_[pc.flush];
+      const size_t off = (f.*offs)[a];
+      if (off == SIZE_MAX) {
+        *all_ones = true;
+        return nullptr;
+      }
+      *all_ones = false;
+      const uint64_t bit0 = (uint64_t)f.vstart(P)[p] + pc.vpos0;  // multiple of 64
+      return f.h_out.data() + off + bit0 / 8;
+    }
+    temps.emplace_back(nb, 0xff);
+    uint8_t* dst = temps.back().data();
+    uint64_t drow = 0;
+    bool any = false;
+    for (const Piece& pc : s.pieces) {
+      const FlushRec& f = flushes_[pc.flush];
+      const size_t off = (f.*offs)[a];
+      const uint32_t len = pc.frow1 - pc.frow0;
+      if (off != SIZE_MAX) {
+        const uint64_t bit0 = (uint64_t)f.vstart(P)[p] + pc.vpos0;
+        CopyBits(f.h_out.data() + off, bit0, dst, drow, len);
+        any = true;
+      }
+      drow += len;
+    }
+    *all_ones = !any;
+    return any ? dst : nullptr;
+  };
+
+  for (size_t fi = 0; fi < fields_.size(); fi++) {
+    const int a = field_array_[fi];
+    if (a < 0) {
+      nodes.push_back(FieldNodeMeta{n, n});
+      continue;
+    }
+    const int kind = sd_.arr_kind[a];
+    int64_t nulls = 0;
+    ChunkedBuffer vb;
+    if (s.hv & (1ull << a)) {
+      rawb += BytesForBits(n);
+      bool ones = true;
+      const uint8_t* bits = gather_bits(&FlushRec::off_valid, a, &ones);
+      if (!ones) {
+        nulls = CountZeros(bits, n);
+        if (nulls > 0) vb.push_back(Chunk{bits, BytesForBits(n)});
+      }
+    }
+    nodes.push_back(FieldNodeMeta{n, nulls});
+    bufs.push_back(vb);
+    if (kind == COL_FIXED) {
+      const int w = sd_.arr_width[a];
+      ChunkedBuffer vals;
+      for (const Piece& pc : s.pieces) {
+        const FlushRec& f = flushes_[pc.flush];
+        const uint8_t* base = f.h_out.data() + f.off_values[a];
+        vals.push_back(Chunk{base + ((size_t)f.pstart(P)[p] + pc.frow0) * w,
+                             (int64_t)(pc.frow1 - pc.frow0) * w});
+      }
+      rawb += (int64_t)n * w;
+      bufs.push_back(vals);
+    } else if (kind == COL_BOOL) {
+      bool ones = true;
+      const uint8_t* bits = gather_bits(&FlushRec::off_bits, a, &ones);
+      if (ones) {
+        temps.emplace_back(BytesForBits(n), 0xff);
+        bits = temps.back().data();
+      }
+      rawb += BytesForBits(n);
+      bufs.push_back(ChunkedBuffer{Chunk{bits, BytesForBits(n)}});
+    } else {
+      const int k = sd_.arr_str[a];
+      ChunkedBuffer offs, chars;
+      offs.push_back(Chunk{kZero4, 4});
+      int64_t clen = 0;
+      for (const Piece& pc : s.pieces) {
+        const FlushRec& f = flushes_[pc.flush];
+        const uint8_t* ob = f.h_out.data() + f.off_values[a];
+        offs.push_back(Chunk{ob + ((size_t)f.pstart(P)[p] + pc.frow0) * 4, (int64_t)(pc.frow1 - pc.frow0) * 4});
+        const uint8_t* cb = f.h_out.data() + f.off_chars[a];
+        const uint32_t c0 = pc.fb0[k], c1 = pc.fb1[k];
+        if (c1 > c0) chars.push_back(Chunk{cb + (size_t)f.cstart(P, nstr)[(size_t)k * P + p] + c0, (int64_t)(c1 - c0)});
+        clen += c1 - c0;
+      }
+      rawb += (int64_t)(n + 1) * 4 + clen;
+      bufs.push_back(offs);
+      bufs.push_back(chars);
+    }
+  }
+  *raw = rawb;
+  if (count_only) {
+    std::vector<int64_t> lens;
+    for (auto& b : bufs) {
+      int64_t l = 0;
+      for (auto& c : b) l += c.len;
+      lens.push_back(l);
+    }
+    s.message_bytes = RecordBatchMessageSize((int64_t)nodes.size(), lens, &s.body_length);
+    return Status::OK();
+  }
+  int64_t body = 0;
+  const int64_t wrote = WriteRecordBatchMessage(sink, n, nodes, bufs, &body);
+  if (wrote < 0) return Status::Error(GZ_IO, "write failed");
+  s.body_length = body;
+  s.message_bytes = wrote;
+  return Status::OK();
+}
+
+Status Splitter::Stop() {
+  if (stopped_) return Status::Error(GZ_INVALID, "splitter already stopped");
+  Status st = Cuda(cudaSetDevice(device_), "cudaSetDevice");
+  if (!st.ok()) return st;
+  st = Flush();
+  if (!st.ok()) return st;
+  st = SyncAndCheck();
+  if (!st.ok()) return st;
+  st = ProcessFlushes();
+  if (!st.ok()) return st;
+  // the open buffer of every partition is emitted at Stop (CacheRecordBatch(pid, true))
+  std::vector<uint32_t> base(P_);
+  std::vector<unsigned long long> hv(P_);
+  st = Cuda(cudaMemcpy(base.data(), st_base_, 4 * (size_t)P_, cudaMemcpyDeviceToHost), "D2H state");
+  if (!st.ok()) return st;
+  st = Cuda(cudaMemcpy(hv.data(), st_hv_, 8 * (size_t)P_, cudaMemcpyDeviceToHost), "D2H state");
+  if (!st.ok()) return st;
+  for (int p = 0; p < P_; p++) {
+    Segment& open = open_[p];
+    if (base[p] > 0) {
+      open.rows = base[p];
+      open.hv = hv[p];
+      open.at_stop = true;
+      uint32_t got = 0;
+      for (auto& pc : open.pieces) got += pc.frow1 - pc.frow0;
+      if (got != open.rows) return Status::Error(GZ_CUDA, "open segment rows do not add up");
+      segments_[p].push_back(std::move(open));
+    }
+    open = Segment();
+  }
+  for (auto& f : flushes_) {
+    st = MoveFlushToHost(f);
+    if (!st.ok()) return st;
+  }
+  // write the data file, partitions in order (Stop, splitter.cc:395-437)
+  const int64_t t0 = NowNs();
+  std::unique_ptr<ByteSink> sink;
+  FileSink* fsink = nullptr;
+  if (data_file_.empty()) {
+    sink.reset(new MemorySink());
+  } else {
+    fsink = new FileSink(data_file_);
+    sink.reset(fsink);
+    if (!fsink->ok()) return Status::Error(GZ_IO, "cannot open data file " + data_file_);
+  }
+  int64_t compress_ns = 0;
+  for (int p = 0; p < P_; p++) {
+    auto& segs = segments_[p];
+    if (segs.empty()) {
+      partition_lengths_[p] = 0;
+      continue;
+    }
+    const int64_t before = sink->Tell();
+    if (opts_.write_schema) {
+      return Status::Error(GZ_NOT_IMPLEMENTED, "write_schema is not implemented yet");
+    }
+    for (Segment& s : segs) {
+      int64_t raw = 0;
+      const int64_t c0 = NowNs();
+      st = AssembleAndWrite(p, s, sink.get(), false, &raw);
+      compress_ns += NowNs() - c0;
+      if (!st.ok()) return st;
+      raw_partition_lengths_[p] += raw;
+      if (s.spilled) total_bytes_spilled_ += s.message_bytes;
+    }
+    if (!WriteEos(sink.get())) return Status::Error(GZ_IO, "write failed");
+    partition_lengths_[p] = sink->Tell() - before;
+    total_bytes_written_ += partition_lengths_[p];
+  }
+  if (fsink) {
+    if (!fsink->Close()) return Status::Error(GZ_IO, "closing the data file failed");
+  } else {
+    data_bytes_ = std::move(static_cast<MemorySink*>(sink.get())->buffer());
+  }
+  total_compress_time_ += compress_ns;
+  total_write_time_ += NowNs() - t0 - compress_ns;
+  stopped_ = true;
+  // release device memory early
+  for (auto& f : flushes_) f.h_out.clear();
+  return Status::OK();
+}
+
+Status Splitter::SpillFixedSize(int64_t size, int64_t* actual) {
+  *actual = 0;
+  if (opts_.prefer_spill) return Status::OK();  // every emitted batch was spilled already
+  // cached batches exist only without prefer_spill: make them visible on the host
+  Status st = Flush();
+  if (!st.ok()) return st;
+  st = SyncAndCheck();
+  if (!st.ok()) return st;
+  st = ProcessFlushes();
+  if (!st.ok()) return st;
+  for (auto& f : flushes_) {
+    st = MoveFlushToHost(f);
+    if (!st.ok()) return st;
+  }
+  // SpillLargestPartition up to 5 times (splitter.cc:741-799): largest cached body bytes
+  int64_t cur = 0;
+  int tries = 0;
+  while (cur < size && tries < 5) {
+    tries++;
+    int64_t best = 0;
+    int pick = -1;
+    for (int p = 0; p < P_; p++) {
+      int64_t cached = 0;
+      for (Segment& s : segments_[p]) {
+        if (s.spilled) continue;
+        if (s.body_length < 0) {
+          int64_t raw;
+          st = AssembleAndWrite(p, s, nullptr, true, &raw);
+          if (!st.ok()) return st;
+        }
+        cached += s.body_length;
+      }
+      if (cached > best) {
+        best = cached;
+        pick = p;
+      }
+    }
+    if (pick < 0) break;
+    for (Segment& s : segments_[pick]) s.spilled = true;
+    cur += best;
+  }
+  *actual = cur;
+  return Status::OK();
+}
+
+Status Splitter::SetCompressType(int32_t codec) {
+  if (codec != 0) return Status::Error(GZ_NOT_IMPLEMENTED, "only uncompressed shuffle output is implemented");
+  return Status::OK();
+}
+
+// IPC body length of the input batch (Splitter::CompressedSize, splitter.cc:358-369).
+Status Splitter::CompressedSize(int32_t num_rows, const int64_t* addrs, const int64_t* sizes,
+                                int32_t n, int64_t* out) {
+  if (n < n_bufs_expected_) return Status::Error(GZ_INVALID, "insufficient number of in_buf_addrs");
+  if (opts_.input_kind != GZ_INPUT_HOST)
+    return Status::Error(GZ_NOT_IMPLEMENTED, "CompressedSize reads host buffers");
+  const uint32_t nr = (uint32_t)std::max(num_rows, 0);
+  auto pad8 = [](int64_t x) { return (x + 7) & ~int64_t(7); };
+  int64_t body = 0;
+  for (size_t f = 0; f < fields_.size(); f++) {
+    const int t = fields_[f].type;
+    if (t == GZ_TYPE_NULL) continue;
+    const int b0 = field_buf0_[f];
+    if (addrs[b0] != 0 && sizes[b0] > 0 && nr > 0) {
+      const int64_t z = CountZeros(reinterpret_cast<const uint8_t*>(addrs[b0]), nr);
+      if (z > 0) body += pad8(BytesForBits(nr));
+    }
+    if (IsBinary(t)) {
+      const int32_t* off = reinterpret_cast<const int32_t*>(addrs[b0 + 1]);
+      body += pad8((int64_t)(nr + 1) * 4);
+      if (nr > 0 && off) body += pad8(off[nr] - off[0]);
+    } else if (t == GZ_TYPE_BOOL) {
+      body += pad8(BytesForBits(nr));
+    } else {
+      body += pad8((int64_t)nr * ByteWidth(t));
+    }
+  }
+  *out = body;
+  return Status::OK();
+}
+
+Status Splitter::LastPids(uint16_t* out, int32_t n) {
+  Status st = Flush();
+  if (!st.ok()) return st;
+  st = SyncAndCheck();
+  if (!st.ok()) return st;
+  if (flushes_.empty() || (uint32_t)n != last_batch_rows_)
+    return Status::Error(GZ_INVALID, "no batch of that size was split last");
+  const FlushRec& f = flushes_.back();
+  // the pids of the last flush sit at the start of the scratch; the last batch is at its end
+  const uint16_t* pids = reinterpret_cast<const uint16_t*>(d_scratch_);
+  return Cuda(cudaMemcpy(out, pids + (f.n_rows - (uint32_t)n), 2 * (size_t)n, cudaMemcpyDeviceToHost),
+              "D2H pids");
+}
+
+Status Splitter::KernelTimes(double* out4) {
+  Status st = SyncAndCheck();
+  if (!st.ok()) return st;
+  for (int i = 0; i < 4; i++) out4[i] = kernel_ms_[i];
+  return Status::OK();
+}
+
+}  // namespace gz

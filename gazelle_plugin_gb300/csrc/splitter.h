@@ -1,0 +1,197 @@
+// gz::Splitter — the host side of the GB300 hash split, keeping the reference Splitter's
+// interface (native-sql-engine/cpp/src/shuffle/splitter.h:55-126): Make / Split / Stop /
+// SpillFixedSize / SetCompressType / CompressedSize and the metric getters.
+//
+// Split() only gathers the batch (host inputs are copied into a pinned staging buffer
+// before it returns, as the JNI contract requires); every `flush_bytes` of input one device
+// pass runs the three kernels on the splitter's stream.  Emission decisions are made on the
+// device by k_plan, so Split never waits for the GPU.  Stop() finishes the device work,
+// assembles every emitted partition batch from the flush outputs and writes the Arrow IPC
+// data file in partition order.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/gz_split.h"
+#include "gz_engine.cuh"
+#include "ipc.h"
+#include "schema_ipc.h"
+
+namespace gz {
+
+struct Status {
+  GzStatus code = GZ_OK;
+  std::string msg;
+  bool ok() const { return code == GZ_OK; }
+  static Status OK() { return Status(); }
+  static Status Error(GzStatus c, std::string m) {
+    Status s;
+    s.code = c;
+    s.msg = std::move(m);
+    return s;
+  }
+};
+
+class Splitter {
+ public:
+  static Status Make(const std::string& short_name, std::vector<Field> fields, int32_t P,
+                     std::vector<int32_t> keys, const GzSplitOptions& opts,
+                     std::unique_ptr<Splitter>* out);
+  ~Splitter();
+
+  Status Split(int32_t num_rows, const int64_t* addrs, const int64_t* sizes, int32_t n);
+  Status CompressedSize(int32_t num_rows, const int64_t* addrs, const int64_t* sizes, int32_t n,
+                        int64_t* out);
+  Status Stop();
+  Status SpillFixedSize(int64_t size, int64_t* actual);
+  Status SetCompressType(int32_t codec);
+  Status LastPids(uint16_t* out, int32_t n);
+  Status KernelTimes(double* out4);
+
+  int64_t TotalBytesWritten() const { return total_bytes_written_; }
+  int64_t TotalBytesSpilled() const { return total_bytes_spilled_; }
+  int64_t TotalWriteTime() const { return total_write_time_; }
+  int64_t TotalSpillTime() const { return total_spill_time_; }
+  int64_t TotalCompressTime() const { return total_compress_time_; }
+  int64_t TotalComputePidTime() const { return total_compute_pid_time_; }
+  const std::vector<int64_t>& PartitionLengths() const { return partition_lengths_; }
+  const std::vector<int64_t>& RawPartitionLengths() const { return raw_partition_lengths_; }
+  const std::vector<uint8_t>& DataBytes() const { return data_bytes_; }
+  int32_t num_partitions() const { return P_; }
+
+ private:
+  struct PendingBatch {
+    uint32_t nrows;
+    uint32_t split_size;
+    uint32_t last_tile_rows;
+    std::vector<ColPtr> cols;          // device addresses, one per schema field
+    uint64_t validity_mask;            // array columns with a validity buffer
+    std::vector<uint64_t> char_bytes;  // per binary column: bytes the output may need
+  };
+
+  // One device pass and what Stop needs from it.
+  struct FlushRec {
+    uint32_t n_rows = 0;
+    uint32_t n_batches = 0;
+    uint8_t* d_out = nullptr;           // device outputs (nullptr once moved to host)
+    size_t out_bytes = 0;
+    std::vector<uint8_t> h_out;         // host copy of the outputs
+    bool on_host = false;
+    std::vector<size_t> off_values, off_bits, off_valid, off_chars;  // per array column, SIZE_MAX: none
+    uint32_t* h_meta = nullptr;         // pinned: rows_f, pstart, vstart, bytes_f, cstart, count, emit
+    size_t meta_words = 0;
+    uint32_t emit_cap = 0;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // k1 start, plan start, k3 start, end
+    const uint32_t* rows_f() const { return h_meta; }
+    const uint32_t* pstart(int P) const { return h_meta + P; }
+    const uint32_t* vstart(int P) const { return h_meta + 2 * (size_t)P; }
+    const uint32_t* bytes_f(int P) const { return h_meta + 3 * (size_t)P; }
+    const uint32_t* cstart(int P, int nstr) const { return h_meta + (3 + (size_t)nstr) * P; }
+    uint32_t emit_count(int P, int nstr) const { return h_meta[(3 + 2 * (size_t)nstr) * P]; }
+    const uint32_t* emits(int P, int nstr) const { return h_meta + (3 + 2 * (size_t)nstr) * P + 1; }
+  };
+
+  struct Piece {
+    int32_t flush;
+    uint32_t frow0, frow1;  // flush-local rows of the partition
+    uint32_t vpos0;         // flush-local validity bit of frow0
+    std::vector<uint32_t> fb0, fb1;  // flush-local byte range per binary column
+  };
+
+  struct Segment {  // one emitted record batch of one partition
+    uint32_t rows = 0;
+    uint64_t hv = 0;
+    bool at_stop = false;
+    bool spilled = false;
+    int64_t body_length = -1;
+    int64_t message_bytes = -1;
+    std::vector<Piece> pieces;
+  };
+
+  Splitter() = default;
+  Status Init(const std::string& short_name, std::vector<Field> fields, int32_t P,
+              std::vector<int32_t> keys, const GzSplitOptions& opts);
+  Status Cuda(cudaError_t e, const char* what);
+  Status EnsureScratch(size_t bytes_needed);
+  Status EnsureStaging(size_t bytes);
+  Status PinnedMeta(size_t bytes, uint32_t** out);
+  Status Flush();
+  Status SyncAndCheck();
+  Status MoveFlushToHost(FlushRec& f);
+  Status ProcessFlushes();
+  Status AssembleAndWrite(int p, Segment& s, ByteSink* sink, bool count_only, int64_t* raw);
+  uint32_t SplitBatchSize(int32_t num_rows, const std::vector<const int32_t*>& host_offsets,
+                          bool* complete);
+
+  // schema
+  std::vector<Field> fields_;
+  int32_t P_ = 0;
+  std::vector<int32_t> keys_;
+  GzSplitOptions opts_{};
+  std::string data_file_;
+  SchemaDesc sd_{};
+  std::vector<int32_t> array_idx_;  // schema index per array column
+  std::vector<int32_t> field_array_;  // array column per schema field (-1 for null type)
+  std::vector<int32_t> field_buf0_;   // index of the field's first buffer in the flat list
+  int32_t n_bufs_expected_ = 0;
+  int32_t fixed_cnt_ = 0, n_str_ = 0, n_array_ = 0;
+  std::vector<uint64_t> empirical_;  // binary_array_empirical_size_
+
+  // device
+  int device_ = 0;
+  cudaStream_t stream_ = nullptr;
+  uint8_t* d_state_ = nullptr;      // persistent partition state
+  uint32_t* st_cap_ = nullptr;
+  uint32_t* st_base_ = nullptr;
+  unsigned long long* st_hv_ = nullptr;
+  uint32_t* st_sb_ = nullptr;
+  unsigned long long* st_ihn_ = nullptr;
+  int32_t* d_err_ = nullptr;
+  uint32_t* d_call_ = nullptr;
+  uint8_t* d_scratch_ = nullptr;
+  size_t scratch_cap_ = 0;
+
+  // staging (host inputs): double-buffered pinned host + device
+  uint8_t* h_stage_[2] = {nullptr, nullptr};
+  uint8_t* d_stage_[2] = {nullptr, nullptr};
+  size_t stage_cap_ = 0;
+  cudaEvent_t stage_ev_[2] = {nullptr, nullptr};
+  bool stage_busy_[2] = {false, false};
+  int cur_ = 0;
+  size_t used_ = 0;
+  uint8_t* h_tables_[2] = {nullptr, nullptr};  // pinned tables for device-retained inputs
+  size_t tables_cap_[2] = {0, 0};
+  cudaEvent_t tab_ev_[2] = {nullptr, nullptr};
+  bool tab_busy_[2] = {false, false};
+  int tab_cur_ = 0;
+  std::vector<void*> meta_chunks_;
+  size_t meta_chunk_cap_ = 0, meta_used_ = 0;
+  std::vector<std::vector<int32_t>> dev_off_;  // offset ends read from device inputs
+  bool seen_rows_ = false;
+
+  std::vector<PendingBatch> pending_;
+  uint64_t pending_bytes_ = 0;
+  std::vector<FlushRec> flushes_;
+  size_t processed_flushes_ = 0;
+  size_t resident_bytes_ = 0;
+
+  // per-partition emitted segments (host view, built from the flush metadata)
+  std::vector<std::vector<Segment>> segments_;
+  std::vector<Segment> open_;  // open segment per partition
+  uint32_t last_batch_rows_ = 0;
+
+  bool stopped_ = false;
+  int64_t total_bytes_written_ = 0, total_bytes_spilled_ = 0, total_write_time_ = 0;
+  int64_t total_spill_time_ = 0, total_compress_time_ = 0, total_compute_pid_time_ = 0;
+  double kernel_ms_[4] = {0, 0, 0, 0};
+  size_t timed_flushes_ = 0;
+  std::vector<int64_t> partition_lengths_, raw_partition_lengths_;
+  std::vector<uint8_t> data_bytes_;
+};
+
+}  // namespace gz

@@ -1,0 +1,277 @@
+"""Python mirror of the reference's shuffle-splitter boundary, over libgzsplit.so.
+
+``ShuffleSplitterJniWrapper`` keeps the method names, argument meaning and error behaviour of
+com.intel.oap.vectorized.ShuffleSplitterJniWrapper
+(native-sql-engine/core/src/main/java/com/intel/oap/vectorized/ShuffleSplitterJniWrapper.java:41-135)
+and ``SplitResult`` the fields of SplitResult.java:21-39.  Every call goes through the C ABI in
+include/gz_split.h; there is no Python or CPU fallback: a missing library raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import os
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgzsplit.so")
+
+GZ_OK, GZ_INVALID, GZ_OOM, GZ_IO, GZ_NOT_IMPLEMENTED, GZ_TIMEOUT, GZ_CUDA = range(7)
+GZ_INPUT_HOST, GZ_INPUT_DEVICE_RETAINED = 0, 1
+_STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "OOM", 3: "IO", 4: "NOT_IMPLEMENTED", 5: "TIMEOUT",
+                 6: "CUDA"}
+
+
+class SplitterError(RuntimeError):
+    """A non-OK GzStatus (the JNI layer throws a Java exception in the same places)."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{_STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class GzSplitOptions(ctypes.Structure):
+    _fields_ = [
+        ("offheap_per_task", ctypes.c_int64),
+        ("buffer_size", ctypes.c_int32),
+        ("num_sub_dirs", ctypes.c_int32),
+        ("batch_compress_threshold", ctypes.c_int32),
+        ("compression", ctypes.c_int32),
+        ("prefer_spill", ctypes.c_int32),
+        ("write_schema", ctypes.c_int32),
+        ("buffered_write", ctypes.c_int32),
+        ("input_kind", ctypes.c_int32),
+        ("device", ctypes.c_int32),
+        ("keep_output_on_device", ctypes.c_int32),
+        ("flush_bytes", ctypes.c_int64),
+        ("device_budget", ctypes.c_int64),
+        ("data_file", ctypes.c_char_p),
+        ("local_dirs", ctypes.c_char_p),
+    ]
+
+
+class GzField(ctypes.Structure):
+    _fields_ = [
+        ("type", ctypes.c_int32),
+        ("nullable", ctypes.c_int32),
+        ("precision", ctypes.c_int32),
+        ("scale", ctypes.c_int32),
+        ("unit", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("name", ctypes.c_char_p),
+    ]
+
+
+class GzSplitResult(ctypes.Structure):
+    _fields_ = [
+        ("total_compute_pid_time", ctypes.c_int64),
+        ("total_write_time", ctypes.c_int64),
+        ("total_spill_time", ctypes.c_int64),
+        ("total_compress_time", ctypes.c_int64),
+        ("total_bytes_written", ctypes.c_int64),
+        ("total_bytes_spilled", ctypes.c_int64),
+        ("partition_lengths", ctypes.POINTER(ctypes.c_int64)),
+        ("raw_partition_lengths", ctypes.POINTER(ctypes.c_int64)),
+    ]
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """The C-ABI library; raises when it has not been built (no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run __graft_entry__.build() first")
+        L = ctypes.CDLL(LIB_PATH)
+        c_i64p = ctypes.POINTER(ctypes.c_int64)
+        L.gz_split_default_options.argtypes = [ctypes.POINTER(GzSplitOptions)]
+        L.gz_split_make.restype = ctypes.c_int
+        L.gz_split_make.argtypes = [ctypes.c_char_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64,
+                                    ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(GzSplitOptions),
+                                    c_i64p]
+        L.gz_split_make_fields.restype = ctypes.c_int
+        L.gz_split_make_fields.argtypes = [ctypes.c_char_p, ctypes.c_int32, ctypes.POINTER(GzField),
+                                           ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32,
+                                           ctypes.POINTER(GzSplitOptions), c_i64p]
+        L.gz_split_split.restype = ctypes.c_int
+        L.gz_split_split.argtypes = [ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                     ctypes.c_int32, ctypes.c_int32, c_i64p]
+        L.gz_split_stop.restype = ctypes.c_int
+        L.gz_split_stop.argtypes = [ctypes.c_int64, ctypes.POINTER(GzSplitResult)]
+        L.gz_split_data.restype = ctypes.c_int
+        L.gz_split_data.argtypes = [ctypes.c_int64, ctypes.c_void_p, c_i64p]
+        L.gz_split_spill.restype = ctypes.c_int
+        L.gz_split_spill.argtypes = [ctypes.c_int64, ctypes.c_int64, c_i64p]
+        L.gz_split_set_compress.restype = ctypes.c_int
+        L.gz_split_set_compress.argtypes = [ctypes.c_int64, ctypes.c_int32]
+        L.gz_split_close.restype = ctypes.c_int
+        L.gz_split_close.argtypes = [ctypes.c_int64]
+        L.gz_split_last_pids.restype = ctypes.c_int
+        L.gz_split_last_pids.argtypes = [ctypes.c_int64, ctypes.c_void_p, ctypes.c_int32]
+        L.gz_last_error.restype = ctypes.c_int
+        L.gz_last_error.argtypes = [ctypes.c_int64, ctypes.c_char_p, ctypes.c_size_t]
+        L.gz_split_kernel_times.restype = ctypes.c_int
+        L.gz_split_kernel_times.argtypes = [ctypes.c_int64, ctypes.POINTER(ctypes.c_double)]
+        _lib = L
+    return _lib
+
+
+def _check(status: int, handle: int = 0) -> None:
+    if status != GZ_OK:
+        buf = ctypes.create_string_buffer(1024)
+        lib().gz_last_error(handle, buf, 1024)
+        raise SplitterError(status, buf.value.decode(errors="replace"))
+
+
+def default_options() -> GzSplitOptions:
+    o = GzSplitOptions()
+    lib().gz_split_default_options(ctypes.byref(o))
+    return o
+
+
+@dataclasses.dataclass
+class SplitResult:
+    """SplitResult.java:21-39."""
+    totalComputePidTime: int
+    totalWriteTime: int
+    totalSpillTime: int
+    totalCompressTime: int
+    totalBytesWritten: int
+    totalBytesSpilled: int
+    partitionLengths: np.ndarray
+    rawPartitionLengths: np.ndarray
+
+
+@dataclasses.dataclass
+class NativePartitioning:
+    """NativePartitioning.java: short name, partition count, Arrow IPC schema bytes and the
+    hash keys.  The keys are schema column indices (the field-reference expressions Spark
+    sends, ColumnarShuffleExchangeExec.scala:307-326).  ``fields`` may stand in for the
+    schema bytes (a list of gazelle_plugin_gb300.workloads.Field)."""
+    shortName: str
+    numPartitions: int
+    schema: Optional[bytes] = None
+    keyColumns: Sequence[int] = ()
+    fields: Optional[list] = None
+
+
+class ShuffleSplitterJniWrapper:
+    """Method-for-method mirror of ShuffleSplitterJniWrapper.java."""
+
+    def make(self, part: NativePartitioning, offheapPerTask: int = 0, bufferSize: int = 4096,
+             codec: Optional[str] = None, batchCompressThreshold: int = 256,
+             dataFile: str = "", subDirsPerLocalDir: int = 64, localDirs: str = "",
+             preferSpill: bool = True, memoryPoolId: int = 0, writeSchema: bool = False,
+             **device_options) -> int:
+        o = default_options()
+        o.offheap_per_task = offheapPerTask
+        if bufferSize > 0:
+            o.buffer_size = bufferSize
+        if subDirsPerLocalDir > 0:
+            o.num_sub_dirs = subDirsPerLocalDir
+        o.batch_compress_threshold = batchCompressThreshold
+        o.compression = 0 if codec in (None, "", "uncompressed", "none") else 1
+        o.prefer_spill = int(preferSpill)
+        o.write_schema = int(writeSchema)
+        o.buffered_write = 1
+        self._keep = [dataFile.encode(), localDirs.encode()]
+        o.data_file = self._keep[0]
+        o.local_dirs = self._keep[1]
+        for k, v in device_options.items():
+            setattr(o, k, v)
+        keys = np.asarray(list(part.keyColumns), np.int32)
+        h = ctypes.c_int64(0)
+        if part.schema is not None:
+            sb = ctypes.create_string_buffer(part.schema, len(part.schema))
+            st = lib().gz_split_make(part.shortName.encode(), part.numPartitions, sb,
+                                     len(part.schema), keys.ctypes.data, len(keys),
+                                     ctypes.byref(o), ctypes.byref(h))
+        else:
+            arr = (GzField * len(part.fields))()
+            self._names = [f.name.encode() for f in part.fields]
+            for i, f in enumerate(part.fields):
+                arr[i].type = f.code
+                arr[i].nullable = int(f.nullable)
+                arr[i].name = self._names[i]
+            st = lib().gz_split_make_fields(part.shortName.encode(), part.numPartitions, arr,
+                                            len(part.fields), keys.ctypes.data, len(keys),
+                                            ctypes.byref(o), ctypes.byref(h))
+        _check(st, 0)
+        self._partitions = {h.value: part.numPartitions}
+        return h.value
+
+    def nativeSpill(self, splitterId: int, size: int, callBySelf: bool = False) -> int:
+        actual = ctypes.c_int64(0)
+        _check(lib().gz_split_spill(splitterId, size, ctypes.byref(actual)), splitterId)
+        return actual.value
+
+    def split(self, splitterId: int, numRows: int, bufAddrs, bufSizes,
+              firstRecordBatch: bool = False) -> int:
+        addrs = np.ascontiguousarray(bufAddrs, dtype=np.int64)
+        sizes = np.ascontiguousarray(bufSizes, dtype=np.int64)
+        if len(addrs) != len(sizes):
+            raise SplitterError(GZ_INVALID, "Native split: length of buf_addrs and buf_sizes mismatch")
+        out = ctypes.c_int64(-1)
+        _check(lib().gz_split_split(splitterId, numRows, addrs.ctypes.data, sizes.ctypes.data,
+                                    len(addrs), int(firstRecordBatch), ctypes.byref(out)),
+               splitterId)
+        return out.value
+
+    def setCompressType(self, splitterId: int, compressType: str) -> None:
+        codec = 0 if compressType in (None, "", "uncompressed", "none") else 1
+        _check(lib().gz_split_set_compress(splitterId, codec), splitterId)
+
+    def stop(self, splitterId: int, numPartitions: Optional[int] = None) -> SplitResult:
+        P = numPartitions or self._partitions[splitterId]
+        pl = np.zeros(P, np.int64)
+        rl = np.zeros(P, np.int64)
+        r = GzSplitResult()
+        r.partition_lengths = pl.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+        r.raw_partition_lengths = rl.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+        _check(lib().gz_split_stop(splitterId, ctypes.byref(r)), splitterId)
+        return SplitResult(r.total_compute_pid_time, r.total_write_time, r.total_spill_time,
+                           r.total_compress_time, r.total_bytes_written, r.total_bytes_spilled,
+                           pl, rl)
+
+    def close(self, splitterId: int) -> None:
+        _check(lib().gz_split_close(splitterId))
+
+    # helpers beyond the Java surface -----------------------------------------------------
+    def data(self, splitterId: int) -> bytes:
+        n = ctypes.c_int64(0)
+        _check(lib().gz_split_data(splitterId, None, ctypes.byref(n)), splitterId)
+        buf = np.zeros(n.value, np.uint8)
+        if n.value:
+            _check(lib().gz_split_data(splitterId, buf.ctypes.data, ctypes.byref(n)), splitterId)
+        return buf.tobytes()
+
+    def lastPids(self, splitterId: int, numRows: int) -> np.ndarray:
+        out = np.zeros(numRows, np.uint16)
+        _check(lib().gz_split_last_pids(splitterId, out.ctypes.data, numRows), splitterId)
+        return out
+
+    def kernelTimes(self, splitterId: int) -> List[float]:
+        out = (ctypes.c_double * 4)()
+        _check(lib().gz_split_kernel_times(splitterId, out), splitterId)
+        return list(out)
+
+
+def split_batches(schema, batches, num_partitions: int, key_cols: Sequence[int],
+                  **make_kwargs):
+    """Make -> Split every batch -> Stop through the C ABI; returns (SplitResult, data)."""
+    w = ShuffleSplitterJniWrapper()
+    h = w.make(NativePartitioning("hash", num_partitions, None, key_cols, list(schema)),
+               **make_kwargs)
+    try:
+        for b in batches:
+            addrs, sizes = b.addrs_sizes()
+            w.split(h, b.num_rows, addrs, sizes, False)
+        res = w.stop(h)
+        data = w.data(h)
+    finally:
+        w.close(h)
+    return res, data

@@ -2,8 +2,9 @@
 
 A batch is held the way the reference's JNI boundary receives it
 (native-sql-engine/cpp/src/jni/jni_common.h:308-382): one flat list of Arrow buffers in
-schema order, ``[validity, (offsets), values]`` per non-null field, where an empty
-validity buffer means the column has no nulls.  Nothing here needs pyarrow.
+schema order, ``[validity, (offsets), values]`` per field (a null-type field takes two
+empty buffers, as the JNI's generic branch consumes them), where an empty validity buffer
+means the column has no nulls.  Nothing here needs pyarrow.
 
 Workloads (seeded numpy PCG64; nulls i.i.d. per cell; a null utf8 cell is a zero-length
 slot; a null fixed-width cell keeps its generated value):
@@ -222,6 +223,7 @@ def random_batch(rng, schema: Sequence[Field], n: int, null_frac: float) -> Batc
     bufs = []
     for f in schema:
         if f.type == "null":
+            bufs += [np.zeros(0, np.uint8), np.zeros(0, np.uint8)]
             continue
         nf = null_frac if rng.random() < 0.7 else 0.0
         if f.is_binary:

@@ -1,0 +1,177 @@
+/*
+ * gz_split.h — C ABI of the GB300 columnar shuffle hash split.
+ *
+ * A drop-in for Gazelle's native shuffle splitter boundary: each entry point replaces one
+ * JNI method of com.intel.oap.vectorized.ShuffleSplitterJniWrapper, implemented in
+ * native-sql-engine/cpp/src/jni/jni_wrapper.cc, over the C++ Splitter of
+ * native-sql-engine/cpp/src/shuffle/splitter.h.  Plain pointers and sizes only.
+ *
+ * Errors: every call returns a GzStatus; gz_last_error() gives the message of the last
+ * failing call on a handle (or of the last failing gz_split_make on this thread when
+ * handle == 0).  Device-side work is asynchronous: a CUDA failure surfaces on the next
+ * call on the same handle, and at the latest from gz_split_stop.
+ */
+#ifndef GZ_SPLIT_H
+#define GZ_SPLIT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum GzStatus {
+  GZ_OK = 0,
+  GZ_INVALID = 1,          /* bad argument / id: the JNI layer throws (jni_wrapper.cc:1160-1163) */
+  GZ_OOM = 2,              /* arrow::Status::OutOfMemory */
+  GZ_IO = 3,               /* data / spill file errors */
+  GZ_NOT_IMPLEMENTED = 4,  /* arrow::Status::NotImplemented (types, codecs, partitioners) */
+  GZ_TIMEOUT = 5,          /* a bounded device-side wait gave up */
+  GZ_CUDA = 6              /* a CUDA runtime error */
+} GzStatus;
+
+/* Arrow field types accepted by the splitter (utils.h:116-158 ToSplitterTypeId subset). */
+typedef enum GzType {
+  GZ_TYPE_NULL = 0, GZ_TYPE_BOOL = 1, GZ_TYPE_INT8 = 2, GZ_TYPE_UINT8 = 3,
+  GZ_TYPE_INT16 = 4, GZ_TYPE_UINT16 = 5, GZ_TYPE_HALF_FLOAT = 6, GZ_TYPE_INT32 = 7,
+  GZ_TYPE_UINT32 = 8, GZ_TYPE_FLOAT32 = 9, GZ_TYPE_DATE32 = 10, GZ_TYPE_TIME32 = 11,
+  GZ_TYPE_INT64 = 12, GZ_TYPE_UINT64 = 13, GZ_TYPE_FLOAT64 = 14, GZ_TYPE_DATE64 = 15,
+  GZ_TYPE_TIME64 = 16, GZ_TYPE_TIMESTAMP = 17, GZ_TYPE_DECIMAL128 = 18,
+  GZ_TYPE_STRING = 19, GZ_TYPE_BINARY = 20
+} GzType;
+
+/* One schema field.  `unit`: time/timestamp unit (0 s, 1 ms, 2 us, 3 ns); `precision` /
+ * `scale`: decimal128.  Only used when writing the schema message (write_schema). */
+typedef struct GzField {
+  int32_t type;       /* GzType */
+  int32_t nullable;
+  int32_t precision;
+  int32_t scale;
+  int32_t unit;
+  int32_t reserved;
+  const char* name;
+} GzField;
+
+/* Where Split reads its buffers from. */
+typedef enum GzInputKind {
+  GZ_INPUT_HOST = 0,            /* host memory, borrowed for the call (the JNI contract) */
+  GZ_INPUT_DEVICE_RETAINED = 1  /* device memory the caller keeps valid and unchanged
+                                   until gz_split_stop returns (resident inputs) */
+} GzInputKind;
+
+/* SplitOptions (native-sql-engine/cpp/src/shuffle/type.h:39-59) plus device knobs.
+ * Initialise with gz_split_default_options(). */
+typedef struct GzSplitOptions {
+  int64_t offheap_per_task;          /* 0: partition buffers hold buffer_size rows */
+  int32_t buffer_size;               /* rows per partition buffer, <= 32768 (default 4096) */
+  int32_t num_sub_dirs;              /* spill sub-directories (default 64) */
+  int32_t batch_compress_threshold;  /* default 256; compression itself is off */
+  int32_t compression;               /* 0 = uncompressed (the only codec supported) */
+  int32_t prefer_spill;              /* default 1 */
+  int32_t write_schema;              /* default 1: schema message before each partition */
+  int32_t buffered_write;            /* accepted for compatibility */
+  int32_t input_kind;                /* GzInputKind, default GZ_INPUT_HOST */
+  int32_t device;                    /* CUDA device ordinal, default 0 */
+  int32_t keep_output_on_device;     /* 1 (default): partition data stays in HBM until Stop
+                                        or until device_budget is exceeded; 0: every flush is
+                                        copied to pinned host memory as soon as it is done */
+  int64_t flush_bytes;               /* input bytes gathered before one device pass
+                                        (default 512 MiB) */
+  int64_t device_budget;             /* HBM bytes for resident partition data before it is
+                                        moved to pinned host memory (default 64 GiB) */
+  const char* data_file;             /* written at Stop; NULL/"" keeps the bytes in memory */
+  const char* local_dirs;            /* comma separated spill dirs (unused: spills go to
+                                        pinned host memory) */
+} GzSplitOptions;
+
+/* SplitResult (native-sql-engine/core/src/main/java/com/intel/oap/vectorized/SplitResult.java:21-39).
+ * partition_lengths / raw_partition_lengths are caller arrays of num_partitions int64. */
+typedef struct GzSplitResult {
+  int64_t total_compute_pid_time;  /* ns */
+  int64_t total_write_time;        /* ns */
+  int64_t total_spill_time;        /* ns */
+  int64_t total_compress_time;     /* ns */
+  int64_t total_bytes_written;
+  int64_t total_bytes_spilled;
+  int64_t* partition_lengths;
+  int64_t* raw_partition_lengths;
+} GzSplitResult;
+
+/* Fills `opts` with the reference defaults (SplitOptions::Defaults, type.h:39-59). */
+void gz_split_default_options(GzSplitOptions* opts);
+
+/* Replaces ShuffleSplitterJniWrapper.nativeMake (jni_wrapper.cc:1031-1134).
+ * `short_name`: "hash" (other partitioners return GZ_NOT_IMPLEMENTED).
+ * `schema_ipc`: Arrow IPC encapsulated Schema message (what MakeSchema reads,
+ * jni_common.h:393-406).  `key_cols`: schema indices of the hash keys, in order; they stand
+ * for the gandiva field-reference expressions (ColumnarShuffleExchangeExec.scala:307-326). */
+GzStatus gz_split_make(const char* short_name, int32_t num_partitions, const uint8_t* schema_ipc,
+                       int64_t schema_len, const int32_t* key_cols, int32_t n_keys,
+                       const GzSplitOptions* opts, int64_t* out_handle);
+
+/* Same as gz_split_make with the schema given as a field array instead of IPC bytes. */
+GzStatus gz_split_make_fields(const char* short_name, int32_t num_partitions,
+                              const GzField* fields, int32_t n_fields, const int32_t* key_cols,
+                              int32_t n_keys, const GzSplitOptions* opts, int64_t* out_handle);
+
+/* Replaces ShuffleSplitterJniWrapper.split (jni_wrapper.cc:1156-1195).
+ * Buffers: flat list in schema order, [validity, (offsets), values] per non-null field; a
+ * zero address or size means an empty buffer, an empty validity buffer means no nulls
+ * (jni_common.h:308-382).  With first_batch != 0 the batch is not split and
+ * *out_compressed_size receives its IPC body length (Splitter::CompressedSize,
+ * splitter.cc:358-369); otherwise *out_compressed_size = -1.  Host inputs are fully read
+ * before the call returns. */
+GzStatus gz_split_split(int64_t handle, int32_t num_rows, const int64_t* buf_addrs,
+                        const int64_t* buf_sizes, int32_t n_bufs, int32_t first_batch,
+                        int64_t* out_compressed_size);
+
+/* Replaces ShuffleSplitterJniWrapper.stop (jni_wrapper.cc:1197-1227): emits every pending
+ * partition buffer, writes the data file (or keeps it in memory) and fills `out`. */
+GzStatus gz_split_stop(int64_t handle, GzSplitResult* out);
+
+/* Size of the data-file bytes produced by Stop; with `dst` non-NULL also copies them
+ * (tests and in-memory callers). */
+GzStatus gz_split_data(int64_t handle, uint8_t* dst, int64_t* out_size);
+
+/* Replaces ShuffleSplitterJniWrapper.nativeSpill (jni_wrapper.cc:984-999 -> SpillFixedSize,
+ * splitter.cc:741-756).  *actual = bytes the reference policy would release. */
+GzStatus gz_split_spill(int64_t handle, int64_t size, int64_t* actual);
+
+/* Replaces ShuffleSplitterJniWrapper.setCompressType (jni_wrapper.cc:1136-1154);
+ * codec 0 (uncompressed) only, anything else is GZ_NOT_IMPLEMENTED. */
+GzStatus gz_split_set_compress(int64_t handle, int32_t codec);
+
+/* Replaces ShuffleSplitterJniWrapper.close (jni_wrapper.cc:1229-1234). */
+GzStatus gz_split_close(int64_t handle);
+
+/* Partition ids of the rows of the most recent gz_split_split call (one uint16 per row,
+ * Spark pmod of the Murmur3 chain).  Test hook; forces the pending device work to finish. */
+GzStatus gz_split_last_pids(int64_t handle, uint16_t* out, int32_t num_rows);
+
+/* Message of the last error on `handle` (0: the calling thread's last make error). */
+GzStatus gz_last_error(int64_t handle, char* buf, size_t len);
+
+/* Device time (ms, CUDA events on the splitter's stream) spent in each kernel family since
+ * make: [hash+count, plan+scan, scatter, total device].  Test / bench hook. */
+GzStatus gz_split_kernel_times(int64_t handle, double* out4);
+
+/* ---- test hooks (no reference counterpart; used by the unit tests) ------------------- */
+
+/* Encodes one Arrow IPC RecordBatch message with the splitter's encoder.  nodes: L pairs
+ * {length, null_count}; bufs/buf_lens: M body buffers.  Writes into `out` (capacity
+ * out_cap) and sets *out_len; GZ_INVALID when it does not fit. */
+GzStatus gz_debug_encode_record_batch(int64_t length, const int64_t* nodes, int32_t n_nodes,
+                                      const uint8_t* const* bufs, const int64_t* buf_lens,
+                                      int32_t n_bufs, uint8_t* out, int64_t out_cap,
+                                      int64_t* out_len);
+
+/* Parses an Arrow IPC Schema message; writes up to `cap` GzType codes and nullable flags. */
+GzStatus gz_debug_parse_schema(const uint8_t* schema_ipc, int64_t len, int32_t* types,
+                               int32_t* nullable, int32_t cap, int32_t* n_fields);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GZ_SPLIT_H */

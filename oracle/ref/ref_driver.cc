@@ -52,6 +52,9 @@ arrow::Status WrapBatch(const std::shared_ptr<arrow::Schema>& schema, int32_t nu
   for (int f = 0; f < schema->num_fields(); f++) {
     auto type = schema->field(f)->type();
     if (type->id() == arrow::Type::NA) {
+      // the JNI generic branch consumes [validity, values] for a null-type field too
+      if (idx + 2 > n) return arrow::Status::Invalid("insufficient number of buffers");
+      idx += 2;
       arrays.push_back(arrow::ArrayData::Make(type, num_rows, {nullptr}, num_rows));
       continue;
     }

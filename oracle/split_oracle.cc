@@ -282,12 +282,17 @@ class OracleSplitter {
     return "";
   }
 
-  // buffers: flat list in schema order [validity, (offsets), values] per non-null field
+  // buffers: flat list in schema order [validity, (offsets), values] per field; a null-type
+  // field takes two ignored buffers (jni_common.h:308-343 generic branch)
   std::string Split(int32_t n, const int64_t* addrs, const int64_t* sizes, int nbuf) {
     std::vector<InCol> cols(fields_.size());
     int idx = 0;
     for (size_t f = 0; f < fields_.size(); f++) {
-      if (fields_[f].type == T_NULL) continue;
+      if (fields_[f].type == T_NULL) {
+        if (idx + 2 > nbuf) return "insufficient number of buffers";
+        idx += 2;
+        continue;
+      }
       if (idx >= nbuf) return "insufficient number of buffers";
       InCol c;
       if (sizes[idx] > 0 && addrs[idx] != 0) c.validity = (const uint8_t*)addrs[idx];

@@ -188,7 +188,8 @@ def ref_fixture_batches():
 def to_batch(rb) -> W.Batch:
     bufs = []
     for col in rb.columns:
-        if col.type.id == 0 or str(col.type) == "null":
+        if str(col.type) == "null":
+            bufs += [np.zeros(0, np.uint8), np.zeros(0, np.uint8)]
             continue
         arr_bufs = col.buffers()
         v = arr_bufs[0]

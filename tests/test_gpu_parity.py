@@ -1,0 +1,234 @@
+"""GPU parity: the CUDA split, called through the C ABI, against the oracle and against the
+golden fixtures made by the reference Splitter.  Every comparison is byte-for-byte."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from gazelle_plugin_gb300 import shuffle as S
+from gazelle_plugin_gb300 import workloads as W
+from oracle import oracle as O
+from tests.golden import make_golden as G
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = json.load(open(os.path.join(HERE, "golden", "splits.json")))["cases"]
+
+
+def gpu_split(schema, batches, P, keys, buffer_size=4096, prefer_spill=True, offheap_per_task=0,
+              **dev):
+    return S.split_batches(schema, batches, P, keys, bufferSize=buffer_size,
+                           preferSpill=prefer_spill, offheapPerTask=offheap_per_task,
+                           writeSchema=False, **dev)
+
+
+def assert_same(res, data, ref, tag=""):
+    assert np.array_equal(res.partitionLengths, ref.partition_lengths), tag
+    assert np.array_equal(res.rawPartitionLengths, ref.raw_partition_lengths), tag
+    for p in range(len(ref.partition_lengths)):
+        s0 = int(ref.partition_lengths[:p].sum())
+        a = data[s0:s0 + int(ref.partition_lengths[p])]
+        b = ref.partition_bytes(p)
+        assert a == b, f"{tag} partition {p}"
+    assert data == ref.data, tag
+    assert res.totalBytesSpilled == ref.bytes_spilled, tag
+    assert res.totalBytesWritten == ref.bytes_written, tag
+
+
+@pytest.mark.parametrize("case", GOLDEN, ids=[c["name"] for c in GOLDEN])
+def test_golden(case):
+    batches = G.regenerate(case)
+    schema = [W.Field(n, t, nl) for n, t, nl in case["schema"]]
+    res, data = gpu_split(schema, batches, case["num_partitions"], case["keys"], **case["options"])
+    assert list(res.partitionLengths) == case["partition_lengths"]
+    assert list(res.rawPartitionLengths) == case["raw_partition_lengths"]
+    assert res.totalBytesSpilled == case["bytes_spilled"]
+    assert hashlib.sha256(data).hexdigest() == case["data_sha256"]
+
+
+def test_reference_unit_test_batches():
+    meta = json.load(open(os.path.join(HERE, "golden", "ref_fixture.json")))
+    z = np.load(os.path.join(HERE, "golden", "ref_fixture.npz"))
+    schema = [W.Field(n, t, nl) for n, t, nl in meta["schema"]]
+    bs = []
+    for i in range(2):
+        nbuf = len([k for k in z.files if k.startswith(f"b{i}_buf")])
+        bs.append(W.Batch(int(z[f"b{i}_rows"][0]), [z[f"b{i}_buf{j}"] for j in range(nbuf)]))
+    seq = [bs[i] for i in meta["sequence"]]
+    for r in meta["runs"]:
+        res, data = gpu_split(schema, seq, r["num_partitions"], r["keys"], buffer_size=r["buffer_size"])
+        assert data == z[f"{r['tag']}_data"].tobytes(), r["tag"]
+        assert np.array_equal(res.partitionLengths, z[f"{r['tag']}_lengths"])
+        assert np.array_equal(res.rawPartitionLengths, z[f"{r['tag']}_raw"])
+
+
+def test_partition_ids_match_oracle():
+    w = S.ShuffleSplitterJniWrapper()
+    for schema, keys, P, batches in [
+        (W.C1_SCHEMA, W.C1_KEYS, 8, W.c1_batches(0, 2, 4096)),
+        (W.C2_SCHEMA, W.C2_KEYS, 200, W.c2_batches(1, 2, 4096)),
+        (W.C3_SCHEMA, W.C3_KEYS, 8000, W.c3_batches(2, 1, 20000, 0.2, 0.1)),
+    ]:
+        h = w.make(S.NativePartitioning("hash", P, None, keys, list(schema)), writeSchema=False)
+        o = O.OracleSplitter(schema, P, keys)
+        for b in batches:
+            addrs, sizes = b.addrs_sizes()
+            w.split(h, b.num_rows, addrs, sizes)
+            o.split(b)
+            assert np.array_equal(w.lastPids(h, b.num_rows), o.last_pids(b.num_rows))
+        w.close(h)
+        o.close()
+
+
+@pytest.mark.parametrize("seed", range(40))
+def test_random_vs_oracle(seed):
+    schema, batches, P, keys, opts = G.random_case(7000 + seed)
+    ref = O.run_oracle(schema, batches, P, keys, **opts)
+    res, data = gpu_split(schema, batches, P, keys, **opts)
+    assert_same(res, data, ref, f"seed {seed}")
+
+
+@pytest.mark.parametrize("flush_bytes", [1, 5000, 100000])
+def test_flush_grouping_does_not_change_bytes(flush_bytes):
+    """Batches cut into device passes at arbitrary points (partition batches then span
+    several passes) give the same bytes."""
+    batches = W.c1_batches(3, 12, 1000)
+    ref = O.run_oracle(W.C1_SCHEMA, batches, 8, W.C1_KEYS, buffer_size=700)
+    res, data = gpu_split(W.C1_SCHEMA, batches, 8, W.C1_KEYS, buffer_size=700,
+                          flush_bytes=flush_bytes)
+    assert_same(res, data, ref)
+
+
+def test_output_copied_to_host_every_pass():
+    batches = W.c2_batches(5, 24, 4096)
+    ref = O.run_oracle(W.C2_SCHEMA, batches, 200, W.C2_KEYS, buffer_size=512)
+    res, data = gpu_split(W.C2_SCHEMA, batches, 200, W.C2_KEYS, buffer_size=512,
+                          keep_output_on_device=0, flush_bytes=1 << 20)
+    assert_same(res, data, ref)
+
+
+@pytest.mark.parametrize("P,null_frac,key_nulls", [(16, 0.0, 0.0), (200, 0.2, 0.0),
+                                                   (2000, 0.2, 0.05), (8000, 0.0, 0.0)])
+def test_zipf_fanout(P, null_frac, key_nulls):
+    batches = W.c3_batches(2, 3, 32768, null_frac, key_nulls)
+    ref = O.run_oracle(W.C3_SCHEMA, batches, P, W.C3_KEYS)
+    res, data = gpu_split(W.C3_SCHEMA, batches, P, W.C3_KEYS)
+    assert_same(res, data, ref, f"P={P}")
+
+
+def test_wide_schema_many_batches():
+    batches = W.c2_batches(9, 300, 4096)
+    ref = O.run_oracle(W.C2_SCHEMA, batches, 200, W.C2_KEYS)
+    res, data = gpu_split(W.C2_SCHEMA, batches, 200, W.C2_KEYS, flush_bytes=64 << 20)
+    assert_same(res, data, ref)
+
+
+def test_prefer_spill_off_and_native_spill():
+    batches = W.c1_batches(0, 30, 512)
+    o = O.OracleSplitter(W.C1_SCHEMA, 8, W.C1_KEYS, buffer_size=512, prefer_spill=False)
+    w = S.ShuffleSplitterJniWrapper()
+    h = w.make(S.NativePartitioning("hash", 8, None, W.C1_KEYS, list(W.C1_SCHEMA)),
+               bufferSize=512, preferSpill=False, writeSchema=False)
+    for i, b in enumerate(batches):
+        o.split(b)
+        addrs, sizes = b.addrs_sizes()
+        w.split(h, b.num_rows, addrs, sizes)
+        if i in (12, 25):
+            assert w.nativeSpill(h, 20000) == o.spill(20000)
+    ref = o.stop()
+    res = w.stop(h)
+    data = w.data(h)
+    w.close(h)
+    assert_same(res, data, ref)
+
+
+def test_offheap_split_size():
+    schema = [W.Field("k", "int64"), W.Field("s", "utf8"), W.Field("t", "utf8")]
+    rng = np.random.default_rng(4)
+    batches = [W.random_batch(rng, schema, 300, 0.1) for _ in range(10)]
+    # first batch: every string empty, so the empirical sizes are learned later
+    b0 = batches[0]
+    b0.buffers[3] = np.zeros(301 * 4, np.uint8)
+    b0.buffers[4] = np.zeros(0, np.uint8)
+    for opts in [dict(offheap_per_task=1 << 16, prefer_spill=False),
+                 dict(offheap_per_task=1 << 18, prefer_spill=False)]:
+        ref = O.run_oracle(schema, batches, 7, [0], **opts)
+        res, data = gpu_split(schema, batches, 7, [0], **opts)
+        assert_same(res, data, ref, str(opts))
+
+
+def test_empty_batches_are_ignored():
+    batches = W.c1_batches(1, 4, 900)
+    empty = W.Batch(0, [np.zeros(0, np.uint8) for _ in batches[0].buffers])
+    seq = [empty, batches[0], empty, batches[1], batches[2], empty, batches[3]]
+    ref = O.run_oracle(W.C1_SCHEMA, batches, 8, W.C1_KEYS)
+    res, data = gpu_split(W.C1_SCHEMA, seq, 8, W.C1_KEYS)
+    assert_same(res, data, ref)
+
+
+def test_device_resident_inputs():
+    torch = pytest.importorskip("torch")
+    batches = W.c2_batches(11, 20, 4096)
+    keep = []
+    dev_batches = []
+    for b in batches:
+        bufs = []
+        for buf in b.buffers:
+            t = torch.from_numpy(buf.copy()).cuda() if buf.nbytes else torch.zeros(0, dtype=torch.uint8).cuda()
+            keep.append(t)
+            bufs.append(t)
+        dev_batches.append((b.num_rows, bufs))
+    w = S.ShuffleSplitterJniWrapper()
+    h = w.make(S.NativePartitioning("hash", 200, None, W.C2_KEYS, list(W.C2_SCHEMA)),
+               writeSchema=False, input_kind=S.GZ_INPUT_DEVICE_RETAINED)
+    for n, bufs in dev_batches:
+        addrs = [t.data_ptr() if t.numel() else 0 for t in bufs]
+        sizes = [t.numel() for t in bufs]
+        w.split(h, n, addrs, sizes)
+    res = w.stop(h)
+    data = w.data(h)
+    w.close(h)
+    ref = O.run_oracle(W.C2_SCHEMA, batches, 200, W.C2_KEYS)
+    assert_same(res, data, ref)
+
+
+def test_schema_ipc_make():
+    pa = pytest.importorskip("pyarrow")
+    batches = W.c1_batches(0, 2, 4096)
+    sbytes = O.to_pyarrow_schema(W.C1_SCHEMA).serialize().to_pybytes()
+    w = S.ShuffleSplitterJniWrapper()
+    h = w.make(S.NativePartitioning("hash", 8, sbytes, W.C1_KEYS), writeSchema=False)
+    for b in batches:
+        addrs, sizes = b.addrs_sizes()
+        w.split(h, b.num_rows, addrs, sizes)
+    res = w.stop(h, 8)
+    data = w.data(h)
+    w.close(h)
+    assert data == O.run_oracle(W.C1_SCHEMA, batches, 8, W.C1_KEYS).data
+
+
+def test_errors_are_reported_not_crashed():
+    w = S.ShuffleSplitterJniWrapper()
+    with pytest.raises(S.SplitterError):
+        w.make(S.NativePartitioning("rr", 4, None, [0], list(W.C1_SCHEMA)))
+    with pytest.raises(S.SplitterError):
+        w.make(S.NativePartitioning("hash", 0, None, [0], list(W.C1_SCHEMA)))
+    with pytest.raises(S.SplitterError):
+        w.make(S.NativePartitioning("hash", 4, None, [3], list(W.C1_SCHEMA)))  # utf8 key
+    h = w.make(S.NativePartitioning("hash", 4, None, [0], list(W.C1_SCHEMA)), writeSchema=False)
+    b = W.c1_batches(0, 1, 100)[0]
+    addrs, sizes = b.addrs_sizes()
+    with pytest.raises(S.SplitterError):
+        w.split(h, b.num_rows, addrs[:3], sizes[:3])
+    sizes2 = sizes.copy()
+    sizes2[3] = 8  # int64 values buffer too small
+    with pytest.raises(S.SplitterError):
+        w.split(h, b.num_rows, addrs, sizes2)
+    with pytest.raises(S.SplitterError):
+        w.split(12345, 1, addrs, sizes)
+    w.split(h, b.num_rows, addrs, sizes)
+    w.stop(h)
+    w.close(h)
