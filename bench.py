@@ -1,0 +1,445 @@
+#!/usr/bin/env python
+"""Hash-split throughput of the GB300 shuffle splitter on the wide fact-table workload.
+
+Workload (one step): 200M rows in 4096-row record batches, 16 columns = 4 int64 keys
+U[0,6e8), 4 float64 U[0,1e5) at 0.01 granularity, 2 int32 U[8000,10600), 3 single-char utf8
+flags over 3-symbol alphabets, 3 utf8 comments of U{10..44} chars over [a-z ]; 2% nulls in the
+12 non-key columns; hash keys = columns 0 and 1; 200 partitions; compression off.  The rows
+are generated on the device with a seeded torch RNG (36 GB of inputs, far above the 126 MB
+L2, so every step reads HBM).
+
+Lines:
+  value : Split of every batch with the inputs resident in HBM (GZ_INPUT_DEVICE_RETAINED),
+          through the C ABI's per-batch loop, until the device work is complete.
+  e2e   : the same through the host-buffer contract (GZ_INPUT_HOST: each batch copied before
+          Split returns), partition data copied back to pinned host memory after every pass.
+  metric: (input buffer bytes + raw partition bytes) / time, in GB/s.
+
+--impl reference times the CPU splitter (the oracle's restatement of the reference
+Splitter; the reference itself needs the Arrow fork and x86) on all host cores, one splitter
+per core over disjoint shards of a bounded sample of the same batches.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "hash-split GB/s ((input + partition bytes) / split time)"
+WORKLOAD = ("wide fact-table split: 200M rows, 4096-row batches, 16 columns "
+            "(4 int64 keys, 4 float64, 2 int32, 3 utf8 flags, 3 utf8 comments), "
+            "2% nulls, hash on keys 0-1, 200 partitions")
+BATCH_ROWS = 4096
+PARTITIONS = 200
+KEYS = [0, 1]
+
+
+def schema():
+    from gazelle_plugin_gb300 import workloads as W
+    return W.C2_SCHEMA
+
+
+# ---------------------------------------------------------------------------------------
+def generate_on_device(total_rows: int, seed: int = 1):
+    """Seeded workload batches on cuda:0.  Returns (rows[int32], addrs[nb, nbufs],
+    sizes[nb, nbufs], tensors) where column j of addrs points into tensors[j] (None for the
+    empty validity buffers of the key columns)."""
+    import torch
+    dev = "cuda"
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    br = BATCH_ROWS
+    nb = (total_rows + br - 1) // br
+    npad = nb * br
+    rows = np.full(nb, br, np.int32)
+    rows[-1] = total_rows - (nb - 1) * br
+    r64 = rows.astype(np.int64)
+    b_idx = np.arange(nb, dtype=np.int64)
+    weights = (2 ** torch.arange(8, device=dev, dtype=torch.int32)).to(torch.int32)
+    bufcols = []  # (tensor or None, addr[nb], size[nb])
+
+    def add(t, addr, size):
+        bufcols.append((t, np.asarray(addr, np.int64), np.asarray(size, np.int64)))
+
+    def validity():
+        v = torch.rand(npad, generator=g, device=dev) >= 0.02
+        bits = (v.view(-1, 8).to(torch.int32) * weights).sum(1).to(torch.uint8)
+        add(bits, bits.data_ptr() + b_idx * (br // 8), (r64 + 7) // 8)
+        return v
+
+    for _ in range(4):
+        t = torch.randint(0, 600_000_000, (npad,), generator=g, device=dev, dtype=torch.int64)
+        add(None, np.zeros(nb), np.zeros(nb))
+        add(t, t.data_ptr() + b_idx * br * 8, r64 * 8)
+    for _ in range(4):
+        validity()
+        t = torch.floor(torch.rand(npad, generator=g, device=dev, dtype=torch.float64) * 1e7) / 100.0
+        add(t, t.data_ptr() + b_idx * br * 8, r64 * 8)
+    for _ in range(2):
+        validity()
+        t = torch.randint(8000, 10600, (npad,), generator=g, device=dev, dtype=torch.int32)
+        add(t, t.data_ptr() + b_idx * br * 4, r64 * 4)
+    for alphabet, lo, hi in [(b"AFN", 1, 1), (b"OFP", 1, 1), (b"RAN", 1, 1),
+                             (b"abcdefghijklmnopqrstuvwxyz ", 10, 44),
+                             (b"abcdefghijklmnopqrstuvwxyz ", 10, 44),
+                             (b"abcdefghijklmnopqrstuvwxyz ", 10, 44)]:
+        v = validity()
+        lens = torch.randint(lo, hi + 1, (npad,), generator=g, device=dev, dtype=torch.int32)
+        lens = lens * v.to(torch.int32)  # a null slot has no characters
+        off = torch.zeros((nb, br + 1), dtype=torch.int32, device=dev)
+        off[:, 1:] = torch.cumsum(lens.view(nb, br), dim=1, dtype=torch.int32)
+        last = torch.from_numpy(rows.astype(np.int64)).to(dev)
+        totals = off.gather(1, last.view(-1, 1)).view(-1).to(torch.int64)
+        starts = torch.cumsum(totals, 0) - totals
+        alpha = torch.tensor(list(alphabet), dtype=torch.uint8, device=dev)
+        chars = alpha[torch.randint(0, len(alphabet), (int(totals.sum().item()) + 16,),
+                                    generator=g, device=dev)]
+        add(off, off.data_ptr() + b_idx * (br + 1) * 4, (r64 + 1) * 4)
+        add(chars, chars.data_ptr() + starts.cpu().numpy(), totals.cpu().numpy())
+    addrs = np.stack([c[1] for c in bufcols], axis=1)
+    sizes = np.stack([c[2] for c in bufcols], axis=1)
+    addrs[sizes == 0] = 0
+    torch.cuda.synchronize()
+    return rows, addrs, sizes, [c[0] for c in bufcols]
+
+
+def host_copy(addrs, sizes, tensors):
+    """Pinned host copies of the generated buffers, laid out like the device ones; returns
+    (host addrs, pinned tensors)."""
+    import torch
+    haddrs = np.zeros_like(addrs)
+    keep = []
+    for j, t in enumerate(tensors):
+        if t is None:
+            continue
+        h = torch.empty(t.numel() * t.element_size(), dtype=torch.uint8, pin_memory=True)
+        h.copy_(t.view(-1).view(torch.uint8))
+        keep.append(h)
+        haddrs[:, j] = addrs[:, j] - t.data_ptr() + h.data_ptr()
+    haddrs[sizes == 0] = 0
+    return haddrs, keep
+
+
+def host_batches(rows, addrs, sizes, tensors, first: int, count: int):
+    """Numpy copies of batches [first, first+count) as workloads.Batch objects."""
+    from gazelle_plugin_gb300 import workloads as W
+    cols = []
+    for j, t in enumerate(tensors):
+        if t is None:
+            cols.append(None)
+            continue
+        lo = int(addrs[first, j] - t.data_ptr())
+        last = first + count - 1
+        hi = int(addrs[last, j] - t.data_ptr() + sizes[last, j])
+        cols.append((lo, t.view(-1).view(__import__("torch").uint8)[lo:hi].cpu().numpy()))
+    out = []
+    for b in range(first, first + count):
+        bufs = []
+        for j, c in enumerate(cols):
+            n = int(sizes[b, j])
+            if c is None or n == 0:
+                bufs.append(np.zeros(0, np.uint8))
+                continue
+            lo, arr = c
+            s0 = int(addrs[b, j] - tensors[j].data_ptr()) - lo
+            bufs.append(arr[s0:s0 + n].copy())
+        out.append(W.Batch(int(rows[b]), bufs))
+    return out
+
+
+# ---------------------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sms, maxs, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sms.append(float(f[1]))
+                maxs.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sms) if sms else None,
+                "sm_max_mhz": max(maxs) if maxs else None,
+                "reasons": sorted(reasons), "samples": len(sms)}
+
+
+def measured_peak_gbs():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------------------
+def cpu_split_sample(batches, threads: int):
+    """Oracle splitters, one per thread over disjoint shards; returns (seconds, bytes)."""
+    from oracle import oracle as O
+    shards = [batches[i::threads] for i in range(threads)]
+    res = [None] * threads
+    sp = [O.OracleSplitter(schema(), PARTITIONS, KEYS) for _ in range(threads)]
+    barrier = threading.Barrier(threads + 1)
+
+    def work(i):
+        barrier.wait()
+        t0 = time.perf_counter()
+        for b in shards[i]:
+            sp[i].split(b)
+        res[i] = time.perf_counter() - t0
+
+    ths = [threading.Thread(target=work, args=(i,)) for i in range(threads)]
+    for t in ths:
+        t.start()
+    barrier.wait()
+    t0 = time.perf_counter()
+    for t in ths:
+        t.join()
+    wall = time.perf_counter() - t0
+    out_bytes = 0
+    for s in sp:
+        out_bytes += int(s.stop().raw_partition_lengths.sum())
+        s.close()
+    in_bytes = sum(b.nbytes for b in batches)
+    return wall, in_bytes + out_bytes
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import torch
+    threads = os.cpu_count() or 1
+    rows, addrs, sizes, keep = generate_on_device(args.sample_batches * BATCH_ROWS, seed=1)
+    batches = host_batches(rows, addrs, sizes, keep, 0, args.sample_batches)
+    del keep
+    torch.cuda.empty_cache()
+    for _ in range(args.warmup):
+        cpu_split_sample(batches[: max(threads, len(batches) // 8)], threads)
+    times, nbytes = [], 0
+    for _ in range(args.steps):
+        dt, nb = cpu_split_sample(batches, threads)
+        times.append(dt)
+        nbytes = nb
+    total = sum(times)
+    value = nbytes * args.steps / total / 1e9
+    sample = f"{len(batches)} batches x {BATCH_ROWS} rows of the workload per step"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+        "data": "synthetic (seeded torch RNG, same distributions)",
+        "config": {"workload": WORKLOAD, "sample": sample},
+        "cpu_baseline": {"value": value, "unit": "GB/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+    from gazelle_plugin_gb300 import shuffle as S
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    w = S.ShuffleSplitterJniWrapper()
+    part = S.NativePartitioning("hash", PARTITIONS, None, KEYS, list(schema()))
+    rows, addrs, sizes, keep = generate_on_device(args.rows, seed=1 + rank)
+    in_bytes = int(sizes.sum())
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # -- value: inputs resident in HBM ---------------------------------------------------
+    dev_opts = dict(writeSchema=False, input_kind=S.GZ_INPUT_DEVICE_RETAINED,
+                    flush_bytes=args.flush_mb << 20, device_budget=200 << 30)
+
+    def one_step(opts, a, s, stats=None):
+        h = w.make(part, **opts)
+        w.splitBatches(h, rows, a, s)
+        w.sync(h)
+        if stats is not None:
+            stats.append(w.kernelTimes(h) + w.stats(h))
+        w.close(h)
+
+    # one full run with Stop for the partition bytes (raw lengths) and the Stop cost
+    h = w.make(part, dataFile="/dev/null", **dev_opts)
+    w.splitBatches(h, rows, addrs, sizes)
+    t0 = time.perf_counter()
+    res = w.stop(h, PARTITIONS)
+    stop_s = time.perf_counter() - t0
+    w.close(h)
+    out_bytes = int(res.rawPartitionLengths.sum())
+    alg_bytes = in_bytes + out_bytes
+
+    for _ in range(args.warmup):
+        one_step(dev_opts, addrs, sizes)
+    barrier()
+    clocks = ClockSampler()
+    clocks.start()
+    stats = []
+    times = []
+    for _ in range(args.steps):
+        barrier()
+        t0 = time.perf_counter()
+        one_step(dev_opts, addrs, sizes, stats)
+        barrier()
+        times.append(time.perf_counter() - t0)
+    clk = clocks.stop()
+    t_local = sum(times)
+    t_max = t_local
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([t_local], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+    value = alg_bytes * args.steps * world / t_max / 1e9
+    ms_per_step = t_max / args.steps * 1e3
+    # kernel timings (CUDA events on the splitter's stream), per step
+    k_hash = statistics.mean(s[0] for s in stats)
+    k_plan = statistics.mean(s[1] for s in stats)
+    k_scat = statistics.mean(s[2] for s in stats)
+    flushes = statistics.mean(s[4] for s in stats)
+    peak, peak_kind = measured_peak_gbs()
+    scat_gbs = alg_bytes / (k_scat / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "k_scatter", "achieved": scat_gbs, "peak": peak,
+                "unit": "GB/s", "frac": scat_gbs / peak, "peak_source": peak_kind,
+                "traffic": args.traffic_per_launch,
+                "launches_per_step": flushes,
+                "algorithmic_bytes_per_launch": alg_bytes / max(flushes, 1),
+                "avg_launch_ms": k_scat / max(flushes, 1)}
+
+    # -- e2e: host buffers through the JNI-style contract ---------------------------------
+    e2e = None
+    if not args.no_e2e:
+        haddrs, host = host_copy(addrs, sizes, keep)
+        host_opts = dict(writeSchema=False, input_kind=S.GZ_INPUT_HOST, keep_output_on_device=0,
+                         flush_bytes=args.flush_mb << 20)
+        for _ in range(max(1, args.warmup - 1)):
+            one_step(host_opts, haddrs, sizes)
+        e_stats, e_times = [], []
+        for _ in range(args.steps):
+            barrier()
+            t0 = time.perf_counter()
+            one_step(host_opts, haddrs, sizes, e_stats)
+            barrier()
+            e_times.append(time.perf_counter() - t0)
+        e_t = sum(e_times)
+        e2e = {"value": alg_bytes * args.steps / e_t / 1e9, "unit": "GB/s",
+               "h2d_bytes_per_step": int(statistics.mean(s[6] for s in e_stats)),
+               "d2h_bytes_per_step": int(statistics.mean(s[7] for s in e_stats)),
+               "ms_per_step": e_t / args.steps * 1e3}
+        del host
+
+    # -- CPU baseline on a bounded sample ---------------------------------------------------
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        sample = host_batches(rows, addrs, sizes, keep, 0, args.sample_batches)
+        cpu_split_sample(sample[: threads * 2], threads)
+        dt, nb = cpu_split_sample(sample, threads)
+        cpu = {"value": nb / dt / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
+               "sample": f"first {len(sample)} batches x {BATCH_ROWS} rows of the workload"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+            "data": "synthetic (seeded torch RNG on the device, workload distributions)",
+            "config": {"workload": WORKLOAD, "rows": int(args.rows), "batch_rows": BATCH_ROWS,
+                       "num_partitions": PARTITIONS, "input_bytes": in_bytes,
+                       "partition_bytes": out_bytes,
+                       "l2": "inputs (36 GB) larger than L2; no flush needed",
+                       "flush_mb": args.flush_mb},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "clocks": clk,
+            "gpu_launches": int(round(3 * flushes * args.steps)),
+            "kernels_ms_per_step": {"k_hash_count": k_hash, "k_plan": k_plan, "k_scatter": k_scat},
+            "rows_per_s": args.rows * args.steps * world / t_max,
+            "input_gbs": in_bytes * args.steps * world / t_max / 1e9,
+            "stop_s": stop_s,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--rows", type=int, default=200_000_000)
+    ap.add_argument("--flush-mb", type=int, default=512)
+    ap.add_argument("--sample-batches", type=int, default=512)
+    ap.add_argument("--traffic-per-launch", type=float, default=None)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

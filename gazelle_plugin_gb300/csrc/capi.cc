@@ -143,6 +143,31 @@ GzStatus gz_split_split(int64_t handle, int32_t num_rows, const int64_t* buf_add
   return Report(e.get(), e->splitter->Split(num_rows, buf_addrs, buf_sizes, n_bufs));
 }
 
+GzStatus gz_split_split_batches(int64_t handle, int32_t n_batches, const int32_t* rows,
+                                const int64_t* buf_addrs, const int64_t* buf_sizes, int32_t n_bufs) {
+  auto e = Lookup(handle);
+  if (!e) {
+    t_make_error = "Invalid splitter id " + std::to_string(handle);
+    return GZ_INVALID;
+  }
+  if (!rows || !buf_addrs || !buf_sizes) {
+    e->last_error = "Native split: null buffer list";
+    return GZ_INVALID;
+  }
+  for (int32_t i = 0; i < n_batches; i++) {
+    GzStatus s = Report(e.get(), e->splitter->Split(rows[i], buf_addrs + (size_t)i * n_bufs,
+                                                    buf_sizes + (size_t)i * n_bufs, n_bufs));
+    if (s != GZ_OK) return s;
+  }
+  return GZ_OK;
+}
+
+GzStatus gz_split_sync(int64_t handle) {
+  auto e = Lookup(handle);
+  if (!e) return GZ_INVALID;
+  return Report(e.get(), e->splitter->Sync());
+}
+
 GzStatus gz_split_stop(int64_t handle, GzSplitResult* out) {
   auto e = Lookup(handle);
   if (!e) {
@@ -224,6 +249,13 @@ GzStatus gz_split_kernel_times(int64_t handle, double* out4) {
   auto e = Lookup(handle);
   if (!e || !out4) return GZ_INVALID;
   return Report(e.get(), e->splitter->KernelTimes(out4));
+}
+
+GzStatus gz_split_stats(int64_t handle, int64_t* out8) {
+  auto e = Lookup(handle);
+  if (!e || !out8) return GZ_INVALID;
+  e->splitter->Stats(out8);
+  return GZ_OK;
 }
 
 GzStatus gz_debug_encode_record_batch(int64_t length, const int64_t* nodes, int32_t n_nodes,

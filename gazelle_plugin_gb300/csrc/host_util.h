@@ -1,0 +1,32 @@
+// Host-side helpers of the splitter: a process-wide pool of pinned host blocks (flush outputs
+// copied out of HBM) and a small thread pool that spreads large memcpys over several cores
+// (staging a caller's host batch before Split returns).
+#pragma once
+#include <stddef.h>
+#include <stdint.h>
+
+#include <vector>
+
+namespace gz {
+
+struct PinnedBlock {
+  uint8_t* ptr = nullptr;
+  size_t cap = 0;
+};
+
+// Pinned (page-locked) host blocks, reused across splitters.  Acquire returns a block of at
+// least `bytes`; ptr == nullptr when cudaHostAlloc failed.
+PinnedBlock PinnedAcquire(size_t bytes);
+void PinnedRelease(PinnedBlock b);
+
+struct CopyJob {
+  uint8_t* dst;
+  const uint8_t* src;
+  size_t n;
+};
+
+// Copies every job; large totals are split over worker threads and the caller.  Returns when
+// all bytes are copied.
+void ParallelCopy(const std::vector<CopyJob>& jobs, size_t total_bytes);
+
+}  // namespace gz

@@ -8,6 +8,7 @@
 #include <numeric>
 
 #include "gz_kernels.h"
+#include "host_util.h"
 
 namespace gz {
 
@@ -200,6 +201,10 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
     if (!st.ok()) return st;
   }
   dev_off_.resize(n_str_);
+  need_.assign(n_bufs_expected_ + 1, Need{nullptr, 0});
+  host_off_.assign(n_str_, nullptr);
+  char_scratch_.assign(std::max(n_str_, 1), 0);
+
   partition_lengths_.assign(P_, 0);
   raw_partition_lengths_.assign(P_, 0);
   segments_.assign(P_, {});
@@ -211,6 +216,7 @@ Splitter::~Splitter() {
   if (stream_) cudaStreamSynchronize(stream_);
   for (auto& f : flushes_) {
     if (f.d_out) cudaFree(f.d_out);
+    PinnedRelease(f.h_block);
     for (auto& e : f.ev)
       if (e) cudaEventDestroy(e);
   }
@@ -280,73 +286,67 @@ Status Splitter::EnsureStaging(size_t bytes) {
 
 Status Splitter::Split(int32_t num_rows, const int64_t* addrs, const int64_t* sizes, int32_t n) {
   if (stopped_) return Status::Error(GZ_INVALID, "split after stop");
-  Status st = Cuda(cudaSetDevice(device_), "cudaSetDevice");
-  if (!st.ok()) return st;
   if (n < n_bufs_expected_) return Status::Error(GZ_INVALID, "insufficient number of in_buf_addrs");
   if (num_rows < 0) return Status::Error(GZ_INVALID, "negative num_rows");
   if (num_rows == 0) return Status::OK();  // an empty batch changes no splitter state
-  last_batch_rows_ = (uint32_t)num_rows;
+  Status st = Cuda(cudaSetDevice(device_), "cudaSetDevice");
+  if (!st.ok()) return st;
   const bool host_in = opts_.input_kind == GZ_INPUT_HOST;
   const uint32_t nr = (uint32_t)num_rows;
+  const size_t C = fields_.size();
 
   // validate and size every buffer that is read
-  struct Need {
-    const uint8_t* src;
-    size_t bytes;
-  };
-  std::vector<Need> need(n_bufs_expected_, Need{nullptr, 0});
-  std::vector<const int32_t*> host_off(n_str_, nullptr);
-  PendingBatch pb;
-  pb.nrows = nr;
-  pb.validity_mask = 0;
-  pb.char_bytes.assign(n_str_, 0);
-  pb.cols.assign(fields_.size(), ColPtr{nullptr, nullptr, nullptr, 0});
+  uint64_t validity_mask = 0;
   size_t batch_bytes = 0;
-  for (size_t f = 0; f < fields_.size(); f++) {
+  for (int k = 0; k < n_str_; k++) host_off_[k] = nullptr;
+  for (size_t f = 0; f < C; f++) {
+    const int b0 = field_buf0_[f];
+    need_[b0] = Need{nullptr, 0};
+    need_[b0 + 1] = Need{nullptr, 0};
     const int a = field_array_[f];
     if (a < 0) continue;  // null type: buffers ignored
     const int t = fields_[f].type;
-    const int b0 = field_buf0_[f];
-    // validity
     if (addrs[b0] != 0 && sizes[b0] > 0) {
       const size_t vb = (size_t)BytesForBits(nr);
       if ((size_t)sizes[b0] < vb) return Status::Error(GZ_INVALID, "validity buffer too small");
-      need[b0] = Need{reinterpret_cast<const uint8_t*>(addrs[b0]), vb};
-      pb.validity_mask |= 1ull << a;
+      need_[b0] = Need{reinterpret_cast<const uint8_t*>(addrs[b0]), vb};
+      validity_mask |= 1ull << a;
     }
-    const int vi = IsBinary(t) ? b0 + 2 : b0 + 1;
     if (IsBinary(t)) {
+      const int vi = b0 + 2;
+      need_[vi] = Need{nullptr, 0};
       const size_t ob = (size_t)(nr + 1) * 4;
       if (addrs[b0 + 1] == 0 || (size_t)sizes[b0 + 1] < ob)
         return Status::Error(GZ_INVALID, "offsets buffer too small");
-      need[b0 + 1] = Need{reinterpret_cast<const uint8_t*>(addrs[b0 + 1]), ob};
+      need_[b0 + 1] = Need{reinterpret_cast<const uint8_t*>(addrs[b0 + 1]), ob};
+      const int k = a - fixed_cnt_;
       size_t cb = (size_t)std::max<int64_t>(sizes[vi], 0);
       if (host_in) {
         const int32_t* off = reinterpret_cast<const int32_t*>(addrs[b0 + 1]);
-        host_off[a - fixed_cnt_] = off;
+        host_off_[k] = off;
         if (off[nr] < off[0] || off[0] < 0 || (int64_t)off[nr] > sizes[vi])
           return Status::Error(GZ_INVALID, "offsets exceed the value buffer");
         cb = (size_t)off[nr];
-        pb.char_bytes[a - fixed_cnt_] = (uint64_t)(off[nr] - off[0]);
+        char_scratch_[k] = (uint64_t)(off[nr] - off[0]);
       } else {
-        pb.char_bytes[a - fixed_cnt_] = (uint64_t)cb;
+        char_scratch_[k] = (uint64_t)cb;
       }
-      if (cb > 0) need[vi] = Need{reinterpret_cast<const uint8_t*>(addrs[vi]), cb};
+      if (cb > 0) need_[vi] = Need{reinterpret_cast<const uint8_t*>(addrs[vi]), cb};
     } else {
       const size_t vbytes = t == GZ_TYPE_BOOL ? (size_t)BytesForBits(nr) : (size_t)nr * ByteWidth(t);
-      if (addrs[vi] == 0 || (size_t)sizes[vi] < vbytes)
+      if (addrs[b0 + 1] == 0 || (size_t)sizes[b0 + 1] < vbytes)
         return Status::Error(GZ_INVALID, "value buffer too small");
-      need[vi] = Need{reinterpret_cast<const uint8_t*>(addrs[vi]), vbytes};
+      need_[b0 + 1] = Need{reinterpret_cast<const uint8_t*>(addrs[b0 + 1]), vbytes};
     }
   }
-  for (auto& nd : need) batch_bytes += AlignUp(nd.bytes, 64);
+  for (int i = 0; i < n_bufs_expected_; i++) batch_bytes += AlignUp(need_[i].bytes, 64);
 
   // CalculateSplitBatchSize.  Its row count depends on the empirical binary sizes only when
   // offheap_per_task > 0; those sizes are learned from the first batch with rows (where every
   // partition allocates, so the reference always computes them) and, while one is still 0,
   // from each later batch in which some partition reaches the function (splitter.cc:804-835).
-  std::vector<uint64_t> empirical_before = empirical_;
   bool probe_call = false;
+  std::vector<uint64_t> empirical_before;
   if (opts_.offheap_per_task > 0 && n_str_ > 0) {
     bool missing = false;
     for (int k = 0; k < n_str_; k++) missing |= empirical_[k] == 0;
@@ -361,36 +361,41 @@ Status Splitter::Split(int32_t num_rows, const int64_t* addrs, const int64_t* si
         if (!st.ok()) return st;
         st = Cuda(cudaMemcpy(&dev_off_[k][nr], doff + nr, 4, cudaMemcpyDeviceToHost), "read offsets");
         if (!st.ok()) return st;
-        host_off[k] = dev_off_[k].data();
+        host_off_[k] = dev_off_[k].data();
       }
     }
     probe_call = missing && seen_rows_;
+    if (probe_call) empirical_before = empirical_;
   }
   bool complete = true;
-  pb.split_size = SplitBatchSize(num_rows, host_off, &complete);
+  const uint32_t split_size = SplitBatchSize(num_rows, host_off_, &complete);
   seen_rows_ = true;
+  last_batch_rows_ = nr;
   const uint32_t ntiles = (nr + kTileRows - 1) / kTileRows;
-  pb.last_tile_rows = nr - (ntiles - 1) * kTileRows;
 
   // make room in the current flush group
-  const size_t tables_extra = sizeof(BatchDesc) + sizeof(TileDesc) * ntiles +
-                              sizeof(ColPtr) * fields_.size() + 1024;
-  auto group_tables = [&](size_t nb_, size_t nt_) {
-    return AlignUp(sizeof(BatchDesc) * nb_, 256) + AlignUp(sizeof(TileDesc) * nt_, 256) +
-           AlignUp(sizeof(ColPtr) * nb_ * fields_.size(), 256);
-  };
-  size_t cur_tiles = 0;
-  for (auto& b : pending_) cur_tiles += (b.nrows + kTileRows - 1) / kTileRows;
+  const size_t NB1 = pending_.size() + 1;
+  const size_t tables_need = AlignUp(sizeof(BatchDesc) * NB1, 256) +
+                             AlignUp(sizeof(TileDesc) * (pending_tiles_ + ntiles), 256) +
+                             AlignUp(sizeof(ColPtr) * NB1 * C, 256) + 256;
   if (!pending_.empty() &&
-      (pending_bytes_ + batch_bytes > (uint64_t)opts_.flush_bytes ||
-       pending_.size() + 1 > (size_t)kMaxBatchesPerFlush ||
-       (host_in && used_ + batch_bytes + group_tables(pending_.size() + 1, cur_tiles + ntiles) +
-                       tables_extra > stage_cap_))) {
+      (pending_bytes_ + batch_bytes > (uint64_t)opts_.flush_bytes || NB1 > (size_t)kMaxBatchesPerFlush ||
+       (host_in && used_ + batch_bytes + tables_need > stage_cap_))) {
     st = Flush();
     if (!st.ok()) return st;
   }
+  ColPtr* cols = nullptr;
+  {
+    const size_t b = pending_.size();
+    pending_cols_.resize((b + 1) * C);
+    pending_chars_.resize((b + 1) * std::max(n_str_, 1));
+    cols = &pending_cols_[b * C];
+    for (int k = 0; k < n_str_; k++) pending_chars_[b * n_str_ + k] = char_scratch_[k];
+  }
   if (host_in) {
-    st = EnsureStaging(batch_bytes + group_tables(1, ntiles) + tables_extra);
+    const size_t tables_one = AlignUp(sizeof(BatchDesc), 256) + AlignUp(sizeof(TileDesc) * ntiles, 256) +
+                              AlignUp(sizeof(ColPtr) * C, 256) + 256;
+    st = EnsureStaging(batch_bytes + tables_one);
     if (!st.ok()) return st;
     if (pending_.empty() && stage_busy_[cur_]) {
       st = Cuda(cudaEventSynchronize(stage_ev_[cur_]), "stage wait");
@@ -398,59 +403,77 @@ Status Splitter::Split(int32_t num_rows, const int64_t* addrs, const int64_t* si
       stage_busy_[cur_] = false;
     }
     // copy the batch into pinned staging; device addresses point into the device twin
-    for (size_t f = 0; f < fields_.size(); f++) {
-      const int a = field_array_[f];
-      if (a < 0) continue;
-      const int t = fields_[f].type;
-      const int b0 = field_buf0_[f];
+    jobs_.clear();
+    size_t copy_bytes = 0;
+    for (size_t f = 0; f < C; f++) {
       ColPtr cp{nullptr, nullptr, nullptr, 0};
-      const int nbuf = IsBinary(t) ? 3 : 2;
-      for (int j = 0; j < nbuf; j++) {
-        const Need& nd = need[b0 + j];
-        if (nd.bytes == 0) continue;
-        memcpy(h_stage_[cur_] + used_, nd.src, nd.bytes);
-        const uint8_t* dptr = d_stage_[cur_] + used_;
-        used_ += AlignUp(nd.bytes, 64);
-        if (j == 0) cp.validity = dptr;
-        else if (IsBinary(t) && j == 1) cp.offsets = reinterpret_cast<const int32_t*>(dptr);
-        else {
-          cp.values = dptr;
-          cp.values_bytes = nd.bytes;
+      const int a = field_array_[f];
+      if (a >= 0) {
+        const int t = fields_[f].type;
+        const int b0 = field_buf0_[f];
+        const int nbuf = IsBinary(t) ? 3 : 2;
+        for (int j = 0; j < nbuf; j++) {
+          const Need& nd = need_[b0 + j];
+          if (nd.bytes == 0) continue;
+          jobs_.push_back(CopyJob{h_stage_[cur_] + used_, nd.src, nd.bytes});
+          copy_bytes += nd.bytes;
+          const uint8_t* dptr = d_stage_[cur_] + used_;
+          used_ += AlignUp(nd.bytes, 64);
+          if (j == 0) cp.validity = dptr;
+          else if (IsBinary(t) && j == 1) cp.offsets = reinterpret_cast<const int32_t*>(dptr);
+          else {
+            cp.values = dptr;
+            cp.values_bytes = nd.bytes;
+          }
+        }
+        if (IsBinary(t) && cp.values == nullptr) cp.values = d_stage_[cur_];  // all strings empty
+      }
+      cols[f] = cp;
+    }
+    ParallelCopy(jobs_, copy_bytes);
+  } else {
+    for (size_t f = 0; f < C; f++) {
+      ColPtr cp{nullptr, nullptr, nullptr, 0};
+      const int a = field_array_[f];
+      if (a >= 0) {
+        const int t = fields_[f].type;
+        const int b0 = field_buf0_[f];
+        if (need_[b0].bytes) cp.validity = need_[b0].src;
+        if (IsBinary(t)) {
+          cp.offsets = reinterpret_cast<const int32_t*>(addrs[b0 + 1]);
+          cp.values = reinterpret_cast<const uint8_t*>(addrs[b0 + 2]);
+          cp.values_bytes = (uint64_t)std::max<int64_t>(sizes[b0 + 2], 0);
+          if (reinterpret_cast<uintptr_t>(cp.offsets) % 4)
+            return Status::Error(GZ_INVALID, "device offsets buffer must be 4-byte aligned");
+        } else {
+          cp.values = need_[b0 + 1].src;
+          const int w = t == GZ_TYPE_BOOL ? 1 : ByteWidth(t);
+          if (reinterpret_cast<uintptr_t>(cp.values) % (uintptr_t)w)
+            return Status::Error(GZ_INVALID, "device value buffer is not aligned to its width");
         }
       }
-      if (IsBinary(t) && cp.values == nullptr) cp.values = d_stage_[cur_];  // all strings empty
-      pb.cols[f] = cp;
-    }
-  } else {
-    for (size_t f = 0; f < fields_.size(); f++) {
-      const int a = field_array_[f];
-      if (a < 0) continue;
-      const int t = fields_[f].type;
-      const int b0 = field_buf0_[f];
-      ColPtr cp{nullptr, nullptr, nullptr, 0};
-      if (need[b0].bytes) cp.validity = need[b0].src;
-      if (IsBinary(t)) {
-        cp.offsets = reinterpret_cast<const int32_t*>(addrs[b0 + 1]);
-        cp.values = reinterpret_cast<const uint8_t*>(addrs[b0 + 2]);
-        cp.values_bytes = (uint64_t)std::max<int64_t>(sizes[b0 + 2], 0);
-        if (reinterpret_cast<uintptr_t>(cp.offsets) % 4)
-          return Status::Error(GZ_INVALID, "device offsets buffer must be 4-byte aligned");
-      } else {
-        cp.values = need[b0 + 1].src;
-        const int w = t == GZ_TYPE_BOOL ? 1 : ByteWidth(t);
-        if (reinterpret_cast<uintptr_t>(cp.values) % (uintptr_t)w)
-          return Status::Error(GZ_INVALID, "device value buffer is not aligned to its width");
-      }
-      pb.cols[f] = cp;
+      cols[f] = cp;
     }
   }
   if (probe_call && !pending_.empty()) {
-    // this batch has to be alone in its device pass so its call flag can be read back
+    // this batch has to be alone in its device pass so its call flag can be read back: move
+    // the earlier batches out first, keeping this batch's column record
+    std::vector<ColPtr> mine(cols, cols + C);
+    std::vector<uint64_t> mine_chars(char_scratch_.begin(), char_scratch_.end());
+    pending_cols_.resize(pending_.size() * C);
+    pending_chars_.resize(pending_.size() * std::max(n_str_, 1));
     st = Flush();
     if (!st.ok()) return st;
+    pending_cols_.assign(mine.begin(), mine.end());
+    pending_chars_.assign(std::max(n_str_, 1), 0);
+    for (int k = 0; k < n_str_; k++) pending_chars_[k] = mine_chars[k];
   }
   pending_bytes_ += batch_bytes;
-  pending_.push_back(std::move(pb));
+  pending_tiles_ += ntiles;
+  stat_input_bytes_ += (int64_t)batch_bytes;
+  stat_batches_++;
+  stat_rows_ += nr;
+  pending_.push_back(PendingBatch{nr, split_size, validity_mask});
   if (probe_call) {
     st = Flush();
     if (!st.ok()) return st;
@@ -511,6 +534,7 @@ Status Splitter::Flush() {
   uint64_t R = 0;
   uint64_t emit_bound_a = 0;
   uint32_t smin = UINT32_MAX, capmax = (uint32_t)opts_.buffer_size;
+  tiles.reserve(pending_tiles_);
   for (uint32_t b = 0; b < NB; b++) {
     const PendingBatch& pb = pending_[b];
     const uint32_t nt = (pb.nrows + kTileRows - 1) / kTileRows;
@@ -554,7 +578,7 @@ Status Splitter::Flush() {
       fr.off_values[a] = o;
       o += AlignUp((size_t)R * 4, 256);
       uint64_t cb = 0;
-      for (auto& pb : pending_) cb += pb.char_bytes[sd_.arr_str[a]];
+      for (uint32_t b = 0; b < NB; b++) cb += pending_chars_[(size_t)b * n_str_ + sd_.arr_str[a]];
       fr.off_chars[a] = o;
       o += AlignUp((size_t)cb + 16, 256);
     }
@@ -673,10 +697,10 @@ Status Splitter::Flush() {
   memcpy(htab, batches.data(), sizeof(BatchDesc) * NB);
   memcpy(htab + tb_batches, tiles.data(), sizeof(TileDesc) * T);
   ColPtr* hc = reinterpret_cast<ColPtr*>(htab + tb_batches + tb_tiles);
-  for (uint32_t b = 0; b < NB; b++)
-    for (size_t c = 0; c < C; c++) hc[b * C + c] = pending_[b].cols[c];
+  memcpy(hc, pending_cols_.data(), sizeof(ColPtr) * NB * C);
   if (host_in) {
     st = Cuda(cudaMemcpyAsync(d_stage_[cur_], h_stage_[cur_], used_, cudaMemcpyHostToDevice, stream_), "H2D");
+    stat_h2d_bytes_ += (int64_t)used_;
     if (!st.ok()) return st;
     st = Cuda(cudaEventRecord(stage_ev_[cur_], stream_), "event");
     if (!st.ok()) return st;
@@ -736,7 +760,10 @@ Status Splitter::Flush() {
   resident_bytes_ += fr.out_bytes;
   flushes_.push_back(std::move(fr));
   pending_.clear();
+  pending_cols_.clear();
+  pending_chars_.clear();
   pending_bytes_ = 0;
+  pending_tiles_ = 0;
   if (host_in) {
     cur_ ^= 1;
     used_ = 0;
@@ -753,20 +780,21 @@ Status Splitter::Flush() {
   return Status::OK();
 }
 
+// Copies a flush's outputs into a pinned host block and releases the HBM copy (both stream
+// ordered); the host bytes are valid once the stream has reached this point.
 Status Splitter::MoveFlushToHost(FlushRec& f) {
   if (f.on_host) return Status::OK();
-  const int64_t t0 = NowNs();
-  f.h_out.resize(f.out_bytes);
-  Status st = Cuda(cudaMemcpyAsync(f.h_out.data(), f.d_out, f.out_bytes, cudaMemcpyDeviceToHost, stream_), "D2H out");
+  f.h_block = PinnedAcquire(f.out_bytes);
+  if (!f.h_block.ptr) return Status::Error(GZ_OOM, "pinned host memory for partition data");
+  Status st = Cuda(cudaMemcpyAsync(f.h_block.ptr, f.d_out, f.out_bytes, cudaMemcpyDeviceToHost, stream_),
+                   "D2H out");
   if (!st.ok()) return st;
   st = Cuda(cudaFreeAsync(f.d_out, stream_), "cudaFreeAsync");
-  if (!st.ok()) return st;
-  st = Cuda(cudaStreamSynchronize(stream_), "sync");
   if (!st.ok()) return st;
   f.d_out = nullptr;
   f.on_host = true;
   resident_bytes_ -= f.out_bytes;
-  total_spill_time_ += NowNs() - t0;
+  spilled_to_host_bytes_ += f.out_bytes;
   return Status::OK();
 }
 
@@ -870,7 +898,7 @@ Status Splitter::AssembleAndWrite(int p, Segment& s, ByteSink* sink, bool count_
       }
       *all_ones = false;
       const uint64_t bit0 = (uint64_t)f.vstart(P)[p] + pc.vpos0;  // multiple of 64
-      return f.h_out.data() + off + bit0 / 8;
+      return f.h_block.ptr + off + bit0 / 8;
     }
     temps.emplace_back(nb, 0xff);
     uint8_t* dst = temps.back().data();
@@ -882,7 +910,7 @@ Status Splitter::AssembleAndWrite(int p, Segment& s, ByteSink* sink, bool count_
       const uint32_t len = pc.frow1 - pc.frow0;
       if (off != SIZE_MAX) {
         const uint64_t bit0 = (uint64_t)f.vstart(P)[p] + pc.vpos0;
-        CopyBits(f.h_out.data() + off, bit0, dst, drow, len);
+        CopyBits(f.h_block.ptr + off, bit0, dst, drow, len);
         any = true;
       }
       drow += len;
@@ -904,6 +932,12 @@ Status Splitter::AssembleAndWrite(int p, Segment& s, ByteSink* sink, bool count_
       rawb += BytesForBits(n);
       bool ones = true;
       const uint8_t* bits = gather_bits(&FlushRec::off_valid, a, &ones);
+      if (!ones && s.valid_wipe_rows > 0) {
+        temps.emplace_back(bits, bits + BytesForBits(n));
+        uint8_t* w = temps.back().data();
+        for (uint32_t r = 0; r < s.valid_wipe_rows && r < n; r++) w[r >> 3] |= (uint8_t)(1u << (r & 7));
+        bits = w;
+      }
       if (!ones) {
         nulls = CountZeros(bits, n);
         if (nulls > 0) vb.push_back(Chunk{bits, BytesForBits(n)});
@@ -916,7 +950,7 @@ Status Splitter::AssembleAndWrite(int p, Segment& s, ByteSink* sink, bool count_
       ChunkedBuffer vals;
       for (const Piece& pc : s.pieces) {
         const FlushRec& f = flushes_[pc.flush];
-        const uint8_t* base = f.h_out.data() + f.off_values[a];
+        const uint8_t* base = f.h_block.ptr + f.off_values[a];
         vals.push_back(Chunk{base + ((size_t)f.pstart(P)[p] + pc.frow0) * w,
                              (int64_t)(pc.frow1 - pc.frow0) * w});
       }
@@ -938,9 +972,9 @@ Status Splitter::AssembleAndWrite(int p, Segment& s, ByteSink* sink, bool count_
       int64_t clen = 0;
       for (const Piece& pc : s.pieces) {
         const FlushRec& f = flushes_[pc.flush];
-        const uint8_t* ob = f.h_out.data() + f.off_values[a];
+        const uint8_t* ob = f.h_block.ptr + f.off_values[a];
         offs.push_back(Chunk{ob + ((size_t)f.pstart(P)[p] + pc.frow0) * 4, (int64_t)(pc.frow1 - pc.frow0) * 4});
-        const uint8_t* cb = f.h_out.data() + f.off_chars[a];
+        const uint8_t* cb = f.h_block.ptr + f.off_chars[a];
         const uint32_t c0 = pc.fb0[k], c1 = pc.fb1[k];
         if (c1 > c0) chars.push_back(Chunk{cb + (size_t)f.cstart(P, nstr)[(size_t)k * P + p] + c0, (int64_t)(c1 - c0)});
         clen += c1 - c0;
@@ -999,10 +1033,14 @@ Status Splitter::Stop() {
     }
     open = Segment();
   }
+  const int64_t m0 = NowNs();
   for (auto& f : flushes_) {
     st = MoveFlushToHost(f);
     if (!st.ok()) return st;
   }
+  st = Cuda(cudaStreamSynchronize(stream_), "D2H partition data");
+  if (!st.ok()) return st;
+  total_spill_time_ += NowNs() - m0;
   // write the data file, partitions in order (Stop, splitter.cc:395-437)
   const int64_t t0 = NowNs();
   std::unique_ptr<ByteSink> sink;
@@ -1044,10 +1082,15 @@ Status Splitter::Stop() {
     data_bytes_ = std::move(static_cast<MemorySink*>(sink.get())->buffer());
   }
   total_compress_time_ += compress_ns;
+  stat_emitted_ = 0;
+  for (auto& v : segments_) stat_emitted_ += (int64_t)v.size();
   total_write_time_ += NowNs() - t0 - compress_ns;
   stopped_ = true;
-  // release device memory early
-  for (auto& f : flushes_) f.h_out.clear();
+  // the pinned copies are no longer needed
+  for (auto& f : flushes_) {
+    PinnedRelease(f.h_block);
+    f.h_block = PinnedBlock{};
+  }
   return Status::OK();
 }
 
@@ -1065,6 +1108,8 @@ Status Splitter::SpillFixedSize(int64_t size, int64_t* actual) {
     st = MoveFlushToHost(f);
     if (!st.ok()) return st;
   }
+  st = Cuda(cudaStreamSynchronize(stream_), "D2H partition data");
+  if (!st.ok()) return st;
   // SpillLargestPartition up to 5 times (splitter.cc:741-799): largest cached body bytes
   int64_t cur = 0;
   int tries = 0;
@@ -1090,6 +1135,10 @@ Status Splitter::SpillFixedSize(int64_t size, int64_t* actual) {
     }
     if (pick < 0) break;
     for (Segment& s : segments_[pick]) s.spilled = true;
+    // SpillPartition also refills the validity of the open buffers, pending rows included
+    uint32_t open_rows = 0;
+    for (const Piece& pc : open_[pick].pieces) open_rows += pc.frow1 - pc.frow0;
+    open_[pick].valid_wipe_rows = std::max(open_[pick].valid_wipe_rows, open_rows);
     cur += best;
   }
   *actual = cur;
@@ -1144,6 +1193,25 @@ Status Splitter::LastPids(uint16_t* out, int32_t n) {
   const uint16_t* pids = reinterpret_cast<const uint16_t*>(d_scratch_);
   return Cuda(cudaMemcpy(out, pids + (f.n_rows - (uint32_t)n), 2 * (size_t)n, cudaMemcpyDeviceToHost),
               "D2H pids");
+}
+
+void Splitter::Stats(int64_t* o) const {
+  o[0] = (int64_t)flushes_.size();
+  o[1] = stat_input_bytes_;
+  o[2] = stat_h2d_bytes_;
+  o[3] = (int64_t)spilled_to_host_bytes_;
+  o[4] = (int64_t)resident_bytes_;
+  o[5] = stat_batches_;
+  o[6] = stat_rows_;
+  o[7] = stat_emitted_;
+}
+
+Status Splitter::Sync() {
+  Status st = Cuda(cudaSetDevice(device_), "cudaSetDevice");
+  if (!st.ok()) return st;
+  st = Flush();
+  if (!st.ok()) return st;
+  return SyncAndCheck();
 }
 
 Status Splitter::KernelTimes(double* out4) {

@@ -19,6 +19,7 @@
 
 #include "../../include/gz_split.h"
 #include "gz_engine.cuh"
+#include "host_util.h"
 #include "ipc.h"
 #include "schema_ipc.h"
 
@@ -52,6 +53,9 @@ class Splitter {
   Status SetCompressType(int32_t codec);
   Status LastPids(uint16_t* out, int32_t n);
   Status KernelTimes(double* out4);
+  // Runs the pending device pass and waits for all device work of the batches split so far.
+  Status Sync();
+  void Stats(int64_t* out8) const;
 
   int64_t TotalBytesWritten() const { return total_bytes_written_; }
   int64_t TotalBytesSpilled() const { return total_bytes_spilled_; }
@@ -68,10 +72,11 @@ class Splitter {
   struct PendingBatch {
     uint32_t nrows;
     uint32_t split_size;
-    uint32_t last_tile_rows;
-    std::vector<ColPtr> cols;          // device addresses, one per schema field
-    uint64_t validity_mask;            // array columns with a validity buffer
-    std::vector<uint64_t> char_bytes;  // per binary column: bytes the output may need
+    uint64_t validity_mask;  // array columns with a validity buffer
+  };
+  struct Need {
+    const uint8_t* src;
+    size_t bytes;
   };
 
   // One device pass and what Stop needs from it.
@@ -80,7 +85,7 @@ class Splitter {
     uint32_t n_batches = 0;
     uint8_t* d_out = nullptr;           // device outputs (nullptr once moved to host)
     size_t out_bytes = 0;
-    std::vector<uint8_t> h_out;         // host copy of the outputs
+    PinnedBlock h_block;                // pinned host copy of the outputs
     bool on_host = false;
     std::vector<size_t> off_values, off_bits, off_valid, off_chars;  // per array column, SIZE_MAX: none
     uint32_t* h_meta = nullptr;         // pinned: rows_f, pstart, vstart, bytes_f, cstart, count, emit
@@ -110,6 +115,9 @@ class Splitter {
     bool spilled = false;
     int64_t body_length = -1;
     int64_t message_bytes = -1;
+    // rows [0, valid_wipe_rows) read as valid in every column: SpillPartition refills the
+    // validity buffers of the partition's open buffers with 0xff (splitter.cc:765-773)
+    uint32_t valid_wipe_rows = 0;
     std::vector<Piece> pieces;
   };
 
@@ -175,7 +183,17 @@ class Splitter {
   bool seen_rows_ = false;
 
   std::vector<PendingBatch> pending_;
+  std::vector<ColPtr> pending_cols_;      // [batch][field]
+  std::vector<uint64_t> pending_chars_;   // [batch][binary column] bytes the output may need
   uint64_t pending_bytes_ = 0;
+  size_t pending_tiles_ = 0;
+  std::vector<Need> need_;                // per-call scratch
+  std::vector<const int32_t*> host_off_;
+  std::vector<uint64_t> char_scratch_;
+  std::vector<CopyJob> jobs_;
+  size_t spilled_to_host_bytes_ = 0;
+  int64_t stat_input_bytes_ = 0, stat_h2d_bytes_ = 0, stat_batches_ = 0, stat_rows_ = 0;
+  int64_t stat_emitted_ = -1;
   std::vector<FlushRec> flushes_;
   size_t processed_flushes_ = 0;
   size_t resident_bytes_ = 0;

@@ -100,6 +100,11 @@ def lib() -> ctypes.CDLL:
         L.gz_split_split.restype = ctypes.c_int
         L.gz_split_split.argtypes = [ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
                                      ctypes.c_int32, ctypes.c_int32, c_i64p]
+        L.gz_split_split_batches.restype = ctypes.c_int
+        L.gz_split_split_batches.argtypes = [ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p,
+                                             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]
+        L.gz_split_sync.restype = ctypes.c_int
+        L.gz_split_sync.argtypes = [ctypes.c_int64]
         L.gz_split_stop.restype = ctypes.c_int
         L.gz_split_stop.argtypes = [ctypes.c_int64, ctypes.POINTER(GzSplitResult)]
         L.gz_split_data.restype = ctypes.c_int
@@ -114,6 +119,8 @@ def lib() -> ctypes.CDLL:
         L.gz_split_last_pids.argtypes = [ctypes.c_int64, ctypes.c_void_p, ctypes.c_int32]
         L.gz_last_error.restype = ctypes.c_int
         L.gz_last_error.argtypes = [ctypes.c_int64, ctypes.c_char_p, ctypes.c_size_t]
+        L.gz_split_stats.restype = ctypes.c_int
+        L.gz_split_stats.argtypes = [ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
         L.gz_split_kernel_times.restype = ctypes.c_int
         L.gz_split_kernel_times.argtypes = [ctypes.c_int64, ctypes.POINTER(ctypes.c_double)]
         _lib = L
@@ -253,6 +260,26 @@ class ShuffleSplitterJniWrapper:
         out = np.zeros(numRows, np.uint16)
         _check(lib().gz_split_last_pids(splitterId, out.ctypes.data, numRows), splitterId)
         return out
+
+    def splitBatches(self, splitterId: int, rows, bufAddrs, bufSizes) -> None:
+        """Split many batches in one call: rows[i], bufAddrs[i, :], bufSizes[i, :]."""
+        rows = np.ascontiguousarray(rows, dtype=np.int32)
+        addrs = np.ascontiguousarray(bufAddrs, dtype=np.int64)
+        sizes = np.ascontiguousarray(bufSizes, dtype=np.int64)
+        assert addrs.shape == sizes.shape and addrs.shape[0] == rows.shape[0]
+        _check(lib().gz_split_split_batches(splitterId, len(rows), rows.ctypes.data,
+                                            addrs.ctypes.data, sizes.ctypes.data, addrs.shape[1]),
+               splitterId)
+
+    def sync(self, splitterId: int) -> None:
+        _check(lib().gz_split_sync(splitterId), splitterId)
+
+    def stats(self, splitterId: int) -> List[int]:
+        """[passes, input bytes, H2D bytes, D2H bytes, HBM-resident bytes, batches, rows,
+        emitted record batches]."""
+        out = (ctypes.c_int64 * 8)()
+        _check(lib().gz_split_stats(splitterId, out), splitterId)
+        return list(out)
 
     def kernelTimes(self, splitterId: int) -> List[float]:
         out = (ctypes.c_double * 4)()

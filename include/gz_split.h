@@ -126,6 +126,17 @@ GzStatus gz_split_split(int64_t handle, int32_t num_rows, const int64_t* buf_add
                         const int64_t* buf_sizes, int32_t n_bufs, int32_t first_batch,
                         int64_t* out_compressed_size);
 
+/* Calls gz_split_split(handle, rows[i], addrs + i * n_bufs, sizes + i * n_bufs, n_bufs, 0,
+ * NULL) for i = 0 .. n_batches-1 (the writer's per-batch loop, ColumnarShuffleWriter.scala:131-185,
+ * run inside the library); stops at the first error.  No reference counterpart. */
+GzStatus gz_split_split_batches(int64_t handle, int32_t n_batches, const int32_t* rows,
+                                const int64_t* buf_addrs, const int64_t* buf_sizes, int32_t n_bufs);
+
+/* Runs the device pass over the batches gathered so far and waits for all device work of
+ * this handle: afterwards every split batch is in its partition buffers, as after a
+ * reference Split call returns.  No reference counterpart (reference Split is synchronous). */
+GzStatus gz_split_sync(int64_t handle);
+
 /* Replaces ShuffleSplitterJniWrapper.stop (jni_wrapper.cc:1197-1227): emits every pending
  * partition buffer, writes the data file (or keeps it in memory) and fills `out`. */
 GzStatus gz_split_stop(int64_t handle, GzSplitResult* out);
@@ -155,6 +166,12 @@ GzStatus gz_last_error(int64_t handle, char* buf, size_t len);
 /* Device time (ms, CUDA events on the splitter's stream) spent in each kernel family since
  * make: [hash+count, plan+scan, scatter, total device].  Test / bench hook. */
 GzStatus gz_split_kernel_times(int64_t handle, double* out4);
+
+/* Counters of this handle: [0] device passes, [1] input bytes gathered, [2] bytes copied
+ * host-to-device, [3] partition bytes copied device-to-host, [4] partition bytes resident in
+ * HBM, [5] batches split, [6] rows split, [7] emitted record batches (after Stop, else -1).
+ * No reference counterpart. */
+GzStatus gz_split_stats(int64_t handle, int64_t* out8);
 
 /* ---- test hooks (no reference counterpart; used by the unit tests) ------------------- */
 
