@@ -107,6 +107,8 @@ struct FlushDesc {
   uint32_t emit_cap;
   uint32_t pad1;
   uint32_t* call_flags;  // [n_batches] 1 when some partition ran CalculateSplitBatchSize
+  uint32_t* rec_idx;     // [n_batches][P] 1 + emission record index when a segment was cut
+  unsigned long long* ihn_out;  // [1] input_has_null_ after the flush
 
   // outputs of this flush, indexed by array column
   uint8_t* out_values[kMaxCols];   // fixed: n_rows * width; binary: n_rows int32 end offsets

@@ -226,19 +226,27 @@ __global__ void __launch_bounds__(256) k_hash_count(const SchemaDesc sd, const F
 }
 
 // =======================================================================================
-// k_plan: one CTA.  Each thread walks its partitions over the flush's batches in order.
+// The plan: three kernels.
+//   k_plan_rows  : one thread per partition walks the flush's batches in order, restating the
+//                  reference's per-pid buffer policy on row counts only; writes the flush-local
+//                  row / validity-bit offsets of every (tile, partition) and the emission
+//                  records, and marks in rec_idx[batch][p] where a segment was cut.
+//   k_plan_bytes : one thread per (binary column, partition): flush-local and in-segment byte
+//                  offsets, resetting at the cuts k_plan_rows marked.
+//   k_plan_scan  : exclusive scans over partitions -> output region starts.
+// Counts are read ahead in groups of kAhead batches so that the serial walk is not a chain of
+// dependent memory loads.
 constexpr int kMaxStrPlan = 32;
+constexpr int kPlanRowsThreads = 128;
+constexpr int kAhead = 8;
 
-__global__ void __launch_bounds__(kPlanThreads) k_plan(const SchemaDesc sd, const FlushDesc fd) {
+__global__ void __launch_bounds__(kPlanRowsThreads) k_plan_rows(const SchemaDesc sd, const FlushDesc fd) {
   extern __shared__ unsigned long long psm[];
-  __shared__ uint32_t scan_scratch[33];
   const int NB = fd.n_batches;
   const int P = sd.P;
   const int A = sd.n_array;
-  const int nstr = sd.n_str;
   unsigned long long* hn = psm;
   unsigned long long* ihn = psm + NB;
-
   for (int b = threadIdx.x; b < NB; b += blockDim.x) {
     unsigned long long m = 0;
     for (int a = 0; a < A; a++)
@@ -253,96 +261,139 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan(const SchemaDesc sd, cons
       m |= hn[b] & sd.quirk_mask;
       ihn[b] = m;
     }
-    *fd.st_ihn = m;
+    if (blockIdx.x == 0) *fd.ihn_out = m;  // k_plan_scan stores it once everyone has read
   }
   __syncthreads();
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
 
-  const int rec_words = kEmitFixedWords + nstr;
-  for (int p = threadIdx.x; p < P; p += blockDim.x) {
-    uint32_t cap = fd.st_cap[p];
-    uint32_t base = fd.st_base[p];
-    unsigned long long hv = fd.st_hv[p];
-    uint32_t sb[kMaxStrPlan], fb[kMaxStrPlan];
-    for (int k = 0; k < nstr; k++) {
-      sb[k] = fd.st_sb[(size_t)k * P + p];
-      fb[k] = 0;
+  uint32_t cap = fd.st_cap[p];
+  uint32_t base = fd.st_base[p];
+  unsigned long long hv = fd.st_hv[p];
+  uint32_t frow = 0, vpos = 0, piece_rows = 0;
+  const int rec_words = kEmitFixedWords + sd.n_str;
+  for (int b0 = 0; b0 < NB; b0 += kAhead) {
+    uint32_t c1[kAhead];
+#pragma unroll
+    for (int i = 0; i < kAhead; i++) {
+      const int b = b0 + i;
+      c1[i] = b < NB ? fd.cnt[(size_t)fd.batches[b].tile0 * P + p] : 0u;
     }
-    uint32_t frow = 0, vpos = 0, piece_rows = 0;
-    for (int b = 0; b < NB; b++) {
+#pragma unroll
+    for (int i = 0; i < kAhead; i++) {
+      const int b = b0 + i;
+      if (b >= NB) break;
       const BatchDesc bd = fd.batches[b];
-      uint32_t c = 0;
-      for (uint32_t t = bd.tile0; t < bd.tile0 + bd.ntiles; t++) c += fd.cnt[(size_t)t * P + p];
-      if (c == 0) continue;  // no tile of this batch reads (t, p)
-      const uint32_t S = bd.split_size;
-      if (cap == 0 || base + c > cap) fd.call_flags[b] = 1u;
-      if (cap == 0) {
-        // first allocation: AllocatePartitionBuffers(max(S, cnt))
-        cap = max(S, c);
-        hv = ihn[b];
-      } else if (base + c > cap) {
-        const uint32_t ns = max(S, c);
-        if (base > 0) {
-          // CacheRecordBatch: the pending rows become one record batch
-          const uint32_t idx = atomicAdd(fd.emit_count, 1u);
-          if (idx < fd.emit_cap) {
-            uint32_t* rec = fd.emit + (size_t)idx * rec_words;
-            rec[0] = (uint32_t)p;
-            rec[1] = frow;
-            rec[2] = base;
-            rec[3] = (uint32_t)hv;
-            rec[4] = (uint32_t)(hv >> 32);
-            for (int k = 0; k < nstr; k++) rec[kEmitFixedWords + k] = fb[k];
-          } else {
-            atomicOr(fd.err, kErrEmitOverflow);
-          }
-          if (piece_rows) vpos = (vpos + 63u) & ~63u;
-          piece_rows = 0;
-          base = 0;
-          for (int k = 0; k < nstr; k++) sb[k] = 0;
-        }
-        if (!sd.prefer_spill || ns > cap) {
-          // buffers reset and reallocated: validity presence restarts from input_has_null_
+      uint32_t c = c1[i];
+      for (uint32_t t = bd.tile0 + 1; t < bd.tile0 + bd.ntiles; t++) c += fd.cnt[(size_t)t * P + p];
+      uint32_t rec = 0;
+      if (c > 0) {
+        const uint32_t S = bd.split_size;
+        if (cap == 0 || base + c > cap) fd.call_flags[b] = 1u;
+        if (cap == 0) {
+          // first allocation: AllocatePartitionBuffers(max(S, cnt))
+          cap = max(S, c);
           hv = ihn[b];
-          cap = ns;
+        } else if (base + c > cap) {
+          const uint32_t ns = max(S, c);
+          if (base > 0) {
+            // CacheRecordBatch: the pending rows become one record batch
+            const uint32_t idx = atomicAdd(fd.emit_count, 1u);
+            if (idx < fd.emit_cap) {
+              uint32_t* r = fd.emit + (size_t)idx * rec_words;
+              r[0] = (uint32_t)p;
+              r[1] = frow;
+              r[2] = base;
+              r[3] = (uint32_t)hv;
+              r[4] = (uint32_t)(hv >> 32);
+              rec = idx + 1;
+            } else {
+              atomicOr(fd.err, kErrEmitOverflow);
+            }
+            if (piece_rows) vpos = (vpos + 63u) & ~63u;
+            piece_rows = 0;
+            base = 0;
+          }
+          if (!sd.prefer_spill || ns > cap) {
+            // buffers reset and reallocated: validity presence restarts from input_has_null_
+            hv = ihn[b];
+            cap = ns;
+          }
+        }
+        hv |= hn[b];  // SplitValidityBuffer allocates validity for every pid with rows
+        for (uint32_t t = bd.tile0; t < bd.tile0 + bd.ntiles; t++) {
+          const size_t ti = (size_t)t * P + p;
+          const uint32_t ct = t == bd.tile0 ? c1[i] : fd.cnt[ti];
+          fd.cnt[ti] = frow;
+          fd.vpos[ti] = vpos;
+          frow += ct;
+          vpos += ct;
+          piece_rows += ct;
+          base += ct;
         }
       }
-      hv |= hn[b];  // SplitValidityBuffer allocates validity for every pid with rows
-      for (uint32_t t = bd.tile0; t < bd.tile0 + bd.ntiles; t++) {
-        const size_t ti = (size_t)t * P + p;
-        const uint32_t ct = fd.cnt[ti];
-        fd.cnt[ti] = frow;
-        fd.vpos[ti] = vpos;
-        frow += ct;
-        vpos += ct;
-        piece_rows += ct;
-        base += ct;
-        for (int k = 0; k < nstr; k++) {
-          const size_t ix = ((size_t)t * nstr + k) * P + p;
-          const uint32_t bc = fd.bcnt[ix];
-          fd.bcnt[ix] = fb[k];
-          fd.sbyte[ix] = sb[k];
-          fb[k] += bc;
-          sb[k] += bc;
-        }
-      }
+      fd.rec_idx[(size_t)b * P + p] = rec;
     }
-    fd.st_cap[p] = cap;
-    fd.st_base[p] = base;
-    fd.st_hv[p] = hv;
-    for (int k = 0; k < nstr; k++) {
-      fd.st_sb[(size_t)k * P + p] = sb[k];
-      fd.bytes_f[(size_t)k * P + p] = fb[k];
-      fd.cstart[(size_t)k * P + p] = fb[k];
-    }
-    fd.rows_f[p] = frow;
-    fd.vbits_f[p] = (vpos + 63u) & ~63u;
-    fd.pstart[p] = frow;
-    fd.vstart[p] = (vpos + 63u) & ~63u;
   }
-  __syncthreads();
+  fd.st_cap[p] = cap;
+  fd.st_base[p] = base;
+  fd.st_hv[p] = hv;
+  fd.rows_f[p] = frow;
+  fd.vbits_f[p] = (vpos + 63u) & ~63u;
+  fd.pstart[p] = frow;
+  fd.vstart[p] = (vpos + 63u) & ~63u;
+}
+
+__global__ void __launch_bounds__(kPlanRowsThreads) k_plan_bytes(const SchemaDesc sd, const FlushDesc fd) {
+  const int P = sd.P;
+  const int nstr = sd.n_str;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= nstr * P) return;
+  const int k = idx / P, p = idx % P;
+  const int T = fd.n_tiles;
+  const int rec_words = kEmitFixedWords + nstr;
+  uint32_t sb = fd.st_sb[(size_t)k * P + p];
+  uint32_t fb = 0;
+  for (int t0 = 0; t0 < T; t0 += kAhead) {
+    uint32_t bc[kAhead], rec[kAhead];
+#pragma unroll
+    for (int i = 0; i < kAhead; i++) {
+      const int t = t0 + i;
+      bc[i] = 0;
+      rec[i] = 0;
+      if (t < T) {
+        const TileDesc td = fd.tiles[t];
+        bc[i] = fd.bcnt[((size_t)t * nstr + k) * P + p];
+        if (td.row0 == 0) rec[i] = fd.rec_idx[(size_t)td.batch * P + p];
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < kAhead; i++) {
+      const int t = t0 + i;
+      if (t >= T) break;
+      if (rec[i]) {
+        fd.emit[(size_t)(rec[i] - 1) * rec_words + kEmitFixedWords + k] = fb;
+        sb = 0;
+      }
+      const size_t ix = ((size_t)t * nstr + k) * P + p;
+      fd.bcnt[ix] = fb;
+      fd.sbyte[ix] = sb;
+      fb += bc[i];
+      sb += bc[i];
+    }
+  }
+  fd.st_sb[(size_t)k * P + p] = sb;
+  fd.bytes_f[(size_t)k * P + p] = fb;
+  fd.cstart[(size_t)k * P + p] = fb;
+}
+
+__global__ void __launch_bounds__(kPlanThreads) k_plan_scan(const SchemaDesc sd, const FlushDesc fd) {
+  __shared__ uint32_t scan_scratch[33];
+  const int P = sd.P;
   block_exscan<kPlanThreads>(fd.pstart, P, scan_scratch);
   block_exscan<kPlanThreads>(fd.vstart, P, scan_scratch);
-  for (int k = 0; k < nstr; k++) block_exscan<kPlanThreads>(fd.cstart + (size_t)k * P, P, scan_scratch);
+  for (int k = 0; k < sd.n_str; k++) block_exscan<kPlanThreads>(fd.cstart + (size_t)k * P, P, scan_scratch);
+  if (threadIdx.x == 0) *fd.st_ihn = *fd.ihn_out;
 }
 
 // =======================================================================================
@@ -562,10 +613,19 @@ cudaError_t launch_hash_count(const SchemaDesc& sd, const FlushDesc& fd, cudaStr
 cudaError_t launch_plan(const SchemaDesc& sd, const FlushDesc& fd, cudaStream_t st) {
   const size_t sm = sizeof(unsigned long long) * 2 * fd.n_batches;
   if (sm > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(k_plan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaError_t e = cudaFuncSetAttribute(k_plan_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
   }
-  k_plan<<<1, kPlanThreads, sm, st>>>(sd, fd);
+  k_plan_rows<<<(sd.P + kPlanRowsThreads - 1) / kPlanRowsThreads, kPlanRowsThreads, sm, st>>>(sd, fd);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  if (sd.n_str > 0) {
+    const int n = sd.n_str * sd.P;
+    k_plan_bytes<<<(n + kPlanRowsThreads - 1) / kPlanRowsThreads, kPlanRowsThreads, 0, st>>>(sd, fd);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  k_plan_scan<<<1, kPlanThreads, 0, st>>>(sd, fd);
   return cudaGetLastError();
 }
 

@@ -619,6 +619,8 @@ Status Splitter::Flush() {
   const size_t s_sbyte = take(TP * nstr * 4 + 4);
   const size_t s_null = take((size_t)NB * A * 4);
   const size_t s_call = take((size_t)NB * 4);
+  const size_t s_rec = take((size_t)NB * P * 4);
+  const size_t s_ihn = take(8);
   const size_t s_vbits = take((size_t)P * 4);
   const size_t meta_words = (3 + 2 * (size_t)nstr) * P + 1 + (size_t)emit_cap * (kEmitFixedWords + nstr);
   const size_t s_meta = take(meta_words * 4);  // rows_f, pstart, vstart, bytes_f, cstart, count, emits
@@ -644,6 +646,8 @@ Status Splitter::Flush() {
   fd.sbyte = reinterpret_cast<uint32_t*>(S + s_sbyte);
   fd.nullcnt = reinterpret_cast<uint32_t*>(S + s_null);
   fd.call_flags = reinterpret_cast<uint32_t*>(S + s_call);
+  fd.rec_idx = reinterpret_cast<uint32_t*>(S + s_rec);
+  fd.ihn_out = reinterpret_cast<unsigned long long*>(S + s_ihn);
   fd.vbits_f = reinterpret_cast<uint32_t*>(S + s_vbits);
   uint32_t* meta = reinterpret_cast<uint32_t*>(S + s_meta);
   fd.rows_f = meta;
