@@ -38,6 +38,7 @@ struct SchemaDesc {
   int32_t prefer_spill;
   int32_t pad0;
   uint64_t quirk_mask;  // array columns a with array_idx_[a] < fixed_width_col_cnt_ (splitter.cc:878-886)
+  uint64_t pmod_magic;  // floor((2^64 - 1) / P) + 1, for the pmod without a divide
   int32_t key_col[kMaxKeys];
   int32_t key_kind[kMaxKeys];
   int32_t arr_col[kMaxCols];    // schema index of array column a
@@ -108,7 +109,8 @@ struct FlushDesc {
   uint32_t pad1;
   uint32_t* call_flags;  // [n_batches] 1 when some partition ran CalculateSplitBatchSize
   uint32_t* rec_idx;     // [n_batches][P] 1 + emission record index when a segment was cut
-  unsigned long long* ihn_out;  // [1] input_has_null_ after the flush
+  unsigned long long* hn;   // [n_batches] columns with nulls in the batch
+  unsigned long long* ihn;  // [n_batches] input_has_null_ after the batch
 
   // outputs of this flush, indexed by array column
   uint8_t* out_values[kMaxCols];   // fixed: n_rows * width; binary: n_rows int32 end offsets

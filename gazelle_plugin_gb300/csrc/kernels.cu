@@ -48,9 +48,18 @@ __device__ __forceinline__ int32_t hash_long(int64_t v, int32_t seed) {
   h1 = mix_h1(h1, mix_k1((uint32_t)(u >> 32)));
   return (int32_t)fmix32(h1, 8);
 }
-__device__ __forceinline__ int32_t pmod(int32_t h, int32_t p) {
-  int32_t r = h % p;
-  return r < 0 ? r + p : r;
+
+// Spark pmod(h, P) without a hardware divide: Lemire, Kaser & Kurz, "Faster remainder by
+// direct computation" (2019): a mod d = hi64((M * a) mod 2^64 * d) with M = floor(2^64-1 / d) + 1.
+__device__ __forceinline__ uint32_t fastmod_u32(uint32_t a, uint32_t d, unsigned long long M) {
+  const unsigned long long low = M * (unsigned long long)a;
+  return (uint32_t)__umul64hi(low, (unsigned long long)d);
+}
+__device__ __forceinline__ uint32_t fast_pmod(int32_t h, uint32_t P, unsigned long long M) {
+  if (P == 1) return 0;
+  if (h >= 0) return fastmod_u32((uint32_t)h, P, M);
+  const uint32_t r = fastmod_u32(0u - (uint32_t)h, P, M);
+  return r == 0 ? 0 : P - r;
 }
 
 __device__ __forceinline__ bool get_bit(const uint8_t* bits, uint32_t i) {
@@ -141,73 +150,75 @@ __device__ uint32_t block_exmax(uint32_t v, uint32_t* scratch) {
 
 // =======================================================================================
 // k_hash_count: one CTA per tile (<= kTileRows rows of one batch).
+constexpr int kMaxStrPlan = 32;
+
 __global__ void __launch_bounds__(256) k_hash_count(const SchemaDesc sd, const FlushDesc fd) {
   extern __shared__ uint32_t smem[];
+  __shared__ ColPtr s_key[kMaxKeys];
+  __shared__ int32_t s_kind[kMaxKeys];
+  __shared__ ColPtr s_str[kMaxStrPlan];
   const TileDesc tile = fd.tiles[blockIdx.x];
   const int P = sd.P;
   const int nstr = sd.n_str;
+  const int nkeys = sd.n_keys;
   const ColPtr* cols = fd.cols + (size_t)tile.batch * sd.n_cols;
+  if (threadIdx.x < nkeys) {
+    s_key[threadIdx.x] = cols[sd.key_col[threadIdx.x]];
+    s_kind[threadIdx.x] = sd.key_kind[threadIdx.x];
+  }
+  if (threadIdx.x < nstr) s_str[threadIdx.x] = cols[sd.arr_col[sd.n_fixed + threadIdx.x]];
   uint32_t* H;
   uint32_t* BH;
   if (fd.hist_in_smem) {
     H = smem;
     BH = smem + P;
     for (int i = threadIdx.x; i < P * (1 + nstr); i += blockDim.x) smem[i] = 0;
-    __syncthreads();
   } else {
     H = fd.cnt + (size_t)blockIdx.x * P;
     BH = fd.bcnt + (size_t)blockIdx.x * nstr * P;
   }
-
-  for (uint32_t base = 0; base < tile.nrows; base += blockDim.x) {
-    const uint32_t i = base + threadIdx.x;
-    const bool active = i < tile.nrows;
+  __syncthreads();
+  const unsigned long long M = sd.pmod_magic;
+  bool bad = false;
+  for (uint32_t i = threadIdx.x; i < tile.nrows; i += blockDim.x) {
     const uint32_t r = tile.row0 + i;
-    int32_t p = 0;
-    if (active) {
-      int32_t h = 42;
-      for (int k = 0; k < sd.n_keys; k++) {
-        const ColPtr c = cols[sd.key_col[k]];
-        if (c.validity != nullptr && !get_bit(c.validity, r)) continue;
-        switch (sd.key_kind[k]) {
-          case KEY_I32: h = hash_int(reinterpret_cast<const int32_t*>(c.values)[r], h); break;
-          case KEY_I64: h = hash_long(reinterpret_cast<const int64_t*>(c.values)[r], h); break;
-          case KEY_I8: h = hash_int(reinterpret_cast<const int8_t*>(c.values)[r], h); break;
-          case KEY_I16: h = hash_int(reinterpret_cast<const int16_t*>(c.values)[r], h); break;
-          default: h = hash_int(get_bit(c.values, r) ? 1 : 0, h); break;
-        }
+    int32_t h = 42;
+    for (int k = 0; k < nkeys; k++) {
+      const ColPtr c = s_key[k];
+      if (c.validity != nullptr && !get_bit(c.validity, r)) continue;  // null: seed passes
+      switch (s_kind[k]) {
+        case KEY_I32: h = hash_int(reinterpret_cast<const int32_t*>(c.values)[r], h); break;
+        case KEY_I64: h = hash_long(reinterpret_cast<const int64_t*>(c.values)[r], h); break;
+        case KEY_I8: h = hash_int(reinterpret_cast<const int8_t*>(c.values)[r], h); break;
+        case KEY_I16: h = hash_int(reinterpret_cast<const int16_t*>(c.values)[r], h); break;
+        default: h = hash_int(get_bit(c.values, r) ? 1 : 0, h); break;
       }
-      p = pmod(h, P);
-      fd.pids[tile.frow0 + i] = (uint16_t)p;
     }
-    const unsigned amask = __ballot_sync(kFull, active);
-    if (active) {
-      const unsigned peers = __match_any_sync(amask, p);
-      const bool leader = (int)lane_id() == __ffs(peers) - 1;
-      if (leader) atomicAdd(&H[p], (uint32_t)__popc(peers));
-      for (int k = 0; k < nstr; k++) {
-        const ColPtr c = cols[sd.arr_col[sd.n_fixed + k]];
-        const int32_t o0 = c.offsets[r], o1 = c.offsets[r + 1];
-        uint32_t len = (uint32_t)(o1 - o0);
-        if (o0 < 0 || o1 < o0 || (uint64_t)o1 > c.values_bytes) {
-          atomicOr(fd.err, kErrBadOffsets);  // k_scatter then copies nothing
-          len = 0;
-        }
-        const uint32_t sum = __reduce_add_sync(peers, len);
-        if (leader) atomicAdd(&BH[k * P + p], sum);
+    const uint32_t p = fast_pmod(h, (uint32_t)P, M);
+    fd.pids[tile.frow0 + i] = (uint16_t)p;
+    atomicAdd(&H[p], 1u);
+    for (int k = 0; k < nstr; k++) {
+      const ColPtr c = s_str[k];
+      const int32_t o0 = c.offsets[r], o1 = c.offsets[r + 1];
+      uint32_t len = (uint32_t)(o1 - o0);
+      if (o0 < 0 || o1 < o0 || (uint64_t)o1 > c.values_bytes) {
+        bad = true;
+        len = 0;
       }
+      if (len) atomicAdd(&BH[k * P + p], len);
     }
   }
+  if (bad) atomicOr(fd.err, kErrBadOffsets);  // k_scatter then copies nothing
 
   // null counts of this tile's slice of every column (GetNullCount of the batch = sum)
   for (int a = 0; a < sd.n_array; a++) {
-    const ColPtr c = cols[sd.arr_col[a]];
-    if (c.validity == nullptr) continue;
+    const uint8_t* validity = cols[sd.arr_col[a]].validity;
+    if (validity == nullptr) continue;
     uint32_t z = 0;
     const uint32_t nbytes = (tile.nrows + 7) >> 3;
-    const uint8_t* vb = c.validity + (tile.row0 >> 3);
+    const uint8_t* vb = validity + (tile.row0 >> 3);
     for (uint32_t j = threadIdx.x; j < nbytes; j += blockDim.x) {
-      uint32_t byte = vb[j];
+      const uint32_t byte = vb[j];
       const uint32_t rem = tile.nrows - j * 8;
       const uint32_t mask = rem >= 8 ? 0xffu : ((1u << rem) - 1);
       z += __popc(~byte & mask);
@@ -226,165 +237,240 @@ __global__ void __launch_bounds__(256) k_hash_count(const SchemaDesc sd, const F
 }
 
 // =======================================================================================
-// The plan: three kernels.
-//   k_plan_rows  : one thread per partition walks the flush's batches in order, restating the
-//                  reference's per-pid buffer policy on row counts only; writes the flush-local
-//                  row / validity-bit offsets of every (tile, partition) and the emission
-//                  records, and marks in rec_idx[batch][p] where a segment was cut.
-//   k_plan_bytes : one thread per (binary column, partition): flush-local and in-segment byte
-//                  offsets, resetting at the cuts k_plan_rows marked.
+// The plan: four small kernels between k_hash_count and k_scatter.
+//   k_plan_prep  : per batch, which columns have nulls (hn) and input_has_null_ after the batch
+//                  (ihn, sticky, quirk columns only, splitter.cc:878-886).
+//   k_plan_rows  : one warp per partition restates the reference's per-pid buffer policy over
+//                  the flush's batches, 32 batches per step: a warp scan of the row counts, then
+//                  only the batches where the policy acts (allocation or a cut) are visited one
+//                  by one, found with a ballot on "rows so far + count > capacity".  Writes the
+//                  flush-local row / validity-bit offsets of every (tile, partition), the
+//                  emission records, and marks cuts in rec_idx[batch][p].
+//   k_plan_bytes : one warp per (binary column, partition): flush-local and in-segment byte
+//                  offsets by warp scans, restarting at the cuts.
 //   k_plan_scan  : exclusive scans over partitions -> output region starts.
-// Counts are read ahead in groups of kAhead batches so that the serial walk is not a chain of
-// dependent memory loads.
-constexpr int kMaxStrPlan = 32;
 constexpr int kPlanRowsThreads = 128;
-constexpr int kAhead = 8;
 
-__global__ void __launch_bounds__(kPlanRowsThreads) k_plan_rows(const SchemaDesc sd, const FlushDesc fd) {
-  extern __shared__ unsigned long long psm[];
+__device__ __forceinline__ uint32_t warp_incl_sum(uint32_t x) {
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(kFull, x, o);
+    if ((int)lane_id() >= o) x += y;
+  }
+  return x;
+}
+__device__ __forceinline__ unsigned long long warp_or64(unsigned long long v) {
+  const uint32_t lo = __reduce_or_sync(kFull, (uint32_t)v);
+  const uint32_t hi = __reduce_or_sync(kFull, (uint32_t)(v >> 32));
+  return ((unsigned long long)hi << 32) | lo;
+}
+__device__ __forceinline__ unsigned long long shfl64(unsigned long long v, int src) {
+  return __shfl_sync(kFull, v, src);
+}
+
+__global__ void __launch_bounds__(kPlanThreads) k_plan_prep(const SchemaDesc sd, const FlushDesc fd) {
+  __shared__ unsigned long long s_warp[kPlanThreads / 32];
   const int NB = fd.n_batches;
-  const int P = sd.P;
   const int A = sd.n_array;
-  unsigned long long* hn = psm;
-  unsigned long long* ihn = psm + NB;
-  for (int b = threadIdx.x; b < NB; b += blockDim.x) {
+  const int per = (NB + kPlanThreads - 1) / kPlanThreads;
+  const int lo = threadIdx.x * per, hi = min(lo + per, NB);
+  unsigned long long run = 0;
+  for (int b = lo; b < hi; b++) {
     unsigned long long m = 0;
     for (int a = 0; a < A; a++)
       if (fd.nullcnt[(size_t)b * A + a]) m |= 1ull << a;
-    hn[b] = m;
+    fd.hn[b] = m;
+    run |= m & sd.quirk_mask;
+  }
+  // exclusive OR-scan of the per-thread ORs across the block
+  unsigned long long x = run;
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long y = __shfl_up_sync(kFull, x, o);
+    if ((int)lane_id() >= o) x |= y;
+  }
+  const int w = threadIdx.x >> 5;
+  if (lane_id() == 31) s_warp[w] = x;
+  __syncthreads();
+  unsigned long long before = *fd.st_ihn;
+  for (int i = 0; i < w; i++) before |= s_warp[i];
+  before |= __shfl_up_sync(kFull, x, 1) * (lane_id() ? 1ull : 0ull);
+  for (int b = lo; b < hi; b++) {
+    before |= fd.hn[b] & sd.quirk_mask;
+    fd.ihn[b] = before;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    // input_has_null_ is sticky and only set for the quirk columns (splitter.cc:878-886)
-    unsigned long long m = *fd.st_ihn;
-    for (int b = 0; b < NB; b++) {
-      m |= hn[b] & sd.quirk_mask;
-      ihn[b] = m;
-    }
-    if (blockIdx.x == 0) *fd.ihn_out = m;  // k_plan_scan stores it once everyone has read
+  if (threadIdx.x == kPlanThreads - 1) {
+    unsigned long long all = *fd.st_ihn;
+    for (int i = 0; i < kPlanThreads / 32; i++) all |= s_warp[i];
+    *fd.st_ihn = all;
   }
-  __syncthreads();
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= P) return;
+}
 
+__global__ void __launch_bounds__(kPlanRowsThreads) k_plan_rows(const SchemaDesc sd, const FlushDesc fd) {
+  const int P = sd.P;
+  const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (p >= P) return;  // whole warps exit together
+  const int lane = lane_id();
+  const int NB = fd.n_batches;
+  const int rec_words = kEmitFixedWords + sd.n_str;
   uint32_t cap = fd.st_cap[p];
   uint32_t base = fd.st_base[p];
   unsigned long long hv = fd.st_hv[p];
-  uint32_t frow = 0, vpos = 0, piece_rows = 0;
-  const int rec_words = kEmitFixedWords + sd.n_str;
-  for (int b0 = 0; b0 < NB; b0 += kAhead) {
-    uint32_t c1[kAhead];
-#pragma unroll
-    for (int i = 0; i < kAhead; i++) {
-      const int b = b0 + i;
-      c1[i] = b < NB ? fd.cnt[(size_t)fd.batches[b].tile0 * P + p] : 0u;
+  uint32_t frow = 0, vpos = 0, piece_start = 0;  // flush-local rows; piece_start = frow of the piece
+  for (int b0 = 0; b0 < NB; b0 += 32) {
+    const int b = b0 + lane;
+    const bool active = b < NB;
+    BatchDesc bd{0, 0, 0, 0};
+    uint32_t c = 0;
+    unsigned long long hn_l = 0, ihn_l = 0;
+    if (active) {
+      bd = fd.batches[b];
+      for (uint32_t t = bd.tile0; t < bd.tile0 + bd.ntiles; t++) c += fd.cnt[(size_t)t * P + p];
+      hn_l = fd.hn[b];
+      ihn_l = fd.ihn[b];
     }
-#pragma unroll
-    for (int i = 0; i < kAhead; i++) {
-      const int b = b0 + i;
-      if (b >= NB) break;
-      const BatchDesc bd = fd.batches[b];
-      uint32_t c = c1[i];
-      for (uint32_t t = bd.tile0 + 1; t < bd.tile0 + bd.ntiles; t++) c += fd.cnt[(size_t)t * P + p];
-      uint32_t rec = 0;
-      if (c > 0) {
-        const uint32_t S = bd.split_size;
-        if (cap == 0 || base + c > cap) fd.call_flags[b] = 1u;
-        if (cap == 0) {
-          // first allocation: AllocatePartitionBuffers(max(S, cnt))
-          cap = max(S, c);
-          hv = ihn[b];
-        } else if (base + c > cap) {
-          const uint32_t ns = max(S, c);
-          if (base > 0) {
-            // CacheRecordBatch: the pending rows become one record batch
-            const uint32_t idx = atomicAdd(fd.emit_count, 1u);
-            if (idx < fd.emit_cap) {
+    const uint32_t X = warp_incl_sum(c);
+    const uint32_t Xex = X - c;
+    const uint32_t total = __shfl_sync(kFull, X, 31);
+    // events (allocation or cut) in lane order; state (cap, base_ref, hv) is warp-uniform.
+    // base before lane l's rows = base_ref + (Xex[l] - Xex[ref]).
+    int ref = 0, from = 0;
+    uint32_t base_ref = base, pad = 0, my_pad = 0, rec = 0;
+    for (;;) {
+      const uint32_t ref_x = __shfl_sync(kFull, Xex, ref);
+      const bool cond = active && lane >= from && c > 0 &&
+                        (cap == 0 || base_ref + (Xex - ref_x) + c > cap);
+      const unsigned m = __ballot_sync(kFull, cond);
+      if (m == 0) break;
+      const int e = __ffs(m) - 1;
+      // validity presence accumulated over the rows since the last event
+      hv |= warp_or64((active && lane >= from && lane < e && c > 0) ? hn_l : 0ull);
+      const uint32_t c_e = __shfl_sync(kFull, c, e);
+      const uint32_t xe = __shfl_sync(kFull, Xex, e);
+      const uint32_t S_e = __shfl_sync(kFull, bd.split_size, e);
+      const unsigned long long hn_e = shfl64(hn_l, e), ihn_e = shfl64(ihn_l, e);
+      uint32_t base_e = base_ref + (xe - ref_x);
+      if (lane == e) fd.call_flags[b] = 1u;
+      if (cap == 0) {
+        // first allocation: AllocatePartitionBuffers(max(S, cnt))
+        cap = max(S_e, c_e);
+        hv = ihn_e;
+      } else {
+        const uint32_t ns = max(S_e, c_e);
+        if (base_e > 0) {
+          // CacheRecordBatch: the pending rows become one record batch
+          uint32_t idx = 0;
+          if (lane == 0) idx = atomicAdd(fd.emit_count, 1u);
+          idx = __shfl_sync(kFull, idx, 0);
+          const uint32_t frow_e = frow + xe;
+          if (idx < fd.emit_cap) {
+            if (lane == 0) {
               uint32_t* r = fd.emit + (size_t)idx * rec_words;
               r[0] = (uint32_t)p;
-              r[1] = frow;
-              r[2] = base;
+              r[1] = frow_e;
+              r[2] = base_e;
               r[3] = (uint32_t)hv;
               r[4] = (uint32_t)(hv >> 32);
-              rec = idx + 1;
-            } else {
-              atomicOr(fd.err, kErrEmitOverflow);
             }
-            if (piece_rows) vpos = (vpos + 63u) & ~63u;
-            piece_rows = 0;
-            base = 0;
+            if (lane == e) rec = idx + 1;
+          } else if (lane == 0) {
+            atomicOr(fd.err, kErrEmitOverflow);
           }
-          if (!sd.prefer_spill || ns > cap) {
-            // buffers reset and reallocated: validity presence restarts from input_has_null_
-            hv = ihn[b];
-            cap = ns;
+          // the next piece of validity bits starts on a 64-bit boundary
+          if (frow_e > piece_start) {
+            const uint32_t v = vpos + xe + pad;
+            pad += ((v + 63u) & ~63u) - v;
           }
+          piece_start = frow_e;
+          base_e = 0;
         }
-        hv |= hn[b];  // SplitValidityBuffer allocates validity for every pid with rows
-        for (uint32_t t = bd.tile0; t < bd.tile0 + bd.ntiles; t++) {
-          const size_t ti = (size_t)t * P + p;
-          const uint32_t ct = t == bd.tile0 ? c1[i] : fd.cnt[ti];
-          fd.cnt[ti] = frow;
-          fd.vpos[ti] = vpos;
-          frow += ct;
-          vpos += ct;
-          piece_rows += ct;
-          base += ct;
+        if (!sd.prefer_spill || ns > cap) {
+          // buffers reset and reallocated: validity presence restarts from input_has_null_
+          hv = ihn_e;
+          cap = ns;
         }
       }
-      fd.rec_idx[(size_t)b * P + p] = rec;
+      hv |= hn_e;  // SplitValidityBuffer: validity for every pid with rows in the batch
+      if (lane >= e) my_pad = pad;
+      ref = e;
+      from = e + 1;
+      base_ref = base_e;
     }
+    hv |= warp_or64((active && lane >= from && c > 0) ? hn_l : 0ull);
+    if (active && c > 0) {
+      uint32_t fr = frow + Xex, vp = vpos + Xex + my_pad;
+      for (uint32_t t = bd.tile0; t < bd.tile0 + bd.ntiles; t++) {
+        const size_t ti = (size_t)t * P + p;
+        const uint32_t ct = fd.cnt[ti];
+        fd.cnt[ti] = fr;
+        fd.vpos[ti] = vp;
+        fr += ct;
+        vp += ct;
+      }
+    }
+    if (active) fd.rec_idx[(size_t)b * P + p] = rec;
+    const uint32_t ref_x = __shfl_sync(kFull, Xex, ref);
+    base = base_ref + (total - ref_x);
+    frow += total;
+    vpos += total + pad;
   }
-  fd.st_cap[p] = cap;
-  fd.st_base[p] = base;
-  fd.st_hv[p] = hv;
-  fd.rows_f[p] = frow;
-  fd.vbits_f[p] = (vpos + 63u) & ~63u;
-  fd.pstart[p] = frow;
-  fd.vstart[p] = (vpos + 63u) & ~63u;
+  if (lane == 0) {
+    fd.st_cap[p] = cap;
+    fd.st_base[p] = base;
+    fd.st_hv[p] = hv;
+    const uint32_t vb = frow > piece_start ? ((vpos + 63u) & ~63u) : vpos;
+    fd.rows_f[p] = frow;
+    fd.vbits_f[p] = vb;
+    fd.pstart[p] = frow;
+    fd.vstart[p] = vb;
+  }
 }
 
 __global__ void __launch_bounds__(kPlanRowsThreads) k_plan_bytes(const SchemaDesc sd, const FlushDesc fd) {
   const int P = sd.P;
   const int nstr = sd.n_str;
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= nstr * P) return;
-  const int k = idx / P, p = idx % P;
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (wid >= nstr * P) return;
+  const int k = wid / P, p = wid % P;
+  const int lane = lane_id();
   const int T = fd.n_tiles;
   const int rec_words = kEmitFixedWords + nstr;
   uint32_t sb = fd.st_sb[(size_t)k * P + p];
   uint32_t fb = 0;
-  for (int t0 = 0; t0 < T; t0 += kAhead) {
-    uint32_t bc[kAhead], rec[kAhead];
-#pragma unroll
-    for (int i = 0; i < kAhead; i++) {
-      const int t = t0 + i;
-      bc[i] = 0;
-      rec[i] = 0;
-      if (t < T) {
-        const TileDesc td = fd.tiles[t];
-        bc[i] = fd.bcnt[((size_t)t * nstr + k) * P + p];
-        if (td.row0 == 0) rec[i] = fd.rec_idx[(size_t)td.batch * P + p];
-      }
+  for (int t0 = 0; t0 < T; t0 += 32) {
+    const int t = t0 + lane;
+    uint32_t bc = 0, rec = 0;
+    if (t < T) {
+      const TileDesc td = fd.tiles[t];
+      bc = fd.bcnt[((size_t)t * nstr + k) * P + p];
+      if (td.row0 == 0) rec = fd.rec_idx[(size_t)td.batch * P + p];
     }
-#pragma unroll
-    for (int i = 0; i < kAhead; i++) {
-      const int t = t0 + i;
-      if (t >= T) break;
-      if (rec[i]) {
-        fd.emit[(size_t)(rec[i] - 1) * rec_words + kEmitFixedWords + k] = fb;
-        sb = 0;
-      }
+    const uint32_t X = warp_incl_sum(bc);
+    const uint32_t fb_l = fb + X - bc;
+    // the last cut at or before this tile
+    int last = rec ? lane : -1;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(kFull, last, o);
+      if (lane >= o) last = max(last, y);
+    }
+    const uint32_t fb_last = __shfl_sync(kFull, fb_l, last < 0 ? 0 : last);
+    const uint32_t sb_l = last < 0 ? sb + (fb_l - fb) : fb_l - fb_last;
+    if (t < T) {
+      if (rec) fd.emit[(size_t)(rec - 1) * rec_words + kEmitFixedWords + k] = fb_l;
       const size_t ix = ((size_t)t * nstr + k) * P + p;
-      fd.bcnt[ix] = fb;
-      fd.sbyte[ix] = sb;
-      fb += bc[i];
-      sb += bc[i];
+      fd.bcnt[ix] = fb_l;
+      fd.sbyte[ix] = sb_l;
     }
+    const uint32_t total = __shfl_sync(kFull, X, 31);
+    const int last31 = __shfl_sync(kFull, last, 31);
+    const uint32_t fb_last31 = __shfl_sync(kFull, fb_l, last31 < 0 ? 0 : last31);
+    sb = last31 < 0 ? sb + total : (fb + total) - fb_last31;
+    fb += total;
   }
-  fd.st_sb[(size_t)k * P + p] = sb;
-  fd.bytes_f[(size_t)k * P + p] = fb;
-  fd.cstart[(size_t)k * P + p] = fb;
+  if (lane == 0) {
+    fd.st_sb[(size_t)k * P + p] = sb;
+    fd.bytes_f[(size_t)k * P + p] = fb;
+    fd.cstart[(size_t)k * P + p] = fb;
+  }
 }
 
 __global__ void __launch_bounds__(kPlanThreads) k_plan_scan(const SchemaDesc sd, const FlushDesc fd) {
@@ -393,7 +479,6 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan_scan(const SchemaDesc sd,
   block_exscan<kPlanThreads>(fd.pstart, P, scan_scratch);
   block_exscan<kPlanThreads>(fd.vstart, P, scan_scratch);
   for (int k = 0; k < sd.n_str; k++) block_exscan<kPlanThreads>(fd.cstart + (size_t)k * P, P, scan_scratch);
-  if (threadIdx.x == 0) *fd.st_ihn = *fd.ihn_out;
 }
 
 // =======================================================================================
@@ -611,17 +696,16 @@ cudaError_t launch_hash_count(const SchemaDesc& sd, const FlushDesc& fd, cudaStr
 }
 
 cudaError_t launch_plan(const SchemaDesc& sd, const FlushDesc& fd, cudaStream_t st) {
-  const size_t sm = sizeof(unsigned long long) * 2 * fd.n_batches;
-  if (sm > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(k_plan_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e != cudaSuccess) return e;
-  }
-  k_plan_rows<<<(sd.P + kPlanRowsThreads - 1) / kPlanRowsThreads, kPlanRowsThreads, sm, st>>>(sd, fd);
+  k_plan_prep<<<1, kPlanThreads, 0, st>>>(sd, fd);
   cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const int wpb = kPlanRowsThreads / 32;
+  k_plan_rows<<<(sd.P + wpb - 1) / wpb, kPlanRowsThreads, 0, st>>>(sd, fd);
+  e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   if (sd.n_str > 0) {
     const int n = sd.n_str * sd.P;
-    k_plan_bytes<<<(n + kPlanRowsThreads - 1) / kPlanRowsThreads, kPlanRowsThreads, 0, st>>>(sd, fd);
+    k_plan_bytes<<<(n + wpb - 1) / wpb, kPlanRowsThreads, 0, st>>>(sd, fd);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }

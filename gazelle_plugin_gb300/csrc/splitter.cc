@@ -125,6 +125,7 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
   sd_.n_str = n_str_;
   sd_.n_keys = (int32_t)keys_.size();
   sd_.prefer_spill = opts_.prefer_spill ? 1 : 0;
+  sd_.pmod_magic = P_ > 1 ? UINT64_MAX / (uint64_t)P_ + 1 : 0;
   for (int a = 0; a < n_array_; a++) {
     const int ci = array_idx_[a];
     field_array_[ci] = a;
@@ -620,7 +621,8 @@ Status Splitter::Flush() {
   const size_t s_null = take((size_t)NB * A * 4);
   const size_t s_call = take((size_t)NB * 4);
   const size_t s_rec = take((size_t)NB * P * 4);
-  const size_t s_ihn = take(8);
+  const size_t s_hn = take((size_t)NB * 8);
+  const size_t s_ihn = take((size_t)NB * 8);
   const size_t s_vbits = take((size_t)P * 4);
   const size_t meta_words = (3 + 2 * (size_t)nstr) * P + 1 + (size_t)emit_cap * (kEmitFixedWords + nstr);
   const size_t s_meta = take(meta_words * 4);  // rows_f, pstart, vstart, bytes_f, cstart, count, emits
@@ -647,7 +649,8 @@ Status Splitter::Flush() {
   fd.nullcnt = reinterpret_cast<uint32_t*>(S + s_null);
   fd.call_flags = reinterpret_cast<uint32_t*>(S + s_call);
   fd.rec_idx = reinterpret_cast<uint32_t*>(S + s_rec);
-  fd.ihn_out = reinterpret_cast<unsigned long long*>(S + s_ihn);
+  fd.hn = reinterpret_cast<unsigned long long*>(S + s_hn);
+  fd.ihn = reinterpret_cast<unsigned long long*>(S + s_ihn);
   fd.vbits_f = reinterpret_cast<uint32_t*>(S + s_vbits);
   uint32_t* meta = reinterpret_cast<uint32_t*>(S + s_meta);
   fd.rows_f = meta;
