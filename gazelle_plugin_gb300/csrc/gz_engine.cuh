@@ -19,8 +19,8 @@ namespace gz {
 constexpr int kMaxKeys = 8;
 constexpr int kMaxCols = 64;    // array columns (fixed + bool + binary)
 constexpr int kMaxSchemaCols = 256;
-constexpr int kTileRows = 4096; // rows per k_hash_count / k_scatter CTA
-constexpr int kScatterThreads = 512;
+constexpr int kTileRows = 2048; // rows per k_hash_count / k_scatter CTA
+constexpr int kScatterThreads = 256;
 constexpr int kPlanThreads = 1024;
 constexpr int kMaxBatchesPerFlush = 4096;
 
@@ -59,6 +59,7 @@ struct ColPtr {
 // bits of FlushDesc::err
 constexpr int32_t kErrEmitOverflow = 1;
 constexpr int32_t kErrBadOffsets = 2;
+constexpr int32_t kErrTimeout = 4;  // a bounded wait in a kernel gave up
 
 struct BatchDesc {
   uint32_t nrows;

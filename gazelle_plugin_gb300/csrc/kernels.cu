@@ -483,8 +483,25 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan_scan(const SchemaDesc sd,
 
 // =======================================================================================
 // k_scatter: one CTA per tile.
+//
+//   1. stable LSD radix sort of the tile's partition ids in shared memory (8-bit digits,
+//      per-warp digit counts, one pass for P <= 256, two otherwise) -> sorted position j holds
+//      source row ps[j]; rows of one partition form a run in input order
+//   2. per sorted row: destination row (partition start + flush-local offset + rank in run)
+//      and destination validity bit
+//   3. column by column: the tile's slice of the column (values / offsets, and its validity
+//      bits) is brought into shared memory by TMA bulk copies (cp.async.bulk, completion on an
+//      mbarrier), double-buffered so the next column streams in while this one is scattered;
+//      rows are then gathered from shared memory and written in sorted order, so the stores of
+//      a run are contiguous.  Validity and bool bits are cleared with warp-merged atomicAnd on
+//      0xff-filled words.  Characters of a binary column are copied one string per lane with
+//      aligned 32-bit destination words built by funnel shifts from aligned source words.
 namespace {
 constexpr int kW = kScatterThreads / 32;
+constexpr int kStageBytes = kTileRows * 8;          // one 8-byte column slice
+constexpr int kStageValid = kTileRows / 8;           // its validity bits
+constexpr int kStageSlot = kStageBytes + 16 + kStageValid + 16;
+constexpr uint32_t kSpinLimit = 1u << 26;
 
 // One stable LSD pass over 8 bits of the keys.
 __device__ void radix_pass(const uint16_t* kin, const uint16_t* pin, uint16_t* kout,
@@ -532,23 +549,105 @@ __device__ void radix_pass(const uint16_t* kin, const uint16_t* pin, uint16_t* k
   __syncthreads();
 }
 
-template <typename T>
-__device__ __forceinline__ void copy_rows(uint8_t* out, const uint8_t* in, const uint16_t* ps,
-                                          const uint32_t* dstrow, uint32_t row0, int n) {
-  T* o = reinterpret_cast<T*>(out);
-  const T* s = reinterpret_cast<const T*>(in) + row0;
-  for (int j = threadIdx.x; j < n; j += blockDim.x) o[dstrow[j]] = s[ps[j]];
+// ---- mbarrier + bulk copy (TMA) helpers -------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+// Bounded wait for phase `parity` of `bar`; false when the limit ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (uint32_t it = 0; it < kSpinLimit; it++) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// Bytes of a staged piece that go by bulk copy: the 16-byte multiple of an aligned source.
+__device__ __forceinline__ uint32_t bulk_part(const uint8_t* src, uint32_t bytes) {
+  if (src == nullptr) return 0;
+  return ((reinterpret_cast<uintptr_t>(src) & 15) == 0) ? (bytes & ~15u) : 0u;
+}
+// Stages `bytes` of `src` at `dst`: the bulk part by TMA (completing on `bar`), the rest by
+// plain loads.  Thread 0, after the barrier expects the bulk bytes.
+__device__ __forceinline__ void stage_piece(uint8_t* dst, const uint8_t* src, uint32_t bytes,
+                                            uint64_t* bar) {
+  if (bytes == 0 || src == nullptr) return;
+  const uint32_t bulk = bulk_part(src, bytes);
+  if (bulk) bulk_g2s(dst, src, bulk, bar);
+  for (uint32_t i = bulk; i < bytes; i++) dst[i] = src[i];
+}
+
+// One string: len bytes from src to dst, aligned 32-bit stores for the body.  Source words are
+// read aligned; `src_end` bounds the bytes that may be read.
+__device__ __forceinline__ void copy_string(uint8_t* dst, const uint8_t* src, uint32_t len,
+                                            const uint8_t* src_end) {
+  uint32_t h = (4u - (uint32_t)(reinterpret_cast<uintptr_t>(dst) & 3)) & 3;
+  if (h > len) h = len;
+  for (uint32_t i = 0; i < h; i++) dst[i] = src[i];
+  dst += h;
+  src += h;
+  len -= h;
+  uint32_t nw = len >> 2;
+  if (nw) {
+    const uint32_t sh = (uint32_t)(reinterpret_cast<uintptr_t>(src) & 3);
+    const uint32_t* sa = reinterpret_cast<const uint32_t*>(src - sh);
+    uint32_t* d32 = reinterpret_cast<uint32_t*>(dst);
+    if (sh == 0) {
+      for (uint32_t w = 0; w < nw; w++) d32[w] = sa[w];
+    } else if (reinterpret_cast<const uint8_t*>(sa + nw + 1) <= src_end) {
+      uint32_t w0 = sa[0];
+      for (uint32_t w = 0; w < nw; w++) {
+        const uint32_t w1 = sa[w + 1];
+        d32[w] = __funnelshift_r(w0, w1, 8 * sh);
+        w0 = w1;
+      }
+    } else {
+      for (uint32_t i = 0; i < 4 * nw; i++) dst[i] = src[i];
+    }
+    dst += 4 * nw;
+    src += 4 * nw;
+    len -= 4 * nw;
+  }
+  for (uint32_t i = 0; i < len; i++) dst[i] = src[i];
 }
 }  // namespace
 
 __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd, const FlushDesc fd) {
-  extern __shared__ __align__(16) uint8_t ssm[];
+  extern __shared__ __align__(128) uint8_t ssm[];
   __shared__ uint32_t scratch[33];
+  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ uint32_t s_bad;
   const int T = kTileRows;
-  uint16_t* kA = reinterpret_cast<uint16_t*>(ssm);          // [T]
-  uint16_t* pA = kA + T;                                    // [T]
-  uint16_t* kB = pA + T;                                    // [T]
-  uint16_t* pB = kB + T;                                    // [T]
+  uint8_t* stage0 = ssm;                                    // [2][kStageSlot]
+  uint16_t* kA = reinterpret_cast<uint16_t*>(ssm + 2 * kStageSlot);
+  uint16_t* pA = kA + T;
+  uint16_t* kB = pA + T;
+  uint16_t* pB = kB + T;
   uint32_t* dbit = reinterpret_cast<uint32_t*>(pB + T);     // [T] (radix offsets while sorting)
   uint16_t* rs = reinterpret_cast<uint16_t*>(dbit + T);     // [T]
   uint32_t* S = reinterpret_cast<uint32_t*>(rs + T);        // [T + 1]
@@ -558,8 +657,52 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
   const int n = (int)tile.nrows;
   const int P = sd.P;
   const int nstr = sd.n_str;
+  const int A = sd.n_array;
   const ColPtr* cols = fd.cols + (size_t)tile.batch * sd.n_cols;
   if (*reinterpret_cast<volatile int32_t*>(fd.err) != 0) return;  // inputs rejected by k_hash_count
+  const uint32_t row0 = tile.row0;
+  const uint32_t* nullcnt = fd.nullcnt + (size_t)tile.batch * A;
+
+  // what column `a` stages: [values or offsets][pad][validity bits]
+  auto issue = [&](int a, int slot) {
+    if (threadIdx.x != 0 || a >= A) return;
+    const ColPtr c = cols[sd.arr_col[a]];
+    uint8_t* dst = stage0 + slot * kStageSlot;
+    const int kind = sd.arr_kind[a];
+    const uint8_t* vsrc = nullptr;
+    uint32_t vbytes = 0;
+    if (kind == COL_FIXED && sd.arr_width[a] <= 8) {
+      vsrc = c.values + (size_t)row0 * sd.arr_width[a];
+      vbytes = (uint32_t)n * sd.arr_width[a];
+    } else if (kind == COL_BOOL) {
+      vsrc = c.values + (row0 >> 3);
+      vbytes = (uint32_t)(n + 7) >> 3;
+    } else if (kind == COL_BINARY) {
+      vsrc = reinterpret_cast<const uint8_t*>(c.offsets + row0);
+      vbytes = (uint32_t)(n + 1) * 4;
+    }
+    const uint8_t* bsrc = nullptr;
+    uint32_t bbytes = 0;
+    if (c.validity != nullptr && nullcnt[a] != 0 && fd.out_valid[a] != nullptr) {
+      bsrc = c.validity + (row0 >> 3);
+      bbytes = (uint32_t)(n + 7) >> 3;
+    }
+    // the barrier learns the bulk bytes before any copy can complete
+    fence_proxy_async();
+    mbar_expect_tx(&bars[slot], bulk_part(vsrc, vbytes) + bulk_part(bsrc, bbytes));
+    stage_piece(dst, vsrc, vbytes, &bars[slot]);
+    stage_piece(dst + kStageBytes + 16, bsrc, bbytes, &bars[slot]);
+  };
+
+  if (threadIdx.x == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    s_bad = 0;
+    fence_mbar_init();
+  }
+  __syncthreads();
+  issue(0, 0);
+  issue(1, 1);
 
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
     kA[j] = fd.pids[tile.frow0 + j];
@@ -601,32 +744,53 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
   }
   __syncthreads();
 
-  const uint32_t row0 = tile.row0;
-  for (int a = 0; a < sd.n_array; a++) {
+  for (int a = 0; a < A; a++) {
+    const int slot = a & 1;
+    const uint32_t parity = (uint32_t)((a >> 1) & 1);
+    if (!mbar_wait(&bars[slot], parity)) {
+      if (threadIdx.x == 0) atomicOr(fd.err, kErrTimeout);
+      s_bad = 1;
+    }
+    __syncthreads();
+    if (s_bad) {
+      mbar_wait(&bars[slot ^ 1], parity);  // let the other copy land before leaving
+      return;
+    }
+    const uint8_t* stg = stage0 + slot * kStageSlot;
     const ColPtr c = cols[sd.arr_col[a]];
     const int kind = sd.arr_kind[a];
     // validity: clear the bits of null rows (destination words start 0xff)
-    if (c.validity != nullptr && fd.out_valid[a] != nullptr &&
-        fd.nullcnt[(size_t)tile.batch * sd.n_array + a] != 0) {
+    if (c.validity != nullptr && nullcnt[a] != 0 && fd.out_valid[a] != nullptr) {
+      const uint8_t* vb = stg + kStageBytes + 16;
       uint32_t* ow = fd.out_valid[a];
       for (int j0 = 0; j0 < n; j0 += blockDim.x) {
         const int j = j0 + threadIdx.x;
         bool clr = false;
         uint32_t pos = 0;
         if (j < n) {
-          clr = !get_bit(c.validity, row0 + ps[j]);
+          clr = !get_bit(vb, ps[j]);
           pos = dbit[j];
         }
         clear_bits(ow, clr, pos);
       }
     }
     if (kind == COL_FIXED) {
-      switch (sd.arr_width[a]) {
-        case 1: copy_rows<uint8_t>(fd.out_values[a], c.values, ps, dstrow, row0, n); break;
-        case 2: copy_rows<uint16_t>(fd.out_values[a], c.values, ps, dstrow, row0, n); break;
-        case 4: copy_rows<uint32_t>(fd.out_values[a], c.values, ps, dstrow, row0, n); break;
-        case 8: copy_rows<uint64_t>(fd.out_values[a], c.values, ps, dstrow, row0, n); break;
-        default: copy_rows<uint4>(fd.out_values[a], c.values, ps, dstrow, row0, n); break;
+      const int w = sd.arr_width[a];
+      uint8_t* out = fd.out_values[a];
+      if (w == 8) {
+        const uint64_t* src = reinterpret_cast<const uint64_t*>(stg);
+        for (int j = threadIdx.x; j < n; j += blockDim.x) reinterpret_cast<uint64_t*>(out)[dstrow[j]] = src[ps[j]];
+      } else if (w == 4) {
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(stg);
+        for (int j = threadIdx.x; j < n; j += blockDim.x) reinterpret_cast<uint32_t*>(out)[dstrow[j]] = src[ps[j]];
+      } else if (w == 2) {
+        const uint16_t* src = reinterpret_cast<const uint16_t*>(stg);
+        for (int j = threadIdx.x; j < n; j += blockDim.x) reinterpret_cast<uint16_t*>(out)[dstrow[j]] = src[ps[j]];
+      } else if (w == 1) {
+        for (int j = threadIdx.x; j < n; j += blockDim.x) out[dstrow[j]] = stg[ps[j]];
+      } else {  // 16-byte values are gathered straight from global memory
+        const uint4* src = reinterpret_cast<const uint4*>(c.values) + row0;
+        for (int j = threadIdx.x; j < n; j += blockDim.x) reinterpret_cast<uint4*>(out)[dstrow[j]] = src[ps[j]];
       }
     } else if (kind == COL_BOOL) {
       uint32_t* ow = fd.out_bits[a];
@@ -635,14 +799,14 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
         bool clr = false;
         uint32_t pos = 0;
         if (j < n) {
-          clr = !get_bit(c.values, row0 + ps[j]);
+          clr = !get_bit(stg, ps[j]);
           pos = dbit[j];
         }
         clear_bits(ow, clr, pos);
       }
     } else {
       const int k = sd.arr_str[a];
-      const int32_t* oin = c.offsets + row0;
+      const int32_t* oin = reinterpret_cast<const int32_t*>(stg);  // offsets of rows row0..row0+n
       for (int j = threadIdx.x; j < n; j += blockDim.x) {
         const int r = ps[j];
         S[j] = (uint32_t)(oin[r + 1] - oin[r]);
@@ -655,31 +819,17 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
       const size_t tk = ((size_t)blockIdx.x * nstr + k) * P;
       const uint32_t* cst = fd.cstart + (size_t)k * P;
       uint8_t* ochars = fd.out_chars[a];
-      // offsets, one row per thread; then characters, one string per warp step
-      for (int j0 = 0; j0 < n; j0 += blockDim.x) {
-        const int j = j0 + threadIdx.x;
-        const uint8_t* src = nullptr;
-        uint8_t* dst = nullptr;
-        uint32_t len = 0;
-        if (j < n) {
-          const int p = ks[j];
-          const uint32_t pref = S[j] - S[rs[j]];
-          len = S[j + 1] - S[j];
-          ooff[dstrow[j]] = (int32_t)(fd.sbyte[tk + p] + pref + len);
-          src = c.values + oin[ps[j]];
-          dst = ochars + cst[p] + fd.bcnt[tk + p] + pref;
-        }
-        for (int s = 0; s < 32; s++) {
-          const uint8_t* ss = reinterpret_cast<const uint8_t*>(
-              __shfl_sync(kFull, reinterpret_cast<unsigned long long>(src), s));
-          uint8_t* dd = reinterpret_cast<uint8_t*>(
-              __shfl_sync(kFull, reinterpret_cast<unsigned long long>(dst), s));
-          const uint32_t ll = __shfl_sync(kFull, len, s);
-          for (uint32_t x = lane_id(); x < ll; x += 32) dd[x] = ss[x];
-        }
+      const uint8_t* src_end = c.values + c.values_bytes;
+      for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const int p = ks[j];
+        const uint32_t pref = S[j] - S[rs[j]];
+        const uint32_t len = S[j + 1] - S[j];
+        ooff[dstrow[j]] = (int32_t)(fd.sbyte[tk + p] + pref + len);
+        copy_string(ochars + cst[p] + fd.bcnt[tk + p] + pref, c.values + oin[ps[j]], len, src_end);
       }
-      __syncthreads();
     }
+    __syncthreads();  // everyone is done with this slot
+    issue(a + 2, slot);
   }
 }
 
@@ -715,7 +865,7 @@ cudaError_t launch_plan(const SchemaDesc& sd, const FlushDesc& fd, cudaStream_t 
 
 size_t scatter_smem_bytes() {
   const int T = kTileRows;
-  return 4 * sizeof(uint16_t) * T + sizeof(uint32_t) * T + sizeof(uint16_t) * T +
+  return 2 * kStageSlot + 4 * sizeof(uint16_t) * T + sizeof(uint32_t) * T + sizeof(uint16_t) * T +
          sizeof(uint32_t) * (T + 1) + sizeof(uint16_t) * kW * 256;
 }
 

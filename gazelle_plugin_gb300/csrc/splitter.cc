@@ -811,6 +811,7 @@ Status Splitter::SyncAndCheck() {
   int32_t err = 0;
   st = Cuda(cudaMemcpy(&err, d_err_, 4, cudaMemcpyDeviceToHost), "read error word");
   if (!st.ok()) return st;
+  if (err & kErrTimeout) return Status::Error(GZ_TIMEOUT, "a device-side wait timed out");
   if (err & kErrBadOffsets)
     return Status::Error(GZ_INVALID, "binary offsets are decreasing or exceed the value buffer");
   if (err) return Status::Error(GZ_CUDA, "device emission list overflow");
