@@ -587,19 +587,29 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   return false;
 }
 
-// Bytes of a staged piece that go by bulk copy: the 16-byte multiple of an aligned source.
+// A staged piece keeps the source's alignment phase: its bytes land at dst + (src & 15), so
+// the 16-byte aligned interior goes by one bulk copy and only the head and tail (< 16 bytes
+// each) by plain loads; nothing outside [src, src + bytes) is read.
 __device__ __forceinline__ uint32_t bulk_part(const uint8_t* src, uint32_t bytes) {
-  if (src == nullptr) return 0;
-  return ((reinterpret_cast<uintptr_t>(src) & 15) == 0) ? (bytes & ~15u) : 0u;
+  if (src == nullptr || bytes == 0) return 0;
+  const uint32_t mis = (uint32_t)(reinterpret_cast<uintptr_t>(src) & 15);
+  const uint32_t head = min(bytes, (16u - mis) & 15u);
+  return (bytes - head) & ~15u;
 }
-// Stages `bytes` of `src` at `dst`: the bulk part by TMA (completing on `bar`), the rest by
-// plain loads.  Thread 0, after the barrier expects the bulk bytes.
-__device__ __forceinline__ void stage_piece(uint8_t* dst, const uint8_t* src, uint32_t bytes,
+__device__ __forceinline__ const uint8_t* staged_ptr(const uint8_t* dst_base, const uint8_t* src) {
+  return dst_base + (reinterpret_cast<uintptr_t>(src) & 15);
+}
+// Thread 0, after the barrier expects the bulk bytes.
+__device__ __forceinline__ void stage_piece(uint8_t* dst_base, const uint8_t* src, uint32_t bytes,
                                             uint64_t* bar) {
   if (bytes == 0 || src == nullptr) return;
-  const uint32_t bulk = bulk_part(src, bytes);
-  if (bulk) bulk_g2s(dst, src, bulk, bar);
-  for (uint32_t i = bulk; i < bytes; i++) dst[i] = src[i];
+  const uint32_t mis = (uint32_t)(reinterpret_cast<uintptr_t>(src) & 15);
+  uint8_t* dst = dst_base + mis;
+  const uint32_t head = min(bytes, (16u - mis) & 15u);
+  const uint32_t bulk = (bytes - head) & ~15u;
+  for (uint32_t i = 0; i < head; i++) dst[i] = src[i];
+  if (bulk) bulk_g2s(dst + head, src + head, bulk, bar);
+  for (uint32_t i = head + bulk; i < bytes; i++) dst[i] = src[i];
 }
 
 // One string: len bytes from src to dst, aligned 32-bit stores for the body.  Source words are
@@ -756,12 +766,16 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
       mbar_wait(&bars[slot ^ 1], parity);  // let the other copy land before leaving
       return;
     }
-    const uint8_t* stg = stage0 + slot * kStageSlot;
     const ColPtr c = cols[sd.arr_col[a]];
     const int kind = sd.arr_kind[a];
+    const uint8_t* slot_base = stage0 + slot * kStageSlot;
+    const uint8_t* stg = slot_base;  // staged values / bits / offsets, at the source's phase
+    if (kind == COL_FIXED && sd.arr_width[a] <= 8) stg = staged_ptr(slot_base, c.values + (size_t)row0 * sd.arr_width[a]);
+    else if (kind == COL_BOOL) stg = staged_ptr(slot_base, c.values + (row0 >> 3));
+    else if (kind == COL_BINARY) stg = staged_ptr(slot_base, reinterpret_cast<const uint8_t*>(c.offsets + row0));
     // validity: clear the bits of null rows (destination words start 0xff)
     if (c.validity != nullptr && nullcnt[a] != 0 && fd.out_valid[a] != nullptr) {
-      const uint8_t* vb = stg + kStageBytes + 16;
+      const uint8_t* vb = staged_ptr(slot_base + kStageBytes + 16, c.validity + (row0 >> 3));
       uint32_t* ow = fd.out_valid[a];
       for (int j0 = 0; j0 < n; j0 += blockDim.x) {
         const int j = j0 + threadIdx.x;
