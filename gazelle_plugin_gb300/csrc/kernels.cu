@@ -612,38 +612,49 @@ __device__ __forceinline__ void stage_piece(uint8_t* dst_base, const uint8_t* sr
   for (uint32_t i = head + bulk; i < bytes; i++) dst[i] = src[i];
 }
 
-// One string: len bytes from src to dst, aligned 32-bit stores for the body.  Source words are
-// read aligned; `src_end` bounds the bytes that may be read.
+// Source word at `a` (4-byte aligned); bytes outside [lo, hi) read as 0 and are never stored.
+__device__ __forceinline__ uint32_t load_word(uintptr_t a, uintptr_t lo, uintptr_t hi) {
+  if (a >= lo && a + 4 <= hi) return *reinterpret_cast<const uint32_t*>(a);
+  uint32_t v = 0;
+  for (int t = 0; t < 4; t++)
+    if (a + t >= lo && a + t < hi) v |= (uint32_t)(*reinterpret_cast<const uint8_t*>(a + t)) << (8 * t);
+  return v;
+}
+
+// One string: `len` bytes from `src` to `dst`.  Destination words are 4-byte aligned; each is
+// built by a funnel shift of two aligned source words.  Eight destination words are produced
+// per step from nine source words loaded up front, so a short string costs one memory latency
+// rather than one per word.  Only bytes inside [buf_lo, buf_hi) of the source are read and only
+// [dst, dst + len) is written.
 __device__ __forceinline__ void copy_string(uint8_t* dst, const uint8_t* src, uint32_t len,
-                                            const uint8_t* src_end) {
-  uint32_t h = (4u - (uint32_t)(reinterpret_cast<uintptr_t>(dst) & 3)) & 3;
-  if (h > len) h = len;
-  for (uint32_t i = 0; i < h; i++) dst[i] = src[i];
-  dst += h;
-  src += h;
-  len -= h;
-  uint32_t nw = len >> 2;
-  if (nw) {
-    const uint32_t sh = (uint32_t)(reinterpret_cast<uintptr_t>(src) & 3);
-    const uint32_t* sa = reinterpret_cast<const uint32_t*>(src - sh);
-    uint32_t* d32 = reinterpret_cast<uint32_t*>(dst);
-    if (sh == 0) {
-      for (uint32_t w = 0; w < nw; w++) d32[w] = sa[w];
-    } else if (reinterpret_cast<const uint8_t*>(sa + nw + 1) <= src_end) {
-      uint32_t w0 = sa[0];
-      for (uint32_t w = 0; w < nw; w++) {
-        const uint32_t w1 = sa[w + 1];
-        d32[w] = __funnelshift_r(w0, w1, 8 * sh);
-        w0 = w1;
+                                            uintptr_t buf_lo, uintptr_t buf_hi) {
+  if (len == 0) return;
+  const uintptr_t d = reinterpret_cast<uintptr_t>(dst);
+  const uintptr_t dw0 = d & ~uintptr_t(3);
+  const int nwd = (int)((((d + len - 1) & ~uintptr_t(3)) - dw0) >> 2) + 1;
+  // source address of byte 0 of destination word 0
+  const uintptr_t bs = reinterpret_cast<uintptr_t>(src) - (d - dw0);
+  const uint32_t sh = (uint32_t)(bs & 3) * 8;
+  const uintptr_t sw0 = bs & ~uintptr_t(3);
+  const uintptr_t lo = reinterpret_cast<uintptr_t>(src) > buf_lo ? reinterpret_cast<uintptr_t>(src) : buf_lo;
+  const uintptr_t hi = reinterpret_cast<uintptr_t>(src) + len < buf_hi ? reinterpret_cast<uintptr_t>(src) + len : buf_hi;
+  for (int g = 0; g < nwd; g += 8) {
+    uint32_t W[9];
+#pragma unroll
+    for (int q = 0; q < 9; q++) W[q] = (g + q <= nwd) ? load_word(sw0 + 4 * (uintptr_t)(g + q), lo, hi) : 0u;
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      if (g + q >= nwd) break;
+      const uint32_t v = sh ? __funnelshift_r(W[q], W[q + 1], sh) : W[q];
+      const uintptr_t A = dw0 + 4 * (uintptr_t)(g + q);
+      if (A >= d && A + 4 <= d + len) {
+        *reinterpret_cast<uint32_t*>(A) = v;
+      } else {
+        for (int t = 0; t < 4; t++)
+          if (A + t >= d && A + t < d + len) *reinterpret_cast<uint8_t*>(A + t) = (uint8_t)(v >> (8 * t));
       }
-    } else {
-      for (uint32_t i = 0; i < 4 * nw; i++) dst[i] = src[i];
     }
-    dst += 4 * nw;
-    src += 4 * nw;
-    len -= 4 * nw;
   }
-  for (uint32_t i = 0; i < len; i++) dst[i] = src[i];
 }
 }  // namespace
 
@@ -661,7 +672,9 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
   uint32_t* dbit = reinterpret_cast<uint32_t*>(pB + T);     // [T] (radix offsets while sorting)
   uint16_t* rs = reinterpret_cast<uint16_t*>(dbit + T);     // [T]
   uint32_t* S = reinterpret_cast<uint32_t*>(rs + T);        // [T + 1]
-  uint16_t* wcnt = reinterpret_cast<uint16_t*>(S + T + 1);  // [kW * 256]
+  uint32_t* rt0 = S + T + 1;                                // [T] run tables (at run starts)
+  uint32_t* rt1 = rt0 + T;                                  // [T]
+  uint16_t* wcnt = reinterpret_cast<uint16_t*>(rt1 + T);    // [kW * 256]
 
   const TileDesc tile = fd.tiles[blockIdx.x];
   const int n = (int)tile.nrows;
@@ -745,12 +758,19 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
     }
   }
   __syncthreads();
+  // destination row / validity bit: one metadata lookup per run, kept at the run start
   const size_t tp = (size_t)blockIdx.x * P;
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
-    const int p = ks[j];
-    const uint32_t rk = (uint32_t)(j - rs[j]);
-    dstrow[j] = fd.pstart[p] + fd.cnt[tp + p] + rk;
-    dbit[j] = fd.vstart[p] + fd.vpos[tp + p] + rk;
+    if (rs[j] == j) {
+      const int p = ks[j];
+      S[j] = fd.pstart[p] + fd.cnt[tp + p] - (uint32_t)j;
+      rt1[j] = fd.vstart[p] + fd.vpos[tp + p] - (uint32_t)j;
+    }
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    dstrow[j] = S[rs[j]] + (uint32_t)j;
+    dbit[j] = rt1[rs[j]] + (uint32_t)j;
   }
   __syncthreads();
 
@@ -833,13 +853,22 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
       const size_t tk = ((size_t)blockIdx.x * nstr + k) * P;
       const uint32_t* cst = fd.cstart + (size_t)k * P;
       uint8_t* ochars = fd.out_chars[a];
-      const uint8_t* src_end = c.values + c.values_bytes;
+      // per run: in-segment byte offset and destination byte of the run's first string
       for (int j = threadIdx.x; j < n; j += blockDim.x) {
-        const int p = ks[j];
-        const uint32_t pref = S[j] - S[rs[j]];
+        if (rs[j] == j) {
+          const int p = ks[j];
+          rt0[j] = fd.sbyte[tk + p] - S[j];
+          rt1[j] = cst[p] + fd.bcnt[tk + p] - S[j];
+        }
+      }
+      __syncthreads();
+      const uintptr_t buf_lo = reinterpret_cast<uintptr_t>(c.values);
+      const uintptr_t buf_hi = buf_lo + c.values_bytes;
+      for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const int r0 = rs[j];
         const uint32_t len = S[j + 1] - S[j];
-        ooff[dstrow[j]] = (int32_t)(fd.sbyte[tk + p] + pref + len);
-        copy_string(ochars + cst[p] + fd.bcnt[tk + p] + pref, c.values + oin[ps[j]], len, src_end);
+        ooff[dstrow[j]] = (int32_t)(rt0[r0] + S[j] + len);
+        copy_string(ochars + rt1[r0] + S[j], c.values + oin[ps[j]], len, buf_lo, buf_hi);
       }
     }
     __syncthreads();  // everyone is done with this slot
@@ -880,7 +909,7 @@ cudaError_t launch_plan(const SchemaDesc& sd, const FlushDesc& fd, cudaStream_t 
 size_t scatter_smem_bytes() {
   const int T = kTileRows;
   return 2 * kStageSlot + 4 * sizeof(uint16_t) * T + sizeof(uint32_t) * T + sizeof(uint16_t) * T +
-         sizeof(uint32_t) * (T + 1) + sizeof(uint16_t) * kW * 256;
+         sizeof(uint32_t) * (T + 1) + 2 * sizeof(uint32_t) * T + sizeof(uint16_t) * kW * 256;
 }
 
 cudaError_t launch_scatter(const SchemaDesc& sd, const FlushDesc& fd, cudaStream_t st) {
