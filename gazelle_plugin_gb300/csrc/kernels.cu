@@ -600,17 +600,35 @@ __device__ __forceinline__ uint32_t bulk_part(const uint8_t* src, uint32_t bytes
 __device__ __forceinline__ const uint8_t* staged_ptr(const uint8_t* dst_base, const uint8_t* src) {
   return dst_base + (reinterpret_cast<uintptr_t>(src) & 15);
 }
-// Thread 0, after the barrier expects the bulk bytes.
-__device__ __forceinline__ void stage_piece(uint8_t* dst_base, const uint8_t* src, uint32_t bytes,
-                                            uint64_t* bar) {
+// Thread 0, after the barrier expects the bulk bytes: the aligned interior by TMA.  The head
+// and tail bytes are fetched by `fetch_edge` into registers when the copy is issued and
+// written to shared memory by `place_edge` when the column is consumed.
+__device__ __forceinline__ void stage_bulk(uint8_t* dst_base, const uint8_t* src, uint32_t bytes,
+                                           uint64_t* bar) {
   if (bytes == 0 || src == nullptr) return;
   const uint32_t mis = (uint32_t)(reinterpret_cast<uintptr_t>(src) & 15);
-  uint8_t* dst = dst_base + mis;
   const uint32_t head = min(bytes, (16u - mis) & 15u);
   const uint32_t bulk = (bytes - head) & ~15u;
-  for (uint32_t i = 0; i < head; i++) dst[i] = src[i];
-  if (bulk) bulk_g2s(dst + head, src + head, bulk, bar);
-  for (uint32_t i = head + bulk; i < bytes; i++) dst[i] = src[i];
+  if (bulk) bulk_g2s(dst_base + mis + head, src + head, bulk, bar);
+}
+// Edge byte e (0..15: head, 16..31: tail) of a piece whose slot offset is `base_off`; returns
+// byte | 0x100 | (slot offset << 9), or 0 when there is no such byte.
+__device__ __forceinline__ uint32_t fetch_edge(const uint8_t* src, uint32_t bytes, uint32_t base_off,
+                                               int e) {
+  if (bytes == 0 || src == nullptr) return 0;
+  const uint32_t mis = (uint32_t)(reinterpret_cast<uintptr_t>(src) & 15);
+  const uint32_t head = min(bytes, (16u - mis) & 15u);
+  const uint32_t bulk = (bytes - head) & ~15u;
+  const uint32_t tail = bytes - head - bulk;
+  uint32_t i;
+  if (e < 16) {
+    if ((uint32_t)e >= head) return 0;
+    i = (uint32_t)e;
+  } else {
+    if ((uint32_t)(e - 16) >= tail) return 0;
+    i = head + bulk + (uint32_t)(e - 16);
+  }
+  return (uint32_t)src[i] | 0x100u | ((base_off + mis + i) << 9);
 }
 
 // Source word at `a` (4-byte aligned); bytes outside [lo, hi) read as 0 and are never stored.
@@ -712,34 +730,44 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
   const uint32_t* nullcnt = fd.nullcnt + (size_t)tile.batch * A;
 
   // what column `a` stages: [values or offsets][pad][validity bits]
-  auto issue = [&](int a, int slot) {
-    if (threadIdx.x != 0 || a >= A) return;
+  auto pieces = [&](int a, const uint8_t** vsrc, uint32_t* vbytes, const uint8_t** bsrc, uint32_t* bbytes) {
     const ColPtr c = cols[sd.arr_col[a]];
-    uint8_t* dst = stage0 + slot * kStageSlot;
     const int kind = sd.arr_kind[a];
-    const uint8_t* vsrc = nullptr;
-    uint32_t vbytes = 0;
+    *vsrc = nullptr;
+    *vbytes = 0;
     if (kind == COL_FIXED && sd.arr_width[a] <= 8) {
-      vsrc = c.values + (size_t)row0 * sd.arr_width[a];
-      vbytes = (uint32_t)n * sd.arr_width[a];
+      *vsrc = c.values + (size_t)row0 * sd.arr_width[a];
+      *vbytes = (uint32_t)n * sd.arr_width[a];
     } else if (kind == COL_BOOL) {
-      vsrc = c.values + (row0 >> 3);
-      vbytes = (uint32_t)(n + 7) >> 3;
+      *vsrc = c.values + (row0 >> 3);
+      *vbytes = (uint32_t)(n + 7) >> 3;
     } else if (kind == COL_BINARY) {
-      vsrc = reinterpret_cast<const uint8_t*>(c.offsets + row0);
-      vbytes = (uint32_t)(n + 1) * 4;
+      *vsrc = reinterpret_cast<const uint8_t*>(c.offsets + row0);
+      *vbytes = (uint32_t)(n + 1) * 4;
     }
-    const uint8_t* bsrc = nullptr;
-    uint32_t bbytes = 0;
+    *bsrc = nullptr;
+    *bbytes = 0;
     if (c.validity != nullptr && nullcnt[a] != 0 && fd.out_valid[a] != nullptr) {
-      bsrc = c.validity + (row0 >> 3);
-      bbytes = (uint32_t)(n + 7) >> 3;
+      *bsrc = c.validity + (row0 >> 3);
+      *bbytes = (uint32_t)(n + 7) >> 3;
     }
-    // the barrier learns the bulk bytes before any copy can complete
-    fence_proxy_async();
-    mbar_expect_tx(&bars[slot], bulk_part(vsrc, vbytes) + bulk_part(bsrc, bbytes));
-    stage_piece(dst, vsrc, vbytes, &bars[slot]);
-    stage_piece(dst + kStageBytes + 16, bsrc, bbytes, &bars[slot]);
+  };
+  // every thread calls it; returns this thread's pending edge byte for the slot
+  auto issue = [&](int a, int slot) -> uint32_t {
+    if (a >= A) return 0u;
+    const uint8_t *vsrc, *bsrc;
+    uint32_t vbytes, bbytes;
+    pieces(a, &vsrc, &vbytes, &bsrc, &bbytes);
+    if (threadIdx.x == 0) {
+      uint8_t* dst = stage0 + slot * kStageSlot;
+      fence_proxy_async();  // earlier generic reads of the slot come first
+      mbar_expect_tx(&bars[slot], bulk_part(vsrc, vbytes) + bulk_part(bsrc, bbytes));
+      stage_bulk(dst, vsrc, vbytes, &bars[slot]);
+      stage_bulk(dst + kStageBytes + 16, bsrc, bbytes, &bars[slot]);
+    }
+    if (threadIdx.x < 32) return fetch_edge(vsrc, vbytes, 0, threadIdx.x);
+    if (threadIdx.x < 64) return fetch_edge(bsrc, bbytes, kStageBytes + 16, threadIdx.x - 32);
+    return 0u;
   };
 
   if (threadIdx.x == 0) {
@@ -749,8 +777,8 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
     fence_mbar_init();
   }
   __syncthreads();
-  issue(0, 0);
-  issue(1, 1);
+  uint32_t pend0 = issue(0, 0);
+  uint32_t pend1 = issue(1, 1);
 
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
     kA[j] = fd.pids[tile.frow0 + j];
@@ -813,6 +841,10 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
     if (!mbar_wait(&bars[slot], parity)) {
       if (threadIdx.x == 0) atomicOr(fd.err, kErrTimeout);
       s_bad = 1;
+    }
+    {
+      const uint32_t pe = slot ? pend1 : pend0;
+      if (pe) stage0[slot * kStageSlot + (pe >> 9)] = (uint8_t)pe;
     }
     __syncthreads();
     if (s_bad) {
@@ -920,7 +952,9 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
       }
     }
     __syncthreads();  // everyone is done with this slot
-    issue(a + 2, slot);
+    const uint32_t pe = issue(a + 2, slot);
+    if (slot) pend1 = pe;
+    else pend0 = pe;
   }
 }
 
