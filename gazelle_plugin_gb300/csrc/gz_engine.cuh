@@ -19,7 +19,7 @@ namespace gz {
 constexpr int kMaxKeys = 8;
 constexpr int kMaxCols = 64;    // array columns (fixed + bool + binary)
 constexpr int kMaxSchemaCols = 256;
-constexpr int kTileRows = 2048; // rows per k_hash_count / k_scatter CTA
+constexpr int kTileRows = 1024; // rows per k_hash_count / k_scatter CTA
 constexpr int kScatterThreads = 256;
 constexpr int kPlanThreads = 1024;
 constexpr int kMaxBatchesPerFlush = 4096;

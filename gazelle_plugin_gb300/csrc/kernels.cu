@@ -501,7 +501,7 @@ constexpr int kW = kScatterThreads / 32;
 constexpr int kStageBytes = kTileRows * 8;          // one 8-byte column slice
 constexpr int kStageValid = kTileRows / 8;           // its validity bits
 constexpr int kStageSlot = kStageBytes + 16 + kStageValid + 16;
-constexpr int kCharBuf = 16384;                      // sorted characters of one chunk
+constexpr int kCharStage = 32768;                    // a tile's source characters of one column
 constexpr uint32_t kSpinLimit = 1u << 26;
 
 // One stable LSD pass over 8 bits of the keys.
@@ -676,38 +676,17 @@ __device__ __forceinline__ void copy_string(uint8_t* dst, const uint8_t* src, ui
   }
 }
 
-// The warp writes `len` bytes from shared memory `src` to global `dst`: lane q writes aligned
-// destination word q, built from two aligned shared-memory words (the buffer has 8 bytes of
-// slack on both sides); partial words at the two ends are written byte by byte.
-__device__ __forceinline__ void warp_copy_out(uint8_t* dst, const uint8_t* src, uint32_t len) {
-  const uintptr_t d = reinterpret_cast<uintptr_t>(dst);
-  const uintptr_t dw0 = d & ~uintptr_t(3);
-  const uint32_t nwd = (uint32_t)((((d + len - 1) & ~uintptr_t(3)) - dw0) >> 2) + 1;
-  const uintptr_t bs = reinterpret_cast<uintptr_t>(src) - (d - dw0);
-  const uint32_t sh = (uint32_t)(bs & 3) * 8;
-  const uint32_t* sw = reinterpret_cast<const uint32_t*>(bs & ~uintptr_t(3));
-  for (uint32_t q = lane_id(); q < nwd; q += 32) {
-    const uint32_t v = sh ? __funnelshift_r(sw[q], sw[q + 1], sh) : sw[q];
-    const uintptr_t A = dw0 + 4 * (uintptr_t)q;
-    if (A >= d && A + 4 <= d + len) {
-      *reinterpret_cast<uint32_t*>(A) = v;
-    } else {
-      for (int t = 0; t < 4; t++)
-        if (A + t >= d && A + t < d + len) *reinterpret_cast<uint8_t*>(A + t) = (uint8_t)(v >> (8 * t));
-    }
-  }
-}
 }  // namespace
 
 __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd, const FlushDesc fd) {
   extern __shared__ __align__(128) uint8_t ssm[];
   __shared__ uint32_t scratch[33];
-  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ __align__(8) uint64_t bars[3];  // two column slots + the character stage
   __shared__ uint32_t s_bad;
   const int T = kTileRows;
   uint8_t* stage0 = ssm;                                    // [2][kStageSlot]
-  uint8_t* cbuf = ssm + 2 * kStageSlot + 8;                 // [kCharBuf], 8 bytes slack each side
-  uint16_t* kA = reinterpret_cast<uint16_t*>(ssm + 2 * kStageSlot + kCharBuf + 16);
+  uint8_t* cstage = ssm + 2 * kStageSlot;                   // [kCharStage + 16]
+  uint16_t* kA = reinterpret_cast<uint16_t*>(ssm + 2 * kStageSlot + kCharStage + 16);
   uint16_t* pA = kA + T;
   uint16_t* kB = pA + T;
   uint16_t* pB = kB + T;
@@ -717,7 +696,6 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
   uint32_t* rt0 = S + T + 1;                                // [T] run tables (at run starts)
   uint32_t* rt1 = rt0 + T;                                  // [T]
   uint16_t* wcnt = reinterpret_cast<uint16_t*>(rt1 + T);    // [kW * 256]
-  uint16_t* runpos = wcnt + kW * 256;                       // [T + 1] sorted position of run r
 
   const TileDesc tile = fd.tiles[blockIdx.x];
   const int n = (int)tile.nrows;
@@ -773,6 +751,7 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
   if (threadIdx.x == 0) {
     mbar_init(&bars[0], 1);
     mbar_init(&bars[1], 1);
+    mbar_init(&bars[2], 1);
     s_bad = 0;
     fence_mbar_init();
   }
@@ -826,14 +805,7 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
     dbit[j] = rt1[rs[j]] + (uint32_t)j;
   }
   __syncthreads();
-  // dense run list: runpos[r] = sorted position where run r starts, runpos[nruns] = n
-  for (int j = threadIdx.x; j < n; j += blockDim.x) S[j] = rs[j] == j ? 1u : 0u;
-  __syncthreads();
-  const uint32_t nruns = block_exscan<kScatterThreads>(S, n, scratch);
-  for (int j = threadIdx.x; j < n; j += blockDim.x)
-    if (rs[j] == j) runpos[S[j]] = (uint16_t)j;
-  if (threadIdx.x == 0) runpos[nruns] = (uint16_t)n;
-  __syncthreads();
+  uint32_t cphase = 0;  // uses of the character stage
 
   for (int a = 0; a < A; a++) {
     const int slot = a & 1;
@@ -927,28 +899,42 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
         }
       }
       __syncthreads();
-      const uintptr_t buf_lo = reinterpret_cast<uintptr_t>(c.values);
-      const uintptr_t buf_hi = buf_lo + c.values_bytes;
       for (int j = threadIdx.x; j < n; j += blockDim.x)
         ooff[dstrow[j]] = (int32_t)(rt0[rs[j]] + S[j + 1]);
-      // characters, kCharBuf bytes of the sorted concatenation at a time: (A) each lane
-      // copies the part of its strings inside the chunk into shared memory, (B) one warp per
-      // partition run writes the run's bytes to its destination with aligned word stores
-      const int warp = threadIdx.x >> 5;
-      for (uint32_t lo = 0; lo < total; lo += kCharBuf) {
-        const uint32_t hi = min(total, lo + (uint32_t)kCharBuf);
-        for (int j = threadIdx.x; j < n; j += blockDim.x) {
-          const uint32_t s0 = S[j], s1 = S[j + 1];
-          const uint32_t a0 = max(s0, lo), a1 = min(s1, hi);
-          if (a0 < a1) copy_string(cbuf + (a0 - lo), c.values + oin[ps[j]] + (a0 - s0), a1 - a0, buf_lo, buf_hi);
+      // the tile's characters [oin[0], oin[n]) are contiguous in the source: one bulk copy
+      // into shared memory when they fit, then one string per lane from there
+      const int32_t c0 = oin[0], c1 = oin[n];
+      const uint8_t* csrc = c.values + c0;
+      const uint32_t cbytes = (uint32_t)(c1 - c0);
+      const bool staged = cbytes > 0 && cbytes <= (uint32_t)kCharStage;
+      const uint8_t* cbase = c.values;  // where string bytes are read from (offset by oin[])
+      uintptr_t buf_lo = reinterpret_cast<uintptr_t>(c.values);
+      uintptr_t buf_hi = buf_lo + c.values_bytes;
+      if (staged) {
+        if (threadIdx.x == 0) {
+          fence_proxy_async();
+          mbar_expect_tx(&bars[2], bulk_part(csrc, cbytes));
+          stage_bulk(cstage, csrc, cbytes, &bars[2]);
         }
-        __syncthreads();
-        for (uint32_t r = warp; r < nruns; r += kW) {
-          const uint32_t j0 = runpos[r], j1 = runpos[r + 1];
-          const uint32_t b0 = max(S[j0], lo), b1 = min(S[j1], hi);
-          if (b0 < b1) warp_copy_out(ochars + rt1[j0] + b0, cbuf + (b0 - lo), b1 - b0);
+        if (threadIdx.x < 32) {
+          const uint32_t pe = fetch_edge(csrc, cbytes, 0, threadIdx.x);
+          if (pe) cstage[pe >> 9] = (uint8_t)pe;
         }
+        if (!mbar_wait(&bars[2], cphase & 1)) {
+          if (threadIdx.x == 0) atomicOr(fd.err, kErrTimeout);
+          s_bad = 1;
+        }
+        cphase++;
         __syncthreads();
+        if (s_bad) return;
+        const uint8_t* sbase = staged_ptr(cstage, csrc);  // byte oin[0] of the column
+        cbase = sbase - c0;
+        buf_lo = reinterpret_cast<uintptr_t>(sbase);
+        buf_hi = buf_lo + cbytes;
+      }
+      for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const uint32_t len = S[j + 1] - S[j];
+        copy_string(ochars + rt1[rs[j]] + S[j], cbase + oin[ps[j]], len, buf_lo, buf_hi);
       }
     }
     __syncthreads();  // everyone is done with this slot
@@ -990,9 +976,9 @@ cudaError_t launch_plan(const SchemaDesc& sd, const FlushDesc& fd, cudaStream_t 
 
 size_t scatter_smem_bytes() {
   const int T = kTileRows;
-  return 2 * kStageSlot + kCharBuf + 16 + 4 * sizeof(uint16_t) * T + sizeof(uint32_t) * T +
+  return 2 * kStageSlot + kCharStage + 16 + 4 * sizeof(uint16_t) * T + sizeof(uint32_t) * T +
          sizeof(uint16_t) * T + sizeof(uint32_t) * (T + 1) + 2 * sizeof(uint32_t) * T +
-         sizeof(uint16_t) * kW * 256 + sizeof(uint16_t) * (T + 1);
+         sizeof(uint16_t) * kW * 256;
 }
 
 cudaError_t launch_scatter(const SchemaDesc& sd, const FlushDesc& fd, cudaStream_t st) {
