@@ -410,7 +410,9 @@ def run_gpu(args):
             "cpu_baseline": cpu,
             "e2e": e2e,
             "clocks": clk,
-            "gpu_launches": int(round(3 * flushes * args.steps)),
+            # per device pass: k_hash_count, k_plan_prep, k_plan_rows, k_plan_bytes (utf8
+            # columns present), k_plan_scan, k_scatter
+            "gpu_launches": int(round(6 * flushes * args.steps)),
             "kernels_ms_per_step": {"k_hash_count": k_hash, "k_plan": k_plan, "k_scatter": k_scat},
             "rows_per_s": args.rows * args.steps * world / t_max,
             "input_gbs": in_bytes * args.steps * world / t_max / 1e9,
