@@ -13,6 +13,7 @@
 #include <string>
 
 #include "../../include/gz_split.h"
+#include "hash_static.h"
 #include "schema_ipc.h"
 #include "splitter.h"
 
@@ -256,6 +257,16 @@ GzStatus gz_split_stats(int64_t handle, int64_t* out8) {
   if (!e || !out8) return GZ_INVALID;
   e->splitter->Stats(out8);
   return GZ_OK;
+}
+
+GzStatus gz_hash_partition_static(int32_t device, int32_t num_partitions, const GzKeyColumn* keys,
+                                  int32_t n_keys, int32_t num_rows, uint16_t* d_pids,
+                                  int64_t* d_counts, void* stream) {
+  std::string msg;
+  GzStatus st = gz::HashPartitionStatic(device, num_partitions, keys, n_keys, num_rows, d_pids,
+                                        d_counts, static_cast<cudaStream_t>(stream), &msg);
+  if (st != GZ_OK) t_make_error = "gz_hash_partition_static: " + msg;
+  return st;
 }
 
 GzStatus gz_debug_encode_record_batch(int64_t length, const int64_t* nodes, int32_t n_nodes,

@@ -173,6 +173,44 @@ GzStatus gz_split_kernel_times(int64_t handle, double* out4);
  * No reference counterpart. */
 GzStatus gz_split_stats(int64_t handle, int64_t* out8);
 
+/* ---- partition ids without device allocation (no counterpart in the reference) -------- */
+
+/* One hash-key column of a batch that is already in device memory. */
+typedef struct GzKeyColumn {
+  int32_t type;             /* GzType: BOOL, INT8, INT16, INT32, FLOAT32, DATE32, INT64, FLOAT64 */
+  int32_t reserved;
+  const uint8_t* validity;  /* device address of the validity bitmap (LSB first); NULL: no nulls */
+  const uint8_t* values;    /* device address of the values (bit-packed for BOOL) */
+} GzKeyColumn;
+
+/* Partition id of every row (one uint16 each, into d_pids) and the row count of every
+ * partition (num_partitions int64, into d_counts) of one batch whose hash keys are already on
+ * device `device`, with the splitter's Spark hash: Murmur3 chained from seed 42 over the keys in
+ * order, a null key passing the seed through, pid = pmod(hash, num_partitions).  Has no
+ * counterpart in the reference.
+ *
+ * It allocates no device memory, for callers that cannot call cudaMalloc: processes whose
+ * device memory all belongs to another allocator (a pool that reserved the free HBM up front,
+ * or an executor that charges every device byte to a task's memory budget, which a hidden
+ * cudaMalloc would escape), and code that must not stall the device, as cudaMalloc and
+ * cudaFree may synchronise it.  Inputs and outputs are the caller's device memory.
+ *
+ * Its scratch, the per-tile row counts, is one 16 MiB array in the library's own device
+ * memory, held on every device where the library runs until the process exits.  A call needs
+ * ceil(num_rows / 1024) * num_partitions 32-bit counters, at most 4,194,304 (e.g. 65,536 rows
+ * at 65,536 partitions, or 21 million rows at 200); a larger call returns GZ_INVALID.  All calls
+ * on a device share the array and it keeps the last call's contents (each call clears what it
+ * uses), so calls that may overlap on the GPU (other streams, other threads) race and give
+ * wrong counts: put them on one stream.  The first call on a device looks up the array's device
+ * address with that device current; make that first call before any stream capture.
+ *
+ * The work is enqueued on `stream` (a cudaStream_t of that device, NULL: its default stream)
+ * and the call returns without waiting; the calling thread's current device is left as it
+ * was.  On error, gz_last_error(0, ...) on the same thread gives the message. */
+GzStatus gz_hash_partition_static(int32_t device, int32_t num_partitions, const GzKeyColumn* keys,
+                                  int32_t n_keys, int32_t num_rows, uint16_t* d_pids,
+                                  int64_t* d_counts, void* stream);
+
 /* ---- test hooks (no reference counterpart; used by the unit tests) ------------------- */
 
 /* Encodes one Arrow IPC RecordBatch message with the splitter's encoder.  nodes: L pairs
