@@ -155,12 +155,7 @@ GzStatus gz_split_split_batches(int64_t handle, int32_t n_batches, const int32_t
     e->last_error = "Native split: null buffer list";
     return GZ_INVALID;
   }
-  for (int32_t i = 0; i < n_batches; i++) {
-    GzStatus s = Report(e.get(), e->splitter->Split(rows[i], buf_addrs + (size_t)i * n_bufs,
-                                                    buf_sizes + (size_t)i * n_bufs, n_bufs));
-    if (s != GZ_OK) return s;
-  }
-  return GZ_OK;
+  return Report(e.get(), e->splitter->SplitBatches(n_batches, rows, buf_addrs, buf_sizes, n_bufs));
 }
 
 GzStatus gz_split_sync(int64_t handle) {

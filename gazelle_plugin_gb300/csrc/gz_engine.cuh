@@ -56,6 +56,14 @@ struct ColPtr {
   uint64_t values_bytes;  // readable bytes at `values` (binary columns: offsets are checked)
 };
 
+// One input buffer the device copies out of host memory (a coherent host-device link lets
+// kernels read host addresses): `bytes` from `src` (host) to `dst` (device staging).
+struct HostCopy {
+  const uint8_t* src;
+  uint8_t* dst;
+  uint64_t bytes;
+};
+
 // bits of FlushDesc::err
 constexpr int32_t kErrEmitOverflow = 1;
 constexpr int32_t kErrBadOffsets = 2;

@@ -9,6 +9,7 @@ namespace gz {
 cudaError_t launch_hash_count(const SchemaDesc& sd, const FlushDesc& fd, cudaStream_t st);
 cudaError_t launch_plan(const SchemaDesc& sd, const FlushDesc& fd, cudaStream_t st);
 cudaError_t launch_scatter(const SchemaDesc& sd, const FlushDesc& fd, cudaStream_t st);
+cudaError_t launch_gather(const HostCopy* jobs, uint32_t n_jobs, cudaStream_t st);
 size_t scatter_smem_bytes();
 int max_str_columns();
 

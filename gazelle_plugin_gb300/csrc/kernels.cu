@@ -899,6 +899,50 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
 }
 
 // =======================================================================================
+// k_gather: host input buffers into device staging, read by the SMs straight from host memory
+// over the coherent link.  Each CTA copies whole buffers, striding over the job list; `jobs`
+// itself lives in pinned host memory.
+// The host places each buffer in staging at its source's alignment phase (mod 16) whenever the
+// source is aligned to its element width, so the body moves as aligned 16-byte words and only
+// a head and a tail of < 16 bytes go byte by byte.  Other phase pairs fall back to 4-byte words
+// or bytes.  Only [src, src + bytes) is read and [dst, dst + bytes) written.
+template <typename V>
+__device__ __forceinline__ void gather_words(const uint8_t* src, uint8_t* dst, uint64_t n) {
+  constexpr uint32_t W = sizeof(V);
+  const uint64_t lead = (W - (reinterpret_cast<uintptr_t>(src) & (W - 1))) & (W - 1);
+  const uint64_t head = n < lead ? n : lead;
+  if (threadIdx.x < head) dst[threadIdx.x] = src[threadIdx.x];
+  const uint64_t nv = (n - head) / W;
+  const V* sv = reinterpret_cast<const V*>(src + head);
+  V* dv = reinterpret_cast<V*>(dst + head);
+  constexpr int U = 4;  // loads in flight per thread
+  uint64_t i = threadIdx.x;
+  for (; i + (U - 1) * 256 < nv; i += U * 256) {
+    V v[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) v[u] = sv[i + u * 256];
+#pragma unroll
+    for (int u = 0; u < U; u++) dv[i + u * 256] = v[u];
+  }
+  for (; i < nv; i += 256) dv[i] = sv[i];
+  for (uint64_t j = head + nv * W + threadIdx.x; j < n; j += 256) dst[j] = src[j];
+}
+
+__global__ void __launch_bounds__(256) k_gather(const HostCopy* __restrict__ jobs, uint32_t n_jobs) {
+  for (uint32_t b = blockIdx.x; b < n_jobs; b += gridDim.x) {
+    const HostCopy job = jobs[b];
+    const uintptr_t phase = reinterpret_cast<uintptr_t>(job.src) ^ reinterpret_cast<uintptr_t>(job.dst);
+    if ((phase & 15) == 0) {
+      gather_words<uint4>(job.src, job.dst, job.bytes);
+    } else if ((phase & 3) == 0) {
+      gather_words<uint32_t>(job.src, job.dst, job.bytes);
+    } else {
+      for (uint64_t j = threadIdx.x; j < job.bytes; j += 256) job.dst[j] = job.src[j];
+    }
+  }
+}
+
+// =======================================================================================
 // launch helpers
 cudaError_t launch_hash_count(const SchemaDesc& sd, const FlushDesc& fd, cudaStream_t st) {
   const size_t sm = fd.hist_in_smem ? sizeof(uint32_t) * sd.P * (1 + sd.n_str) : 0;
@@ -925,6 +969,21 @@ cudaError_t launch_plan(const SchemaDesc& sd, const FlushDesc& fd, cudaStream_t 
     if (e != cudaSuccess) return e;
   }
   k_plan_scan<<<1, kPlanThreads, 0, st>>>(sd, fd);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather(const HostCopy* jobs, uint32_t n_jobs, cudaStream_t st) {
+  if (n_jobs == 0) return cudaSuccess;
+  // two CTAs per SM stride over the buffers: enough loads in flight to fill the host link
+  // while leaving the SMs to the device pass that runs concurrently
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 152;
+  }
+  const uint32_t grid = n_jobs < (uint32_t)(2 * sms) ? n_jobs : (uint32_t)(2 * sms);
+  k_gather<<<grid, 256, 0, st>>>(jobs, n_jobs);
   return cudaGetLastError();
 }
 

@@ -172,6 +172,31 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
   st = Cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
   if (!st.ok()) return st;
   {
+    // host reads get the higher priority: their CTAs are scheduled ahead of a running pass's
+    int least = 0, greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    st = Cuda(cudaStreamCreateWithPriority(&cstream_, cudaStreamNonBlocking, greatest), "cudaStreamCreate");
+    if (!st.ok()) return st;
+  }
+  st = Cuda(cudaStreamCreateWithFlags(&ostream_, cudaStreamNonBlocking), "cudaStreamCreate");
+  if (!st.ok()) return st;
+  st = Cuda(cudaEventCreateWithFlags(&gather_ev_, cudaEventDisableTiming), "cudaEventCreate");
+  if (!st.ok()) return st;
+  if (opts_.input_kind == GZ_INPUT_HOST && opts_.host_read == GZ_HOST_READ_AUTO) {
+    // kernels may dereference any host address when the device walks the host page tables
+    // (a coherent CPU-GPU link): host inputs are then read by k_gather, no CPU copy
+    int pageable = 0, host_tables = 0;
+    cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device_);
+    cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device_);
+    direct_ = pageable != 0 && host_tables != 0;
+  }
+  if (direct_) {
+    jobs_cap_ = size_t(1) << 20;  // 24 MiB of descriptors: a refill waits for the device
+    st = Cuda(cudaHostAlloc(reinterpret_cast<void**>(&h_jobs_), jobs_cap_ * sizeof(HostCopy),
+                            cudaHostAllocDefault), "cudaHostAlloc(gather jobs)");
+    if (!st.ok()) return st;
+  }
+  {
     cudaMemPool_t pool;
     if (cudaDeviceGetDefaultMemPool(&pool, device_) == cudaSuccess) {
       uint64_t thr = UINT64_MAX;
@@ -214,7 +239,9 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
 }
 
 Splitter::~Splitter() {
+  if (cstream_) cudaStreamSynchronize(cstream_);
   if (stream_) cudaStreamSynchronize(stream_);
+  if (ostream_) cudaStreamSynchronize(ostream_);
   for (auto& f : flushes_) {
     if (f.d_out) cudaFree(f.d_out);
     PinnedRelease(f.h_block);
@@ -233,6 +260,10 @@ Splitter::~Splitter() {
   }
   if (d_scratch_) cudaFree(d_scratch_);
   if (d_state_) cudaFree(d_state_);
+  if (h_jobs_) cudaFreeHost(h_jobs_);
+  if (gather_ev_) cudaEventDestroy(gather_ev_);
+  if (cstream_) cudaStreamDestroy(cstream_);
+  if (ostream_) cudaStreamDestroy(ostream_);
   if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -267,7 +298,9 @@ uint32_t Splitter::SplitBatchSize(int32_t num_rows, const std::vector<const int3
 
 Status Splitter::EnsureStaging(size_t bytes) {
   if (bytes <= stage_cap_) return Status::OK();
-  Status st = Cuda(cudaStreamSynchronize(stream_), "sync");
+  Status st = FinishHostReads();
+  if (!st.ok()) return st;
+  st = Cuda(cudaStreamSynchronize(stream_), "sync");
   if (!st.ok()) return st;
   size_t cap = AlignUp(std::max<size_t>(bytes, (size_t)opts_.flush_bytes + (8u << 20)), 1 << 20);
   for (int i = 0; i < 2; i++) {
@@ -275,8 +308,10 @@ Status Splitter::EnsureStaging(size_t bytes) {
     if (d_stage_[i]) cudaFree(d_stage_[i]);
     h_stage_[i] = nullptr;
     d_stage_[i] = nullptr;
-    st = Cuda(cudaHostAlloc(&h_stage_[i], cap, cudaHostAllocDefault), "cudaHostAlloc(stage)");
-    if (!st.ok()) return st;
+    if (!direct_) {
+      st = Cuda(cudaHostAlloc(&h_stage_[i], cap, cudaHostAllocDefault), "cudaHostAlloc(stage)");
+      if (!st.ok()) return st;
+    }
     st = Cuda(cudaMalloc(&d_stage_[i], cap), "cudaMalloc(stage)");
     if (!st.ok()) return st;
     stage_busy_[i] = false;
@@ -286,6 +321,45 @@ Status Splitter::EnsureStaging(size_t bytes) {
 }
 
 Status Splitter::Split(int32_t num_rows, const int64_t* addrs, const int64_t* sizes, int32_t n) {
+  Status st = SplitOne(num_rows, addrs, sizes, n);
+  Status fin = FinishHostReads();
+  return st.ok() ? fin : st;
+}
+
+Status Splitter::SplitBatches(int32_t n_batches, const int32_t* rows, const int64_t* addrs,
+                              const int64_t* sizes, int32_t n) {
+  Status st;
+  for (int32_t i = 0; i < n_batches && st.ok(); i++)
+    st = SplitOne(rows[i], addrs + (size_t)i * n, sizes + (size_t)i * n, n);
+  Status fin = FinishHostReads();
+  return st.ok() ? fin : st;
+}
+
+// Launches k_gather over the descriptors queued since the last launch.
+Status Splitter::LaunchGather() {
+  const size_t n = jobs_end_ - jobs_begin_;
+  if (n == 0) return Status::OK();
+  Status st = Cuda(launch_gather(h_jobs_ + jobs_begin_, (uint32_t)n, cstream_), "k_gather");
+  jobs_begin_ = jobs_end_;
+  gather_pending_bytes_ = 0;
+  return st;
+}
+
+// Waits until every queued host read has landed in device staging; afterwards the caller's
+// host buffers are no longer needed and the descriptor ring starts over.
+Status Splitter::FinishHostReads() {
+  if (!direct_ || jobs_end_ == 0) return Status::OK();
+  Status st = LaunchGather();
+  if (!st.ok()) return st;
+  st = Cuda(cudaEventRecord(gather_ev_, cstream_), "event");
+  if (!st.ok()) return st;
+  st = Cuda(cudaEventSynchronize(gather_ev_), "host reads");
+  if (!st.ok()) return st;
+  jobs_begin_ = jobs_end_ = 0;
+  return Status::OK();
+}
+
+Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t* sizes, int32_t n) {
   if (stopped_) return Status::Error(GZ_INVALID, "split after stop");
   if (n < n_bufs_expected_) return Status::Error(GZ_INVALID, "insufficient number of in_buf_addrs");
   if (num_rows < 0) return Status::Error(GZ_INVALID, "negative num_rows");
@@ -341,6 +415,8 @@ Status Splitter::Split(int32_t num_rows, const int64_t* addrs, const int64_t* si
     }
   }
   for (int i = 0; i < n_bufs_expected_; i++) batch_bytes += AlignUp(need_[i].bytes, 64);
+  // staging room for buffers kept at their source's 16-byte phase (k_gather)
+  const size_t phase_slack = direct_ ? (size_t)64 * n_bufs_expected_ : 0;
 
   // CalculateSplitBatchSize.  Its row count depends on the empirical binary sizes only when
   // offheap_per_task > 0; those sizes are learned from the first batch with rows (where every
@@ -381,7 +457,7 @@ Status Splitter::Split(int32_t num_rows, const int64_t* addrs, const int64_t* si
                              AlignUp(sizeof(ColPtr) * NB1 * C, 256) + 256;
   if (!pending_.empty() &&
       (pending_bytes_ + batch_bytes > (uint64_t)opts_.flush_bytes || NB1 > (size_t)kMaxBatchesPerFlush ||
-       (host_in && used_ + batch_bytes + tables_need > stage_cap_))) {
+       (host_in && used_ + batch_bytes + (direct_ ? phase_slack : tables_need) > stage_cap_))) {
     st = Flush();
     if (!st.ok()) return st;
   }
@@ -396,14 +472,21 @@ Status Splitter::Split(int32_t num_rows, const int64_t* addrs, const int64_t* si
   if (host_in) {
     const size_t tables_one = AlignUp(sizeof(BatchDesc), 256) + AlignUp(sizeof(TileDesc) * ntiles, 256) +
                               AlignUp(sizeof(ColPtr) * C, 256) + 256;
-    st = EnsureStaging(batch_bytes + tables_one);
+    st = EnsureStaging(batch_bytes + (direct_ ? phase_slack : tables_one));
     if (!st.ok()) return st;
     if (pending_.empty() && stage_busy_[cur_]) {
-      st = Cuda(cudaEventSynchronize(stage_ev_[cur_]), "stage wait");
+      // the device pass that last read this staging buffer must be done before it is refilled
+      if (direct_) st = Cuda(cudaStreamWaitEvent(cstream_, stage_ev_[cur_], 0), "stage wait");
+      else st = Cuda(cudaEventSynchronize(stage_ev_[cur_]), "stage wait");
       if (!st.ok()) return st;
       stage_busy_[cur_] = false;
     }
-    // copy the batch into pinned staging; device addresses point into the device twin
+    if (direct_ && jobs_end_ + (size_t)n_bufs_expected_ > jobs_cap_) {
+      st = FinishHostReads();
+      if (!st.ok()) return st;
+    }
+    // the batch goes to device staging: read there by k_gather (direct_) or copied by the CPU
+    // into the pinned twin; device addresses point into the device buffer
     jobs_.clear();
     size_t copy_bytes = 0;
     for (size_t f = 0; f < C; f++) {
@@ -416,10 +499,20 @@ Status Splitter::Split(int32_t num_rows, const int64_t* addrs, const int64_t* si
         for (int j = 0; j < nbuf; j++) {
           const Need& nd = need_[b0 + j];
           if (nd.bytes == 0) continue;
-          jobs_.push_back(CopyJob{h_stage_[cur_] + used_, nd.src, nd.bytes});
+          size_t phase = 0;
+          if (direct_) {
+            // same 16-byte phase as the source when that keeps the elements aligned
+            const uintptr_t sp = reinterpret_cast<uintptr_t>(nd.src);
+            const uintptr_t elem = j == 0 ? 1 : IsBinary(t) ? (j == 1 ? 4 : 1)
+                                 : t == GZ_TYPE_BOOL ? 1 : (uintptr_t)ByteWidth(t);
+            if (sp % elem == 0) phase = sp & 15;
+            h_jobs_[jobs_end_++] = HostCopy{nd.src, d_stage_[cur_] + used_ + phase, nd.bytes};
+          } else {
+            jobs_.push_back(CopyJob{h_stage_[cur_] + used_, nd.src, nd.bytes});
+          }
           copy_bytes += nd.bytes;
-          const uint8_t* dptr = d_stage_[cur_] + used_;
-          used_ += AlignUp(nd.bytes, 64);
+          const uint8_t* dptr = d_stage_[cur_] + used_ + phase;
+          used_ += AlignUp(phase + nd.bytes, 64);
           if (j == 0) cp.validity = dptr;
           else if (IsBinary(t) && j == 1) cp.offsets = reinterpret_cast<const int32_t*>(dptr);
           else {
@@ -431,7 +524,16 @@ Status Splitter::Split(int32_t num_rows, const int64_t* addrs, const int64_t* si
       }
       cols[f] = cp;
     }
-    ParallelCopy(jobs_, copy_bytes);
+    if (direct_) {
+      stat_h2d_bytes_ += (int64_t)copy_bytes;
+      gather_pending_bytes_ += copy_bytes;
+      if (gather_pending_bytes_ >= (32u << 20)) {
+        st = LaunchGather();
+        if (!st.ok()) return st;
+      }
+    } else {
+      ParallelCopy(jobs_, copy_bytes);
+    }
   } else {
     for (size_t f = 0; f < C; f++) {
       ColPtr cp{nullptr, nullptr, nullptr, 0};
@@ -630,7 +732,8 @@ Status Splitter::Flush() {
   const size_t tb_tiles = AlignUp(sizeof(TileDesc) * T, 256);
   const size_t tb_cols = AlignUp(sizeof(ColPtr) * NB * C, 256);
   const size_t tb_total = tb_batches + tb_tiles + tb_cols;
-  const size_t s_tab = host_in ? 0 : take(tb_total);
+  const bool staged_tables = host_in && !direct_;  // tables travel with the pinned staging copy
+  const size_t s_tab = staged_tables ? 0 : take(tb_total);
   st = EnsureScratch(so);
   if (!st.ok()) return st;
   uint8_t* S = d_scratch_;
@@ -677,7 +780,7 @@ Status Splitter::Flush() {
   // tables into staging (host inputs) or a pinned table buffer
   uint8_t* htab;
   uint8_t* dtab;
-  if (host_in) {
+  if (staged_tables) {
     used_ = AlignUp(used_, 256);
     if (used_ + tb_total > stage_cap_) return Status::Error(GZ_INVALID, "staging overflow");
     htab = h_stage_[cur_] + used_;
@@ -705,7 +808,7 @@ Status Splitter::Flush() {
   memcpy(htab + tb_batches, tiles.data(), sizeof(TileDesc) * T);
   ColPtr* hc = reinterpret_cast<ColPtr*>(htab + tb_batches + tb_tiles);
   memcpy(hc, pending_cols_.data(), sizeof(ColPtr) * NB * C);
-  if (host_in) {
+  if (staged_tables) {
     st = Cuda(cudaMemcpyAsync(d_stage_[cur_], h_stage_[cur_], used_, cudaMemcpyHostToDevice, stream_), "H2D");
     stat_h2d_bytes_ += (int64_t)used_;
     if (!st.ok()) return st;
@@ -713,6 +816,14 @@ Status Splitter::Flush() {
     if (!st.ok()) return st;
     stage_busy_[cur_] = true;
   } else {
+    if (direct_) {  // the pass reads what k_gather wrote
+      st = LaunchGather();
+      if (!st.ok()) return st;
+      st = Cuda(cudaEventRecord(gather_ev_, cstream_), "event");
+      if (!st.ok()) return st;
+      st = Cuda(cudaStreamWaitEvent(stream_, gather_ev_, 0), "wait gather");
+      if (!st.ok()) return st;
+    }
     dtab = S + s_tab;
     st = Cuda(cudaMemcpyAsync(dtab, htab, tb_total, cudaMemcpyHostToDevice, stream_), "H2D tables");
     if (!st.ok()) return st;
@@ -753,6 +864,11 @@ Status Splitter::Flush() {
   st = Cuda(launch_scatter(sd_, fd, stream_), "k_scatter");
   if (!st.ok()) return st;
   cudaEventRecord(fr.ev[3], stream_);
+  if (direct_) {  // staging is free again once the kernels are done
+    st = Cuda(cudaEventRecord(stage_ev_[cur_], stream_), "event");
+    if (!st.ok()) return st;
+    stage_busy_[cur_] = true;
+  }
   // the last batch's call flag, for the empirical-size bookkeeping
   st = Cuda(cudaMemcpyAsync(d_call_, fd.call_flags + (NB - 1), 4, cudaMemcpyDeviceToDevice, stream_), "D2D");
   if (!st.ok()) return st;
@@ -793,10 +909,13 @@ Status Splitter::MoveFlushToHost(FlushRec& f) {
   if (f.on_host) return Status::OK();
   f.h_block = PinnedAcquire(f.out_bytes);
   if (!f.h_block.ptr) return Status::Error(GZ_OOM, "pinned host memory for partition data");
-  Status st = Cuda(cudaMemcpyAsync(f.h_block.ptr, f.d_out, f.out_bytes, cudaMemcpyDeviceToHost, stream_),
-                   "D2H out");
+  // on its own stream, after the pass's kernels, so the copy overlaps the next pass
+  Status st = Cuda(cudaStreamWaitEvent(ostream_, f.ev[3], 0), "wait pass");
   if (!st.ok()) return st;
-  st = Cuda(cudaFreeAsync(f.d_out, stream_), "cudaFreeAsync");
+  st = Cuda(cudaMemcpyAsync(f.h_block.ptr, f.d_out, f.out_bytes, cudaMemcpyDeviceToHost, ostream_),
+            "D2H out");
+  if (!st.ok()) return st;
+  st = Cuda(cudaFreeAsync(f.d_out, ostream_), "cudaFreeAsync");
   if (!st.ok()) return st;
   f.d_out = nullptr;
   f.on_host = true;
@@ -806,7 +925,11 @@ Status Splitter::MoveFlushToHost(FlushRec& f) {
 }
 
 Status Splitter::SyncAndCheck() {
-  Status st = Cuda(cudaStreamSynchronize(stream_), "device work");
+  Status st = Cuda(cudaStreamSynchronize(cstream_), "host reads");
+  if (!st.ok()) return st;
+  st = Cuda(cudaStreamSynchronize(stream_), "device work");
+  if (!st.ok()) return st;
+  st = Cuda(cudaStreamSynchronize(ostream_), "partition data to host");
   if (!st.ok()) return st;
   int32_t err = 0;
   st = Cuda(cudaMemcpy(&err, d_err_, 4, cudaMemcpyDeviceToHost), "read error word");
@@ -1046,7 +1169,7 @@ Status Splitter::Stop() {
     st = MoveFlushToHost(f);
     if (!st.ok()) return st;
   }
-  st = Cuda(cudaStreamSynchronize(stream_), "D2H partition data");
+  st = Cuda(cudaStreamSynchronize(ostream_), "D2H partition data");
   if (!st.ok()) return st;
   total_spill_time_ += NowNs() - m0;
   // write the data file, partitions in order (Stop, splitter.cc:395-437)
@@ -1116,7 +1239,7 @@ Status Splitter::SpillFixedSize(int64_t size, int64_t* actual) {
     st = MoveFlushToHost(f);
     if (!st.ok()) return st;
   }
-  st = Cuda(cudaStreamSynchronize(stream_), "D2H partition data");
+  st = Cuda(cudaStreamSynchronize(ostream_), "D2H partition data");
   if (!st.ok()) return st;
   // SpillLargestPartition up to 5 times (splitter.cc:741-799): largest cached body bytes
   int64_t cur = 0;

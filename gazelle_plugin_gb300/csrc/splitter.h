@@ -2,9 +2,11 @@
 // interface (native-sql-engine/cpp/src/shuffle/splitter.h:55-126): Make / Split / Stop /
 // SpillFixedSize / SetCompressType / CompressedSize and the metric getters.
 //
-// Split() only gathers the batch (host inputs are copied into a pinned staging buffer
-// before it returns, as the JNI contract requires); every `flush_bytes` of input one device
-// pass runs the three kernels on the splitter's stream.  Emission decisions are made on the
+// Split() only gathers the batch: host inputs are read before it returns, as the JNI contract
+// requires, either by the GPU itself over a coherent host link (k_gather into device staging,
+// where the device can read pageable host memory through the host page tables) or by a CPU
+// copy into pinned staging; every `flush_bytes` of input one device pass runs the kernels on
+// the splitter's stream.  Emission decisions are made on the
 // device by k_plan, so Split never waits for the GPU.  Stop() finishes the device work,
 // assembles every emitted partition batch from the flush outputs and writes the Arrow IPC
 // data file in partition order.
@@ -45,7 +47,12 @@ class Splitter {
                      std::unique_ptr<Splitter>* out);
   ~Splitter();
 
+  // One batch; host inputs are fully read when it returns.
   Status Split(int32_t num_rows, const int64_t* addrs, const int64_t* sizes, int32_t n);
+  // Split(rows[i], addrs + i * n, sizes + i * n, n) for every batch; host inputs are fully
+  // read when it returns (also on error).
+  Status SplitBatches(int32_t n_batches, const int32_t* rows, const int64_t* addrs,
+                      const int64_t* sizes, int32_t n);
   Status CompressedSize(int32_t num_rows, const int64_t* addrs, const int64_t* sizes, int32_t n,
                         int64_t* out);
   Status Stop();
@@ -127,6 +134,9 @@ class Splitter {
   Status Cuda(cudaError_t e, const char* what);
   Status EnsureScratch(size_t bytes_needed);
   Status EnsureStaging(size_t bytes);
+  Status SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t* sizes, int32_t n);
+  Status LaunchGather();
+  Status FinishHostReads();
   Status PinnedMeta(size_t bytes, uint32_t** out);
   Status Flush();
   Status SyncAndCheck();
@@ -164,7 +174,15 @@ class Splitter {
   uint8_t* d_scratch_ = nullptr;
   size_t scratch_cap_ = 0;
 
-  // staging (host inputs): double-buffered pinned host + device
+  // staging (host inputs): double-buffered device buffers, filled by k_gather (direct_) or
+  // by H2D copies of pinned host twins
+  bool direct_ = false;              // the device reads pageable host memory (coherent link)
+  cudaStream_t cstream_ = nullptr;   // k_gather
+  cudaStream_t ostream_ = nullptr;   // partition data to host
+  cudaEvent_t gather_ev_ = nullptr;
+  HostCopy* h_jobs_ = nullptr;       // pinned ring of k_gather descriptors
+  size_t jobs_cap_ = 0, jobs_begin_ = 0, jobs_end_ = 0;
+  size_t gather_pending_bytes_ = 0;
   uint8_t* h_stage_[2] = {nullptr, nullptr};
   uint8_t* d_stage_[2] = {nullptr, nullptr};
   size_t stage_cap_ = 0;

@@ -20,6 +20,7 @@ LIB_PATH = os.path.join(HERE, "libgzsplit.so")
 
 GZ_OK, GZ_INVALID, GZ_OOM, GZ_IO, GZ_NOT_IMPLEMENTED, GZ_TIMEOUT, GZ_CUDA = range(7)
 GZ_INPUT_HOST, GZ_INPUT_DEVICE_RETAINED = 0, 1
+GZ_HOST_READ_AUTO, GZ_HOST_READ_CPU_COPY = 0, 1
 _STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "OOM", 3: "IO", 4: "NOT_IMPLEMENTED", 5: "TIMEOUT",
                  6: "CUDA"}
 
@@ -49,6 +50,8 @@ class GzSplitOptions(ctypes.Structure):
         ("device_budget", ctypes.c_int64),
         ("data_file", ctypes.c_char_p),
         ("local_dirs", ctypes.c_char_p),
+        ("host_read", ctypes.c_int32),
+        ("reserved0", ctypes.c_int32),
     ]
 
 

@@ -60,6 +60,13 @@ typedef enum GzInputKind {
                                    until gz_split_stop returns (resident inputs) */
 } GzInputKind;
 
+/* How host inputs (GZ_INPUT_HOST) reach the device before gz_split_split returns. */
+typedef enum GzHostRead {
+  GZ_HOST_READ_AUTO = 0,     /* the GPU reads the caller's buffers itself when it can walk the
+                                host page tables (coherent CPU-GPU link), else as CPU_COPY */
+  GZ_HOST_READ_CPU_COPY = 1  /* CPU copy into pinned staging, then one copy per device pass */
+} GzHostRead;
+
 /* SplitOptions (native-sql-engine/cpp/src/shuffle/type.h:39-59) plus device knobs.
  * Initialise with gz_split_default_options(). */
 typedef struct GzSplitOptions {
@@ -83,6 +90,8 @@ typedef struct GzSplitOptions {
   const char* data_file;             /* written at Stop; NULL/"" keeps the bytes in memory */
   const char* local_dirs;            /* comma separated spill dirs (unused: spills go to
                                         pinned host memory) */
+  int32_t host_read;                 /* GzHostRead, default GZ_HOST_READ_AUTO */
+  int32_t reserved0;
 } GzSplitOptions;
 
 /* SplitResult (native-sql-engine/core/src/main/java/com/intel/oap/vectorized/SplitResult.java:21-39).

@@ -102,6 +102,72 @@ def test_flush_grouping_does_not_change_bytes(flush_bytes):
     assert_same(res, data, ref)
 
 
+@pytest.mark.parametrize("host_read,flush_mb", [(S.GZ_HOST_READ_AUTO, 4), (S.GZ_HOST_READ_AUTO, 64),
+                                               (S.GZ_HOST_READ_CPU_COPY, 4)])
+def test_host_read_modes_batched_call(host_read, flush_mb):
+    """Both ways host inputs reach the device (the GPU reading host memory itself, or a CPU copy
+    into pinned staging), many batches per call, staging buffers reused across passes."""
+    batches = W.c2_batches(11, 100, 4096)
+    ref = O.run_oracle(W.C2_SCHEMA, batches, 200, W.C2_KEYS, buffer_size=1024)
+    w = S.ShuffleSplitterJniWrapper()
+    h = w.make(S.NativePartitioning("hash", 200, None, W.C2_KEYS, list(W.C2_SCHEMA)),
+               bufferSize=1024, writeSchema=False, host_read=host_read, flush_bytes=flush_mb << 20,
+               keep_output_on_device=0)
+    try:
+        rows = np.array([b.num_rows for b in batches], np.int32)
+        pairs = [b.addrs_sizes() for b in batches]
+        w.splitBatches(h, rows, np.stack([a for a, _ in pairs]), np.stack([z for _, z in pairs]))
+        res = w.stop(h)
+        data = w.data(h)
+    finally:
+        w.close(h)
+    assert_same(res, data, ref)
+
+
+@pytest.mark.parametrize("shift", [1, 4, 8, 13])
+def test_unaligned_host_buffers(shift):
+    """Host buffers at every alignment: each buffer of each batch starts `shift` + (its index)
+    bytes past a 64-byte boundary, so values, offsets and characters arrive at all phases."""
+    batches = W.c2_batches(13, 6, 3000)
+    ref = O.run_oracle(W.C2_SCHEMA, batches, 200, W.C2_KEYS, buffer_size=2048)
+    keep = []
+    shifted = []
+    for b in batches:
+        bufs = []
+        for i, x in enumerate(b.buffers):
+            raw = x.view(np.uint8).ravel()
+            off = (shift + i) % 64
+            host = np.zeros(raw.nbytes + 128, np.uint8)
+            base = (-host.ctypes.data) % 64 + off
+            host[base:base + raw.nbytes] = raw
+            keep.append(host)
+            bufs.append(host[base:base + raw.nbytes])
+        shifted.append(W.Batch(b.num_rows, bufs))
+    res, data = gpu_split(W.C2_SCHEMA, shifted, 200, W.C2_KEYS, buffer_size=2048)
+    assert_same(res, data, ref)
+
+
+def test_host_buffers_reusable_when_split_returns():
+    """The JNI contract: the writer may overwrite or free a batch's buffers as soon as split
+    returns, so every host byte must have been read by then."""
+    batches = W.c1_batches(12, 20, 4096)
+    ref = O.run_oracle(W.C1_SCHEMA, batches, 8, W.C1_KEYS)
+    w = S.ShuffleSplitterJniWrapper()
+    h = w.make(S.NativePartitioning("hash", 8, None, W.C1_KEYS, list(W.C1_SCHEMA)), writeSchema=False)
+    try:
+        for b in batches:
+            work = W.Batch(b.num_rows, [x.copy() for x in b.buffers])
+            addrs, sizes = work.addrs_sizes()
+            w.split(h, work.num_rows, addrs, sizes)
+            for x in work.buffers:
+                x.view(np.uint8)[:] = 0xA5
+        res = w.stop(h)
+        data = w.data(h)
+    finally:
+        w.close(h)
+    assert_same(res, data, ref)
+
+
 def test_output_copied_to_host_every_pass():
     batches = W.c2_batches(5, 24, 4096)
     ref = O.run_oracle(W.C2_SCHEMA, batches, 200, W.C2_KEYS, buffer_size=512)
