@@ -40,6 +40,9 @@ WORKLOAD = ("wide fact-table split: 200M rows, 4096-row batches, 16 columns "
             "(4 int64 keys, 4 float64, 2 int32, 3 utf8 flags, 3 utf8 comments), "
             "2% nulls, hash on keys 0-1, 200 partitions")
 BATCH_ROWS = 4096
+# DRAM bytes that one k_scatter launch moves per algorithmic byte, from an ncu capture of one
+# full 512 MiB pass of this workload (profiles/k_scatter_wide_fact_table.md).
+K_SCATTER_DRAM_PER_ALG_BYTE = 1.010
 PARTITIONS = 200
 KEYS = [0, 1]
 
@@ -358,7 +361,12 @@ def run_gpu(args):
     scat_gbs = alg_bytes / (k_scat / 1e3) / 1e9
     roofline = {"bound": "hbm", "kernel": "k_scatter", "achieved": scat_gbs, "peak": peak,
                 "unit": "GB/s", "frac": scat_gbs / peak, "peak_source": peak_kind,
-                "traffic": args.traffic_per_launch,
+                "traffic": (args.traffic_per_launch or
+                            K_SCATTER_DRAM_PER_ALG_BYTE * alg_bytes / max(flushes, 1)),
+                "traffic_source": ("--traffic-per-launch" if args.traffic_per_launch else
+                                   "ncu dram__bytes_read.sum + dram__bytes_write.sum of a full "
+                                   "512 MiB pass (1.085 GB for 1.074 GB algorithmic), scaled "
+                                   "to this run's average pass"),
                 "launches_per_step": flushes,
                 "algorithmic_bytes_per_launch": alg_bytes / max(flushes, 1),
                 "avg_launch_ms": k_scat / max(flushes, 1)}
