@@ -456,6 +456,7 @@ constexpr int kStageBytes = kTileRows * 8;          // one 8-byte column slice
 constexpr int kStageValid = kTileRows / 8;           // its validity bits
 constexpr int kStageSlot = kStageBytes + 16 + kStageValid + 16;
 constexpr int kCharStage = 32768;                    // a tile's source characters of one column
+constexpr int kCharSlack = 32;                       // read-only slack around the staged characters
 constexpr uint32_t kSpinLimit = 1u << 26;
 
 // One stable LSD pass over 8 bits of the keys.
@@ -630,6 +631,36 @@ __device__ __forceinline__ void copy_string(uint8_t* dst, const uint8_t* src, ui
   }
 }
 
+// One string whose source bytes are in shared memory: `len` bytes from `src` to global `dst`.
+// Up to 3 head bytes bring the destination to a 4-byte boundary, then whole aligned words, each a
+// funnel shift of two aligned source words, then up to 3 tail bytes.  The aligned source words
+// may reach up to 3 bytes before `src` and 7 bytes past `src + len`: the staging buffer keeps
+// that slack, and those bytes are never stored.
+__device__ __forceinline__ void copy_string_smem(uint8_t* dst, const uint8_t* src, uint32_t len) {
+  const uintptr_t d = reinterpret_cast<uintptr_t>(dst);
+  const uint32_t lead = (uint32_t)((4 - (d & 3)) & 3);
+  const uint32_t head = len < lead ? len : lead;
+#pragma unroll
+  for (uint32_t t = 0; t < 3; t++)
+    if (t < head) dst[t] = src[t];
+  const uint32_t nw = (len - head) >> 2;
+  const uintptr_t s = reinterpret_cast<uintptr_t>(src) + head;
+  const uint32_t* sw = reinterpret_cast<const uint32_t*>(s & ~uintptr_t(3));
+  const uint32_t sh = (uint32_t)(s & 3) * 8;
+  uint32_t* dw = reinterpret_cast<uint32_t*>(d + head);
+  uint32_t lo = sw[0];
+#pragma unroll 4
+  for (uint32_t k = 0; k < nw; k++) {
+    const uint32_t hi = sw[k + 1];
+    dw[k] = __funnelshift_r(lo, hi, sh);
+    lo = hi;
+  }
+  const uint32_t done = head + 4 * nw;
+#pragma unroll
+  for (uint32_t t = 0; t < 3; t++)
+    if (done + t < len) dst[done + t] = src[done + t];
+}
+
 }  // namespace
 
 __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd, const FlushDesc fd) {
@@ -639,8 +670,8 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
   __shared__ uint32_t s_bad;
   const int T = kTileRows;
   uint8_t* stage0 = ssm;                                    // [2][kStageSlot]
-  uint8_t* cstage = ssm + 2 * kStageSlot;                   // [kCharStage + 16]
-  uint16_t* kA = reinterpret_cast<uint16_t*>(ssm + 2 * kStageSlot + kCharStage + 16);
+  uint8_t* cstage = ssm + 2 * kStageSlot + kCharSlack;      // [kCharStage + 16] inside slack
+  uint16_t* kA = reinterpret_cast<uint16_t*>(ssm + 2 * kStageSlot + kCharStage + 16 + 2 * kCharSlack);
   uint16_t* pA = kA + T;
   uint16_t* kB = pA + T;
   uint16_t* pB = kB + T;
@@ -886,9 +917,14 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
         buf_lo = reinterpret_cast<uintptr_t>(sbase);
         buf_hi = buf_lo + cbytes;
       }
-      for (int j = threadIdx.x; j < n; j += blockDim.x) {
-        const uint32_t len = S[j + 1] - S[j];
-        copy_string(ochars + rt1[rs[j]] + S[j], cbase + oin[ps[j]], len, buf_lo, buf_hi);
+      if (staged) {
+        for (int j = threadIdx.x; j < n; j += blockDim.x)
+          copy_string_smem(ochars + rt1[rs[j]] + S[j], cbase + oin[ps[j]], S[j + 1] - S[j]);
+      } else {
+        for (int j = threadIdx.x; j < n; j += blockDim.x) {
+          const uint32_t len = S[j + 1] - S[j];
+          copy_string(ochars + rt1[rs[j]] + S[j], cbase + oin[ps[j]], len, buf_lo, buf_hi);
+        }
       }
     }
     __syncthreads();  // everyone is done with this slot
@@ -989,7 +1025,7 @@ cudaError_t launch_gather(const HostCopy* jobs, uint32_t n_jobs, cudaStream_t st
 
 size_t scatter_smem_bytes() {
   const int T = kTileRows;
-  return 2 * kStageSlot + kCharStage + 16 + 4 * sizeof(uint16_t) * T + sizeof(uint32_t) * T +
+  return 2 * kStageSlot + kCharStage + 16 + 2 * kCharSlack + 4 * sizeof(uint16_t) * T + sizeof(uint32_t) * T +
          sizeof(uint16_t) * T + sizeof(uint32_t) * (T + 1) + 2 * sizeof(uint32_t) * T +
          sizeof(uint16_t) * kW * 256;
 }
