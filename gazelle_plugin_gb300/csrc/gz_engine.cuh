@@ -45,6 +45,7 @@ struct SchemaDesc {
   int32_t arr_kind[kMaxCols];   // ColKind
   int32_t arr_width[kMaxCols];  // value bytes of a fixed column
   int32_t arr_str[kMaxCols];    // binary ordinal k of a binary column, -1 otherwise
+  int32_t order[kMaxCols];      // order in which k_scatter processes the array columns
 };
 
 // Device addresses of one input column of one batch.  offsets only for binary columns;
@@ -103,6 +104,7 @@ struct FlushDesc {
   uint32_t* vpos;     // [n_tiles][P] validity bit offset (pieces start on 64-bit boundaries)
   uint32_t* sbyte;    // [n_tiles][n_str][P] byte offset inside the partition's segment
   uint32_t* nullcnt;  // [n_batches][n_array]
+  int2* crange;       // [n_tiles][n_str] offsets of the tile's first and one-past-last row
 
   // per-partition results of this flush
   uint32_t* rows_f;   // [P]

@@ -155,6 +155,8 @@ __global__ void __launch_bounds__(256) k_hash_count(const SchemaDesc sd, const F
       const ColPtr c = s_str[k];
       const int32_t o0 = c.offsets[r], o1 = c.offsets[r + 1];
       uint32_t len = (uint32_t)(o1 - o0);
+      if (i == 0) fd.crange[(size_t)blockIdx.x * nstr + k].x = o0;
+      if (i + 1 == tile.nrows) fd.crange[(size_t)blockIdx.x * nstr + k].y = o1;
       if (o0 < 0 || o1 < o0 || (uint64_t)o1 > c.values_bytes) {
         bad = true;
         len = 0;
@@ -452,11 +454,12 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan_scan(const SchemaDesc sd,
 //      aligned 32-bit destination words built by funnel shifts from aligned source words.
 namespace {
 constexpr int kW = kScatterThreads / 32;
-constexpr int kStageBytes = kTileRows * 8;          // one 8-byte column slice
-constexpr int kStageValid = kTileRows / 8;           // its validity bits
-constexpr int kStageSlot = kStageBytes + 16 + kStageValid + 16;
-constexpr int kCharStage = 32768;                    // a tile's source characters of one column
-constexpr int kCharSlack = 32;                       // read-only slack around the staged characters
+constexpr int kSlots = 4;                            // column slices in flight
+constexpr int kStageBytes = kTileRows * 8 + 32;      // one 8-byte column slice, granule-aligned
+constexpr int kStageValid = kTileRows / 8 + 32;      // its validity bits, granule-aligned
+constexpr int kStageSlot = kStageBytes + kStageValid;
+constexpr int kCharStage = 32768;                    // largest character slice that is staged
+constexpr int kCharRegion = kCharStage + 64;         // + granule ends + read slack of the copy
 constexpr uint32_t kSpinLimit = 1u << 26;
 
 // One stable LSD pass over 8 bits of the keys.
@@ -543,47 +546,24 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   return false;
 }
 
-// A staged piece keeps the source's alignment phase: its bytes land at dst + (src & 15), so
-// the 16-byte aligned interior goes by one bulk copy and only the head and tail (< 16 bytes
-// each) by plain loads; nothing outside [src, src + bytes) is read.
-__device__ __forceinline__ uint32_t bulk_part(const uint8_t* src, uint32_t bytes) {
+// A staged piece keeps the source's alignment phase: the aligned 16-byte granules covering
+// [src, src + bytes) are copied by one bulk copy to a 16-byte aligned `dst_base`, so source byte x
+// lands at dst_base + (x - (src & ~15)) and `src` itself at staged_ptr(dst_base, src).  The granules
+// around a valid byte never leave its page, so the few extra bytes read at either end are always
+// readable; they are never used.
+__device__ __forceinline__ uint32_t super_bytes(const uint8_t* src, uint32_t bytes) {
   if (src == nullptr || bytes == 0) return 0;
-  const uint32_t mis = (uint32_t)(reinterpret_cast<uintptr_t>(src) & 15);
-  const uint32_t head = min(bytes, (16u - mis) & 15u);
-  return (bytes - head) & ~15u;
+  const uintptr_t lo = reinterpret_cast<uintptr_t>(src) & ~uintptr_t(15);
+  const uintptr_t hi = (reinterpret_cast<uintptr_t>(src) + bytes + 15) & ~uintptr_t(15);
+  return (uint32_t)(hi - lo);
 }
 __device__ __forceinline__ const uint8_t* staged_ptr(const uint8_t* dst_base, const uint8_t* src) {
   return dst_base + (reinterpret_cast<uintptr_t>(src) & 15);
 }
-// Thread 0, after the barrier expects the bulk bytes: the aligned interior by TMA.  The head
-// and tail bytes are fetched by `fetch_edge` into registers when the copy is issued and
-// written to shared memory by `place_edge` when the column is consumed.
-__device__ __forceinline__ void stage_bulk(uint8_t* dst_base, const uint8_t* src, uint32_t bytes,
-                                           uint64_t* bar) {
-  if (bytes == 0 || src == nullptr) return;
-  const uint32_t mis = (uint32_t)(reinterpret_cast<uintptr_t>(src) & 15);
-  const uint32_t head = min(bytes, (16u - mis) & 15u);
-  const uint32_t bulk = (bytes - head) & ~15u;
-  if (bulk) bulk_g2s(dst_base + mis + head, src + head, bulk, bar);
-}
-// Edge byte e (0..15: head, 16..31: tail) of a piece whose slot offset is `base_off`; returns
-// byte | 0x100 | (slot offset << 9), or 0 when there is no such byte.
-__device__ __forceinline__ uint32_t fetch_edge(const uint8_t* src, uint32_t bytes, uint32_t base_off,
-                                               int e) {
-  if (bytes == 0 || src == nullptr) return 0;
-  const uint32_t mis = (uint32_t)(reinterpret_cast<uintptr_t>(src) & 15);
-  const uint32_t head = min(bytes, (16u - mis) & 15u);
-  const uint32_t bulk = (bytes - head) & ~15u;
-  const uint32_t tail = bytes - head - bulk;
-  uint32_t i;
-  if (e < 16) {
-    if ((uint32_t)e >= head) return 0;
-    i = (uint32_t)e;
-  } else {
-    if ((uint32_t)(e - 16) >= tail) return 0;
-    i = head + bulk + (uint32_t)(e - 16);
-  }
-  return (uint32_t)src[i] | 0x100u | ((base_off + mis + i) << 9);
+__device__ __forceinline__ void stage_super(uint8_t* dst_base, const uint8_t* src, uint32_t super,
+                                            uint64_t* bar) {
+  if (super) bulk_g2s(dst_base, reinterpret_cast<const void*>(reinterpret_cast<uintptr_t>(src) & ~uintptr_t(15)),
+                      super, bar);
 }
 
 // Source word at `a` (4-byte aligned); bytes outside [lo, hi) read as 0 and are never stored.
@@ -666,12 +646,15 @@ __device__ __forceinline__ void copy_string_smem(uint8_t* dst, const uint8_t* sr
 __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd, const FlushDesc fd) {
   extern __shared__ __align__(128) uint8_t ssm[];
   __shared__ uint32_t scratch[33];
-  __shared__ __align__(8) uint64_t bars[3];  // two column slots + the character stage
+  __shared__ __align__(8) uint64_t bars[kSlots + 1];  // column slots + the character stage
+  __shared__ ColPtr s_col[kMaxCols];                   // this batch's columns, by array index
+  __shared__ uint32_t s_nc[kMaxCols];                  // their null counts in the batch
+  __shared__ int2 s_cr[kMaxStrPlan];                   // character range of the tile per binary column
   __shared__ uint32_t s_bad;
   const int T = kTileRows;
-  uint8_t* stage0 = ssm;                                    // [2][kStageSlot]
-  uint8_t* cstage = ssm + 2 * kStageSlot + kCharSlack;      // [kCharStage + 16] inside slack
-  uint16_t* kA = reinterpret_cast<uint16_t*>(ssm + 2 * kStageSlot + kCharStage + 16 + 2 * kCharSlack);
+  uint8_t* stage0 = ssm;                                         // [kSlots][kStageSlot]
+  uint8_t* cstage = ssm + kSlots * kStageSlot;                   // [kCharRegion]
+  uint16_t* kA = reinterpret_cast<uint16_t*>(cstage + kCharRegion);
   uint16_t* pA = kA + T;
   uint16_t* kB = pA + T;
   uint16_t* pB = kB + T;
@@ -682,67 +665,89 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
   uint32_t* rt1 = rt0 + T;                                  // [T]
   uint16_t* wcnt = reinterpret_cast<uint16_t*>(rt1 + T);    // [kW * 256]
 
+  if (*reinterpret_cast<volatile int32_t*>(fd.err) != 0) return;  // inputs rejected by k_hash_count
   const TileDesc tile = fd.tiles[blockIdx.x];
   const int n = (int)tile.nrows;
   const int P = sd.P;
   const int nstr = sd.n_str;
   const int A = sd.n_array;
-  const ColPtr* cols = fd.cols + (size_t)tile.batch * sd.n_cols;
-  if (*reinterpret_cast<volatile int32_t*>(fd.err) != 0) return;  // inputs rejected by k_hash_count
   const uint32_t row0 = tile.row0;
-  const uint32_t* nullcnt = fd.nullcnt + (size_t)tile.batch * A;
-
-  // what column `a` stages: [values or offsets][pad][validity bits]
-  auto pieces = [&](int a, const uint8_t** vsrc, uint32_t* vbytes, const uint8_t** bsrc, uint32_t* bbytes) {
-    const ColPtr c = cols[sd.arr_col[a]];
-    const int kind = sd.arr_kind[a];
-    *vsrc = nullptr;
-    *vbytes = 0;
-    if (kind == COL_FIXED && sd.arr_width[a] <= 8) {
-      *vsrc = c.values + (size_t)row0 * sd.arr_width[a];
-      *vbytes = (uint32_t)n * sd.arr_width[a];
-    } else if (kind == COL_BOOL) {
-      *vsrc = c.values + (row0 >> 3);
-      *vbytes = (uint32_t)(n + 7) >> 3;
-    } else if (kind == COL_BINARY) {
-      *vsrc = reinterpret_cast<const uint8_t*>(c.offsets + row0);
-      *vbytes = (uint32_t)(n + 1) * 4;
+  {
+    const ColPtr* cols = fd.cols + (size_t)tile.batch * sd.n_cols;
+    if ((int)threadIdx.x < A) {
+      s_col[threadIdx.x] = cols[sd.arr_col[threadIdx.x]];
+      s_nc[threadIdx.x] = fd.nullcnt[(size_t)tile.batch * A + threadIdx.x];
     }
-    *bsrc = nullptr;
-    *bbytes = 0;
-    if (c.validity != nullptr && nullcnt[a] != 0 && fd.out_valid[a] != nullptr) {
-      *bsrc = c.validity + (row0 >> 3);
-      *bbytes = (uint32_t)(n + 7) >> 3;
-    }
-  };
-  // every thread calls it; returns this thread's pending edge byte for the slot
-  auto issue = [&](int a, int slot) -> uint32_t {
-    if (a >= A) return 0u;
-    const uint8_t *vsrc, *bsrc;
-    uint32_t vbytes, bbytes;
-    pieces(a, &vsrc, &vbytes, &bsrc, &bbytes);
-    if (threadIdx.x == 0) {
-      uint8_t* dst = stage0 + slot * kStageSlot;
-      fence_proxy_async();  // earlier generic reads of the slot come first
-      mbar_expect_tx(&bars[slot], bulk_part(vsrc, vbytes) + bulk_part(bsrc, bbytes));
-      stage_bulk(dst, vsrc, vbytes, &bars[slot]);
-      stage_bulk(dst + kStageBytes + 16, bsrc, bbytes, &bars[slot]);
-    }
-    if (threadIdx.x < 32) return fetch_edge(vsrc, vbytes, 0, threadIdx.x);
-    if (threadIdx.x < 64) return fetch_edge(bsrc, bbytes, kStageBytes + 16, threadIdx.x - 32);
-    return 0u;
-  };
-
+    if ((int)threadIdx.x < nstr) s_cr[threadIdx.x] = fd.crange[(size_t)blockIdx.x * nstr + threadIdx.x];
+  }
   if (threadIdx.x == 0) {
-    mbar_init(&bars[0], 1);
-    mbar_init(&bars[1], 1);
-    mbar_init(&bars[2], 1);
+    for (int i = 0; i <= kSlots; i++) mbar_init(&bars[i], 1);
     s_bad = 0;
     fence_mbar_init();
   }
   __syncthreads();
-  uint32_t pend0 = issue(0, 0);
-  uint32_t pend1 = issue(1, 1);
+
+  // characters of binary column k are staged when the tile's slice fits the stage
+  auto chars_staged = [&](int k) {
+    const int32_t len = s_cr[k].y - s_cr[k].x;
+    return len > 0 && len <= kCharStage;
+  };
+  // thread 0: the slice of the column processed i-th (values / offsets and validity bits)
+  int issued_cols = 0;  // thread 0 only
+  auto issue_col = [&](int i) {
+    if (i >= A) return;
+    issued_cols = i + 1;
+    const int a = sd.order[i];
+    const ColPtr c = s_col[a];
+    const int kind = sd.arr_kind[a];
+    const uint8_t* vsrc = nullptr;
+    uint32_t vbytes = 0;
+    if (kind == COL_FIXED && sd.arr_width[a] <= 8) {
+      vsrc = c.values + (size_t)row0 * sd.arr_width[a];
+      vbytes = (uint32_t)n * sd.arr_width[a];
+    } else if (kind == COL_BOOL) {
+      vsrc = c.values + (row0 >> 3);
+      vbytes = (uint32_t)(n + 7) >> 3;
+    } else if (kind == COL_BINARY) {
+      vsrc = reinterpret_cast<const uint8_t*>(c.offsets + row0);
+      vbytes = (uint32_t)(n + 1) * 4;
+    }
+    const uint8_t* bsrc = nullptr;
+    uint32_t bbytes = 0;
+    if (c.validity != nullptr && s_nc[a] != 0 && fd.out_valid[a] != nullptr) {
+      bsrc = c.validity + (row0 >> 3);
+      bbytes = (uint32_t)(n + 7) >> 3;
+    }
+    const uint32_t vs = super_bytes(vsrc, vbytes), bs = super_bytes(bsrc, bbytes);
+    uint8_t* dst = stage0 + (i % kSlots) * kStageSlot;
+    fence_proxy_async();  // earlier generic reads of the slot come first
+    mbar_expect_tx(&bars[i % kSlots], vs + bs);
+    stage_super(dst, vsrc, vs, &bars[i % kSlots]);
+    stage_super(dst + kStageBytes, bsrc, bs, &bars[i % kSlots]);
+  };
+  // thread 0: characters of the first binary column at processing index >= next_chars that
+  // stages them; next_chars moves past it
+  int next_chars = 0;         // thread 0 only
+  uint32_t chars_issued = 0;  // thread 0 only
+  auto issue_chars = [&]() {
+    for (; next_chars < A; next_chars++) {
+      const int a = sd.order[next_chars];
+      if (sd.arr_kind[a] != COL_BINARY || !chars_staged(sd.arr_str[a])) continue;
+      const int k = sd.arr_str[a];
+      const uint8_t* src = s_col[a].values + s_cr[k].x;
+      const uint32_t sb = super_bytes(src, (uint32_t)(s_cr[k].y - s_cr[k].x));
+      fence_proxy_async();
+      mbar_expect_tx(&bars[kSlots], sb);
+      stage_super(cstage, src, sb, &bars[kSlots]);
+      chars_issued++;
+      next_chars++;
+      return;
+    }
+  };
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kSlots; i++) issue_col(i);
+    issue_chars();
+  }
 
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
     kA[j] = fd.pids[tile.frow0 + j];
@@ -790,25 +795,22 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
     dbit[j] = rt1[rs[j]] + (uint32_t)j;
   }
   __syncthreads();
-  uint32_t cphase = 0;  // uses of the character stage
+  uint32_t cphase = 0;  // staged character slices consumed
+  int i_stop = A;       // first column whose slice was not consumed (a wait gave up)
 
-  for (int a = 0; a < A; a++) {
-    const int slot = a & 1;
-    const uint32_t parity = (uint32_t)((a >> 1) & 1);
-    if (!mbar_wait(&bars[slot], parity)) {
+  for (int i = 0; i < A; i++) {
+    const int a = sd.order[i];
+    const int slot = i % kSlots;
+    if (!mbar_wait(&bars[slot], (uint32_t)((i / kSlots) & 1))) {
       if (threadIdx.x == 0) atomicOr(fd.err, kErrTimeout);
       s_bad = 1;
     }
-    {
-      const uint32_t pe = slot ? pend1 : pend0;
-      if (pe) stage0[slot * kStageSlot + (pe >> 9)] = (uint8_t)pe;
-    }
     __syncthreads();
     if (s_bad) {
-      mbar_wait(&bars[slot ^ 1], parity);  // let the other copy land before leaving
-      return;
+      i_stop = i;
+      break;
     }
-    const ColPtr c = cols[sd.arr_col[a]];
+    const ColPtr c = s_col[a];
     const int kind = sd.arr_kind[a];
     const uint8_t* slot_base = stage0 + slot * kStageSlot;
     const uint8_t* stg = slot_base;  // staged values / bits / offsets, at the source's phase
@@ -816,8 +818,8 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
     else if (kind == COL_BOOL) stg = staged_ptr(slot_base, c.values + (row0 >> 3));
     else if (kind == COL_BINARY) stg = staged_ptr(slot_base, reinterpret_cast<const uint8_t*>(c.offsets + row0));
     // validity: clear the bits of null rows (destination words start 0xff)
-    if (c.validity != nullptr && nullcnt[a] != 0 && fd.out_valid[a] != nullptr) {
-      const uint8_t* vb = staged_ptr(slot_base + kStageBytes + 16, c.validity + (row0 >> 3));
+    if (c.validity != nullptr && s_nc[a] != 0 && fd.out_valid[a] != nullptr) {
+      const uint8_t* vb = staged_ptr(slot_base + kStageBytes, c.validity + (row0 >> 3));
       uint32_t* ow = fd.out_valid[a];
       for (int j0 = 0; j0 < n; j0 += blockDim.x) {
         const int j = j0 + threadIdx.x;
@@ -830,6 +832,7 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
         clear_bits(ow, clr, pos);
       }
     }
+    bool used_chars = false;
     if (kind == COL_FIXED) {
       const int w = sd.arr_width[a];
       uint8_t* out = fd.out_values[a];
@@ -886,51 +889,40 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
       __syncthreads();
       for (int j = threadIdx.x; j < n; j += blockDim.x)
         ooff[dstrow[j]] = (int32_t)(rt0[rs[j]] + S[j + 1]);
-      // the tile's characters [oin[0], oin[n]) are contiguous in the source: one bulk copy
-      // into shared memory when they fit, then one string per lane from there
-      const int32_t c0 = oin[0], c1 = oin[n];
-      const uint8_t* csrc = c.values + c0;
-      const uint32_t cbytes = (uint32_t)(c1 - c0);
-      const bool staged = cbytes > 0 && cbytes <= (uint32_t)kCharStage;
-      const uint8_t* cbase = c.values;  // where string bytes are read from (offset by oin[])
-      uintptr_t buf_lo = reinterpret_cast<uintptr_t>(c.values);
-      uintptr_t buf_hi = buf_lo + c.values_bytes;
-      if (staged) {
-        if (threadIdx.x == 0) {
-          fence_proxy_async();
-          mbar_expect_tx(&bars[2], bulk_part(csrc, cbytes));
-          stage_bulk(cstage, csrc, cbytes, &bars[2]);
-        }
-        if (threadIdx.x < 32) {
-          const uint32_t pe = fetch_edge(csrc, cbytes, 0, threadIdx.x);
-          if (pe) cstage[pe >> 9] = (uint8_t)pe;
-        }
-        if (!mbar_wait(&bars[2], cphase & 1)) {
+      if (chars_staged(k)) {
+        // the tile's characters [oin[0], oin[n]) arrived in the character stage
+        if (!mbar_wait(&bars[kSlots], cphase & 1)) {
           if (threadIdx.x == 0) atomicOr(fd.err, kErrTimeout);
           s_bad = 1;
         }
-        cphase++;
         __syncthreads();
-        if (s_bad) return;
-        const uint8_t* sbase = staged_ptr(cstage, csrc);  // byte oin[0] of the column
-        cbase = sbase - c0;
-        buf_lo = reinterpret_cast<uintptr_t>(sbase);
-        buf_hi = buf_lo + cbytes;
-      }
-      if (staged) {
+        if (s_bad) {
+          i_stop = i + 1;  // this column's slot was consumed
+          break;
+        }
+        cphase++;
+        used_chars = true;
+        const uint8_t* cbase = staged_ptr(cstage, c.values + s_cr[k].x) - s_cr[k].x;
         for (int j = threadIdx.x; j < n; j += blockDim.x)
           copy_string_smem(ochars + rt1[rs[j]] + S[j], cbase + oin[ps[j]], S[j + 1] - S[j]);
       } else {
-        for (int j = threadIdx.x; j < n; j += blockDim.x) {
-          const uint32_t len = S[j + 1] - S[j];
-          copy_string(ochars + rt1[rs[j]] + S[j], cbase + oin[ps[j]], len, buf_lo, buf_hi);
-        }
+        const uintptr_t buf_lo = reinterpret_cast<uintptr_t>(c.values);
+        const uintptr_t buf_hi = buf_lo + c.values_bytes;
+        for (int j = threadIdx.x; j < n; j += blockDim.x)
+          copy_string(ochars + rt1[rs[j]] + S[j], c.values + oin[ps[j]], S[j + 1] - S[j], buf_lo, buf_hi);
       }
     }
-    __syncthreads();  // everyone is done with this slot
-    const uint32_t pe = issue(a + 2, slot);
-    if (slot) pend1 = pe;
-    else pend0 = pe;
+    __syncthreads();  // everyone is done with this slot (and with the character stage)
+    if (threadIdx.x == 0) {
+      issue_col(i + kSlots);
+      if (used_chars) issue_chars();
+    }
+  }
+  if (s_bad && threadIdx.x == 0) {
+    // leave no bulk copy in flight into this CTA's shared memory: wait (bounded) for the
+    // slots issued but not consumed, and for characters still on their way
+    for (int i = i_stop; i < issued_cols; i++) mbar_wait(&bars[i % kSlots], (uint32_t)((i / kSlots) & 1));
+    if (chars_issued > cphase) mbar_wait(&bars[kSlots], cphase & 1);
   }
 }
 
@@ -1025,7 +1017,7 @@ cudaError_t launch_gather(const HostCopy* jobs, uint32_t n_jobs, cudaStream_t st
 
 size_t scatter_smem_bytes() {
   const int T = kTileRows;
-  return 2 * kStageSlot + kCharStage + 16 + 2 * kCharSlack + 4 * sizeof(uint16_t) * T + sizeof(uint32_t) * T +
+  return kSlots * kStageSlot + kCharRegion + 4 * sizeof(uint16_t) * T + sizeof(uint32_t) * T +
          sizeof(uint16_t) * T + sizeof(uint32_t) * (T + 1) + 2 * sizeof(uint32_t) * T +
          sizeof(uint16_t) * kW * 256;
 }

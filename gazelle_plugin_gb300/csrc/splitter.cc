@@ -136,6 +136,19 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
     sd_.arr_str[a] = a >= fixed_cnt_ ? a - fixed_cnt_ : -1;
     if (ci < fixed_cnt_) sd_.quirk_mask |= 1ull << a;
   }
+  // k_scatter processing order: binary columns spread evenly among the fixed ones, so the
+  // characters of the next binary column stream in while fixed columns are scattered
+  {
+    std::vector<int32_t> fixed, binary;
+    for (int a = 0; a < n_array_; a++) (sd_.arr_kind[a] == COL_BINARY ? binary : fixed).push_back(a);
+    size_t fi = 0, bi = 0;
+    for (int i = 0; i < n_array_; i++) {
+      // binary column bi goes to position floor(bi * n_array / n_binary)
+      const bool take_binary =
+          bi < binary.size() && (fi == fixed.size() || (int64_t)i >= (int64_t)bi * n_array_ / (int64_t)binary.size());
+      sd_.order[i] = take_binary ? binary[bi++] : fixed[fi++];
+    }
+  }
   // hash chain (HashSplitter::CreateProjector, splitter.cc:1402-1438)
   for (size_t k = 0; k < keys_.size(); k++) {
     const int ci = keys_[k];
@@ -721,6 +734,7 @@ Status Splitter::Flush() {
   const size_t s_bcnt = take(TP * nstr * 4 + 4);
   const size_t s_sbyte = take(TP * nstr * 4 + 4);
   const size_t s_null = take((size_t)NB * A * 4);
+  const size_t s_crange = take((size_t)T * std::max(nstr, 1) * 8);
   const size_t s_call = take((size_t)NB * 4);
   const size_t s_rec = take((size_t)NB * P * 4);
   const size_t s_hn = take((size_t)NB * 8);
@@ -750,6 +764,7 @@ Status Splitter::Flush() {
   fd.bcnt = reinterpret_cast<uint32_t*>(S + s_bcnt);
   fd.sbyte = reinterpret_cast<uint32_t*>(S + s_sbyte);
   fd.nullcnt = reinterpret_cast<uint32_t*>(S + s_null);
+  fd.crange = reinterpret_cast<int2*>(S + s_crange);
   fd.call_flags = reinterpret_cast<uint32_t*>(S + s_call);
   fd.rec_idx = reinterpret_cast<uint32_t*>(S + s_rec);
   fd.hn = reinterpret_cast<unsigned long long*>(S + s_hn);
