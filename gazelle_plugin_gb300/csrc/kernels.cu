@@ -629,8 +629,16 @@ __device__ __forceinline__ void copy_string_smem(uint8_t* dst, const uint8_t* sr
   const uint32_t sh = (uint32_t)(s & 3) * 8;
   uint32_t* dw = reinterpret_cast<uint32_t*>(d + head);
   uint32_t lo = sw[0];
-#pragma unroll 4
-  for (uint32_t k = 0; k < nw; k++) {
+  uint32_t k = 0;
+  for (; k + 4 <= nw; k += 4) {  // four source words loaded before any store
+    const uint32_t w1 = sw[k + 1], w2 = sw[k + 2], w3 = sw[k + 3], w4 = sw[k + 4];
+    dw[k] = __funnelshift_r(lo, w1, sh);
+    dw[k + 1] = __funnelshift_r(w1, w2, sh);
+    dw[k + 2] = __funnelshift_r(w2, w3, sh);
+    dw[k + 3] = __funnelshift_r(w3, w4, sh);
+    lo = w4;
+  }
+  for (; k < nw; k++) {
     const uint32_t hi = sw[k + 1];
     dw[k] = __funnelshift_r(lo, hi, sh);
     lo = hi;
@@ -639,6 +647,50 @@ __device__ __forceinline__ void copy_string_smem(uint8_t* dst, const uint8_t* sr
 #pragma unroll
   for (uint32_t t = 0; t < 3; t++)
     if (done + t < len) dst[done + t] = src[done + t];
+}
+
+// Rows a thread handles in a tile: j = threadIdx.x + u * kScatterThreads, u < kRowsPerThread.
+// Loops over them load everything first and store afterwards, so the shared-memory loads of
+// all rows are in flight together instead of each waiting behind the previous row's store.
+constexpr int kRowsPerThread = kTileRows / kScatterThreads;
+static_assert(kRowsPerThread * kScatterThreads == kTileRows, "tile rows per thread");
+
+template <typename V>
+__device__ __forceinline__ void gather_rows(V* out, const V* src, const uint16_t* ps,
+                                            const uint32_t* dstrow, int n) {
+  V v[kRowsPerThread];
+  uint32_t d[kRowsPerThread];
+#pragma unroll
+  for (int u = 0; u < kRowsPerThread; u++) {
+    const int j = threadIdx.x + u * kScatterThreads;
+    if (j < n) {
+      d[u] = dstrow[j];
+      v[u] = src[ps[j]];
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < kRowsPerThread; u++)
+    if (threadIdx.x + u * kScatterThreads < n) out[d[u]] = v[u];
+}
+
+// Bit of sorted row j (source bit ps[j] of `bits`) cleared at destination bit dbit[j] of `words`
+// when it is 0.  All threads of the block call it.
+__device__ __forceinline__ void scatter_zero_bits(uint32_t* words, const uint8_t* bits, const uint16_t* ps,
+                                                  const uint32_t* dbit, int n) {
+  bool clr[kRowsPerThread];
+  uint32_t pos[kRowsPerThread];
+#pragma unroll
+  for (int u = 0; u < kRowsPerThread; u++) {
+    const int j = threadIdx.x + u * kScatterThreads;
+    clr[u] = false;
+    pos[u] = 0;
+    if (j < n) {
+      clr[u] = !get_bit(bits, ps[j]);
+      pos[u] = dbit[j];
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < kRowsPerThread; u++) clear_bits(words, clr[u], pos[u]);
 }
 
 }  // namespace
@@ -818,57 +870,42 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
     else if (kind == COL_BOOL) stg = staged_ptr(slot_base, c.values + (row0 >> 3));
     else if (kind == COL_BINARY) stg = staged_ptr(slot_base, reinterpret_cast<const uint8_t*>(c.offsets + row0));
     // validity: clear the bits of null rows (destination words start 0xff)
-    if (c.validity != nullptr && s_nc[a] != 0 && fd.out_valid[a] != nullptr) {
-      const uint8_t* vb = staged_ptr(slot_base + kStageBytes, c.validity + (row0 >> 3));
-      uint32_t* ow = fd.out_valid[a];
-      for (int j0 = 0; j0 < n; j0 += blockDim.x) {
-        const int j = j0 + threadIdx.x;
-        bool clr = false;
-        uint32_t pos = 0;
-        if (j < n) {
-          clr = !get_bit(vb, ps[j]);
-          pos = dbit[j];
-        }
-        clear_bits(ow, clr, pos);
-      }
-    }
+    if (c.validity != nullptr && s_nc[a] != 0 && fd.out_valid[a] != nullptr)
+      scatter_zero_bits(fd.out_valid[a], staged_ptr(slot_base + kStageBytes, c.validity + (row0 >> 3)), ps,
+                        dbit, n);
     bool used_chars = false;
     if (kind == COL_FIXED) {
       const int w = sd.arr_width[a];
       uint8_t* out = fd.out_values[a];
       if (w == 8) {
-        const uint64_t* src = reinterpret_cast<const uint64_t*>(stg);
-        for (int j = threadIdx.x; j < n; j += blockDim.x) reinterpret_cast<uint64_t*>(out)[dstrow[j]] = src[ps[j]];
+        gather_rows(reinterpret_cast<uint64_t*>(out), reinterpret_cast<const uint64_t*>(stg), ps, dstrow, n);
       } else if (w == 4) {
-        const uint32_t* src = reinterpret_cast<const uint32_t*>(stg);
-        for (int j = threadIdx.x; j < n; j += blockDim.x) reinterpret_cast<uint32_t*>(out)[dstrow[j]] = src[ps[j]];
+        gather_rows(reinterpret_cast<uint32_t*>(out), reinterpret_cast<const uint32_t*>(stg), ps, dstrow, n);
       } else if (w == 2) {
-        const uint16_t* src = reinterpret_cast<const uint16_t*>(stg);
-        for (int j = threadIdx.x; j < n; j += blockDim.x) reinterpret_cast<uint16_t*>(out)[dstrow[j]] = src[ps[j]];
+        gather_rows(reinterpret_cast<uint16_t*>(out), reinterpret_cast<const uint16_t*>(stg), ps, dstrow, n);
       } else if (w == 1) {
-        for (int j = threadIdx.x; j < n; j += blockDim.x) out[dstrow[j]] = stg[ps[j]];
+        gather_rows(out, stg, ps, dstrow, n);
       } else {  // 16-byte values are gathered straight from global memory
-        const uint4* src = reinterpret_cast<const uint4*>(c.values) + row0;
-        for (int j = threadIdx.x; j < n; j += blockDim.x) reinterpret_cast<uint4*>(out)[dstrow[j]] = src[ps[j]];
+        gather_rows(reinterpret_cast<uint4*>(out), reinterpret_cast<const uint4*>(c.values) + row0, ps, dstrow, n);
       }
     } else if (kind == COL_BOOL) {
-      uint32_t* ow = fd.out_bits[a];
-      for (int j0 = 0; j0 < n; j0 += blockDim.x) {
-        const int j = j0 + threadIdx.x;
-        bool clr = false;
-        uint32_t pos = 0;
-        if (j < n) {
-          clr = !get_bit(stg, ps[j]);
-          pos = dbit[j];
-        }
-        clear_bits(ow, clr, pos);
-      }
+      scatter_zero_bits(fd.out_bits[a], stg, ps, dbit, n);
     } else {
       const int k = sd.arr_str[a];
       const int32_t* oin = reinterpret_cast<const int32_t*>(stg);  // offsets of rows row0..row0+n
-      for (int j = threadIdx.x; j < n; j += blockDim.x) {
-        const int r = ps[j];
-        S[j] = (uint32_t)(oin[r + 1] - oin[r]);
+      {
+        uint32_t len[kRowsPerThread];
+#pragma unroll
+        for (int u = 0; u < kRowsPerThread; u++) {
+          const int j = threadIdx.x + u * kScatterThreads;
+          if (j < n) {
+            const int r = ps[j];
+            len[u] = (uint32_t)(oin[r + 1] - oin[r]);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kRowsPerThread; u++)
+          if (threadIdx.x + u * kScatterThreads < n) S[threadIdx.x + u * kScatterThreads] = len[u];
       }
       __syncthreads();
       const uint32_t total = block_exscan<kScatterThreads>(S, n, scratch);
@@ -887,8 +924,20 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
         }
       }
       __syncthreads();
-      for (int j = threadIdx.x; j < n; j += blockDim.x)
-        ooff[dstrow[j]] = (int32_t)(rt0[rs[j]] + S[j + 1]);
+      {
+        uint32_t d[kRowsPerThread], v[kRowsPerThread];
+#pragma unroll
+        for (int u = 0; u < kRowsPerThread; u++) {
+          const int j = threadIdx.x + u * kScatterThreads;
+          if (j < n) {
+            d[u] = dstrow[j];
+            v[u] = rt0[rs[j]] + S[j + 1];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kRowsPerThread; u++)
+          if (threadIdx.x + u * kScatterThreads < n) ooff[d[u]] = (int32_t)v[u];
+      }
       if (chars_staged(k)) {
         // the tile's characters [oin[0], oin[n]) arrived in the character stage
         if (!mbar_wait(&bars[kSlots], cphase & 1)) {
