@@ -33,9 +33,16 @@ __device__ __forceinline__ void clear_bits(uint32_t* words, bool clear, uint32_t
   }
 }
 
-// Block-wide exclusive scan of data[0..n) (u32) in place; returns the total.  Every thread
-// of the block must call it.  scratch: >= 33 u32.
-template <int NT>
+// Barrier over the NT threads 0..NT-1: the whole block (BAR 0) or named barrier BAR.
+template <int NT, int BAR>
+__device__ __forceinline__ void group_sync() {
+  if constexpr (BAR == 0) __syncthreads();
+  else asm volatile("bar.sync %0, %1;" ::"n"(BAR), "n"(NT) : "memory");
+}
+
+// Exclusive scan of data[0..n) (u32) in place over threads 0..NT-1; returns the total.  Every
+// one of them must call it.  scratch: >= 33 u32.
+template <int NT, int BAR = 0>
 __device__ uint32_t block_exscan(uint32_t* data, int n, uint32_t* scratch) {
   const int per = (n + NT - 1) / NT;
   const int lo = threadIdx.x * per;
@@ -50,7 +57,7 @@ __device__ uint32_t block_exscan(uint32_t* data, int n, uint32_t* scratch) {
   }
   const int w = threadIdx.x >> 5;
   if (lane_id() == 31) scratch[w] = x;
-  __syncthreads();
+  group_sync<NT, BAR>();
   if (w == 0) {
     uint32_t v = (int)lane_id() < NT / 32 ? scratch[lane_id()] : 0;
     for (int o = 1; o < 32; o <<= 1) {
@@ -60,7 +67,7 @@ __device__ uint32_t block_exscan(uint32_t* data, int n, uint32_t* scratch) {
     if ((int)lane_id() < NT / 32) scratch[lane_id()] = v;
     if (lane_id() == 31) scratch[32] = v;
   }
-  __syncthreads();
+  group_sync<NT, BAR>();
   uint32_t run = (w ? scratch[w - 1] : 0) + x - s;
   for (int i = lo; i < hi; i++) {
     uint32_t v = data[i];
@@ -68,13 +75,13 @@ __device__ uint32_t block_exscan(uint32_t* data, int n, uint32_t* scratch) {
     run += v;
   }
   uint32_t total = scratch[32];
-  __syncthreads();
+  group_sync<NT, BAR>();
   return total;
 }
 
-// Block-wide inclusive max scan of per-thread values; returns the exclusive max for this
-// thread (0 for thread 0).
-template <int NT>
+// Inclusive max scan of per-thread values over threads 0..NT-1; returns the exclusive max for
+// this thread (0 for thread 0).
+template <int NT, int BAR = 0>
 __device__ uint32_t block_exmax(uint32_t v, uint32_t* scratch) {
   uint32_t x = v;
   for (int o = 1; o < 32; o <<= 1) {
@@ -83,7 +90,7 @@ __device__ uint32_t block_exmax(uint32_t v, uint32_t* scratch) {
   }
   const int w = threadIdx.x >> 5;
   if (lane_id() == 31) scratch[w] = x;
-  __syncthreads();
+  group_sync<NT, BAR>();
   if (w == 0) {
     uint32_t t = (int)lane_id() < NT / 32 ? scratch[lane_id()] : 0;
     for (int o = 1; o < 32; o <<= 1) {
@@ -92,11 +99,11 @@ __device__ uint32_t block_exmax(uint32_t v, uint32_t* scratch) {
     }
     if ((int)lane_id() < NT / 32) scratch[lane_id()] = t;
   }
-  __syncthreads();
+  group_sync<NT, BAR>();
   uint32_t prev_warps = w ? scratch[w - 1] : 0;
   uint32_t xin = __shfl_up_sync(kFull, x, 1);
   uint32_t excl = lane_id() ? max(prev_warps, xin) : prev_warps;
-  __syncthreads();
+  group_sync<NT, BAR>();
   return excl;
 }
 
@@ -454,6 +461,8 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan_scan(const SchemaDesc sd,
 //      aligned 32-bit destination words built by funnel shifts from aligned source words.
 namespace {
 constexpr int kW = kScatterThreads / 32;
+constexpr int kConsumers = kScatterThreads;          // threads that scatter; one more warp issues copies
+constexpr int kScatterBlock = kConsumers + 32;
 constexpr int kSlots = 4;                            // column slices in flight
 constexpr int kStageBytes = kTileRows * 8 + 32;      // one 8-byte column slice, granule-aligned
 constexpr int kStageValid = kTileRows / 8 + 32;      // its validity bits, granule-aligned
@@ -462,14 +471,17 @@ constexpr int kCharStage = 32768;                    // largest character slice 
 constexpr int kCharRegion = kCharStage + 64;         // + granule ends + read slack of the copy
 constexpr uint32_t kSpinLimit = 1u << 26;
 
+// Barrier of the scattering threads (the issuing warp never joins it).
+__device__ __forceinline__ void csync() { group_sync<kConsumers, 1>(); }
+
 // One stable LSD pass over 8 bits of the keys.
 __device__ void radix_pass(const uint16_t* kin, const uint16_t* pin, uint16_t* kout,
                            uint16_t* pout, int n, int shift, uint16_t* wcnt, uint32_t* off,
                            uint32_t* scratch) {
   const int w = threadIdx.x >> 5;
   const int seg = ((n + kW * 32 - 1) / (kW * 32)) * 32;
-  for (int i = threadIdx.x; i < kW * 256; i += blockDim.x) wcnt[i] = 0;
-  __syncthreads();
+  for (int i = threadIdx.x; i < kW * 256; i += kConsumers) wcnt[i] = 0;
+  csync();
   for (int c = 0; c < seg; c += 32) {
     const int i = w * seg + c + lane_id();
     const bool act = i < n;
@@ -481,13 +493,13 @@ __device__ void radix_pass(const uint16_t* kin, const uint16_t* pin, uint16_t* k
     }
     __syncwarp();
   }
-  __syncthreads();
-  for (int i = threadIdx.x; i < kW * 256; i += blockDim.x) {
+  csync();
+  for (int i = threadIdx.x; i < kW * 256; i += kConsumers) {
     const int d = i / kW, ww = i % kW;
     off[i] = wcnt[ww * 256 + d];
   }
-  __syncthreads();
-  block_exscan<kScatterThreads>(off, kW * 256, scratch);
+  csync();
+  block_exscan<kConsumers, 1>(off, kW * 256, scratch);
   for (int c = 0; c < seg; c += 32) {
     const int i = w * seg + c + lane_id();
     const bool act = i < n;
@@ -505,7 +517,7 @@ __device__ void radix_pass(const uint16_t* kin, const uint16_t* pin, uint16_t* k
     if (act && (int)lane_id() == __ffs(peers) - 1) off[d * kW + w] += __popc(peers);
     __syncwarp();
   }
-  __syncthreads();
+  csync();
 }
 
 // ---- mbarrier + bulk copy (TMA) helpers -------------------------------------------------
@@ -531,6 +543,15 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
           smem_addr(dst)),
       "l"(src), "r"(bytes), "r"(smem_addr(bar))
       : "memory");
+}
+// 4-byte asynchronous global -> shared copies (no register holds the value in flight)
+__device__ __forceinline__ void cp_async4(void* sdst, const void* gsrc) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(sdst)), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 // Bounded wait for phase `parity` of `bar`; false when the limit ran out.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
@@ -611,27 +632,39 @@ __device__ __forceinline__ void copy_string(uint8_t* dst, const uint8_t* src, ui
   }
 }
 
-// One string whose source bytes are in shared memory: `len` bytes from `src` to global `dst`.
-// Up to 3 head bytes bring the destination to a 4-byte boundary, then whole aligned words, each a
-// funnel shift of two aligned source words, then up to 3 tail bytes.  The aligned source words
-// may reach up to 3 bytes before `src` and 7 bytes past `src + len`: the staging buffer keeps
-// that slack, and those bytes are never stored.
-__device__ __forceinline__ void copy_string_smem(uint8_t* dst, const uint8_t* src, uint32_t len) {
+__device__ __forceinline__ uint32_t lds32(uint32_t addr) {
+  uint32_t v;
+  asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(addr));
+  return v;
+}
+__device__ __forceinline__ uint32_t lds8(uint32_t addr) {
+  uint16_t v;
+  asm volatile("ld.shared.u8 %0, [%1];" : "=h"(v) : "r"(addr));
+  return v;
+}
+
+// One string whose source bytes are in shared memory (shared address `src`): `len` bytes to
+// global `dst`.  Up to 3 head bytes bring the destination to a 4-byte boundary, then whole
+// aligned words, each a funnel shift of two aligned source words, then up to 3 tail bytes.  The
+// aligned source words may reach 7 bytes past `src + len`: the staging buffer keeps that slack,
+// and those bytes are never stored.
+__device__ __forceinline__ void copy_string_smem(uint8_t* dst, uint32_t src, uint32_t len) {
   const uintptr_t d = reinterpret_cast<uintptr_t>(dst);
   const uint32_t lead = (uint32_t)((4 - (d & 3)) & 3);
   const uint32_t head = len < lead ? len : lead;
 #pragma unroll
   for (uint32_t t = 0; t < 3; t++)
-    if (t < head) dst[t] = src[t];
+    if (t < head) dst[t] = (uint8_t)lds8(src + t);
   const uint32_t nw = (len - head) >> 2;
-  const uintptr_t s = reinterpret_cast<uintptr_t>(src) + head;
-  const uint32_t* sw = reinterpret_cast<const uint32_t*>(s & ~uintptr_t(3));
-  const uint32_t sh = (uint32_t)(s & 3) * 8;
+  const uint32_t s = src + head;
+  const uint32_t sw = s & ~3u;
+  const uint32_t sh = (s & 3) * 8;
   uint32_t* dw = reinterpret_cast<uint32_t*>(d + head);
-  uint32_t lo = sw[0];
+  uint32_t lo = lds32(sw);
   uint32_t k = 0;
   for (; k + 4 <= nw; k += 4) {  // four source words loaded before any store
-    const uint32_t w1 = sw[k + 1], w2 = sw[k + 2], w3 = sw[k + 3], w4 = sw[k + 4];
+    const uint32_t w1 = lds32(sw + 4 * k + 4), w2 = lds32(sw + 4 * k + 8);
+    const uint32_t w3 = lds32(sw + 4 * k + 12), w4 = lds32(sw + 4 * k + 16);
     dw[k] = __funnelshift_r(lo, w1, sh);
     dw[k + 1] = __funnelshift_r(w1, w2, sh);
     dw[k + 2] = __funnelshift_r(w2, w3, sh);
@@ -639,14 +672,14 @@ __device__ __forceinline__ void copy_string_smem(uint8_t* dst, const uint8_t* sr
     lo = w4;
   }
   for (; k < nw; k++) {
-    const uint32_t hi = sw[k + 1];
+    const uint32_t hi = lds32(sw + 4 * k + 4);
     dw[k] = __funnelshift_r(lo, hi, sh);
     lo = hi;
   }
   const uint32_t done = head + 4 * nw;
 #pragma unroll
   for (uint32_t t = 0; t < 3; t++)
-    if (done + t < len) dst[done + t] = src[done + t];
+    if (done + t < len) dst[done + t] = (uint8_t)lds8(src + done + t);
 }
 
 // Rows a thread handles in a tile: j = threadIdx.x + u * kScatterThreads, u < kRowsPerThread.
@@ -695,13 +728,15 @@ __device__ __forceinline__ void scatter_zero_bits(uint32_t* words, const uint8_t
 
 }  // namespace
 
-__global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd, const FlushDesc fd) {
+__global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc sd, const FlushDesc fd) {
   extern __shared__ __align__(128) uint8_t ssm[];
   __shared__ uint32_t scratch[33];
-  __shared__ __align__(8) uint64_t bars[kSlots + 1];  // column slots + the character stage
-  __shared__ ColPtr s_col[kMaxCols];                   // this batch's columns, by array index
-  __shared__ uint32_t s_nc[kMaxCols];                  // their null counts in the batch
-  __shared__ int2 s_cr[kMaxStrPlan];                   // character range of the tile per binary column
+  __shared__ __align__(8) uint64_t full[kSlots];   // slice i landed (issuer: expect_tx)
+  __shared__ __align__(8) uint64_t empty[kSlots];  // slice i consumed (every scattering warp)
+  __shared__ __align__(8) uint64_t cfull, cempty;  // the same for the character stage
+  __shared__ ColPtr s_col[kMaxCols];               // this batch's columns, by array index
+  __shared__ uint32_t s_nc[kMaxCols];              // their null counts in the batch
+  __shared__ int2 s_cr[kMaxStrPlan];               // character range of the tile per binary column
   __shared__ uint32_t s_bad;
   const int T = kTileRows;
   uint8_t* stage0 = ssm;                                         // [kSlots][kStageSlot]
@@ -716,8 +751,13 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
   uint32_t* rt0 = S + T + 1;                                // [T] run tables (at run starts)
   uint32_t* rt1 = rt0 + T;                                  // [T]
   uint16_t* wcnt = reinterpret_cast<uint16_t*>(rt1 + T);    // [kW * 256]
+  uint32_t* nm2 = reinterpret_cast<uint32_t*>(wcnt + kW * 256);  // [T]
+  // run metadata of the next binary column, by sorted position of the run start (S and wcnt
+  // are free once the destinations are computed and the sort is done)
+  uint32_t* nm0 = S;
+  uint32_t* nm1 = reinterpret_cast<uint32_t*>(wcnt);
+  static_assert(kW * 256 * sizeof(uint16_t) >= kTileRows * sizeof(uint32_t), "wcnt holds a row table");
 
-  if (*reinterpret_cast<volatile int32_t*>(fd.err) != 0) return;  // inputs rejected by k_hash_count
   const TileDesc tile = fd.tiles[blockIdx.x];
   const int n = (int)tile.nrows;
   const int P = sd.P;
@@ -733,79 +773,97 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
     if ((int)threadIdx.x < nstr) s_cr[threadIdx.x] = fd.crange[(size_t)blockIdx.x * nstr + threadIdx.x];
   }
   if (threadIdx.x == 0) {
-    for (int i = 0; i <= kSlots; i++) mbar_init(&bars[i], 1);
-    s_bad = 0;
+    for (int i = 0; i < kSlots; i++) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], kW);
+    }
+    mbar_init(&cfull, 1);
+    mbar_init(&cempty, kW);
+    // inputs rejected by k_hash_count: copy nothing (read once, so the whole block agrees)
+    s_bad = (*reinterpret_cast<volatile int32_t*>(fd.err) & kErrBadOffsets) != 0;
     fence_mbar_init();
   }
-  __syncthreads();
+  __syncthreads();  // the last barrier of the whole block: the issuing warp leaves early
+  if (s_bad) return;
 
   // characters of binary column k are staged when the tile's slice fits the stage
   auto chars_staged = [&](int k) {
     const int32_t len = s_cr[k].y - s_cr[k].x;
     return len > 0 && len <= kCharStage;
   };
-  // thread 0: the slice of the column processed i-th (values / offsets and validity bits)
-  int issued_cols = 0;  // thread 0 only
-  auto issue_col = [&](int i) {
-    if (i >= A) return;
-    issued_cols = i + 1;
-    const int a = sd.order[i];
-    const ColPtr c = s_col[a];
-    const int kind = sd.arr_kind[a];
-    const uint8_t* vsrc = nullptr;
-    uint32_t vbytes = 0;
-    if (kind == COL_FIXED && sd.arr_width[a] <= 8) {
-      vsrc = c.values + (size_t)row0 * sd.arr_width[a];
-      vbytes = (uint32_t)n * sd.arr_width[a];
-    } else if (kind == COL_BOOL) {
-      vsrc = c.values + (row0 >> 3);
-      vbytes = (uint32_t)(n + 7) >> 3;
-    } else if (kind == COL_BINARY) {
-      vsrc = reinterpret_cast<const uint8_t*>(c.offsets + row0);
-      vbytes = (uint32_t)(n + 1) * 4;
+  auto staged_binary = [&](int a) { return sd.arr_kind[a] == COL_BINARY && chars_staged(sd.arr_str[a]); };
+
+  // ---- issuing warp: lane 0 streams the column slices, lane 1 the character slices ----------
+  if (threadIdx.x >= kConsumers) {
+    const int lane = threadIdx.x - kConsumers;
+    if (lane == 0) {
+      int issued = 0;
+      for (int i = 0; i < A; i++) {
+        if (i >= kSlots && !mbar_wait(&empty[i % kSlots], (uint32_t)((i / kSlots - 1) & 1))) {
+          atomicOr(fd.err, kErrTimeout);
+          break;
+        }
+        const int a = sd.order[i];
+        const ColPtr c = s_col[a];
+        const int kind = sd.arr_kind[a];
+        const uint8_t* vsrc = nullptr;
+        uint32_t vbytes = 0;
+        if (kind == COL_FIXED && sd.arr_width[a] <= 8) {
+          vsrc = c.values + (size_t)row0 * sd.arr_width[a];
+          vbytes = (uint32_t)n * sd.arr_width[a];
+        } else if (kind == COL_BOOL) {
+          vsrc = c.values + (row0 >> 3);
+          vbytes = (uint32_t)(n + 7) >> 3;
+        } else if (kind == COL_BINARY) {
+          vsrc = reinterpret_cast<const uint8_t*>(c.offsets + row0);
+          vbytes = (uint32_t)(n + 1) * 4;
+        }
+        const uint8_t* bsrc = nullptr;
+        uint32_t bbytes = 0;
+        if (c.validity != nullptr && s_nc[a] != 0 && fd.out_valid[a] != nullptr) {
+          bsrc = c.validity + (row0 >> 3);
+          bbytes = (uint32_t)(n + 7) >> 3;
+        }
+        const uint32_t vs = super_bytes(vsrc, vbytes), bs = super_bytes(bsrc, bbytes);
+        uint8_t* dst = stage0 + (i % kSlots) * kStageSlot;
+        fence_proxy_async();  // the scattering threads' generic reads of the slot come first
+        mbar_expect_tx(&full[i % kSlots], vs + bs);
+        stage_super(dst, vsrc, vs, &full[i % kSlots]);
+        stage_super(dst + kStageBytes, bsrc, bs, &full[i % kSlots]);
+        issued = i + 1;
+      }
+      // leave no copy in flight into this CTA's shared memory: wait (bounded) for the last
+      // phase issued on every slot
+      for (int i = max(0, issued - kSlots); i < issued; i++)
+        mbar_wait(&full[i % kSlots], (uint32_t)((i / kSlots) & 1));
+    } else if (lane == 1) {
+      uint32_t uses = 0;
+      for (int i = 0; i < A; i++) {
+        const int a = sd.order[i];
+        if (!staged_binary(a)) continue;
+        if (uses > 0 && !mbar_wait(&cempty, (uses - 1) & 1)) {
+          atomicOr(fd.err, kErrTimeout);
+          break;
+        }
+        const int k = sd.arr_str[a];
+        const uint8_t* src = s_col[a].values + s_cr[k].x;
+        const uint32_t sb = super_bytes(src, (uint32_t)(s_cr[k].y - s_cr[k].x));
+        fence_proxy_async();
+        mbar_expect_tx(&cfull, sb);
+        stage_super(cstage, src, sb, &cfull);
+        uses++;
+      }
+      if (uses > 0) mbar_wait(&cfull, (uses - 1) & 1);
     }
-    const uint8_t* bsrc = nullptr;
-    uint32_t bbytes = 0;
-    if (c.validity != nullptr && s_nc[a] != 0 && fd.out_valid[a] != nullptr) {
-      bsrc = c.validity + (row0 >> 3);
-      bbytes = (uint32_t)(n + 7) >> 3;
-    }
-    const uint32_t vs = super_bytes(vsrc, vbytes), bs = super_bytes(bsrc, bbytes);
-    uint8_t* dst = stage0 + (i % kSlots) * kStageSlot;
-    fence_proxy_async();  // earlier generic reads of the slot come first
-    mbar_expect_tx(&bars[i % kSlots], vs + bs);
-    stage_super(dst, vsrc, vs, &bars[i % kSlots]);
-    stage_super(dst + kStageBytes, bsrc, bs, &bars[i % kSlots]);
-  };
-  // thread 0: characters of the first binary column at processing index >= next_chars that
-  // stages them; next_chars moves past it
-  int next_chars = 0;         // thread 0 only
-  uint32_t chars_issued = 0;  // thread 0 only
-  auto issue_chars = [&]() {
-    for (; next_chars < A; next_chars++) {
-      const int a = sd.order[next_chars];
-      if (sd.arr_kind[a] != COL_BINARY || !chars_staged(sd.arr_str[a])) continue;
-      const int k = sd.arr_str[a];
-      const uint8_t* src = s_col[a].values + s_cr[k].x;
-      const uint32_t sb = super_bytes(src, (uint32_t)(s_cr[k].y - s_cr[k].x));
-      fence_proxy_async();
-      mbar_expect_tx(&bars[kSlots], sb);
-      stage_super(cstage, src, sb, &bars[kSlots]);
-      chars_issued++;
-      next_chars++;
-      return;
-    }
-  };
-  if (threadIdx.x == 0) {
-    for (int i = 0; i < kSlots; i++) issue_col(i);
-    issue_chars();
+    return;
   }
 
-  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+  // ---- scattering threads --------------------------------------------------------------------
+  for (int j = threadIdx.x; j < n; j += kConsumers) {
     kA[j] = fd.pids[tile.frow0 + j];
     pA[j] = (uint16_t)j;
   }
-  __syncthreads();
+  csync();
   radix_pass(kA, pA, kB, pB, n, 0, wcnt, dbit, scratch);
   uint16_t* ks = kB;
   uint16_t* ps = pB;
@@ -819,49 +877,76 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
 
   // run starts: rs[j] = first sorted position with the same partition id
   {
-    const int per = (n + kScatterThreads - 1) / kScatterThreads;
+    const int per = (n + kConsumers - 1) / kConsumers;
     const int lo = threadIdx.x * per;
     const int hi = min(lo + per, n);
     uint32_t mx = 0;
     for (int j = lo; j < hi; j++)
       if (j == 0 || ks[j] != ks[j - 1]) mx = j;
-    uint32_t carry = block_exmax<kScatterThreads>(mx, scratch);
+    uint32_t carry = block_exmax<kConsumers, 1>(mx, scratch);
     for (int j = lo; j < hi; j++) {
       if (j == 0 || ks[j] != ks[j - 1]) carry = j;
       rs[j] = (uint16_t)carry;
     }
   }
-  __syncthreads();
+  csync();
   // destination row / validity bit: one metadata lookup per run, kept at the run start
   const size_t tp = (size_t)blockIdx.x * P;
-  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+  for (int j = threadIdx.x; j < n; j += kConsumers) {
     if (rs[j] == j) {
       const int p = ks[j];
       S[j] = fd.pstart[p] + fd.cnt[tp + p] - (uint32_t)j;
       rt1[j] = fd.vstart[p] + fd.vpos[tp + p] - (uint32_t)j;
     }
   }
-  __syncthreads();
-  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+  csync();
+  for (int j = threadIdx.x; j < n; j += kConsumers) {
     dstrow[j] = S[rs[j]] + (uint32_t)j;
     dbit[j] = rt1[rs[j]] + (uint32_t)j;
   }
-  __syncthreads();
-  uint32_t cphase = 0;  // staged character slices consumed
-  int i_stop = A;       // first column whose slice was not consumed (a wait gave up)
+
+  // Binary columns: thread t owns sorted positions t + u * kConsumers, u < kRowsPerThread.  The
+  // run metadata of the next binary column (in-segment byte offset and destination byte of each
+  // run that starts at an owned position) is copied asynchronously into nm0/nm1/nm2 one binary
+  // column ahead, so its latency is hidden behind the columns processed in between; only the
+  // owning thread reads it back.
+  auto load_run_meta = [&](int i_from) {
+    for (int i = i_from; i < A; i++) {
+      const int a = sd.order[i];
+      if (sd.arr_kind[a] != COL_BINARY) continue;
+      const int k = sd.arr_str[a];
+      const size_t tk = ((size_t)blockIdx.x * nstr + k) * P;
+      const uint32_t* cst = fd.cstart + (size_t)k * P;
+#pragma unroll
+      for (int u = 0; u < kRowsPerThread; u++) {
+        const int j = threadIdx.x + u * kConsumers;
+        if (j < n && rs[j] == j) {
+          const int p = ks[j];
+          cp_async4(&nm0[j], &fd.sbyte[tk + p]);
+          cp_async4(&nm1[j], &fd.bcnt[tk + p]);
+          cp_async4(&nm2[j], &cst[p]);
+        }
+      }
+      cp_async_commit();
+      return;
+    }
+  };
+  csync();  // rs and the tables of the run starts are complete
+  load_run_meta(0);
+  uint32_t cuse = 0;  // staged character slices consumed
 
   for (int i = 0; i < A; i++) {
     const int a = sd.order[i];
     const int slot = i % kSlots;
-    if (!mbar_wait(&bars[slot], (uint32_t)((i / kSlots) & 1))) {
+    const bool chars = staged_binary(a);
+    bool ok = mbar_wait(&full[slot], (uint32_t)((i / kSlots) & 1));
+    if (chars) ok = mbar_wait(&cfull, cuse & 1) && ok;
+    if (!ok) {
       if (threadIdx.x == 0) atomicOr(fd.err, kErrTimeout);
       s_bad = 1;
     }
-    __syncthreads();
-    if (s_bad) {
-      i_stop = i;
-      break;
-    }
+    csync();  // also: every thread is done with the previous column's shared tables
+    if (s_bad) break;
     const ColPtr c = s_col[a];
     const int kind = sd.arr_kind[a];
     const uint8_t* slot_base = stage0 + slot * kStageSlot;
@@ -873,7 +958,6 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
     if (c.validity != nullptr && s_nc[a] != 0 && fd.out_valid[a] != nullptr)
       scatter_zero_bits(fd.out_valid[a], staged_ptr(slot_base + kStageBytes, c.validity + (row0 >> 3)), ps,
                         dbit, n);
-    bool used_chars = false;
     if (kind == COL_FIXED) {
       const int w = sd.arr_width[a];
       uint8_t* out = fd.out_values[a];
@@ -886,92 +970,108 @@ __global__ void __launch_bounds__(kScatterThreads) k_scatter(const SchemaDesc sd
       } else if (w == 1) {
         gather_rows(out, stg, ps, dstrow, n);
       } else {  // 16-byte values are gathered straight from global memory
-        gather_rows(reinterpret_cast<uint4*>(out), reinterpret_cast<const uint4*>(c.values) + row0, ps, dstrow, n);
+        const uint4* src = reinterpret_cast<const uint4*>(c.values) + row0;
+        for (int j = threadIdx.x; j < n; j += kConsumers) reinterpret_cast<uint4*>(out)[dstrow[j]] = src[ps[j]];
       }
     } else if (kind == COL_BOOL) {
       scatter_zero_bits(fd.out_bits[a], stg, ps, dbit, n);
     } else {
-      const int k = sd.arr_str[a];
       const int32_t* oin = reinterpret_cast<const int32_t*>(stg);  // offsets of rows row0..row0+n
-      {
-        uint32_t len[kRowsPerThread];
+      // lengths of the owned positions; exclusive prefix over the tile = the lengths of all
+      // earlier rows u' < u of positions + this row's prefix, one fused warp scan per row u
+      uint32_t len[kRowsPerThread], pre[kRowsPerThread];
+#pragma unroll
+      for (int u = 0; u < kRowsPerThread; u++) {
+        const int j = threadIdx.x + u * kConsumers;
+        len[u] = 0;
+        if (j < n) {
+          const int r = ps[j];
+          len[u] = (uint32_t)(oin[r + 1] - oin[r]);
+        }
+        pre[u] = len[u];
+      }
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
 #pragma unroll
         for (int u = 0; u < kRowsPerThread; u++) {
-          const int j = threadIdx.x + u * kScatterThreads;
-          if (j < n) {
-            const int r = ps[j];
-            len[u] = (uint32_t)(oin[r + 1] - oin[r]);
-          }
+          const uint32_t y = __shfl_up_sync(kFull, pre[u], o);
+          if ((int)lane_id() >= o) pre[u] += y;
         }
+      }
+      const int w = threadIdx.x >> 5;
+      if (lane_id() == 31) {
 #pragma unroll
-        for (int u = 0; u < kRowsPerThread; u++)
-          if (threadIdx.x + u * kScatterThreads < n) S[threadIdx.x + u * kScatterThreads] = len[u];
+        for (int u = 0; u < kRowsPerThread; u++) scratch[u * kW + w] = pre[u];
       }
-      __syncthreads();
-      const uint32_t total = block_exscan<kScatterThreads>(S, n, scratch);
-      if (threadIdx.x == 0) S[n] = total;
-      __syncthreads();
-      int32_t* ooff = reinterpret_cast<int32_t*>(fd.out_values[a]);
-      const size_t tk = ((size_t)blockIdx.x * nstr + k) * P;
-      const uint32_t* cst = fd.cstart + (size_t)k * P;
-      uint8_t* ochars = fd.out_chars[a];
-      // per run: in-segment byte offset and destination byte of the run's first string
-      for (int j = threadIdx.x; j < n; j += blockDim.x) {
-        if (rs[j] == j) {
-          const int p = ks[j];
-          rt0[j] = fd.sbyte[tk + p] - S[j];
-          rt1[j] = cst[p] + fd.bcnt[tk + p] - S[j];
+      csync();
+      {
+        uint32_t before = 0;  // all positions of earlier rows, then earlier warps of this row
+#pragma unroll
+        for (int u = 0; u < kRowsPerThread; u++) {
+          uint32_t row_total = 0, warps_before = 0;
+          for (int q = 0; q < kW; q++) {
+            const uint32_t t = scratch[u * kW + q];
+            row_total += t;
+            if (q < w) warps_before += t;
+          }
+          pre[u] = before + warps_before + pre[u] - len[u];
+          before += row_total;
         }
       }
-      __syncthreads();
+      // run tables at the run starts: destination of the run's first string and its offset
+      // inside the partition's segment, both relative to the tile prefix
+      cp_async_wait_all();
+#pragma unroll
+      for (int u = 0; u < kRowsPerThread; u++) {
+        const int j = threadIdx.x + u * kConsumers;
+        if (j < n && rs[j] == j) {
+          rt0[j] = nm0[j] - pre[u];
+          rt1[j] = nm2[j] + nm1[j] - pre[u];
+        }
+      }
+      load_run_meta(i + 1);
+      csync();
+      int32_t* ooff = reinterpret_cast<int32_t*>(fd.out_values[a]);
+      uint8_t* ochars = fd.out_chars[a];
       {
         uint32_t d[kRowsPerThread], v[kRowsPerThread];
 #pragma unroll
         for (int u = 0; u < kRowsPerThread; u++) {
-          const int j = threadIdx.x + u * kScatterThreads;
+          const int j = threadIdx.x + u * kConsumers;
           if (j < n) {
             d[u] = dstrow[j];
-            v[u] = rt0[rs[j]] + S[j + 1];
+            v[u] = rt0[rs[j]] + pre[u] + len[u];
           }
         }
 #pragma unroll
         for (int u = 0; u < kRowsPerThread; u++)
-          if (threadIdx.x + u * kScatterThreads < n) ooff[d[u]] = (int32_t)v[u];
+          if (threadIdx.x + u * kConsumers < n) ooff[d[u]] = (int32_t)v[u];
       }
-      if (chars_staged(k)) {
-        // the tile's characters [oin[0], oin[n]) arrived in the character stage
-        if (!mbar_wait(&bars[kSlots], cphase & 1)) {
-          if (threadIdx.x == 0) atomicOr(fd.err, kErrTimeout);
-          s_bad = 1;
+      const int k = sd.arr_str[a];
+      if (chars) {
+        // shared address of byte 0 of the column (offsets index from there)
+        const uint32_t cbase = smem_addr(staged_ptr(cstage, c.values + s_cr[k].x)) - (uint32_t)s_cr[k].x;
+#pragma unroll
+        for (int u = 0; u < kRowsPerThread; u++) {
+          const int j = threadIdx.x + u * kConsumers;
+          if (j < n) copy_string_smem(ochars + rt1[rs[j]] + pre[u], cbase + (uint32_t)oin[ps[j]], len[u]);
         }
-        __syncthreads();
-        if (s_bad) {
-          i_stop = i + 1;  // this column's slot was consumed
-          break;
-        }
-        cphase++;
-        used_chars = true;
-        const uint8_t* cbase = staged_ptr(cstage, c.values + s_cr[k].x) - s_cr[k].x;
-        for (int j = threadIdx.x; j < n; j += blockDim.x)
-          copy_string_smem(ochars + rt1[rs[j]] + S[j], cbase + oin[ps[j]], S[j + 1] - S[j]);
       } else {
         const uintptr_t buf_lo = reinterpret_cast<uintptr_t>(c.values);
         const uintptr_t buf_hi = buf_lo + c.values_bytes;
-        for (int j = threadIdx.x; j < n; j += blockDim.x)
-          copy_string(ochars + rt1[rs[j]] + S[j], c.values + oin[ps[j]], S[j + 1] - S[j], buf_lo, buf_hi);
+#pragma unroll
+        for (int u = 0; u < kRowsPerThread; u++) {
+          const int j = threadIdx.x + u * kConsumers;
+          if (j < n) copy_string(ochars + rt1[rs[j]] + pre[u], c.values + oin[ps[j]], len[u], buf_lo, buf_hi);
+        }
       }
     }
-    __syncthreads();  // everyone is done with this slot (and with the character stage)
-    if (threadIdx.x == 0) {
-      issue_col(i + kSlots);
-      if (used_chars) issue_chars();
+    __syncwarp();  // the whole warp is done with the slice (and the character stage)
+    if (lane_id() == 0) {
+      mbar_arrive(&empty[slot]);
+      if (chars) mbar_arrive(&cempty);
     }
-  }
-  if (s_bad && threadIdx.x == 0) {
-    // leave no bulk copy in flight into this CTA's shared memory: wait (bounded) for the
-    // slots issued but not consumed, and for characters still on their way
-    for (int i = i_stop; i < issued_cols; i++) mbar_wait(&bars[i % kSlots], (uint32_t)((i / kSlots) & 1));
-    if (chars_issued > cphase) mbar_wait(&bars[kSlots], cphase & 1);
+    if (chars) cuse++;
   }
 }
 
@@ -1068,7 +1168,7 @@ size_t scatter_smem_bytes() {
   const int T = kTileRows;
   return kSlots * kStageSlot + kCharRegion + 4 * sizeof(uint16_t) * T + sizeof(uint32_t) * T +
          sizeof(uint16_t) * T + sizeof(uint32_t) * (T + 1) + 2 * sizeof(uint32_t) * T +
-         sizeof(uint16_t) * kW * 256;
+         sizeof(uint16_t) * kW * 256 + sizeof(uint32_t) * T;
 }
 
 cudaError_t launch_scatter(const SchemaDesc& sd, const FlushDesc& fd, cudaStream_t st) {
@@ -1079,7 +1179,7 @@ cudaError_t launch_scatter(const SchemaDesc& sd, const FlushDesc& fd, cudaStream
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  k_scatter<<<fd.n_tiles, kScatterThreads, sm, st>>>(sd, fd);
+  k_scatter<<<fd.n_tiles, kScatterBlock, sm, st>>>(sd, fd);
   return cudaGetLastError();
 }
 
