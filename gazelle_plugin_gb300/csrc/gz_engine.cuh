@@ -1,13 +1,17 @@
 // Shared host/device definitions of the GB300 hash-split engine.
 //
 // One "flush" is a device pass over a group of consecutive input batches:
-//   k_hash_count : Spark Murmur3 chain + pmod per row, per-tile partition histograms
+//   k_hash_count : Spark Murmur3 chain + pmod per row, per-segment partition histograms
 //                  (rows, and bytes of every utf8 column), per-batch null counts
 //   k_plan       : per-partition walk over the flush's batches that restates the reference
 //                  buffer policy (allocate / emit / reuse, validity presence) and turns the
 //                  histograms into destination offsets; then scans over partitions
-//   k_scatter    : per-tile stable counting sort by partition id in shared memory, then a
-//                  coalesced scatter of every column into partition-contiguous output
+//   k_scatter    : per 1024-row tile, a stable counting sort by partition id in shared memory,
+//                  then a coalesced scatter of every column into partition-contiguous output
+// A segment is up to seg_tiles consecutive tiles of one batch: the unit of k_hash_count and of
+// the plan's offsets.  k_hash_count also records, for every tile after the first of its
+// segment, how many rows and bytes each partition received from the segment's earlier tiles, so
+// each k_scatter CTA (one tile) finds its destinations without the others.
 // Output of a flush, per array column, is partition-major: all rows of partition 0 in input
 // order, then partition 1, ...  An emitted record batch (reference CacheRecordBatch) is a
 // contiguous row range of one partition, possibly continued from the previous flush.
@@ -19,7 +23,9 @@ namespace gz {
 constexpr int kMaxKeys = 8;
 constexpr int kMaxCols = 64;    // array columns (fixed + bool + binary)
 constexpr int kMaxSchemaCols = 256;
-constexpr int kTileRows = 1024; // rows per k_hash_count / k_scatter CTA
+constexpr int kTileRows = 1024; // rows per k_scatter tile
+constexpr int kMaxSegTiles = 4; // tiles per segment
+constexpr int kSegStateWords = 2048;  // most (1 + n_str) * P for multi-tile segments
 constexpr int kScatterThreads = 256;
 constexpr int kPlanThreads = 1024;
 constexpr int kMaxBatchesPerFlush = 4096;
@@ -72,8 +78,8 @@ constexpr int32_t kErrTimeout = 4;  // a bounded wait in a kernel gave up
 
 struct BatchDesc {
   uint32_t nrows;
-  uint32_t tile0;
-  uint32_t ntiles;
+  uint32_t seg0;        // first segment
+  uint32_t nsegs;
   uint32_t split_size;  // CalculateSplitBatchSize for this batch (splitter.cc:800-853)
 };
 
@@ -82,6 +88,18 @@ struct TileDesc {
   uint32_t row0;   // first row inside the batch
   uint32_t nrows;
   uint32_t frow0;  // first row inside the flush (index into pids)
+  uint32_t seg;    // its segment
+  uint32_t tseg;   // its index inside the segment (0: no earlier tiles)
+  uint32_t pad[2];
+};
+
+struct SegDesc {
+  uint32_t batch;
+  uint32_t row0;   // first row inside the batch (a multiple of kTileRows)
+  uint32_t nrows;
+  uint32_t frow0;  // first row inside the flush (index into pids)
+  uint32_t tile0;  // first tile inside the flush (index into crange)
+  uint32_t pad[3];
 };
 
 // Emission record written by k_plan: [p, frow_end, rows, hv_lo, hv_hi, fb_end[n_str]]
@@ -89,22 +107,27 @@ constexpr int kEmitFixedWords = 5;
 
 struct FlushDesc {
   uint32_t n_batches;
-  uint32_t n_tiles;
+  uint32_t n_segs;
   uint32_t n_rows;
   uint32_t hist_in_smem;  // 1: k_hash_count histograms in shared memory
+  uint32_t n_tiles;
+  uint32_t seg_tiles;     // tiles per segment (1 when the running counts do not fit)
 
   const BatchDesc* batches;  // [n_batches]
+  const SegDesc* segs;       // [n_segs]
   const TileDesc* tiles;     // [n_tiles]
   const ColPtr* cols;        // [n_batches][n_cols]
 
   // scratch (reused across flushes)
   uint16_t* pids;     // [n_rows]
-  uint32_t* cnt;      // [n_tiles][P] rows; rewritten by k_plan to the flush-local row offset
-  uint32_t* bcnt;     // [n_tiles][n_str][P] bytes; rewritten to the flush-local byte offset
-  uint32_t* vpos;     // [n_tiles][P] validity bit offset (pieces start on 64-bit boundaries)
-  uint32_t* sbyte;    // [n_tiles][n_str][P] byte offset inside the partition's segment
+  uint32_t* cnt;      // [n_segs][P] rows; rewritten by k_plan to the flush-local row offset
+  uint32_t* bcnt;     // [n_segs][n_str][P] bytes; rewritten to the flush-local byte offset
+  uint32_t* vpos;     // [n_segs][P] validity bit offset (pieces start on 64-bit boundaries)
+  uint32_t* sbyte;    // [n_segs][n_str][P] byte offset inside the partition's emitted batch
   uint32_t* nullcnt;  // [n_batches][n_array]
   int2* crange;       // [n_tiles][n_str] offsets of the tile's first and one-past-last row
+  uint32_t* tilepre;  // [n_tiles][P] rows from the segment's earlier tiles (seg_tiles > 1)
+  uint32_t* tilebpre; // [n_tiles][n_str][P] bytes from the segment's earlier tiles
 
   // per-partition results of this flush
   uint32_t* rows_f;   // [P]

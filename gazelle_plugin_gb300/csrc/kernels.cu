@@ -110,7 +110,7 @@ __device__ uint32_t block_exmax(uint32_t v, uint32_t* scratch) {
 }  // namespace
 
 // =======================================================================================
-// k_hash_count: one CTA per tile (<= kTileRows rows of one batch).
+// k_hash_count: one CTA per segment (<= seg_tiles * kTileRows rows of one batch).
 constexpr int kMaxStrPlan = 32;
 
 __global__ void __launch_bounds__(256) k_hash_count(const SchemaDesc sd, const FlushDesc fd) {
@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(256) k_hash_count(const SchemaDesc sd, const F
   __shared__ ColPtr s_key[kMaxKeys];
   __shared__ int32_t s_kind[kMaxKeys];
   __shared__ ColPtr s_str[kMaxStrPlan];
-  const TileDesc tile = fd.tiles[blockIdx.x];
+  const SegDesc tile = fd.segs[blockIdx.x];
   const int P = sd.P;
   const int nstr = sd.n_str;
   const int nkeys = sd.n_keys;
@@ -141,7 +141,17 @@ __global__ void __launch_bounds__(256) k_hash_count(const SchemaDesc sd, const F
   __syncthreads();
   const unsigned long long M = sd.pmod_magic;
   bool bad = false;
-  for (uint32_t i = threadIdx.x; i < tile.nrows; i += blockDim.x) {
+  // tile by tile; before every tile after the first, the counts so far are the tile's prefix
+  for (uint32_t t0 = 0; t0 < tile.nrows; t0 += kTileRows) {
+  if (t0 > 0 && fd.tilepre != nullptr) {
+    __syncthreads();  // every row of the earlier tiles is counted
+    const size_t ti = (size_t)tile.tile0 + t0 / kTileRows;
+    for (int q = threadIdx.x; q < P; q += blockDim.x) fd.tilepre[ti * P + q] = H[q];
+    for (int q = threadIdx.x; q < nstr * P; q += blockDim.x) fd.tilebpre[ti * nstr * P + q] = BH[q];
+    __syncthreads();  // the copies are read before the next tile's rows are added
+  }
+  const uint32_t t1 = min(tile.nrows, t0 + (uint32_t)kTileRows);
+  for (uint32_t i = t0 + threadIdx.x; i < t1; i += blockDim.x) {
     const uint32_t r = tile.row0 + i;
     int32_t h = 42;
     for (int k = 0; k < nkeys; k++) {
@@ -162,8 +172,10 @@ __global__ void __launch_bounds__(256) k_hash_count(const SchemaDesc sd, const F
       const ColPtr c = s_str[k];
       const int32_t o0 = c.offsets[r], o1 = c.offsets[r + 1];
       uint32_t len = (uint32_t)(o1 - o0);
-      if (i == 0) fd.crange[(size_t)blockIdx.x * nstr + k].x = o0;
-      if (i + 1 == tile.nrows) fd.crange[(size_t)blockIdx.x * nstr + k].y = o1;
+      // offsets of the first and one-past-last row of every kTileRows tile (k_scatter stages them)
+      const size_t ct = ((size_t)tile.tile0 + i / kTileRows) * nstr + k;
+      if (i % kTileRows == 0) fd.crange[ct].x = o0;
+      if (i % kTileRows == kTileRows - 1 || i + 1 == tile.nrows) fd.crange[ct].y = o1;
       if (o0 < 0 || o1 < o0 || (uint64_t)o1 > c.values_bytes) {
         bad = true;
         len = 0;
@@ -171,9 +183,10 @@ __global__ void __launch_bounds__(256) k_hash_count(const SchemaDesc sd, const F
       if (len) atomicAdd(&BH[k * P + p], len);
     }
   }
+  }
   if (bad) atomicOr(fd.err, kErrBadOffsets);  // k_scatter then copies nothing
 
-  // null counts of this tile's slice of every column (GetNullCount of the batch = sum)
+  // null counts of this segment's slice of every column (GetNullCount of the batch = sum)
   for (int a = 0; a < sd.n_array; a++) {
     const uint8_t* validity = cols[sd.arr_col[a]].validity;
     if (validity == nullptr) continue;
@@ -207,7 +220,7 @@ __global__ void __launch_bounds__(256) k_hash_count(const SchemaDesc sd, const F
 //                  the flush's batches, 32 batches per step: a warp scan of the row counts, then
 //                  only the batches where the policy acts (allocation or a cut) are visited one
 //                  by one, found with a ballot on "rows so far + count > capacity".  Writes the
-//                  flush-local row / validity-bit offsets of every (tile, partition), the
+//                  flush-local row / validity-bit offsets of every (segment, partition), the
 //                  emission records, and marks cuts in rec_idx[batch][p].
 //   k_plan_bytes : one warp per (binary column, partition): flush-local and in-segment byte
 //                  offsets by warp scans, restarting at the cuts.
@@ -287,7 +300,7 @@ __global__ void __launch_bounds__(kPlanRowsThreads) k_plan_rows(const SchemaDesc
     unsigned long long hn_l = 0, ihn_l = 0;
     if (active) {
       bd = fd.batches[b];
-      for (uint32_t t = bd.tile0; t < bd.tile0 + bd.ntiles; t++) c += fd.cnt[(size_t)t * P + p];
+      for (uint32_t t = bd.seg0; t < bd.seg0 + bd.nsegs; t++) c += fd.cnt[(size_t)t * P + p];
       hn_l = fd.hn[b];
       ihn_l = fd.ihn[b];
     }
@@ -361,7 +374,7 @@ __global__ void __launch_bounds__(kPlanRowsThreads) k_plan_rows(const SchemaDesc
     hv |= warp_or64((active && lane >= from && c > 0) ? hn_l : 0ull);
     if (active && c > 0) {
       uint32_t fr = frow + Xex, vp = vpos + Xex + my_pad;
-      for (uint32_t t = bd.tile0; t < bd.tile0 + bd.ntiles; t++) {
+      for (uint32_t t = bd.seg0; t < bd.seg0 + bd.nsegs; t++) {
         const size_t ti = (size_t)t * P + p;
         const uint32_t ct = fd.cnt[ti];
         fd.cnt[ti] = fr;
@@ -395,7 +408,7 @@ __global__ void __launch_bounds__(kPlanRowsThreads) k_plan_bytes(const SchemaDes
   if (wid >= nstr * P) return;
   const int k = wid / P, p = wid % P;
   const int lane = lane_id();
-  const int T = fd.n_tiles;
+  const int T = fd.n_segs;
   const int rec_words = kEmitFixedWords + nstr;
   uint32_t sb = fd.st_sb[(size_t)k * P + p];
   uint32_t fb = 0;
@@ -403,7 +416,7 @@ __global__ void __launch_bounds__(kPlanRowsThreads) k_plan_bytes(const SchemaDes
     const int t = t0 + lane;
     uint32_t bc = 0, rec = 0;
     if (t < T) {
-      const TileDesc td = fd.tiles[t];
+      const SegDesc td = fd.segs[t];
       bc = fd.bcnt[((size_t)t * nstr + k) * P + p];
       if (td.row0 == 0) rec = fd.rec_idx[(size_t)td.batch * P + p];
     }
@@ -752,6 +765,7 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
   uint32_t* rt1 = rt0 + T;                                  // [T]
   uint16_t* wcnt = reinterpret_cast<uint16_t*>(rt1 + T);    // [kW * 256]
   uint32_t* nm2 = reinterpret_cast<uint32_t*>(wcnt + kW * 256);  // [T]
+  uint32_t* nm3 = nm2 + T;                                         // [T]
   // run metadata of the next binary column, by sorted position of the run start (S and wcnt
   // are free once the destinations are computed and the sort is done)
   uint32_t* nm0 = S;
@@ -891,12 +905,15 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
   }
   csync();
   // destination row / validity bit: one metadata lookup per run, kept at the run start
-  const size_t tp = (size_t)blockIdx.x * P;
+  // segment offset from the plan + rows from the segment's earlier tiles
+  const size_t tp = (size_t)tile.seg * P;
+  const bool has_pre = tile.tseg > 0;
   for (int j = threadIdx.x; j < n; j += kConsumers) {
     if (rs[j] == j) {
       const int p = ks[j];
-      S[j] = fd.pstart[p] + fd.cnt[tp + p] - (uint32_t)j;
-      rt1[j] = fd.vstart[p] + fd.vpos[tp + p] - (uint32_t)j;
+      const uint32_t before = has_pre ? fd.tilepre[(size_t)blockIdx.x * P + p] : 0u;
+      S[j] = fd.pstart[p] + fd.cnt[tp + p] + before - (uint32_t)j;
+      rt1[j] = fd.vstart[p] + fd.vpos[tp + p] + before - (uint32_t)j;
     }
   }
   csync();
@@ -915,7 +932,8 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
       const int a = sd.order[i];
       if (sd.arr_kind[a] != COL_BINARY) continue;
       const int k = sd.arr_str[a];
-      const size_t tk = ((size_t)blockIdx.x * nstr + k) * P;
+      const size_t tk = ((size_t)tile.seg * nstr + k) * P;
+      const size_t tb = ((size_t)blockIdx.x * nstr + k) * P;
       const uint32_t* cst = fd.cstart + (size_t)k * P;
 #pragma unroll
       for (int u = 0; u < kRowsPerThread; u++) {
@@ -925,6 +943,7 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
           cp_async4(&nm0[j], &fd.sbyte[tk + p]);
           cp_async4(&nm1[j], &fd.bcnt[tk + p]);
           cp_async4(&nm2[j], &cst[p]);
+          if (has_pre) cp_async4(&nm3[j], &fd.tilebpre[tb + p]);
         }
       }
       cp_async_commit();
@@ -1025,8 +1044,9 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
       for (int u = 0; u < kRowsPerThread; u++) {
         const int j = threadIdx.x + u * kConsumers;
         if (j < n && rs[j] == j) {
-          rt0[j] = nm0[j] - pre[u];
-          rt1[j] = nm2[j] + nm1[j] - pre[u];
+          const uint32_t before = has_pre ? nm3[j] : 0u;  // bytes from the segment's earlier tiles
+          rt0[j] = nm0[j] + before - pre[u];
+          rt1[j] = nm2[j] + nm1[j] + before - pre[u];
         }
       }
       load_run_meta(i + 1);
@@ -1127,7 +1147,7 @@ cudaError_t launch_hash_count(const SchemaDesc& sd, const FlushDesc& fd, cudaStr
     cudaError_t e = cudaFuncSetAttribute(k_hash_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
   }
-  k_hash_count<<<fd.n_tiles, 256, sm, st>>>(sd, fd);
+  k_hash_count<<<fd.n_segs, 256, sm, st>>>(sd, fd);
   return cudaGetLastError();
 }
 
@@ -1168,7 +1188,7 @@ size_t scatter_smem_bytes() {
   const int T = kTileRows;
   return kSlots * kStageSlot + kCharRegion + 4 * sizeof(uint16_t) * T + sizeof(uint32_t) * T +
          sizeof(uint16_t) * T + sizeof(uint32_t) * (T + 1) + 2 * sizeof(uint32_t) * T +
-         sizeof(uint16_t) * kW * 256 + sizeof(uint32_t) * T;
+         sizeof(uint16_t) * kW * 256 + 2 * sizeof(uint32_t) * T;
 }
 
 cudaError_t launch_scatter(const SchemaDesc& sd, const FlushDesc& fd, cudaStream_t st) {

@@ -149,6 +149,9 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
       sd_.order[i] = take_binary ? binary[bi++] : fixed[fi++];
     }
   }
+  // the plan works on segments of up to kMaxSegTiles tiles when k_hash_count can keep the
+  // running rows and bytes of every partition of a segment in shared memory
+  seg_tiles_ = (int64_t)(1 + n_str_) * P_ <= kSegStateWords ? kMaxSegTiles : 1;
   // hash chain (HashSplitter::CreateProjector, splitter.cc:1402-1438)
   for (size_t k = 0; k < keys_.size(); k++) {
     const int ci = keys_[k];
@@ -466,7 +469,7 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
   // make room in the current flush group
   const size_t NB1 = pending_.size() + 1;
   const size_t tables_need = AlignUp(sizeof(BatchDesc) * NB1, 256) +
-                             AlignUp(sizeof(TileDesc) * (pending_tiles_ + ntiles), 256) +
+                             2 * AlignUp(sizeof(TileDesc) * (pending_tiles_ + ntiles), 256) +
                              AlignUp(sizeof(ColPtr) * NB1 * C, 256) + 256;
   if (!pending_.empty() &&
       (pending_bytes_ + batch_bytes > (uint64_t)opts_.flush_bytes || NB1 > (size_t)kMaxBatchesPerFlush ||
@@ -483,7 +486,7 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
     for (int k = 0; k < n_str_; k++) pending_chars_[b * n_str_ + k] = char_scratch_[k];
   }
   if (host_in) {
-    const size_t tables_one = AlignUp(sizeof(BatchDesc), 256) + AlignUp(sizeof(TileDesc) * ntiles, 256) +
+    const size_t tables_one = AlignUp(sizeof(BatchDesc), 256) + 2 * AlignUp(sizeof(TileDesc) * ntiles, 256) +
                               AlignUp(sizeof(ColPtr) * C, 256) + 256;
     st = EnsureStaging(batch_bytes + (direct_ ? phase_slack : tables_one));
     if (!st.ok()) return st;
@@ -646,18 +649,29 @@ Status Splitter::Flush() {
 
   // tables
   std::vector<BatchDesc> batches(NB);
+  std::vector<SegDesc> segs;
   std::vector<TileDesc> tiles;
   uint64_t R = 0;
   uint64_t emit_bound_a = 0;
   uint32_t smin = UINT32_MAX, capmax = (uint32_t)opts_.buffer_size;
+  uint32_t NT = 0;  // tiles
+  segs.reserve(pending_tiles_);
   tiles.reserve(pending_tiles_);
+  const uint32_t seg_rows = seg_tiles_ * (uint32_t)kTileRows;
   for (uint32_t b = 0; b < NB; b++) {
     const PendingBatch& pb = pending_[b];
-    const uint32_t nt = (pb.nrows + kTileRows - 1) / kTileRows;
-    batches[b] = BatchDesc{pb.nrows, (uint32_t)tiles.size(), nt, pb.split_size};
-    for (uint32_t t = 0; t < nt; t++) {
-      const uint32_t r0 = t * kTileRows;
-      tiles.push_back(TileDesc{b, r0, std::min<uint32_t>(kTileRows, pb.nrows - r0), (uint32_t)(R + r0)});
+    const uint32_t ns = (pb.nrows + seg_rows - 1) / seg_rows;
+    batches[b] = BatchDesc{pb.nrows, (uint32_t)segs.size(), ns, pb.split_size};
+    for (uint32_t g = 0; g < ns; g++) {
+      const uint32_t r0 = g * seg_rows;
+      const uint32_t nr = std::min<uint32_t>(seg_rows, pb.nrows - r0);
+      segs.push_back(SegDesc{b, r0, nr, (uint32_t)(R + r0), NT, {0, 0, 0}});
+      for (uint32_t q = 0; q * kTileRows < nr; q++) {
+        const uint32_t tr0 = r0 + q * kTileRows;
+        tiles.push_back(TileDesc{b, tr0, std::min<uint32_t>(kTileRows, pb.nrows - tr0), (uint32_t)(R + tr0),
+                                 (uint32_t)segs.size() - 1, q, {0, 0}});
+      }
+      NT = (uint32_t)tiles.size();
     }
     R += pb.nrows;
     emit_bound_a += std::min<uint64_t>((uint64_t)P, pb.nrows);
@@ -665,7 +679,7 @@ Status Splitter::Flush() {
     capmax = std::max(capmax, pb.nrows);
   }
   if (R >= (1ull << 31)) return Status::Error(GZ_INVALID, "flush too large");
-  const uint32_t T = (uint32_t)tiles.size();
+  const uint32_t T = (uint32_t)segs.size();
   const uint64_t emit_bound_b =
       2 * (R + (uint64_t)P * capmax) / std::max<uint32_t>(smin, 1) + 2 * (uint64_t)P + 16;
   const uint32_t emit_cap = (uint32_t)std::min(emit_bound_a, emit_bound_b) + 1;
@@ -734,7 +748,10 @@ Status Splitter::Flush() {
   const size_t s_bcnt = take(TP * nstr * 4 + 4);
   const size_t s_sbyte = take(TP * nstr * 4 + 4);
   const size_t s_null = take((size_t)NB * A * 4);
-  const size_t s_crange = take((size_t)T * std::max(nstr, 1) * 8);
+  const size_t s_crange = take((size_t)NT * std::max(nstr, 1) * 8);
+  const bool tile_prefix = seg_tiles_ > 1;
+  const size_t s_tpre = tile_prefix ? take((size_t)NT * P * 4) : 0;
+  const size_t s_tbpre = tile_prefix ? take((size_t)NT * std::max(nstr, 1) * P * 4) : 0;
   const size_t s_call = take((size_t)NB * 4);
   const size_t s_rec = take((size_t)NB * P * 4);
   const size_t s_hn = take((size_t)NB * 8);
@@ -743,9 +760,10 @@ Status Splitter::Flush() {
   const size_t meta_words = (3 + 2 * (size_t)nstr) * P + 1 + (size_t)emit_cap * (kEmitFixedWords + nstr);
   const size_t s_meta = take(meta_words * 4);  // rows_f, pstart, vstart, bytes_f, cstart, count, emits
   const size_t tb_batches = AlignUp(sizeof(BatchDesc) * NB, 256);
-  const size_t tb_tiles = AlignUp(sizeof(TileDesc) * T, 256);
+  const size_t tb_tiles = AlignUp(sizeof(SegDesc) * T, 256);
   const size_t tb_cols = AlignUp(sizeof(ColPtr) * NB * C, 256);
-  const size_t tb_total = tb_batches + tb_tiles + tb_cols;
+  const size_t tb_tdesc = AlignUp(sizeof(TileDesc) * NT, 256);
+  const size_t tb_total = tb_batches + tb_tiles + tb_cols + tb_tdesc;
   const bool staged_tables = host_in && !direct_;  // tables travel with the pinned staging copy
   const size_t s_tab = staged_tables ? 0 : take(tb_total);
   st = EnsureScratch(so);
@@ -755,7 +773,9 @@ Status Splitter::Flush() {
   FlushDesc fd;
   memset(&fd, 0, sizeof(fd));
   fd.n_batches = NB;
-  fd.n_tiles = T;
+  fd.n_segs = T;
+  fd.n_tiles = NT;
+  fd.seg_tiles = seg_tiles_;
   fd.n_rows = (uint32_t)R;
   fd.hist_in_smem = (size_t)P * (1 + nstr) * 4 <= 96 * 1024 ? 1 : 0;
   fd.pids = reinterpret_cast<uint16_t*>(S + s_pids);
@@ -765,6 +785,8 @@ Status Splitter::Flush() {
   fd.sbyte = reinterpret_cast<uint32_t*>(S + s_sbyte);
   fd.nullcnt = reinterpret_cast<uint32_t*>(S + s_null);
   fd.crange = reinterpret_cast<int2*>(S + s_crange);
+  fd.tilepre = tile_prefix ? reinterpret_cast<uint32_t*>(S + s_tpre) : nullptr;
+  fd.tilebpre = tile_prefix ? reinterpret_cast<uint32_t*>(S + s_tbpre) : nullptr;
   fd.call_flags = reinterpret_cast<uint32_t*>(S + s_call);
   fd.rec_idx = reinterpret_cast<uint32_t*>(S + s_rec);
   fd.hn = reinterpret_cast<unsigned long long*>(S + s_hn);
@@ -820,9 +842,10 @@ Status Splitter::Flush() {
     dtab = nullptr;
   }
   memcpy(htab, batches.data(), sizeof(BatchDesc) * NB);
-  memcpy(htab + tb_batches, tiles.data(), sizeof(TileDesc) * T);
+  memcpy(htab + tb_batches, segs.data(), sizeof(SegDesc) * T);
   ColPtr* hc = reinterpret_cast<ColPtr*>(htab + tb_batches + tb_tiles);
   memcpy(hc, pending_cols_.data(), sizeof(ColPtr) * NB * C);
+  memcpy(htab + tb_batches + tb_tiles + tb_cols, tiles.data(), sizeof(TileDesc) * NT);
   if (staged_tables) {
     st = Cuda(cudaMemcpyAsync(d_stage_[cur_], h_stage_[cur_], used_, cudaMemcpyHostToDevice, stream_), "H2D");
     stat_h2d_bytes_ += (int64_t)used_;
@@ -848,8 +871,9 @@ Status Splitter::Flush() {
     tab_cur_ ^= 1;
   }
   fd.batches = reinterpret_cast<const BatchDesc*>(dtab);
-  fd.tiles = reinterpret_cast<const TileDesc*>(dtab + tb_batches);
+  fd.segs = reinterpret_cast<const SegDesc*>(dtab + tb_batches);
   fd.cols = reinterpret_cast<const ColPtr*>(dtab + tb_batches + tb_tiles);
+  fd.tiles = reinterpret_cast<const TileDesc*>(dtab + tb_batches + tb_tiles + tb_cols);
 
   st = Cuda(cudaMemsetAsync(S + s_null, 0, (size_t)NB * A * 4, stream_), "memset");
   if (!st.ok()) return st;

@@ -158,6 +158,7 @@ class Splitter {
   std::vector<int32_t> field_buf0_;   // index of the field's first buffer in the flat list
   int32_t n_bufs_expected_ = 0;
   int32_t fixed_cnt_ = 0, n_str_ = 0, n_array_ = 0;
+  uint32_t seg_tiles_ = 1;  // tiles per k_scatter segment
   std::vector<uint64_t> empirical_;  // binary_array_empirical_size_
 
   // device
