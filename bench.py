@@ -286,6 +286,226 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------------------------------
+# Mixed-task forms.  Batches of three schemas (workload c1's, the wide fact table's, and
+# 6 int32 + 2 utf8 hashed on the first int32), rows log-uniform 1k-64k, partitions 64 / 200 / 1024.
+# A batch of r rows is the first r rows of one 65536-row batch per schema (slices of its
+# buffers), so no time goes into generating gigabytes of input.
+def _mixed_pool(seed: int):
+    from gazelle_plugin_gb300 import workloads as W
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return [W.c4_batch(rng, s, 65536) for s in range(3)]
+
+
+def _prefix_batch(batch, schema, r: int):
+    from gazelle_plugin_gb300 import workloads as W
+    bufs, i = [], 0
+    for f in schema:
+        if f.type == "null":
+            bufs += [batch.buffers[i], batch.buffers[i + 1]]
+            i += 2
+            continue
+        v = batch.buffers[i]
+        bufs.append(v[: (r + 7) // 8] if v.nbytes else v)
+        i += 1
+        if f.is_binary:
+            off = batch.buffers[i].view(np.int32)
+            bufs.append(off[: r + 1].view(np.uint8))
+            bufs.append(batch.buffers[i + 1][: int(off[r])])
+            i += 2
+        else:
+            nb = (r + 7) // 8 if f.type == "bool" else r * W.BYTE_WIDTH[f.type]
+            bufs.append(batch.buffers[i][:nb])
+            i += 1
+    return W.Batch(r, bufs)
+
+
+def run_batched(seed: int = 3, n_batches: int = 512, fuse_bytes: int = 64 << 20):
+    """Config 4: 512 uneven batches, each task = (schema, partitions); plain = every Split its own
+    device pass, waited for; batched = each task's batches fused into device passes of up to
+    `fuse_bytes` of input, the tasks' passes overlapping on the GPU."""
+    from gazelle_plugin_gb300 import shuffle as S
+    from gazelle_plugin_gb300 import workloads as W
+    pool = _mixed_pool(seed)
+    rng = np.random.Generator(np.random.PCG64(seed + 100))
+    calls = []
+    for _ in range(n_batches):
+        si = int(rng.integers(0, 3))
+        P = int(rng.choice(W.C4_PARTITIONS))
+        r = int(W.c4_rows(rng))
+        calls.append((si, P, _prefix_batch(pool[si], W.C4_SCHEMAS[si][0], r)))
+    in_bytes = sum(b.nbytes for _, _, b in calls)
+
+    def one(plain: bool):
+        w = S.ShuffleSplitterJniWrapper()
+        hs = {}
+        for si, P, _ in calls:
+            if (si, P) not in hs:
+                schema, keys = W.C4_SCHEMAS[si]
+                hs[(si, P)] = w.make(S.NativePartitioning("hash", P, None, keys, list(schema)),
+                                     writeSchema=False, dataFile="/dev/null",
+                                     flush_bytes=1 if plain else fuse_bytes)
+        t0 = time.perf_counter()
+        for si, P, b in calls:
+            a, z = b.addrs_sizes()
+            w.split(hs[(si, P)], b.num_rows, a, z)
+            if plain:
+                w.sync(hs[(si, P)])
+        for h in hs.values():
+            w.sync(h)
+        dt = time.perf_counter() - t0
+        out = 0
+        for (si, P), h in hs.items():
+            out += int(w.stop(h, P).rawPartitionLengths.sum())
+            w.close(h)
+        return dt, out
+
+    one(False)  # warm-up (allocations, pinned pools)
+    dt_p, out = one(True)
+    dt_b, _ = one(False)
+    alg = in_bytes + out
+    return {"workload": f"{n_batches} batches, rows log-uniform 1k-64k, 3 schemas x P in {{64,200,1024}}",
+            "fused_pass_bytes": fuse_bytes, "input_bytes": in_bytes, "partition_bytes": out,
+            "plain_gbs": alg / dt_p / 1e9, "batched_gbs": alg / dt_b / 1e9, "speedup": dt_p / dt_b}
+
+
+def _served_stream(seed: int, n_tasks: int, rate: float, gb_per_task: float):
+    """Config 5 call stream: Poisson arrivals (`rate` Split calls/s in total), each to a random
+    task still below its input quota; returns (task specs, [(t, task, si, rows)])."""
+    from gazelle_plugin_gb300 import workloads as W
+    rng = np.random.Generator(np.random.PCG64(seed))
+    specs = [(int(rng.integers(0, 3)), int(rng.choice(W.C4_PARTITIONS))) for _ in range(n_tasks)]
+    pool = _mixed_pool(seed)
+    # bytes of an r-row prefix, by schema, from the pool's cumulative sizes
+    per_row = [b.nbytes / b.num_rows for b in pool]
+    quota = gb_per_task * 1e9
+    got = [0.0] * n_tasks
+    live = list(range(n_tasks))
+    t, calls = 0.0, []
+    while live:
+        t += rng.exponential(1.0 / rate)
+        k = live[int(rng.integers(0, len(live)))]
+        r = int(W.c4_rows(rng))
+        calls.append((t, k, specs[k][0], r))
+        got[k] += r * per_row[specs[k][0]]
+        if got[k] >= quota:
+            live.remove(k)
+    return specs, calls, pool
+
+
+def run_served(seed: int = 4, n_tasks: int = 32, rate: float = 4000.0, gb_per_task: float = 2.0,
+               slots: int = 8, budget: int = 40 << 30, threshold: int = 256 << 20):
+    """Config 5: the call stream through the serving loop, and the same calls made one at a time
+    by the plain path (each Split its own device pass, waited for, in arrival order).  Each is run
+    paced at the arrival times (latency at the offered load) and unpaced (capacity)."""
+    import queue
+    from gazelle_plugin_gb300 import shuffle as S
+    from gazelle_plugin_gb300 import workloads as W
+    specs, calls, pool = _served_stream(seed, n_tasks, rate, gb_per_task)
+    batches = {}
+
+    def batch(si, r):
+        key = (si, r)
+        if key not in batches:
+            batches[key] = _prefix_batch(pool[si], W.C4_SCHEMAS[si][0], r)
+        return batches[key]
+
+    in_bytes = sum(batch(si, r).nbytes for _, _, si, r in calls)
+    last = {}
+    for i, (_, k, _, _) in enumerate(calls):
+        last[k] = i
+    opts = dict(writeSchema=False, dataFile="/dev/null", device_budget=threshold, flush_bytes=64 << 20)
+    # pinned host memory for the partition data spilled past the thresholds, taken up front as a
+    # server would at start (not timed)
+    S.pinned_reserve(max(0, int(1.1 * in_bytes) - n_tasks * threshold))
+    w = S.ShuffleSplitterJniWrapper()
+
+    def served(paced: bool):
+        """Submitter at the arrival times (or as fast as possible), a waiter collecting latencies."""
+        srv = S.ServeLoop(slots=slots, hbmBudget=budget)
+        tasks = [srv.open(W.C4_SCHEMAS[si][0], P, W.C4_SCHEMAS[si][1], **opts) for si, P in specs]
+        tickets = queue.Queue()
+        lat = []
+
+        def waiter():
+            while True:
+                tk = tickets.get()
+                if tk is None:
+                    return
+                lat.append(srv.wait(tk))
+
+        th = threading.Thread(target=waiter)
+        th.start()
+        syncs = []
+        t0 = time.perf_counter()
+        for i, (t, k, si, r) in enumerate(calls):
+            if paced:
+                d = t0 + t - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+            b = batch(si, r)
+            a, z = b.addrs_sizes()
+            tickets.put(srv.split(tasks[k], r, a, z))
+            if last[k] == i:
+                syncs.append(srv.sync(tasks[k]))  # the task's device work, after its last call
+        tickets.put(None)
+        th.join()
+        for tk in syncs:
+            srv.wait(tk)
+        dt = time.perf_counter() - t0
+        out = 0
+        for k, h in enumerate(tasks):
+            srv.wait(srv.stop(h))
+            out += int(w.stop(h, specs[k][1]).rawPartitionLengths.sum())
+            w.close(h)
+        srv.shutdown()
+        return lat, dt, out
+
+    def plain(paced: bool):
+        hs = [w.make(S.NativePartitioning("hash", P, None, W.C4_SCHEMAS[si][1], list(W.C4_SCHEMAS[si][0])),
+                     **dict(opts, flush_bytes=1)) for si, P in specs]
+        lat = []
+        t0 = time.perf_counter()
+        for t, k, si, r in calls:
+            if paced:
+                d = t0 + t - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+            b = batch(si, r)
+            a, z = b.addrs_sizes()
+            w.split(hs[k], r, a, z)
+            w.sync(hs[k])
+            lat.append((time.perf_counter() - t0 - (t if paced else 0.0)) * 1e9)
+        dt = time.perf_counter() - t0
+        out = 0
+        for k, h in enumerate(hs):
+            out += int(w.stop(h, specs[k][1]).rawPartitionLengths.sum())
+            w.close(h)
+        return lat, dt, out
+
+    def pct(v, q):
+        return float(np.percentile(np.asarray(v, np.float64), q)) / 1e6
+
+    res = {}
+    for name, fn in (("served", served), ("plain", plain)):
+        lat, dt, out = fn(True)
+        _, dt_cap, _ = fn(False)
+        alg = in_bytes + out
+        res[name] = {"p50_ms": pct(lat, 50), "p90_ms": pct(lat, 90), "p99_ms": pct(lat, 99),
+                     "max_ms": max(lat) / 1e6, "gbs_at_offered_load": alg / dt / 1e9,
+                     "capacity_gbs": alg / dt_cap / 1e9, "capacity_splits_per_s": len(calls) / dt_cap}
+        res["partition_bytes"] = out
+    return {"workload": (f"{n_tasks} tasks, Poisson {rate:.0f} Split/s, rows log-uniform 1k-64k, "
+                         f"3 schemas x P in {{64,200,1024}}, stop after {gb_per_task:g} GB input per task, "
+                         f"spill threshold {threshold >> 20} MiB, HBM budget {budget >> 30} GiB, "
+                         f"{slots} serving workers"),
+            "latency": "per Split call, submission (paced at its arrival time) to completion",
+            "capacity": "the same calls submitted without pacing",
+            "calls": len(calls), "input_bytes": in_bytes, "partition_bytes": res.pop("partition_bytes"),
+            "served": res["served"], "plain": res["plain"],
+            "capacity_ratio": res["served"]["capacity_gbs"] / res["plain"]["capacity_gbs"]}
+
+
+# ---------------------------------------------------------------------------------------
 def run_gpu(args):
     import torch
     from gazelle_plugin_gb300 import shuffle as S
@@ -426,6 +646,9 @@ def run_gpu(args):
             "input_gbs": in_bytes * args.steps * world / t_max / 1e9,
             "stop_s": stop_s,
         }
+        if not args.no_forms:
+            line["batched"] = run_batched()
+            line["served"] = run_served(gb_per_task=args.served_gb_per_task)
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -444,6 +667,8 @@ def main():
     ap.add_argument("--traffic-per-launch", type=float, default=None)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the batched and served forms")
+    ap.add_argument("--served-gb-per-task", type=float, default=2.0)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

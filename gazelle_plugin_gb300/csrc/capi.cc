@@ -14,7 +14,9 @@
 
 #include "../../include/gz_split.h"
 #include "hash_static.h"
+#include "host_util.h"
 #include "schema_ipc.h"
+#include "serve.h"
 #include "splitter.h"
 
 namespace {
@@ -22,10 +24,15 @@ namespace {
 struct Entry {
   std::unique_ptr<gz::Splitter> splitter;
   std::string last_error;
+  int64_t server = 0;   // serving loop of a served task (0: called directly)
+  int32_t slot = 0;     // its worker
+  int64_t reserve = 0;  // HBM budget it holds until it stops
 };
 
-std::mutex g_mu;
-std::map<int64_t, std::shared_ptr<Entry>> g_table;
+// Process-wide tables are never destroyed: handles still open at exit are not torn down by
+// static destructors, whose order across files (the pinned pool, the CUDA runtime) is unspecified.
+std::mutex& g_mu = *new std::mutex;
+std::map<int64_t, std::shared_ptr<Entry>>& g_table = *new std::map<int64_t, std::shared_ptr<Entry>>;
 int64_t g_next_id = 4;
 thread_local std::string t_make_error;
 
@@ -40,9 +47,17 @@ GzStatus Report(Entry* e, const gz::Status& st) {
   return st.code;
 }
 
+std::map<int64_t, std::shared_ptr<gz::ServeLoop>>& g_servers = *new std::map<int64_t, std::shared_ptr<gz::ServeLoop>>;
+
+std::shared_ptr<gz::ServeLoop> LookupServer(int64_t id) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_servers.find(id);
+  return it == g_servers.end() ? nullptr : it->second;
+}
+
 GzStatus MakeCommon(const char* short_name, int32_t num_partitions, std::vector<gz::Field> fields,
                     const int32_t* key_cols, int32_t n_keys, const GzSplitOptions* opts,
-                    int64_t* out_handle) {
+                    int64_t* out_handle, std::shared_ptr<Entry>* out_entry = nullptr) {
   if (out_handle == nullptr || short_name == nullptr) {
     t_make_error = "null argument";
     return GZ_INVALID;
@@ -59,10 +74,26 @@ GzStatus MakeCommon(const char* short_name, int32_t num_partitions, std::vector<
   }
   auto e = std::make_shared<Entry>();
   e->splitter = std::move(s);
+  if (out_entry) *out_entry = e;
   std::lock_guard<std::mutex> lk(g_mu);
   *out_handle = g_next_id++;
   g_table[*out_handle] = e;
   return GZ_OK;
+}
+
+std::vector<gz::Field> FieldsFrom(const GzField* fields, int32_t n_fields) {
+  std::vector<gz::Field> fs;
+  for (int i = 0; i < n_fields; i++) {
+    gz::Field f;
+    f.type = fields[i].type;
+    f.nullable = fields[i].nullable != 0;
+    f.precision = fields[i].precision;
+    f.scale = fields[i].scale;
+    f.unit = fields[i].unit;
+    f.name = fields[i].name ? fields[i].name : "";
+    fs.push_back(f);
+  }
+  return fs;
 }
 
 }  // namespace
@@ -108,18 +139,7 @@ GzStatus gz_split_make_fields(const char* short_name, int32_t num_partitions,
     t_make_error = "Make splitter schema can't be null";
     return GZ_INVALID;
   }
-  std::vector<gz::Field> fs;
-  for (int i = 0; i < n_fields; i++) {
-    gz::Field f;
-    f.type = fields[i].type;
-    f.nullable = fields[i].nullable != 0;
-    f.precision = fields[i].precision;
-    f.scale = fields[i].scale;
-    f.unit = fields[i].unit;
-    f.name = fields[i].name ? fields[i].name : "";
-    fs.push_back(f);
-  }
-  return MakeCommon(short_name, num_partitions, std::move(fs), key_cols, n_keys, opts, out_handle);
+  return MakeCommon(short_name, num_partitions, FieldsFrom(fields, n_fields), key_cols, n_keys, opts, out_handle);
 }
 
 GzStatus gz_split_split(int64_t handle, int32_t num_rows, const int64_t* buf_addrs,
@@ -170,7 +190,8 @@ GzStatus gz_split_stop(int64_t handle, GzSplitResult* out) {
     t_make_error = "Invalid splitter id " + std::to_string(handle);
     return GZ_INVALID;
   }
-  GzStatus s = Report(e.get(), e->splitter->Stop());
+  // a served task was stopped by its loop; its results are read here
+  GzStatus s = (e->server && e->splitter->stopped()) ? GZ_OK : Report(e.get(), e->splitter->Stop());
   if (s != GZ_OK || out == nullptr) return s;
   gz::Splitter& sp = *e->splitter;
   out->total_compute_pid_time = sp.TotalComputePidTime();
@@ -219,6 +240,11 @@ GzStatus gz_split_close(int64_t handle) {
     e = it->second;
     g_table.erase(it);
   }
+  if (e->server && e->reserve > 0) {  // a served task closed without stopping
+    auto srv = LookupServer(e->server);
+    if (srv) srv->Release(e->reserve);
+    e->reserve = 0;
+  }
   return GZ_OK;
 }
 
@@ -251,6 +277,121 @@ GzStatus gz_split_stats(int64_t handle, int64_t* out8) {
   auto e = Lookup(handle);
   if (!e || !out8) return GZ_INVALID;
   e->splitter->Stats(out8);
+  return GZ_OK;
+}
+
+GzStatus gz_serve_start(int32_t slots, int64_t hbm_budget, int64_t* out_server) {
+  if (out_server == nullptr || hbm_budget <= 0) {
+    t_make_error = "gz_serve_start: null out_server or non-positive budget";
+    return GZ_INVALID;
+  }
+  auto srv = std::make_shared<gz::ServeLoop>(slots, hbm_budget);
+  std::lock_guard<std::mutex> lk(g_mu);
+  *out_server = g_next_id++;
+  g_servers[*out_server] = srv;
+  return GZ_OK;
+}
+
+GzStatus gz_serve_open(int64_t server, const char* short_name, int32_t num_partitions, const GzField* fields,
+                       int32_t n_fields, const int32_t* key_cols, int32_t n_keys, const GzSplitOptions* opts,
+                       int64_t* out_task) {
+  auto srv = LookupServer(server);
+  if (!srv || out_task == nullptr || (fields == nullptr && n_fields > 0)) {
+    t_make_error = "gz_serve_open: invalid server or arguments";
+    return GZ_INVALID;
+  }
+  GzSplitOptions o;
+  if (opts) o = *opts;
+  else gz_split_default_options(&o);
+  // its share of the budget: resident partition data up to the spill threshold, two staging
+  // buffers and the pass scratch
+  const int64_t reserve = std::max<int64_t>(o.device_budget, 0) + 3 * std::max<int64_t>(o.flush_bytes, 0) + (64ll << 20);
+  gz::Status st = srv->Admit(reserve);
+  if (!st.ok()) {
+    t_make_error = "gz_serve_open: " + st.msg;
+    return st.code;
+  }
+  std::shared_ptr<Entry> e;
+  GzStatus s = MakeCommon(short_name, num_partitions, FieldsFrom(fields, n_fields), key_cols, n_keys, &o,
+                          out_task, &e);
+  if (s != GZ_OK) {
+    srv->Release(reserve);
+    return s;
+  }
+  e->server = server;
+  e->slot = srv->AssignSlot();
+  e->reserve = reserve;
+  return GZ_OK;
+}
+
+GzStatus gz_serve_split(int64_t server, int64_t task, int32_t num_rows, const int64_t* buf_addrs,
+                        const int64_t* buf_sizes, int32_t n_bufs, int64_t* out_ticket) {
+  auto srv = LookupServer(server);
+  auto e = Lookup(task);
+  if (!srv || !e || e->server != server || !buf_addrs || !buf_sizes || !out_ticket) {
+    t_make_error = "gz_serve_split: invalid server, task or arguments";
+    return GZ_INVALID;
+  }
+  *out_ticket = srv->Submit(e->slot, e->splitter.get(), e, gz::ServeLoop::kSplit, num_rows, buf_addrs, buf_sizes,
+                            n_bufs, 0);
+  return GZ_OK;
+}
+
+GzStatus gz_serve_stop(int64_t server, int64_t task, int64_t* out_ticket) {
+  auto srv = LookupServer(server);
+  auto e = Lookup(task);
+  if (!srv || !e || e->server != server || !out_ticket) {
+    t_make_error = "gz_serve_stop: invalid server, task or arguments";
+    return GZ_INVALID;
+  }
+  const int64_t release = e->reserve;
+  e->reserve = 0;
+  *out_ticket = srv->Submit(e->slot, e->splitter.get(), e, gz::ServeLoop::kStop, 0, nullptr, nullptr, 0, release);
+  return GZ_OK;
+}
+
+GzStatus gz_serve_sync(int64_t server, int64_t task, int64_t* out_ticket) {
+  auto srv = LookupServer(server);
+  auto e = Lookup(task);
+  if (!srv || !e || e->server != server || !out_ticket) {
+    t_make_error = "gz_serve_sync: invalid server, task or arguments";
+    return GZ_INVALID;
+  }
+  *out_ticket = srv->Submit(e->slot, e->splitter.get(), e, gz::ServeLoop::kSync, 0, nullptr, nullptr, 0, 0);
+  return GZ_OK;
+}
+
+GzStatus gz_serve_wait(int64_t server, int64_t ticket, int64_t* out_latency_ns, int64_t* out_service_ns) {
+  auto srv = LookupServer(server);
+  if (!srv) {
+    t_make_error = "gz_serve_wait: invalid server";
+    return GZ_INVALID;
+  }
+  gz::Status st = srv->Wait(ticket, out_latency_ns, out_service_ns);
+  if (!st.ok()) t_make_error = st.msg;
+  return st.code;
+}
+
+GzStatus gz_pinned_reserve(int64_t bytes, int64_t* out_reserved) {
+  const int64_t got = gz::PinnedReserve(bytes, gz::kPinnedSlab);
+  if (out_reserved) *out_reserved = got;
+  if (got < bytes) {
+    t_make_error = "gz_pinned_reserve: pinned host memory ran out after " + std::to_string(got) + " bytes";
+    return GZ_OOM;
+  }
+  return GZ_OK;
+}
+
+GzStatus gz_serve_shutdown(int64_t server) {
+  std::shared_ptr<gz::ServeLoop> srv;
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_servers.find(server);
+    if (it == g_servers.end()) return GZ_OK;
+    srv = it->second;
+    g_servers.erase(it);
+  }
+  srv.reset();  // finishes queued calls and joins the workers (when no other call holds it)
   return GZ_OK;
 }
 

@@ -14,35 +14,101 @@
 namespace gz {
 
 // ---------------------------------------------------------------------------------------
+// Pinned pool: slabs of page-locked memory (cudaHostAlloc is slow and never undone here),
+// carved best-fit into blocks in 64 KiB units; a freed block merges with free neighbours of the
+// same slab.  Blocks never span two slabs, so each is inside one cudaHostAlloc allocation.
 namespace {
-std::mutex g_pin_mu;
-std::multimap<size_t, uint8_t*> g_pin_free;  // cap -> block
+constexpr size_t kPinUnit = size_t(64) << 10;
+constexpr size_t kSlab = size_t(1) << 30;
+
+struct PinPool {
+  std::mutex mu;
+  std::map<uint8_t*, std::pair<size_t, int>> free_by_addr;  // start -> (bytes, slab)
+  std::multimap<size_t, uint8_t*> free_by_size;              // bytes -> start
+  std::vector<std::pair<uint8_t*, size_t>> slabs;
+
+  void insert(uint8_t* p, size_t n, int slab) {
+    free_by_addr[p] = {n, slab};
+    free_by_size.emplace(n, p);
+  }
+  void erase_size(uint8_t* p, size_t n) {
+    auto r = free_by_size.equal_range(n);
+    for (auto it = r.first; it != r.second; ++it)
+      if (it->second == p) {
+        free_by_size.erase(it);
+        return;
+      }
+  }
+  int slab_of(uint8_t* p) const {
+    for (size_t i = 0; i < slabs.size(); i++)
+      if (p >= slabs[i].first && p < slabs[i].first + slabs[i].second) return (int)i;
+    return -1;
+  }
+  bool add_slab(size_t n) {  // mu held
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, n, cudaHostAllocDefault) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    slabs.push_back({static_cast<uint8_t*>(p), n});
+    insert(static_cast<uint8_t*>(p), n, (int)slabs.size() - 1);
+    return true;
+  }
+};
+// never destroyed: splitters may give blocks back during exit
+PinPool& g_pin = *new PinPool;
 }  // namespace
 
 PinnedBlock PinnedAcquire(size_t bytes) {
-  const size_t gran = 2u << 20;
-  const size_t cap = (bytes + gran - 1) / gran * gran;
-  {
-    std::lock_guard<std::mutex> lk(g_pin_mu);
-    auto it = g_pin_free.lower_bound(cap);
-    if (it != g_pin_free.end() && it->first <= 2 * cap + gran) {
-      PinnedBlock b{it->second, it->first};
-      g_pin_free.erase(it);
-      return b;
-    }
+  const size_t n = (std::max<size_t>(bytes, 1) + kPinUnit - 1) / kPinUnit * kPinUnit;
+  std::lock_guard<std::mutex> lk(g_pin.mu);
+  auto it = g_pin.free_by_size.lower_bound(n);
+  if (it == g_pin.free_by_size.end()) {
+    if (!g_pin.add_slab(std::max(n, kSlab))) return PinnedBlock{};
+    it = g_pin.free_by_size.lower_bound(n);
   }
-  void* p = nullptr;
-  if (cudaHostAlloc(&p, cap, cudaHostAllocDefault) != cudaSuccess) {
-    cudaGetLastError();
-    return PinnedBlock{};
-  }
-  return PinnedBlock{static_cast<uint8_t*>(p), cap};
+  uint8_t* p = it->second;
+  const size_t have = it->first;
+  g_pin.free_by_size.erase(it);
+  const int slab = g_pin.free_by_addr[p].second;
+  g_pin.free_by_addr.erase(p);
+  if (have > n) g_pin.insert(p + n, have - n, slab);
+  return PinnedBlock{p, n};
 }
 
 void PinnedRelease(PinnedBlock b) {
   if (!b.ptr) return;
-  std::lock_guard<std::mutex> lk(g_pin_mu);
-  g_pin_free.emplace(b.cap, b.ptr);
+  std::lock_guard<std::mutex> lk(g_pin.mu);
+  uint8_t* p = b.ptr;
+  size_t n = b.cap;
+  const int slab = g_pin.slab_of(p);
+  auto next = g_pin.free_by_addr.find(p + n);
+  if (next != g_pin.free_by_addr.end() && next->second.second == slab) {
+    n += next->second.first;
+    g_pin.erase_size(next->first, next->second.first);
+    g_pin.free_by_addr.erase(next);
+  }
+  auto prev = g_pin.free_by_addr.lower_bound(p);
+  if (prev != g_pin.free_by_addr.begin()) {
+    --prev;
+    if (prev->first + prev->second.first == p && prev->second.second == slab) {
+      p = prev->first;
+      n += prev->second.first;
+      g_pin.erase_size(prev->first, prev->second.first);
+      g_pin.free_by_addr.erase(prev);
+    }
+  }
+  g_pin.insert(p, n, slab);
+}
+
+int64_t PinnedReserve(int64_t bytes, size_t block) {
+  int64_t got = 0;
+  std::lock_guard<std::mutex> lk(g_pin.mu);
+  while (got < bytes) {
+    if (!g_pin.add_slab(block)) break;
+    got += (int64_t)block;
+  }
+  return got;
 }
 
 // ---------------------------------------------------------------------------------------

@@ -15,9 +15,14 @@ struct PinnedBlock {
 };
 
 // Pinned (page-locked) host blocks, reused across splitters.  Acquire returns a block of at
-// least `bytes`; ptr == nullptr when cudaHostAlloc failed.
+// least `bytes` (cap = its size); ptr == nullptr when cudaHostAlloc failed.  Release takes back
+// exactly a block Acquire returned.
 PinnedBlock PinnedAcquire(size_t bytes);
 void PinnedRelease(PinnedBlock b);
+// Adds about `bytes` of pinned slabs of `block` bytes to the pool up front (cudaHostAlloc is
+// slow, so a server takes that cost at start instead of inside calls); returns the bytes added.
+int64_t PinnedReserve(int64_t bytes, size_t block);
+constexpr size_t kPinnedSlab = size_t(1) << 30;
 
 struct CopyJob {
   uint8_t* dst;

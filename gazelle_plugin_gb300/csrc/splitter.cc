@@ -208,9 +208,10 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
   }
   if (direct_) {
     jobs_cap_ = size_t(1) << 20;  // 24 MiB of descriptors: a refill waits for the device
-    st = Cuda(cudaHostAlloc(reinterpret_cast<void**>(&h_jobs_), jobs_cap_ * sizeof(HostCopy),
-                            cudaHostAllocDefault), "cudaHostAlloc(gather jobs)");
-    if (!st.ok()) return st;
+    const PinnedBlock b = PinnedAcquire(jobs_cap_ * sizeof(HostCopy));
+    if (!b.ptr) return Status::Error(GZ_OOM, "pinned host memory for the gather descriptors");
+    h_jobs_ = reinterpret_cast<HostCopy*>(b.ptr);
+    h_jobs_bytes_ = b.cap;
   }
   {
     cudaMemPool_t pool;
@@ -224,7 +225,7 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
                              AlignUp(sizeof(unsigned long long) * P_, 256) +
                              AlignUp(sizeof(uint32_t) * (size_t)std::max(n_str_, 1) * P_, 256) +
                              256 * 3;
-  st = Cuda(cudaMalloc(&d_state_, state_bytes), "cudaMalloc(state)");
+  st = Cuda(cudaMallocAsync(reinterpret_cast<void**>(&d_state_), state_bytes, stream_), "cudaMallocAsync(state)");
   if (!st.ok()) return st;
   st = Cuda(cudaMemsetAsync(d_state_, 0, state_bytes, stream_), "cudaMemset(state)");
   if (!st.ok()) return st;
@@ -259,24 +260,24 @@ Splitter::~Splitter() {
   if (stream_) cudaStreamSynchronize(stream_);
   if (ostream_) cudaStreamSynchronize(ostream_);
   for (auto& f : flushes_) {
-    if (f.d_out) cudaFree(f.d_out);
-    PinnedRelease(f.h_block);
+    if (f.d_out) cudaFreeAsync(f.d_out, stream_);
     for (auto& e : f.ev)
       if (e) cudaEventDestroy(e);
   }
-  for (auto& c : meta_chunks_) cudaFreeHost(c);
+  ReleaseHost();
+  for (auto& c : meta_chunks_) PinnedRelease(c);
   for (int i = 0; i < 2; i++) {
-    if (h_tables_[i]) cudaFreeHost(h_tables_[i]);
+    PinnedRelease(PinnedBlock{h_tables_[i], tables_cap_[i]});
     if (tab_ev_[i]) cudaEventDestroy(tab_ev_[i]);
   }
   for (int i = 0; i < 2; i++) {
-    if (h_stage_[i]) cudaFreeHost(h_stage_[i]);
-    if (d_stage_[i]) cudaFree(d_stage_[i]);
+    PinnedRelease(PinnedBlock{h_stage_[i], h_stage_cap_});
+    if (d_stage_[i]) cudaFreeAsync(d_stage_[i], stream_);
     if (stage_ev_[i]) cudaEventDestroy(stage_ev_[i]);
   }
-  if (d_scratch_) cudaFree(d_scratch_);
-  if (d_state_) cudaFree(d_state_);
-  if (h_jobs_) cudaFreeHost(h_jobs_);
+  if (d_scratch_) cudaFreeAsync(d_scratch_, stream_);
+  if (d_state_) cudaFreeAsync(d_state_, stream_);
+  PinnedRelease(PinnedBlock{reinterpret_cast<uint8_t*>(h_jobs_), h_jobs_bytes_});
   if (gather_ev_) cudaEventDestroy(gather_ev_);
   if (cstream_) cudaStreamDestroy(cstream_);
   if (ostream_) cudaStreamDestroy(ostream_);
@@ -320,20 +321,23 @@ Status Splitter::EnsureStaging(size_t bytes) {
   if (!st.ok()) return st;
   size_t cap = AlignUp(std::max<size_t>(bytes, (size_t)opts_.flush_bytes + (8u << 20)), 1 << 20);
   for (int i = 0; i < 2; i++) {
-    if (h_stage_[i]) cudaFreeHost(h_stage_[i]);
-    if (d_stage_[i]) cudaFree(d_stage_[i]);
+    PinnedRelease(PinnedBlock{h_stage_[i], h_stage_cap_});
+    if (d_stage_[i]) cudaFreeAsync(d_stage_[i], stream_);
     h_stage_[i] = nullptr;
     d_stage_[i] = nullptr;
     if (!direct_) {
-      st = Cuda(cudaHostAlloc(&h_stage_[i], cap, cudaHostAllocDefault), "cudaHostAlloc(stage)");
-      if (!st.ok()) return st;
+      const PinnedBlock b = PinnedAcquire(cap);
+      if (!b.ptr) return Status::Error(GZ_OOM, "pinned host memory for staging");
+      h_stage_[i] = b.ptr;
+      h_stage_cap_ = b.cap;
     }
-    st = Cuda(cudaMalloc(&d_stage_[i], cap), "cudaMalloc(stage)");
+    st = Cuda(cudaMallocAsync(reinterpret_cast<void**>(&d_stage_[i]), cap, stream_), "cudaMallocAsync(stage)");
     if (!st.ok()) return st;
     stage_busy_[i] = false;
   }
   stage_cap_ = cap;
-  return Status::OK();
+  // the staging is written on cstream_ (k_gather): its allocation on stream_ must be complete
+  return Cuda(cudaStreamSynchronize(stream_), "sync");
 }
 
 Status Splitter::Split(int32_t num_rows, const int64_t* addrs, const int64_t* sizes, int32_t n) {
@@ -610,29 +614,28 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
 Status Splitter::PinnedMeta(size_t bytes, uint32_t** out) {
   bytes = AlignUp(bytes, 256);
   if (meta_chunks_.empty() || meta_used_ + bytes > meta_chunk_cap_) {
-    const size_t cap = std::max<size_t>(bytes, 4u << 20);
-    void* c = nullptr;
-    Status st = Cuda(cudaHostAlloc(&c, cap, cudaHostAllocDefault), "cudaHostAlloc(meta)");
-    if (!st.ok()) return st;
+    const PinnedBlock c = PinnedAcquire(std::max<size_t>(bytes, 4u << 20));
+    if (!c.ptr) return Status::Error(GZ_OOM, "pinned host memory for pass metadata");
     meta_chunks_.push_back(c);
-    meta_chunk_cap_ = cap;
+    meta_chunk_cap_ = c.cap;
     meta_used_ = 0;
   }
-  *out = reinterpret_cast<uint32_t*>(static_cast<uint8_t*>(meta_chunks_.back()) + meta_used_);
+  *out = reinterpret_cast<uint32_t*>(meta_chunks_.back().ptr + meta_used_);
   meta_used_ += bytes;
   return Status::OK();
 }
 
 Status Splitter::EnsureScratch(size_t bytes) {
   if (bytes <= scratch_cap_) return Status::OK();
+  // stream-ordered (no wait for the whole device, which other splitters may be using): the old
+  // scratch is freed after the passes already queued on stream_
   if (d_scratch_) {
-    Status st = Cuda(cudaStreamSynchronize(stream_), "sync");
+    Status st = Cuda(cudaFreeAsync(d_scratch_, stream_), "cudaFreeAsync(scratch)");
     if (!st.ok()) return st;
-    cudaFree(d_scratch_);
     d_scratch_ = nullptr;
   }
   size_t cap = AlignUp(bytes + bytes / 4, 1 << 20);
-  Status st = Cuda(cudaMalloc(&d_scratch_, cap), "cudaMalloc(scratch)");
+  Status st = Cuda(cudaMallocAsync(reinterpret_cast<void**>(&d_scratch_), cap, stream_), "cudaMallocAsync(scratch)");
   if (!st.ok()) return st;
   scratch_cap_ = cap;
   return Status::OK();
@@ -832,10 +835,12 @@ Status Splitter::Flush() {
       tab_busy_[ti] = false;
     }
     if (tb_total > tables_cap_[ti]) {
-      if (h_tables_[ti]) cudaFreeHost(h_tables_[ti]);
+      PinnedRelease(PinnedBlock{h_tables_[ti], tables_cap_[ti]});
       h_tables_[ti] = nullptr;
-      tables_cap_[ti] = AlignUp(tb_total * 2, 1 << 16);
-      st = Cuda(cudaHostAlloc(&h_tables_[ti], tables_cap_[ti], cudaHostAllocDefault), "cudaHostAlloc(tables)");
+      const PinnedBlock b = PinnedAcquire(AlignUp(tb_total * 2, 1 << 20));
+      if (!b.ptr) return Status::Error(GZ_OOM, "pinned host memory for the pass tables");
+      h_tables_[ti] = b.ptr;
+      tables_cap_[ti] = b.cap;
       if (!st.ok()) return st;
     }
     htab = h_tables_[ti];
@@ -946,12 +951,12 @@ Status Splitter::Flush() {
 // ordered); the host bytes are valid once the stream has reached this point.
 Status Splitter::MoveFlushToHost(FlushRec& f) {
   if (f.on_host) return Status::OK();
-  f.h_block = PinnedAcquire(f.out_bytes);
-  if (!f.h_block.ptr) return Status::Error(GZ_OOM, "pinned host memory for partition data");
+  f.h_out = HostAlloc(f.out_bytes);
+  if (!f.h_out) return Status::Error(GZ_OOM, "pinned host memory for partition data");
   // on its own stream, after the pass's kernels, so the copy overlaps the next pass
   Status st = Cuda(cudaStreamWaitEvent(ostream_, f.ev[3], 0), "wait pass");
   if (!st.ok()) return st;
-  st = Cuda(cudaMemcpyAsync(f.h_block.ptr, f.d_out, f.out_bytes, cudaMemcpyDeviceToHost, ostream_),
+  st = Cuda(cudaMemcpyAsync(f.h_out, f.d_out, f.out_bytes, cudaMemcpyDeviceToHost, ostream_),
             "D2H out");
   if (!st.ok()) return st;
   st = Cuda(cudaFreeAsync(f.d_out, ostream_), "cudaFreeAsync");
@@ -1068,7 +1073,7 @@ Status Splitter::AssembleAndWrite(int p, Segment& s, ByteSink* sink, bool count_
       }
       *all_ones = false;
       const uint64_t bit0 = (uint64_t)f.vstart(P)[p] + pc.vpos0;  // multiple of 64
-      return f.h_block.ptr + off + bit0 / 8;
+      return f.h_out + off + bit0 / 8;
     }
     temps.emplace_back(nb, 0xff);
     uint8_t* dst = temps.back().data();
@@ -1080,7 +1085,7 @@ Status Splitter::AssembleAndWrite(int p, Segment& s, ByteSink* sink, bool count_
       const uint32_t len = pc.frow1 - pc.frow0;
       if (off != SIZE_MAX) {
         const uint64_t bit0 = (uint64_t)f.vstart(P)[p] + pc.vpos0;
-        CopyBits(f.h_block.ptr + off, bit0, dst, drow, len);
+        CopyBits(f.h_out + off, bit0, dst, drow, len);
         any = true;
       }
       drow += len;
@@ -1120,7 +1125,7 @@ Status Splitter::AssembleAndWrite(int p, Segment& s, ByteSink* sink, bool count_
       ChunkedBuffer vals;
       for (const Piece& pc : s.pieces) {
         const FlushRec& f = flushes_[pc.flush];
-        const uint8_t* base = f.h_block.ptr + f.off_values[a];
+        const uint8_t* base = f.h_out + f.off_values[a];
         vals.push_back(Chunk{base + ((size_t)f.pstart(P)[p] + pc.frow0) * w,
                              (int64_t)(pc.frow1 - pc.frow0) * w});
       }
@@ -1142,9 +1147,9 @@ Status Splitter::AssembleAndWrite(int p, Segment& s, ByteSink* sink, bool count_
       int64_t clen = 0;
       for (const Piece& pc : s.pieces) {
         const FlushRec& f = flushes_[pc.flush];
-        const uint8_t* ob = f.h_block.ptr + f.off_values[a];
+        const uint8_t* ob = f.h_out + f.off_values[a];
         offs.push_back(Chunk{ob + ((size_t)f.pstart(P)[p] + pc.frow0) * 4, (int64_t)(pc.frow1 - pc.frow0) * 4});
-        const uint8_t* cb = f.h_block.ptr + f.off_chars[a];
+        const uint8_t* cb = f.h_out + f.off_chars[a];
         const uint32_t c0 = pc.fb0[k], c1 = pc.fb1[k];
         if (c1 > c0) chars.push_back(Chunk{cb + (size_t)f.cstart(P, nstr)[(size_t)k * P + p] + c0, (int64_t)(c1 - c0)});
         clen += c1 - c0;
@@ -1257,11 +1262,39 @@ Status Splitter::Stop() {
   total_write_time_ += NowNs() - t0 - compress_ns;
   stopped_ = true;
   // the pinned copies are no longer needed
-  for (auto& f : flushes_) {
-    PinnedRelease(f.h_block);
-    f.h_block = PinnedBlock{};
-  }
+  ReleaseHost();
+  ReleaseStaging();
   return Status::OK();
+}
+
+// Pinned host space for one pass's partition data, from the process-wide pool; everything goes
+// back at Stop.
+uint8_t* Splitter::HostAlloc(size_t bytes) {
+  PinnedBlock b = PinnedAcquire(bytes);
+  if (!b.ptr) return nullptr;
+  host_chunks_.push_back(b);
+  return b.ptr;
+}
+
+void Splitter::ReleaseHost() {
+  for (auto& b : host_chunks_) PinnedRelease(b);
+  host_chunks_.clear();
+  for (auto& f : flushes_) f.h_out = nullptr;
+}
+
+// After Stop nothing more is split: staging and scratch go back (all streams are idle).
+void Splitter::ReleaseStaging() {
+  for (int i = 0; i < 2; i++) {
+    PinnedRelease(PinnedBlock{h_stage_[i], h_stage_cap_});
+    if (d_stage_[i]) cudaFreeAsync(d_stage_[i], stream_);
+    h_stage_[i] = nullptr;
+    d_stage_[i] = nullptr;
+    stage_busy_[i] = false;
+  }
+  stage_cap_ = 0;
+  if (d_scratch_) cudaFreeAsync(d_scratch_, stream_);
+  d_scratch_ = nullptr;
+  scratch_cap_ = 0;
 }
 
 Status Splitter::SpillFixedSize(int64_t size, int64_t* actual) {
@@ -1356,8 +1389,8 @@ Status Splitter::LastPids(uint16_t* out, int32_t n) {
   if (!st.ok()) return st;
   st = SyncAndCheck();
   if (!st.ok()) return st;
-  if (flushes_.empty() || (uint32_t)n != last_batch_rows_)
-    return Status::Error(GZ_INVALID, "no batch of that size was split last");
+  if (flushes_.empty() || (uint32_t)n != last_batch_rows_ || d_scratch_ == nullptr)
+    return Status::Error(GZ_INVALID, "no batch of that size was split last (or the splitter stopped)");
   const FlushRec& f = flushes_.back();
   // the pids of the last flush sit at the start of the scratch; the last batch is at its end
   const uint16_t* pids = reinterpret_cast<const uint16_t*>(d_scratch_);

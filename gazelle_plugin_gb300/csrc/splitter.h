@@ -74,6 +74,7 @@ class Splitter {
   const std::vector<int64_t>& RawPartitionLengths() const { return raw_partition_lengths_; }
   const std::vector<uint8_t>& DataBytes() const { return data_bytes_; }
   int32_t num_partitions() const { return P_; }
+  bool stopped() const { return stopped_; }
 
  private:
   struct PendingBatch {
@@ -92,7 +93,7 @@ class Splitter {
     uint32_t n_batches = 0;
     uint8_t* d_out = nullptr;           // device outputs (nullptr once moved to host)
     size_t out_bytes = 0;
-    PinnedBlock h_block;                // pinned host copy of the outputs
+    uint8_t* h_out = nullptr;           // pinned host copy of the outputs (in host_chunks_)
     bool on_host = false;
     std::vector<size_t> off_values, off_bits, off_valid, off_chars;  // per array column, SIZE_MAX: none
     uint32_t* h_meta = nullptr;         // pinned: rows_f, pstart, vstart, bytes_f, cstart, count, emit
@@ -134,6 +135,9 @@ class Splitter {
   Status Cuda(cudaError_t e, const char* what);
   Status EnsureScratch(size_t bytes_needed);
   Status EnsureStaging(size_t bytes);
+  void ReleaseStaging();
+  uint8_t* HostAlloc(size_t bytes);
+  void ReleaseHost();
   Status SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t* sizes, int32_t n);
   Status LaunchGather();
   Status FinishHostReads();
@@ -182,9 +186,11 @@ class Splitter {
   cudaStream_t ostream_ = nullptr;   // partition data to host
   cudaEvent_t gather_ev_ = nullptr;
   HostCopy* h_jobs_ = nullptr;       // pinned ring of k_gather descriptors
+  size_t h_jobs_bytes_ = 0;
   size_t jobs_cap_ = 0, jobs_begin_ = 0, jobs_end_ = 0;
   size_t gather_pending_bytes_ = 0;
   uint8_t* h_stage_[2] = {nullptr, nullptr};
+  size_t h_stage_cap_ = 0;
   uint8_t* d_stage_[2] = {nullptr, nullptr};
   size_t stage_cap_ = 0;
   cudaEvent_t stage_ev_[2] = {nullptr, nullptr};
@@ -196,7 +202,8 @@ class Splitter {
   cudaEvent_t tab_ev_[2] = {nullptr, nullptr};
   bool tab_busy_[2] = {false, false};
   int tab_cur_ = 0;
-  std::vector<void*> meta_chunks_;
+  std::vector<PinnedBlock> meta_chunks_;
+  std::vector<PinnedBlock> host_chunks_;  // pinned host partition data of moved passes
   size_t meta_chunk_cap_ = 0, meta_used_ = 0;
   std::vector<std::vector<int32_t>> dev_off_;  // offset ends read from device inputs
   bool seen_rows_ = false;

@@ -126,6 +126,25 @@ def lib() -> ctypes.CDLL:
         L.gz_split_stats.argtypes = [ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
         L.gz_split_kernel_times.restype = ctypes.c_int
         L.gz_split_kernel_times.argtypes = [ctypes.c_int64, ctypes.POINTER(ctypes.c_double)]
+        L.gz_serve_start.restype = ctypes.c_int
+        L.gz_serve_start.argtypes = [ctypes.c_int32, ctypes.c_int64, c_i64p]
+        L.gz_serve_open.restype = ctypes.c_int
+        L.gz_serve_open.argtypes = [ctypes.c_int64, ctypes.c_char_p, ctypes.c_int32, ctypes.POINTER(GzField),
+                                    ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32,
+                                    ctypes.POINTER(GzSplitOptions), c_i64p]
+        L.gz_serve_split.restype = ctypes.c_int
+        L.gz_serve_split.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p,
+                                     ctypes.c_void_p, ctypes.c_int32, c_i64p]
+        L.gz_serve_stop.restype = ctypes.c_int
+        L.gz_serve_stop.argtypes = [ctypes.c_int64, ctypes.c_int64, c_i64p]
+        L.gz_serve_sync.restype = ctypes.c_int
+        L.gz_serve_sync.argtypes = [ctypes.c_int64, ctypes.c_int64, c_i64p]
+        L.gz_serve_wait.restype = ctypes.c_int
+        L.gz_serve_wait.argtypes = [ctypes.c_int64, ctypes.c_int64, c_i64p, c_i64p]
+        L.gz_pinned_reserve.restype = ctypes.c_int
+        L.gz_pinned_reserve.argtypes = [ctypes.c_int64, c_i64p]
+        L.gz_serve_shutdown.restype = ctypes.c_int
+        L.gz_serve_shutdown.argtypes = [ctypes.c_int64]
         _lib = L
     return _lib
 
@@ -141,6 +160,41 @@ def default_options() -> GzSplitOptions:
     o = GzSplitOptions()
     lib().gz_split_default_options(ctypes.byref(o))
     return o
+
+
+def split_options(offheapPerTask: int = 0, bufferSize: int = 4096, codec: Optional[str] = None,
+                  batchCompressThreshold: int = 256, dataFile: str = "", subDirsPerLocalDir: int = 64,
+                  localDirs: str = "", preferSpill: bool = True, writeSchema: bool = False,
+                  **device_options):
+    """GzSplitOptions from nativeMake's arguments plus device knobs; returns (options, the byte
+    strings the options point to, which must outlive the call that reads them)."""
+    o = default_options()
+    o.offheap_per_task = offheapPerTask
+    if bufferSize > 0:
+        o.buffer_size = bufferSize
+    if subDirsPerLocalDir > 0:
+        o.num_sub_dirs = subDirsPerLocalDir
+    o.batch_compress_threshold = batchCompressThreshold
+    o.compression = 0 if codec in (None, "", "uncompressed", "none") else 1
+    o.prefer_spill = int(preferSpill)
+    o.write_schema = int(writeSchema)
+    o.buffered_write = 1
+    keep = [dataFile.encode(), localDirs.encode()]
+    o.data_file = keep[0]
+    o.local_dirs = keep[1]
+    for k, v in device_options.items():
+        setattr(o, k, v)
+    return o, keep
+
+
+def _fields(schema):
+    arr = (GzField * len(schema))()
+    names = [f.name.encode() for f in schema]
+    for i, f in enumerate(schema):
+        arr[i].type = f.code
+        arr[i].nullable = int(f.nullable)
+        arr[i].name = names[i]
+    return arr, names
 
 
 @dataclasses.dataclass
@@ -177,22 +231,8 @@ class ShuffleSplitterJniWrapper:
              dataFile: str = "", subDirsPerLocalDir: int = 64, localDirs: str = "",
              preferSpill: bool = True, memoryPoolId: int = 0, writeSchema: bool = False,
              **device_options) -> int:
-        o = default_options()
-        o.offheap_per_task = offheapPerTask
-        if bufferSize > 0:
-            o.buffer_size = bufferSize
-        if subDirsPerLocalDir > 0:
-            o.num_sub_dirs = subDirsPerLocalDir
-        o.batch_compress_threshold = batchCompressThreshold
-        o.compression = 0 if codec in (None, "", "uncompressed", "none") else 1
-        o.prefer_spill = int(preferSpill)
-        o.write_schema = int(writeSchema)
-        o.buffered_write = 1
-        self._keep = [dataFile.encode(), localDirs.encode()]
-        o.data_file = self._keep[0]
-        o.local_dirs = self._keep[1]
-        for k, v in device_options.items():
-            setattr(o, k, v)
+        o, self._keep = split_options(offheapPerTask, bufferSize, codec, batchCompressThreshold, dataFile,
+                                      subDirsPerLocalDir, localDirs, preferSpill, writeSchema, **device_options)
         keys = np.asarray(list(part.keyColumns), np.int32)
         h = ctypes.c_int64(0)
         if part.schema is not None:
@@ -305,3 +345,66 @@ def split_batches(schema, batches, num_partitions: int, key_cols: Sequence[int],
     finally:
         w.close(h)
     return res, data
+
+
+def pinned_reserve(nbytes: int) -> int:
+    """Pins about `nbytes` of host memory into the library's pool up front (gz_pinned_reserve)."""
+    got = ctypes.c_int64(0)
+    _check(lib().gz_pinned_reserve(nbytes, ctypes.byref(got)), 0)
+    return got.value
+
+
+class ServeLoop:
+    """The served form (gz_serve_*): Split / Stop calls of many concurrent tasks on one GPU,
+    asynchronous, with per-call latency.  A task is an ordinary splitter handle, so
+    ShuffleSplitterJniWrapper.stop / data / close read its results after its stop ticket."""
+
+    def __init__(self, slots: int = 4, hbmBudget: int = 40 << 30):
+        h = ctypes.c_int64(0)
+        _check(lib().gz_serve_start(slots, hbmBudget, ctypes.byref(h)), 0)
+        self.handle = h.value
+        self._keep = {}
+
+    def open(self, schema, numPartitions: int, keyColumns: Sequence[int], **make_kwargs) -> int:
+        """Blocks until the HBM budget admits the task; returns its splitter handle."""
+        o, keep = split_options(**make_kwargs)
+        arr, names = _fields(schema)
+        keys = np.asarray(list(keyColumns), np.int32)
+        t = ctypes.c_int64(0)
+        _check(lib().gz_serve_open(self.handle, b"hash", numPartitions, arr, len(schema), keys.ctypes.data,
+                                   len(keys), ctypes.byref(o), ctypes.byref(t)), 0)
+        self._keep[t.value] = (keep, names)
+        return t.value
+
+    def split(self, task: int, numRows: int, bufAddrs, bufSizes) -> int:
+        """Queues one Split; the buffers stay valid until wait(ticket) returns."""
+        addrs = np.ascontiguousarray(bufAddrs, dtype=np.int64)
+        sizes = np.ascontiguousarray(bufSizes, dtype=np.int64)
+        t = ctypes.c_int64(0)
+        _check(lib().gz_serve_split(self.handle, task, numRows, addrs.ctypes.data, sizes.ctypes.data,
+                                    len(addrs), ctypes.byref(t)), 0)
+        return t.value
+
+    def stop(self, task: int) -> int:
+        t = ctypes.c_int64(0)
+        _check(lib().gz_serve_stop(self.handle, task, ctypes.byref(t)), 0)
+        return t.value
+
+    def sync(self, task: int) -> int:
+        """Queues a wait for the task's device work so far; returns the ticket."""
+        t = ctypes.c_int64(0)
+        _check(lib().gz_serve_sync(self.handle, task, ctypes.byref(t)), 0)
+        return t.value
+
+    def wait(self, ticket: int, service: bool = False):
+        """Latency of the call in ns (submission to completion), and with service=True also the
+        ns its worker spent on it; raises on its error."""
+        lat = ctypes.c_int64(0)
+        svc = ctypes.c_int64(0)
+        _check(lib().gz_serve_wait(self.handle, ticket, ctypes.byref(lat), ctypes.byref(svc)), 0)
+        return (lat.value, svc.value) if service else lat.value
+
+    def shutdown(self) -> None:
+        if self.handle:
+            lib().gz_serve_shutdown(self.handle)
+            self.handle = 0

@@ -206,6 +206,37 @@ def c3_batches(seed: int = 2, num_batches: int = 4, rows: int = 32768, null_frac
 
 
 # --------------------------------------------------------------------------------------
+# mixed-task workloads (batched and served forms): uneven batches from three schemas
+C4_SCHEMA_3 = [Field(f"i{k}", "int32") for k in range(6)] + [Field("u0", "utf8"), Field("u1", "utf8")]
+C4_KEYS_3 = [0]
+C4_SCHEMAS = [(C1_SCHEMA, C1_KEYS), (C2_SCHEMA, C2_KEYS), (C4_SCHEMA_3, C4_KEYS_3)]
+C4_PARTITIONS = [64, 200, 1024]
+
+
+def c4_schema3_batch(rng, n: int) -> Batch:
+    bufs = []
+    for k in range(6):
+        bufs += _column(rng, C4_SCHEMA_3[k], n, rng.integers(-2**31, 2**31, size=n), 0.0 if k == 0 else 0.02)
+    for k in range(2):
+        bufs += _column(rng, C4_SCHEMA_3[6 + k], n, None, 0.02, (0, 32, AZ))
+    return Batch(n, bufs)
+
+
+def c4_batch(rng, schema_index: int, n: int) -> Batch:
+    """A batch of `n` rows of mixed-task schema 0 (workload c1), 1 (c2) or 2 (6 int32 + 2 utf8)."""
+    if schema_index == 0:
+        return c1_batch(rng, n)
+    if schema_index == 1:
+        return c2_batch(rng, n)
+    return c4_schema3_batch(rng, n)
+
+
+def c4_rows(rng, size=None):
+    """Batch rows log-uniform over [1000, 65536]."""
+    return np.exp(rng.uniform(np.log(1000), np.log(65536), size=size)).astype(np.int64)
+
+
+# --------------------------------------------------------------------------------------
 # random schemas for property tests
 RANDOM_TYPES = ["bool", "int8", "int16", "int32", "int64", "float32", "float64", "date32",
                 "uint64", "decimal128", "utf8", "binary", "null", "timestamp", "float16"]

@@ -182,6 +182,53 @@ GzStatus gz_split_kernel_times(int64_t handle, double* out4);
  * No reference counterpart. */
 GzStatus gz_split_stats(int64_t handle, int64_t* out8);
 
+/* ---- served form (no reference counterpart) --------------------------------------------
+ * Split / Stop calls of many concurrent tasks, each an ordinary splitter with its own schema,
+ * batch sizes and partition count, executed by one serving loop on one GPU.  Each task is
+ * pinned to one of `slots` workers: its calls run in order, calls of tasks on other workers run
+ * at the same time and their device work overlaps.  A task is admitted when its share of
+ * `hbm_budget` is free: its spill threshold (opts.device_budget: partition data kept in HBM
+ * before it moves to pinned host memory) + 3 * opts.flush_bytes + 64 MiB; it returns the share
+ * when it stops or closes.  Calls are asynchronous: each returns a ticket; gz_serve_wait gives
+ * the call's status and its latency from submission to completion (host inputs read, batch
+ * queued for the device; for a stop, the data file written).  Buffers passed to gz_serve_split
+ * stay valid until its ticket completes.  After the stop ticket completes, gz_split_stop(task)
+ * fills the SplitResult and gz_split_data(task) gives the bytes; gz_split_close(task) frees the
+ * task.  A served task must not be called directly (gz_split_split) while it is served.  Errors
+ * of these calls: gz_last_error(0, ...) on the calling thread. */
+
+/* Starts a serving loop with `slots` workers and an HBM budget in bytes. */
+GzStatus gz_serve_start(int32_t slots, int64_t hbm_budget, int64_t* out_server);
+
+/* Opens a task (gz_split_make_fields arguments); blocks until the budget admits it.  The task id
+ * is a splitter handle. */
+GzStatus gz_serve_open(int64_t server, const char* short_name, int32_t num_partitions,
+                       const GzField* fields, int32_t n_fields, const int32_t* key_cols,
+                       int32_t n_keys, const GzSplitOptions* opts, int64_t* out_task);
+
+/* Queues one Split call of `task` (gz_split_split arguments, first_batch = 0). */
+GzStatus gz_serve_split(int64_t server, int64_t task, int32_t num_rows, const int64_t* buf_addrs,
+                        const int64_t* buf_sizes, int32_t n_bufs, int64_t* out_ticket);
+
+/* Queues the Stop of `task`, after its queued splits. */
+GzStatus gz_serve_stop(int64_t server, int64_t task, int64_t* out_ticket);
+
+/* Queues a wait for all device work of `task` so far (gz_split_sync), after its queued calls. */
+GzStatus gz_serve_sync(int64_t server, int64_t task, int64_t* out_ticket);
+
+/* Waits for a ticket: the call's status; *out_latency_ns = submission to completion,
+ * *out_service_ns = the part its worker spent on it (the rest queued).  Either may be NULL. */
+GzStatus gz_serve_wait(int64_t server, int64_t ticket, int64_t* out_latency_ns,
+                       int64_t* out_service_ns);
+
+/* Adds about `bytes` of pinned host memory to the library's pool up front, in the chunks that
+ * partition data moved out of HBM is carved from.  Pinning is slow; a server calls this at
+ * start so that spills inside calls do not pay it.  *out_reserved = bytes added. */
+GzStatus gz_pinned_reserve(int64_t bytes, int64_t* out_reserved);
+
+/* Finishes the queued calls and stops the workers. */
+GzStatus gz_serve_shutdown(int64_t server);
+
 /* ---- partition ids without device allocation (no counterpart in the reference) -------- */
 
 /* One hash-key column of a batch that is already in device memory. */
