@@ -24,8 +24,8 @@ constexpr int kMaxKeys = 8;
 constexpr int kMaxCols = 64;    // array columns (fixed + bool + binary)
 constexpr int kMaxSchemaCols = 256;
 constexpr int kTileRows = 1024; // rows per k_scatter tile
-constexpr int kMaxSegTiles = 4; // tiles per segment
-constexpr int kSegStateWords = 2048;  // most (1 + n_str) * P for multi-tile segments
+constexpr int kMaxSegTiles = 32;  // tiles per segment
+constexpr size_t kHistSmemBytes = 96 * 1024;  // k_hash_count's histograms in shared memory up to this
 constexpr int kScatterThreads = 256;
 constexpr int kPlanThreads = 1024;
 constexpr int kMaxBatchesPerFlush = 4096;

@@ -149,9 +149,11 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
       sd_.order[i] = take_binary ? binary[bi++] : fixed[fi++];
     }
   }
-  // the plan works on segments of up to kMaxSegTiles tiles when k_hash_count can keep the
-  // running rows and bytes of every partition of a segment in shared memory
-  seg_tiles_ = (int64_t)(1 + n_str_) * P_ <= kSegStateWords ? kMaxSegTiles : 1;
+  // The plan works on segments of several tiles when k_hash_count keeps the running rows and
+  // bytes of every partition in shared memory (it then records each tile's prefix).  Its work
+  // grows with segments x partitions, so segments are longer for more partitions.
+  if ((size_t)(1 + n_str_) * P_ * 4 > kHistSmemBytes) seg_tiles_ = 1;
+  else seg_tiles_ = (uint32_t)std::min<int64_t>(kMaxSegTiles, std::max<int64_t>(4, P_ / 256));
   // hash chain (HashSplitter::CreateProjector, splitter.cc:1402-1438)
   for (size_t k = 0; k < keys_.size(); k++) {
     const int ci = keys_[k];
@@ -780,7 +782,7 @@ Status Splitter::Flush() {
   fd.n_tiles = NT;
   fd.seg_tiles = seg_tiles_;
   fd.n_rows = (uint32_t)R;
-  fd.hist_in_smem = (size_t)P * (1 + nstr) * 4 <= 96 * 1024 ? 1 : 0;
+  fd.hist_in_smem = (size_t)P * (1 + nstr) * 4 <= kHistSmemBytes ? 1 : 0;
   fd.pids = reinterpret_cast<uint16_t*>(S + s_pids);
   fd.cnt = reinterpret_cast<uint32_t*>(S + s_cnt);
   fd.vpos = reinterpret_cast<uint32_t*>(S + s_vpos);
