@@ -426,6 +426,21 @@ GzStatus gz_debug_encode_record_batch(int64_t length, const int64_t* nodes, int3
   return GZ_OK;
 }
 
+GzStatus gz_debug_reencode_schema(const uint8_t* schema_ipc, int64_t len, uint8_t* out, int64_t cap,
+                                  int64_t* out_len) {
+  std::vector<gz::Field> fields;
+  std::string err;
+  if (!gz::ParseSchemaIpc(schema_ipc, len, &fields, &err)) {
+    t_make_error = err;
+    return GZ_INVALID;
+  }
+  const std::vector<uint8_t> msg = gz::EncodeSchemaMessage(fields);
+  *out_len = (int64_t)msg.size();
+  if (*out_len > cap) return GZ_INVALID;
+  memcpy(out, msg.data(), msg.size());
+  return GZ_OK;
+}
+
 GzStatus gz_debug_parse_schema(const uint8_t* schema_ipc, int64_t len, int32_t* types,
                                int32_t* nullable, int32_t cap, int32_t* n_fields) {
   std::vector<gz::Field> fields;

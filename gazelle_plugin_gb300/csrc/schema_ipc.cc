@@ -5,6 +5,8 @@
 
 #include <string.h>
 
+#include <algorithm>
+
 #include "../../include/gz_split.h"
 
 namespace gz {
@@ -163,6 +165,7 @@ bool ParseSchemaIpc(const uint8_t* data, int64_t len, std::vector<Field>* out, s
       case 10:
         f.type = GZ_TYPE_TIMESTAMP;
         f.unit = tp >= 0 ? r.Scalar<int16_t>(tp, 0, 0) : 0;
+        if (tp >= 0) r.String(tp, 1, &f.timezone);
         break;
       default:
         *err = "field type " + std::to_string(tt) + " is not implemented by the GPU splitter";
@@ -171,6 +174,213 @@ bool ParseSchemaIpc(const uint8_t* data, int64_t len, std::vector<Field>* out, s
     out->push_back(f);
   }
   return true;
+}
+
+// ---------------------------------------------------------------------------------------
+// Writing: a flatbuffers builder following the published flatbuffers algorithm (the buffer
+// grows toward the front, offsets are distances from its end, each table ends with a vtable that
+// is shared with an identical earlier one) and Arrow's schema tables built in the order, and
+// with the field order inside each table, that Arrow C++ uses, so the bytes match.
+namespace {
+
+class Builder {
+ public:
+  uint32_t Size() const { return (uint32_t)buf_.size(); }
+  void Pad(size_t n) { buf_.insert(buf_.begin(), n, 0); }
+  void Align(size_t a) {
+    minalign_ = std::max(minalign_, a);
+    Pad((~buf_.size() + 1) & (a - 1));
+  }
+  void PreAlign(size_t len, size_t a) {
+    if (len == 0) return;
+    minalign_ = std::max(minalign_, a);
+    Pad((~(buf_.size() + len) + 1) & (a - 1));
+  }
+  template <typename T>
+  uint32_t Push(T v) {
+    Align(sizeof(T));
+    uint8_t tmp[sizeof(T)];
+    memcpy(tmp, &v, sizeof(T));
+    buf_.insert(buf_.begin(), tmp, tmp + sizeof(T));
+    return Size();
+  }
+  uint32_t ReferTo(uint32_t off) {
+    Align(4);
+    return Size() - off + 4;
+  }
+  uint32_t String(const std::string& s) {
+    PreAlign(s.size() + 1, 4);
+    buf_.insert(buf_.begin(), 1, 0);
+    buf_.insert(buf_.begin(), s.begin(), s.end());
+    return Push<uint32_t>((uint32_t)s.size());
+  }
+  uint32_t OffsetVector(const std::vector<uint32_t>& offs) {
+    PreAlign(offs.size() * 4, 4);
+    for (size_t i = offs.size(); i-- > 0;) Push<uint32_t>(ReferTo(offs[i]));
+    return Push<uint32_t>((uint32_t)offs.size());
+  }
+  void StartTable() {
+    fields_.clear();
+    table_start_ = Size();
+  }
+  template <typename T>
+  void AddScalar(uint16_t voff, T v, T def) {
+    if (v == def) return;  // defaults are not stored
+    fields_.push_back({voff, Push<T>(v)});
+  }
+  void AddOffset(uint16_t voff, uint32_t off) {
+    if (off == 0) return;
+    fields_.push_back({voff, Push<uint32_t>(ReferTo(off))});
+  }
+  uint32_t EndTable() {
+    const uint32_t loc = Push<int32_t>(0);
+    uint16_t vsize = 4;
+    for (auto& f : fields_) vsize = std::max<uint16_t>(vsize, (uint16_t)(f.first + 2));
+    std::vector<uint16_t> vt(vsize / 2, 0);
+    vt[0] = vsize;
+    vt[1] = (uint16_t)(loc - table_start_);
+    for (auto& f : fields_) vt[f.first / 2] = (uint16_t)(loc - f.second);
+    std::vector<uint8_t> bytes(vsize);
+    memcpy(bytes.data(), vt.data(), vsize);
+    uint32_t use = 0;
+    for (uint32_t prev : vtables_) {  // the first identical vtable written
+      if (memcmp(&buf_[buf_.size() - prev], bytes.data(), vsize) == 0) {
+        uint16_t psize;
+        memcpy(&psize, &buf_[buf_.size() - prev], 2);
+        if (psize == vsize) {
+          use = prev;
+          break;
+        }
+      }
+    }
+    if (use == 0) {
+      buf_.insert(buf_.begin(), bytes.begin(), bytes.end());
+      use = Size();
+      vtables_.push_back(use);
+    }
+    const int32_t soff = (int32_t)use - (int32_t)loc;
+    memcpy(&buf_[buf_.size() - loc], &soff, 4);
+    return loc;
+  }
+  std::vector<uint8_t> Finish(uint32_t root) {
+    PreAlign(4, minalign_);
+    Push<uint32_t>(ReferTo(root));
+    return buf_;
+  }
+
+ private:
+  std::vector<uint8_t> buf_;
+  size_t minalign_ = 1;
+  uint32_t table_start_ = 0;
+  std::vector<std::pair<uint16_t, uint32_t>> fields_;
+  std::vector<uint32_t> vtables_;
+};
+
+// Arrow Schema.fbs: the Type union tag and table of a field.  Inside a table the fields are
+// added largest first and, among equal sizes, last declared first (the generated Create*).
+uint8_t TypeTable(Builder& b, const Field& f, uint32_t* table) {
+  auto empty = [&]() {
+    b.StartTable();
+    return b.EndTable();
+  };
+  auto integer = [&](int32_t bits, bool sign) {
+    b.StartTable();
+    b.AddScalar<int32_t>(4, bits, 0);
+    b.AddScalar<uint8_t>(6, sign ? 1 : 0, 0);
+    return b.EndTable();
+  };
+  auto floating = [&](int16_t prec) {
+    b.StartTable();
+    b.AddScalar<int16_t>(4, prec, 0);
+    return b.EndTable();
+  };
+  switch (f.type) {
+    case GZ_TYPE_NULL: *table = empty(); return 1;
+    case GZ_TYPE_BOOL: *table = empty(); return 6;
+    case GZ_TYPE_INT8: *table = integer(8, true); return 2;
+    case GZ_TYPE_UINT8: *table = integer(8, false); return 2;
+    case GZ_TYPE_INT16: *table = integer(16, true); return 2;
+    case GZ_TYPE_UINT16: *table = integer(16, false); return 2;
+    case GZ_TYPE_INT32: *table = integer(32, true); return 2;
+    case GZ_TYPE_UINT32: *table = integer(32, false); return 2;
+    case GZ_TYPE_INT64: *table = integer(64, true); return 2;
+    case GZ_TYPE_UINT64: *table = integer(64, false); return 2;
+    case GZ_TYPE_HALF_FLOAT: *table = floating(0); return 3;
+    case GZ_TYPE_FLOAT32: *table = floating(1); return 3;
+    case GZ_TYPE_FLOAT64: *table = floating(2); return 3;
+    case GZ_TYPE_BINARY: *table = empty(); return 4;
+    case GZ_TYPE_STRING: *table = empty(); return 5;
+    case GZ_TYPE_DECIMAL128:  // Decimal { precision, scale, bitWidth = 128 }
+      b.StartTable();
+      b.AddScalar<int32_t>(8, 128, 128);
+      b.AddScalar<int32_t>(6, f.scale, 0);
+      b.AddScalar<int32_t>(4, f.precision, 0);
+      *table = b.EndTable();
+      return 7;
+    case GZ_TYPE_DATE32:
+    case GZ_TYPE_DATE64:  // Date { unit = MILLISECOND }
+      b.StartTable();
+      b.AddScalar<int16_t>(4, f.type == GZ_TYPE_DATE32 ? 0 : 1, 1);
+      *table = b.EndTable();
+      return 8;
+    case GZ_TYPE_TIME32:
+    case GZ_TYPE_TIME64:  // Time { unit = MILLISECOND, bitWidth = 32 }
+      b.StartTable();
+      b.AddScalar<int32_t>(6, f.type == GZ_TYPE_TIME32 ? 32 : 64, 32);
+      b.AddScalar<int16_t>(4, (int16_t)f.unit, 1);
+      *table = b.EndTable();
+      return 9;
+    case GZ_TYPE_TIMESTAMP: {  // Timestamp { unit, timezone }
+      const uint32_t tz = f.timezone.empty() ? 0 : b.String(f.timezone);
+      b.StartTable();
+      b.AddOffset(6, tz);
+      b.AddScalar<int16_t>(4, (int16_t)f.unit, 0);
+      *table = b.EndTable();
+      return 10;
+    }
+    default: *table = empty(); return 0;
+  }
+}
+
+}  // namespace
+
+std::vector<uint8_t> EncodeSchemaMessage(const std::vector<Field>& fields) {
+  Builder b;
+  std::vector<uint32_t> offs;
+  for (const Field& f : fields) {
+    uint32_t type_table = 0;
+    const uint8_t tag = TypeTable(b, f, &type_table);  // type first, then name, then children
+    const uint32_t name = b.String(f.name);
+    const uint32_t children = b.OffsetVector({});
+    b.StartTable();  // Field { name, nullable, type_type, type, dictionary, children, custom_metadata }
+    b.AddOffset(14, children);
+    b.AddOffset(10, type_table);
+    b.AddOffset(4, name);
+    b.AddScalar<uint8_t>(8, tag, 0);
+    b.AddScalar<uint8_t>(6, f.nullable ? 1 : 0, 0);
+    offs.push_back(b.EndTable());
+  }
+  const uint32_t vec = b.OffsetVector(offs);
+  b.StartTable();  // Schema { endianness = Little, fields, custom_metadata, features }
+  b.AddOffset(6, vec);
+  b.AddScalar<int16_t>(4, 0, 0);
+  const uint32_t schema = b.EndTable();
+  b.StartTable();  // Message { version, header_type, header, bodyLength, custom_metadata }
+  b.AddScalar<int64_t>(10, 0, 0);
+  b.AddOffset(8, schema);
+  b.AddScalar<int16_t>(4, 4 /* V5 */, 0);
+  b.AddScalar<uint8_t>(6, 1 /* Schema */, 0);
+  const uint32_t msg = b.EndTable();
+  const std::vector<uint8_t> meta = b.Finish(msg);
+  // encapsulation: continuation marker, metadata length (padded to 8), metadata, padding
+  const size_t padded = (meta.size() + 8 + 7) & ~size_t(7);
+  std::vector<uint8_t> out(padded, 0);
+  const uint32_t cont = 0xFFFFFFFFu;
+  const int32_t mlen = (int32_t)(padded - 8);
+  memcpy(out.data(), &cont, 4);
+  memcpy(out.data() + 4, &mlen, 4);
+  memcpy(out.data() + 8, meta.data(), meta.size());
+  return out;
 }
 
 }  // namespace gz

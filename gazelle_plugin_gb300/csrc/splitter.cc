@@ -1230,6 +1230,9 @@ Status Splitter::Stop() {
     if (!fsink->ok()) return Status::Error(GZ_IO, "cannot open data file " + data_file_);
   }
   int64_t compress_ns = 0;
+  // the schema message written before every partition with rows (WriteSchemaPayload,
+  // splitter.cc:88-90, 145-151)
+  const std::vector<uint8_t> schema_msg = opts_.write_schema ? EncodeSchemaMessage(fields_) : std::vector<uint8_t>();
   for (int p = 0; p < P_; p++) {
     auto& segs = segments_[p];
     if (segs.empty()) {
@@ -1237,9 +1240,8 @@ Status Splitter::Stop() {
       continue;
     }
     const int64_t before = sink->Tell();
-    if (opts_.write_schema) {
-      return Status::Error(GZ_NOT_IMPLEMENTED, "write_schema is not implemented yet");
-    }
+    if (!schema_msg.empty() && !sink->Write(schema_msg.data(), (int64_t)schema_msg.size()))
+      return Status::Error(GZ_IO, "write failed");
     for (Segment& s : segs) {
       int64_t raw = 0;
       const int64_t c0 = NowNs();

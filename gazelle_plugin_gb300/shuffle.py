@@ -193,6 +193,7 @@ def _fields(schema):
     for i, f in enumerate(schema):
         arr[i].type = f.code
         arr[i].nullable = int(f.nullable)
+        arr[i].precision, arr[i].scale, arr[i].unit = f.params
         arr[i].name = names[i]
     return arr, names
 
@@ -241,12 +242,7 @@ class ShuffleSplitterJniWrapper:
                                      len(part.schema), keys.ctypes.data, len(keys),
                                      ctypes.byref(o), ctypes.byref(h))
         else:
-            arr = (GzField * len(part.fields))()
-            self._names = [f.name.encode() for f in part.fields]
-            for i, f in enumerate(part.fields):
-                arr[i].type = f.code
-                arr[i].nullable = int(f.nullable)
-                arr[i].name = self._names[i]
+            arr, self._names = _fields(part.fields)
             st = lib().gz_split_make_fields(part.shortName.encode(), part.numPartitions, arr,
                                             len(part.fields), keys.ctypes.data, len(keys),
                                             ctypes.byref(o), ctypes.byref(h))

@@ -59,6 +59,13 @@ class Field:
     def is_binary(self) -> bool:
         return self.type in ("utf8", "binary")
 
+    @property
+    def params(self):
+        """(precision, scale, time unit 0 s / 1 ms / 2 us / 3 ns) of the Arrow type the field
+        stands for: time32[ms], time64[us], timestamp[us], decimal128(30, 2)."""
+        return {"decimal128": (30, 2, 0), "time32": (0, 0, 1), "time64": (0, 0, 2),
+                "timestamp": (0, 0, 2)}.get(self.type, (0, 0, 0))
+
 
 @dataclasses.dataclass
 class Batch:

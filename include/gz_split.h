@@ -277,6 +277,11 @@ GzStatus gz_debug_encode_record_batch(int64_t length, const int64_t* nodes, int3
                                       int32_t n_bufs, uint8_t* out, int64_t out_cap,
                                       int64_t* out_len);
 
+/* Parses an Arrow IPC Schema message and encodes it again with the splitter's schema writer (the
+ * message written before each partition when write_schema is set). */
+GzStatus gz_debug_reencode_schema(const uint8_t* schema_ipc, int64_t len, uint8_t* out, int64_t cap,
+                                  int64_t* out_len);
+
 /* Parses an Arrow IPC Schema message; writes up to `cap` GzType codes and nullable flags. */
 GzStatus gz_debug_parse_schema(const uint8_t* schema_ipc, int64_t len, int32_t* types,
                                int32_t* nullable, int32_t cap, int32_t* n_fields);

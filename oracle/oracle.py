@@ -59,7 +59,9 @@ class SplitOutput:
 
 
 class OracleSplitter:
-    """Restated reference Splitter (hash partitioning, compression off, write_schema off)."""
+    """Restated reference Splitter (hash partitioning, compression off).  With write_schema the
+    schema message is serialised by Arrow itself (pyarrow), as the reference's GetSchemaPayload
+    does."""
 
     _lib = None
 
@@ -84,6 +86,7 @@ class OracleSplitter:
             lib.gzo_spill.restype = ctypes.c_int64
             lib.gzo_spill.argtypes = [ctypes.c_void_p, ctypes.c_int64]
             lib.gzo_close.argtypes = [ctypes.c_void_p]
+            lib.gzo_set_schema_message.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]
             lib.gzo_hash_int.restype = ctypes.c_int32
             lib.gzo_hash_int.argtypes = [ctypes.c_int32, ctypes.c_int32]
             lib.gzo_hash_long.restype = ctypes.c_int32
@@ -96,7 +99,8 @@ class OracleSplitter:
         return cls._lib
 
     def __init__(self, schema, num_partitions: int, key_cols: Sequence[int],
-                 offheap_per_task: int = 0, buffer_size: int = 4096, prefer_spill: bool = True):
+                 offheap_per_task: int = 0, buffer_size: int = 4096, prefer_spill: bool = True,
+                 write_schema: bool = False):
         self.P = num_partitions
         types = np.array([f.code for f in schema], np.int32)
         keys = np.array(key_cols, np.int32)
@@ -106,6 +110,9 @@ class OracleSplitter:
                                      buffer_size, int(prefer_spill), err, 512)
         if not self.h:
             raise ValueError(err.value.decode())
+        if write_schema:
+            msg = to_pyarrow_schema(schema).serialize().to_pybytes()
+            self.lib().gzo_set_schema_message(self.h, msg, len(msg))
 
     def split(self, batch) -> None:
         addrs, sizes = batch.addrs_sizes()
@@ -168,7 +175,20 @@ def to_pyarrow_schema(schema):
          "uint64": pa.uint64(), "float64": pa.float64(), "date64": pa.date64(),
          "time64": pa.time64("us"), "timestamp": pa.timestamp("us"),
          "decimal128": pa.decimal128(30, 2), "utf8": pa.string(), "binary": pa.binary()}
-    return pa.schema([pa.field(f.name, m[f.type], f.nullable) for f in schema])
+    units = ["s", "ms", "us", "ns"]
+
+    def typ(f):
+        prec, scale, unit = f.params
+        if f.type == "decimal128":
+            return pa.decimal128(prec, scale)
+        if f.type == "time32":
+            return pa.time32(units[unit])
+        if f.type == "time64":
+            return pa.time64(units[unit])
+        if f.type == "timestamp":
+            return pa.timestamp(units[unit])
+        return m[f.type]
+    return pa.schema([pa.field(f.name, typ(f), f.nullable) for f in schema])
 
 
 class RefSplitter:

@@ -330,6 +330,13 @@ class OracleSplitter {
     return cur;
   }
 
+  // The encapsulated IPC Schema message GetSchemaPayload + WriteIpcPayload give for the schema
+  // (splitter.cc:145-151, 1355-1364); the caller serialises it with Arrow itself.
+  void SetSchemaMessage(const uint8_t* p, size_t n) {
+    opt_.write_schema = true;
+    schema_msg_.assign(p, p + n);
+  }
+
   std::string Stop(const char* data_file, std::vector<uint8_t>* file_bytes) {
     std::vector<uint8_t> out;
     for (int p = 0; p < P_; p++) {
@@ -337,6 +344,8 @@ class OracleSplitter {
       if (cached_size_[p] > 0) writer_[p] = true;
       if (writer_[p]) {
         size_t before = out.size();
+        // WriteSchemaPayload before the partition's batches when write_schema (splitter.cc:88-90)
+        if (opt_.write_schema) out.insert(out.end(), schema_msg_.begin(), schema_msg_.end());
         if (!spill_opened_[p] && cached_size_[p] == 0) return "Partition writer got empty partition";
         if (spill_opened_[p]) {
           out.insert(out.end(), spilled_[p].begin(), spilled_[p].end());
@@ -640,6 +649,7 @@ class OracleSplitter {
   int P_;
   std::vector<int> keys_;
   Options opt_;
+  std::vector<uint8_t> schema_msg_;
   std::vector<int> array_idx_;
   int fixed_cnt_ = 0;
   std::vector<std::vector<PartBufs>> bufs_;
@@ -655,6 +665,12 @@ class OracleSplitter {
   std::vector<uint32_t> cnt_;
   int64_t bytes_written_ = 0, bytes_spilled_ = 0, compute_pid_ns_ = 0;
 };
+
+}  // namespace
+
+extern "C" void gzo_set_schema_message(void* hp, const uint8_t* msg, int64_t len);
+
+namespace {
 
 struct Handle {
   std::unique_ptr<OracleSplitter> s;
@@ -685,6 +701,10 @@ void* gzo_make(const int32_t* types, int32_t nf, int32_t num_partitions, const i
     return nullptr;
   }
   return h;
+}
+
+void gzo_set_schema_message(void* hp, const uint8_t* msg, int64_t len) {
+  ((Handle*)hp)->s->SetSchemaMessage(msg, (size_t)len);
 }
 
 int gzo_split(void* hp, int32_t num_rows, const int64_t* addrs, const int64_t* sizes,

@@ -104,6 +104,15 @@ def cases():
                    for _ in range(nb)]
         yield (f"random_{seed}", schema, batches, P, keys, opts,
                {"workload": "random", "seed": 1000 + seed})
+    # with the schema message before every partition (write_schema)
+    yield ("c1_write_schema", W.C1_SCHEMA, W.c1_batches(0, 4, 4096), 8, W.C1_KEYS,
+           {"write_schema": True}, {"workload": "c1", "seed": 0, "num_batches": 4, "rows": 4096})
+    yield ("c2_write_schema", W.C2_SCHEMA, W.c2_batches(1, 3, 4096), 200, W.C2_KEYS,
+           {"write_schema": True}, {"workload": "c2", "seed": 1, "num_batches": 3, "rows": 4096})
+    for seed in range(8):
+        schema, batches, P, keys, opts = random_case(1000 + seed)
+        yield (f"random_{seed}_write_schema", schema, batches, P, keys, dict(opts, write_schema=True),
+               {"workload": "random", "seed": 1000 + seed})
 
 
 def random_case(seed):

@@ -127,3 +127,35 @@ def test_schema_ipc_parser():
     assert nulls == [int(f.nullable) for f in schema]
     st, _, _ = parse_schema(pa.schema([pa.field("l", pa.list_(pa.int32()))]).serialize().to_pybytes())
     assert st != 0
+
+
+def test_schema_message_matches_arrow_writer():
+    """The schema message written before each partition (write_schema) is byte for byte what
+    Arrow C++ writes for the same schema (GetSchemaPayload + WriteIpcPayload, which
+    pyarrow.Schema.serialize also uses): 300 random schemas over every splittable type."""
+    pa = pytest.importorskip("pyarrow")
+    import random
+    lib = S.lib()
+    lib.gz_debug_reencode_schema.restype = ctypes.c_int
+    lib.gz_debug_reencode_schema.argtypes = [ctypes.c_char_p, ctypes.c_int64, ctypes.c_void_p,
+                                             ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
+    types = [pa.bool_(), pa.int8(), pa.int16(), pa.int32(), pa.int64(), pa.uint8(), pa.uint16(),
+             pa.uint32(), pa.uint64(), pa.float16(), pa.float32(), pa.float64(), pa.date32(),
+             pa.date64(), pa.time32("s"), pa.time32("ms"), pa.time64("us"), pa.time64("ns"),
+             pa.timestamp("s"), pa.timestamp("ms"), pa.timestamp("us"), pa.timestamp("ns"),
+             pa.timestamp("us", tz="UTC"), pa.timestamp("ns", tz="America/New_York"),
+             pa.decimal128(10, 2), pa.decimal128(38, 0), pa.decimal128(1, 0), pa.utf8(),
+             pa.binary(), pa.null()]
+    rnd = random.Random(7)
+    out = np.zeros(1 << 16, np.uint8)
+    n = ctypes.c_int64(0)
+    for _ in range(300):
+        fields = []
+        for i in range(rnd.randint(1, 24)):
+            t = rnd.choice(types)
+            name = "c%d_%s" % (i, "x" * rnd.randint(0, 13))
+            fields.append(pa.field(name, t, True if t == pa.null() else rnd.random() < 0.7))
+        want = pa.schema(fields).serialize().to_pybytes()
+        assert lib.gz_debug_reencode_schema(want, len(want), out.ctypes.data, out.nbytes,
+                                            ctypes.byref(n)) == 0
+        assert out[: n.value].tobytes() == want, pa.schema(fields)

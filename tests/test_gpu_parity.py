@@ -19,10 +19,10 @@ GOLDEN = json.load(open(os.path.join(HERE, "golden", "splits.json")))["cases"]
 
 
 def gpu_split(schema, batches, P, keys, buffer_size=4096, prefer_spill=True, offheap_per_task=0,
-              **dev):
+              write_schema=False, **dev):
     return S.split_batches(schema, batches, P, keys, bufferSize=buffer_size,
                            preferSpill=prefer_spill, offheapPerTask=offheap_per_task,
-                           writeSchema=False, **dev)
+                           writeSchema=write_schema, **dev)
 
 
 def assert_same(res, data, ref, tag=""):
