@@ -739,6 +739,28 @@ __device__ __forceinline__ void scatter_zero_bits(uint32_t* words, const uint8_t
   for (int u = 0; u < kRowsPerThread; u++) clear_bits(words, clr[u], pos[u]);
 }
 
+// Validity of one column: clears, at its destination bit, the bit of every null row of the tile
+// (destination words start 0xff).  Thread t < ceil(n / 32) takes source rows 32t .. 32t + 31 and
+// visits only the nulls among them; `bits` is the shared address of the tile's staged validity
+// (the bytes past the tile's last row are slack of the stage and masked off), dbs[r] the
+// destination bit of source row r.
+__device__ __forceinline__ void scatter_null_bits(uint32_t* words, uint32_t bits, const uint32_t* dbs, int n) {
+  const int nw = (n + 31) >> 5;
+  for (int t = threadIdx.x; t < nw; t += kConsumers) {
+    const uint32_t a = bits + 4 * t;
+    const uint32_t v = lds8(a) | (lds8(a + 1) << 8) | (lds8(a + 2) << 16) | (lds8(a + 3) << 24);
+    uint32_t nulls = ~v;
+    const int rem = n - 32 * t;
+    if (rem < 32) nulls &= (1u << rem) - 1;
+    while (nulls) {
+      const int b = __ffs(nulls) - 1;
+      nulls &= nulls - 1;
+      const uint32_t pos = dbs[32 * t + b];
+      atomicAnd(words + (pos >> 5), ~(1u << (pos & 31)));
+    }
+  }
+}
+
 }  // namespace
 
 __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc sd, const FlushDesc fd) {
@@ -766,6 +788,7 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
   uint16_t* wcnt = reinterpret_cast<uint16_t*>(rt1 + T);    // [kW * 256]
   uint32_t* nm2 = reinterpret_cast<uint32_t*>(wcnt + kW * 256);  // [T]
   uint32_t* nm3 = nm2 + T;                                         // [T]
+  uint32_t* dbs = nm3 + T;                                         // [T] destination bit by source row
   // run metadata of the next binary column, by sorted position of the run start (S and wcnt
   // are free once the destinations are computed and the sort is done)
   uint32_t* nm0 = S;
@@ -919,7 +942,9 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
   csync();
   for (int j = threadIdx.x; j < n; j += kConsumers) {
     dstrow[j] = S[rs[j]] + (uint32_t)j;
-    dbit[j] = rt1[rs[j]] + (uint32_t)j;
+    const uint32_t db = rt1[rs[j]] + (uint32_t)j;
+    dbit[j] = db;
+    dbs[ps[j]] = db;
   }
 
   // Binary columns: thread t owns sorted positions t + u * kConsumers, u < kRowsPerThread.  The
@@ -975,8 +1000,8 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
     else if (kind == COL_BINARY) stg = staged_ptr(slot_base, reinterpret_cast<const uint8_t*>(c.offsets + row0));
     // validity: clear the bits of null rows (destination words start 0xff)
     if (c.validity != nullptr && s_nc[a] != 0 && fd.out_valid[a] != nullptr)
-      scatter_zero_bits(fd.out_valid[a], staged_ptr(slot_base + kStageBytes, c.validity + (row0 >> 3)), ps,
-                        dbit, n);
+      scatter_null_bits(fd.out_valid[a], smem_addr(staged_ptr(slot_base + kStageBytes, c.validity + (row0 >> 3))),
+                        dbs, n);
     if (kind == COL_FIXED) {
       const int w = sd.arr_width[a];
       uint8_t* out = fd.out_values[a];
@@ -1188,7 +1213,7 @@ size_t scatter_smem_bytes() {
   const int T = kTileRows;
   return kSlots * kStageSlot + kCharRegion + 4 * sizeof(uint16_t) * T + sizeof(uint32_t) * T +
          sizeof(uint16_t) * T + sizeof(uint32_t) * (T + 1) + 2 * sizeof(uint32_t) * T +
-         sizeof(uint16_t) * kW * 256 + 2 * sizeof(uint32_t) * T;
+         sizeof(uint16_t) * kW * 256 + 3 * sizeof(uint32_t) * T;
 }
 
 cudaError_t launch_scatter(const SchemaDesc& sd, const FlushDesc& fd, cudaStream_t st) {
