@@ -21,18 +21,6 @@ constexpr unsigned kFull = 0xffffffffu;
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31; }
 
-// Clears bit `pos` of `words` for every lane with `clear`; lanes that hit the same 32-bit word
-// are merged into one atomicAnd.  Must be reached by all lanes of the warp.
-__device__ __forceinline__ void clear_bits(uint32_t* words, bool clear, uint32_t pos) {
-  unsigned m = __ballot_sync(kFull, clear);
-  if (clear) {
-    uint32_t w = pos >> 5;
-    unsigned peers = __match_any_sync(m, w);
-    uint32_t bits = __reduce_or_sync(peers, 1u << (pos & 31));
-    if ((int)lane_id() == __ffs(peers) - 1) atomicAnd(words + w, ~bits);
-  }
-}
-
 // Barrier over the NT threads 0..NT-1: the whole block (BAR 0) or named barrier BAR.
 template <int NT, int BAR>
 __device__ __forceinline__ void group_sync() {
@@ -469,9 +457,10 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan_scan(const SchemaDesc sd,
 //      bits) is brought into shared memory by TMA bulk copies (cp.async.bulk, completion on an
 //      mbarrier), double-buffered so the next column streams in while this one is scattered;
 //      rows are then gathered from shared memory and written in sorted order, so the stores of
-//      a run are contiguous.  Validity and bool bits are cleared with warp-merged atomicAnd on
-//      0xff-filled words.  Characters of a binary column are copied one string per lane with
-//      aligned 32-bit destination words built by funnel shifts from aligned source words.
+//      a run are contiguous.  Validity and bool bits start as 0xff-filled words; the zeros of the
+//      tile (null rows, false values) are visited in source order and cleared by atomicAnd.
+//      Characters of a binary column are copied one string per lane with aligned 32-bit
+//      destination words built by funnel shifts from aligned source words.
 namespace {
 constexpr int kW = kScatterThreads / 32;
 constexpr int kConsumers = kScatterThreads;          // threads that scatter; one more warp issues copies
@@ -719,43 +708,22 @@ __device__ __forceinline__ void gather_rows(V* out, const V* src, const uint16_t
     if (threadIdx.x + u * kScatterThreads < n) out[d[u]] = v[u];
 }
 
-// Bit of sorted row j (source bit ps[j] of `bits`) cleared at destination bit dbit[j] of `words`
-// when it is 0.  All threads of the block call it.
-__device__ __forceinline__ void scatter_zero_bits(uint32_t* words, const uint8_t* bits, const uint16_t* ps,
-                                                  const uint32_t* dbit, int n) {
-  bool clr[kRowsPerThread];
-  uint32_t pos[kRowsPerThread];
-#pragma unroll
-  for (int u = 0; u < kRowsPerThread; u++) {
-    const int j = threadIdx.x + u * kScatterThreads;
-    clr[u] = false;
-    pos[u] = 0;
-    if (j < n) {
-      clr[u] = !get_bit(bits, ps[j]);
-      pos[u] = dbit[j];
-    }
-  }
-#pragma unroll
-  for (int u = 0; u < kRowsPerThread; u++) clear_bits(words, clr[u], pos[u]);
-}
-
-// Validity of one column: clears, at its destination bit, the bit of every null row of the tile
-// (destination words start 0xff).  Thread t < ceil(n / 32) takes source rows 32t .. 32t + 31 and
-// visits only the nulls among them; `bits` is the shared address of the tile's staged validity
-// (the bytes past the tile's last row are slack of the stage and masked off), dbs[r] the
-// destination bit of source row r.
-__device__ __forceinline__ void scatter_null_bits(uint32_t* words, uint32_t bits, const uint32_t* dbs, int n) {
-  const int nw = (n + 31) >> 5;
-  for (int t = threadIdx.x; t < nw; t += kConsumers) {
-    const uint32_t a = bits + 4 * t;
-    const uint32_t v = lds8(a) | (lds8(a + 1) << 8) | (lds8(a + 2) << 16) | (lds8(a + 3) << 24);
-    uint32_t nulls = ~v;
-    const int rem = n - 32 * t;
-    if (rem < 32) nulls &= (1u << rem) - 1;
-    while (nulls) {
-      const int b = __ffs(nulls) - 1;
-      nulls &= nulls - 1;
-      const uint32_t pos = dbs[32 * t + b];
+// Clears, at its destination bit, the bit of every source row of the tile whose bit in `bits`
+// is 0 (destination words start 0xff): the null rows of a validity bitmap, or the false values
+// of a bool column.  Thread t < ceil(n / 8) takes source rows 8t .. 8t + 7 and visits only the
+// zeros among them; `bits` is the shared address of the tile's staged bitmap (the bits past the
+// tile's last row are slack of the stage and masked off), dbs[r] the destination bit of source
+// row r.  Zeros of one destination word are cleared by separate atomicAnd calls.
+__device__ __forceinline__ void scatter_zero_bits(uint32_t* words, uint32_t bits, const uint32_t* dbs, int n) {
+  const int nb = (n + 7) >> 3;
+  for (int t = threadIdx.x; t < nb; t += kConsumers) {
+    uint32_t zeros = ~lds8(bits + t) & 0xffu;
+    const int rem = n - 8 * t;
+    if (rem < 8) zeros &= (1u << rem) - 1;
+    while (zeros) {
+      const int b = __ffs(zeros) - 1;
+      zeros &= zeros - 1;
+      const uint32_t pos = dbs[8 * t + b];
       atomicAnd(words + (pos >> 5), ~(1u << (pos & 31)));
     }
   }
@@ -780,8 +748,7 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
   uint16_t* pA = kA + T;
   uint16_t* kB = pA + T;
   uint16_t* pB = kB + T;
-  uint32_t* dbit = reinterpret_cast<uint32_t*>(pB + T);     // [T] (radix offsets while sorting)
-  uint16_t* rs = reinterpret_cast<uint16_t*>(dbit + T);     // [T]
+  uint16_t* rs = pB + T;                                    // [T]
   uint32_t* S = reinterpret_cast<uint32_t*>(rs + T);        // [T + 1]
   uint32_t* rt0 = S + T + 1;                                // [T] run tables (at run starts)
   uint32_t* rt1 = rt0 + T;                                  // [T]
@@ -789,6 +756,10 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
   uint32_t* nm2 = reinterpret_cast<uint32_t*>(wcnt + kW * 256);  // [T]
   uint32_t* nm3 = nm2 + T;                                         // [T]
   uint32_t* dbs = nm3 + T;                                         // [T] destination bit by source row
+  // radix offsets while sorting: rs, S and the start of rt0 are written only after the sort
+  uint32_t* roff = reinterpret_cast<uint32_t*>(rs);
+  static_assert(kW * 256 * sizeof(uint32_t) <= sizeof(uint16_t) * kTileRows + 2 * sizeof(uint32_t) * kTileRows,
+                "radix offsets fit over rs, S and rt0");
   // run metadata of the next binary column, by sorted position of the run start (S and wcnt
   // are free once the destinations are computed and the sort is done)
   uint32_t* nm0 = S;
@@ -901,12 +872,12 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
     pA[j] = (uint16_t)j;
   }
   csync();
-  radix_pass(kA, pA, kB, pB, n, 0, wcnt, dbit, scratch);
+  radix_pass(kA, pA, kB, pB, n, 0, wcnt, roff, scratch);
   uint16_t* ks = kB;
   uint16_t* ps = pB;
   uint32_t* dstrow = reinterpret_cast<uint32_t*>(kA);  // kA,pA are free after one pass
   if (P > 256) {
-    radix_pass(kB, pB, kA, pA, n, 8, wcnt, dbit, scratch);
+    radix_pass(kB, pB, kA, pA, n, 8, wcnt, roff, scratch);
     ks = kA;
     ps = pA;
     dstrow = reinterpret_cast<uint32_t*>(kB);
@@ -942,9 +913,7 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
   csync();
   for (int j = threadIdx.x; j < n; j += kConsumers) {
     dstrow[j] = S[rs[j]] + (uint32_t)j;
-    const uint32_t db = rt1[rs[j]] + (uint32_t)j;
-    dbit[j] = db;
-    dbs[ps[j]] = db;
+    dbs[ps[j]] = rt1[rs[j]] + (uint32_t)j;
   }
 
   // Binary columns: thread t owns sorted positions t + u * kConsumers, u < kRowsPerThread.  The
@@ -1000,7 +969,7 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
     else if (kind == COL_BINARY) stg = staged_ptr(slot_base, reinterpret_cast<const uint8_t*>(c.offsets + row0));
     // validity: clear the bits of null rows (destination words start 0xff)
     if (c.validity != nullptr && s_nc[a] != 0 && fd.out_valid[a] != nullptr)
-      scatter_null_bits(fd.out_valid[a], smem_addr(staged_ptr(slot_base + kStageBytes, c.validity + (row0 >> 3))),
+      scatter_zero_bits(fd.out_valid[a], smem_addr(staged_ptr(slot_base + kStageBytes, c.validity + (row0 >> 3))),
                         dbs, n);
     if (kind == COL_FIXED) {
       const int w = sd.arr_width[a];
@@ -1018,7 +987,7 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
         for (int j = threadIdx.x; j < n; j += kConsumers) reinterpret_cast<uint4*>(out)[dstrow[j]] = src[ps[j]];
       }
     } else if (kind == COL_BOOL) {
-      scatter_zero_bits(fd.out_bits[a], stg, ps, dbit, n);
+      scatter_zero_bits(fd.out_bits[a], smem_addr(stg), dbs, n);
     } else {
       const int32_t* oin = reinterpret_cast<const int32_t*>(stg);  // offsets of rows row0..row0+n
       // lengths of the owned positions; exclusive prefix over the tile = the lengths of all
@@ -1211,7 +1180,7 @@ cudaError_t launch_gather(const HostCopy* jobs, uint32_t n_jobs, cudaStream_t st
 
 size_t scatter_smem_bytes() {
   const int T = kTileRows;
-  return kSlots * kStageSlot + kCharRegion + 4 * sizeof(uint16_t) * T + sizeof(uint32_t) * T +
+  return kSlots * kStageSlot + kCharRegion + 4 * sizeof(uint16_t) * T +
          sizeof(uint16_t) * T + sizeof(uint32_t) * (T + 1) + 2 * sizeof(uint32_t) * T +
          sizeof(uint16_t) * kW * 256 + 3 * sizeof(uint32_t) * T;
 }

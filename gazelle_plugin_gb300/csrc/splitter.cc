@@ -187,19 +187,29 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
   (void)dummy;
   Status st = Cuda(cudaSetDevice(device_), "cudaSetDevice");
   if (!st.ok()) return st;
-  st = Cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
-  if (!st.ok()) return st;
   {
-    // host reads get the higher priority: their CTAs are scheduled ahead of a running pass's
+    // host reads, then k_hash_count and the plan, get the higher priorities: their CTAs are
+    // scheduled ahead of the remaining CTAs of a running k_scatter
     int least = 0, greatest = 0;
     cudaDeviceGetStreamPriorityRange(&least, &greatest);
     st = Cuda(cudaStreamCreateWithPriority(&cstream_, cudaStreamNonBlocking, greatest), "cudaStreamCreate");
+    if (!st.ok()) return st;
+    st = Cuda(cudaStreamCreateWithPriority(&stream_, cudaStreamNonBlocking, std::min(greatest + 1, least)),
+              "cudaStreamCreate");
+    if (!st.ok()) return st;
+    st = Cuda(cudaStreamCreateWithPriority(&sstream_, cudaStreamNonBlocking, least), "cudaStreamCreate");
     if (!st.ok()) return st;
   }
   st = Cuda(cudaStreamCreateWithFlags(&ostream_, cudaStreamNonBlocking), "cudaStreamCreate");
   if (!st.ok()) return st;
   st = Cuda(cudaEventCreateWithFlags(&gather_ev_, cudaEventDisableTiming), "cudaEventCreate");
   if (!st.ok()) return st;
+  st = Cuda(cudaEventCreateWithFlags(&plan_ev_, cudaEventDisableTiming), "cudaEventCreate");
+  if (!st.ok()) return st;
+  for (int i = 0; i < 2; i++) {
+    st = Cuda(cudaEventCreateWithFlags(&scr_ev_[i], cudaEventDisableTiming), "cudaEventCreate");
+    if (!st.ok()) return st;
+  }
   if (opts_.input_kind == GZ_INPUT_HOST && opts_.host_read == GZ_HOST_READ_AUTO) {
     // kernels may dereference any host address when the device walks the host page tables
     // (a coherent CPU-GPU link): host inputs are then read by k_gather, no CPU copy
@@ -260,6 +270,7 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
 Splitter::~Splitter() {
   if (cstream_) cudaStreamSynchronize(cstream_);
   if (stream_) cudaStreamSynchronize(stream_);
+  if (sstream_) cudaStreamSynchronize(sstream_);
   if (ostream_) cudaStreamSynchronize(ostream_);
   for (auto& f : flushes_) {
     if (f.d_out) cudaFreeAsync(f.d_out, stream_);
@@ -277,10 +288,15 @@ Splitter::~Splitter() {
     if (d_stage_[i]) cudaFreeAsync(d_stage_[i], stream_);
     if (stage_ev_[i]) cudaEventDestroy(stage_ev_[i]);
   }
-  if (d_scratch_) cudaFreeAsync(d_scratch_, stream_);
+  for (int i = 0; i < 2; i++) {
+    if (d_scratch_[i]) cudaFreeAsync(d_scratch_[i], stream_);
+    if (scr_ev_[i]) cudaEventDestroy(scr_ev_[i]);
+  }
   if (d_state_) cudaFreeAsync(d_state_, stream_);
   PinnedRelease(PinnedBlock{reinterpret_cast<uint8_t*>(h_jobs_), h_jobs_bytes_});
   if (gather_ev_) cudaEventDestroy(gather_ev_);
+  if (plan_ev_) cudaEventDestroy(plan_ev_);
+  if (sstream_) cudaStreamDestroy(sstream_);
   if (cstream_) cudaStreamDestroy(cstream_);
   if (ostream_) cudaStreamDestroy(ostream_);
   if (stream_) cudaStreamDestroy(stream_);
@@ -320,6 +336,8 @@ Status Splitter::EnsureStaging(size_t bytes) {
   Status st = FinishHostReads();
   if (!st.ok()) return st;
   st = Cuda(cudaStreamSynchronize(stream_), "sync");
+  if (!st.ok()) return st;
+  st = Cuda(cudaStreamSynchronize(sstream_), "sync");
   if (!st.ok()) return st;
   size_t cap = AlignUp(std::max<size_t>(bytes, (size_t)opts_.flush_bytes + (8u << 20)), 1 << 20);
   for (int i = 0; i < 2; i++) {
@@ -628,18 +646,19 @@ Status Splitter::PinnedMeta(size_t bytes, uint32_t** out) {
 }
 
 Status Splitter::EnsureScratch(size_t bytes) {
-  if (bytes <= scratch_cap_) return Status::OK();
+  const int i = scr_cur_;
+  if (bytes <= scratch_cap_[i]) return Status::OK();
   // stream-ordered (no wait for the whole device, which other splitters may be using): the old
-  // scratch is freed after the passes already queued on stream_
-  if (d_scratch_) {
-    Status st = Cuda(cudaFreeAsync(d_scratch_, stream_), "cudaFreeAsync(scratch)");
+  // buffer is freed on stream_, which already waits for the last k_scatter that read it
+  if (d_scratch_[i]) {
+    Status st = Cuda(cudaFreeAsync(d_scratch_[i], stream_), "cudaFreeAsync(scratch)");
     if (!st.ok()) return st;
-    d_scratch_ = nullptr;
+    d_scratch_[i] = nullptr;
   }
   size_t cap = AlignUp(bytes + bytes / 4, 1 << 20);
-  Status st = Cuda(cudaMallocAsync(reinterpret_cast<void**>(&d_scratch_), cap, stream_), "cudaMallocAsync(scratch)");
+  Status st = Cuda(cudaMallocAsync(reinterpret_cast<void**>(&d_scratch_[i]), cap, stream_), "cudaMallocAsync(scratch)");
   if (!st.ok()) return st;
-  scratch_cap_ = cap;
+  scratch_cap_[i] = cap;
   return Status::OK();
 }
 
@@ -771,9 +790,16 @@ Status Splitter::Flush() {
   const size_t tb_total = tb_batches + tb_tiles + tb_cols + tb_tdesc;
   const bool staged_tables = host_in && !direct_;  // tables travel with the pinned staging copy
   const size_t s_tab = staged_tables ? 0 : take(tb_total);
+  // this pass's scratch buffer: free once the k_scatter that last read it has finished
+  if (scr_busy_[scr_cur_]) {
+    st = Cuda(cudaStreamWaitEvent(stream_, scr_ev_[scr_cur_], 0), "wait scratch");
+    if (!st.ok()) return st;
+    scr_busy_[scr_cur_] = false;
+  }
   st = EnsureScratch(so);
   if (!st.ok()) return st;
-  uint8_t* S = d_scratch_;
+  uint8_t* S = d_scratch_[scr_cur_];
+  fr.scratch = scr_cur_;
 
   FlushDesc fd;
   memset(&fd, 0, sizeof(fd));
@@ -857,9 +883,6 @@ Status Splitter::Flush() {
     st = Cuda(cudaMemcpyAsync(d_stage_[cur_], h_stage_[cur_], used_, cudaMemcpyHostToDevice, stream_), "H2D");
     stat_h2d_bytes_ += (int64_t)used_;
     if (!st.ok()) return st;
-    st = Cuda(cudaEventRecord(stage_ev_[cur_], stream_), "event");
-    if (!st.ok()) return st;
-    stage_busy_[cur_] = true;
   } else {
     if (direct_) {  // the pass reads what k_gather wrote
       st = LaunchGather();
@@ -907,11 +930,21 @@ Status Splitter::Flush() {
   st = Cuda(launch_plan(sd_, fd, stream_), "k_plan");
   if (!st.ok()) return st;
   cudaEventRecord(fr.ev[2], stream_);
-  st = Cuda(launch_scatter(sd_, fd, stream_), "k_scatter");
+  // k_scatter on its own stream: the next pass's k_hash_count and plan need not wait for it
+  st = Cuda(cudaEventRecord(plan_ev_, stream_), "event");
   if (!st.ok()) return st;
-  cudaEventRecord(fr.ev[3], stream_);
-  if (direct_) {  // staging is free again once the kernels are done
-    st = Cuda(cudaEventRecord(stage_ev_[cur_], stream_), "event");
+  st = Cuda(cudaStreamWaitEvent(sstream_, plan_ev_, 0), "wait plan");
+  if (!st.ok()) return st;
+  cudaEventRecord(fr.ev[4], sstream_);
+  st = Cuda(launch_scatter(sd_, fd, sstream_), "k_scatter");
+  if (!st.ok()) return st;
+  cudaEventRecord(fr.ev[3], sstream_);
+  st = Cuda(cudaEventRecord(scr_ev_[scr_cur_], sstream_), "event");
+  if (!st.ok()) return st;
+  scr_busy_[scr_cur_] = true;
+  scr_cur_ ^= 1;
+  if (host_in) {  // the staging (inputs, and tables when staged) is free again after k_scatter
+    st = Cuda(cudaEventRecord(stage_ev_[cur_], sstream_), "event");
     if (!st.ok()) return st;
     stage_busy_[cur_] = true;
   }
@@ -975,6 +1008,8 @@ Status Splitter::SyncAndCheck() {
   if (!st.ok()) return st;
   st = Cuda(cudaStreamSynchronize(stream_), "device work");
   if (!st.ok()) return st;
+  st = Cuda(cudaStreamSynchronize(sstream_), "device work");
+  if (!st.ok()) return st;
   st = Cuda(cudaStreamSynchronize(ostream_), "partition data to host");
   if (!st.ok()) return st;
   int32_t err = 0;
@@ -987,7 +1022,9 @@ Status Splitter::SyncAndCheck() {
   for (; timed_flushes_ < flushes_.size(); timed_flushes_++) {
     FlushRec& f = flushes_[timed_flushes_];
     float ms[3] = {0, 0, 0};
-    for (int i = 0; i < 3; i++) cudaEventElapsedTime(&ms[i], f.ev[i], f.ev[i + 1]);
+    cudaEventElapsedTime(&ms[0], f.ev[0], f.ev[1]);
+    cudaEventElapsedTime(&ms[1], f.ev[1], f.ev[2]);
+    cudaEventElapsedTime(&ms[2], f.ev[4], f.ev[3]);
     kernel_ms_[0] += ms[0];
     kernel_ms_[1] += ms[1];
     kernel_ms_[2] += ms[2];
@@ -1296,9 +1333,12 @@ void Splitter::ReleaseStaging() {
     stage_busy_[i] = false;
   }
   stage_cap_ = 0;
-  if (d_scratch_) cudaFreeAsync(d_scratch_, stream_);
-  d_scratch_ = nullptr;
-  scratch_cap_ = 0;
+  for (int i = 0; i < 2; i++) {
+    if (d_scratch_[i]) cudaFreeAsync(d_scratch_[i], stream_);
+    d_scratch_[i] = nullptr;
+    scratch_cap_[i] = 0;
+    scr_busy_[i] = false;
+  }
 }
 
 Status Splitter::SpillFixedSize(int64_t size, int64_t* actual) {
@@ -1393,11 +1433,11 @@ Status Splitter::LastPids(uint16_t* out, int32_t n) {
   if (!st.ok()) return st;
   st = SyncAndCheck();
   if (!st.ok()) return st;
-  if (flushes_.empty() || (uint32_t)n != last_batch_rows_ || d_scratch_ == nullptr)
+  if (flushes_.empty() || (uint32_t)n != last_batch_rows_ || d_scratch_[flushes_.back().scratch] == nullptr)
     return Status::Error(GZ_INVALID, "no batch of that size was split last (or the splitter stopped)");
   const FlushRec& f = flushes_.back();
-  // the pids of the last flush sit at the start of the scratch; the last batch is at its end
-  const uint16_t* pids = reinterpret_cast<const uint16_t*>(d_scratch_);
+  // the pids of the last flush sit at the start of its scratch; the last batch is at their end
+  const uint16_t* pids = reinterpret_cast<const uint16_t*>(d_scratch_[f.scratch]);
   return Cuda(cudaMemcpy(out, pids + (f.n_rows - (uint32_t)n), 2 * (size_t)n, cudaMemcpyDeviceToHost),
               "D2H pids");
 }

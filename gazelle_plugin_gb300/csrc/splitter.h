@@ -99,7 +99,9 @@ class Splitter {
     uint32_t* h_meta = nullptr;         // pinned: rows_f, pstart, vstart, bytes_f, cstart, count, emit
     size_t meta_words = 0;
     uint32_t emit_cap = 0;
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // k1 start, plan start, k3 start, end
+    // k_hash_count start, plan start, plan end (stream_), k_scatter end, k_scatter start (sstream_)
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    int scratch = 0;                    // which scratch buffer the pass used
     const uint32_t* rows_f() const { return h_meta; }
     const uint32_t* pstart(int P) const { return h_meta + P; }
     const uint32_t* vstart(int P) const { return h_meta + 2 * (size_t)P; }
@@ -176,8 +178,16 @@ class Splitter {
   unsigned long long* st_ihn_ = nullptr;
   int32_t* d_err_ = nullptr;
   uint32_t* d_call_ = nullptr;
-  uint8_t* d_scratch_ = nullptr;
-  size_t scratch_cap_ = 0;
+  // k_scatter runs on sstream_, so a pass's scatter overlaps the next pass's k_hash_count and
+  // plan on stream_; the per-pass scratch is double-buffered, scr_ev_[i] marks the end of the
+  // last scatter that read buffer i
+  cudaStream_t sstream_ = nullptr;
+  cudaEvent_t plan_ev_ = nullptr;
+  uint8_t* d_scratch_[2] = {nullptr, nullptr};
+  size_t scratch_cap_[2] = {0, 0};
+  cudaEvent_t scr_ev_[2] = {nullptr, nullptr};
+  bool scr_busy_[2] = {false, false};
+  int scr_cur_ = 0;
 
   // staging (host inputs): double-buffered device buffers, filled by k_gather (direct_) or
   // by H2D copies of pinned host twins
