@@ -116,6 +116,27 @@ def generate_on_device(total_rows: int, seed: int = 1):
     return rows, addrs, sizes, [c[0] for c in bufcols]
 
 
+def link_bandwidth(nbytes: int = 1 << 30) -> dict:
+    """Host link of this box: one pinned 1 GiB buffer copied host->device and device->host (best
+    of 3, CUDA events).  The end-to-end figure moves the input and the partition bytes over it."""
+    import torch
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    out = {}
+    for name, dst, src in (("h2d_gbs", d, h), ("d2h_gbs", h, d)):
+        best = 0.0
+        for _ in range(3):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            dst.copy_(src, non_blocking=True)
+            b.record()
+            b.synchronize()
+            best = max(best, nbytes / (a.elapsed_time(b) * 1e-3) / 1e9)
+        out[name] = best
+    del h, d
+    return out
+
+
 def host_copy(addrs, sizes, tensors):
     """Pinned host copies of the generated buffers, laid out like the device ones; returns
     (host addrs, pinned tensors)."""
@@ -594,6 +615,7 @@ def run_gpu(args):
     # -- e2e: host buffers through the JNI-style contract ---------------------------------
     e2e = None
     if not args.no_e2e:
+        link = link_bandwidth()
         haddrs, host = host_copy(addrs, sizes, keep)
         host_opts = dict(writeSchema=False, input_kind=S.GZ_INPUT_HOST, keep_output_on_device=0,
                          flush_bytes=args.flush_mb << 20)
@@ -610,7 +632,8 @@ def run_gpu(args):
         e2e = {"value": alg_bytes * args.steps / e_t / 1e9, "unit": "GB/s",
                "h2d_bytes_per_step": int(statistics.mean(s[6] for s in e_stats)),
                "d2h_bytes_per_step": int(statistics.mean(s[7] for s in e_stats)),
-               "ms_per_step": e_t / args.steps * 1e3}
+               "ms_per_step": e_t / args.steps * 1e3,
+               "link": link}
         del host
 
     # -- CPU baseline on a bounded sample ---------------------------------------------------
@@ -662,7 +685,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--rows", type=int, default=200_000_000)
-    ap.add_argument("--flush-mb", type=int, default=512)
+    ap.add_argument("--flush-mb", type=int, default=2048)
     ap.add_argument("--sample-batches", type=int, default=512)
     ap.add_argument("--traffic-per-launch", type=float, default=None)
     ap.add_argument("--no-e2e", action="store_true")

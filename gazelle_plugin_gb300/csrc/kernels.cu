@@ -101,7 +101,11 @@ __device__ uint32_t block_exmax(uint32_t v, uint32_t* scratch) {
 // k_hash_count: one CTA per segment (<= seg_tiles * kTileRows rows of one batch).
 constexpr int kMaxStrPlan = 32;
 
-__global__ void __launch_bounds__(256) k_hash_count(const SchemaDesc sd, const FlushDesc fd) {
+constexpr int kHashThreads = 256;
+constexpr int kHashRows = kTileRows / kHashThreads;  // rows of a tile per thread
+static_assert(kHashRows * kHashThreads == kTileRows, "hash rows per thread");
+
+__global__ void __launch_bounds__(kHashThreads) k_hash_count(const SchemaDesc sd, const FlushDesc fd) {
   extern __shared__ uint32_t smem[];
   __shared__ ColPtr s_key[kMaxKeys];
   __shared__ int32_t s_kind[kMaxKeys];
@@ -139,37 +143,71 @@ __global__ void __launch_bounds__(256) k_hash_count(const SchemaDesc sd, const F
     __syncthreads();  // the copies are read before the next tile's rows are added
   }
   const uint32_t t1 = min(tile.nrows, t0 + (uint32_t)kTileRows);
-  for (uint32_t i = t0 + threadIdx.x; i < t1; i += blockDim.x) {
-    const uint32_t r = tile.row0 + i;
-    int32_t h = 42;
-    for (int k = 0; k < nkeys; k++) {
-      const ColPtr c = s_key[k];
-      if (c.validity != nullptr && !get_bit(c.validity, r)) continue;  // null: seed passes
-      switch (s_kind[k]) {
-        case KEY_I32: h = hash_int(reinterpret_cast<const int32_t*>(c.values)[r], h); break;
-        case KEY_I64: h = hash_long(reinterpret_cast<const int64_t*>(c.values)[r], h); break;
-        case KEY_I8: h = hash_int(reinterpret_cast<const int8_t*>(c.values)[r], h); break;
-        case KEY_I16: h = hash_int(reinterpret_cast<const int16_t*>(c.values)[r], h); break;
-        default: h = hash_int(get_bit(c.values, r) ? 1 : 0, h); break;
+  // rows t0 + threadIdx.x + u * kHashThreads, u < kHashRows: each key / offset column is loaded
+  // for all of them before any is used, so a thread has kHashRows loads in flight
+  bool act[kHashRows];
+  uint32_t rr[kHashRows];
+  int32_t h[kHashRows];
+#pragma unroll
+  for (int u = 0; u < kHashRows; u++) {
+    const uint32_t i = t0 + threadIdx.x + u * kHashThreads;
+    act[u] = i < t1;
+    rr[u] = tile.row0 + (act[u] ? i : t0);
+    h[u] = 42;
+  }
+  for (int k = 0; k < nkeys; k++) {
+    const ColPtr c = s_key[k];
+    const int kind = s_kind[k];
+    int64_t v[kHashRows];
+    bool valid[kHashRows];
+#pragma unroll
+    for (int u = 0; u < kHashRows; u++) {
+      const uint32_t r = rr[u];
+      valid[u] = c.validity == nullptr || get_bit(c.validity, r);  // null: seed passes
+      switch (kind) {
+        case KEY_I32: v[u] = reinterpret_cast<const int32_t*>(c.values)[r]; break;
+        case KEY_I64: v[u] = reinterpret_cast<const int64_t*>(c.values)[r]; break;
+        case KEY_I8: v[u] = reinterpret_cast<const int8_t*>(c.values)[r]; break;
+        case KEY_I16: v[u] = reinterpret_cast<const int16_t*>(c.values)[r]; break;
+        default: v[u] = get_bit(c.values, r) ? 1 : 0; break;
       }
     }
-    const uint32_t p = fast_pmod(h, (uint32_t)P, M);
-    fd.pids[tile.frow0 + i] = (uint16_t)p;
-    atomicAdd(&H[p], 1u);
-    for (int k = 0; k < nstr; k++) {
-      const ColPtr c = s_str[k];
-      const int32_t o0 = c.offsets[r], o1 = c.offsets[r + 1];
-      uint32_t len = (uint32_t)(o1 - o0);
-      // offsets of the first and one-past-last row of every kTileRows tile (k_scatter stages them)
-      const size_t ct = ((size_t)tile.tile0 + i / kTileRows) * nstr + k;
-      if (i % kTileRows == 0) fd.crange[ct].x = o0;
-      if (i % kTileRows == kTileRows - 1 || i + 1 == tile.nrows) fd.crange[ct].y = o1;
-      if (o0 < 0 || o1 < o0 || (uint64_t)o1 > c.values_bytes) {
+#pragma unroll
+    for (int u = 0; u < kHashRows; u++)
+      if (valid[u]) h[u] = kind == KEY_I64 ? hash_long(v[u], h[u]) : hash_int((int32_t)v[u], h[u]);
+  }
+  uint32_t p[kHashRows];
+#pragma unroll
+  for (int u = 0; u < kHashRows; u++) {
+    p[u] = fast_pmod(h[u], (uint32_t)P, M);
+    if (act[u]) {
+      fd.pids[tile.frow0 + t0 + threadIdx.x + u * kHashThreads] = (uint16_t)p[u];
+      atomicAdd(&H[p[u]], 1u);
+    }
+  }
+  for (int k = 0; k < nstr; k++) {
+    const ColPtr c = s_str[k];
+    int32_t o0[kHashRows], o1[kHashRows];
+#pragma unroll
+    for (int u = 0; u < kHashRows; u++) {
+      o0[u] = c.offsets[rr[u]];
+      o1[u] = c.offsets[rr[u] + 1];
+    }
+#pragma unroll
+    for (int u = 0; u < kHashRows; u++) {
+      uint32_t len = (uint32_t)(o1[u] - o0[u]);
+      if (o0[u] < 0 || o1[u] < o0[u] || (uint64_t)o1[u] > c.values_bytes) {
         bad = true;
         len = 0;
       }
-      if (len) atomicAdd(&BH[k * P + p], len);
+      if (act[u] && len) atomicAdd(&BH[k * P + p[u]], len);
     }
+  }
+  // offsets of the tile's first and one-past-last row (k_scatter stages the characters between)
+  if (threadIdx.x < nstr) {
+    const ColPtr c = s_str[threadIdx.x];
+    const size_t ct = ((size_t)tile.tile0 + t0 / kTileRows) * nstr + threadIdx.x;
+    fd.crange[ct] = make_int2(c.offsets[tile.row0 + t0], c.offsets[tile.row0 + t1]);
   }
   }
   if (bad) atomicOr(fd.err, kErrBadOffsets);  // k_scatter then copies nothing
@@ -1141,7 +1179,7 @@ cudaError_t launch_hash_count(const SchemaDesc& sd, const FlushDesc& fd, cudaStr
     cudaError_t e = cudaFuncSetAttribute(k_hash_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
   }
-  k_hash_count<<<fd.n_segs, 256, sm, st>>>(sd, fd);
+  k_hash_count<<<fd.n_segs, kHashThreads, sm, st>>>(sd, fd);
   return cudaGetLastError();
 }
 
