@@ -683,28 +683,52 @@ __device__ __forceinline__ uint32_t lds8(uint32_t addr) {
   return v;
 }
 
+// Bytes [lo, hi) of word `w` to the 4-byte aligned `p`: a byte at an odd start, then a halfword,
+// then a last byte (at most two stores).
+__device__ __forceinline__ void store_word_part(uint8_t* p, uint32_t w, uint32_t lo, uint32_t hi) {
+  uint32_t x = lo;
+  if (x & 1) {
+    p[x] = (uint8_t)(w >> (8 * x));
+    x++;
+  }
+  if (x + 2 <= hi) {
+    *reinterpret_cast<uint16_t*>(p + x) = (uint16_t)(w >> (8 * x));
+    x += 2;
+  }
+  if (x < hi) p[x] = (uint8_t)(w >> (8 * x));
+}
+
 // One string whose source bytes are in shared memory (shared address `src`): `len` bytes to
-// global `dst`.  Up to 3 head bytes bring the destination to a 4-byte boundary, then whole
-// aligned words, each a funnel shift of two aligned source words, then up to 3 tail bytes.  The
-// aligned source words may reach 7 bytes past `src + len`: the staging buffer keeps that slack,
-// and those bytes are never stored.
+// global `dst`, written in the aligned 4-byte words of the destination.  Every destination word
+// is a funnel shift of two aligned source words (one shift for the whole string), loaded as a
+// stream; the first and last words, when the string covers them only in part, are stored as a
+// byte and / or a halfword.  The aligned source words may reach 6 bytes before `src` and 7 past
+// `src + len`: the staging buffer keeps that slack, and those bytes are never stored.
 __device__ __forceinline__ void copy_string_smem(uint8_t* dst, uint32_t src, uint32_t len) {
+  if (len == 0) return;
   const uintptr_t d = reinterpret_cast<uintptr_t>(dst);
-  const uint32_t lead = (uint32_t)((4 - (d & 3)) & 3);
-  const uint32_t head = len < lead ? len : lead;
-#pragma unroll
-  for (uint32_t t = 0; t < 3; t++)
-    if (t < head) dst[t] = (uint8_t)lds8(src + t);
-  const uint32_t nw = (len - head) >> 2;
-  const uint32_t s = src + head;
-  const uint32_t sw = s & ~3u;
-  const uint32_t sh = (s & 3) * 8;
-  uint32_t* dw = reinterpret_cast<uint32_t*>(d + head);
-  uint32_t lo = lds32(sw);
+  const uint32_t ph = (uint32_t)(d & 3);
+  const uint32_t a = src - ph;  // source byte that maps to the first destination word
+  uint32_t sb = a & ~3u;
+  const uint32_t sh = (a & 3) * 8;
+  uint8_t* X = dst - ph;
+  uint32_t lo = lds32(sb);
+  uint32_t rem = len;
+  if (ph) {  // the string starts inside its first destination word
+    const uint32_t hi = lds32(sb + 4);
+    const uint32_t e = min(4u, ph + len);
+    store_word_part(X, __funnelshift_r(lo, hi, sh), ph, e);
+    rem -= e - ph;
+    X += 4;
+    sb += 4;
+    lo = hi;
+  }
+  uint32_t* dw = reinterpret_cast<uint32_t*>(X);
+  const uint32_t nw = rem >> 2;
   uint32_t k = 0;
   for (; k + 4 <= nw; k += 4) {  // four source words loaded before any store
-    const uint32_t w1 = lds32(sw + 4 * k + 4), w2 = lds32(sw + 4 * k + 8);
-    const uint32_t w3 = lds32(sw + 4 * k + 12), w4 = lds32(sw + 4 * k + 16);
+    const uint32_t w1 = lds32(sb + 4 * k + 4), w2 = lds32(sb + 4 * k + 8);
+    const uint32_t w3 = lds32(sb + 4 * k + 12), w4 = lds32(sb + 4 * k + 16);
     dw[k] = __funnelshift_r(lo, w1, sh);
     dw[k + 1] = __funnelshift_r(w1, w2, sh);
     dw[k + 2] = __funnelshift_r(w2, w3, sh);
@@ -712,14 +736,14 @@ __device__ __forceinline__ void copy_string_smem(uint8_t* dst, uint32_t src, uin
     lo = w4;
   }
   for (; k < nw; k++) {
-    const uint32_t hi = lds32(sw + 4 * k + 4);
+    const uint32_t hi = lds32(sb + 4 * k + 4);
     dw[k] = __funnelshift_r(lo, hi, sh);
     lo = hi;
   }
-  const uint32_t done = head + 4 * nw;
-#pragma unroll
-  for (uint32_t t = 0; t < 3; t++)
-    if (done + t < len) dst[done + t] = (uint8_t)lds8(src + done + t);
+  if (rem & 3) {  // the string ends inside its last destination word
+    const uint32_t hi = lds32(sb + 4 * nw + 4);
+    store_word_part(reinterpret_cast<uint8_t*>(dw + nw), __funnelshift_r(lo, hi, sh), 0, rem & 3);
+  }
 }
 
 // Rows a thread handles in a tile: j = threadIdx.x + u * kScatterThreads, u < kRowsPerThread.
@@ -986,135 +1010,145 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
   load_run_meta(0);
   uint32_t cuse = 0;  // staged character slices consumed
 
+  // Warps run through fixed-width and bool columns at their own pace (the slots' mbarriers keep
+  // the fastest within kSlots columns of the slowest); only a binary column, which rewrites the
+  // shared run tables, starts with a barrier of the scattering threads.  A wait that times out
+  // marks the block bad: from then on columns are skipped, but every thread still reaches every
+  // barrier (the skip decision of a binary column is taken after its barrier, so it is the same
+  // in all threads).
+  volatile uint32_t* vbad = &s_bad;
   for (int i = 0; i < A; i++) {
     const int a = sd.order[i];
     const int slot = i % kSlots;
     const bool chars = staged_binary(a);
-    bool ok = mbar_wait(&full[slot], (uint32_t)((i / kSlots) & 1));
-    if (chars) ok = mbar_wait(&cfull, cuse & 1) && ok;
-    if (!ok) {
-      if (threadIdx.x == 0) atomicOr(fd.err, kErrTimeout);
-      s_bad = 1;
-    }
-    csync();  // also: every thread is done with the previous column's shared tables
-    if (s_bad) break;
-    const ColPtr c = s_col[a];
     const int kind = sd.arr_kind[a];
-    const uint8_t* slot_base = stage0 + slot * kStageSlot;
-    const uint8_t* stg = slot_base;  // staged values / bits / offsets, at the source's phase
-    if (kind == COL_FIXED && sd.arr_width[a] <= 8) stg = staged_ptr(slot_base, c.values + (size_t)row0 * sd.arr_width[a]);
-    else if (kind == COL_BOOL) stg = staged_ptr(slot_base, c.values + (row0 >> 3));
-    else if (kind == COL_BINARY) stg = staged_ptr(slot_base, reinterpret_cast<const uint8_t*>(c.offsets + row0));
-    // validity: clear the bits of null rows (destination words start 0xff)
-    if (c.validity != nullptr && s_nc[a] != 0 && fd.out_valid[a] != nullptr)
-      scatter_zero_bits(fd.out_valid[a], smem_addr(staged_ptr(slot_base + kStageBytes, c.validity + (row0 >> 3))),
-                        dbs, n);
-    if (kind == COL_FIXED) {
-      const int w = sd.arr_width[a];
-      uint8_t* out = fd.out_values[a];
-      if (w == 8) {
-        gather_rows(reinterpret_cast<uint64_t*>(out), reinterpret_cast<const uint64_t*>(stg), ps, dstrow, n);
-      } else if (w == 4) {
-        gather_rows(reinterpret_cast<uint32_t*>(out), reinterpret_cast<const uint32_t*>(stg), ps, dstrow, n);
-      } else if (w == 2) {
-        gather_rows(reinterpret_cast<uint16_t*>(out), reinterpret_cast<const uint16_t*>(stg), ps, dstrow, n);
-      } else if (w == 1) {
-        gather_rows(out, stg, ps, dstrow, n);
-      } else {  // 16-byte values are gathered straight from global memory
-        const uint4* src = reinterpret_cast<const uint4*>(c.values) + row0;
-        for (int j = threadIdx.x; j < n; j += kConsumers) reinterpret_cast<uint4*>(out)[dstrow[j]] = src[ps[j]];
+    if (!*vbad) {
+      bool ok = mbar_wait(&full[slot], (uint32_t)((i / kSlots) & 1));
+      if (chars) ok = mbar_wait(&cfull, cuse & 1) && ok;
+      if (!ok) {
+        atomicOr(fd.err, kErrTimeout);
+        *vbad = 1;
       }
-    } else if (kind == COL_BOOL) {
-      scatter_zero_bits(fd.out_bits[a], smem_addr(stg), dbs, n);
-    } else {
-      const int32_t* oin = reinterpret_cast<const int32_t*>(stg);  // offsets of rows row0..row0+n
-      // lengths of the owned positions; exclusive prefix over the tile = the lengths of all
-      // earlier rows u' < u of positions + this row's prefix, one fused warp scan per row u
-      uint32_t len[kRowsPerThread], pre[kRowsPerThread];
-#pragma unroll
-      for (int u = 0; u < kRowsPerThread; u++) {
-        const int j = threadIdx.x + u * kConsumers;
-        len[u] = 0;
-        if (j < n) {
-          const int r = ps[j];
-          len[u] = (uint32_t)(oin[r + 1] - oin[r]);
+    }
+    if (kind == COL_BINARY) csync();
+    if (!*vbad) {
+      const ColPtr c = s_col[a];
+      const uint8_t* slot_base = stage0 + slot * kStageSlot;
+      const uint8_t* stg = slot_base;  // staged values / bits / offsets, at the source's phase
+      if (kind == COL_FIXED && sd.arr_width[a] <= 8) stg = staged_ptr(slot_base, c.values + (size_t)row0 * sd.arr_width[a]);
+      else if (kind == COL_BOOL) stg = staged_ptr(slot_base, c.values + (row0 >> 3));
+      else if (kind == COL_BINARY) stg = staged_ptr(slot_base, reinterpret_cast<const uint8_t*>(c.offsets + row0));
+      // validity: clear the bits of null rows (destination words start 0xff)
+      if (c.validity != nullptr && s_nc[a] != 0 && fd.out_valid[a] != nullptr)
+        scatter_zero_bits(fd.out_valid[a], smem_addr(staged_ptr(slot_base + kStageBytes, c.validity + (row0 >> 3))),
+                          dbs, n);
+      if (kind == COL_FIXED) {
+        const int w = sd.arr_width[a];
+        uint8_t* out = fd.out_values[a];
+        if (w == 8) {
+          gather_rows(reinterpret_cast<uint64_t*>(out), reinterpret_cast<const uint64_t*>(stg), ps, dstrow, n);
+        } else if (w == 4) {
+          gather_rows(reinterpret_cast<uint32_t*>(out), reinterpret_cast<const uint32_t*>(stg), ps, dstrow, n);
+        } else if (w == 2) {
+          gather_rows(reinterpret_cast<uint16_t*>(out), reinterpret_cast<const uint16_t*>(stg), ps, dstrow, n);
+        } else if (w == 1) {
+          gather_rows(out, stg, ps, dstrow, n);
+        } else {  // 16-byte values are gathered straight from global memory
+          const uint4* src = reinterpret_cast<const uint4*>(c.values) + row0;
+          for (int j = threadIdx.x; j < n; j += kConsumers) reinterpret_cast<uint4*>(out)[dstrow[j]] = src[ps[j]];
         }
-        pre[u] = len[u];
-      }
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-#pragma unroll
-        for (int u = 0; u < kRowsPerThread; u++) {
-          const uint32_t y = __shfl_up_sync(kFull, pre[u], o);
-          if ((int)lane_id() >= o) pre[u] += y;
-        }
-      }
-      const int w = threadIdx.x >> 5;
-      if (lane_id() == 31) {
-#pragma unroll
-        for (int u = 0; u < kRowsPerThread; u++) scratch[u * kW + w] = pre[u];
-      }
-      csync();
-      {
-        uint32_t before = 0;  // all positions of earlier rows, then earlier warps of this row
-#pragma unroll
-        for (int u = 0; u < kRowsPerThread; u++) {
-          uint32_t row_total = 0, warps_before = 0;
-          for (int q = 0; q < kW; q++) {
-            const uint32_t t = scratch[u * kW + q];
-            row_total += t;
-            if (q < w) warps_before += t;
-          }
-          pre[u] = before + warps_before + pre[u] - len[u];
-          before += row_total;
-        }
-      }
-      // run tables at the run starts: destination of the run's first string and its offset
-      // inside the partition's segment, both relative to the tile prefix
-      cp_async_wait_all();
-#pragma unroll
-      for (int u = 0; u < kRowsPerThread; u++) {
-        const int j = threadIdx.x + u * kConsumers;
-        if (j < n && rs[j] == j) {
-          const uint32_t before = has_pre ? nm3[j] : 0u;  // bytes from the segment's earlier tiles
-          rt0[j] = nm0[j] + before - pre[u];
-          rt1[j] = nm2[j] + nm1[j] + before - pre[u];
-        }
-      }
-      load_run_meta(i + 1);
-      csync();
-      int32_t* ooff = reinterpret_cast<int32_t*>(fd.out_values[a]);
-      uint8_t* ochars = fd.out_chars[a];
-      {
-        uint32_t d[kRowsPerThread], v[kRowsPerThread];
-#pragma unroll
-        for (int u = 0; u < kRowsPerThread; u++) {
-          const int j = threadIdx.x + u * kConsumers;
-          if (j < n) {
-            d[u] = dstrow[j];
-            v[u] = rt0[rs[j]] + pre[u] + len[u];
-          }
-        }
-#pragma unroll
-        for (int u = 0; u < kRowsPerThread; u++)
-          if (threadIdx.x + u * kConsumers < n) ooff[d[u]] = (int32_t)v[u];
-      }
-      const int k = sd.arr_str[a];
-      if (chars) {
-        // shared address of byte 0 of the column (offsets index from there)
-        const uint32_t cbase = smem_addr(staged_ptr(cstage, c.values + s_cr[k].x)) - (uint32_t)s_cr[k].x;
-#pragma unroll
-        for (int u = 0; u < kRowsPerThread; u++) {
-          const int j = threadIdx.x + u * kConsumers;
-          if (j < n) copy_string_smem(ochars + rt1[rs[j]] + pre[u], cbase + (uint32_t)oin[ps[j]], len[u]);
-        }
+      } else if (kind == COL_BOOL) {
+        scatter_zero_bits(fd.out_bits[a], smem_addr(stg), dbs, n);
       } else {
-        const uintptr_t buf_lo = reinterpret_cast<uintptr_t>(c.values);
-        const uintptr_t buf_hi = buf_lo + c.values_bytes;
+        const int32_t* oin = reinterpret_cast<const int32_t*>(stg);  // offsets of rows row0..row0+n
+        // lengths of the owned positions; exclusive prefix over the tile = the lengths of all
+        // earlier rows u' < u of positions + this row's prefix, one fused warp scan per row u
+        uint32_t len[kRowsPerThread], pre[kRowsPerThread];
 #pragma unroll
         for (int u = 0; u < kRowsPerThread; u++) {
           const int j = threadIdx.x + u * kConsumers;
-          if (j < n) copy_string(ochars + rt1[rs[j]] + pre[u], c.values + oin[ps[j]], len[u], buf_lo, buf_hi);
+          len[u] = 0;
+          if (j < n) {
+            const int r = ps[j];
+            len[u] = (uint32_t)(oin[r + 1] - oin[r]);
+          }
+          pre[u] = len[u];
+        }
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+          for (int u = 0; u < kRowsPerThread; u++) {
+            const uint32_t y = __shfl_up_sync(kFull, pre[u], o);
+            if ((int)lane_id() >= o) pre[u] += y;
+          }
+        }
+        const int w = threadIdx.x >> 5;
+        if (lane_id() == 31) {
+#pragma unroll
+          for (int u = 0; u < kRowsPerThread; u++) scratch[u * kW + w] = pre[u];
+        }
+        csync();
+        {
+          uint32_t before = 0;  // all positions of earlier rows, then earlier warps of this row
+#pragma unroll
+          for (int u = 0; u < kRowsPerThread; u++) {
+            uint32_t row_total = 0, warps_before = 0;
+            for (int q = 0; q < kW; q++) {
+              const uint32_t t = scratch[u * kW + q];
+              row_total += t;
+              if (q < w) warps_before += t;
+            }
+            pre[u] = before + warps_before + pre[u] - len[u];
+            before += row_total;
+          }
+        }
+        // run tables at the run starts: destination of the run's first string and its offset
+        // inside the partition's segment, both relative to the tile prefix
+        cp_async_wait_all();
+#pragma unroll
+        for (int u = 0; u < kRowsPerThread; u++) {
+          const int j = threadIdx.x + u * kConsumers;
+          if (j < n && rs[j] == j) {
+            const uint32_t before = has_pre ? nm3[j] : 0u;  // bytes from the segment's earlier tiles
+            rt0[j] = nm0[j] + before - pre[u];
+            rt1[j] = nm2[j] + nm1[j] + before - pre[u];
+          }
+        }
+        load_run_meta(i + 1);
+        csync();
+        int32_t* ooff = reinterpret_cast<int32_t*>(fd.out_values[a]);
+        uint8_t* ochars = fd.out_chars[a];
+        {
+          uint32_t d[kRowsPerThread], v[kRowsPerThread];
+#pragma unroll
+          for (int u = 0; u < kRowsPerThread; u++) {
+            const int j = threadIdx.x + u * kConsumers;
+            if (j < n) {
+              d[u] = dstrow[j];
+              v[u] = rt0[rs[j]] + pre[u] + len[u];
+            }
+          }
+#pragma unroll
+          for (int u = 0; u < kRowsPerThread; u++)
+            if (threadIdx.x + u * kConsumers < n) ooff[d[u]] = (int32_t)v[u];
+        }
+        const int k = sd.arr_str[a];
+        if (chars) {
+          // shared address of byte 0 of the column (offsets index from there)
+          const uint32_t cbase = smem_addr(staged_ptr(cstage, c.values + s_cr[k].x)) - (uint32_t)s_cr[k].x;
+#pragma unroll
+          for (int u = 0; u < kRowsPerThread; u++) {
+            const int j = threadIdx.x + u * kConsumers;
+            if (j < n) copy_string_smem(ochars + rt1[rs[j]] + pre[u], cbase + (uint32_t)oin[ps[j]], len[u]);
+          }
+        } else {
+          const uintptr_t buf_lo = reinterpret_cast<uintptr_t>(c.values);
+          const uintptr_t buf_hi = buf_lo + c.values_bytes;
+#pragma unroll
+          for (int u = 0; u < kRowsPerThread; u++) {
+            const int j = threadIdx.x + u * kConsumers;
+            if (j < n) copy_string(ochars + rt1[rs[j]] + pre[u], c.values + oin[ps[j]], len[u], buf_lo, buf_hi);
+          }
         }
       }
     }
@@ -1125,6 +1159,7 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
     }
     if (chars) cuse++;
   }
+  cp_async_wait_all();  // no run-metadata copy is left in flight when the block exits
 }
 
 // =======================================================================================
