@@ -41,8 +41,9 @@ WORKLOAD = ("wide fact-table split: 200M rows, 4096-row batches, 16 columns "
             "2% nulls, hash on keys 0-1, 200 partitions")
 BATCH_ROWS = 4096
 # DRAM bytes that one k_scatter launch moves per algorithmic byte, from an ncu capture of one
-# full 512 MiB pass of this workload (profiles/k_scatter_wide_fact_table.md).
-K_SCATTER_DRAM_PER_ALG_BYTE = 1.010
+# pass of this workload (2,036,224 rows: 732.9 MB of DRAM traffic for 732.4 MB algorithmic;
+# profiles/k_scatter_wide_fact_table.md).
+K_SCATTER_DRAM_PER_ALG_BYTE = 1.001
 PARTITIONS = 200
 KEYS = [0, 1]
 
@@ -605,9 +606,11 @@ def run_gpu(args):
                 "traffic": (args.traffic_per_launch or
                             K_SCATTER_DRAM_PER_ALG_BYTE * alg_bytes / max(flushes, 1)),
                 "traffic_source": ("--traffic-per-launch" if args.traffic_per_launch else
-                                   "ncu dram__bytes_read.sum + dram__bytes_write.sum of a full "
-                                   "512 MiB pass (1.085 GB for 1.074 GB algorithmic), scaled "
-                                   "to this run's average pass"),
+                                   "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
+                                   "pass (732.9 MB for 732.4 MB algorithmic), scaled to this "
+                                   "run's average pass"),
+                "overlap": ("k_scatter of pass i runs beside k_hash_count and the plan of pass "
+                            "i + 1; its duration is the live one, with that overlap"),
                 "launches_per_step": flushes,
                 "algorithmic_bytes_per_launch": alg_bytes / max(flushes, 1),
                 "avg_launch_ms": k_scat / max(flushes, 1)}
@@ -685,7 +688,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--rows", type=int, default=200_000_000)
-    ap.add_argument("--flush-mb", type=int, default=2048)
+    ap.add_argument("--flush-mb", type=int, default=1024)
     ap.add_argument("--sample-batches", type=int, default=512)
     ap.add_argument("--traffic-per-launch", type=float, default=None)
     ap.add_argument("--no-e2e", action="store_true")

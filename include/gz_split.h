@@ -84,7 +84,7 @@ typedef struct GzSplitOptions {
                                         or until device_budget is exceeded; 0: every flush is
                                         copied to pinned host memory as soon as it is done */
   int64_t flush_bytes;               /* input bytes gathered before one device pass
-                                        (default 512 MiB) */
+                                        (default 512 MiB, at most 1 GiB) */
   int64_t device_budget;             /* HBM bytes for resident partition data before it is
                                         moved to pinned host memory (default 64 GiB) */
   const char* data_file;             /* written at Stop; NULL/"" keeps the bytes in memory */
