@@ -18,7 +18,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgzsplit.so")
 
 SOURCES = ["kernels.cu", "splitter.cc", "ipc.cc", "schema_ipc.cc", "capi.cc", "host_util.cc",
-           "hash_static.cu", "serve.cc"]
+           "hash_static.cu", "serve.cc", "tune.cc"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

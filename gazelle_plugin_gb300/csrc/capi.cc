@@ -7,6 +7,9 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
+#include <chrono>
+
 #include <map>
 #include <memory>
 #include <mutex>
@@ -18,6 +21,7 @@
 #include "schema_ipc.h"
 #include "serve.h"
 #include "splitter.h"
+#include "tune.h"
 
 namespace {
 
@@ -304,8 +308,17 @@ GzStatus gz_serve_open(int64_t server, const char* short_name, int32_t num_parti
   if (opts) o = *opts;
   else gz_split_default_options(&o);
   // its share of the budget: resident partition data up to the spill threshold, two staging
-  // buffers and the pass scratch
-  const int64_t reserve = std::max<int64_t>(o.device_budget, 0) + 3 * std::max<int64_t>(o.flush_bytes, 0) + (64ll << 20);
+  // buffers and the pass scratch (a pass size of 0 is the autotuner's choice, else 512 MiB)
+  int64_t flush = o.flush_bytes;
+  if (flush <= 0) {
+    gz::TuneChoice tc;
+    const std::vector<int32_t> keys(key_cols, key_cols + (key_cols && n_keys > 0 ? n_keys : 0));
+    flush = gz::TuneLookup(gz::SchemaSignature(FieldsFrom(fields, n_fields), keys, num_partitions), &tc)
+                ? tc.flush_bytes
+                : (512ll << 20);
+  }
+  flush = std::min<int64_t>(flush, 1ll << 30);
+  const int64_t reserve = std::max<int64_t>(o.device_budget, 0) + 3 * flush + (64ll << 20);
   gz::Status st = srv->Admit(reserve);
   if (!st.ok()) {
     t_make_error = "gz_serve_open: " + st.msg;
@@ -368,6 +381,98 @@ GzStatus gz_serve_wait(int64_t server, int64_t ticket, int64_t* out_latency_ns, 
     return GZ_INVALID;
   }
   gz::Status st = srv->Wait(ticket, out_latency_ns, out_service_ns);
+  if (!st.ok()) t_make_error = st.msg;
+  return st.code;
+}
+
+GzStatus gz_autotune(const char* short_name, int32_t num_partitions, const GzField* fields, int32_t n_fields,
+                     const int32_t* key_cols, int32_t n_keys, const GzSplitOptions* opts, int32_t n_batches,
+                     const int32_t* rows, const int64_t* buf_addrs, const int64_t* buf_sizes, int32_t n_bufs,
+                     GzTuneResult* out) {
+  if (!short_name || (!fields && n_fields > 0) || n_batches <= 0 || !rows || !buf_addrs || !buf_sizes ||
+      n_bufs <= 0 || (!key_cols && n_keys > 0)) {
+    t_make_error = "gz_autotune: invalid arguments";
+    return GZ_INVALID;
+  }
+  GzSplitOptions base;
+  if (opts) base = *opts;
+  else gz_split_default_options(&base);
+  base.data_file = nullptr;  // nothing is written: the candidates are never stopped
+  const std::vector<gz::Field> fs = FieldsFrom(fields, n_fields);
+  const std::vector<int32_t> keys(key_cols, key_cols + (n_keys > 0 ? n_keys : 0));
+  int64_t sample = 0;
+  for (int64_t i = 0; i < (int64_t)n_batches * n_bufs; i++) sample += std::max<int64_t>(buf_sizes[i], 0);
+  int32_t runs = 0;
+  // one candidate: made, warmed up once, then timed from the first Split to the end of its device work
+  auto measure = [&](int64_t flush, int32_t seg, double* gbs) -> gz::Status {
+    GzSplitOptions o = base;
+    o.flush_bytes = flush;
+    o.seg_tiles = seg;
+    for (int rep = 0; rep < 2; rep++) {
+      std::unique_ptr<gz::Splitter> sp;
+      gz::Status st = gz::Splitter::Make(short_name, fs, num_partitions, keys, o, &sp);
+      if (!st.ok()) return st;
+      const auto t0 = std::chrono::steady_clock::now();
+      st = sp->SplitBatches(n_batches, rows, buf_addrs, buf_sizes, n_bufs);
+      if (st.ok()) st = sp->Sync();
+      const auto t1 = std::chrono::steady_clock::now();
+      if (!st.ok()) return st;
+      if (rep == 1) {
+        *gbs = (double)sample / std::chrono::duration<double>(t1 - t0).count() / 1e9;
+        runs++;
+      }
+    }
+    return gz::Status::OK();
+  };
+  gz::TuneChoice best;
+  double def_gbs = 0;
+  gz::Status st;
+  // pass sizes 16 MiB .. 1 GiB; once one pass holds the whole sample, larger ones are the same
+  double last = 0;
+  bool covered = false;
+  for (int64_t flush = 16ll << 20; flush <= (1ll << 30) && st.ok(); flush *= 2) {
+    double g = last;
+    if (!covered) {
+      st = measure(flush, 0, &g);
+      if (!st.ok()) break;
+      if (g > best.gbs) best = gz::TuneChoice{flush, 0, g};
+      last = g;
+      covered = flush >= sample;
+    }
+    if (flush == (512ll << 20)) def_gbs = g;
+  }
+  // segment lengths at the best pass size
+  for (int32_t seg : {1, 4, 8, 16, 32}) {
+    if (!st.ok()) break;
+    double g = 0;
+    st = measure(best.flush_bytes, seg, &g);
+    if (st.ok() && g > best.gbs) best = gz::TuneChoice{best.flush_bytes, seg, g};
+  }
+  if (!st.ok()) {
+    t_make_error = "gz_autotune: " + st.msg;
+    return st.code;
+  }
+  gz::TuneStore(gz::SchemaSignature(fs, keys, num_partitions), best);
+  if (out) {
+    out->flush_bytes = best.flush_bytes;
+    out->seg_tiles = best.seg_tiles;
+    out->runs = runs;
+    out->best_gbs = best.gbs;
+    out->default_gbs = def_gbs;
+  }
+  return GZ_OK;
+}
+
+GzStatus gz_tune_save(const char* path) {
+  if (!path) return GZ_INVALID;
+  gz::Status st = gz::TuneSave(path);
+  if (!st.ok()) t_make_error = st.msg;
+  return st.code;
+}
+
+GzStatus gz_tune_load(const char* path) {
+  if (!path) return GZ_INVALID;
+  gz::Status st = gz::TuneLoad(path);
   if (!st.ok()) t_make_error = st.msg;
   return st.code;
 }

@@ -9,6 +9,7 @@
 
 #include "gz_kernels.h"
 #include "host_util.h"
+#include "tune.h"
 
 namespace gz {
 
@@ -88,8 +89,6 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
   if (opts_.buffer_size > 32 * 1024) return Status::Error(GZ_INVALID, "buffer_size must be <= 32768");
   if (opts_.compression != 0)
     return Status::Error(GZ_NOT_IMPLEMENTED, "only uncompressed shuffle output is implemented");
-  if (opts_.flush_bytes <= 0) opts_.flush_bytes = 512ll << 20;
-  if (opts_.flush_bytes > (1ll << 30)) opts_.flush_bytes = 1ll << 30;
   data_file_ = opts.data_file ? opts.data_file : "";
   opts_.data_file = nullptr;
   opts_.local_dirs = nullptr;
@@ -97,6 +96,17 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
   fields_ = std::move(fields);
   P_ = P;
   keys_ = std::move(keys);
+  // pass size and segment length: given, else the autotuner's choice for this schema
+  if (opts_.flush_bytes <= 0 || opts_.seg_tiles <= 0) {
+    TuneChoice tc;
+    if (TuneLookup(SchemaSignature(fields_, keys_, P_), &tc)) {
+      if (opts_.flush_bytes <= 0) opts_.flush_bytes = tc.flush_bytes;
+      if (opts_.seg_tiles <= 0) opts_.seg_tiles = tc.seg_tiles;
+    }
+  }
+  if (opts_.flush_bytes <= 0) opts_.flush_bytes = 512ll << 20;
+  if (opts_.flush_bytes > (1ll << 30)) opts_.flush_bytes = 1ll << 30;
+  if (opts_.seg_tiles > kMaxSegTiles) opts_.seg_tiles = kMaxSegTiles;
 
   // Splitter::Init column classification (splitter.cc:246-269)
   std::vector<int32_t> bin;
@@ -153,6 +163,7 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
   // bytes of every partition in shared memory (it then records each tile's prefix).  Its work
   // grows with segments x partitions, so segments are longer for more partitions.
   if ((size_t)(1 + n_str_) * P_ * 4 > kHistSmemBytes) seg_tiles_ = 1;
+  else if (opts_.seg_tiles > 0) seg_tiles_ = (uint32_t)opts_.seg_tiles;
   else seg_tiles_ = (uint32_t)std::min<int64_t>(kMaxSegTiles, std::max<int64_t>(4, P_ / 256));
   // hash chain (HashSplitter::CreateProjector, splitter.cc:1402-1438)
   for (size_t k = 0; k < keys_.size(); k++) {

@@ -51,7 +51,7 @@ class GzSplitOptions(ctypes.Structure):
         ("data_file", ctypes.c_char_p),
         ("local_dirs", ctypes.c_char_p),
         ("host_read", ctypes.c_int32),
-        ("reserved0", ctypes.c_int32),
+        ("seg_tiles", ctypes.c_int32),
     ]
 
 
@@ -145,6 +145,15 @@ def lib() -> ctypes.CDLL:
         L.gz_pinned_reserve.argtypes = [ctypes.c_int64, c_i64p]
         L.gz_serve_shutdown.restype = ctypes.c_int
         L.gz_serve_shutdown.argtypes = [ctypes.c_int64]
+        L.gz_autotune.restype = ctypes.c_int
+        L.gz_autotune.argtypes = [ctypes.c_char_p, ctypes.c_int32, ctypes.POINTER(GzField), ctypes.c_int32,
+                                  ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(GzSplitOptions),
+                                  ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                  ctypes.c_int32, ctypes.POINTER(GzTuneResult)]
+        L.gz_tune_save.restype = ctypes.c_int
+        L.gz_tune_save.argtypes = [ctypes.c_char_p]
+        L.gz_tune_load.restype = ctypes.c_int
+        L.gz_tune_load.argtypes = [ctypes.c_char_p]
         _lib = L
     return _lib
 
@@ -341,6 +350,39 @@ def split_batches(schema, batches, num_partitions: int, key_cols: Sequence[int],
     finally:
         w.close(h)
     return res, data
+
+
+class GzTuneResult(ctypes.Structure):
+    _fields_ = [("flush_bytes", ctypes.c_int64), ("seg_tiles", ctypes.c_int32), ("runs", ctypes.c_int32),
+                ("best_gbs", ctypes.c_double), ("default_gbs", ctypes.c_double)]
+
+
+def autotune(schema, num_partitions: int, key_cols: Sequence[int], batches, **make_kwargs) -> dict:
+    """gz_autotune over sample batches (workloads.Batch, host memory unless input_kind says
+    otherwise): times candidate pass sizes and segment lengths and caches the fastest for this
+    schema, key columns and partition count; splitters made afterwards with flush_bytes=0 and
+    seg_tiles=0 use it.  Returns the choice and the sample throughputs."""
+    o, keep = split_options(**make_kwargs)
+    arr, names = _fields(schema)
+    keys = np.ascontiguousarray(key_cols, dtype=np.int32)
+    rows = np.ascontiguousarray([b.num_rows for b in batches], dtype=np.int32)
+    pairs = [b.addrs_sizes() for b in batches]
+    addrs = np.ascontiguousarray(np.stack([a for a, _ in pairs]), dtype=np.int64)
+    sizes = np.ascontiguousarray(np.stack([z for _, z in pairs]), dtype=np.int64)
+    r = GzTuneResult()
+    _check(lib().gz_autotune(b"hash", num_partitions, arr, len(schema), keys.ctypes.data, len(keys),
+                             ctypes.byref(o), len(batches), rows.ctypes.data, addrs.ctypes.data,
+                             sizes.ctypes.data, addrs.shape[1], ctypes.byref(r)), 0)
+    return {"flush_bytes": r.flush_bytes, "seg_tiles": r.seg_tiles, "runs": r.runs,
+            "best_gbs": r.best_gbs, "default_gbs": r.default_gbs}
+
+
+def tune_save(path: str) -> None:
+    _check(lib().gz_tune_save(path.encode()), 0)
+
+
+def tune_load(path: str) -> None:
+    _check(lib().gz_tune_load(path.encode()), 0)
 
 
 def pinned_reserve(nbytes: int) -> int:

@@ -84,14 +84,17 @@ typedef struct GzSplitOptions {
                                         or until device_budget is exceeded; 0: every flush is
                                         copied to pinned host memory as soon as it is done */
   int64_t flush_bytes;               /* input bytes gathered before one device pass
-                                        (default 512 MiB, at most 1 GiB) */
+                                        (default 512 MiB, at most 1 GiB; 0: the choice
+                                        gz_autotune cached for this schema, else 512 MiB) */
   int64_t device_budget;             /* HBM bytes for resident partition data before it is
                                         moved to pinned host memory (default 64 GiB) */
   const char* data_file;             /* written at Stop; NULL/"" keeps the bytes in memory */
   const char* local_dirs;            /* comma separated spill dirs (unused: spills go to
                                         pinned host memory) */
   int32_t host_read;                 /* GzHostRead, default GZ_HOST_READ_AUTO */
-  int32_t reserved0;
+  int32_t seg_tiles;                 /* 1024-row tiles per k_hash_count segment, 1..32;
+                                        0 (default): the gz_autotune choice for this schema,
+                                        else 4..32 growing with num_partitions */
 } GzSplitOptions;
 
 /* SplitResult (native-sql-engine/core/src/main/java/com/intel/oap/vectorized/SplitResult.java:21-39).
@@ -181,6 +184,31 @@ GzStatus gz_split_kernel_times(int64_t handle, double* out4);
  * HBM, [5] batches split, [6] rows split, [7] emitted record batches (after Stop, else -1).
  * No reference counterpart. */
 GzStatus gz_split_stats(int64_t handle, int64_t* out8);
+
+/* ---- Autotuner (no reference counterpart) ---------------------------------------------
+ * The device pass has two run-time knobs: flush_bytes (its size) and seg_tiles (the segment
+ * length of k_hash_count and the plan).  gz_autotune splits the sample batches with candidate
+ * settings (opts otherwise as given; each candidate once to warm up, once timed from the first
+ * Split to the end of the device work) and caches the fastest under the schema's signature
+ * (field types, key columns, num_partitions).  Splitters made later in the process with
+ * flush_bytes 0 / seg_tiles 0 take the cached choice.  gz_tune_save / gz_tune_load write / merge
+ * the cache as a text file; $GZ_TUNE_CACHE, when set, is loaded on first use.  Tile size, rows
+ * per warp and staging depth of k_scatter are compile-time constants, not tuned. */
+typedef struct GzTuneResult {
+  int64_t flush_bytes;  /* chosen pass size */
+  int32_t seg_tiles;    /* chosen segment length */
+  int32_t runs;         /* timed candidate runs */
+  double best_gbs;      /* sample input GB/s at the chosen settings */
+  double default_gbs;   /* sample input GB/s at 512 MiB passes and automatic segments */
+} GzTuneResult;
+
+GzStatus gz_autotune(const char* short_name, int32_t num_partitions, const GzField* fields,
+                     int32_t n_fields, const int32_t* key_cols, int32_t n_keys,
+                     const GzSplitOptions* opts, int32_t n_batches, const int32_t* rows,
+                     const int64_t* buf_addrs, const int64_t* buf_sizes, int32_t n_bufs,
+                     GzTuneResult* out);
+GzStatus gz_tune_save(const char* path);
+GzStatus gz_tune_load(const char* path);
 
 /* ---- served form (no reference counterpart) --------------------------------------------
  * Split / Stop calls of many concurrent tasks, each an ordinary splitter with its own schema,
