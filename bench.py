@@ -14,6 +14,9 @@ Lines:
   e2e   : the same through the host-buffer contract (GZ_INPUT_HOST: each batch copied before
           Split returns), partition data copied back to pinned host memory after every pass.
   metric: (input buffer bytes + raw partition bytes) / time, in GB/s.
+  forms : batched (512 uneven batches of 3 schemas, autotuned passes), served (32 tasks through
+          the serving loop, per-Split latency) and fanout (Zipf keys, 16..8000 partitions), each
+          beside its plain per-batch counterpart where it has one; --no-forms skips them.
 
 --impl reference times the CPU splitter (the oracle's restatement of the reference
 Splitter; the reference itself needs the Arrow fork and x86) on all host cores, one splitter
@@ -410,6 +413,49 @@ def run_batched(seed: int = 3, n_batches: int = 512, window: int = 64, tune_batc
             "plain_gbs": alg / dt_p / 1e9, "batched_gbs": alg / dt_b / 1e9, "speedup": dt_p / dt_b}
 
 
+def run_fanout(distinct: int = 256, reps: int = 12, rows: int = 32768):
+    """Config 3 (skew and fan-out): Zipf(1.1) int64 key over 1e7 values, 2x int64 + float64 +
+    utf8 0-64 payload, 0% and 20% nulls, P in {16, 200, 2000, 8000}; ~100M rows = `distinct`
+    seeded 32768-row batches resident in HBM, split `reps` times over.  Per (nulls, P): one
+    warm-up split (stopped, for the partition bytes), then one timed split through
+    gz_split_split_batches until its device work is done."""
+    import torch
+    from gazelle_plugin_gb300 import shuffle as S
+    from gazelle_plugin_gb300 import workloads as W
+    out = []
+    w = S.ShuffleSplitterJniWrapper()
+    for nullf in (0.0, 0.2):
+        batches = W.c3_batches(2, distinct, rows, nullf, 0.0)
+        dev = [[torch.from_numpy(x.view(np.uint8).copy()).cuda() if x.nbytes else None for x in b.buffers]
+               for b in batches]
+        a1 = np.array([[t.data_ptr() if t is not None else 0 for t in ts] for ts in dev], np.int64)
+        z1 = np.array([[x.nbytes for x in b.buffers] for b in batches], np.int64)
+        addrs, sizes = np.tile(a1, (reps, 1)), np.tile(z1, (reps, 1))
+        nrows = np.full(distinct * reps, rows, np.int32)
+        in_bytes = int(sizes.sum())
+        for P in (16, 200, 2000, 8000):
+            part = S.NativePartitioning("hash", P, None, W.C3_KEYS, list(W.C3_SCHEMA))
+            opts = dict(writeSchema=False, dataFile="/dev/null", input_kind=S.GZ_INPUT_DEVICE_RETAINED,
+                        flush_bytes=1 << 30)
+            h = w.make(part, **opts)
+            w.splitBatches(h, nrows, addrs, sizes)
+            part_bytes = int(w.stop(h, P).rawPartitionLengths.sum())
+            w.close(h)
+            h = w.make(part, **opts)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            w.splitBatches(h, nrows, addrs, sizes)
+            w.sync(h)
+            dt = time.perf_counter() - t0
+            w.close(h)
+            out.append({"nulls": nullf, "P": P, "gbs": round((in_bytes + part_bytes) / dt / 1e9, 1),
+                        "ms": round(dt * 1e3, 2)})
+        del dev
+    return {"workload": (f"Zipf(1.1) int64 key over 1e7 values + 2x int64 + float64 + utf8 0-64, "
+                         f"{distinct * reps * rows} rows ({distinct} distinct 32768-row batches x {reps}), "
+                         f"resident in HBM"), "splits": out}
+
+
 def _served_stream(seed: int, n_tasks: int, rate: float, gb_per_task: float):
     """Config 5 call stream: Poisson arrivals (`rate` Split calls/s in total), each to a random
     task still below its input quota; returns (task specs, [(t, task, si, rows)])."""
@@ -695,6 +741,7 @@ def run_gpu(args):
         if not args.no_forms:
             line["batched"] = run_batched()
             line["served"] = run_served(gb_per_task=args.served_gb_per_task)
+            line["fanout"] = run_fanout()
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
