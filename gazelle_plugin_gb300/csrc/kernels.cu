@@ -699,8 +699,9 @@ __device__ __forceinline__ void store_word_part(uint8_t* p, uint32_t w, uint32_t
 }
 
 // One string whose source bytes are in shared memory (shared address `src`): `len` bytes to
-// global `dst`, written in the aligned 4-byte words of the destination, whole words in 8-byte
-// aligned pairs where they can be.  Every destination word is a funnel shift of two aligned
+// global `dst`, written in the aligned 4-byte words of the destination: whole words as 16-byte
+// stores of four, with a word and / or an 8-byte pair before them up to that alignment and after
+// them for the rest.  Every destination word is a funnel shift of two aligned
 // source words (one shift for the whole string), loaded as a stream; the first and last words,
 // when the string covers them only in part, are stored as a byte and / or a halfword.  The aligned source words may reach 6 bytes before `src` and 7 past
 // `src + len`: the staging buffer keeps that slack, and those bytes are never stored.
@@ -726,17 +727,24 @@ __device__ __forceinline__ void copy_string_smem(uint8_t* dst, uint32_t src, uin
   uint32_t* dw = reinterpret_cast<uint32_t*>(X);
   const uint32_t nw = rem >> 2;
   uint32_t k = 0;
-  if (nw && (reinterpret_cast<uintptr_t>(dw) & 4)) {  // one word, then 8-byte aligned pairs
-    const uint32_t hi = lds32(sb + 4);
-    dw[0] = __funnelshift_r(lo, hi, sh);
+  // up to 16-byte alignment: a word, then a pair
+  if (nw > k && (reinterpret_cast<uintptr_t>(dw + k) & 4)) {
+    const uint32_t hi = lds32(sb + 4 * k + 4);
+    dw[k] = __funnelshift_r(lo, hi, sh);
     lo = hi;
-    k = 1;
+    k += 1;
   }
-  for (; k + 4 <= nw; k += 4) {  // four source words loaded before any store
+  if (nw >= k + 2 && (reinterpret_cast<uintptr_t>(dw + k) & 8)) {
+    const uint32_t w1 = lds32(sb + 4 * k + 4), w2 = lds32(sb + 4 * k + 8);
+    *reinterpret_cast<uint2*>(dw + k) = make_uint2(__funnelshift_r(lo, w1, sh), __funnelshift_r(w1, w2, sh));
+    lo = w2;
+    k += 2;
+  }
+  for (; k + 4 <= nw; k += 4) {  // four source words loaded before one 16-byte store
     const uint32_t w1 = lds32(sb + 4 * k + 4), w2 = lds32(sb + 4 * k + 8);
     const uint32_t w3 = lds32(sb + 4 * k + 12), w4 = lds32(sb + 4 * k + 16);
-    *reinterpret_cast<uint2*>(dw + k) = make_uint2(__funnelshift_r(lo, w1, sh), __funnelshift_r(w1, w2, sh));
-    *reinterpret_cast<uint2*>(dw + k + 2) = make_uint2(__funnelshift_r(w2, w3, sh), __funnelshift_r(w3, w4, sh));
+    *reinterpret_cast<uint4*>(dw + k) = make_uint4(__funnelshift_r(lo, w1, sh), __funnelshift_r(w1, w2, sh),
+                                                   __funnelshift_r(w2, w3, sh), __funnelshift_r(w3, w4, sh));
     lo = w4;
   }
   if (k + 2 <= nw) {
