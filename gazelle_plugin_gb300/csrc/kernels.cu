@@ -143,16 +143,21 @@ __global__ void __launch_bounds__(kHashThreads) k_hash_count(const SchemaDesc sd
     __syncthreads();  // the copies are read before the next tile's rows are added
   }
   const uint32_t t1 = min(tile.nrows, t0 + (uint32_t)kTileRows);
-  // rows t0 + threadIdx.x + u * kHashThreads, u < kHashRows: each key / offset column is loaded
-  // for all of them before any is used, so a thread has kHashRows loads in flight
+  // rows i0 .. i0 + 3 (i0 = t0 + 4 * thread) of the tile: a whole group is loaded with 16-byte
+  // vector loads when the column's buffer is 16-byte aligned (the group's first row is a
+  // multiple of 4, so then every group is), otherwise and for the tile's last partial group row
+  // by row; all loads of a column are issued before any is used
+  const uint32_t i0 = t0 + kHashRows * threadIdx.x;
+  const uint32_t m = i0 < t1 ? min((uint32_t)kHashRows, t1 - i0) : 0u;  // rows of this thread
+  const uint32_t r0 = tile.row0 + (m ? i0 : t1 - 1);  // a thread without rows reads a valid one
+  const bool whole = m == kHashRows;
   bool act[kHashRows];
   uint32_t rr[kHashRows];
   int32_t h[kHashRows];
 #pragma unroll
   for (int u = 0; u < kHashRows; u++) {
-    const uint32_t i = t0 + threadIdx.x + u * kHashThreads;
-    act[u] = i < t1;
-    rr[u] = tile.row0 + (act[u] ? i : t0);
+    act[u] = u < m;
+    rr[u] = act[u] ? r0 + u : r0;
     h[u] = 42;
   }
   for (int k = 0; k < nkeys; k++) {
@@ -160,20 +165,37 @@ __global__ void __launch_bounds__(kHashThreads) k_hash_count(const SchemaDesc sd
     const int kind = s_kind[k];
     int64_t v[kHashRows];
     bool valid[kHashRows];
+    const bool aligned16 = (reinterpret_cast<uintptr_t>(c.values) & 15) == 0;
+    if (whole && aligned16 && kind == KEY_I64) {
+      const longlong2 a0 = reinterpret_cast<const longlong2*>(c.values)[r0 >> 1];
+      const longlong2 a1 = reinterpret_cast<const longlong2*>(c.values)[(r0 >> 1) + 1];
+      v[0] = a0.x;
+      v[1] = a0.y;
+      v[2] = a1.x;
+      v[3] = a1.y;
+    } else if (whole && aligned16 && kind == KEY_I32) {
+      const int4 a0 = reinterpret_cast<const int4*>(c.values)[r0 >> 2];
+      v[0] = a0.x;
+      v[1] = a0.y;
+      v[2] = a0.z;
+      v[3] = a0.w;
+    } else {
 #pragma unroll
-    for (int u = 0; u < kHashRows; u++) {
-      const uint32_t r = rr[u];
-      valid[u] = c.validity == nullptr || get_bit(c.validity, r);  // null: seed passes
-      switch (kind) {
-        case KEY_I32: v[u] = reinterpret_cast<const int32_t*>(c.values)[r]; break;
-        case KEY_I64: v[u] = reinterpret_cast<const int64_t*>(c.values)[r]; break;
-        case KEY_I8: v[u] = reinterpret_cast<const int8_t*>(c.values)[r]; break;
-        case KEY_I16: v[u] = reinterpret_cast<const int16_t*>(c.values)[r]; break;
-        default: v[u] = get_bit(c.values, r) ? 1 : 0; break;
+      for (int u = 0; u < kHashRows; u++) {
+        const uint32_t r = rr[u];
+        switch (kind) {
+          case KEY_I32: v[u] = reinterpret_cast<const int32_t*>(c.values)[r]; break;
+          case KEY_I64: v[u] = reinterpret_cast<const int64_t*>(c.values)[r]; break;
+          case KEY_I8: v[u] = reinterpret_cast<const int8_t*>(c.values)[r]; break;
+          case KEY_I16: v[u] = reinterpret_cast<const int16_t*>(c.values)[r]; break;
+          default: v[u] = get_bit(c.values, r) ? 1 : 0; break;
+        }
       }
     }
 #pragma unroll
-    for (int u = 0; u < kHashRows; u++)
+    for (int u = 0; u < kHashRows; u++) valid[u] = c.validity == nullptr || get_bit(c.validity, rr[u]);
+#pragma unroll
+    for (int u = 0; u < kHashRows; u++)  // null: seed passes
       if (valid[u]) h[u] = kind == KEY_I64 ? hash_long(v[u], h[u]) : hash_int((int32_t)v[u], h[u]);
   }
   uint32_t p[kHashRows];
@@ -181,22 +203,29 @@ __global__ void __launch_bounds__(kHashThreads) k_hash_count(const SchemaDesc sd
   for (int u = 0; u < kHashRows; u++) {
     p[u] = fast_pmod(h[u], (uint32_t)P, M);
     if (act[u]) {
-      fd.pids[tile.frow0 + t0 + threadIdx.x + u * kHashThreads] = (uint16_t)p[u];
+      fd.pids[tile.frow0 + i0 + u] = (uint16_t)p[u];
       atomicAdd(&H[p[u]], 1u);
     }
   }
   for (int k = 0; k < nstr; k++) {
     const ColPtr c = s_str[k];
-    int32_t o0[kHashRows], o1[kHashRows];
+    // o[u] = offsets[r0 + min(u, m)]: row u < m spans o[u] .. o[u + 1]
+    int32_t o[kHashRows + 1];
+    if (whole && (reinterpret_cast<uintptr_t>(c.offsets) & 15) == 0) {
+      const int4 a0 = reinterpret_cast<const int4*>(c.offsets)[r0 >> 2];
+      o[0] = a0.x;
+      o[1] = a0.y;
+      o[2] = a0.z;
+      o[3] = a0.w;
+      o[4] = c.offsets[r0 + kHashRows];
+    } else {
 #pragma unroll
-    for (int u = 0; u < kHashRows; u++) {
-      o0[u] = c.offsets[rr[u]];
-      o1[u] = c.offsets[rr[u] + 1];
+      for (int u = 0; u <= kHashRows; u++) o[u] = c.offsets[r0 + min((uint32_t)u, m)];
     }
 #pragma unroll
     for (int u = 0; u < kHashRows; u++) {
-      uint32_t len = (uint32_t)(o1[u] - o0[u]);
-      if (o0[u] < 0 || o1[u] < o0[u] || (uint64_t)o1[u] > c.values_bytes) {
+      uint32_t len = (uint32_t)(o[u + 1] - o[u]);
+      if (act[u] && (o[u] < 0 || o[u + 1] < o[u] || (uint64_t)o[u + 1] > c.values_bytes)) {
         bad = true;
         len = 0;
       }
@@ -212,21 +241,34 @@ __global__ void __launch_bounds__(kHashThreads) k_hash_count(const SchemaDesc sd
   }
   if (bad) atomicOr(fd.err, kErrBadOffsets);  // k_scatter then copies nothing
 
-  // null counts of this segment's slice of every column (GetNullCount of the batch = sum)
-  for (int a = 0; a < sd.n_array; a++) {
-    const uint8_t* validity = cols[sd.arr_col[a]].validity;
-    if (validity == nullptr) continue;
-    uint32_t z = 0;
+  // null counts of this segment's slice of every column (GetNullCount of the batch = sum): one
+  // warp per column, 32 rows per 4-byte word when the slice is word aligned, else byte by byte
+  {
+    const int lane = (int)lane_id();
+    const int nwarps = (int)(blockDim.x >> 5);
     const uint32_t nbytes = (tile.nrows + 7) >> 3;
-    const uint8_t* vb = validity + (tile.row0 >> 3);
-    for (uint32_t j = threadIdx.x; j < nbytes; j += blockDim.x) {
-      const uint32_t byte = vb[j];
-      const uint32_t rem = tile.nrows - j * 8;
-      const uint32_t mask = rem >= 8 ? 0xffu : ((1u << rem) - 1);
-      z += __popc(~byte & mask);
+    for (int a = (int)(threadIdx.x >> 5); a < sd.n_array; a += nwarps) {
+      const uint8_t* validity = cols[sd.arr_col[a]].validity;
+      if (validity == nullptr) continue;
+      const uint8_t* vb = validity + (tile.row0 >> 3);
+      uint32_t z = 0;
+      uint32_t j0 = 0;  // first byte left to the byte loop
+      if ((reinterpret_cast<uintptr_t>(vb) & 3) == 0) {
+        const uint32_t nw = nbytes >> 2;
+        const uint32_t* vw = reinterpret_cast<const uint32_t*>(vb);
+        for (uint32_t q = lane; q < nw; q += 32) {
+          const uint32_t rem = tile.nrows - q * 32;
+          z += __popc(~vw[q] & (rem >= 32 ? 0xffffffffu : ((1u << rem) - 1)));
+        }
+        j0 = nw << 2;
+      }
+      for (uint32_t j = j0 + lane; j < nbytes; j += 32) {
+        const uint32_t rem = tile.nrows - j * 8;
+        z += __popc(~(uint32_t)vb[j] & (rem >= 8 ? 0xffu : ((1u << rem) - 1)));
+      }
+      for (int o = 16; o; o >>= 1) z += __shfl_xor_sync(kFull, z, o);
+      if (lane == 0 && z) atomicAdd(&fd.nullcnt[(size_t)tile.batch * sd.n_array + a], z);
     }
-    for (int o = 16; o; o >>= 1) z += __shfl_xor_sync(kFull, z, o);
-    if (lane_id() == 0 && z) atomicAdd(&fd.nullcnt[(size_t)tile.batch * sd.n_array + a], z);
   }
 
   if (fd.hist_in_smem) {
