@@ -1149,18 +1149,19 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
         }
         csync();
         {
-          uint32_t before = 0;  // all positions of earlier rows, then earlier warps of this row
+          // the warp totals in (row, warp) order, one per lane: their exclusive scan is what all
+          // earlier rows and this row's earlier warps hold (every warp scans them itself)
+          static_assert(kRowsPerThread * kW == 32, "one warp total per lane");
+          const uint32_t sv = scratch[lane_id()];
+          uint32_t incl = sv;
 #pragma unroll
-          for (int u = 0; u < kRowsPerThread; u++) {
-            uint32_t row_total = 0, warps_before = 0;
-            for (int q = 0; q < kW; q++) {
-              const uint32_t t = scratch[u * kW + q];
-              row_total += t;
-              if (q < w) warps_before += t;
-            }
-            pre[u] = before + warps_before + pre[u] - len[u];
-            before += row_total;
+          for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(kFull, incl, o);
+            if ((int)lane_id() >= o) incl += y;
           }
+          const uint32_t excl = incl - sv;
+#pragma unroll
+          for (int u = 0; u < kRowsPerThread; u++) pre[u] = __shfl_sync(kFull, excl, u * kW + w) + pre[u] - len[u];
         }
         // run tables at the run starts: destination of the run's first string and its offset
         // inside the partition's segment, both relative to the tile prefix
