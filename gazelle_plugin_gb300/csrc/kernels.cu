@@ -1123,14 +1123,16 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
         const int32_t* oin = reinterpret_cast<const int32_t*>(stg);  // offsets of rows row0..row0+n
         // lengths of the owned positions; exclusive prefix over the tile = the lengths of all
         // earlier rows u' < u of positions + this row's prefix, one fused warp scan per row u
-        uint32_t len[kRowsPerThread], pre[kRowsPerThread];
+        uint32_t len[kRowsPerThread], pre[kRowsPerThread], so[kRowsPerThread];  // so: source offset
 #pragma unroll
         for (int u = 0; u < kRowsPerThread; u++) {
           const int j = threadIdx.x + u * kConsumers;
           len[u] = 0;
+          so[u] = 0;
           if (j < n) {
             const int r = ps[j];
-            len[u] = (uint32_t)(oin[r + 1] - oin[r]);
+            so[u] = (uint32_t)oin[r];
+            len[u] = (uint32_t)oin[r + 1] - so[u];
           }
           pre[u] = len[u];
         }
@@ -1179,14 +1181,17 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
         csync();
         int32_t* ooff = reinterpret_cast<int32_t*>(fd.out_values[a]);
         uint8_t* ochars = fd.out_chars[a];
+        uint32_t cd[kRowsPerThread];  // destination of each string in the column's characters
         {
           uint32_t d[kRowsPerThread], v[kRowsPerThread];
 #pragma unroll
           for (int u = 0; u < kRowsPerThread; u++) {
             const int j = threadIdx.x + u * kConsumers;
             if (j < n) {
+              const int q = rs[j];
               d[u] = dstrow[j];
-              v[u] = rt0[rs[j]] + pre[u] + len[u];
+              v[u] = rt0[q] + pre[u] + len[u];
+              cd[u] = rt1[q] + pre[u];
             }
           }
 #pragma unroll
@@ -1200,7 +1205,7 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
 #pragma unroll
           for (int u = 0; u < kRowsPerThread; u++) {
             const int j = threadIdx.x + u * kConsumers;
-            if (j < n) copy_string_smem(ochars + rt1[rs[j]] + pre[u], cbase + (uint32_t)oin[ps[j]], len[u]);
+            if (j < n) copy_string_smem(ochars + cd[u], cbase + so[u], len[u]);
           }
         } else {
           const uintptr_t buf_lo = reinterpret_cast<uintptr_t>(c.values);
@@ -1208,7 +1213,7 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
 #pragma unroll
           for (int u = 0; u < kRowsPerThread; u++) {
             const int j = threadIdx.x + u * kConsumers;
-            if (j < n) copy_string(ochars + rt1[rs[j]] + pre[u], c.values + oin[ps[j]], len[u], buf_lo, buf_hi);
+            if (j < n) copy_string(ochars + cd[u], c.values + so[u], len[u], buf_lo, buf_hi);
           }
         }
       }
