@@ -556,7 +556,9 @@ constexpr uint32_t kSpinLimit = 1u << 26;
 // Barrier of the scattering threads (the issuing warp never joins it).
 __device__ __forceinline__ void csync() { group_sync<kConsumers, 1>(); }
 
-// One stable LSD pass over 8 bits of the keys.
+// One stable LSD pass over 8 bits of the keys.  Warp w takes positions [w * seg, (w + 1) * seg);
+// its keys, payloads and match masks stay in registers between the counting and the scatter.
+constexpr int kSortIters = kTileRows / (kW * 32);  // 32-row groups per warp
 __device__ void radix_pass(const uint16_t* kin, const uint16_t* pin, uint16_t* kout,
                            uint16_t* pout, int n, int shift, uint16_t* wcnt, uint32_t* off,
                            uint32_t* scratch) {
@@ -564,14 +566,23 @@ __device__ void radix_pass(const uint16_t* kin, const uint16_t* pin, uint16_t* k
   const int seg = ((n + kW * 32 - 1) / (kW * 32)) * 32;
   for (int i = threadIdx.x; i < kW * 256; i += kConsumers) wcnt[i] = 0;
   csync();
-  for (int c = 0; c < seg; c += 32) {
+  uint16_t kv[kSortIters], pv[kSortIters];
+  unsigned pe[kSortIters];
+#pragma unroll
+  for (int it = 0; it < kSortIters; it++) {
+    const int c = it * 32;
     const int i = w * seg + c + lane_id();
-    const bool act = i < n;
+    const bool act = c < seg && i < n;
     const unsigned m = __ballot_sync(kFull, act);
+    kv[it] = 0;
+    pv[it] = 0;
+    pe[it] = 0;
     if (act) {
-      const unsigned d = (kin[i] >> shift) & 255u;
-      const unsigned peers = __match_any_sync(m, d);
-      if ((int)lane_id() == __ffs(peers) - 1) wcnt[w * 256 + d] += (uint16_t)__popc(peers);
+      kv[it] = kin[i];
+      pv[it] = pin[i];
+      const unsigned d = (kv[it] >> shift) & 255u;
+      pe[it] = __match_any_sync(m, d);
+      if ((int)lane_id() == __ffs(pe[it]) - 1) wcnt[w * 256 + d] += (uint16_t)__popc(pe[it]);
     }
     __syncwarp();
   }
@@ -582,21 +593,19 @@ __device__ void radix_pass(const uint16_t* kin, const uint16_t* pin, uint16_t* k
   }
   csync();
   block_exscan<kConsumers, 1>(off, kW * 256, scratch);
-  for (int c = 0; c < seg; c += 32) {
-    const int i = w * seg + c + lane_id();
-    const bool act = i < n;
-    const unsigned m = __ballot_sync(kFull, act);
-    unsigned d = 0, peers = 0;
+#pragma unroll
+  for (int it = 0; it < kSortIters; it++) {
+    const int c = it * 32;
+    const bool act = c < seg && w * seg + c + (int)lane_id() < n;
+    const unsigned d = (kv[it] >> shift) & 255u;
     if (act) {
-      d = (kin[i] >> shift) & 255u;
-      peers = __match_any_sync(m, d);
-      const unsigned rank = __popc(peers & ((1u << lane_id()) - 1));
+      const unsigned rank = __popc(pe[it] & ((1u << lane_id()) - 1));
       const uint32_t pos = off[d * kW + w] + rank;
-      kout[pos] = kin[i];
-      pout[pos] = pin[i];
+      kout[pos] = kv[it];
+      pout[pos] = pv[it];
     }
     __syncwarp();
-    if (act && (int)lane_id() == __ffs(peers) - 1) off[d * kW + w] += __popc(peers);
+    if (act && (int)lane_id() == __ffs(pe[it]) - 1) off[d * kW + w] += __popc(pe[it]);
     __syncwarp();
   }
   csync();
