@@ -201,28 +201,22 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
   Status st = Cuda(cudaSetDevice(device_), "cudaSetDevice");
   if (!st.ok()) return st;
   {
-    // host reads, then k_hash_count and the plan, get the higher priorities: their CTAs are
-    // scheduled ahead of the remaining CTAs of a running k_scatter
+    // host reads, then the plan kernels, get the higher priorities: their few CTAs are
+    // scheduled ahead of the remaining CTAs of a running k_hash_count / k_scatter
     int least = 0, greatest = 0;
     cudaDeviceGetStreamPriorityRange(&least, &greatest);
     st = Cuda(cudaStreamCreateWithPriority(&cstream_, cudaStreamNonBlocking, greatest), "cudaStreamCreate");
     if (!st.ok()) return st;
-    st = Cuda(cudaStreamCreateWithPriority(&stream_, cudaStreamNonBlocking, std::min(greatest + 1, least)),
+    st = Cuda(cudaStreamCreateWithPriority(&pstream_, cudaStreamNonBlocking, std::min(greatest + 1, least)),
               "cudaStreamCreate");
     if (!st.ok()) return st;
-    st = Cuda(cudaStreamCreateWithPriority(&sstream_, cudaStreamNonBlocking, least), "cudaStreamCreate");
+    st = Cuda(cudaStreamCreateWithPriority(&stream_, cudaStreamNonBlocking, least), "cudaStreamCreate");
     if (!st.ok()) return st;
   }
   st = Cuda(cudaStreamCreateWithFlags(&ostream_, cudaStreamNonBlocking), "cudaStreamCreate");
   if (!st.ok()) return st;
   st = Cuda(cudaEventCreateWithFlags(&gather_ev_, cudaEventDisableTiming), "cudaEventCreate");
   if (!st.ok()) return st;
-  st = Cuda(cudaEventCreateWithFlags(&plan_ev_, cudaEventDisableTiming), "cudaEventCreate");
-  if (!st.ok()) return st;
-  for (int i = 0; i < 2; i++) {
-    st = Cuda(cudaEventCreateWithFlags(&scr_ev_[i], cudaEventDisableTiming), "cudaEventCreate");
-    if (!st.ok()) return st;
-  }
   if (opts_.input_kind == GZ_INPUT_HOST && opts_.host_read == GZ_HOST_READ_AUTO) {
     // kernels may dereference any host address when the device walks the host page tables
     // (a coherent CPU-GPU link): host inputs are then read by k_gather, no CPU copy
@@ -283,7 +277,7 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
 Splitter::~Splitter() {
   if (cstream_) cudaStreamSynchronize(cstream_);
   if (stream_) cudaStreamSynchronize(stream_);
-  if (sstream_) cudaStreamSynchronize(sstream_);
+  if (pstream_) cudaStreamSynchronize(pstream_);
   if (ostream_) cudaStreamSynchronize(ostream_);
   for (auto& f : flushes_) {
     if (f.d_out) cudaFreeAsync(f.d_out, stream_);
@@ -303,13 +297,11 @@ Splitter::~Splitter() {
   }
   for (int i = 0; i < 2; i++) {
     if (d_scratch_[i]) cudaFreeAsync(d_scratch_[i], stream_);
-    if (scr_ev_[i]) cudaEventDestroy(scr_ev_[i]);
   }
   if (d_state_) cudaFreeAsync(d_state_, stream_);
   PinnedRelease(PinnedBlock{reinterpret_cast<uint8_t*>(h_jobs_), h_jobs_bytes_});
   if (gather_ev_) cudaEventDestroy(gather_ev_);
-  if (plan_ev_) cudaEventDestroy(plan_ev_);
-  if (sstream_) cudaStreamDestroy(sstream_);
+  if (pstream_) cudaStreamDestroy(pstream_);
   if (cstream_) cudaStreamDestroy(cstream_);
   if (ostream_) cudaStreamDestroy(ostream_);
   if (stream_) cudaStreamDestroy(stream_);
@@ -346,11 +338,14 @@ uint32_t Splitter::SplitBatchSize(int32_t num_rows, const std::vector<const int3
 
 Status Splitter::EnsureStaging(size_t bytes) {
   if (bytes <= stage_cap_) return Status::OK();
-  Status st = FinishHostReads();
+  // the old buffers go: the last pass's k_scatter, which reads them, is queued first
+  Status st = LaunchPendingScatter();
+  if (!st.ok()) return st;
+  st = FinishHostReads();
   if (!st.ok()) return st;
   st = Cuda(cudaStreamSynchronize(stream_), "sync");
   if (!st.ok()) return st;
-  st = Cuda(cudaStreamSynchronize(sstream_), "sync");
+  st = Cuda(cudaStreamSynchronize(pstream_), "sync");
   if (!st.ok()) return st;
   size_t cap = AlignUp(std::max<size_t>(bytes, (size_t)opts_.flush_bytes + (8u << 20)), 1 << 20);
   for (int i = 0; i < 2; i++) {
@@ -508,8 +503,11 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
   const size_t tables_need = AlignUp(sizeof(BatchDesc) * NB1, 256) +
                              2 * AlignUp(sizeof(TileDesc) * (pending_tiles_ + ntiles), 256) +
                              AlignUp(sizeof(ColPtr) * NB1 * C, 256) + 256;
+  // (a batch whose call flag is read back has to be alone in its device pass: the earlier
+  // batches go first, before this one is staged, so each pass reads its own staging buffer)
   if (!pending_.empty() &&
-      (pending_bytes_ + batch_bytes > (uint64_t)opts_.flush_bytes || NB1 > (size_t)kMaxBatchesPerFlush ||
+      (probe_call || pending_bytes_ + batch_bytes > (uint64_t)opts_.flush_bytes ||
+       NB1 > (size_t)kMaxBatchesPerFlush ||
        (host_in && used_ + batch_bytes + (direct_ ? phase_slack : tables_need) > stage_cap_))) {
     st = Flush();
     if (!st.ok()) return st;
@@ -611,19 +609,6 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
       cols[f] = cp;
     }
   }
-  if (probe_call && !pending_.empty()) {
-    // this batch has to be alone in its device pass so its call flag can be read back: move
-    // the earlier batches out first, keeping this batch's column record
-    std::vector<ColPtr> mine(cols, cols + C);
-    std::vector<uint64_t> mine_chars(char_scratch_.begin(), char_scratch_.end());
-    pending_cols_.resize(pending_.size() * C);
-    pending_chars_.resize(pending_.size() * std::max(n_str_, 1));
-    st = Flush();
-    if (!st.ok()) return st;
-    pending_cols_.assign(mine.begin(), mine.end());
-    pending_chars_.assign(std::max(n_str_, 1), 0);
-    for (int k = 0; k < n_str_; k++) pending_chars_[k] = mine_chars[k];
-  }
   pending_bytes_ += batch_bytes;
   pending_tiles_ += ntiles;
   stat_input_bytes_ += (int64_t)batch_bytes;
@@ -634,9 +619,9 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
     st = Flush();
     if (!st.ok()) return st;
     uint32_t called = 0;
-    st = Cuda(cudaMemcpyAsync(&called, d_call_, 4, cudaMemcpyDeviceToHost, stream_), "read call flag");
+    st = Cuda(cudaMemcpyAsync(&called, d_call_, 4, cudaMemcpyDeviceToHost, pstream_), "read call flag");
     if (!st.ok()) return st;
-    st = Cuda(cudaStreamSynchronize(stream_), "sync");
+    st = Cuda(cudaStreamSynchronize(pstream_), "sync");
     if (!st.ok()) return st;
     if (!called) empirical_ = empirical_before;  // nobody recomputed the sizes in this batch
   }
@@ -805,16 +790,11 @@ Status Splitter::Flush() {
   const size_t tb_total = tb_batches + tb_tiles + tb_cols + tb_tdesc;
   const bool staged_tables = host_in && !direct_;  // tables travel with the pinned staging copy
   const size_t s_tab = staged_tables ? 0 : take(tb_total);
-  // this pass's scratch buffer: free once the k_scatter that last read it has finished
-  if (scr_busy_[scr_cur_]) {
-    st = Cuda(cudaStreamWaitEvent(stream_, scr_ev_[scr_cur_], 0), "wait scratch");
-    if (!st.ok()) return st;
-    scr_busy_[scr_cur_] = false;
-  }
+  // this pass's scratch buffer: stream_ already runs this pass's work after the k_scatter that
+  // last read it (queued by the previous Flush)
   st = EnsureScratch(so);
   if (!st.ok()) return st;
   uint8_t* S = d_scratch_[scr_cur_];
-  fr.scratch = scr_cur_;
 
   FlushDesc fd;
   memset(&fd, 0, sizeof(fd));
@@ -942,37 +922,33 @@ Status Splitter::Flush() {
   st = Cuda(launch_hash_count(sd_, fd, stream_), "k_hash_count");
   if (!st.ok()) return st;
   cudaEventRecord(fr.ev[1], stream_);
-  st = Cuda(launch_plan(sd_, fd, stream_), "k_plan");
+  // the plan on pstream_, after this pass's k_hash_count (and the previous pass's plan)
+  st = Cuda(cudaStreamWaitEvent(pstream_, fr.ev[1], 0), "wait k_hash_count");
   if (!st.ok()) return st;
-  cudaEventRecord(fr.ev[2], stream_);
-  // k_scatter on its own stream: the next pass's k_hash_count and plan need not wait for it
-  st = Cuda(cudaEventRecord(plan_ev_, stream_), "event");
+  cudaEventRecord(fr.ev[5], pstream_);
+  st = Cuda(launch_plan(sd_, fd, pstream_), "k_plan");
   if (!st.ok()) return st;
-  st = Cuda(cudaStreamWaitEvent(sstream_, plan_ev_, 0), "wait plan");
-  if (!st.ok()) return st;
-  cudaEventRecord(fr.ev[4], sstream_);
-  st = Cuda(launch_scatter(sd_, fd, sstream_), "k_scatter");
-  if (!st.ok()) return st;
-  cudaEventRecord(fr.ev[3], sstream_);
-  st = Cuda(cudaEventRecord(scr_ev_[scr_cur_], sstream_), "event");
-  if (!st.ok()) return st;
-  scr_busy_[scr_cur_] = true;
-  scr_cur_ ^= 1;
-  if (host_in) {  // the staging (inputs, and tables when staged) is free again after k_scatter
-    st = Cuda(cudaEventRecord(stage_ev_[cur_], sstream_), "event");
-    if (!st.ok()) return st;
-    stage_busy_[cur_] = true;
-  }
+  cudaEventRecord(fr.ev[2], pstream_);
   // the last batch's call flag, for the empirical-size bookkeeping
-  st = Cuda(cudaMemcpyAsync(d_call_, fd.call_flags + (NB - 1), 4, cudaMemcpyDeviceToDevice, stream_), "D2D");
+  st = Cuda(cudaMemcpyAsync(d_call_, fd.call_flags + (NB - 1), 4, cudaMemcpyDeviceToDevice, pstream_), "D2D");
   if (!st.ok()) return st;
-
   // flush metadata to pinned host memory
   fr.meta_words = meta_words;
   st = PinnedMeta(meta_words * 4, &fr.h_meta);
   if (!st.ok()) return st;
-  st = Cuda(cudaMemcpyAsync(fr.h_meta, meta, meta_words * 4, cudaMemcpyDeviceToHost, stream_), "D2H meta");
+  st = Cuda(cudaMemcpyAsync(fr.h_meta, meta, meta_words * 4, cudaMemcpyDeviceToHost, pstream_), "D2H meta");
   if (!st.ok()) return st;
+  cudaEventRecord(fr.ev[6], pstream_);
+  // the previous pass's k_scatter goes behind this k_hash_count; this pass's waits for the next
+  st = LaunchPendingScatter();
+  if (!st.ok()) return st;
+  pend_.valid = true;
+  pend_.fd = fd;
+  pend_.flush = flushes_.size();
+  pend_.stage = cur_;
+  pend_.host_in = host_in;
+  fr.scratch = scr_cur_;
+  scr_cur_ ^= 1;
 
   resident_bytes_ += fr.out_bytes;
   flushes_.push_back(std::move(fr));
@@ -989,12 +965,39 @@ Status Splitter::Flush() {
   const size_t budget = opts_.device_budget > 0 ? (size_t)opts_.device_budget : (64ull << 30);
   for (auto& f : flushes_) {
     if (!(opts_.keep_output_on_device == 0 || resident_bytes_ > budget)) break;
-    if (!f.on_host) {
+    if (!f.on_host && f.launched) {
       st = MoveFlushToHost(f);
       if (!st.ok()) return st;
     }
   }
   return Status::OK();
+}
+
+// Queues the k_scatter of the last flushed pass on stream_, after that pass's plan and metadata
+// copies; the pass's staging is free again once it has run.
+Status Splitter::LaunchPendingScatter() {
+  if (!pend_.valid) return Status::OK();
+  pend_.valid = false;
+  FlushRec& f = flushes_[pend_.flush];
+  Status st = Cuda(cudaStreamWaitEvent(stream_, f.ev[6], 0), "wait plan");
+  if (!st.ok()) return st;
+  cudaEventRecord(f.ev[4], stream_);
+  st = Cuda(launch_scatter(sd_, pend_.fd, stream_), "k_scatter");
+  if (!st.ok()) return st;
+  cudaEventRecord(f.ev[3], stream_);
+  f.launched = true;
+  if (pend_.host_in) {
+    st = Cuda(cudaEventRecord(stage_ev_[pend_.stage], stream_), "event");
+    if (!st.ok()) return st;
+    stage_busy_[pend_.stage] = true;
+  }
+  return Status::OK();
+}
+
+Status Splitter::Drain() {
+  Status st = Flush();
+  if (!st.ok()) return st;
+  return LaunchPendingScatter();
 }
 
 // Copies a flush's outputs into a pinned host block and releases the HBM copy (both stream
@@ -1004,6 +1007,7 @@ Status Splitter::MoveFlushToHost(FlushRec& f) {
   f.h_out = HostAlloc(f.out_bytes);
   if (!f.h_out) return Status::Error(GZ_OOM, "pinned host memory for partition data");
   // on its own stream, after the pass's kernels, so the copy overlaps the next pass
+  if (!f.launched) return Status::Error(GZ_CUDA, "partition data of a pass whose k_scatter is not queued");
   Status st = Cuda(cudaStreamWaitEvent(ostream_, f.ev[3], 0), "wait pass");
   if (!st.ok()) return st;
   st = Cuda(cudaMemcpyAsync(f.h_out, f.d_out, f.out_bytes, cudaMemcpyDeviceToHost, ostream_),
@@ -1023,7 +1027,7 @@ Status Splitter::SyncAndCheck() {
   if (!st.ok()) return st;
   st = Cuda(cudaStreamSynchronize(stream_), "device work");
   if (!st.ok()) return st;
-  st = Cuda(cudaStreamSynchronize(sstream_), "device work");
+  st = Cuda(cudaStreamSynchronize(pstream_), "device work");
   if (!st.ok()) return st;
   st = Cuda(cudaStreamSynchronize(ostream_), "partition data to host");
   if (!st.ok()) return st;
@@ -1034,11 +1038,11 @@ Status Splitter::SyncAndCheck() {
   if (err & kErrBadOffsets)
     return Status::Error(GZ_INVALID, "binary offsets are decreasing or exceed the value buffer");
   if (err) return Status::Error(GZ_CUDA, "device emission list overflow");
-  for (; timed_flushes_ < flushes_.size(); timed_flushes_++) {
+  for (; timed_flushes_ < flushes_.size() && flushes_[timed_flushes_].launched; timed_flushes_++) {
     FlushRec& f = flushes_[timed_flushes_];
     float ms[3] = {0, 0, 0};
     cudaEventElapsedTime(&ms[0], f.ev[0], f.ev[1]);
-    cudaEventElapsedTime(&ms[1], f.ev[1], f.ev[2]);
+    cudaEventElapsedTime(&ms[1], f.ev[5], f.ev[2]);
     cudaEventElapsedTime(&ms[2], f.ev[4], f.ev[3]);
     kernel_ms_[0] += ms[0];
     kernel_ms_[1] += ms[1];
@@ -1236,7 +1240,7 @@ Status Splitter::Stop() {
   if (stopped_) return Status::Error(GZ_INVALID, "splitter already stopped");
   Status st = Cuda(cudaSetDevice(device_), "cudaSetDevice");
   if (!st.ok()) return st;
-  st = Flush();
+  st = Drain();
   if (!st.ok()) return st;
   st = SyncAndCheck();
   if (!st.ok()) return st;
@@ -1352,7 +1356,6 @@ void Splitter::ReleaseStaging() {
     if (d_scratch_[i]) cudaFreeAsync(d_scratch_[i], stream_);
     d_scratch_[i] = nullptr;
     scratch_cap_[i] = 0;
-    scr_busy_[i] = false;
   }
 }
 
@@ -1360,7 +1363,7 @@ Status Splitter::SpillFixedSize(int64_t size, int64_t* actual) {
   *actual = 0;
   if (opts_.prefer_spill) return Status::OK();  // every emitted batch was spilled already
   // cached batches exist only without prefer_spill: make them visible on the host
-  Status st = Flush();
+  Status st = Drain();
   if (!st.ok()) return st;
   st = SyncAndCheck();
   if (!st.ok()) return st;
@@ -1444,7 +1447,7 @@ Status Splitter::CompressedSize(int32_t num_rows, const int64_t* addrs, const in
 }
 
 Status Splitter::LastPids(uint16_t* out, int32_t n) {
-  Status st = Flush();
+  Status st = Drain();
   if (!st.ok()) return st;
   st = SyncAndCheck();
   if (!st.ok()) return st;
@@ -1471,7 +1474,7 @@ void Splitter::Stats(int64_t* o) const {
 Status Splitter::Sync() {
   Status st = Cuda(cudaSetDevice(device_), "cudaSetDevice");
   if (!st.ok()) return st;
-  st = Flush();
+  st = Drain();
   if (!st.ok()) return st;
   return SyncAndCheck();
 }

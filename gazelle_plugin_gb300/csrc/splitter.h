@@ -99,8 +99,10 @@ class Splitter {
     uint32_t* h_meta = nullptr;         // pinned: rows_f, pstart, vstart, bytes_f, cstart, count, emit
     size_t meta_words = 0;
     uint32_t emit_cap = 0;
-    // k_hash_count start, plan start, plan end (stream_), k_scatter end, k_scatter start (sstream_)
-    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    // [0] k_hash_count start, [1] its end, [4] k_scatter start, [3] its end (stream_); [5] plan
+    // start, [2] its end, [6] the end of the pass's work on pstream_ (plan + metadata copies)
+    cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    bool launched = false;              // its k_scatter is queued (ev[3] recorded)
     int scratch = 0;                    // which scratch buffer the pass used
     const uint32_t* rows_f() const { return h_meta; }
     const uint32_t* pstart(int P) const { return h_meta + P; }
@@ -178,16 +180,26 @@ class Splitter {
   unsigned long long* st_ihn_ = nullptr;
   int32_t* d_err_ = nullptr;
   uint32_t* d_call_ = nullptr;
-  // k_scatter runs on sstream_, so a pass's scatter overlaps the next pass's k_hash_count and
-  // plan on stream_; the per-pass scratch is double-buffered, scr_ev_[i] marks the end of the
-  // last scatter that read buffer i
-  cudaStream_t sstream_ = nullptr;
-  cudaEvent_t plan_ev_ = nullptr;
+  // The pass schedule: k_hash_count and k_scatter run one after the other on stream_, the plan
+  // kernels on pstream_.  A pass's k_scatter is queued only when the next pass is (or at a sync),
+  // after that pass's k_hash_count, so the plan of pass i runs beside k_hash_count of pass i + 1
+  // and k_scatter of pass i - 1 instead of delaying stream_.  The per-pass scratch is therefore
+  // double-buffered (scr_cur_: the buffer of the next pass); stream order keeps a buffer's next
+  // k_hash_count behind the k_scatter that last read it.
+  cudaStream_t pstream_ = nullptr;
   uint8_t* d_scratch_[2] = {nullptr, nullptr};
   size_t scratch_cap_[2] = {0, 0};
-  cudaEvent_t scr_ev_[2] = {nullptr, nullptr};
-  bool scr_busy_[2] = {false, false};
   int scr_cur_ = 0;
+  struct PendingScatter {
+    bool valid = false;
+    FlushDesc fd;
+    size_t flush = 0;  // index in flushes_
+    int stage = 0;     // staging buffer the pass reads (host inputs)
+    bool host_in = false;
+  };
+  PendingScatter pend_;
+  Status LaunchPendingScatter();
+  Status Drain();  // Flush, then queue the pending k_scatter
 
   // staging (host inputs): double-buffered device buffers, filled by k_gather (direct_) or
   // by H2D copies of pinned host twins
