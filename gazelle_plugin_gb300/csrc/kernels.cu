@@ -360,17 +360,31 @@ __global__ void __launch_bounds__(kPlanRowsThreads) k_plan_rows(const SchemaDesc
   uint32_t base = fd.st_base[p];
   unsigned long long hv = fd.st_hv[p];
   uint32_t frow = 0, vpos = 0, piece_start = 0;  // flush-local rows; piece_start = frow of the piece
+  // software pipeline over chunks of 32 batches: the next chunk's descriptors are loaded while
+  // this chunk's events are resolved, and its row counts while this chunk's offsets are written
+  BatchDesc bd_n{0, 0, 0, 0};
+  unsigned long long hn_n = 0, ihn_n = 0;
+  uint32_t c_n = 0;
+  if (lane < NB) {
+    bd_n = fd.batches[lane];
+    hn_n = fd.hn[lane];
+    ihn_n = fd.ihn[lane];
+    for (uint32_t t = bd_n.seg0; t < bd_n.seg0 + bd_n.nsegs; t++) c_n += fd.cnt[(size_t)t * P + p];
+  }
   for (int b0 = 0; b0 < NB; b0 += 32) {
     const int b = b0 + lane;
     const bool active = b < NB;
-    BatchDesc bd{0, 0, 0, 0};
-    uint32_t c = 0;
-    unsigned long long hn_l = 0, ihn_l = 0;
-    if (active) {
-      bd = fd.batches[b];
-      for (uint32_t t = bd.seg0; t < bd.seg0 + bd.nsegs; t++) c += fd.cnt[(size_t)t * P + p];
-      hn_l = fd.hn[b];
-      ihn_l = fd.ihn[b];
+    const BatchDesc bd = bd_n;
+    const uint32_t c = c_n;
+    const unsigned long long hn_l = hn_n, ihn_l = ihn_n;
+    const bool next = b + 32 < NB;
+    if (next) {
+      bd_n = fd.batches[b + 32];
+      hn_n = fd.hn[b + 32];
+      ihn_n = fd.ihn[b + 32];
+    } else {
+      bd_n = BatchDesc{0, 0, 0, 0};
+      hn_n = ihn_n = 0;
     }
     const uint32_t X = warp_incl_sum(c);
     const uint32_t Xex = X - c;
@@ -440,11 +454,14 @@ __global__ void __launch_bounds__(kPlanRowsThreads) k_plan_rows(const SchemaDesc
       base_ref = base_e;
     }
     hv |= warp_or64((active && lane >= from && c > 0) ? hn_l : 0ull);
+    c_n = 0;
+    if (next)
+      for (uint32_t t = bd_n.seg0; t < bd_n.seg0 + bd_n.nsegs; t++) c_n += fd.cnt[(size_t)t * P + p];
     if (active && c > 0) {
       uint32_t fr = frow + Xex, vp = vpos + Xex + my_pad;
       for (uint32_t t = bd.seg0; t < bd.seg0 + bd.nsegs; t++) {
         const size_t ti = (size_t)t * P + p;
-        const uint32_t ct = fd.cnt[ti];
+        const uint32_t ct = bd.nsegs == 1 ? c : fd.cnt[ti];  // a batch's only segment has its rows
         fd.cnt[ti] = fr;
         fd.vpos[ti] = vp;
         fr += ct;
@@ -480,13 +497,23 @@ __global__ void __launch_bounds__(kPlanRowsThreads) k_plan_bytes(const SchemaDes
   const int rec_words = kEmitFixedWords + nstr;
   uint32_t sb = fd.st_sb[(size_t)k * P + p];
   uint32_t fb = 0;
+  // software pipeline over chunks of 32 segments: the next chunk's segment and byte counts are
+  // loaded at the top of an iteration, its cut records (which need the segment) in the middle
+  uint32_t bc_n = 0, rec_n = 0;
+  SegDesc td_n{0, 0, 0, 0, 0, {0, 0, 0}};
+  if (lane < T) {
+    td_n = fd.segs[lane];
+    bc_n = fd.bcnt[((size_t)lane * nstr + k) * P + p];
+    if (td_n.row0 == 0) rec_n = fd.rec_idx[(size_t)td_n.batch * P + p];
+  }
   for (int t0 = 0; t0 < T; t0 += 32) {
     const int t = t0 + lane;
-    uint32_t bc = 0, rec = 0;
-    if (t < T) {
-      const SegDesc td = fd.segs[t];
-      bc = fd.bcnt[((size_t)t * nstr + k) * P + p];
-      if (td.row0 == 0) rec = fd.rec_idx[(size_t)td.batch * P + p];
+    const uint32_t bc = bc_n, rec = rec_n;
+    const bool next = t + 32 < T;
+    bc_n = 0;
+    if (next) {
+      td_n = fd.segs[t + 32];
+      bc_n = fd.bcnt[((size_t)(t + 32) * nstr + k) * P + p];
     }
     const uint32_t X = warp_incl_sum(bc);
     const uint32_t fb_l = fb + X - bc;
@@ -498,6 +525,7 @@ __global__ void __launch_bounds__(kPlanRowsThreads) k_plan_bytes(const SchemaDes
     }
     const uint32_t fb_last = __shfl_sync(kFull, fb_l, last < 0 ? 0 : last);
     const uint32_t sb_l = last < 0 ? sb + (fb_l - fb) : fb_l - fb_last;
+    rec_n = next && td_n.row0 == 0 ? fd.rec_idx[(size_t)td_n.batch * P + p] : 0u;
     if (t < T) {
       if (rec) fd.emit[(size_t)(rec - 1) * rec_words + kEmitFixedWords + k] = fb_l;
       const size_t ix = ((size_t)t * nstr + k) * P + p;
