@@ -360,32 +360,37 @@ __global__ void __launch_bounds__(kPlanRowsThreads) k_plan_rows(const SchemaDesc
   uint32_t base = fd.st_base[p];
   unsigned long long hv = fd.st_hv[p];
   uint32_t frow = 0, vpos = 0, piece_start = 0;  // flush-local rows; piece_start = frow of the piece
-  // software pipeline over chunks of 32 batches: the next chunk's descriptors are loaded while
-  // this chunk's events are resolved, and its row counts while this chunk's offsets are written
-  BatchDesc bd_n{0, 0, 0, 0};
-  unsigned long long hn_n = 0, ihn_n = 0;
-  uint32_t c_n = 0;
-  if (lane < NB) {
-    bd_n = fd.batches[lane];
-    hn_n = fd.hn[lane];
-    ihn_n = fd.ihn[lane];
-    for (uint32_t t = bd_n.seg0; t < bd_n.seg0 + bd_n.nsegs; t++) c_n += fd.cnt[(size_t)t * P + p];
-  }
+  // software pipeline over chunks of 32 batches: while chunk j is resolved, the descriptors of
+  // chunk j + 2 are loaded and the row counts of chunk j + 1 (whose descriptors arrived during
+  // chunk j - 1)
+  auto load_desc = [&](int b, BatchDesc& bd, unsigned long long& hn, unsigned long long& ihn) {
+    if (b < NB) {
+      bd = fd.batches[b];
+      hn = fd.hn[b];
+      ihn = fd.ihn[b];
+    } else {
+      bd = BatchDesc{0, 0, 0, 0};
+      hn = ihn = 0;
+    }
+  };
+  auto load_rows = [&](const BatchDesc& bd) {
+    uint32_t c = 0;
+    for (uint32_t t = bd.seg0; t < bd.seg0 + bd.nsegs; t++) c += fd.cnt[(size_t)t * P + p];
+    return c;
+  };
+  BatchDesc bd_c, bd_x, bd_y;
+  unsigned long long hn_c, ihn_c, hn_x, ihn_x, hn_y, ihn_y;
+  load_desc(lane, bd_c, hn_c, ihn_c);
+  load_desc(lane + 32, bd_x, hn_x, ihn_x);
+  uint32_t c_c = load_rows(bd_c);
   for (int b0 = 0; b0 < NB; b0 += 32) {
     const int b = b0 + lane;
     const bool active = b < NB;
-    const BatchDesc bd = bd_n;
-    const uint32_t c = c_n;
-    const unsigned long long hn_l = hn_n, ihn_l = ihn_n;
-    const bool next = b + 32 < NB;
-    if (next) {
-      bd_n = fd.batches[b + 32];
-      hn_n = fd.hn[b + 32];
-      ihn_n = fd.ihn[b + 32];
-    } else {
-      bd_n = BatchDesc{0, 0, 0, 0};
-      hn_n = ihn_n = 0;
-    }
+    const BatchDesc bd = bd_c;
+    const uint32_t c = c_c;
+    const unsigned long long hn_l = hn_c, ihn_l = ihn_c;
+    load_desc(b + 64, bd_y, hn_y, ihn_y);
+    const uint32_t c_x = load_rows(bd_x);
     const uint32_t X = warp_incl_sum(c);
     const uint32_t Xex = X - c;
     const uint32_t total = __shfl_sync(kFull, X, 31);
@@ -454,9 +459,6 @@ __global__ void __launch_bounds__(kPlanRowsThreads) k_plan_rows(const SchemaDesc
       base_ref = base_e;
     }
     hv |= warp_or64((active && lane >= from && c > 0) ? hn_l : 0ull);
-    c_n = 0;
-    if (next)
-      for (uint32_t t = bd_n.seg0; t < bd_n.seg0 + bd_n.nsegs; t++) c_n += fd.cnt[(size_t)t * P + p];
     if (active && c > 0) {
       uint32_t fr = frow + Xex, vp = vpos + Xex + my_pad;
       for (uint32_t t = bd.seg0; t < bd.seg0 + bd.nsegs; t++) {
@@ -473,6 +475,13 @@ __global__ void __launch_bounds__(kPlanRowsThreads) k_plan_rows(const SchemaDesc
     base = base_ref + (total - ref_x);
     frow += total;
     vpos += total + pad;
+    bd_c = bd_x;
+    hn_c = hn_x;
+    ihn_c = ihn_x;
+    c_c = c_x;
+    bd_x = bd_y;
+    hn_x = hn_y;
+    ihn_x = ihn_y;
   }
   if (lane == 0) {
     fd.st_cap[p] = cap;
@@ -497,24 +506,31 @@ __global__ void __launch_bounds__(kPlanRowsThreads) k_plan_bytes(const SchemaDes
   const int rec_words = kEmitFixedWords + nstr;
   uint32_t sb = fd.st_sb[(size_t)k * P + p];
   uint32_t fb = 0;
-  // software pipeline over chunks of 32 segments: the next chunk's segment and byte counts are
-  // loaded at the top of an iteration, its cut records (which need the segment) in the middle
-  uint32_t bc_n = 0, rec_n = 0;
-  SegDesc td_n{0, 0, 0, 0, 0, {0, 0, 0}};
-  if (lane < T) {
-    td_n = fd.segs[lane];
-    bc_n = fd.bcnt[((size_t)lane * nstr + k) * P + p];
-    if (td_n.row0 == 0) rec_n = fd.rec_idx[(size_t)td_n.batch * P + p];
-  }
+  // software pipeline over chunks of 32 segments: while chunk j is resolved, the segments and
+  // byte counts of chunk j + 2 are loaded and the cut records of chunk j + 1 (whose segments
+  // arrived during chunk j - 1)
+  auto load_seg = [&](int t, SegDesc& td, uint32_t& bc) {
+    if (t < T) {
+      td = fd.segs[t];
+      bc = fd.bcnt[((size_t)t * nstr + k) * P + p];
+    } else {
+      td = SegDesc{0, 1, 0, 0, 0, {0, 0, 0}};  // row0 != 0: no cut record
+      bc = 0;
+    }
+  };
+  auto load_rec = [&](const SegDesc& td) {
+    return td.row0 == 0 ? fd.rec_idx[(size_t)td.batch * P + p] : 0u;
+  };
+  SegDesc td_c, td_x, td_y;
+  uint32_t bc_c, bc_x, bc_y;
+  load_seg(lane, td_c, bc_c);
+  load_seg(lane + 32, td_x, bc_x);
+  uint32_t rec_c = load_rec(td_c);
   for (int t0 = 0; t0 < T; t0 += 32) {
     const int t = t0 + lane;
-    const uint32_t bc = bc_n, rec = rec_n;
-    const bool next = t + 32 < T;
-    bc_n = 0;
-    if (next) {
-      td_n = fd.segs[t + 32];
-      bc_n = fd.bcnt[((size_t)(t + 32) * nstr + k) * P + p];
-    }
+    const uint32_t bc = bc_c, rec = rec_c;
+    load_seg(t + 64, td_y, bc_y);
+    const uint32_t rec_x = load_rec(td_x);
     const uint32_t X = warp_incl_sum(bc);
     const uint32_t fb_l = fb + X - bc;
     // the last cut at or before this tile
@@ -525,7 +541,6 @@ __global__ void __launch_bounds__(kPlanRowsThreads) k_plan_bytes(const SchemaDes
     }
     const uint32_t fb_last = __shfl_sync(kFull, fb_l, last < 0 ? 0 : last);
     const uint32_t sb_l = last < 0 ? sb + (fb_l - fb) : fb_l - fb_last;
-    rec_n = next && td_n.row0 == 0 ? fd.rec_idx[(size_t)td_n.batch * P + p] : 0u;
     if (t < T) {
       if (rec) fd.emit[(size_t)(rec - 1) * rec_words + kEmitFixedWords + k] = fb_l;
       const size_t ix = ((size_t)t * nstr + k) * P + p;
@@ -537,6 +552,10 @@ __global__ void __launch_bounds__(kPlanRowsThreads) k_plan_bytes(const SchemaDes
     const uint32_t fb_last31 = __shfl_sync(kFull, fb_l, last31 < 0 ? 0 : last31);
     sb = last31 < 0 ? sb + total : (fb + total) - fb_last31;
     fb += total;
+    bc_c = bc_x;
+    rec_c = rec_x;
+    td_x = td_y;
+    bc_x = bc_y;
   }
   if (lane == 0) {
     fd.st_sb[(size_t)k * P + p] = sb;
