@@ -949,9 +949,16 @@ Status Splitter::Flush() {
   pend_.host_in = host_in;
   fr.scratch = scr_cur_;
   scr_cur_ ^= 1;
+  // host inputs: the pass is bound by the host link, not by the device; its k_scatter goes
+  // right away so its partition data can start back to the host sooner
+  const bool scatter_now = host_in;
 
   resident_bytes_ += fr.out_bytes;
   flushes_.push_back(std::move(fr));
+  if (scatter_now) {
+    st = LaunchPendingScatter();
+    if (!st.ok()) return st;
+  }
   pending_.clear();
   pending_cols_.clear();
   pending_chars_.clear();
@@ -961,12 +968,17 @@ Status Splitter::Flush() {
     cur_ ^= 1;
     used_ = 0;
   }
-  // keep HBM use under the budget (or move every flush out when asked to)
+  return MoveOutputs();
+}
+
+// Keeps HBM use under the budget (or moves every finished pass out when asked to): passes whose
+// k_scatter is queued go to pinned host memory, oldest first.
+Status Splitter::MoveOutputs() {
   const size_t budget = opts_.device_budget > 0 ? (size_t)opts_.device_budget : (64ull << 30);
   for (auto& f : flushes_) {
     if (!(opts_.keep_output_on_device == 0 || resident_bytes_ > budget)) break;
     if (!f.on_host && f.launched) {
-      st = MoveFlushToHost(f);
+      Status st = MoveFlushToHost(f);
       if (!st.ok()) return st;
     }
   }
@@ -997,7 +1009,9 @@ Status Splitter::LaunchPendingScatter() {
 Status Splitter::Drain() {
   Status st = Flush();
   if (!st.ok()) return st;
-  return LaunchPendingScatter();
+  st = LaunchPendingScatter();
+  if (!st.ok()) return st;
+  return MoveOutputs();
 }
 
 // Copies a flush's outputs into a pinned host block and releases the HBM copy (both stream

@@ -181,9 +181,10 @@ class Splitter {
   int32_t* d_err_ = nullptr;
   uint32_t* d_call_ = nullptr;
   // The pass schedule: k_hash_count and k_scatter run one after the other on stream_, the plan
-  // kernels on pstream_.  A pass's k_scatter is queued only when the next pass is (or at a sync),
-  // after that pass's k_hash_count, so the plan of pass i runs beside k_hash_count of pass i + 1
-  // and k_scatter of pass i - 1 instead of delaying stream_.  The per-pass scratch is therefore
+  // kernels on pstream_.  With device-resident inputs a pass's k_scatter is queued only when the
+  // next pass is (or at a sync), after that pass's k_hash_count, so the plan of pass i runs beside
+  // k_hash_count of pass i + 1 and k_scatter of pass i - 1 instead of delaying stream_; with host
+  // inputs (bound by the host link) it is queued right after its own plan.  The per-pass scratch is therefore
   // double-buffered (scr_cur_: the buffer of the next pass); stream order keeps a buffer's next
   // k_hash_count behind the k_scatter that last read it.
   cudaStream_t pstream_ = nullptr;
@@ -200,6 +201,7 @@ class Splitter {
   PendingScatter pend_;
   Status LaunchPendingScatter();
   Status Drain();  // Flush, then queue the pending k_scatter
+  Status MoveOutputs();
 
   // staging (host inputs): double-buffered device buffers, filled by k_gather (direct_) or
   // by H2D copies of pinned host twins
