@@ -44,9 +44,9 @@ WORKLOAD = ("wide fact-table split: 200M rows, 4096-row batches, 16 columns "
             "2% nulls, hash on keys 0-1, 200 partitions")
 BATCH_ROWS = 4096
 # DRAM bytes that one k_scatter launch moves per algorithmic byte, from an ncu capture of one
-# pass of this workload (2,036,224 rows: 732.9 MB of DRAM traffic for 732.4 MB algorithmic;
-# profiles/k_scatter_wide_fact_table.md).
-K_SCATTER_DRAM_PER_ALG_BYTE = 1.001
+# full 1 GiB pass of this workload (5,963,776 rows: 2.228 GB of DRAM traffic for 2.145 GB
+# algorithmic; profiles/k_scatter_wide_fact_table.md).
+K_SCATTER_DRAM_PER_ALG_BYTE = 1.039
 PARTITIONS = 200
 KEYS = [0, 1]
 
@@ -673,10 +673,11 @@ def run_gpu(args):
                             K_SCATTER_DRAM_PER_ALG_BYTE * alg_bytes / max(flushes, 1)),
                 "traffic_source": ("--traffic-per-launch" if args.traffic_per_launch else
                                    "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
-                                   "pass (732.9 MB for 732.4 MB algorithmic), scaled to this "
-                                   "run's average pass"),
-                "overlap": ("k_scatter of pass i runs beside k_hash_count and the plan of pass "
-                            "i + 1; its duration is the live one, with that overlap"),
+                                   "full 1 GiB pass (2.228 GB for 2.145 GB algorithmic), scaled "
+                                   "to this run's average pass"),
+                "overlap": ("k_scatter of pass i runs after k_hash_count of pass i + 1 on one "
+                            "stream, beside the plan kernels of pass i + 1; its duration is the "
+                            "live one"),
                 "launches_per_step": flushes,
                 "algorithmic_bytes_per_launch": alg_bytes / max(flushes, 1),
                 "avg_launch_ms": k_scat / max(flushes, 1)}
