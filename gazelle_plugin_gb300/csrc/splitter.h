@@ -6,7 +6,7 @@
 // requires, either by the GPU itself over a coherent host link (k_gather into device staging,
 // where the device can read pageable host memory through the host page tables) or by a CPU
 // copy into pinned staging; every `flush_bytes` of input one device pass runs the kernels on
-// the splitter's stream.  Emission decisions are made on the
+// the splitter's streams (see the pass schedule below).  Emission decisions are made on the
 // device by k_plan, so Split never waits for the GPU.  Stop() finishes the device work,
 // assembles every emitted partition batch from the flush outputs and writes the Arrow IPC
 // data file in partition order.
