@@ -607,8 +607,9 @@ __device__ __forceinline__ void csync() { group_sync<kConsumers, 1>(); }
 // its keys, payloads and match masks stay in registers between the counting and the scatter.
 constexpr int kSortIters = kTileRows / (kW * 32);  // 32-row groups per warp
 __device__ void radix_pass(const uint16_t* kin, const uint16_t* pin, uint16_t* kout,
-                           uint16_t* pout, int n, int shift, uint16_t* wcnt, uint32_t* off,
+                           uint16_t* pout, int n, int shift, int ndig, uint16_t* wcnt, uint32_t* off,
                            uint32_t* scratch) {
+  // ndig: digit values that occur (keys < P), so only kW * ndig counters are transposed / scanned
   const int w = threadIdx.x >> 5;
   const int seg = ((n + kW * 32 - 1) / (kW * 32)) * 32;
   for (int i = threadIdx.x; i < kW * 256; i += kConsumers) wcnt[i] = 0;
@@ -634,12 +635,12 @@ __device__ void radix_pass(const uint16_t* kin, const uint16_t* pin, uint16_t* k
     __syncwarp();
   }
   csync();
-  for (int i = threadIdx.x; i < kW * 256; i += kConsumers) {
+  for (int i = threadIdx.x; i < kW * ndig; i += kConsumers) {
     const int d = i / kW, ww = i % kW;
     off[i] = wcnt[ww * 256 + d];
   }
   csync();
-  block_exscan<kConsumers, 1>(off, kW * 256, scratch);
+  block_exscan<kConsumers, 1>(off, kW * ndig, scratch);
 #pragma unroll
   for (int it = 0; it < kSortIters; it++) {
     const int c = it * 32;
@@ -804,7 +805,10 @@ __device__ __forceinline__ void store_word_part(uint8_t* p, uint32_t w, uint32_t
 // when the string covers them only in part, are stored as a byte and / or a halfword.  The aligned source words may reach 6 bytes before `src` and 7 past
 // `src + len`: the staging buffer keeps that slack, and those bytes are never stored.
 __device__ __forceinline__ void copy_string_smem(uint8_t* dst, uint32_t src, uint32_t len) {
-  if (len == 0) return;
+  if (len <= 1) {  // empty, or one character (flag-like columns)
+    if (len) dst[0] = (uint8_t)lds8(src);
+    return;
+  }
   const uintptr_t d = reinterpret_cast<uintptr_t>(dst);
   const uint32_t ph = (uint32_t)(d & 3);
   const uint32_t a = src - ph;  // source byte that maps to the first destination word
@@ -1050,12 +1054,12 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
     pA[j] = (uint16_t)j;
   }
   csync();
-  radix_pass(kA, pA, kB, pB, n, 0, wcnt, roff, scratch);
+  radix_pass(kA, pA, kB, pB, n, 0, min(P, 256), wcnt, roff, scratch);
   uint16_t* ks = kB;
   uint16_t* ps = pB;
   uint32_t* dstrow = reinterpret_cast<uint32_t*>(kA);  // kA,pA are free after one pass
   if (P > 256) {
-    radix_pass(kB, pB, kA, pA, n, 8, wcnt, roff, scratch);
+    radix_pass(kB, pB, kA, pA, n, 8, ((P - 1) >> 8) + 1, wcnt, roff, scratch);
     ks = kA;
     ps = pA;
     dstrow = reinterpret_cast<uint32_t*>(kB);
