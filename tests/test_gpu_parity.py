@@ -261,6 +261,67 @@ def test_device_resident_inputs():
     assert_same(res, data, ref)
 
 
+def _device_batches(torch, batches):
+    keep, out = [], []
+    for b in batches:
+        bufs = []
+        for buf in b.buffers:
+            t = torch.from_numpy(buf.copy()).cuda() if buf.nbytes else torch.zeros(0, dtype=torch.uint8).cuda()
+            keep.append(t)
+            bufs.append(t)
+        out.append((b.num_rows, [t.data_ptr() if t.numel() else 0 for t in bufs], [t.numel() for t in bufs]))
+    return keep, out
+
+
+@pytest.mark.parametrize("flush,keep_dev,budget", [(1 << 20, 1, 64 << 30), (3 << 20, 0, 64 << 30),
+                                                   (2 << 20, 1, 4 << 20)])
+def test_device_resident_inputs_many_passes(flush, keep_dev, budget):
+    # device-resident inputs: each pass's k_scatter is queued behind the next pass's
+    # k_hash_count; outputs moved to host after every pass, or past a small HBM budget
+    torch = pytest.importorskip("torch")
+    batches = W.c2_batches(12, 24, 4096) + W.c2_batches(13, 3, 1000)
+    keep, dev = _device_batches(torch, batches)
+    w = S.ShuffleSplitterJniWrapper()
+    h = w.make(S.NativePartitioning("hash", 200, None, W.C2_KEYS, list(W.C2_SCHEMA)),
+               writeSchema=False, input_kind=S.GZ_INPUT_DEVICE_RETAINED, flush_bytes=flush,
+               keep_output_on_device=keep_dev, device_budget=budget)
+    for i, (n, addrs, sizes) in enumerate(dev):
+        w.split(h, n, addrs, sizes)
+        if i == 10:
+            w.sync(h)  # a sync in the middle queues the pending k_scatter early
+    assert w.stats(h)[0] >= 4
+    res = w.stop(h)
+    data = w.data(h)
+    w.close(h)
+    ref = O.run_oracle(W.C2_SCHEMA, batches, 200, W.C2_KEYS)
+    assert_same(res, data, ref)
+
+
+def test_device_resident_inputs_offheap_split_size():
+    # device inputs with offheap_per_task: the batches whose call flag is read back get their own
+    # pass while earlier passes' k_scatter are still queued behind them
+    torch = pytest.importorskip("torch")
+    schema = [W.Field("k", "int64"), W.Field("s", "utf8"), W.Field("t", "utf8")]
+    rng = np.random.default_rng(14)
+    batches = [W.random_batch(rng, schema, 300, 0.1) for _ in range(12)]
+    b0 = batches[0]
+    b0.buffers[3] = np.zeros(301 * 4, np.uint8)
+    b0.buffers[4] = np.zeros(0, np.uint8)
+    keep, dev = _device_batches(torch, batches)
+    opts = dict(offheap_per_task=1 << 16, prefer_spill=False)
+    w = S.ShuffleSplitterJniWrapper()
+    h = w.make(S.NativePartitioning("hash", 7, None, [0], list(schema)), writeSchema=False,
+               input_kind=S.GZ_INPUT_DEVICE_RETAINED, flush_bytes=1 << 14,
+               offheapPerTask=opts["offheap_per_task"], preferSpill=False)
+    for n, addrs, sizes in dev:
+        w.split(h, n, addrs, sizes)
+    res = w.stop(h)
+    data = w.data(h)
+    w.close(h)
+    ref = O.run_oracle(schema, batches, 7, [0], **opts)
+    assert_same(res, data, ref)
+
+
 def test_schema_ipc_make():
     pa = pytest.importorskip("pyarrow")
     batches = W.c1_batches(0, 2, 4096)
