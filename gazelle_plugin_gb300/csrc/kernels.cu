@@ -916,6 +916,7 @@ __device__ __forceinline__ void scatter_zero_bits(uint32_t* words, uint32_t bits
 __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc sd, const FlushDesc fd) {
   extern __shared__ __align__(128) uint8_t ssm[];
   __shared__ uint32_t scratch[33];
+  __shared__ uint32_t wtot[2][32];                 // warp totals of a binary column, by column parity
   __shared__ __align__(8) uint64_t full[kSlots];   // slice i landed (issuer: expect_tx)
   __shared__ __align__(8) uint64_t empty[kSlots];  // slice i consumed (every scattering warp)
   __shared__ __align__(8) uint64_t cfull, cempty;  // the same for the character stage
@@ -1131,12 +1132,13 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
   uint32_t cuse = 0;  // staged character slices consumed
 
   // Warps run through fixed-width and bool columns at their own pace (the slots' mbarriers keep
-  // the fastest within kSlots columns of the slowest); only a binary column, which rewrites the
-  // shared run tables, starts with a barrier of the scattering threads.  A wait that times out
+  // the fastest within kSlots columns of the slowest); a binary column has two barriers of the
+  // scattering threads, after its warp totals and after its run tables.  A wait that times out
   // marks the block bad: from then on columns are skipped, but every thread still reaches every
-  // barrier (the skip decision of a binary column is taken after its barrier, so it is the same
+  // barrier (a binary column's skip decision is taken after its first barrier, so it is the same
   // in all threads).
   volatile uint32_t* vbad = &s_bad;
+  int nbin = 0;  // binary columns done (the parity of their warp-total buffer)
   for (int i = 0; i < A; i++) {
     const int a = sd.order[i];
     const int slot = i % kSlots;
@@ -1150,8 +1152,8 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
         *vbad = 1;
       }
     }
-    if (kind == COL_BINARY) csync();
-    if (!*vbad) {
+    const bool live = !*vbad;  // fixed / bool columns: this thread's view is enough
+    if (live || kind == COL_BINARY) {
       const ColPtr c = s_col[a];
       const uint8_t* slot_base = stage0 + slot * kStageSlot;
       const uint8_t* stg = slot_base;  // staged values / bits / offsets, at the source's phase
@@ -1159,10 +1161,10 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
       else if (kind == COL_BOOL) stg = staged_ptr(slot_base, c.values + (row0 >> 3));
       else if (kind == COL_BINARY) stg = staged_ptr(slot_base, reinterpret_cast<const uint8_t*>(c.offsets + row0));
       // validity: clear the bits of null rows (destination words start 0xff)
-      if (c.validity != nullptr && s_nc[a] != 0 && fd.out_valid[a] != nullptr)
+      if (live && c.validity != nullptr && s_nc[a] != 0 && fd.out_valid[a] != nullptr)
         scatter_zero_bits(fd.out_valid[a], smem_addr(staged_ptr(slot_base + kStageBytes, c.validity + (row0 >> 3))),
                           dbs, n);
-      if (kind == COL_FIXED) {
+      if (kind == COL_FIXED && live) {
         const int w = sd.arr_width[a];
         uint8_t* out = fd.out_values[a];
         if (w == 8) {
@@ -1177,9 +1179,12 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
           const uint4* src = reinterpret_cast<const uint4*>(c.values) + row0;
           for (int j = threadIdx.x; j < n; j += kConsumers) reinterpret_cast<uint4*>(out)[dstrow[j]] = src[ps[j]];
         }
-      } else if (kind == COL_BOOL) {
+      } else if (kind == COL_BOOL && live) {
         scatter_zero_bits(fd.out_bits[a], smem_addr(stg), dbs, n);
-      } else {
+      } else if (kind == COL_BINARY) {
+        // every thread takes both barriers of a binary column; the lengths and their warp scans
+        // read only the slot (in bounds whether or not its copy arrived), and after the first
+        // barrier the block's state, the same in every thread, decides whether the rest runs
         const int32_t* oin = reinterpret_cast<const int32_t*>(stg);  // offsets of rows row0..row0+n
         // lengths of the owned positions; exclusive prefix over the tile = the lengths of all
         // earlier rows u' < u of positions + this row's prefix, one fused warp scan per row u
@@ -1205,16 +1210,18 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
           }
         }
         const int w = threadIdx.x >> 5;
+        uint32_t* tot = wtot[nbin & 1];  // the previous binary column's totals may still be read
         if (lane_id() == 31) {
 #pragma unroll
-          for (int u = 0; u < kRowsPerThread; u++) scratch[u * kW + w] = pre[u];
+          for (int u = 0; u < kRowsPerThread; u++) tot[u * kW + w] = pre[u];
         }
         csync();
-        {
+        const bool run = !*vbad;
+        if (run) {
           // the warp totals in (row, warp) order, one per lane: their exclusive scan is what all
           // earlier rows and this row's earlier warps hold (every warp scans them itself)
           static_assert(kRowsPerThread * kW == 32, "one warp total per lane");
-          const uint32_t sv = scratch[lane_id()];
+          const uint32_t sv = tot[lane_id()];
           uint32_t incl = sv;
 #pragma unroll
           for (int o = 1; o < 32; o <<= 1) {
@@ -1224,21 +1231,24 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
           const uint32_t excl = incl - sv;
 #pragma unroll
           for (int u = 0; u < kRowsPerThread; u++) pre[u] = __shfl_sync(kFull, excl, u * kW + w) + pre[u] - len[u];
-        }
-        // run tables at the run starts: destination of the run's first string and its offset
-        // inside the partition's segment, both relative to the tile prefix
-        cp_async_wait_all();
+          // run tables at the run starts: destination of the run's first string and its offset
+          // inside the partition's segment, both relative to the tile prefix (every thread has
+          // finished the previous binary column's reads of them: it passed the barrier above)
+          cp_async_wait_all();
 #pragma unroll
-        for (int u = 0; u < kRowsPerThread; u++) {
-          const int j = threadIdx.x + u * kConsumers;
-          if (j < n && rs[j] == j) {
-            const uint32_t before = has_pre ? nm3[j] : 0u;  // bytes from the segment's earlier tiles
-            rt0[j] = nm0[j] + before - pre[u];
-            rt1[j] = nm2[j] + nm1[j] + before - pre[u];
+          for (int u = 0; u < kRowsPerThread; u++) {
+            const int j = threadIdx.x + u * kConsumers;
+            if (j < n && rs[j] == j) {
+              const uint32_t before = has_pre ? nm3[j] : 0u;  // bytes from the segment's earlier tiles
+              rt0[j] = nm0[j] + before - pre[u];
+              rt1[j] = nm2[j] + nm1[j] + before - pre[u];
+            }
           }
+          load_run_meta(i + 1);
         }
-        load_run_meta(i + 1);
         csync();
+        nbin++;
+        if (run) {
         int32_t* ooff = reinterpret_cast<int32_t*>(fd.out_values[a]);
         uint8_t* ochars = fd.out_chars[a];
         uint32_t cd[kRowsPerThread];  // destination of each string in the column's characters
@@ -1275,6 +1285,7 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
             const int j = threadIdx.x + u * kConsumers;
             if (j < n) copy_string(ochars + cd[u], c.values + so[u], len[u], buf_lo, buf_hi);
           }
+        }
         }
       }
     }
