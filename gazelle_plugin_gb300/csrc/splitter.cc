@@ -950,8 +950,9 @@ Status Splitter::Flush() {
   fr.scratch = scr_cur_;
   scr_cur_ ^= 1;
   // host inputs: the pass is bound by the host link, not by the device; its k_scatter goes
-  // right away so its partition data can start back to the host sooner
-  const bool scatter_now = host_in;
+  // right away so its partition data can start back to the host sooner.  So does the first
+  // pass's: the device has nothing else to do while the host gathers the next pass.
+  const bool scatter_now = host_in || flushes_.empty();
 
   resident_bytes_ += fr.out_bytes;
   flushes_.push_back(std::move(fr));
