@@ -8,8 +8,8 @@
 //                  histograms into destination offsets; then scans over partitions
 //   k_scatter    : per 1024-row tile, a stable counting sort by partition id in shared memory,
 //                  then a coalesced scatter of every column into partition-contiguous output
-// A segment is up to seg_tiles consecutive tiles of one batch: the unit of k_hash_count and of
-// the plan's offsets.  k_hash_count also records, for every tile after the first of its
+// A segment is up to seg_tiles consecutive tiles of one batch (a batch is cut into equal
+// segments): the unit of k_hash_count and of the plan's offsets.  k_hash_count also records, for every tile after the first of its
 // segment, how many rows and bytes each partition received from the segment's earlier tiles, so
 // each k_scatter CTA (one tile) finds its destinations without the others.
 // Output of a flush, per array column, is partition-major: all rows of partition 0 in input
@@ -118,7 +118,7 @@ struct FlushDesc {
   const TileDesc* tiles;     // [n_tiles]
   const ColPtr* cols;        // [n_batches][n_cols]
 
-  // scratch (reused across flushes)
+  // scratch (two buffers, used by alternate flushes)
   uint16_t* pids;     // [n_rows]
   uint32_t* cnt;      // [n_segs][P] rows; rewritten by k_plan to the flush-local row offset
   uint32_t* bcnt;     // [n_segs][n_str][P] bytes; rewritten to the flush-local byte offset
