@@ -120,6 +120,18 @@ def generate_on_device(total_rows: int, seed: int = 1):
     return rows, addrs, sizes, [c[0] for c in bufcols]
 
 
+def reduce_over_ranks(x: float, op: str = "max") -> float:
+    """Max or sum of a per-rank figure over the process group (identity without one): replicas
+    split disjoint inputs with no data-path collective, only their times and bytes are combined."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def link_bandwidth(nbytes: int = 1 << 30) -> dict:
     """Host link of this box: one pinned 1 GiB buffer copied host->device and device->host (best
     of 3, CUDA events).  The end-to-end figure moves the input and the partition bytes over it."""
@@ -652,13 +664,10 @@ def run_gpu(args):
         times.append(time.perf_counter() - t0)
     clk = clocks.stop()
     t_local = sum(times)
-    t_max = t_local
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t_local], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
-    value = alg_bytes * args.steps * world / t_max / 1e9
+    t_max = reduce_over_ranks(t_local, "max")
+    alg_all = reduce_over_ranks(float(alg_bytes), "sum")  # every rank's own partition bytes
+    in_all = reduce_over_ranks(float(in_bytes), "sum")
+    value = alg_all * args.steps / t_max / 1e9
     ms_per_step = t_max / args.steps * 1e3
     # kernel timings (CUDA events on the splitter's stream), per step
     k_hash = statistics.mean(s[0] for s in stats)
@@ -698,10 +707,10 @@ def run_gpu(args):
             one_step(host_opts, haddrs, sizes, e_stats)
             barrier()
             e_times.append(time.perf_counter() - t0)
-        e_t = sum(e_times)
-        e2e = {"value": alg_bytes * args.steps / e_t / 1e9, "unit": "GB/s",
-               "h2d_bytes_per_step": int(statistics.mean(s[6] for s in e_stats)),
-               "d2h_bytes_per_step": int(statistics.mean(s[7] for s in e_stats)),
+        e_t = reduce_over_ranks(sum(e_times), "max")
+        e2e = {"value": alg_all * args.steps / e_t / 1e9, "unit": "GB/s",
+               "h2d_bytes_per_step": int(reduce_over_ranks(statistics.mean(s[6] for s in e_stats), "sum")),
+               "d2h_bytes_per_step": int(reduce_over_ranks(statistics.mean(s[7] for s in e_stats), "sum")),
                "ms_per_step": e_t / args.steps * 1e3,
                "link": link}
         del host
@@ -736,7 +745,7 @@ def run_gpu(args):
             "gpu_launches": int(round(6 * flushes * args.steps)),
             "kernels_ms_per_step": {"k_hash_count": k_hash, "k_plan": k_plan, "k_scatter": k_scat},
             "rows_per_s": args.rows * args.steps * world / t_max,
-            "input_gbs": in_bytes * args.steps * world / t_max / 1e9,
+            "input_gbs": in_all * args.steps / t_max / 1e9,
             "stop_s": stop_s,
         }
         if not args.no_forms:
