@@ -17,22 +17,21 @@ def _free_port() -> int:
         return s.getsockname()[1]
 
 
-def _rank_main(rank: int, world: int, port: int, out):
+def _rank_main(rank: int, world: int, port: int, out_dir: str):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     dist.init_process_group("gloo", rank=rank, world_size=world)
     import bench as B
     t = B.reduce_over_ranks(1.5 + rank, "max")
     b = B.reduce_over_ranks(1000.0 * (rank + 1), "sum")
-    out[rank] = (t, b)
+    with open(os.path.join(out_dir, f"rank{rank}.txt"), "w") as f:
+        f.write(f"{t} {b}")
     dist.destroy_process_group()
 
 
-def test_two_gloo_ranks_combine_times_and_bytes():
-    port = _free_port()
-    with mp.Manager() as m:
-        out = m.dict()
-        mp.spawn(_rank_main, args=(2, port, out), nprocs=2, join=True)
-        assert dict(out) == {0: (2.5, 3000.0), 1: (2.5, 3000.0)}
+def test_two_gloo_ranks_combine_times_and_bytes(tmp_path):
+    mp.spawn(_rank_main, args=(2, _free_port(), str(tmp_path)), nprocs=2, join=True)  # spawn, not fork
+    for r in range(2):
+        assert (tmp_path / f"rank{r}.txt").read_text() == "2.5 3000.0"
 
 
 def test_single_process_is_the_identity():
