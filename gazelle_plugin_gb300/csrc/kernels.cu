@@ -924,6 +924,10 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
   __shared__ uint32_t s_nc[kMaxCols];              // their null counts in the batch
   __shared__ int2 s_cr[kMaxStrPlan];               // character range of the tile per binary column
   __shared__ uint32_t s_bad;
+  // per column of the tile in processing order: x = its staged slice's offset in shared memory,
+  // y = shared address of its staged validity bits, z = kind | width << 8 | staged characters
+  // << 16 | validity to clear << 17 | binary column index << 24, w = array column
+  __shared__ uint4 s_ct[kMaxCols];
   const int T = kTileRows;
   uint8_t* stage0 = ssm;                                         // [kSlots][kStageSlot]
   uint8_t* cstage = ssm + kSlots * kStageSlot;                   // [kCharRegion]
@@ -1050,6 +1054,23 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
   }
 
   // ---- scattering threads --------------------------------------------------------------------
+  for (int i = threadIdx.x; i < A; i += kConsumers) {
+    const int a = sd.order[i];
+    const int kind = sd.arr_kind[a];
+    const int w = sd.arr_width[a];
+    const ColPtr c = s_col[a];
+    const uint8_t* slot_base = stage0 + (i % kSlots) * kStageSlot;
+    const uint8_t* stg = slot_base;  // staged values / bits / offsets, at the source's phase
+    if (kind == COL_FIXED && w <= 8) stg = staged_ptr(slot_base, c.values + (size_t)row0 * w);
+    else if (kind == COL_BOOL) stg = staged_ptr(slot_base, c.values + (row0 >> 3));
+    else if (kind == COL_BINARY) stg = staged_ptr(slot_base, reinterpret_cast<const uint8_t*>(c.offsets + row0));
+    const bool vwork = c.validity != nullptr && s_nc[a] != 0 && fd.out_valid[a] != nullptr;
+    const uint32_t vb = vwork ? smem_addr(staged_ptr(slot_base + kStageBytes, c.validity + (row0 >> 3))) : 0u;
+    s_ct[i] = make_uint4((uint32_t)(stg - ssm), vb,
+                         (uint32_t)kind | ((uint32_t)w << 8) | ((uint32_t)staged_binary(a) << 16) |
+                             ((uint32_t)vwork << 17) | ((uint32_t)(kind == COL_BINARY ? sd.arr_str[a] : 0) << 24),
+                         (uint32_t)a);
+  }
   for (int j = threadIdx.x; j < n; j += kConsumers) {
     kA[j] = fd.pids[tile.frow0 + j];
     pA[j] = (uint16_t)j;
@@ -1140,10 +1161,11 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
   volatile uint32_t* vbad = &s_bad;
   int nbin = 0;  // binary columns done (the parity of their warp-total buffer)
   for (int i = 0; i < A; i++) {
-    const int a = sd.order[i];
+    const uint4 ct = s_ct[i];
+    const int a = (int)ct.w;
     const int slot = i % kSlots;
-    const bool chars = staged_binary(a);
-    const int kind = sd.arr_kind[a];
+    const bool chars = (ct.z >> 16) & 1u;
+    const int kind = (int)(ct.z & 255u);
     if (!*vbad) {
       bool ok = mbar_wait(&full[slot], (uint32_t)((i / kSlots) & 1));
       if (chars) ok = mbar_wait(&cfull, cuse & 1) && ok;
@@ -1154,18 +1176,11 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
     }
     const bool live = !*vbad;  // fixed / bool columns: this thread's view is enough
     if (live || kind == COL_BINARY) {
-      const ColPtr c = s_col[a];
-      const uint8_t* slot_base = stage0 + slot * kStageSlot;
-      const uint8_t* stg = slot_base;  // staged values / bits / offsets, at the source's phase
-      if (kind == COL_FIXED && sd.arr_width[a] <= 8) stg = staged_ptr(slot_base, c.values + (size_t)row0 * sd.arr_width[a]);
-      else if (kind == COL_BOOL) stg = staged_ptr(slot_base, c.values + (row0 >> 3));
-      else if (kind == COL_BINARY) stg = staged_ptr(slot_base, reinterpret_cast<const uint8_t*>(c.offsets + row0));
+      const uint8_t* stg = ssm + ct.x;  // staged values / bits / offsets, at the source's phase
       // validity: clear the bits of null rows (destination words start 0xff)
-      if (live && c.validity != nullptr && s_nc[a] != 0 && fd.out_valid[a] != nullptr)
-        scatter_zero_bits(fd.out_valid[a], smem_addr(staged_ptr(slot_base + kStageBytes, c.validity + (row0 >> 3))),
-                          dbs, n);
+      if (live && ((ct.z >> 17) & 1u)) scatter_zero_bits(fd.out_valid[a], ct.y, dbs, n);
       if (kind == COL_FIXED && live) {
-        const int w = sd.arr_width[a];
+        const int w = (int)((ct.z >> 8) & 255u);
         uint8_t* out = fd.out_values[a];
         if (w == 8) {
           gather_rows(reinterpret_cast<uint64_t*>(out), reinterpret_cast<const uint64_t*>(stg), ps, dstrow, n);
@@ -1176,7 +1191,7 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
         } else if (w == 1) {
           gather_rows(out, stg, ps, dstrow, n);
         } else {  // 16-byte values are gathered straight from global memory
-          const uint4* src = reinterpret_cast<const uint4*>(c.values) + row0;
+          const uint4* src = reinterpret_cast<const uint4*>(s_col[a].values) + row0;
           for (int j = threadIdx.x; j < n; j += kConsumers) reinterpret_cast<uint4*>(out)[dstrow[j]] = src[ps[j]];
         }
       } else if (kind == COL_BOOL && live) {
@@ -1185,6 +1200,7 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
         // every thread takes both barriers of a binary column; the lengths and their warp scans
         // read only the slot (in bounds whether or not its copy arrived), and after the first
         // barrier the block's state, the same in every thread, decides whether the rest runs
+        const ColPtr c = s_col[a];
         const int32_t* oin = reinterpret_cast<const int32_t*>(stg);  // offsets of rows row0..row0+n
         // lengths of the owned positions; exclusive prefix over the tile = the lengths of all
         // earlier rows u' < u of positions + this row's prefix, one fused warp scan per row u
@@ -1268,7 +1284,7 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
           for (int u = 0; u < kRowsPerThread; u++)
             if (threadIdx.x + u * kConsumers < n) ooff[d[u]] = (int32_t)v[u];
         }
-        const int k = sd.arr_str[a];
+        const int k = (int)(ct.z >> 24);
         if (chars) {
           // shared address of byte 0 of the column (offsets index from there)
           const uint32_t cbase = smem_addr(staged_ptr(cstage, c.values + s_cr[k].x)) - (uint32_t)s_cr[k].x;
