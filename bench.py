@@ -56,6 +56,41 @@ def schema():
     return W.C2_SCHEMA
 
 
+def metric_and_workload(partitioner: str):
+    """The headline is the hash split; --partitioner rr / range time the same table split by
+    the round-robin selection or by a uniform int32 partition id column in front of it."""
+    if partitioner == "hash":
+        return METRIC, WORKLOAD
+    what = {"rr": "round-robin", "range": "int32 partition ids U[0, 200) as field 0"}[partitioner]
+    return (METRIC.replace("hash-split", f"{partitioner}-split"),
+            WORKLOAD.replace("hash on keys 0-1", what))
+
+
+def workload_inputs(total_rows: int, seed: int, partitioner: str):
+    """(schema, keys, rows, addrs, sizes, tensors) of the workload on cuda:0; the range split
+    gets its partition id column as field 0."""
+    import torch
+    from gazelle_plugin_gb300 import workloads as W
+    rows, addrs, sizes, keep = generate_on_device(total_rows, seed=seed)
+    sch, keys = list(schema()), list(KEYS)
+    if partitioner != "hash":
+        keys = []
+    if partitioner == "range":
+        g = torch.Generator(device="cuda")
+        g.manual_seed(1000 + seed)
+        nb = len(rows)
+        pid = torch.randint(0, PARTITIONS, (nb * BATCH_ROWS,), generator=g, device="cuda",
+                            dtype=torch.int32)
+        r64 = rows.astype(np.int64)
+        pa = pid.data_ptr() + np.arange(nb, dtype=np.int64) * BATCH_ROWS * 4
+        addrs = np.concatenate([np.zeros((nb, 1), np.int64), pa[:, None], addrs], axis=1)
+        sizes = np.concatenate([np.zeros((nb, 1), np.int64), (r64 * 4)[:, None], sizes], axis=1)
+        keep = [None, pid] + list(keep)
+        sch = [W.Field("pid", "int32", False)] + sch
+        torch.cuda.synchronize()
+    return sch, keys, rows, addrs, sizes, keep
+
+
 # ---------------------------------------------------------------------------------------
 def generate_on_device(total_rows: int, seed: int = 1):
     """Seeded workload batches on cuda:0.  Returns (rows[int32], addrs[nb, nbufs],
@@ -258,12 +293,14 @@ def measured_peak_gbs():
 
 
 # ---------------------------------------------------------------------------------------
-def cpu_split_sample(batches, threads: int):
+def cpu_split_sample(batches, threads: int, sch=None, keys=None, partitioner: str = "hash"):
     """Oracle splitters, one per thread over disjoint shards; returns (seconds, bytes)."""
     from oracle import oracle as O
     shards = [batches[i::threads] for i in range(threads)]
     res = [None] * threads
-    sp = [O.OracleSplitter(schema(), PARTITIONS, KEYS) for _ in range(threads)]
+    sch = schema() if sch is None else sch
+    keys = KEYS if keys is None else keys
+    sp = [O.OracleSplitter(sch, PARTITIONS, keys, short_name=partitioner) for _ in range(threads)]
     barrier = threading.Barrier(threads + 1)
 
     def work(i):
@@ -295,26 +332,29 @@ def run_reference(args):
         return
     import torch
     threads = os.cpu_count() or 1
-    rows, addrs, sizes, keep = generate_on_device(args.sample_batches * BATCH_ROWS, seed=1)
+    sch, keys, rows, addrs, sizes, keep = workload_inputs(args.sample_batches * BATCH_ROWS, 1,
+                                                          args.partitioner)
     batches = host_batches(rows, addrs, sizes, keep, 0, args.sample_batches)
     del keep
     torch.cuda.empty_cache()
+    part = dict(sch=sch, keys=keys, partitioner=args.partitioner)
     for _ in range(args.warmup):
-        cpu_split_sample(batches[: max(threads, len(batches) // 8)], threads)
+        cpu_split_sample(batches[: max(threads, len(batches) // 8)], threads, **part)
     times, nbytes = [], 0
     for _ in range(args.steps):
-        dt, nb = cpu_split_sample(batches, threads)
+        dt, nb = cpu_split_sample(batches, threads, **part)
         times.append(dt)
         nbytes = nb
     total = sum(times)
     value = nbytes * args.steps / total / 1e9
     sample = f"{len(batches)} batches x {BATCH_ROWS} rows of the workload per step"
+    metric, workload = metric_and_workload(args.partitioner)
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": args.gpus,
+        "impl": "reference", "metric": metric, "value": value, "unit": "GB/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
         "data": "synthetic (seeded torch RNG, same distributions)",
-        "config": {"workload": WORKLOAD, "sample": sample},
+        "config": {"workload": workload, "sample": sample},
         "cpu_baseline": {"value": value, "unit": "GB/s", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -617,8 +657,8 @@ def run_gpu(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     w = S.ShuffleSplitterJniWrapper()
-    part = S.NativePartitioning("hash", PARTITIONS, None, KEYS, list(schema()))
-    rows, addrs, sizes, keep = generate_on_device(args.rows, seed=1 + rank)
+    sch, keys, rows, addrs, sizes, keep = workload_inputs(args.rows, 1 + rank, args.partitioner)
+    part = S.NativePartitioning(args.partitioner, PARTITIONS, None, keys, sch)
     in_bytes = int(sizes.sum())
 
     def barrier():
@@ -720,18 +760,20 @@ def run_gpu(args):
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         sample = host_batches(rows, addrs, sizes, keep, 0, args.sample_batches)
-        cpu_split_sample(sample[: threads * 2], threads)
-        dt, nb = cpu_split_sample(sample, threads)
+        cpart = dict(sch=sch, keys=keys, partitioner=args.partitioner)
+        cpu_split_sample(sample[: threads * 2], threads, **cpart)
+        dt, nb = cpu_split_sample(sample, threads, **cpart)
         cpu = {"value": nb / dt / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
                "sample": f"first {len(sample)} batches x {BATCH_ROWS} rows of the workload"}
 
     if rank == 0:
+        metric, workload = metric_and_workload(args.partitioner)
         line = {
-            "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world,
+            "metric": metric, "value": value, "unit": "GB/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
             "data": "synthetic (seeded torch RNG on the device, workload distributions)",
-            "config": {"workload": WORKLOAD, "rows": int(args.rows), "batch_rows": BATCH_ROWS,
+            "config": {"workload": workload, "rows": int(args.rows), "batch_rows": BATCH_ROWS,
                        "num_partitions": PARTITIONS, "input_bytes": in_bytes,
                        "partition_bytes": out_bytes,
                        "l2": "inputs (36 GB) larger than L2; no flush needed",
@@ -772,6 +814,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched and served forms")
     ap.add_argument("--served-gb-per-task", type=float, default=2.0)
+    ap.add_argument("--partitioner", default="hash", choices=["hash", "rr", "range"],
+                    help="Splitter::Make short name; the headline is hash")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

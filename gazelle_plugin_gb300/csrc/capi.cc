@@ -313,7 +313,8 @@ GzStatus gz_serve_open(int64_t server, const char* short_name, int32_t num_parti
   if (flush <= 0) {
     gz::TuneChoice tc;
     const std::vector<int32_t> keys(key_cols, key_cols + (key_cols && n_keys > 0 ? n_keys : 0));
-    flush = gz::TuneLookup(gz::SchemaSignature(FieldsFrom(fields, n_fields), keys, num_partitions), &tc)
+    flush = gz::TuneLookup(gz::SchemaSignature(short_name ? short_name : "", FieldsFrom(fields, n_fields), keys,
+                                               num_partitions), &tc)
                 ? tc.flush_bytes
                 : (512ll << 20);
   }
@@ -452,7 +453,7 @@ GzStatus gz_autotune(const char* short_name, int32_t num_partitions, const GzFie
     t_make_error = "gz_autotune: " + st.msg;
     return st.code;
   }
-  gz::TuneStore(gz::SchemaSignature(fs, keys, num_partitions), best);
+  gz::TuneStore(gz::SchemaSignature(short_name, fs, keys, num_partitions), best);
   if (out) {
     out->flush_bytes = best.flush_bytes;
     out->seg_tiles = best.seg_tiles;

@@ -1,8 +1,9 @@
 // Shared host/device definitions of the GB300 hash-split engine.
 //
 // One "flush" is a device pass over a group of consecutive input batches:
-//   k_hash_count : Spark Murmur3 chain + pmod per row, per-segment partition histograms
-//                  (rows, and bytes of every utf8 column), per-batch null counts
+//   k_hash_count : the partition id of every row (Spark Murmur3 chain + pmod, the running
+//                  round-robin selection, or the range partitioner's id column), per-segment
+//                  partition histograms (rows, and bytes of every utf8 column), null counts
 //   k_plan       : per-partition walk over the flush's batches that restates the reference
 //                  buffer policy (allocate / emit / reuse, validity presence) and turns the
 //                  histograms into destination offsets; then scans over partitions
@@ -31,6 +32,10 @@ constexpr int kPlanThreads = 1024;
 constexpr int kMaxBatchesPerFlush = 4096;
 
 enum KeyKind : int32_t { KEY_I32 = 0, KEY_I64 = 1, KEY_I8 = 2, KEY_I16 = 3, KEY_BOOL = 4 };
+// Splitter::Make short names (native-sql-engine/cpp/src/shuffle/splitter.cc:190-208):
+// "hash" (HashSplitter), "rr" and "single" (RoundRobinSplitter, single = 1 partition),
+// "range" (FallbackRangeSplitter: int32 ids in schema field 0, key_col[0] = 0)
+enum Partitioner : int32_t { PART_HASH = 0, PART_RR = 1, PART_RANGE = 2 };
 enum ColKind : int32_t { COL_FIXED = 0, COL_BOOL = 1, COL_BINARY = 2 };
 
 // Static description of the split, copied to the device once at make.
@@ -42,7 +47,7 @@ struct SchemaDesc {
   int32_t n_str;       // binary columns
   int32_t n_keys;
   int32_t prefer_spill;
-  int32_t pad0;
+  int32_t partitioner;  // Partitioner
   uint64_t quirk_mask;  // array columns a with array_idx_[a] < fixed_width_col_cnt_ (splitter.cc:878-886)
   uint64_t pmod_magic;  // floor((2^64 - 1) / P) + 1, for the pmod without a divide
   int32_t key_col[kMaxKeys];
@@ -75,6 +80,7 @@ struct HostCopy {
 constexpr int32_t kErrEmitOverflow = 1;
 constexpr int32_t kErrBadOffsets = 2;
 constexpr int32_t kErrTimeout = 4;  // a bounded wait in a kernel gave up
+constexpr int32_t kErrBadPid = 8;   // a range partition id is negative or >= P
 
 struct BatchDesc {
   uint32_t nrows;
@@ -140,7 +146,7 @@ struct FlushDesc {
   uint32_t* emit;        // [emit_cap][kEmitFixedWords + n_str]
   uint32_t* emit_count;  // [1]
   uint32_t emit_cap;
-  uint32_t pad1;
+  uint32_t rr_base;      // round-robin selection at the pass's first row (pid_selection_)
   uint32_t* call_flags;  // [n_batches] 1 when some partition ran CalculateSplitBatchSize
   uint32_t* rec_idx;     // [n_batches][P] 1 + emission record index when a segment was cut
   unsigned long long* hn;   // [n_batches] columns with nulls in the batch

@@ -2,6 +2,7 @@
 //
 // Reference behaviour restated here (native-sql-engine/cpp/src/shuffle/splitter.cc):
 //   hash chain + pmod + histogram          HashSplitter::ComputeAndCountPartitionId :1440-1470
+//   round-robin / range partition ids      RoundRobinSplitter :1379-1387, FallbackRangeSplitter :1499-1519
 //   buffer policy / emission / validity    DoSplit :855-938, AllocatePartitionBuffers :610-713,
 //                                          SplitValidityBuffer :1179-1207
 //   stable scatter                         DoSplit :859-874 + Split*Buffer :939-1303
@@ -132,7 +133,9 @@ __global__ void __launch_bounds__(kHashThreads) k_hash_count(const SchemaDesc sd
   }
   __syncthreads();
   const unsigned long long M = sd.pmod_magic;
+  const int part = sd.partitioner;
   bool bad = false;
+  bool bad_pid = false;
   // tile by tile; before every tile after the first, the counts so far are the tile's prefix
   for (uint32_t t0 = 0; t0 < tile.nrows; t0 += kTileRows) {
   if (t0 > 0 && fd.tilepre != nullptr) {
@@ -192,6 +195,11 @@ __global__ void __launch_bounds__(kHashThreads) k_hash_count(const SchemaDesc sd
         }
       }
     }
+    if (part == PART_RANGE) {  // the values are the partition ids; their validity is not read
+#pragma unroll
+      for (int u = 0; u < kHashRows; u++) h[u] = (int32_t)v[u];
+      continue;
+    }
 #pragma unroll
     for (int u = 0; u < kHashRows; u++) valid[u] = c.validity == nullptr || get_bit(c.validity, rr[u]);
 #pragma unroll
@@ -201,7 +209,18 @@ __global__ void __launch_bounds__(kHashThreads) k_hash_count(const SchemaDesc sd
   uint32_t p[kHashRows];
 #pragma unroll
   for (int u = 0; u < kHashRows; u++) {
-    p[u] = fast_pmod(h[u], (uint32_t)P, M);
+    if (part == PART_HASH) {
+      p[u] = fast_pmod(h[u], (uint32_t)P, M);
+    } else if (part == PART_RR) {
+      // the selection runs on from row to row and batch to batch, wrapping at P
+      p[u] = fastmod_u32(fd.rr_base + tile.frow0 + i0 + u, (uint32_t)P, M);
+    } else {
+      p[u] = (uint32_t)h[u];
+      if (p[u] >= (uint32_t)P) {  // negative or too large: the batch is rejected
+        bad_pid |= act[u];
+        p[u] = 0;
+      }
+    }
     if (act[u]) {
       fd.pids[tile.frow0 + i0 + u] = (uint16_t)p[u];
       atomicAdd(&H[p[u]], 1u);
@@ -240,6 +259,7 @@ __global__ void __launch_bounds__(kHashThreads) k_hash_count(const SchemaDesc sd
   }
   }
   if (bad) atomicOr(fd.err, kErrBadOffsets);  // k_scatter then copies nothing
+  if (bad_pid) atomicOr(fd.err, kErrBadPid);
 
   // null counts of this segment's slice of every column (GetNullCount of the batch = sum): one
   // warp per column, 32 rows per 4-byte word when the slice is word aligned, else byte by byte
@@ -975,7 +995,7 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
     mbar_init(&cfull, 1);
     mbar_init(&cempty, kW);
     // inputs rejected by k_hash_count: copy nothing (read once, so the whole block agrees)
-    s_bad = (*reinterpret_cast<volatile int32_t*>(fd.err) & kErrBadOffsets) != 0;
+    s_bad = (*reinterpret_cast<volatile int32_t*>(fd.err) & (kErrBadOffsets | kErrBadPid)) != 0;
     fence_mbar_init();
   }
   __syncthreads();  // the last barrier of the whole block: the issuing warp leaves early

@@ -77,12 +77,25 @@ Status Splitter::Make(const std::string& short_name, std::vector<Field> fields, 
 
 Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, int32_t P,
                       std::vector<int32_t> keys, const GzSplitOptions& opts) {
-  if (short_name != "hash") {
-    if (short_name == "rr" || short_name == "range" || short_name == "single")
-      return Status::Error(GZ_NOT_IMPLEMENTED,
-                           "Partitioning " + short_name + " is not implemented by the GPU splitter");
+  // Splitter::Make (splitter.cc:190-208): "single" is round-robin over one partition; the
+  // round-robin and range partitioners take no key expressions
+  if (short_name == "hash") {
+    partitioner_ = PART_HASH;
+  } else if (short_name == "rr" || short_name == "single") {
+    partitioner_ = PART_RR;
+    if (short_name == "single") P = 1;
+    keys.clear();
+  } else if (short_name == "range") {
+    // FallbackRangeSplitter::Init (splitter.cc:1486-1490): field 0 holds the partition ids and
+    // the output schema is the input schema without it
+    partitioner_ = PART_RANGE;
+    if (fields.empty()) return Status::Error(GZ_INVALID, "range partitioning needs a partition id field");
+    pid_field_ = 0;
+    keys.assign(1, 0);
+  } else {
     return Status::Error(GZ_NOT_IMPLEMENTED, "Partitioning " + short_name + " not supported yet.");
   }
+  short_name_ = short_name;
   if (P <= 0 || P > 64 * 1024) return Status::Error(GZ_INVALID, "num_partitions must be in [1, 65536]");
   opts_ = opts;
   if (opts_.buffer_size <= 0) opts_.buffer_size = 4096;
@@ -99,7 +112,7 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
   // pass size and segment length: given, else the autotuner's choice for this schema
   if (opts_.flush_bytes <= 0 || opts_.seg_tiles <= 0) {
     TuneChoice tc;
-    if (TuneLookup(SchemaSignature(fields_, keys_, P_), &tc)) {
+    if (TuneLookup(SchemaSignature(short_name_, fields_, keys_, P_), &tc)) {
       if (opts_.flush_bytes <= 0) opts_.flush_bytes = tc.flush_bytes;
       if (opts_.seg_tiles <= 0) opts_.seg_tiles = tc.seg_tiles;
     }
@@ -113,6 +126,7 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
   field_array_.assign(fields_.size(), -1);
   for (size_t i = 0; i < fields_.size(); i++) {
     const int t = fields_[i].type;
+    if ((int)i == pid_field_) continue;  // not an output column
     if (IsBinary(t)) bin.push_back((int32_t)i);
     else if (t == GZ_TYPE_NULL) continue;
     else if (t == GZ_TYPE_BOOL || ByteWidth(t) > 0) array_idx_.push_back((int32_t)i);
@@ -135,6 +149,7 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
   sd_.n_str = n_str_;
   sd_.n_keys = (int32_t)keys_.size();
   sd_.prefer_spill = opts_.prefer_spill ? 1 : 0;
+  sd_.partitioner = partitioner_;
   sd_.pmod_magic = P_ > 1 ? UINT64_MAX / (uint64_t)P_ + 1 : 0;
   for (int a = 0; a < n_array_; a++) {
     const int ci = array_idx_[a];
@@ -144,7 +159,8 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
     sd_.arr_kind[a] = IsBinary(t) ? COL_BINARY : t == GZ_TYPE_BOOL ? COL_BOOL : COL_FIXED;
     sd_.arr_width[a] = ByteWidth(t);
     sd_.arr_str[a] = a >= fixed_cnt_ ? a - fixed_cnt_ : -1;
-    if (ci < fixed_cnt_) sd_.quirk_mask |= 1ull << a;
+    // compared as an index of the output schema (the range partitioner's ids are not in it)
+    if (ci - out_shift() < fixed_cnt_) sd_.quirk_mask |= 1ull << a;
   }
   // k_scatter processing order: binary columns spread evenly among the fixed ones, so the
   // characters of the next binary column stream in while fixed columns are scattered
@@ -167,12 +183,13 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
   if ((size_t)(1 + n_str_) * P_ * 4 > kHistSmemBytes) seg_tiles_ = 1;
   else if (opts_.seg_tiles > 0) seg_tiles_ = (uint32_t)opts_.seg_tiles;
   else seg_tiles_ = P_ >= 1024 ? (uint32_t)kMaxSegTiles : 4u;
-  // hash chain (HashSplitter::CreateProjector, splitter.cc:1402-1438)
+  // hash chain (HashSplitter::CreateProjector, splitter.cc:1402-1438); the range partitioner's
+  // one "key" is its id column, read as int32 values (a wrong type fails every Split)
   for (size_t k = 0; k < keys_.size(); k++) {
     const int ci = keys_[k];
     if (ci < 0 || ci >= (int)fields_.size()) return Status::Error(GZ_INVALID, "key column out of range");
     int kind;
-    switch (fields_[ci].type) {
+    switch (partitioner_ == PART_RANGE ? GZ_TYPE_INT32 : fields_[ci].type) {
       case GZ_TYPE_BOOL: kind = KEY_BOOL; break;
       case GZ_TYPE_INT8: kind = KEY_I8; break;
       case GZ_TYPE_INT16: kind = KEY_I16; break;
@@ -324,7 +341,7 @@ uint32_t Splitter::SplitBatchSize(int32_t num_rows, const std::vector<const int3
   for (int k = 0; k < n_str_; k++) size_per_row += (uint32_t)empirical_[k];
   for (int a = 0; a < n_array_; a++) {
     const int ci = array_idx_[a];
-    if (ci < fixed_cnt_) {
+    if (ci - out_shift() < fixed_cnt_) {  // an index of the output schema, as in the reference
       const int t = fields_[ci].type;
       size_per_row += t == GZ_TYPE_BOOL ? 0 : ByteWidth(t);
     }
@@ -426,6 +443,17 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
     const int b0 = field_buf0_[f];
     need_[b0] = Need{nullptr, 0};
     need_[b0 + 1] = Need{nullptr, 0};
+    if ((int)f == pid_field_) {
+      // FallbackRangeSplitter::ComputeAndCountPartitionId (splitter.cc:1499-1516): int32 ids,
+      // validity not read
+      if (fields_[f].type != GZ_TYPE_INT32)
+        return Status::Error(GZ_INVALID, "RecordBatch field 0 should be int32");
+      const size_t vbytes = (size_t)nr * 4;
+      if (addrs[b0 + 1] == 0 || (size_t)sizes[b0 + 1] < vbytes)
+        return Status::Error(GZ_INVALID, "partition id buffer too small");
+      need_[b0 + 1] = Need{reinterpret_cast<const uint8_t*>(addrs[b0 + 1]), vbytes};
+      continue;
+    }
     const int a = field_array_[f];
     if (a < 0) continue;  // null type: buffers ignored
     const int t = fields_[f].type;
@@ -543,7 +571,7 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
     for (size_t f = 0; f < C; f++) {
       ColPtr cp{nullptr, nullptr, nullptr, 0};
       const int a = field_array_[f];
-      if (a >= 0) {
+      if (a >= 0 || (int)f == pid_field_) {
         const int t = fields_[f].type;
         const int b0 = field_buf0_[f];
         const int nbuf = IsBinary(t) ? 3 : 2;
@@ -589,7 +617,7 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
     for (size_t f = 0; f < C; f++) {
       ColPtr cp{nullptr, nullptr, nullptr, 0};
       const int a = field_array_[f];
-      if (a >= 0) {
+      if (a >= 0 || (int)f == pid_field_) {
         const int t = fields_[f].type;
         const int b0 = field_buf0_[f];
         if (need_[b0].bytes) cp.validity = need_[b0].src;
@@ -839,6 +867,8 @@ Status Splitter::Flush() {
   fd.st_sb = st_sb_;
   fd.st_ihn = st_ihn_;
   fd.err = d_err_;
+  fd.rr_base = rr_sel_;
+  rr_sel_ = (uint32_t)((rr_sel_ + R) % (uint64_t)P);
 
   // tables into staging (host inputs) or a pinned table buffer
   uint8_t* htab;
@@ -1052,6 +1082,8 @@ Status Splitter::SyncAndCheck() {
   if (err & kErrTimeout) return Status::Error(GZ_TIMEOUT, "a device-side wait timed out");
   if (err & kErrBadOffsets)
     return Status::Error(GZ_INVALID, "binary offsets are decreasing or exceed the value buffer");
+  if (err & kErrBadPid)
+    return Status::Error(GZ_INVALID, "a partition id is negative or not less than num_partitions");
   if (err) return Status::Error(GZ_CUDA, "device emission list overflow");
   for (; timed_flushes_ < flushes_.size() && flushes_[timed_flushes_].launched; timed_flushes_++) {
     FlushRec& f = flushes_[timed_flushes_];
@@ -1168,6 +1200,7 @@ Status Splitter::AssembleAndWrite(int p, Segment& s, ByteSink* sink, bool count_
   };
 
   for (size_t fi = 0; fi < fields_.size(); fi++) {
+    if ((int)fi == pid_field_) continue;  // not in the output schema
     const int a = field_array_[fi];
     if (a < 0) {
       nodes.push_back(FieldNodeMeta{n, n});
@@ -1303,7 +1336,9 @@ Status Splitter::Stop() {
   int64_t compress_ns = 0;
   // the schema message written before every partition with rows (WriteSchemaPayload,
   // splitter.cc:88-90, 145-151)
-  const std::vector<uint8_t> schema_msg = opts_.write_schema ? EncodeSchemaMessage(fields_) : std::vector<uint8_t>();
+  std::vector<Field> out_fields = fields_;
+  if (pid_field_ >= 0) out_fields.erase(out_fields.begin() + pid_field_);
+  const std::vector<uint8_t> schema_msg = opts_.write_schema ? EncodeSchemaMessage(out_fields) : std::vector<uint8_t>();
   for (int p = 0; p < P_; p++) {
     auto& segs = segments_[p];
     if (segs.empty()) {

@@ -155,9 +155,15 @@ class Splitter {
                           bool* complete);
 
   // schema
-  std::vector<Field> fields_;
+  std::vector<Field> fields_;  // the input schema (the range partitioner's id field included)
   int32_t P_ = 0;
   std::vector<int32_t> keys_;
+  std::string short_name_;
+  int32_t partitioner_ = PART_HASH;
+  int32_t pid_field_ = -1;  // range: the partition id field (0), not an output column
+  uint32_t rr_sel_ = 0;     // round-robin selection at the next pass's first row
+  // input field index minus this = output schema index
+  int32_t out_shift() const { return pid_field_ >= 0 ? 1 : 0; }
   GzSplitOptions opts_{};
   std::string data_file_;
   SchemaDesc sd_{};

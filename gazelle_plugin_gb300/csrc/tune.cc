@@ -49,11 +49,14 @@ void LoadEnvOnce(Cache& c) {
 
 }  // namespace
 
-std::string SchemaSignature(const std::vector<Field>& fields, const std::vector<int32_t>& keys, int32_t P) {
-  std::string s = "t=";
+std::string SchemaSignature(const std::string& short_name, const std::vector<Field>& fields,
+                            const std::vector<int32_t>& keys, int32_t P) {
+  const bool hash = short_name == "hash";
+  if (short_name == "single") P = 1;  // whatever count was asked for
+  std::string s = hash ? "t=" : "m=" + short_name + ";t=";
   for (size_t i = 0; i < fields.size(); i++) s += (i ? "," : "") + std::to_string(fields[i].type);
   s += ";k=";
-  for (size_t i = 0; i < keys.size(); i++) s += (i ? "," : "") + std::to_string(keys[i]);
+  for (size_t i = 0; hash && i < keys.size(); i++) s += (i ? "," : "") + std::to_string(keys[i]);
   s += ";P=" + std::to_string(P);
   return s;
 }

@@ -26,7 +26,10 @@ struct TuneChoice {
   double gbs = 0;  // input GB/s of the sample at this choice
 };
 
-std::string SchemaSignature(const std::vector<Field>& fields, const std::vector<int32_t>& keys, int32_t P);
+// Cache key of a split: field types, key columns and partition count; partitioners other than
+// "hash" are named in front and their keys dropped (they take none).
+std::string SchemaSignature(const std::string& short_name, const std::vector<Field>& fields,
+                            const std::vector<int32_t>& keys, int32_t P);
 bool TuneLookup(const std::string& signature, TuneChoice* out);
 void TuneStore(const std::string& signature, const TuneChoice& choice);
 Status TuneSave(const std::string& path);

@@ -223,9 +223,12 @@ class SplitResult:
 @dataclasses.dataclass
 class NativePartitioning:
     """NativePartitioning.java: short name, partition count, Arrow IPC schema bytes and the
-    hash keys.  The keys are schema column indices (the field-reference expressions Spark
-    sends, ColumnarShuffleExchangeExec.scala:307-326).  ``fields`` may stand in for the
-    schema bytes (a list of gazelle_plugin_gb300.workloads.Field)."""
+    hash keys.  Short names as Splitter::Make takes them (splitter.cc:190-208): "hash" (by the
+    key columns), "rr" (round-robin), "single" (one partition, whatever the count) and
+    "range" (int32 partition ids in schema field 0, which the output leaves out).  The keys are
+    schema column indices (the field-reference expressions Spark sends,
+    ColumnarShuffleExchangeExec.scala:307-326); the other partitioners ignore them.  ``fields``
+    may stand in for the schema bytes (a list of gazelle_plugin_gb300.workloads.Field)."""
     shortName: str
     numPartitions: int
     schema: Optional[bytes] = None
@@ -235,6 +238,9 @@ class NativePartitioning:
 
 class ShuffleSplitterJniWrapper:
     """Method-for-method mirror of ShuffleSplitterJniWrapper.java."""
+
+    def __init__(self):
+        self._partitions = {}  # handle -> partition count (the length of its SplitResult arrays)
 
     def make(self, part: NativePartitioning, offheapPerTask: int = 0, bufferSize: int = 4096,
              codec: Optional[str] = None, batchCompressThreshold: int = 256,
@@ -256,7 +262,7 @@ class ShuffleSplitterJniWrapper:
                                             len(part.fields), keys.ctypes.data, len(keys),
                                             ctypes.byref(o), ctypes.byref(h))
         _check(st, 0)
-        self._partitions = {h.value: part.numPartitions}
+        self._partitions[h.value] = 1 if part.shortName == "single" else part.numPartitions
         return h.value
 
     def nativeSpill(self, splitterId: int, size: int, callBySelf: bool = False) -> int:
@@ -336,10 +342,10 @@ class ShuffleSplitterJniWrapper:
 
 
 def split_batches(schema, batches, num_partitions: int, key_cols: Sequence[int],
-                  **make_kwargs):
+                  shortName: str = "hash", **make_kwargs):
     """Make -> Split every batch -> Stop through the C ABI; returns (SplitResult, data)."""
     w = ShuffleSplitterJniWrapper()
-    h = w.make(NativePartitioning("hash", num_partitions, None, key_cols, list(schema)),
+    h = w.make(NativePartitioning(shortName, num_partitions, None, key_cols, list(schema)),
                **make_kwargs)
     try:
         for b in batches:
@@ -357,7 +363,8 @@ class GzTuneResult(ctypes.Structure):
                 ("best_gbs", ctypes.c_double), ("default_gbs", ctypes.c_double)]
 
 
-def autotune(schema, num_partitions: int, key_cols: Sequence[int], batches, **make_kwargs) -> dict:
+def autotune(schema, num_partitions: int, key_cols: Sequence[int], batches, shortName: str = "hash",
+             **make_kwargs) -> dict:
     """gz_autotune over sample batches (workloads.Batch, host memory unless input_kind says
     otherwise): times candidate pass sizes and segment lengths and caches the fastest for this
     schema, key columns and partition count; splitters made afterwards with flush_bytes=0 and
@@ -370,7 +377,7 @@ def autotune(schema, num_partitions: int, key_cols: Sequence[int], batches, **ma
     addrs = np.ascontiguousarray(np.stack([a for a, _ in pairs]), dtype=np.int64)
     sizes = np.ascontiguousarray(np.stack([z for _, z in pairs]), dtype=np.int64)
     r = GzTuneResult()
-    _check(lib().gz_autotune(b"hash", num_partitions, arr, len(schema), keys.ctypes.data, len(keys),
+    _check(lib().gz_autotune(shortName.encode(), num_partitions, arr, len(schema), keys.ctypes.data, len(keys),
                              ctypes.byref(o), len(batches), rows.ctypes.data, addrs.ctypes.data,
                              sizes.ctypes.data, addrs.shape[1], ctypes.byref(r)), 0)
     return {"flush_bytes": r.flush_bytes, "seg_tiles": r.seg_tiles, "runs": r.runs,
@@ -403,13 +410,14 @@ class ServeLoop:
         self.handle = h.value
         self._keep = {}
 
-    def open(self, schema, numPartitions: int, keyColumns: Sequence[int], **make_kwargs) -> int:
+    def open(self, schema, numPartitions: int, keyColumns: Sequence[int], shortName: str = "hash",
+             **make_kwargs) -> int:
         """Blocks until the HBM budget admits the task; returns its splitter handle."""
         o, keep = split_options(**make_kwargs)
         arr, names = _fields(schema)
         keys = np.asarray(list(keyColumns), np.int32)
         t = ctypes.c_int64(0)
-        _check(lib().gz_serve_open(self.handle, b"hash", numPartitions, arr, len(schema), keys.ctypes.data,
+        _check(lib().gz_serve_open(self.handle, shortName.encode(), numPartitions, arr, len(schema), keys.ctypes.data,
                                    len(keys), ctypes.byref(o), ctypes.byref(t)), 0)
         self._keep[t.value] = (keep, names)
         return t.value

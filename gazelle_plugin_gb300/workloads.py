@@ -279,3 +279,16 @@ def random_batch(rng, schema: Sequence[Field], n: int, null_frac: float) -> Batc
             hi = 2 ** (8 * w - 1) if w < 8 else 2**62
             bufs += _column(rng, f, n, rng.integers(-hi if f.type[0] != "u" else 0, hi, size=n), nf)
     return Batch(n, bufs)
+
+
+def with_partition_ids(schema: Sequence[Field], batches: Sequence[Batch], pids) -> tuple:
+    """The range partitioner's input (FallbackRangeSplitter, splitter.cc:1486-1519): int32
+    partition ids as schema field 0, in front of ``schema`` and of every batch's buffers.
+    ``pids[i]`` holds batch i's ids; an id's validity is never read, so the column has none."""
+    s = [Field("pid", "int32", False)] + list(schema)
+    out = []
+    for b, p in zip(batches, pids):
+        p = np.ascontiguousarray(p, dtype=np.int32)
+        assert p.shape == (b.num_rows,)
+        out.append(Batch(b.num_rows, [np.zeros(0, np.uint8), p] + list(b.buffers)))
+    return s, out

@@ -114,7 +114,12 @@ typedef struct GzSplitResult {
 void gz_split_default_options(GzSplitOptions* opts);
 
 /* Replaces ShuffleSplitterJniWrapper.nativeMake (jni_wrapper.cc:1031-1134).
- * `short_name`: "hash" (other partitioners return GZ_NOT_IMPLEMENTED).
+ * `short_name` (Splitter::Make, splitter.cc:190-208): "hash" (by `key_cols`), "rr"
+ * (round-robin, the selection carried from batch to batch), "single" (one partition, whatever
+ * `num_partitions` says; Stop fills one length), "range" (FallbackRangeSplitter: schema field 0
+ * holds int32 partition ids, left out of the output; an id < 0 or >= num_partitions fails the
+ * split with GZ_INVALID, reported by the next synchronising call); "rr", "single" and "range"
+ * ignore `key_cols`.  Any other name returns GZ_NOT_IMPLEMENTED.
  * `schema_ipc`: Arrow IPC encapsulated Schema message (what MakeSchema reads,
  * jni_common.h:393-406).  `key_cols`: schema indices of the hash keys, in order; they stand
  * for the gandiva field-reference expressions (ColumnarShuffleExchangeExec.scala:307-326). */

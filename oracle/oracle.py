@@ -1,7 +1,8 @@
 """ORACLE - test infrastructure only.
 
 ctypes front-ends for
-  * ``libgz_oracle.so``  - the CPU restatement of the reference hash Splitter
+  * ``libgz_oracle.so``  - the CPU restatement of the reference Splitter (hash, rr, single,
+    range partitioning)
     (oracle/split_oracle.cc); travels everywhere, built by ``build()``;
   * ``_ref/libgzref_splitter.so`` - the reference Splitter itself compiled from the
     reference tree (oracle/ref/Makefile); exists only where the reference sources and
@@ -59,9 +60,10 @@ class SplitOutput:
 
 
 class OracleSplitter:
-    """Restated reference Splitter (hash partitioning, compression off).  With write_schema the
-    schema message is serialised by Arrow itself (pyarrow), as the reference's GetSchemaPayload
-    does."""
+    """Restated reference Splitter (compression off), partitioned by ``short_name``: "hash"
+    (the key columns), "rr", "single" or "range" (int32 partition ids in schema field 0, which
+    the output leaves out).  With write_schema the schema message is serialised by Arrow itself
+    (pyarrow), as the reference's GetSchemaPayload does."""
 
     _lib = None
 
@@ -70,7 +72,7 @@ class OracleSplitter:
         if cls._lib is None:
             lib = ctypes.CDLL(build_oracle())
             lib.gzo_make.restype = ctypes.c_void_p
-            lib.gzo_make.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+            lib.gzo_make.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                                      ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64,
                                      ctypes.c_int32, ctypes.c_int32, ctypes.c_char_p,
                                      ctypes.c_int]
@@ -100,18 +102,19 @@ class OracleSplitter:
 
     def __init__(self, schema, num_partitions: int, key_cols: Sequence[int],
                  offheap_per_task: int = 0, buffer_size: int = 4096, prefer_spill: bool = True,
-                 write_schema: bool = False):
-        self.P = num_partitions
+                 write_schema: bool = False, short_name: str = "hash"):
+        self.P = 1 if short_name == "single" else num_partitions
         types = np.array([f.code for f in schema], np.int32)
         keys = np.array(key_cols, np.int32)
         err = ctypes.create_string_buffer(512)
-        self.h = self.lib().gzo_make(types.ctypes.data, len(types), num_partitions,
-                                     keys.ctypes.data, len(keys), offheap_per_task,
-                                     buffer_size, int(prefer_spill), err, 512)
+        self.h = self.lib().gzo_make(short_name.encode(), types.ctypes.data, len(types),
+                                     num_partitions, keys.ctypes.data, len(keys),
+                                     offheap_per_task, buffer_size, int(prefer_spill), err, 512)
         if not self.h:
             raise ValueError(err.value.decode())
         if write_schema:
-            msg = to_pyarrow_schema(schema).serialize().to_pybytes()
+            out_schema = list(schema)[1:] if short_name == "range" else schema
+            msg = to_pyarrow_schema(out_schema).serialize().to_pybytes()
             self.lib().gzo_set_schema_message(self.h, msg, len(msg))
 
     def split(self, batch) -> None:
@@ -205,7 +208,7 @@ class RefSplitter:
         if cls._lib is None:
             lib = ctypes.CDLL(REF_SO)
             lib.gzref_make.restype = ctypes.c_void_p
-            lib.gzref_make.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32,
+            lib.gzref_make.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32,
                                        ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64,
                                        ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                        ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
@@ -226,15 +229,15 @@ class RefSplitter:
 
     def __init__(self, schema, num_partitions: int, key_cols: Sequence[int],
                  offheap_per_task: int = 0, buffer_size: int = 4096, prefer_spill: bool = True,
-                 write_schema: bool = False):
-        self.P = num_partitions
+                 write_schema: bool = False, short_name: str = "hash"):
+        self.P = 1 if short_name == "single" else num_partitions
         self.tmp = tempfile.TemporaryDirectory(prefix="gzref-")
         self.data_file = os.path.join(self.tmp.name, "data")
         sbytes = to_pyarrow_schema(schema).serialize().to_pybytes()
         self._sbuf = ctypes.create_string_buffer(sbytes, len(sbytes))
         keys = np.array(key_cols, np.int32)
         err = ctypes.create_string_buffer(512)
-        self.h = self.lib().gzref_make(self._sbuf, len(sbytes), num_partitions,
+        self.h = self.lib().gzref_make(short_name.encode(), self._sbuf, len(sbytes), num_partitions,
                                        keys.ctypes.data, len(keys), offheap_per_task,
                                        buffer_size, int(prefer_spill), int(write_schema),
                                        self.data_file.encode(),

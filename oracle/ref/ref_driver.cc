@@ -78,7 +78,8 @@ arrow::Status WrapBatch(const std::shared_ptr<arrow::Schema>& schema, int32_t nu
 
 extern "C" {
 
-void* gzref_make(const uint8_t* schema_ipc, int64_t schema_len, int32_t num_partitions,
+void* gzref_make(const char* short_name, const uint8_t* schema_ipc, int64_t schema_len,
+                 int32_t num_partitions,
                  const int32_t* key_cols, int32_t n_keys, int64_t offheap_per_task,
                  int32_t buffer_size, int32_t prefer_spill, int32_t write_schema,
                  const char* data_file, const char* local_dirs, char* err, int errlen) {
@@ -106,7 +107,8 @@ void* gzref_make(const uint8_t* schema_ipc, int64_t schema_len, int32_t num_part
   opts.write_schema = write_schema != 0;
   opts.buffered_write = true;
   opts.data_file = data_file ? data_file : "";
-  auto maybe = Splitter::Make("hash", schema, num_partitions, exprs, std::move(opts));
+  auto maybe = Splitter::Make(short_name ? short_name : "hash", schema, num_partitions, exprs,
+                              std::move(opts));
   if (!maybe.ok()) {
     SetErr(maybe.status(), err, errlen);
     return nullptr;

@@ -1,12 +1,15 @@
 /*
  * ORACLE — test infrastructure only.  A plain, row-at-a-time CPU restatement of the
- * reference hash Splitter (native-sql-engine/cpp/src/shuffle/splitter.{h,cc}), used by
+ * reference Splitter (native-sql-engine/cpp/src/shuffle/splitter.{h,cc}), used by
  * tests/, the smoke check and bench.py's CPU-baseline leg to check the CUDA product.
  * It is never linked into, loaded by or called from the product library.
  *
  * What it restates (reference file:line in native-sql-engine/cpp/src/shuffle/):
  *   Init: column classification fixed-then-binary, P <= 64K, buffer_size <= 32K  splitter.cc:216-335
+ *   Splitter::Make partitioners hash / rr / single / range                      splitter.cc:190-208
  *   hash chain (seed 42, Spark Murmur3, nulls pass the seed) + pmod + histogram  splitter.cc:1402-1470
+ *   round-robin pid_selection_ carried across batches (single = rr over 1)      splitter.cc:1379-1387
+ *   range: int32 partition ids in input field 0, which leaves the output schema splitter.cc:1486-1519
  *   DoSplit: sticky input_has_null_ quirk, per-pid prepare/emit/spill policy     splitter.cc:855-938
  *   CalculateSplitBatchSize (empirical binary sizes, offheap rule)               splitter.cc:800-853
  *   AllocatePartitionBuffers (validity iff input_has_null_, 0xff fill)           splitter.cc:610-713
@@ -223,7 +226,11 @@ struct InCol {
   int64_t null_count = 0;
 };
 
+// Splitter::Make short names (splitter.cc:190-208); "single" is round-robin over one partition.
+enum Mode { M_HASH = 0, M_RR = 1, M_RANGE = 2 };
+
 struct Options {
+  int mode = M_HASH;
   int64_t offheap_per_task = 0;
   int32_t buffer_size = 4096;
   int32_t batch_compress_threshold = 256;
@@ -247,6 +254,14 @@ class OracleSplitter {
       : fields_(std::move(fields)), P_(P), keys_(std::move(keys)), opt_(o) {}
 
   std::string Init() {
+    if (opt_.mode == M_RANGE) {
+      // FallbackRangeSplitter::Init: the output schema is the input schema without field 0
+      // (splitter.cc:1486-1490); field 0 holds the partition ids
+      if (fields_.empty()) return "range partitioning needs a partition id field";
+      in_type0_ = fields_[0].type;
+      fields_.erase(fields_.begin());
+    }
+    if (opt_.mode != M_HASH) keys_.clear();  // rr / range take no key expressions
     if (P_ <= 0 || P_ > 65536) return "num_partitions must be in [1, 65536]";
     if (opt_.buffer_size > 32768) return "buffer_size must be <= 32768";
     std::vector<int> bin;
@@ -287,6 +302,18 @@ class OracleSplitter {
   std::string Split(int32_t n, const int64_t* addrs, const int64_t* sizes, int nbuf) {
     std::vector<InCol> cols(fields_.size());
     int idx = 0;
+    range_pids_ = nullptr;
+    if (opt_.mode == M_RANGE) {
+      // FallbackRangeSplitter::ComputeAndCountPartitionId (splitter.cc:1499-1519): field 0 must
+      // be int32; its values (validity ignored) are the partition ids
+      const int nb0 = IsBinary(in_type0_) ? 3 : 2;
+      if (nbuf < nb0) return "insufficient number of buffers";
+      if (in_type0_ != T_INT32) return "RecordBatch field 0 should be int32";
+      range_pids_ = (const int32_t*)addrs[1];
+      addrs += nb0;
+      sizes += nb0;
+      nbuf -= nb0;
+    }
     for (size_t f = 0; f < fields_.size(); f++) {
       if (fields_[f].type == T_NULL) {
         if (idx + 2 > nbuf) return "insufficient number of buffers";
@@ -311,7 +338,8 @@ class OracleSplitter {
       cols[f] = c;
     }
     auto t0 = std::chrono::steady_clock::now();
-    ComputePid(n, cols);
+    std::string e = ComputePid(n, cols);
+    if (!e.empty()) return e;
     compute_pid_ns_ += std::chrono::duration_cast<std::chrono::nanoseconds>(
                            std::chrono::steady_clock::now() - t0).count();
     return DoSplit(n, cols);
@@ -384,10 +412,33 @@ class OracleSplitter {
   const std::vector<uint16_t>& last_pids() const { return pid_; }
 
  private:
-  // HashSplitter::ComputeAndCountPartitionId (splitter.cc:1440-1470)
-  void ComputePid(int32_t n, const std::vector<InCol>& cols) {
+  // ComputeAndCountPartitionId of the three partitioners
+  std::string ComputePid(int32_t n, const std::vector<InCol>& cols) {
     pid_.assign(n, 0);
     cnt_.assign(P_, 0);
+    if (opt_.mode == M_RR) {
+      // RoundRobinSplitter (splitter.cc:1379-1387): the selection wraps at P and carries over
+      // to the next batch
+      for (int32_t r = 0; r < n; r++) {
+        pid_[r] = (uint16_t)rr_sel_;
+        cnt_[rr_sel_]++;
+        rr_sel_ = rr_sel_ + 1 == P_ ? 0 : rr_sel_ + 1;
+      }
+      return "";
+    }
+    if (opt_.mode == M_RANGE) {
+      // FallbackRangeSplitter (splitter.cc:1508-1516).  An id >= P fails the batch; a negative
+      // id (undefined in the reference, which indexes its counters with it) fails it too
+      for (int32_t r = 0; r < n; r++) {
+        const int32_t p = range_pids_[r];
+        if (p >= P_) return "Partition id " + std::to_string(p) + " is equal or greater than " + std::to_string(P_);
+        if (p < 0) return "Partition id " + std::to_string(p) + " is negative";
+        pid_[r] = (uint16_t)p;
+        cnt_[p]++;
+      }
+      return "";
+    }
+    // HashSplitter::ComputeAndCountPartitionId (splitter.cc:1440-1470)
     for (int32_t r = 0; r < n; r++) {
       int32_t h = 42;
       for (int k : keys_) {
@@ -414,6 +465,7 @@ class OracleSplitter {
       pid_[r] = (uint16_t)p;
       cnt_[p]++;
     }
+    return "";
   }
 
   static int32_t SparkHashBytes(const uint8_t* p, int32_t len, int32_t seed) {
@@ -662,6 +714,9 @@ class OracleSplitter {
   std::vector<bool> writer_, spill_opened_;
   std::vector<int64_t> partition_lengths_, raw_lengths_;
   std::vector<uint16_t> pid_;
+  int32_t rr_sel_ = 0;                   // RoundRobinSplitter::pid_selection_
+  int in_type0_ = T_NULL;                // range: type of input field 0
+  const int32_t* range_pids_ = nullptr;  // range: partition ids of the batch being split
   std::vector<uint32_t> cnt_;
   int64_t bytes_written_ = 0, bytes_spilled_ = 0, compute_pid_ns_ = 0;
 };
@@ -682,13 +737,23 @@ struct Handle {
 
 extern "C" {
 
-/* fields: types[nf] (GZ_TYPE_* codes); keys: column indices; opts: see Options. */
-void* gzo_make(const int32_t* types, int32_t nf, int32_t num_partitions, const int32_t* keys,
-               int32_t n_keys, int64_t offheap_per_task, int32_t buffer_size,
+/* mode: "hash", "rr", "single" or "range" (Splitter::Make); fields: types[nf] (GZ_TYPE_*
+ * codes, the input schema); keys: column indices (hash only); opts: see Options. */
+void* gzo_make(const char* mode, const int32_t* types, int32_t nf, int32_t num_partitions,
+               const int32_t* keys, int32_t n_keys, int64_t offheap_per_task, int32_t buffer_size,
                int32_t prefer_spill, char* err, int errlen) {
   std::vector<Field> fields;
   for (int i = 0; i < nf; i++) fields.push_back({types[i], "f" + std::to_string(i)});
   Options o;
+  const std::string m = mode ? mode : "hash";
+  if (m == "hash") o.mode = M_HASH;
+  else if (m == "rr") o.mode = M_RR;
+  else if (m == "single") o.mode = M_RR, num_partitions = 1;
+  else if (m == "range") o.mode = M_RANGE;
+  else {
+    if (err) snprintf(err, errlen, "Partitioning %s not supported yet.", m.c_str());
+    return nullptr;
+  }
   o.offheap_per_task = offheap_per_task;
   if (buffer_size > 0) o.buffer_size = buffer_size;
   o.prefer_spill = prefer_spill != 0;

@@ -9,7 +9,9 @@ seeded inputs from gazelle_plugin_gb300.workloads, recording for every case the 
 the input buffers, of the whole shuffle data file and of every partition's bytes, plus
 partition_lengths, raw_partition_lengths and bytes spilled.  The reference's own unit-test
 batches (native-sql-engine/cpp/src/tests/shuffle_split_test.cc:186-208) are materialised
-into ref_fixture.npz together with the expected data-file bytes.
+into ref_fixture.npz together with the expected data-file bytes.  partitioners.json records
+the same digests for the round-robin, single and range partitioners (Splitter::Make "rr",
+"single", "range"), on those unit-test batches and on seeded workloads.
 
 The reference hashes through gandiva, which is absent; oracle/ref/stub supplies the same
 Spark Murmur3 chain (oracle/spark_hash.h), so what these fixtures pin is everything after
@@ -51,9 +53,12 @@ def input_digest(batches) -> str:
     return h.hexdigest()
 
 
-def record(name, schema, batches, P, keys, opts, gen):
-    out = O.run_ref(schema, batches, P, keys, **opts)
+def record(name, schema, batches, P, keys, opts, gen, short_name="hash"):
+    out = O.run_ref(schema, batches, P, keys, short_name=short_name, **opts)
+    P = len(out.partition_lengths)
+    rec = {"short_name": short_name} if short_name != "hash" else {}
     return {
+        **rec,
         "name": name,
         "gen": gen,
         "schema": [[f.name, f.type, f.nullable] for f in schema],
@@ -210,6 +215,75 @@ def to_batch(rb) -> W.Batch:
     return W.Batch(rb.num_rows, bufs)
 
 
+# ---------------------------------------------------------------------------------------
+# round-robin / single / range partitioners
+def ref_unit_sequence():
+    """The reference unit-test batches in the order its tests split them ([b1, b2, b1]), read
+    back from ref_fixture.npz (no pyarrow needed)."""
+    z = np.load(os.path.join(HERE, "ref_fixture.npz"))
+    bs = []
+    for i in range(2):
+        nbuf = len([k for k in z.files if k.startswith(f"b{i}_buf")])
+        bs.append(W.Batch(int(z[f"b{i}_rows"][0]), [z[f"b{i}_buf{j}"] for j in range(nbuf)]))
+    return [bs[0], bs[1], bs[0]]
+
+
+def _pids(gen, batches, P):
+    """Partition ids of a range case: 0, 1, 0, 1, ... per batch ("alternate", the reference's
+    TestFallbackRangeSplitter) or seeded uniform draws in [0, P)."""
+    if gen["pids"] == "alternate":
+        return [np.arange(b.num_rows, dtype=np.int32) % 2 for b in batches]
+    rng = np.random.default_rng(gen["pid_seed"])
+    return [rng.integers(0, P, size=b.num_rows).astype(np.int32) for b in batches]
+
+
+def _base_batches(gen):
+    if gen["workload"] == "ref_unit":
+        return REF_FIXTURE_SCHEMA, ref_unit_sequence()
+    if gen["workload"] == "random":
+        schema, batches, _, _, _ = random_case(gen["seed"])
+        return schema, batches
+    schema = {"c1": W.C1_SCHEMA, "c2": W.C2_SCHEMA, "c3": W.C3_SCHEMA}[gen["workload"]]
+    return schema, regenerate({"gen": gen})
+
+
+def partitioner_inputs(short_name, gen, P):
+    """(schema, batches) of a partitioner case; range cases get the id column in front."""
+    schema, batches = _base_batches(gen)
+    if short_name == "range":
+        return W.with_partition_ids(schema, batches, _pids(gen, batches, P))
+    return list(schema), batches
+
+
+def partitioner_cases():
+    """(name, short_name, P, options, generator description)"""
+    # TestSingleSplitter, TestRoundRobinSplitter, TestFallbackRangeSplitter
+    # (shuffle_split_test.cc:210-253, 255-319, 390-472)
+    unit = {"workload": "ref_unit"}
+    yield ("ref_single_b10", "single", 1, {"buffer_size": 10}, unit)
+    yield ("ref_rr_p2_b4", "rr", 2, {"buffer_size": 4}, unit)
+    yield ("ref_range_p2_b4", "range", 2, {"buffer_size": 4}, dict(unit, pids="alternate"))
+    yield ("ref_rr_p3_write_schema", "rr", 3, {"write_schema": True}, unit)
+    yield ("ref_range_p2_write_schema", "range", 2, {"write_schema": True}, dict(unit, pids="alternate"))
+    c1 = {"workload": "c1", "seed": 0, "num_batches": 10, "rows": 4096}
+    c2 = {"workload": "c2", "seed": 1, "num_batches": 6, "rows": 4096}
+    c3 = {"workload": "c3", "seed": 2, "num_batches": 3, "rows": 4096, "null_frac": 0.2,
+          "key_nulls": 0.0}
+    yield ("c1_rr_p8", "rr", 8, {}, c1)
+    yield ("c1_single", "single", 1, {}, c1)
+    yield ("c2_rr_p200", "rr", 200, {}, c2)
+    yield ("c2_range_p200", "range", 200, {}, dict(c2, pids="uniform", pid_seed=11))
+    yield ("c3_range_p2000_buf8", "range", 2000, {"buffer_size": 8}, dict(c3, pids="uniform", pid_seed=12))
+    yield ("c3_rr_p7", "rr", 7, {}, c3)
+    for seed in range(12):
+        _, batches, P, _, opts = random_case(2000 + seed)
+        g = {"workload": "random", "seed": 2000 + seed}
+        if seed % 2:
+            yield (f"random_{seed}_range", "range", P, opts, dict(g, pids="uniform", pid_seed=3000 + seed))
+        else:
+            yield (f"random_{seed}_rr", "rr", P, opts, g)
+
+
 def main():
     ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     if not O.build_ref(ref_root):
@@ -242,6 +316,14 @@ def main():
         json.dump({"schema": [[x.name, x.type, x.nullable] for x in REF_FIXTURE_SCHEMA],
                    "sequence": [0, 1, 0], "runs": meta}, f, indent=1)
     print("ref fixture", [m["tag"] for m in meta])
+
+    precs = []
+    for name, short_name, P, opts, gen in partitioner_cases():
+        schema, batches = partitioner_inputs(short_name, gen, P)
+        precs.append(record(name, schema, batches, P, [], opts, gen, short_name))
+        print(name, precs[-1]["data_sha256"][:16])
+    with open(os.path.join(HERE, "partitioners.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py", "cases": precs}, f, indent=1)
 
 
 if __name__ == "__main__":

@@ -339,8 +339,9 @@ def test_schema_ipc_make():
 
 def test_errors_are_reported_not_crashed():
     w = S.ShuffleSplitterJniWrapper()
-    with pytest.raises(S.SplitterError):
-        w.make(S.NativePartitioning("rr", 4, None, [0], list(W.C1_SCHEMA)))
+    with pytest.raises(S.SplitterError) as e:
+        w.make(S.NativePartitioning("roundrobin", 4, None, [0], list(W.C1_SCHEMA)))
+    assert e.value.status == S.GZ_NOT_IMPLEMENTED
     with pytest.raises(S.SplitterError):
         w.make(S.NativePartitioning("hash", 0, None, [0], list(W.C1_SCHEMA)))
     with pytest.raises(S.SplitterError):
