@@ -18,6 +18,10 @@ Lines:
           the serving loop, per-Split latency) and fanout (Zipf keys, 16..8000 partitions), each
           beside its plain per-batch counterpart where it has one; --no-forms skips them.
 
+--partitioner rr | range times the same table split by the round-robin selection or by an
+int32 partition id column U[0, 200) put in front of it (Splitter::Make "rr" / "range"); the
+headline is hash.
+
 --impl reference times the CPU splitter (the oracle's restatement of the reference
 Splitter; the reference itself needs the Arrow fork and x86) on all host cores, one splitter
 per core over disjoint shards of a bounded sample of the same batches.
