@@ -330,6 +330,16 @@ def cpu_split_sample(batches, threads: int, sch=None, keys=None, partitioner: st
     return wall, in_bytes + out_bytes
 
 
+def single_core(batches, part: dict, n: int = 128) -> dict:
+    """One oracle splitter on one core over the first `n` batches (the 1-core column of the
+    CPU baseline, beside the all-cores figure)."""
+    sub = batches[:n]
+    cpu_split_sample(sub[:8], 1, **part)
+    dt, nb = cpu_split_sample(sub, 1, **part)
+    return {"value": nb / dt / 1e9, "unit": "GB/s", "cores": 1,
+            "sample": f"first {len(sub)} batches x {BATCH_ROWS} rows of the workload"}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -360,7 +370,7 @@ def run_reference(args):
         "data": "synthetic (seeded torch RNG, same distributions)",
         "config": {"workload": workload, "sample": sample},
         "cpu_baseline": {"value": value, "unit": "GB/s", "cores": threads, "kind": "port",
-                         "sample": sample},
+                         "sample": sample, "single_core": single_core(batches, part)},
         "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -768,7 +778,8 @@ def run_gpu(args):
         cpu_split_sample(sample[: threads * 2], threads, **cpart)
         dt, nb = cpu_split_sample(sample, threads, **cpart)
         cpu = {"value": nb / dt / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
-               "sample": f"first {len(sample)} batches x {BATCH_ROWS} rows of the workload"}
+               "sample": f"first {len(sample)} batches x {BATCH_ROWS} rows of the workload",
+               "single_core": single_core(sample, cpart)}
 
     if rank == 0:
         metric, workload = metric_and_workload(args.partitioner)
