@@ -62,7 +62,7 @@ std::shared_ptr<gz::ServeLoop> LookupServer(int64_t id) {
 GzStatus MakeCommon(const char* short_name, int32_t num_partitions, std::vector<gz::Field> fields,
                     const int32_t* key_cols, int32_t n_keys, const GzSplitOptions* opts,
                     int64_t* out_handle, std::shared_ptr<Entry>* out_entry = nullptr) {
-  if (out_handle == nullptr || short_name == nullptr) {
+  if (out_handle == nullptr || short_name == nullptr || (key_cols == nullptr && n_keys > 0)) {
     t_make_error = "null argument";
     return GZ_INVALID;
   }

@@ -159,3 +159,33 @@ def test_schema_message_matches_arrow_writer():
         assert lib.gz_debug_reencode_schema(want, len(want), out.ctypes.data, out.nbytes,
                                             ctypes.byref(n)) == 0
         assert out[: n.value].tobytes() == want, pa.schema(fields)
+
+
+def test_make_rejects_bad_arguments_before_touching_the_device():
+    """Splitter::Make's argument checks (splitter.cc:190-208, 219-221; key types of
+    HashSplitter::CreateProjector) answer before any CUDA call, so they run without a GPU."""
+    from gazelle_plugin_gb300 import workloads as W
+    lib = S.lib()
+    o = S.default_options()
+
+    def make(short_name, P, schema, keys, null_keys=False, **opt):
+        for k, v in opt.items():
+            setattr(o, k, v)
+        arr, names = S._fields(schema)
+        ks = np.asarray(keys, np.int32)
+        h = ctypes.c_int64(0)
+        st = lib.gz_split_make_fields(short_name.encode(), P, arr, len(schema),
+                                      None if null_keys else ks.ctypes.data, len(ks),
+                                      ctypes.byref(o), ctypes.byref(h))
+        o.buffer_size = 4096
+        return st
+
+    c1 = list(W.C1_SCHEMA)
+    assert make("roundrobin", 4, c1, [0]) == S.GZ_NOT_IMPLEMENTED
+    assert make("range", 4, [], []) == S.GZ_INVALID
+    assert make("hash", 0, c1, [0]) == S.GZ_INVALID
+    assert make("hash", 65537, c1, [0]) == S.GZ_INVALID
+    assert make("rr", 4, c1, [], buffer_size=40000) == S.GZ_INVALID
+    assert make("hash", 4, c1, [3]) == S.GZ_NOT_IMPLEMENTED  # utf8 key: no Spark-compatible hash here
+    assert make("hash", 4, c1, [9]) == S.GZ_INVALID          # key column out of range
+    assert make("hash", 4, c1, [0], null_keys=True) == S.GZ_INVALID
