@@ -9,11 +9,17 @@ are generated on the device with a seeded torch RNG (36 GB of inputs, far above 
 L2, so every step reads HBM).
 
 Lines:
-  value : Split of every batch with the inputs resident in HBM (GZ_INPUT_DEVICE_RETAINED),
-          through the C ABI's per-batch loop, until the device work is complete.
-  e2e   : the same through the host-buffer contract (GZ_INPUT_HOST: each batch copied before
-          Split returns), partition data copied back to pinned host memory after every pass.
+  value : the split with the inputs resident in HBM (GZ_INPUT_DEVICE_RETAINED), the batches
+          handed over by gz_split_split_batches (the writer's per-batch loop run inside the
+          library), until the device work is complete.  Explains the kernels; not the drop-in.
+  e2e   : the drop-in as a Spark executor calls it: T map tasks at once (one per host core, as
+          the CPU arm), each a native loop of make / one gz_split_split per 4096-row batch on
+          pageable host buffers / gz_split_stop writing its data file to tmpfs / close
+          (libgztask.so, ColumnarShuffleWriter.write's loop); plus the same with one task.
   metric: (input buffer bytes + raw partition bytes) / time, in GB/s.
+  output check: the e2e data files are digested and compared with the oracle's data files for
+          the same task shards (the CPU baseline leg, which splits the whole workload on all
+          host cores with Stop writing its files too).
   forms : batched (512 uneven batches of 3 schemas, autotuned passes), served (32 tasks through
           the serving loop, per-Split latency) and fanout (Zipf keys, 16..8000 partitions), each
           beside its plain per-batch counterpart where it has one; --no-forms skips them.
@@ -22,9 +28,9 @@ Lines:
 int32 partition id column U[0, 200) put in front of it (Splitter::Make "rr" / "range"); the
 headline is hash.
 
---impl reference times the CPU splitter (the oracle's restatement of the reference
-Splitter; the reference itself needs the Arrow fork and x86) on all host cores, one splitter
-per core over disjoint shards of a bounded sample of the same batches.
+--impl reference times the CPU splitter (the oracle's restatement of the reference Splitter;
+the reference itself needs the Arrow fork and x86) as map tasks on all host cores, split and
+Stop with data files, over a bounded sample of the same batches.
 """
 from __future__ import annotations
 
@@ -47,11 +53,15 @@ WORKLOAD = ("wide fact-table split: 200M rows, 4096-row batches, 16 columns "
             "(4 int64 keys, 4 float64, 2 int32, 3 utf8 flags, 3 utf8 comments), "
             "2% nulls, hash on keys 0-1, 200 partitions")
 BATCH_ROWS = 4096
-# DRAM bytes that one k_scatter launch moves per algorithmic byte, from an ncu capture of one
-# full 1 GiB pass of this workload (5,963,776 rows: 2.228 GB of DRAM traffic for 2.145 GB
-# algorithmic; profiles/k_scatter_wide_fact_table.md).
-K_SCATTER_DRAM_PER_ALG_BYTE = 1.039
 PARTITIONS = 200
+# ncu DRAM traffic of one k_scatter launch of this workload (dram__bytes_read.sum +
+# dram__bytes_write.sum) against its algorithmic bytes, written with the command that made it
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "k_scatter_traffic.json")
+# The restatement runs slower than the reference Splitter itself: measured on one x86 core on
+# 256 batches of this workload, split + Stop with a data file: 0.910 GB/s restated vs 1.120 GB/s
+# for the reference compiled from its sources (split alone 1.103 vs 1.456).  The reference
+# cannot be built on the Arm host (its x86 intrinsics and the Arrow library it links).
+REFERENCE_OVER_PORT = 1.120 / 0.910
 KEYS = [0, 1]
 
 
@@ -192,48 +202,105 @@ def link_bandwidth(nbytes: int = 1 << 30) -> dict:
     return out
 
 
-def host_copy(addrs, sizes, tensors):
-    """Pinned host copies of the generated buffers, laid out like the device ones; returns
-    (host addrs, pinned tensors)."""
+def pageable_copy(addrs, sizes, tensors):
+    """Ordinary (pageable) host copies of the generated buffers, laid out like the device ones:
+    the kind of memory Arrow Java's off-heap buffers live in.  Returns (host addrs, arrays)."""
     import torch
     haddrs = np.zeros_like(addrs)
     keep = []
     for j, t in enumerate(tensors):
         if t is None:
             continue
-        h = torch.empty(t.numel() * t.element_size(), dtype=torch.uint8, pin_memory=True)
-        h.copy_(t.view(-1).view(torch.uint8))
+        h = t.view(-1).view(torch.uint8).cpu().numpy()  # torch's CPU allocator: not pinned
         keep.append(h)
-        haddrs[:, j] = addrs[:, j] - t.data_ptr() + h.data_ptr()
+        haddrs[:, j] = addrs[:, j] - t.data_ptr() + h.ctypes.data
     haddrs[sizes == 0] = 0
     return haddrs, keep
 
 
-def host_batches(rows, addrs, sizes, tensors, first: int, count: int):
-    """Numpy copies of batches [first, first+count) as workloads.Batch objects."""
-    from gazelle_plugin_gb300 import workloads as W
-    cols = []
-    for j, t in enumerate(tensors):
-        if t is None:
-            cols.append(None)
-            continue
-        lo = int(addrs[first, j] - t.data_ptr())
-        last = first + count - 1
-        hi = int(addrs[last, j] - t.data_ptr() + sizes[last, j])
-        cols.append((lo, t.view(-1).view(__import__("torch").uint8)[lo:hi].cpu().numpy()))
-    out = []
-    for b in range(first, first + count):
-        bufs = []
-        for j, c in enumerate(cols):
-            n = int(sizes[b, j])
-            if c is None or n == 0:
-                bufs.append(np.zeros(0, np.uint8))
+def scratch_dir() -> str:
+    """A fresh directory for data files, on tmpfs when the box has one."""
+    import tempfile
+    base = "/dev/shm" if os.path.isdir("/dev/shm") and os.access("/dev/shm", os.W_OK) else None
+    return tempfile.mkdtemp(prefix="gz-bench-", dir=base)
+
+
+def remove_dir(d: str) -> None:
+    import shutil
+    shutil.rmtree(d, ignore_errors=True)
+
+
+def task_files(ddir: str, n: int):
+    return [os.path.join(ddir, f"task-{t:04d}.data") for t in range(n)]
+
+
+def digests(paths):
+    """(checksum, bytes) of every file, computed on all host cores."""
+    from concurrent.futures import ThreadPoolExecutor
+    from gazelle_plugin_gb300 import shuffle as S
+    with ThreadPoolExecutor(max_workers=min(len(paths), os.cpu_count() or 1)) as ex:
+        return list(ex.map(S.digest_file, paths))
+
+
+def oracle_tasks(sch, keys, partitioner, rows, haddrs, sizes, n_tasks: int, ddir: str, digest: bool = False):
+    """The CPU splitter as map tasks: `n_tasks` oracle splitters on their own threads, each over a
+    contiguous range of the batches (the same ranges the GPU tasks take), split then Stop writing
+    <ddir>/task-<t>.data.  Returns (wall seconds, input bytes, raw partition bytes, [per-task
+    partition lengths], [per-task (checksum, size)] or None).  With `digest`, each task checksums
+    and deletes its file after its clock has stopped (keeps host memory low)."""
+    import ctypes
+    from oracle import oracle as O
+    L = O.OracleSplitter.lib()
+    nb = len(rows)
+    rows = np.ascontiguousarray(rows, np.int32)
+    haddrs = np.ascontiguousarray(haddrs, np.int64)
+    sizes = np.ascontiguousarray(sizes, np.int64)
+    nbufs = haddrs.shape[1]
+    paths = task_files(ddir, n_tasks)
+    res = [None] * n_tasks
+    errs = [None] * n_tasks
+    sps = [O.OracleSplitter(sch, PARTITIONS, keys, short_name=partitioner) for _ in range(n_tasks)]
+    barrier = threading.Barrier(n_tasks + 1)
+    a0, z0, row_bytes = haddrs.ctypes.data, sizes.ctypes.data, nbufs * 8
+
+    def work(t):
+        b0, b1 = nb * t // n_tasks, nb * (t + 1) // n_tasks
+        sp = sps[t]
+        P = sp.P
+        err = ctypes.create_string_buffer(512)
+        lengths, raw, m = np.zeros(P, np.int64), np.zeros(P, np.int64), np.zeros(3, np.int64)
+        barrier.wait()
+        for b in range(b0, b1):
+            if rows[b] == 0:
                 continue
-            lo, arr = c
-            s0 = int(addrs[b, j] - tensors[j].data_ptr()) - lo
-            bufs.append(arr[s0:s0 + n].copy())
-        out.append(W.Batch(int(rows[b]), bufs))
-    return out
+            if L.gzo_split(sp.h, int(rows[b]), a0 + b * row_bytes, z0 + b * row_bytes, nbufs, err, 512):
+                errs[t] = err.value.decode()
+                return
+        if L.gzo_stop(sp.h, paths[t].encode(), lengths.ctypes.data, raw.ctypes.data, m.ctypes.data,
+                      err, 512) < 0:
+            errs[t] = err.value.decode()
+            return
+        sp.close()
+        t_end = time.perf_counter()
+        dig = None
+        if digest:
+            from gazelle_plugin_gb300 import shuffle as S
+            dig = S.digest_file(paths[t])
+            os.remove(paths[t])
+        res[t] = (t_end, int(raw.sum()), lengths, dig)
+
+    ths = [threading.Thread(target=work, args=(t,)) for t in range(n_tasks)]
+    for t in ths:
+        t.start()
+    barrier.wait()
+    t0 = time.perf_counter()
+    for t in ths:
+        t.join()
+    if any(r is None for r in res):
+        raise RuntimeError(f"an oracle task failed: {[e for e in errs if e]}")
+    wall = max(r[0] for r in res) - t0
+    return (wall, int(sizes[:nb].sum()), sum(r[1] for r in res), [r[2] for r in res],
+            [r[3] for r in res] if digest else None)
 
 
 # ---------------------------------------------------------------------------------------
@@ -288,6 +355,19 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sms)}
 
 
+def traffic_per_launch(alg_per_launch: float, given=None):
+    """DRAM bytes of one k_scatter launch: given, else the algorithmic bytes of this run's average
+    launch times the DRAM / algorithmic ratio of the committed ncu capture (None without one)."""
+    if given:
+        return given
+    try:
+        with open(TRAFFIC_FILE) as f:
+            t = json.load(f)
+        return alg_per_launch * t["dram_bytes"] / t["algorithmic_bytes"]
+    except (OSError, KeyError, ValueError, ZeroDivisionError):
+        return None
+
+
 def measured_peak_gbs():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -297,71 +377,32 @@ def measured_peak_gbs():
 
 
 # ---------------------------------------------------------------------------------------
-def cpu_split_sample(batches, threads: int, sch=None, keys=None, partitioner: str = "hash"):
-    """Oracle splitters, one per thread over disjoint shards; returns (seconds, bytes)."""
-    from oracle import oracle as O
-    shards = [batches[i::threads] for i in range(threads)]
-    res = [None] * threads
-    sch = schema() if sch is None else sch
-    keys = KEYS if keys is None else keys
-    sp = [O.OracleSplitter(sch, PARTITIONS, keys, short_name=partitioner) for _ in range(threads)]
-    barrier = threading.Barrier(threads + 1)
-
-    def work(i):
-        barrier.wait()
-        t0 = time.perf_counter()
-        for b in shards[i]:
-            sp[i].split(b)
-        res[i] = time.perf_counter() - t0
-
-    ths = [threading.Thread(target=work, args=(i,)) for i in range(threads)]
-    for t in ths:
-        t.start()
-    barrier.wait()
-    t0 = time.perf_counter()
-    for t in ths:
-        t.join()
-    wall = time.perf_counter() - t0
-    out_bytes = 0
-    for s in sp:
-        out_bytes += int(s.stop().raw_partition_lengths.sum())
-        s.close()
-    in_bytes = sum(b.nbytes for b in batches)
-    return wall, in_bytes + out_bytes
-
-
-def single_core(batches, part: dict, n: int = 128) -> dict:
-    """One oracle splitter on one core over the first `n` batches (the 1-core column of the
-    CPU baseline, beside the all-cores figure)."""
-    sub = batches[:n]
-    cpu_split_sample(sub[:8], 1, **part)
-    dt, nb = cpu_split_sample(sub, 1, **part)
-    return {"value": nb / dt / 1e9, "unit": "GB/s", "cores": 1,
-            "sample": f"first {len(sub)} batches x {BATCH_ROWS} rows of the workload"}
-
-
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     import torch
-    threads = os.cpu_count() or 1
-    sch, keys, rows, addrs, sizes, keep = workload_inputs(args.sample_batches * BATCH_ROWS, 1,
-                                                          args.partitioner)
-    batches = host_batches(rows, addrs, sizes, keep, 0, args.sample_batches)
+    threads = args.tasks or min(os.cpu_count() or 1, 16)
+    n_rows = min(args.ref_rows, args.rows)
+    sch, keys, rows, addrs, sizes, keep = workload_inputs(n_rows, 1, args.partitioner)
+    haddrs, host = pageable_copy(addrs, sizes, keep)
     del keep
     torch.cuda.empty_cache()
-    part = dict(sch=sch, keys=keys, partitioner=args.partitioner)
-    for _ in range(args.warmup):
-        cpu_split_sample(batches[: max(threads, len(batches) // 8)], threads, **part)
-    times, nbytes = [], 0
-    for _ in range(args.steps):
-        dt, nb = cpu_split_sample(batches, threads, **part)
-        times.append(dt)
-        nbytes = nb
+    ddir = scratch_dir()
+    try:
+        for _ in range(args.warmup):
+            oracle_tasks(sch, keys, args.partitioner, rows, haddrs, sizes, threads, ddir)
+        times, nbytes = [], 0
+        for _ in range(args.steps):
+            dt, nin, nraw, _, _ = oracle_tasks(sch, keys, args.partitioner, rows, haddrs, sizes, threads, ddir)
+            times.append(dt)
+            nbytes = nin + nraw
+    finally:
+        remove_dir(ddir)
     total = sum(times)
     value = nbytes * args.steps / total / 1e9
-    sample = f"{len(batches)} batches x {BATCH_ROWS} rows of the workload per step"
+    sample = (f"the first {n_rows} rows ({len(rows)} batches) of the workload per step, as {threads} map "
+              f"tasks over contiguous ranges, each split then Stop writing its data file to tmpfs")
     metric, workload = metric_and_workload(args.partitioner)
     line = {
         "impl": "reference", "metric": metric, "value": value, "unit": "GB/s", "n_gpus": args.gpus,
@@ -370,7 +411,9 @@ def run_reference(args):
         "data": "synthetic (seeded torch RNG, same distributions)",
         "config": {"workload": workload, "sample": sample},
         "cpu_baseline": {"value": value, "unit": "GB/s", "cores": threads, "kind": "port",
-                         "sample": sample, "single_core": single_core(batches, part)},
+                         "sample": sample,
+                         "reference_over_port": REFERENCE_OVER_PORT,
+                         "reference_estimate": value * REFERENCE_OVER_PORT},
         "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -702,6 +745,18 @@ def run_gpu(args):
     w.close(h)
     out_bytes = int(res.rawPartitionLengths.sum())
     alg_bytes = in_bytes + out_bytes
+    # Stop again with the pinned pool warm, writing a real data file to tmpfs
+    sdir = scratch_dir()
+    try:
+        h = w.make(part, dataFile=os.path.join(sdir, "stop.data"), **dev_opts)
+        w.splitBatches(h, rows, addrs, sizes)
+        w.sync(h)
+        t0 = time.perf_counter()
+        w.stop(h, PARTITIONS)
+        stop_warm_s = time.perf_counter() - t0
+        w.close(h)
+    finally:
+        remove_dir(sdir)
 
     for _ in range(args.warmup):
         one_step(dev_opts, addrs, sizes)
@@ -732,12 +787,12 @@ def run_gpu(args):
     scat_gbs = alg_bytes / (k_scat / 1e3) / 1e9
     roofline = {"bound": "hbm", "kernel": "k_scatter", "achieved": scat_gbs, "peak": peak,
                 "unit": "GB/s", "frac": scat_gbs / peak, "peak_source": peak_kind,
-                "traffic": (args.traffic_per_launch or
-                            K_SCATTER_DRAM_PER_ALG_BYTE * alg_bytes / max(flushes, 1)),
+                "traffic": traffic_per_launch(alg_bytes / max(flushes, 1), args.traffic_per_launch),
                 "traffic_source": ("--traffic-per-launch" if args.traffic_per_launch else
-                                   "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
-                                   "full 1 GiB pass (2.228 GB for 2.145 GB algorithmic), scaled "
-                                   "to this run's average pass"),
+                                   "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_scatter "
+                                   "launch of this workload (its ratio to that launch's algorithmic "
+                                   "bytes, from the committed capture summary), scaled to this run's "
+                                   "average launch"),
                 "overlap": ("k_scatter of pass i runs after k_hash_count of pass i + 1 on one "
                             "stream, beside the plan kernels of pass i + 1; its duration is the "
                             "live one"),
@@ -745,41 +800,68 @@ def run_gpu(args):
                 "algorithmic_bytes_per_launch": alg_bytes / max(flushes, 1),
                 "avg_launch_ms": k_scat / max(flushes, 1)}
 
-    # -- e2e: host buffers through the JNI-style contract ---------------------------------
+    # -- e2e: the drop-in as an executor's map tasks call it --------------------------------
     e2e = None
+    cpu = None
+    out_check = None
+    tasks = args.tasks or min(os.cpu_count() or 1, 16)
     if not args.no_e2e:
         link = link_bandwidth()
-        haddrs, host = host_copy(addrs, sizes, keep)
-        host_opts = dict(writeSchema=False, input_kind=S.GZ_INPUT_HOST, keep_output_on_device=0,
-                         flush_bytes=args.flush_mb << 20)
-        for _ in range(max(1, args.warmup - 1)):
-            one_step(host_opts, haddrs, sizes)
-        e_stats, e_times = [], []
-        for _ in range(args.steps):
-            barrier()
-            t0 = time.perf_counter()
-            one_step(host_opts, haddrs, sizes, e_stats)
-            barrier()
-            e_times.append(time.perf_counter() - t0)
-        e_t = reduce_over_ranks(sum(e_times), "max")
-        e2e = {"value": alg_all * args.steps / e_t / 1e9, "unit": "GB/s",
-               "h2d_bytes_per_step": int(reduce_over_ranks(statistics.mean(s[6] for s in e_stats), "sum")),
-               "d2h_bytes_per_step": int(reduce_over_ranks(statistics.mean(s[7] for s in e_stats), "sum")),
-               "ms_per_step": e_t / args.steps * 1e3,
-               "link": link}
+        haddrs, host = pageable_copy(addrs, sizes, keep)
+        ddir = scratch_dir()
+        e2e_opts = dict(writeSchema=False, input_kind=S.GZ_INPUT_HOST,
+                        flush_bytes=args.e2e_flush_mb << 20, host_read=args.host_read)
+        try:
+            for _ in range(max(1, args.warmup - 1)):
+                S.run_map_tasks(part, rows, haddrs, sizes, tasks, ddir, **e2e_opts)
+            runs = []
+            for _ in range(args.steps):
+                barrier()
+                runs.append(S.run_map_tasks(part, rows, haddrs, sizes, tasks, ddir, **e2e_opts))
+                barrier()
+            gpu_files = digests(task_files(ddir, tasks))
+            gpu_lengths = runs[-1]["partition_lengths"]
+            remove_dir(ddir)
+            ddir = scratch_dir()
+            one = S.run_map_tasks(part, rows, haddrs, sizes, 1, ddir, **e2e_opts)
+            remove_dir(ddir)
+            ddir = scratch_dir()
+            e_t = reduce_over_ranks(sum(r["wall_s"] for r in runs), "max")
+            e_alg = runs[-1]["input_bytes"] + runs[-1]["raw_partition_bytes"]
+            e2e = {"value": reduce_over_ranks(float(e_alg), "sum") * args.steps / e_t / 1e9, "unit": "GB/s",
+                   "h2d_bytes_per_step": int(reduce_over_ranks(float(runs[-1]["input_bytes"]), "sum")),
+                   "d2h_bytes_per_step": int(reduce_over_ranks(float(runs[-1]["raw_partition_bytes"]), "sum")),
+                   "ms_per_step": e_t / args.steps * 1e3,
+                   "path": (f"{tasks} map tasks at once, each make / gz_split_split per 4096-row batch on "
+                            f"pageable host buffers / gz_split_stop writing its data file to "
+                            f"{os.path.dirname(ddir)} / close (native loop, libgztask.so)"),
+                   "tasks": tasks, "host_read": args.host_read, "flush_mb": args.e2e_flush_mb,
+                   "split_s_max": statistics.mean(r["split_s_max"] for r in runs),
+                   "stop_s_max": statistics.mean(r["stop_s_max"] for r in runs),
+                   "bytes_written_per_step": runs[-1]["bytes_written"],
+                   "one_task": {"value": (one["input_bytes"] + one["raw_partition_bytes"]) / one["wall_s"] / 1e9,
+                                "unit": "GB/s", "wall_s": one["wall_s"], "split_s": one["split_s_max"],
+                                "stop_s": one["stop_s_max"]},
+                   "link": link}
+            # -- CPU baseline on the whole workload, and the output check ------------------------
+            if rank == 0 and world == 1 and not args.no_cpu:
+                dt, nin, nraw, cpu_lengths, cpu_files = oracle_tasks(sch, keys, args.partitioner, rows, haddrs,
+                                                                     sizes, tasks, ddir, digest=True)
+                cpu = {"value": (nin + nraw) / dt / 1e9, "unit": "GB/s", "cores": tasks, "kind": "port",
+                       "sample": (f"the whole workload ({args.rows} rows) as {tasks} map tasks over the same "
+                                  f"batch ranges, split then Stop writing each task's data file"),
+                       "seconds": dt, "reference_over_port": REFERENCE_OVER_PORT,
+                       "reference_estimate": (nin + nraw) / dt / 1e9 * REFERENCE_OVER_PORT}
+                same_files = [g == c for g, c in zip(gpu_files, cpu_files)]
+                same_lengths = all(np.array_equal(g, c) for g, c in zip(gpu_lengths, cpu_lengths))
+                out_check = {"tasks": tasks, "data_files_identical": all(same_files),
+                             "partition_lengths_identical": bool(same_lengths),
+                             "files_differing": [t for t, ok in enumerate(same_files) if not ok],
+                             "bytes_compared": int(sum(n for _, n in gpu_files)),
+                             "how": "64-bit checksum + size of every task's data file, GPU e2e run vs oracle"}
+        finally:
+            remove_dir(ddir)
         del host
-
-    # -- CPU baseline on a bounded sample ---------------------------------------------------
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
-        threads = os.cpu_count() or 1
-        sample = host_batches(rows, addrs, sizes, keep, 0, args.sample_batches)
-        cpart = dict(sch=sch, keys=keys, partitioner=args.partitioner)
-        cpu_split_sample(sample[: threads * 2], threads, **cpart)
-        dt, nb = cpu_split_sample(sample, threads, **cpart)
-        cpu = {"value": nb / dt / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
-               "sample": f"first {len(sample)} batches x {BATCH_ROWS} rows of the workload",
-               "single_core": single_core(sample, cpart)}
 
     if rank == 0:
         metric, workload = metric_and_workload(args.partitioner)
@@ -796,6 +878,7 @@ def run_gpu(args):
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "output_check": out_check,
             "clocks": clk,
             # per device pass: k_hash_count, k_plan_prep, k_plan_rows, k_plan_bytes (utf8
             # columns present), k_plan_scan, k_scatter
@@ -804,6 +887,7 @@ def run_gpu(args):
             "rows_per_s": args.rows * args.steps * world / t_max,
             "input_gbs": in_all * args.steps / t_max / 1e9,
             "stop_s": stop_s,
+            "stop_warm_s": stop_warm_s,
         }
         if not args.no_forms:
             line["batched"] = run_batched()
@@ -823,7 +907,11 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--rows", type=int, default=200_000_000)
     ap.add_argument("--flush-mb", type=int, default=1024)
-    ap.add_argument("--sample-batches", type=int, default=512)
+    ap.add_argument("--ref-rows", type=int, default=25_000_000,
+                    help="rows of the workload the reference arm splits per step")
+    ap.add_argument("--tasks", type=int, default=0, help="map tasks of the e2e run (0: host cores, at most 16)")
+    ap.add_argument("--e2e-flush-mb", type=int, default=256)
+    ap.add_argument("--host-read", type=int, default=0, help="GzHostRead of the e2e run (0 auto, 1 CPU copy)")
     ap.add_argument("--traffic-per-launch", type=float, default=None)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

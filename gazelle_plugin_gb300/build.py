@@ -16,9 +16,11 @@ CSRC = os.path.join(HERE, "csrc")
 ROOT = os.path.dirname(HERE)
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgzsplit.so")
+TASK_LIB = os.path.join(HERE, "libgztask.so")  # simulated map tasks calling the C ABI
 
 SOURCES = ["kernels.cu", "splitter.cc", "ipc.cc", "schema_ipc.cc", "capi.cc", "host_util.cc",
-           "hash_static.cu", "serve.cc", "tune.cc"]
+           "hash_static.cu", "serve.cc", "tune.cc", "reader.cc", "read_kernels.cu"]
+NOT_IN_LIB = {"task_driver.cc"}  # built into libgztask.so
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -47,13 +49,31 @@ def _stale() -> bool:
     if not os.path.exists(LIB):
         return True
     t = os.path.getmtime(LIB)
-    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [
-        os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
+    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f not in NOT_IN_LIB] + [
+        os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include")) if f != "gz_task.h"]
     return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build_task_driver(force: bool = False) -> str:
+    """libgztask.so: the map-task driver (csrc/task_driver.cc), linked against libgzsplit.so and
+    calling only its C ABI."""
+    src = os.path.join(CSRC, "task_driver.cc")
+    deps = [src, LIB] + [os.path.join(ROOT, "include", f) for f in ("gz_split.h", "gz_task.h")]
+    if not force and os.path.exists(TASK_LIB) and all(os.path.getmtime(d) <= os.path.getmtime(TASK_LIB) for d in deps):
+        return TASK_LIB
+    tmp = TASK_LIB + ".tmp"
+    cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-I", os.path.join(ROOT, "include"), src,
+           "-o", tmp, "-L", HERE, "-lgzsplit", "-Wl,-rpath,$ORIGIN", "-pthread"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"task driver build failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, TASK_LIB)
+    return TASK_LIB
 
 
 def build_library(force: bool = False, verbose: bool = False) -> str:
     if not force and not _stale():
+        build_task_driver()
         return LIB
     os.makedirs(BUILD_DIR, exist_ok=True)
     with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
@@ -64,6 +84,7 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_task_driver(force=True)
     return LIB
 
 

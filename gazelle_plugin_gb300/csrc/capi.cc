@@ -17,6 +17,7 @@
 
 #include "../../include/gz_split.h"
 #include "hash_static.h"
+#include "reader.h"
 #include "host_util.h"
 #include "schema_ipc.h"
 #include "serve.h"
@@ -82,6 +83,45 @@ GzStatus MakeCommon(const char* short_name, int32_t num_partitions, std::vector<
   std::lock_guard<std::mutex> lk(g_mu);
   *out_handle = g_next_id++;
   g_table[*out_handle] = e;
+  return GZ_OK;
+}
+
+struct ReaderEntry {
+  std::unique_ptr<gz::PartitionReader> reader;
+  std::string last_error;
+};
+std::map<int64_t, std::shared_ptr<ReaderEntry>>& g_readers = *new std::map<int64_t, std::shared_ptr<ReaderEntry>>;
+
+std::shared_ptr<ReaderEntry> LookupReader(int64_t id) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_readers.find(id);
+  if (it == g_readers.end()) {
+    t_make_error = "Invalid reader id " + std::to_string(id);
+    return nullptr;
+  }
+  return it->second;
+}
+
+GzStatus ReportReader(ReaderEntry* e, const gz::Status& st) {
+  if (!st.ok()) {
+    e->last_error = st.msg;
+    t_make_error = st.msg;
+  }
+  return st.code;
+}
+
+GzStatus MakeReader(std::vector<gz::Field> fields, int32_t device, int64_t* out_handle) {
+  std::unique_ptr<gz::PartitionReader> r;
+  gz::Status st = gz::PartitionReader::Make(std::move(fields), device, &r);
+  if (!st.ok()) {
+    t_make_error = "reader: " + st.msg;
+    return st.code;
+  }
+  auto e = std::make_shared<ReaderEntry>();
+  e->reader = std::move(r);
+  std::lock_guard<std::mutex> lk(g_mu);
+  *out_handle = g_next_id++;
+  g_readers[*out_handle] = e;
   return GZ_OK;
 }
 
@@ -275,6 +315,62 @@ GzStatus gz_split_kernel_times(int64_t handle, double* out4) {
   auto e = Lookup(handle);
   if (!e || !out4) return GZ_INVALID;
   return Report(e.get(), e->splitter->KernelTimes(out4));
+}
+
+GzStatus gz_reader_make(const uint8_t* schema_ipc, int64_t schema_len, int32_t device, int64_t* out_handle) {
+  std::vector<gz::Field> fields;
+  std::string err;
+  if (out_handle == nullptr || !gz::ParseSchemaIpc(schema_ipc, schema_len, &fields, &err)) {
+    t_make_error = "reader schema: " + (out_handle ? err : std::string("null out_handle"));
+    return GZ_INVALID;
+  }
+  return MakeReader(std::move(fields), device, out_handle);
+}
+
+GzStatus gz_reader_make_fields(const GzField* fields, int32_t n_fields, int32_t device, int64_t* out_handle) {
+  if (out_handle == nullptr || (fields == nullptr && n_fields > 0)) {
+    t_make_error = "reader: null argument";
+    return GZ_INVALID;
+  }
+  return MakeReader(FieldsFrom(fields, n_fields), device, out_handle);
+}
+
+GzStatus gz_reader_add_stream(int64_t handle, const uint8_t* stream, int64_t len) {
+  auto r = LookupReader(handle);
+  if (!r) return GZ_INVALID;
+  return ReportReader(r.get(), r->reader->AddStream(stream, len));
+}
+
+GzStatus gz_reader_finish(int64_t handle, int64_t* out_rows, int32_t* out_batches) {
+  auto r = LookupReader(handle);
+  if (!r) return GZ_INVALID;
+  return ReportReader(r.get(), r->reader->Finish(out_rows, out_batches));
+}
+
+GzStatus gz_reader_column(int64_t handle, int32_t field, GzDeviceColumn* out) {
+  auto r = LookupReader(handle);
+  if (!r || out == nullptr) return GZ_INVALID;
+  return ReportReader(r.get(), r->reader->Column(field, out));
+}
+
+GzStatus gz_reader_column_to_host(int64_t handle, int32_t field, uint8_t* validity, int32_t* offsets,
+                                  uint8_t* values) {
+  auto r = LookupReader(handle);
+  if (!r) return GZ_INVALID;
+  return ReportReader(r.get(), r->reader->ColumnToHost(field, validity, offsets, values));
+}
+
+GzStatus gz_reader_close(int64_t handle) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_readers.erase(handle);
+  return GZ_OK;
+}
+
+GzStatus gz_debug_set_spin_limit(int64_t handle, uint32_t polls) {
+  auto e = Lookup(handle);
+  if (!e) return GZ_INVALID;
+  e->splitter->SetSpinLimit(polls);
+  return GZ_OK;
 }
 
 GzStatus gz_split_stats(int64_t handle, int64_t* out8) {

@@ -147,6 +147,7 @@ struct FlushDesc {
   uint32_t* emit_count;  // [1]
   uint32_t emit_cap;
   uint32_t rr_base;      // round-robin selection at the pass's first row (pid_selection_)
+  uint32_t spin_limit;   // polls of k_scatter's waits for data / free slots; 0: the default
   uint32_t* call_flags;  // [n_batches] 1 when some partition ran CalculateSplitBatchSize
   uint32_t* rec_idx;     // [n_batches][P] 1 + emission record index when a segment was cut
   unsigned long long* hn;   // [n_batches] columns with nulls in the batch

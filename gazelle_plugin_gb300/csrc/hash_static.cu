@@ -95,7 +95,9 @@ k_sum_tile_counts(const uint32_t* __restrict__ tile_counts, uint32_t n_tiles, ui
 }
 
 std::mutex g_mu;
-std::vector<uint32_t*> g_addr;  // device address of g_tile_counts, per device ordinal
+// device address of g_tile_counts, per device ordinal, in that device's primary context (the
+// one the runtime API uses; other contexts are not supported)
+std::vector<uint32_t*> g_addr;
 
 // Looks up (once per device, with `device` current) the device address of g_tile_counts.
 cudaError_t ScratchAddress(int device, uint32_t** out) {
@@ -128,9 +130,12 @@ GzStatus HashPartitionStatic(int32_t device, int32_t P, const GzKeyColumn* keys,
     *msg = "num_rows must be >= 0 and the output pointers non-null";
     return GZ_INVALID;
   }
+  // A null-type key has no hash function and leaves the chain unchanged (the NullType case of
+  // HashSplitter::CreateProjector, splitter.cc:1407-1408): it takes no slot of the key list.
   KeySet ks{};
-  ks.n = n_keys;
+  ks.n = 0;
   for (int k = 0; k < n_keys; k++) {
+    if (keys[k].type == GZ_TYPE_NULL) continue;
     int kind;
     switch (keys[k].type) {
       case GZ_TYPE_BOOL: kind = KEY_BOOL; break;
@@ -147,9 +152,10 @@ GzStatus HashPartitionStatic(int32_t device, int32_t P, const GzKeyColumn* keys,
       *msg = "key " + std::to_string(k) + ": null values pointer";
       return GZ_INVALID;
     }
-    ks.kind[k] = kind;
-    ks.validity[k] = keys[k].validity;
-    ks.values[k] = keys[k].values;
+    ks.kind[ks.n] = kind;
+    ks.validity[ks.n] = keys[k].validity;
+    ks.values[ks.n] = keys[k].values;
+    ks.n++;
   }
   const uint64_t n_tiles = ((uint64_t)num_rows + kTile - 1) / kTile;
   if (n_tiles * (uint64_t)P > kStaticScratchWords) {
@@ -159,11 +165,31 @@ GzStatus HashPartitionStatic(int32_t device, int32_t P, const GzKeyColumn* keys,
     return GZ_INVALID;
   }
 
+  // An error already pending on this thread came from the caller's earlier work, not from this
+  // call: report it as such (and leave it pending) instead of taking it for a launch failure.
+  {
+    const cudaError_t before = cudaPeekAtLastError();
+    if (before != cudaSuccess) {
+      *msg = std::string("a CUDA error from earlier work on this thread is pending (nothing was "
+                         "launched): ") + cudaGetErrorString(before);
+      return GZ_CUDA;
+    }
+  }
   int prev = -1;
   cudaError_t e = cudaGetDevice(&prev);
   if (e == cudaSuccess) e = cudaSetDevice(device);
   uint32_t* scratch = nullptr;
-  if (e == cudaSuccess) e = ScratchAddress(device, &scratch);
+  if (e == cudaSuccess) {
+    e = ScratchAddress(device, &scratch);
+    if (e == cudaErrorMemoryAllocation) {
+      // with lazy module loading the array is reserved here, on the first call on a device
+      cudaGetLastError();
+      if (prev >= 0 && prev != device) cudaSetDevice(prev);
+      *msg = "out of device memory reserving the library's 16 MiB static scratch array on device " +
+             std::to_string(device) + ": make the first call on each device before reserving its free memory";
+      return GZ_OOM;
+    }
+  }
   if (e == cudaSuccess && n_tiles > 0) {
     const int smem_hist = P <= (int32_t)kSmemHistMaxP;
     const size_t sm = smem_hist ? sizeof(uint32_t) * P : 0;

@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <atomic>
 #include <condition_variable>
+#include <deque>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -198,6 +199,89 @@ class CopyPool {
 };
 
 }  // namespace
+
+// ---------------------------------------------------------------------------------------
+namespace {
+
+struct ForJob {
+  const std::function<void(size_t)>* fn;
+  size_t n;
+  std::atomic<size_t> next{0};
+  std::atomic<size_t> done{0};
+  std::mutex mu;
+  std::condition_variable cv;
+
+  void Work() {
+    for (;;) {
+      const size_t i = next.fetch_add(1);
+      if (i >= n) return;
+      (*fn)(i);
+      if (done.fetch_add(1) + 1 == n) {
+        std::lock_guard<std::mutex> lk(mu);
+        cv.notify_all();
+      }
+    }
+  }
+};
+
+class ForPool {
+ public:
+  static ForPool& Get() {
+    static ForPool* pool = new ForPool();  // workers live until process exit
+    return *pool;
+  }
+  int workers() const { return n_; }
+  void Post(const std::shared_ptr<ForJob>& job, int tickets) {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      for (int i = 0; i < tickets; i++) q_.push_back(job);
+    }
+    if (tickets == 1) cv_.notify_one();
+    else cv_.notify_all();
+  }
+
+ private:
+  ForPool() {
+    const unsigned hc = std::thread::hardware_concurrency();
+    n_ = (int)std::max<unsigned>(1, std::min<unsigned>(31, hc > 1 ? hc - 1 : 1));
+    for (int i = 0; i < n_; i++) std::thread([this] { Loop(); }).detach();
+  }
+  void Loop() {
+    for (;;) {
+      std::shared_ptr<ForJob> job;
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return !q_.empty(); });
+        job = q_.front();
+        q_.pop_front();
+      }
+      job->Work();
+    }
+  }
+  int n_ = 1;
+  std::mutex mu_;
+  std::condition_variable cv_;
+  std::deque<std::shared_ptr<ForJob>> q_;
+};
+
+}  // namespace
+
+void ParallelFor(size_t n, const std::function<void(size_t)>& fn, int max_helpers) {
+  if (n == 0) return;
+  if (n == 1 || max_helpers <= 0) {
+    for (size_t i = 0; i < n; i++) fn(i);
+    return;
+  }
+  auto job = std::make_shared<ForJob>();
+  job->fn = &fn;
+  job->n = n;
+  ForPool& pool = ForPool::Get();
+  const int helpers = (int)std::min<size_t>({(size_t)max_helpers, (size_t)pool.workers(), n - 1});
+  pool.Post(job, helpers);
+  job->Work();
+  std::unique_lock<std::mutex> lk(job->mu);
+  job->cv.wait(lk, [&] { return job->done.load() == n; });
+}
 
 void ParallelCopy(const std::vector<CopyJob>& jobs, size_t total_bytes) {
   if (total_bytes < (1u << 20)) {

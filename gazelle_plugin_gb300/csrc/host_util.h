@@ -5,6 +5,7 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <functional>
 #include <vector>
 
 namespace gz {
@@ -33,5 +34,10 @@ struct CopyJob {
 // Copies every job; large totals are split over worker threads and the caller.  Returns when
 // all bytes are copied.
 void ParallelCopy(const std::vector<CopyJob>& jobs, size_t total_bytes);
+
+// Runs fn(i) for every i in [0, n) on the calling thread and up to `max_helpers` threads of a
+// process-wide pool (shared by all splitters: concurrent calls share its workers); returns when
+// every fn(i) has returned.  Items are claimed one at a time, so long and short items balance.
+void ParallelFor(size_t n, const std::function<void(size_t)>& fn, int max_helpers = 15);
 
 }  // namespace gz

@@ -93,14 +93,11 @@ int64_t RecordBatchMessageSize(int64_t n_nodes, const std::vector<int64_t>& buff
   return 8 + 88 + 16 * (n_nodes + (int64_t)buffer_lengths.size()) + body;
 }
 
-int64_t WriteRecordBatchMessage(ByteSink* sink, int64_t length,
-                                const std::vector<FieldNodeMeta>& nodes,
-                                const std::vector<ChunkedBuffer>& buffers, int64_t* body_length) {
+void RecordBatchHeader(int64_t length, const std::vector<FieldNodeMeta>& nodes,
+                       const std::vector<int64_t>& lens, std::vector<uint8_t>* out,
+                       int64_t* body_length) {
   const int64_t L = (int64_t)nodes.size();
-  const int64_t M = (int64_t)buffers.size();
-  std::vector<int64_t> lens(M, 0);
-  for (int64_t i = 0; i < M; i++)
-    for (const Chunk& c : buffers[i]) lens[i] += c.len;
+  const int64_t M = (int64_t)lens.size();
   int64_t body = 0;
   const int64_t fb_size = 88 + 16 * (L + M);
   std::vector<uint8_t> meta(8 + fb_size, 0);
@@ -136,6 +133,19 @@ int64_t WriteRecordBatchMessage(ByteSink* sink, int64_t length,
     Put<int64_t>(nm + 4 + 16 * i + 8, nodes[i].null_count);
   }
   *body_length = body;
+  *out = std::move(meta);
+}
+
+int64_t WriteRecordBatchMessage(ByteSink* sink, int64_t length,
+                                const std::vector<FieldNodeMeta>& nodes,
+                                const std::vector<ChunkedBuffer>& buffers, int64_t* body_length) {
+  const int64_t M = (int64_t)buffers.size();
+  std::vector<int64_t> lens(M, 0);
+  for (int64_t i = 0; i < M; i++)
+    for (const Chunk& c : buffers[i]) lens[i] += c.len;
+  std::vector<uint8_t> meta;
+  RecordBatchHeader(length, nodes, lens, &meta, body_length);
+  const int64_t body = *body_length;
   if (!sink->Write(meta.data(), (int64_t)meta.size())) return -1;
   for (int64_t i = 0; i < M; i++) {
     for (const Chunk& c : buffers[i]) {

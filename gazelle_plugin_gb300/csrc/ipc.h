@@ -65,6 +65,12 @@ int64_t WriteRecordBatchMessage(ByteSink* sink, int64_t length,
                                 const std::vector<FieldNodeMeta>& nodes,
                                 const std::vector<ChunkedBuffer>& buffers, int64_t* body_length);
 
+// The metadata of that message (continuation token, metadata length, flatbuffer) for body
+// buffers of lengths `lens`; the body follows it, each buffer padded to 8 bytes.
+void RecordBatchHeader(int64_t length, const std::vector<FieldNodeMeta>& nodes,
+                       const std::vector<int64_t>& lens, std::vector<uint8_t>* out,
+                       int64_t* body_length);
+
 // Size of that message without writing it.
 int64_t RecordBatchMessageSize(int64_t n_nodes, const std::vector<int64_t>& buffer_lengths,
                                int64_t* body_length);

@@ -221,9 +221,14 @@ __global__ void __launch_bounds__(kHashThreads) k_hash_count(const SchemaDesc sd
         p[u] = 0;
       }
     }
-    if (act[u]) {
-      fd.pids[tile.frow0 + i0 + u] = (uint16_t)p[u];
-      atomicAdd(&H[p[u]], 1u);
+    if (act[u]) fd.pids[tile.frow0 + i0 + u] = (uint16_t)p[u];
+    if (part == PART_RR) {  // consecutive rows, distinct partitions: nothing to aggregate
+      if (act[u]) atomicAdd(&H[p[u]], 1u);
+    } else {
+      // warp-aggregated: the lanes whose row went to the same partition add once (skewed keys
+      // otherwise serialise on one counter)
+      const unsigned grp = __match_any_sync(kFull, act[u] ? p[u] : 0xffffffffu);
+      if (act[u] && (int)lane_id() == __ffs(grp) - 1) atomicAdd(&H[p[u]], (uint32_t)__popc(grp));
     }
   }
   for (int k = 0; k < nstr; k++) {
@@ -712,9 +717,9 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
-// Bounded wait for phase `parity` of `bar`; false when the limit ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (uint32_t it = 0; it < kSpinLimit; it++) {
+// Bounded wait for phase `parity` of `bar`; false when `limit` polls ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = kSpinLimit) {
+  for (uint32_t it = 0; it < limit; it++) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
@@ -1008,16 +1013,24 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
   };
   auto staged_binary = [&](int a) { return sd.arr_kind[a] == COL_BINARY && chars_staged(sd.arr_str[a]); };
 
+  // Polls of a wait for data or for a free slot before the block gives up (a test lowers it to
+  // make the waits run out); waits for copies already in flight always use kSpinLimit.
+  const uint32_t lim = fd.spin_limit ? fd.spin_limit : kSpinLimit;
+  volatile uint32_t* vbad = &s_bad;
+
   // ---- issuing warp: lane 0 streams the column slices, lane 1 the character slices ----------
+  // Once a scattering warp has given up on a slice (s_bad, written before that warp releases the
+  // slot), nothing more is issued: the slot's last copy may still be landing.
   if (threadIdx.x >= kConsumers) {
     const int lane = threadIdx.x - kConsumers;
     if (lane == 0) {
       int issued = 0;
       for (int i = 0; i < A; i++) {
-        if (i >= kSlots && !mbar_wait(&empty[i % kSlots], (uint32_t)((i / kSlots - 1) & 1))) {
+        if (i >= kSlots && !mbar_wait(&empty[i % kSlots], (uint32_t)((i / kSlots - 1) & 1), lim)) {
           atomicOr(fd.err, kErrTimeout);
           break;
         }
+        if (*vbad) break;
         const int a = sd.order[i];
         const ColPtr c = s_col[a];
         const int kind = sd.arr_kind[a];
@@ -1056,10 +1069,11 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
       for (int i = 0; i < A; i++) {
         const int a = sd.order[i];
         if (!staged_binary(a)) continue;
-        if (uses > 0 && !mbar_wait(&cempty, (uses - 1) & 1)) {
+        if (uses > 0 && !mbar_wait(&cempty, (uses - 1) & 1, lim)) {
           atomicOr(fd.err, kErrTimeout);
           break;
         }
+        if (*vbad) break;
         const int k = sd.arr_str[a];
         const uint8_t* src = s_col[a].values + s_cr[k].x;
         const uint32_t sb = super_bytes(src, (uint32_t)(s_cr[k].y - s_cr[k].x));
@@ -1178,7 +1192,6 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
   // marks the block bad: from then on columns are skipped, but every thread still reaches every
   // barrier (a binary column's skip decision is taken after its first barrier, so it is the same
   // in all threads).
-  volatile uint32_t* vbad = &s_bad;
   int nbin = 0;  // binary columns done (the parity of their warp-total buffer)
   for (int i = 0; i < A; i++) {
     const uint4 ct = s_ct[i];
@@ -1187,8 +1200,8 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
     const bool chars = (ct.z >> 16) & 1u;
     const int kind = (int)(ct.z & 255u);
     if (!*vbad) {
-      bool ok = mbar_wait(&full[slot], (uint32_t)((i / kSlots) & 1));
-      if (chars) ok = mbar_wait(&cfull, cuse & 1) && ok;
+      bool ok = mbar_wait(&full[slot], (uint32_t)((i / kSlots) & 1), lim);
+      if (chars) ok = mbar_wait(&cfull, cuse & 1, lim) && ok;
       if (!ok) {
         atomicOr(fd.err, kErrTimeout);
         *vbad = 1;

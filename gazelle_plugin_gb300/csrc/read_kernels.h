@@ -1,0 +1,33 @@
+// Job lists of the reduce-side read kernels (read_kernels.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gz {
+
+struct ByteJob {  // bytes [src, src + bytes) to dst
+  const uint8_t* src;
+  uint8_t* dst;
+  uint64_t bytes;
+};
+
+struct OffsetJob {  // dst[i] = src[i] + add, i < n
+  const int32_t* src;
+  int32_t* dst;
+  uint32_t n;
+  int32_t add;
+};
+
+struct BitJob {  // bits [src_bit, src_bit + nbits) of src (all ones when src is null) ORed into dst at dst_bit
+  const uint32_t* src;
+  uint32_t* dst;
+  uint64_t src_bit;
+  uint64_t dst_bit;
+  uint64_t nbits;
+};
+
+// Runs the three job lists on `st` (the job arrays in device memory).
+cudaError_t launch_read_jobs(const ByteJob* bytes, uint32_t n_bytes, const OffsetJob* offs, uint32_t n_offs,
+                             const BitJob* bits, uint32_t n_bits, cudaStream_t st);
+
+}  // namespace gz

@@ -1,0 +1,364 @@
+// Reduce-side read on the GPU (see reader.h).
+#include "reader.h"
+
+#include <string.h>
+
+#include <algorithm>
+
+#include "flatbuf.h"
+#include "read_kernels.h"
+
+namespace gz {
+
+namespace {
+
+inline int64_t Pad8(int64_t n) { return (n + 7) & ~int64_t(7); }
+inline size_t AlignUp(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+bool IsBinaryType(int t) { return t == GZ_TYPE_STRING || t == GZ_TYPE_BINARY; }
+
+int FixedWidth(int t) {
+  switch (t) {
+    case GZ_TYPE_INT8: case GZ_TYPE_UINT8: return 1;
+    case GZ_TYPE_INT16: case GZ_TYPE_UINT16: case GZ_TYPE_HALF_FLOAT: return 2;
+    case GZ_TYPE_INT32: case GZ_TYPE_UINT32: case GZ_TYPE_FLOAT32: case GZ_TYPE_DATE32:
+    case GZ_TYPE_TIME32: return 4;
+    case GZ_TYPE_INT64: case GZ_TYPE_UINT64: case GZ_TYPE_FLOAT64: case GZ_TYPE_DATE64:
+    case GZ_TYPE_TIME64: case GZ_TYPE_TIMESTAMP: return 8;
+    case GZ_TYPE_DECIMAL128: return 16;
+    default: return 0;
+  }
+}
+
+// Arrow IPC metadata (Message.fbs / Schema.fbs): Message {version, header_type, header,
+// bodyLength}; RecordBatch {length, nodes: [FieldNode{length, null_count}], buffers:
+// [Buffer{offset, length}], compression: BodyCompression{codec, method}}.
+constexpr uint8_t kHeaderSchema = 1, kHeaderRecordBatch = 3;
+
+}  // namespace
+
+Status PartitionReader::Cuda(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return Status::OK();
+  cudaGetLastError();
+  return Status::Error(e == cudaErrorMemoryAllocation ? GZ_OOM : GZ_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+Status PartitionReader::Make(std::vector<Field> fields, int device, std::unique_ptr<PartitionReader>* out) {
+  std::unique_ptr<PartitionReader> r(new PartitionReader());
+  for (const Field& f : fields) {
+    if (f.type != GZ_TYPE_NULL && f.type != GZ_TYPE_BOOL && !IsBinaryType(f.type) && FixedWidth(f.type) == 0)
+      return Status::Error(GZ_NOT_IMPLEMENTED, "field type not implemented by the reader");
+  }
+  r->fields_ = std::move(fields);
+  r->device_ = device;
+  Status st = r->Cuda(cudaSetDevice(device), "cudaSetDevice");
+  if (!st.ok()) return st;
+  st = r->Cuda(cudaStreamCreateWithFlags(&r->stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+  if (!st.ok()) return st;
+  r->out_.assign(r->fields_.size(), OutCol());
+  *out = std::move(r);
+  return Status::OK();
+}
+
+PartitionReader::~PartitionReader() {
+  if (stream_) cudaStreamSynchronize(stream_);
+  for (uint8_t* p : images_)
+    if (p) cudaFreeAsync(p, stream_);
+  if (out_mem_) cudaFreeAsync(out_mem_, stream_);
+  if (stream_) {
+    cudaStreamSynchronize(stream_);
+    cudaStreamDestroy(stream_);
+  }
+}
+
+// Walks the messages of one stream: an optional schema message, record batches, then the
+// end-of-stream marker (or the end of the bytes).  Buffer ranges are recorded relative to the
+// stream start, where the device copy keeps them.
+Status PartitionReader::ParseStream(const uint8_t* data, int64_t len, int stream, std::vector<Batch>* out) {
+  int64_t pos = 0;
+  while (pos < len) {
+    if (len - pos < 4) return Status::Error(GZ_INVALID, "truncated IPC stream");
+    uint32_t first;
+    memcpy(&first, data + pos, 4);
+    int32_t meta_len;
+    int64_t meta_pos;
+    if (first == 0xFFFFFFFFu) {  // continuation token, then the metadata length
+      if (len - pos < 8) return Status::Error(GZ_INVALID, "truncated IPC stream");
+      memcpy(&meta_len, data + pos + 4, 4);
+      meta_pos = pos + 8;
+    } else {  // legacy framing: the length alone
+      meta_len = (int32_t)first;
+      meta_pos = pos + 4;
+    }
+    if (meta_len == 0) break;  // end of stream
+    if (meta_len < 0 || meta_pos + meta_len > len) return Status::Error(GZ_INVALID, "bad IPC message length");
+    FlatReader r(data + meta_pos, meta_len);
+    uint32_t root;
+    if (!r.Get(0, &root)) return Status::Error(GZ_INVALID, "bad IPC message");
+    const int64_t msg = root;
+    const uint8_t header_type = r.Scalar<uint8_t>(msg, 1, 0);
+    const int64_t body_len = r.Scalar<int64_t>(msg, 3, 0);
+    const int64_t body_pos = meta_pos + meta_len;
+    if (body_len < 0 || body_pos + body_len > len) return Status::Error(GZ_INVALID, "IPC message body exceeds the stream");
+    if (body_pos & 7) return Status::Error(GZ_NOT_IMPLEMENTED, "IPC message body not on an 8-byte boundary");
+    if (header_type == kHeaderSchema) {
+      std::vector<Field> fs;
+      std::string err;
+      if (!ParseSchemaIpc(data + pos, body_pos - pos, &fs, &err))
+        return Status::Error(GZ_INVALID, "schema message in the stream: " + err);
+      if (fs.size() != fields_.size()) return Status::Error(GZ_INVALID, "stream schema differs from the reader's");
+      for (size_t i = 0; i < fs.size(); i++)
+        if (fs[i].type != fields_[i].type) return Status::Error(GZ_INVALID, "stream schema differs from the reader's");
+    } else if (header_type == kHeaderRecordBatch) {
+      const int64_t rb = r.Table(msg, 2);
+      if (rb < 0) return Status::Error(GZ_INVALID, "record batch without header");
+      if (r.Table(rb, 3) >= 0) return Status::Error(GZ_NOT_IMPLEMENTED, "compressed record batch bodies");
+      Batch b;
+      b.stream = stream;
+      b.rows = r.Scalar<int64_t>(rb, 0, 0);
+      const int64_t nodes = r.Table(rb, 1), bufs = r.Table(rb, 2);
+      uint32_t n_nodes = 0, n_bufs = 0;
+      if (nodes < 0 || bufs < 0 || !r.Get(nodes, &n_nodes) || !r.Get(bufs, &n_bufs))
+        return Status::Error(GZ_INVALID, "record batch without nodes or buffers");
+      uint32_t node = 0, buf = 0;
+      auto next_buf = [&](BufRef* out_ref) -> bool {
+        int64_t off, l;
+        if (buf >= n_bufs || !r.Get(bufs + 4 + 16 * (int64_t)buf, &off) || !r.Get(bufs + 4 + 16 * (int64_t)buf + 8, &l))
+          return false;
+        buf++;
+        if (off < 0 || l < 0 || off + l > body_len || (off & 7)) return false;
+        out_ref->offset = body_pos + off;
+        out_ref->length = l;
+        return true;
+      };
+      b.cols.resize(fields_.size());
+      for (size_t f = 0; f < fields_.size(); f++) {
+        int64_t nl, nn;
+        if (node >= n_nodes || !r.Get(nodes + 4 + 16 * (int64_t)node, &nl) ||
+            !r.Get(nodes + 4 + 16 * (int64_t)node + 8, &nn))
+          return Status::Error(GZ_INVALID, "record batch has too few field nodes");
+        node++;
+        if (nl != b.rows) return Status::Error(GZ_INVALID, "field length differs from the batch length");
+        ColRef& c = b.cols[f];
+        c.null_count = nn;
+        const int t = fields_[f].type;
+        if (t == GZ_TYPE_NULL) continue;  // no buffers
+        bool ok = next_buf(&c.validity);
+        if (IsBinaryType(t)) ok = ok && next_buf(&c.offsets);
+        ok = ok && next_buf(&c.values);
+        if (!ok) return Status::Error(GZ_INVALID, "bad buffer list in a record batch");
+        if (nn > 0 && c.validity.length < (b.rows + 7) / 8) return Status::Error(GZ_INVALID, "validity buffer too short");
+        if (nn == 0) c.validity.length = 0;
+        const int64_t need = t == GZ_TYPE_BOOL ? (b.rows + 7) / 8
+                             : IsBinaryType(t) ? 0 : b.rows * FixedWidth(t);
+        if (c.values.length < need) return Status::Error(GZ_INVALID, "value buffer too short");
+        if (IsBinaryType(t)) {
+          if (c.offsets.length < (b.rows + 1) * 4) return Status::Error(GZ_INVALID, "offsets buffer too short");
+          memcpy(&c.o0, data + c.offsets.offset, 4);
+          memcpy(&c.o1, data + c.offsets.offset + 4 * b.rows, 4);
+          if (c.o0 < 0 || c.o1 < c.o0 || c.o1 > c.values.length)
+            return Status::Error(GZ_INVALID, "offsets exceed the characters");
+        }
+      }
+      if (b.rows > 0) out->push_back(std::move(b));
+    } else {
+      return Status::Error(GZ_NOT_IMPLEMENTED, "IPC message type " + std::to_string(header_type) + " in a shuffle stream");
+    }
+    pos = body_pos + Pad8(body_len);
+  }
+  return Status::OK();
+}
+
+Status PartitionReader::AddStream(const uint8_t* data, int64_t len) {
+  if (finished_) return Status::Error(GZ_INVALID, "reader already finished");
+  if (len < 0 || (len > 0 && data == nullptr)) return Status::Error(GZ_INVALID, "null stream");
+  std::vector<Batch> bs;
+  const int idx = (int)images_.size();
+  Status st = ParseStream(data, len, idx, &bs);
+  if (!st.ok()) return st;
+  st = Cuda(cudaSetDevice(device_), "cudaSetDevice");
+  if (!st.ok()) return st;
+  uint8_t* d = nullptr;
+  if (!bs.empty()) {
+    st = Cuda(cudaMallocAsync(reinterpret_cast<void**>(&d), AlignUp((size_t)len, 256), stream_), "cudaMallocAsync(stream)");
+    if (!st.ok()) return st;
+    // the caller's bytes are read before the call returns
+    st = Cuda(cudaMemcpyAsync(d, data, (size_t)len, cudaMemcpyHostToDevice, stream_), "H2D stream");
+    if (!st.ok()) return st;
+    st = Cuda(cudaStreamSynchronize(stream_), "H2D stream");
+    if (!st.ok()) return st;
+  }
+  images_.push_back(d);
+  for (Batch& b : bs) batches_.push_back(std::move(b));
+  return Status::OK();
+}
+
+Status PartitionReader::Finish(int64_t* rows, int32_t* n_batches) {
+  if (finished_) return Status::Error(GZ_INVALID, "reader already finished");
+  Status st = Cuda(cudaSetDevice(device_), "cudaSetDevice");
+  if (!st.ok()) return st;
+  const size_t F = fields_.size();
+  int64_t R = 0;
+  for (const Batch& b : batches_) R += b.rows;
+  if (R >= (1ll << 31)) return Status::Error(GZ_INVALID, "more than 2^31 - 1 rows in one partition");
+  // output layout: per field validity (when some batch has nulls), offsets, values / characters
+  std::vector<size_t> o_valid(F, SIZE_MAX), o_off(F, SIZE_MAX), o_val(F, SIZE_MAX);
+  std::vector<int64_t> chars(F, 0);
+  size_t total = 0;
+  const size_t bit_bytes = AlignUp((size_t)((R + 31) / 32) * 4, 256);
+  for (size_t f = 0; f < F; f++) {
+    const int t = fields_[f].type;
+    OutCol& oc = out_[f];
+    oc = OutCol();
+    if (t == GZ_TYPE_NULL) {
+      oc.null_count = R;
+      continue;
+    }
+    for (const Batch& b : batches_) {
+      oc.null_count += b.cols[f].null_count;
+      if (IsBinaryType(t)) chars[f] += b.cols[f].o1 - b.cols[f].o0;
+    }
+    if (chars[f] >= (1ll << 31)) return Status::Error(GZ_INVALID, "more than 2^31 - 1 characters in one column");
+    if (oc.null_count > 0) {
+      o_valid[f] = total;
+      total += bit_bytes;
+    }
+    if (IsBinaryType(t)) {
+      o_off[f] = total;
+      total += AlignUp((size_t)(R + 1) * 4, 256);
+    }
+    o_val[f] = total;
+    total += t == GZ_TYPE_BOOL ? bit_bytes
+             : IsBinaryType(t) ? AlignUp((size_t)chars[f] + 16, 256)
+                               : AlignUp((size_t)R * FixedWidth(t), 256);
+  }
+  total = std::max<size_t>(total, 256);
+  st = Cuda(cudaMallocAsync(reinterpret_cast<void**>(&out_mem_), total, stream_), "cudaMallocAsync(columns)");
+  if (!st.ok()) return st;
+  st = Cuda(cudaMemsetAsync(out_mem_, 0, total, stream_), "memset(columns)");
+  if (!st.ok()) return st;
+
+  // job lists, built on the host and copied to the device in one piece
+  std::vector<ByteJob> bj;
+  std::vector<OffsetJob> oj;
+  std::vector<BitJob> tj;
+  constexpr uint64_t kChunk = 256u << 10;   // bytes per byte job
+  constexpr uint64_t kBitChunk = 1u << 20;  // bits per bit job
+  auto add_bytes = [&](const uint8_t* src, uint8_t* dst, uint64_t n) {
+    for (uint64_t x = 0; x < n; x += kChunk) bj.push_back(ByteJob{src + x, dst + x, std::min(kChunk, n - x)});
+  };
+  auto add_bits = [&](const uint8_t* src, uint32_t* dst, uint64_t dst_bit, uint64_t n) {
+    for (uint64_t x = 0; x < n; x += kBitChunk)
+      tj.push_back(BitJob{reinterpret_cast<const uint32_t*>(src), dst, src ? x : 0, dst_bit + x, std::min(kBitChunk, n - x)});
+  };
+  std::vector<int64_t> char_pos(F, 0);
+  int64_t row = 0;
+  for (size_t bi = 0; bi < batches_.size(); bi++) {
+    const Batch& b = batches_[bi];
+    const uint8_t* img = images_[b.stream];
+    const bool last = bi + 1 == batches_.size();
+    for (size_t f = 0; f < F; f++) {
+      const int t = fields_[f].type;
+      if (t == GZ_TYPE_NULL) continue;
+      const ColRef& c = b.cols[f];
+      if (o_valid[f] != SIZE_MAX)
+        add_bits(c.validity.length ? img + c.validity.offset : nullptr,
+                 reinterpret_cast<uint32_t*>(out_mem_ + o_valid[f]), (uint64_t)row, (uint64_t)b.rows);
+      if (t == GZ_TYPE_BOOL) {
+        add_bits(img + c.values.offset, reinterpret_cast<uint32_t*>(out_mem_ + o_val[f]), (uint64_t)row,
+                 (uint64_t)b.rows);
+      } else if (IsBinaryType(t)) {
+        // offsets rebased onto the characters of the earlier batches; the last batch also writes
+        // the final offset
+        const int32_t* src_off = reinterpret_cast<const int32_t*>(img + c.offsets.offset);
+        int32_t* dst_off = reinterpret_cast<int32_t*>(out_mem_ + o_off[f]) + row;
+        const int32_t add = (int32_t)(char_pos[f] - c.o0);
+        const uint64_t n = (uint64_t)b.rows + (last ? 1 : 0);
+        for (uint64_t x = 0; x < n; x += kChunk / 4)
+          oj.push_back(OffsetJob{src_off + x, dst_off + x, (uint32_t)std::min<uint64_t>(kChunk / 4, n - x), add});
+        add_bytes(img + c.values.offset + c.o0, out_mem_ + o_val[f] + char_pos[f], (uint64_t)(c.o1 - c.o0));
+        char_pos[f] += c.o1 - c.o0;
+      } else {
+        const int w = FixedWidth(t);
+        add_bytes(img + c.values.offset, out_mem_ + o_val[f] + (size_t)row * w, (uint64_t)b.rows * w);
+      }
+    }
+    row += b.rows;
+  }
+  const size_t jb = AlignUp(sizeof(ByteJob) * bj.size(), 256), jo = AlignUp(sizeof(OffsetJob) * oj.size(), 256),
+               jt = AlignUp(sizeof(BitJob) * tj.size(), 256);
+  std::vector<uint8_t> hj(std::max<size_t>(jb + jo + jt, 256), 0);
+  if (!bj.empty()) memcpy(hj.data(), bj.data(), sizeof(ByteJob) * bj.size());
+  if (!oj.empty()) memcpy(hj.data() + jb, oj.data(), sizeof(OffsetJob) * oj.size());
+  if (!tj.empty()) memcpy(hj.data() + jb + jo, tj.data(), sizeof(BitJob) * tj.size());
+  uint8_t* dj = nullptr;
+  st = Cuda(cudaMallocAsync(reinterpret_cast<void**>(&dj), hj.size(), stream_), "cudaMallocAsync(jobs)");
+  if (!st.ok()) return st;
+  st = Cuda(cudaMemcpyAsync(dj, hj.data(), hj.size(), cudaMemcpyHostToDevice, stream_), "H2D jobs");
+  if (st.ok())
+    st = Cuda(launch_read_jobs(reinterpret_cast<const ByteJob*>(dj), (uint32_t)bj.size(),
+                               reinterpret_cast<const OffsetJob*>(dj + jb), (uint32_t)oj.size(),
+                               reinterpret_cast<const BitJob*>(dj + jb + jo), (uint32_t)tj.size(), stream_),
+              "reader kernels");
+  cudaFreeAsync(dj, stream_);
+  if (!st.ok()) return st;
+  // the stream images are no longer needed
+  for (uint8_t*& p : images_) {
+    if (p) cudaFreeAsync(p, stream_);
+    p = nullptr;
+  }
+  st = Cuda(cudaStreamSynchronize(stream_), "reader kernels");
+  if (!st.ok()) return st;
+  for (size_t f = 0; f < F; f++) {
+    OutCol& oc = out_[f];
+    const int t = fields_[f].type;
+    if (t == GZ_TYPE_NULL) continue;
+    if (o_valid[f] != SIZE_MAX) oc.validity = out_mem_ + o_valid[f];
+    if (o_off[f] != SIZE_MAX) oc.offsets = reinterpret_cast<int32_t*>(out_mem_ + o_off[f]);
+    oc.values = out_mem_ + o_val[f];
+    oc.values_bytes = t == GZ_TYPE_BOOL ? (R + 7) / 8 : IsBinaryType(t) ? chars[f] : R * FixedWidth(t);
+  }
+  rows_ = R;
+  finished_ = true;
+  if (rows) *rows = R;
+  if (n_batches) *n_batches = (int32_t)batches_.size();
+  return Status::OK();
+}
+
+Status PartitionReader::Column(int field, GzDeviceColumn* out) const {
+  if (!finished_) return Status::Error(GZ_INVALID, "reader not finished");
+  if (field < 0 || field >= (int)fields_.size()) return Status::Error(GZ_INVALID, "field out of range");
+  const OutCol& c = out_[field];
+  out->type = fields_[field].type;
+  out->reserved = 0;
+  out->length = rows_;
+  out->null_count = c.null_count;
+  out->validity = c.validity;
+  out->offsets = c.offsets;
+  out->values = c.values;
+  out->values_bytes = c.values_bytes;
+  return Status::OK();
+}
+
+Status PartitionReader::ColumnToHost(int field, uint8_t* validity, int32_t* offsets, uint8_t* values) {
+  GzDeviceColumn c;
+  Status st = Column(field, &c);
+  if (!st.ok()) return st;
+  st = Cuda(cudaSetDevice(device_), "cudaSetDevice");
+  if (!st.ok()) return st;
+  if (validity && c.validity) {
+    st = Cuda(cudaMemcpyAsync(validity, c.validity, (size_t)(c.length + 7) / 8, cudaMemcpyDeviceToHost, stream_), "D2H");
+    if (!st.ok()) return st;
+  }
+  if (offsets && c.offsets) {
+    st = Cuda(cudaMemcpyAsync(offsets, c.offsets, (size_t)(c.length + 1) * 4, cudaMemcpyDeviceToHost, stream_), "D2H");
+    if (!st.ok()) return st;
+  }
+  if (values && c.values && c.values_bytes > 0) {
+    st = Cuda(cudaMemcpyAsync(values, c.values, (size_t)c.values_bytes, cudaMemcpyDeviceToHost, stream_), "D2H");
+    if (!st.ok()) return st;
+  }
+  return Cuda(cudaStreamSynchronize(stream_), "D2H");
+}
+
+}  // namespace gz

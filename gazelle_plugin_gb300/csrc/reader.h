@@ -1,0 +1,77 @@
+// gz::PartitionReader — the reduce side of the shuffle on the GPU: the Arrow IPC streams of one
+// partition (one per map output, each the partition's byte range of a data file: optional schema
+// message, record batches, end-of-stream) read into one set of Arrow columns in HBM.
+//
+// The reference's reduce side reads each stream with Arrow Java (ArrowColumnarBatchSerializer,
+// native-sql-engine/core/src/main/scala/org/apache/spark/sql/execution/ArrowColumnarBatchSerializer.scala:110-240)
+// and decompresses compressed bodies natively (ShuffleDecompressionJniWrapper, jni_wrapper.cc:1236-1322);
+// each record batch becomes one ColumnarBatch.  Here the host parses only the metadata; the bodies
+// go to HBM in one copy per stream and device kernels concatenate the batches of all streams
+// (values and characters copied, offsets rebased, validity bits shifted into place), so the
+// consumer gets one batch per partition.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/gz_split.h"
+#include "schema_ipc.h"
+#include "splitter.h"  // Status
+
+namespace gz {
+
+class PartitionReader {
+ public:
+  static Status Make(std::vector<Field> fields, int device, std::unique_ptr<PartitionReader>* out);
+  ~PartitionReader();
+
+  // Parses one IPC stream (host bytes, read before the call returns) and copies its bodies to
+  // the device.  Streams may carry the schema message first (write_schema) or not.
+  Status AddStream(const uint8_t* data, int64_t len);
+  // Concatenates every batch added so far into device columns; waits for the device.
+  Status Finish(int64_t* rows, int32_t* batches);
+  Status Column(int field, GzDeviceColumn* out) const;
+  Status ColumnToHost(int field, uint8_t* validity, int32_t* offsets, uint8_t* values);
+
+ private:
+  struct BufRef {
+    int64_t offset = 0;  // inside the stream's device copy
+    int64_t length = 0;
+  };
+  struct ColRef {
+    int64_t null_count = 0;
+    BufRef validity, offsets, values;
+    int32_t o0 = 0, o1 = 0;  // binary: first and last offset (the batch's characters)
+  };
+  struct Batch {
+    int stream = 0;
+    int64_t rows = 0;
+    std::vector<ColRef> cols;  // per schema field
+  };
+  struct OutCol {
+    int64_t null_count = 0;
+    uint8_t* validity = nullptr;
+    int32_t* offsets = nullptr;
+    uint8_t* values = nullptr;
+    int64_t values_bytes = 0;
+  };
+
+  PartitionReader() = default;
+  Status Cuda(cudaError_t e, const char* what);
+  Status ParseStream(const uint8_t* data, int64_t len, int stream, std::vector<Batch>* out);
+
+  std::vector<Field> fields_;
+  int device_ = 0;
+  cudaStream_t stream_ = nullptr;
+  std::vector<uint8_t*> images_;  // device copy of every stream
+  std::vector<Batch> batches_;
+  std::vector<OutCol> out_;
+  uint8_t* out_mem_ = nullptr;
+  int64_t rows_ = 0;
+  bool finished_ = false;
+};
+
+}  // namespace gz

@@ -1,7 +1,12 @@
 // Host engine of the GB300 hash split (see splitter.h).
 #include "splitter.h"
 
+#include <errno.h>
+#include <fcntl.h>
 #include <string.h>
+#include <sys/stat.h>
+#include <sys/uio.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <chrono>
@@ -185,9 +190,13 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
   else seg_tiles_ = P_ >= 1024 ? (uint32_t)kMaxSegTiles : 4u;
   // hash chain (HashSplitter::CreateProjector, splitter.cc:1402-1438); the range partitioner's
   // one "key" is its id column, read as int32 values (a wrong type fails every Split)
+  // A null-type key has no hash function and leaves the chain unchanged (the NullType case,
+  // splitter.cc:1407-1408), so it takes no slot of the device key list.
+  int nk = 0;
   for (size_t k = 0; k < keys_.size(); k++) {
     const int ci = keys_[k];
     if (ci < 0 || ci >= (int)fields_.size()) return Status::Error(GZ_INVALID, "key column out of range");
+    if (partitioner_ != PART_RANGE && fields_[ci].type == GZ_TYPE_NULL) continue;
     int kind;
     switch (partitioner_ == PART_RANGE ? GZ_TYPE_INT32 : fields_[ci].type) {
       case GZ_TYPE_BOOL: kind = KEY_BOOL; break;
@@ -199,9 +208,11 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
         return Status::Error(GZ_NOT_IMPLEMENTED,
                              "hash key type has no Spark-compatible hash in the GPU splitter");
     }
-    sd_.key_col[k] = ci;
-    sd_.key_kind[k] = kind;
+    sd_.key_col[nk] = ci;
+    sd_.key_kind[nk] = kind;
+    nk++;
   }
+  sd_.n_keys = nk;
   // JNI buffer layout (jni_common.h:308-382): [validity, (offsets), values] per field
   field_buf0_.resize(fields_.size());
   int nb = 0;
@@ -868,6 +879,7 @@ Status Splitter::Flush() {
   fd.st_ihn = st_ihn_;
   fd.err = d_err_;
   fd.rr_base = rr_sel_;
+  fd.spin_limit = spin_limit_;
   rr_sel_ = (uint32_t)((rr_sel_ + R) % (uint64_t)P);
 
   // tables into staging (host inputs) or a pinned table buffer
@@ -1153,14 +1165,17 @@ Status Splitter::ProcessFlushes() {
 }
 
 // Assembles the record batch of segment `s` of partition `p` from the host copies of the
-// flush outputs and writes it as one IPC message (CacheRecordBatch + WriteIpcPayload).
-Status Splitter::AssembleAndWrite(int p, Segment& s, ByteSink* sink, bool count_only, int64_t* raw) {
+// flush outputs (CacheRecordBatch): its IPC metadata and the byte ranges of its body, padding
+// included, ready to be written (WriteIpcPayload).  Reads only, so partitions can be built in
+// parallel.
+Status Splitter::BuildSegment(int p, const Segment& s, SegMsg* msg) const {
   const int P = P_;
   const int nstr = n_str_;
   const uint32_t n = s.rows;
   std::vector<FieldNodeMeta> nodes;
   std::vector<ChunkedBuffer> bufs;
-  std::vector<std::vector<uint8_t>> temps;
+  std::vector<std::vector<uint8_t>>& temps = msg->temps;
+  temps.clear();
   temps.reserve(2 * fields_.size());
   static const uint8_t kZero4[4] = {0, 0, 0, 0};
   int64_t rawb = 0;
@@ -1265,24 +1280,75 @@ Status Splitter::AssembleAndWrite(int p, Segment& s, ByteSink* sink, bool count_
       bufs.push_back(chars);
     }
   }
-  *raw = rawb;
-  if (count_only) {
-    std::vector<int64_t> lens;
-    for (auto& b : bufs) {
-      int64_t l = 0;
-      for (auto& c : b) l += c.len;
-      lens.push_back(l);
-    }
-    s.message_bytes = RecordBatchMessageSize((int64_t)nodes.size(), lens, &s.body_length);
-    return Status::OK();
+  msg->raw = rawb;
+  std::vector<int64_t> lens(bufs.size(), 0);
+  for (size_t i = 0; i < bufs.size(); i++)
+    for (const Chunk& c : bufs[i]) lens[i] += c.len;
+  RecordBatchHeader(n, nodes, lens, &msg->header, &msg->body);
+  // the body: every buffer's chunks, then zeros up to its 8-byte boundary
+  static const uint8_t kZero8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  msg->pieces.clear();
+  for (size_t i = 0; i < bufs.size(); i++) {
+    for (const Chunk& c : bufs[i])
+      if (c.len > 0) msg->pieces.push_back(c);
+    const int64_t pad = ((lens[i] + 7) & ~int64_t(7)) - lens[i];
+    if (pad) msg->pieces.push_back(Chunk{kZero8, pad});
   }
-  int64_t body = 0;
-  const int64_t wrote = WriteRecordBatchMessage(sink, n, nodes, bufs, &body);
-  if (wrote < 0) return Status::Error(GZ_IO, "write failed");
-  s.body_length = body;
-  s.message_bytes = wrote;
+  msg->bytes = (int64_t)msg->header.size() + msg->body;
   return Status::OK();
 }
+
+namespace {
+
+// Gathers byte ranges and writes them at consecutive offsets of a file (pwritev, at most
+// IOV_MAX ranges a call) or copies them into memory.
+class RangeWriter {
+ public:
+  RangeWriter(int fd, uint8_t* mem, int64_t offset) : fd_(fd), mem_(mem), off_(offset) {}
+  bool Add(const void* p, int64_t n) {
+    if (n <= 0) return true;
+    if (mem_) {
+      memcpy(mem_ + off_, p, (size_t)n);
+      off_ += n;
+      return true;
+    }
+    iov_.push_back(iovec{const_cast<void*>(p), (size_t)n});
+    pending_ += n;
+    return iov_.size() < kMaxIov || Flush();
+  }
+  bool Flush() {
+    size_t i = 0;
+    while (i < iov_.size()) {
+      const int cnt = (int)std::min(iov_.size() - i, kMaxIov);
+      const ssize_t w = pwritev(fd_, iov_.data() + i, cnt, off_);
+      if (w < 0) {
+        if (errno == EINTR) continue;
+        return false;
+      }
+      off_ += w;
+      // drop the ranges written in full; shorten a range written in part
+      size_t left = (size_t)w;
+      while (i < iov_.size() && left >= iov_[i].iov_len) left -= iov_[i++].iov_len;
+      if (left) {
+        iov_[i].iov_base = static_cast<uint8_t*>(iov_[i].iov_base) + left;
+        iov_[i].iov_len -= left;
+      }
+    }
+    iov_.clear();
+    pending_ = 0;
+    return true;
+  }
+
+ private:
+  static constexpr size_t kMaxIov = 1024;
+  int fd_;
+  uint8_t* mem_;
+  int64_t off_;
+  int64_t pending_ = 0;
+  std::vector<iovec> iov_;
+};
+
+}  // namespace
 
 Status Splitter::Stop() {
   if (stopped_) return Status::Error(GZ_INVALID, "splitter already stopped");
@@ -1322,54 +1388,92 @@ Status Splitter::Stop() {
   st = Cuda(cudaStreamSynchronize(ostream_), "D2H partition data");
   if (!st.ok()) return st;
   total_spill_time_ += NowNs() - m0;
-  // write the data file, partitions in order (Stop, splitter.cc:395-437)
-  const int64_t t0 = NowNs();
-  std::unique_ptr<ByteSink> sink;
-  FileSink* fsink = nullptr;
-  if (data_file_.empty()) {
-    sink.reset(new MemorySink());
-  } else {
-    fsink = new FileSink(data_file_);
-    sink.reset(fsink);
-    if (!fsink->ok()) return Status::Error(GZ_IO, "cannot open data file " + data_file_);
-  }
-  int64_t compress_ns = 0;
-  // the schema message written before every partition with rows (WriteSchemaPayload,
-  // splitter.cc:88-90, 145-151)
+
+  // Stop (splitter.cc:395-437): partitions in order, each [schema message if write_schema] +
+  // its record batches + EOS when it has rows, else nothing.  Partitions are independent: their
+  // messages are built in parallel, which gives every partition's length and so its offset in
+  // the data file; then they are written in parallel at those offsets.
+  const int64_t c0 = NowNs();
   std::vector<Field> out_fields = fields_;
   if (pid_field_ >= 0) out_fields.erase(out_fields.begin() + pid_field_);
   const std::vector<uint8_t> schema_msg = opts_.write_schema ? EncodeSchemaMessage(out_fields) : std::vector<uint8_t>();
-  for (int p = 0; p < P_; p++) {
-    auto& segs = segments_[p];
+  std::vector<std::vector<SegMsg>> msgs(P_);
+  std::vector<Status> pst(P_);
+  ParallelFor((size_t)P_, [&](size_t pi) {
+    const int p = (int)pi;
+    const auto& segs = segments_[p];
     if (segs.empty()) {
       partition_lengths_[p] = 0;
-      continue;
+      return;
     }
-    const int64_t before = sink->Tell();
-    if (!schema_msg.empty() && !sink->Write(schema_msg.data(), (int64_t)schema_msg.size()))
-      return Status::Error(GZ_IO, "write failed");
-    for (Segment& s : segs) {
-      int64_t raw = 0;
-      const int64_t c0 = NowNs();
-      st = AssembleAndWrite(p, s, sink.get(), false, &raw);
-      compress_ns += NowNs() - c0;
-      if (!st.ok()) return st;
-      raw_partition_lengths_[p] += raw;
-      if (s.spilled) total_bytes_spilled_ += s.message_bytes;
+    msgs[p].resize(segs.size());
+    int64_t len = (int64_t)schema_msg.size() + 8;  // + EOS
+    int64_t raw = 0;
+    for (size_t i = 0; i < segs.size(); i++) {
+      Status b = BuildSegment(p, segs[i], &msgs[p][i]);
+      if (!b.ok()) {
+        pst[p] = b;
+        return;
+      }
+      len += msgs[p][i].bytes;
+      raw += msgs[p][i].raw;
     }
-    if (!WriteEos(sink.get())) return Status::Error(GZ_IO, "write failed");
-    partition_lengths_[p] = sink->Tell() - before;
-    total_bytes_written_ += partition_lengths_[p];
+    partition_lengths_[p] = len;
+    raw_partition_lengths_[p] += raw;
+  });
+  for (int p = 0; p < P_; p++)
+    if (!pst[p].ok()) return pst[p];
+  std::vector<int64_t> start(P_ + 1, 0);
+  for (int p = 0; p < P_; p++) {
+    start[p + 1] = start[p] + partition_lengths_[p];
+    for (size_t i = 0; i < segments_[p].size(); i++) {
+      segments_[p][i].message_bytes = msgs[p][i].bytes;
+      segments_[p][i].body_length = msgs[p][i].body;
+      if (segments_[p][i].spilled) total_bytes_spilled_ += msgs[p][i].bytes;
+    }
   }
-  if (fsink) {
-    if (!fsink->Close()) return Status::Error(GZ_IO, "closing the data file failed");
+  const int64_t total = start[P_];
+  total_compress_time_ += NowNs() - c0;
+
+  const int64_t t0 = NowNs();
+  int fd = -1;
+  uint8_t* mem = nullptr;
+  if (data_file_.empty()) {
+    data_bytes_.assign((size_t)total, 0);
+    mem = data_bytes_.data();
   } else {
-    data_bytes_ = std::move(static_cast<MemorySink*>(sink.get())->buffer());
+    fd = open(data_file_.c_str(), O_WRONLY | O_CREAT | O_TRUNC, 0644);
+    if (fd < 0) return Status::Error(GZ_IO, "cannot open data file " + data_file_ + ": " + strerror(errno));
+    struct stat sb;
+    const bool regular = fstat(fd, &sb) == 0 && S_ISREG(sb.st_mode);  // not e.g. /dev/null
+    if (regular && total > 0 && ftruncate(fd, total) != 0) {
+      const std::string why = strerror(errno);
+      close(fd);
+      return Status::Error(GZ_IO, "cannot size data file " + data_file_ + ": " + why);
+    }
   }
-  total_compress_time_ += compress_ns;
+  static const uint32_t kEos[2] = {0xFFFFFFFFu, 0u};  // WriteEOS (splitter.cc:166-172)
+  std::vector<char> wrote(P_, 1);
+  ParallelFor((size_t)P_, [&](size_t pi) {
+    const int p = (int)pi;
+    if (msgs[p].empty()) return;
+    RangeWriter w(fd, mem, start[p]);
+    bool ok = w.Add(schema_msg.data(), (int64_t)schema_msg.size());
+    for (const SegMsg& m : msgs[p]) {
+      ok = ok && w.Add(m.header.data(), (int64_t)m.header.size());
+      for (const Chunk& c : m.pieces) ok = ok && w.Add(c.data, c.len);
+    }
+    ok = ok && w.Add(kEos, 8) && w.Flush();
+    wrote[p] = ok;
+  });
+  bool ok = true;
+  for (int p = 0; p < P_; p++) ok = ok && wrote[p];
+  if (fd >= 0 && close(fd) != 0) ok = false;
+  if (!ok) return Status::Error(GZ_IO, "writing the data file failed: " + data_file_);
+  total_bytes_written_ += total;
   stat_emitted_ = 0;
   for (auto& v : segments_) stat_emitted_ += (int64_t)v.size();
-  total_write_time_ += NowNs() - t0 - compress_ns;
+  total_write_time_ += NowNs() - t0;
   stopped_ = true;
   // the pinned copies are no longer needed
   ReleaseHost();
@@ -1437,9 +1541,11 @@ Status Splitter::SpillFixedSize(int64_t size, int64_t* actual) {
       for (Segment& s : segments_[p]) {
         if (s.spilled) continue;
         if (s.body_length < 0) {
-          int64_t raw;
-          st = AssembleAndWrite(p, s, nullptr, true, &raw);
+          SegMsg m;
+          st = BuildSegment(p, s, &m);
           if (!st.ok()) return st;
+          s.body_length = m.body;
+          s.message_bytes = m.bytes;
         }
         cached += s.body_length;
       }

@@ -60,6 +60,8 @@ class Splitter {
   Status SetCompressType(int32_t codec);
   Status LastPids(uint16_t* out, int32_t n);
   Status KernelTimes(double* out4);
+  // Polls of k_scatter's bounded waits for data and free slots in later passes (0: default).
+  void SetSpinLimit(uint32_t polls) { spin_limit_ = polls; }
   // Runs the pending device pass and waits for all device work of the batches split so far.
   Status Sync();
   void Stats(int64_t* out8) const;
@@ -150,7 +152,16 @@ class Splitter {
   Status SyncAndCheck();
   Status MoveFlushToHost(FlushRec& f);
   Status ProcessFlushes();
-  Status AssembleAndWrite(int p, Segment& s, ByteSink* sink, bool count_only, int64_t* raw);
+  // One emitted record batch ready to write: IPC metadata and the byte ranges of its body.
+  struct SegMsg {
+    std::vector<uint8_t> header;
+    std::vector<Chunk> pieces;  // the body in order, padding included
+    std::vector<std::vector<uint8_t>> temps;  // bitmaps assembled for it
+    int64_t bytes = 0;  // header + body
+    int64_t body = 0;
+    int64_t raw = 0;    // its raw buffer bytes (batch_nbytes)
+  };
+  Status BuildSegment(int p, const Segment& s, SegMsg* msg) const;
   uint32_t SplitBatchSize(int32_t num_rows, const std::vector<const int32_t*>& host_offsets,
                           bool* complete);
 
@@ -162,6 +173,7 @@ class Splitter {
   int32_t partitioner_ = PART_HASH;
   int32_t pid_field_ = -1;  // range: the partition id field (0), not an output column
   uint32_t rr_sel_ = 0;     // round-robin selection at the next pass's first row
+  uint32_t spin_limit_ = 0; // k_scatter wait limit (0: the kernel's default)
   // input field index minus this = output schema index
   int32_t out_shift() const { return pid_field_ >= 0 ? 1 : 0; }
   GzSplitOptions opts_{};

@@ -122,10 +122,27 @@ def lib() -> ctypes.CDLL:
         L.gz_split_last_pids.argtypes = [ctypes.c_int64, ctypes.c_void_p, ctypes.c_int32]
         L.gz_last_error.restype = ctypes.c_int
         L.gz_last_error.argtypes = [ctypes.c_int64, ctypes.c_char_p, ctypes.c_size_t]
+        L.gz_debug_set_spin_limit.restype = ctypes.c_int
+        L.gz_debug_set_spin_limit.argtypes = [ctypes.c_int64, ctypes.c_uint32]
         L.gz_split_stats.restype = ctypes.c_int
         L.gz_split_stats.argtypes = [ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
         L.gz_split_kernel_times.restype = ctypes.c_int
         L.gz_split_kernel_times.argtypes = [ctypes.c_int64, ctypes.POINTER(ctypes.c_double)]
+        L.gz_reader_make.restype = ctypes.c_int
+        L.gz_reader_make.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, c_i64p]
+        L.gz_reader_make_fields.restype = ctypes.c_int
+        L.gz_reader_make_fields.argtypes = [ctypes.POINTER(GzField), ctypes.c_int32, ctypes.c_int32, c_i64p]
+        L.gz_reader_add_stream.restype = ctypes.c_int
+        L.gz_reader_add_stream.argtypes = [ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64]
+        L.gz_reader_finish.restype = ctypes.c_int
+        L.gz_reader_finish.argtypes = [ctypes.c_int64, c_i64p, ctypes.POINTER(ctypes.c_int32)]
+        L.gz_reader_column.restype = ctypes.c_int
+        L.gz_reader_column.argtypes = [ctypes.c_int64, ctypes.c_int32, ctypes.POINTER(GzDeviceColumn)]
+        L.gz_reader_column_to_host.restype = ctypes.c_int
+        L.gz_reader_column_to_host.argtypes = [ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.c_void_p]
+        L.gz_reader_close.restype = ctypes.c_int
+        L.gz_reader_close.argtypes = [ctypes.c_int64]
         L.gz_serve_start.restype = ctypes.c_int
         L.gz_serve_start.argtypes = [ctypes.c_int32, ctypes.c_int64, c_i64p]
         L.gz_serve_open.restype = ctypes.c_int
@@ -156,6 +173,117 @@ def lib() -> ctypes.CDLL:
         L.gz_tune_load.argtypes = [ctypes.c_char_p]
         _lib = L
     return _lib
+
+
+TASK_LIB_PATH = os.path.join(HERE, "libgztask.so")
+
+
+class GzTaskJob(ctypes.Structure):
+    _fields_ = [
+        ("short_name", ctypes.c_char_p),
+        ("num_partitions", ctypes.c_int32),
+        ("fields", ctypes.POINTER(GzField)),
+        ("n_fields", ctypes.c_int32),
+        ("key_cols", ctypes.c_void_p),
+        ("n_keys", ctypes.c_int32),
+        ("opts", ctypes.POINTER(GzSplitOptions)),
+        ("data_dir", ctypes.c_char_p),
+        ("n_tasks", ctypes.c_int32),
+        ("n_batches", ctypes.c_int32),
+        ("rows", ctypes.c_void_p),
+        ("addrs", ctypes.c_void_p),
+        ("sizes", ctypes.c_void_p),
+        ("n_bufs", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
+class GzTaskResult(ctypes.Structure):
+    _fields_ = [
+        ("wall_s", ctypes.c_double),
+        ("split_s_max", ctypes.c_double),
+        ("stop_s_max", ctypes.c_double),
+        ("input_bytes", ctypes.c_int64),
+        ("raw_partition_bytes", ctypes.c_int64),
+        ("bytes_written", ctypes.c_int64),
+        ("partition_lengths", ctypes.POINTER(ctypes.c_int64)),
+        ("error", ctypes.c_char * 512),
+    ]
+
+
+_task_lib = None
+
+
+def task_lib() -> ctypes.CDLL:
+    """libgztask.so: simulated map tasks calling the C ABI (include/gz_task.h)."""
+    global _task_lib
+    if _task_lib is None:
+        lib()  # the splitter library first
+        if not os.path.exists(TASK_LIB_PATH):
+            raise RuntimeError(f"{TASK_LIB_PATH} is missing: run __graft_entry__.build() first")
+        L = ctypes.CDLL(TASK_LIB_PATH)
+        L.gz_task_run.restype = ctypes.c_int
+        L.gz_task_run.argtypes = [ctypes.POINTER(GzTaskJob), ctypes.POINTER(GzTaskResult)]
+        L.gz_task_digest_file.restype = ctypes.c_int
+        L.gz_task_digest_file.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint64),
+                                          ctypes.POINTER(ctypes.c_int64)]
+        L.gz_task_digest.restype = ctypes.c_uint64
+        L.gz_task_digest.argtypes = [ctypes.c_void_p, ctypes.c_int64]
+        _task_lib = L
+    return _task_lib
+
+
+def run_map_tasks(part: "NativePartitioning", rows, bufAddrs, bufSizes, nTasks: int,
+                  dataDir: str = "", **options) -> dict:
+    """Runs `nTasks` simulated map tasks (the writer's make / split per batch / stop / close loop,
+    natively, on their own threads) over contiguous ranges of the batches; each writes
+    <dataDir>/task-<t>.data.  Returns the timings, byte counts and per-task partition lengths."""
+    o, keep = split_options(**options)
+    arr, names = _fields(part.fields)
+    keys = np.asarray(list(part.keyColumns), np.int32)
+    rows = np.ascontiguousarray(rows, dtype=np.int32)
+    addrs = np.ascontiguousarray(bufAddrs, dtype=np.int64)
+    sizes = np.ascontiguousarray(bufSizes, dtype=np.int64)
+    P = 1 if part.shortName == "single" else part.numPartitions
+    pl = np.zeros((nTasks, P), np.int64)
+    job = GzTaskJob(part.shortName.encode(), part.numPartitions, arr, len(part.fields), keys.ctypes.data,
+                    len(keys), ctypes.pointer(o), dataDir.encode(), nTasks, len(rows), rows.ctypes.data,
+                    addrs.ctypes.data, sizes.ctypes.data, addrs.shape[1], 0)
+    res = GzTaskResult()
+    res.partition_lengths = pl.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+    st = task_lib().gz_task_run(ctypes.byref(job), ctypes.byref(res))
+    del keep, names
+    if st != GZ_OK:
+        raise SplitterError(st, res.error.decode(errors="replace"))
+    return {"wall_s": res.wall_s, "split_s_max": res.split_s_max, "stop_s_max": res.stop_s_max,
+            "input_bytes": res.input_bytes, "raw_partition_bytes": res.raw_partition_bytes,
+            "bytes_written": res.bytes_written, "partition_lengths": pl}
+
+
+def digest_file(path: str):
+    """(checksum, size) of a file, as libgztask computes it."""
+    d, n = ctypes.c_uint64(0), ctypes.c_int64(0)
+    if task_lib().gz_task_digest_file(path.encode(), ctypes.byref(d), ctypes.byref(n)) != 0:
+        raise OSError(f"cannot read {path}")
+    return d.value, n.value
+
+
+def digest_bytes(data) -> int:
+    b = np.frombuffer(data, np.uint8) if not isinstance(data, np.ndarray) else data
+    return int(task_lib().gz_task_digest(b.ctypes.data if b.nbytes else None, b.nbytes))
+
+
+class GzDeviceColumn(ctypes.Structure):
+    _fields_ = [
+        ("type", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("length", ctypes.c_int64),
+        ("null_count", ctypes.c_int64),
+        ("validity", ctypes.c_void_p),
+        ("offsets", ctypes.c_void_p),
+        ("values", ctypes.c_void_p),
+        ("values_bytes", ctypes.c_int64),
+    ]
 
 
 def _check(status: int, handle: int = 0) -> None:
@@ -328,6 +456,10 @@ class ShuffleSplitterJniWrapper:
     def sync(self, splitterId: int) -> None:
         _check(lib().gz_split_sync(splitterId), splitterId)
 
+    def setSpinLimit(self, splitterId: int, polls: int) -> None:
+        """Test hook: polls of k_scatter's bounded waits in later passes (0: the default)."""
+        _check(lib().gz_debug_set_spin_limit(splitterId, polls), splitterId)
+
     def stats(self, splitterId: int) -> List[int]:
         """[passes, input bytes, H2D bytes, D2H bytes, HBM-resident bytes, batches, rows,
         emitted record batches]."""
@@ -454,3 +586,56 @@ class ServeLoop:
         if self.handle:
             lib().gz_serve_shutdown(self.handle)
             self.handle = 0
+
+
+class PartitionReader:
+    """The reduce side: the IPC streams of one partition (a map output's partition_lengths[p]
+    bytes of its data file each) read into one set of Arrow columns in device memory.  Stands in
+    for the reference's ArrowColumnarBatchSerializer + ShuffleDecompressionJniWrapper read path."""
+
+    def __init__(self, schema, device: int = 0):
+        h = ctypes.c_int64(0)
+        if isinstance(schema, (bytes, bytearray)):
+            sb = ctypes.create_string_buffer(bytes(schema), len(schema))
+            _check(lib().gz_reader_make(sb, len(schema), device, ctypes.byref(h)))
+        else:
+            arr, self._names = _fields(schema)
+            _check(lib().gz_reader_make_fields(arr, len(schema), device, ctypes.byref(h)))
+        self.h = h.value
+        self.schema = schema
+
+    def addStream(self, data) -> None:
+        b = np.frombuffer(data, np.uint8) if not isinstance(data, np.ndarray) else data.view(np.uint8)
+        _check(lib().gz_reader_add_stream(self.h, b.ctypes.data if b.nbytes else None, b.nbytes))
+
+    def finish(self):
+        rows, nb = ctypes.c_int64(0), ctypes.c_int32(0)
+        _check(lib().gz_reader_finish(self.h, ctypes.byref(rows), ctypes.byref(nb)))
+        return rows.value, nb.value
+
+    def column(self, field: int) -> GzDeviceColumn:
+        c = GzDeviceColumn()
+        _check(lib().gz_reader_column(self.h, field, ctypes.byref(c)))
+        return c
+
+    def column_to_host(self, field: int):
+        """(validity bytes or None, offsets or None, values bytes) of a concatenated column."""
+        c = self.column(field)
+        valid = np.zeros((c.length + 7) // 8, np.uint8) if c.validity else None
+        offs = np.zeros(c.length + 1, np.int32) if c.offsets else None
+        vals = np.zeros(c.values_bytes, np.uint8)
+        _check(lib().gz_reader_column_to_host(self.h, field, valid.ctypes.data if valid is not None else None,
+                                              offs.ctypes.data if offs is not None else None,
+                                              vals.ctypes.data if vals.nbytes else None))
+        return valid, offs, vals
+
+    def close(self) -> None:
+        if self.h:
+            lib().gz_reader_close(self.h)
+            self.h = 0
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

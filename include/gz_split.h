@@ -266,7 +266,8 @@ GzStatus gz_serve_shutdown(int64_t server);
 
 /* One hash-key column of a batch that is already in device memory. */
 typedef struct GzKeyColumn {
-  int32_t type;             /* GzType: BOOL, INT8, INT16, INT32, FLOAT32, DATE32, INT64, FLOAT64 */
+  int32_t type;             /* GzType: BOOL, INT8, INT16, INT32, FLOAT32, DATE32, INT64, FLOAT64;
+                               NULL: a null-type key, which leaves the hash unchanged */
   int32_t reserved;
   const uint8_t* validity;  /* device address of the validity bitmap (LSB first); NULL: no nulls */
   const uint8_t* values;    /* device address of the values (bit-packed for BOOL) */
@@ -285,13 +286,18 @@ typedef struct GzKeyColumn {
  * cudaFree may synchronise it.  Inputs and outputs are the caller's device memory.
  *
  * Its scratch, the per-tile row counts, is one 16 MiB array in the library's own device
- * memory, held on every device where the library runs until the process exits.  A call needs
+ * memory, held until the process exits on every device where the library has run.  With CUDA's
+ * lazy module loading (the default) the array is reserved on a device by the first call there,
+ * so make that first call (a zero-row call will do) before a pool reserves the device's free
+ * memory; if it cannot be reserved the call returns GZ_OOM.  A call needs
  * ceil(num_rows / 1024) * num_partitions 32-bit counters, at most 4,194,304 (e.g. 65,536 rows
  * at 65,536 partitions, or 21 million rows at 200); a larger call returns GZ_INVALID.  All calls
  * on a device share the array and it keeps the last call's contents (each call clears what it
  * uses), so calls that may overlap on the GPU (other streams, other threads) race and give
  * wrong counts: put them on one stream.  The first call on a device looks up the array's device
- * address with that device current; make that first call before any stream capture.
+ * address with that device current; make that first call before any stream capture.  Only the
+ * device's primary context (the CUDA runtime's) is supported.  A CUDA error already pending on
+ * the calling thread is reported as GZ_CUDA before anything is launched and is left pending.
  *
  * The work is enqueued on `stream` (a cudaStream_t of that device, NULL: its default stream)
  * and the call returns without waiting; the calling thread's current device is left as it
@@ -299,6 +305,57 @@ typedef struct GzKeyColumn {
 GzStatus gz_hash_partition_static(int32_t device, int32_t num_partitions, const GzKeyColumn* keys,
                                   int32_t n_keys, int32_t num_rows, uint16_t* d_pids,
                                   int64_t* d_counts, void* stream);
+
+/* ---- reduce-side read (replaces the reference's read of a partition's shuffle blocks) ---
+ * The reference reads each map output's bytes of a partition with Arrow Java
+ * (ArrowColumnarBatchSerializer.scala:110-240: an IPC stream reader, one ColumnarBatch per
+ * record batch) and decompresses compressed bodies through ShuffleDecompressionJniWrapper
+ * (jni_wrapper.cc:1236-1322).  Here the streams of one partition are read into HBM: the host
+ * parses the IPC metadata, the bodies go to the device in one copy per stream, and device
+ * kernels concatenate the record batches of all streams into one set of Arrow columns (values
+ * and characters copied, offsets rebased, validity bits moved to their rows).  The result stays
+ * in device memory owned by the reader until gz_reader_close. */
+
+/* One column of the concatenated partition, in device memory. */
+typedef struct GzDeviceColumn {
+  int32_t type;            /* GzType */
+  int32_t reserved;
+  int64_t length;          /* rows */
+  int64_t null_count;
+  const uint8_t* validity; /* LSB-first bitmap, (length + 7) / 8 bytes; NULL: no nulls */
+  const int32_t* offsets;  /* binary / utf8: length + 1 offsets from 0; NULL otherwise */
+  const uint8_t* values;   /* fixed width: length * width bytes; bool: bitmap; binary: characters */
+  int64_t values_bytes;
+} GzDeviceColumn;
+
+/* A reader for partitions of `schema_ipc` (an encapsulated Arrow IPC Schema message, as
+ * ShuffleDecompressionJniWrapper.make receives) on CUDA device `device`. */
+GzStatus gz_reader_make(const uint8_t* schema_ipc, int64_t schema_len, int32_t device, int64_t* out_handle);
+
+/* Same with the schema as a field array. */
+GzStatus gz_reader_make_fields(const GzField* fields, int32_t n_fields, int32_t device, int64_t* out_handle);
+
+/* Adds one IPC stream of the partition (host bytes: a map output's partition_lengths[p] bytes of
+ * its data file, with or without the schema message in front, ending with the end-of-stream
+ * marker); the bytes are read before the call returns.  Compressed bodies return
+ * GZ_NOT_IMPLEMENTED. */
+GzStatus gz_reader_add_stream(int64_t handle, const uint8_t* stream, int64_t len);
+
+/* Concatenates the record batches of every stream added, in order, into device columns and
+ * waits for the device; *out_rows = rows, *out_batches = record batches read. */
+GzStatus gz_reader_finish(int64_t handle, int64_t* out_rows, int32_t* out_batches);
+
+/* The concatenated column of schema field `field` (after gz_reader_finish). */
+GzStatus gz_reader_column(int64_t handle, int32_t field, GzDeviceColumn* out);
+
+/* Copies the concatenated column of `field` to host memory: `validity` ((length + 7) / 8 bytes;
+ * skipped when NULL or when the column has no nulls), `offsets` (length + 1 int32, binary only),
+ * `values` (values_bytes bytes).  Waits for the copies. */
+GzStatus gz_reader_column_to_host(int64_t handle, int32_t field, uint8_t* validity, int32_t* offsets,
+                                  uint8_t* values);
+
+/* Frees the reader and its device columns. */
+GzStatus gz_reader_close(int64_t handle);
 
 /* ---- test hooks (no reference counterpart; used by the unit tests) ------------------- */
 
@@ -314,6 +371,13 @@ GzStatus gz_debug_encode_record_batch(int64_t length, const int64_t* nodes, int3
  * message written before each partition when write_schema is set). */
 GzStatus gz_debug_reencode_schema(const uint8_t* schema_ipc, int64_t len, uint8_t* out, int64_t cap,
                                   int64_t* out_len);
+
+/* Sets how many times k_scatter polls a wait for a staged slice or a free staging slot in the
+ * handle's later device passes before it gives up (0: the default, about 2^26).  A block that
+ * gives up stops issuing copies, waits (with the default limit) for the copies already in flight,
+ * skips its remaining work and sets an error bit: the next synchronising call returns GZ_TIMEOUT
+ * and the device stays usable.  Lets a test make the bounded waits run out. */
+GzStatus gz_debug_set_spin_limit(int64_t handle, uint32_t polls);
 
 /* Parses an Arrow IPC Schema message; writes up to `cap` GzType codes and nullable flags. */
 GzStatus gz_debug_parse_schema(const uint8_t* schema_ipc, int64_t len, int32_t* types,

@@ -1,0 +1,133 @@
+"""ORACLE - test infrastructure only.
+
+A plain-Python restatement of the reduce-side read of the shuffle: Arrow IPC streams (the
+encapsulated message format the reference's partition writers produce, splitter.cc:84-172, and
+Arrow Java reads back on the reduce side, ArrowColumnarBatchSerializer.scala:110-240) parsed
+message by message, and the record batches of all streams of a partition concatenated into one
+set of columns, as numpy arrays.  Pinned against pyarrow's IPC reader and concat in the CPU
+tests; the GPU tests check the CUDA reader (gz_reader_*) against it.
+
+Only tests/ use this file.
+"""
+from __future__ import annotations
+
+import struct
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+
+# Arrow Message.fbs: MessageHeader union values
+HEADER_SCHEMA, HEADER_RECORD_BATCH = 1, 3
+BYTE_WIDTH = {"int8": 1, "uint8": 1, "int16": 2, "uint16": 2, "float16": 2, "int32": 4, "uint32": 4,
+              "float32": 4, "date32": 4, "time32": 4, "int64": 8, "uint64": 8, "float64": 8,
+              "date64": 8, "time64": 8, "timestamp": 8, "decimal128": 16}
+
+
+class _Flat:
+    """Flatbuffer tables: field `i` of the table at `t` through its vtable."""
+
+    def __init__(self, b: bytes):
+        self.b = b
+
+    def u32(self, p):
+        return struct.unpack_from("<I", self.b, p)[0]
+
+    def field(self, t, i):
+        vt = t - struct.unpack_from("<i", self.b, t)[0]
+        vsize = struct.unpack_from("<H", self.b, vt)[0]
+        if 4 + 2 * i >= vsize:
+            return None
+        off = struct.unpack_from("<H", self.b, vt + 4 + 2 * i)[0]
+        return t + off if off else None
+
+    def scalar(self, t, i, fmt, default=0):
+        f = self.field(t, i)
+        return struct.unpack_from("<" + fmt, self.b, f)[0] if f is not None else default
+
+    def table(self, t, i):
+        f = self.field(t, i)
+        return None if f is None else f + self.u32(f)
+
+
+def parse_stream(data: bytes, schema) -> List[Tuple[int, list]]:
+    """Record batches of one stream: [(rows, [per field (null_count, [buffer bytes...])])]."""
+    out = []
+    pos = 0
+    n = len(data)
+    while pos < n:
+        first = struct.unpack_from("<I", data, pos)[0]
+        if first == 0xFFFFFFFF:
+            meta_len = struct.unpack_from("<i", data, pos + 4)[0]
+            meta_pos = pos + 8
+        else:
+            meta_len, meta_pos = first, pos + 4
+        if meta_len == 0:
+            break
+        fb = _Flat(data[meta_pos:meta_pos + meta_len])
+        msg = fb.u32(0)
+        htype = fb.scalar(msg, 1, "B")
+        body_len = fb.scalar(msg, 3, "q")
+        body = meta_pos + meta_len
+        if htype == HEADER_RECORD_BATCH:
+            rb = fb.table(msg, 2)
+            assert fb.table(rb, 3) is None, "compressed bodies"
+            rows = fb.scalar(rb, 0, "q")
+            nodes, bufs = fb.table(rb, 1), fb.table(rb, 2)
+            nn, nb = fb.u32(nodes), fb.u32(bufs)
+            node_list = [struct.unpack_from("<qq", fb.b, nodes + 4 + 16 * i) for i in range(nn)]
+            buf_list = [struct.unpack_from("<qq", fb.b, bufs + 4 + 16 * i) for i in range(nb)]
+            cols, bi = [], 0
+            for f, (length, nulls) in zip(schema, node_list):
+                assert length == rows
+                k = 0 if f.type == "null" else (3 if f.is_binary else 2)
+                cols.append((nulls, [data[body + o: body + o + l] for o, l in buf_list[bi:bi + k]]))
+                bi += k
+            out.append((rows, cols))
+        elif htype != HEADER_SCHEMA:
+            raise ValueError(f"message type {htype}")
+        pos = body + ((body_len + 7) & ~7)
+    return out
+
+
+def _bits(buf: bytes, n: int) -> np.ndarray:
+    return np.unpackbits(np.frombuffer(buf, np.uint8), bitorder="little")[:n].astype(bool)
+
+
+def read_partition(schema, streams: Sequence[bytes]):
+    """Concatenation of the record batches of `streams`, in order: (rows, per field (validity
+    bits as a bool array or None when the column has no nulls, int32 offsets or None, values as
+    bytes; bool values as a bool array))."""
+    batches = [b for s in streams for b in parse_stream(s, schema)]
+    rows = sum(r for r, _ in batches)
+    cols = []
+    for fi, f in enumerate(schema):
+        if f.type == "null":
+            cols.append((None, None, b""))
+            continue
+        nulls = sum(c[fi][0] for _, c in batches)
+        valid = None
+        if nulls:
+            valid = np.concatenate([_bits(c[fi][1][0], r) if c[fi][0] else np.ones(r, bool)
+                                    for r, c in batches]) if batches else np.zeros(0, bool)
+        if f.type == "bool":
+            vals = np.concatenate([_bits(c[fi][1][1], r) for r, c in batches]) if batches else np.zeros(0, bool)
+            cols.append((valid, None, vals))
+        elif f.is_binary:
+            offs, chars, base = [np.zeros(1, np.int32)], [], 0
+            for r, c in batches:
+                o = np.frombuffer(c[fi][1][1], np.int32)[:r + 1]
+                chars.append(c[fi][1][2][o[0]:o[r]])
+                offs.append((o[1:] - o[0] + base).astype(np.int32))
+                base += int(o[r] - o[0])
+            cols.append((valid, np.concatenate(offs), b"".join(chars)))
+        else:
+            w = BYTE_WIDTH[f.type]
+            cols.append((valid, None, b"".join(c[fi][1][1][:r * w] for r, c in batches)))
+    return rows, cols
+
+
+def pack_bits(v: Optional[np.ndarray]) -> Optional[bytes]:
+    """An LSB-first bitmap of a bool array, zero padded (None stays None)."""
+    if v is None:
+        return None
+    return np.packbits(v.astype(np.uint8), bitorder="little").tobytes()

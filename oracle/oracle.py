@@ -38,9 +38,23 @@ def build_oracle(force: bool = False) -> str:
     return ORACLE_SO
 
 
-def build_ref(ref_root: str = "/root/reference") -> bool:
+def reference_root():
+    """The reference source tree to compile and read fixtures from: $GZ_REFERENCE_ROOT, else the
+    recipe's default (REF in oracle/ref/Makefile); None when neither names a tree."""
+    root = os.environ.get("GZ_REFERENCE_ROOT")
+    if not root:
+        try:
+            out = subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), "print-ref"],
+                                 capture_output=True, text=True, timeout=30)
+            root = out.stdout.strip() if out.returncode == 0 else ""
+        except (OSError, subprocess.SubprocessError):
+            root = ""
+    return root if root and os.path.isdir(os.path.join(root, "native-sql-engine")) else None
+
+
+def build_ref(ref_root: str) -> bool:
     """Compile the reference Splitter (x86_64 + pyarrow + reference tree only)."""
-    if not os.path.isdir(os.path.join(ref_root, "native-sql-engine")):
+    if not ref_root or not os.path.isdir(os.path.join(ref_root, "native-sql-engine")):
         return False
     subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "ref"), f"REF={ref_root}"])
     return os.path.exists(REF_SO)

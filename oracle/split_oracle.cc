@@ -277,7 +277,9 @@ class OracleSplitter {
     for (int k : keys_) {
       if (k < 0 || k >= (int)fields_.size()) return "key column out of range";
       int t = fields_[k].type;
-      if (!(t == T_BOOL || t == T_INT8 || t == T_INT16 || t == T_INT32 || t == T_DATE32 ||
+      // a null-type key adds nothing to the chain (CreateProjector's NullType case,
+      // splitter.cc:1407-1408)
+      if (!(t == T_NULL || t == T_BOOL || t == T_INT8 || t == T_INT16 || t == T_INT32 || t == T_DATE32 ||
             t == T_FLOAT32 || t == T_INT64 || t == T_FLOAT64 || t == T_STRING))
         return "key type has no Spark hash";
     }
@@ -365,12 +367,21 @@ class OracleSplitter {
     schema_msg_.assign(p, p + n);
   }
 
+  // With a data file, each partition is written as soon as it is assembled, as the reference's
+  // partition writers append to the data file (WriteCachedRecordBatchAndClose, splitter.cc:84-109);
+  // without one the bytes are kept in *file_bytes.
   std::string Stop(const char* data_file, std::vector<uint8_t>* file_bytes) {
     std::vector<uint8_t> out;
+    FILE* f = nullptr;
+    if (data_file && data_file[0]) {
+      f = fopen(data_file, "wb");
+      if (!f) return std::string("cannot open data file ") + data_file;
+    }
     for (int p = 0; p < P_; p++) {
       CacheRecordBatch(p, true);
       if (cached_size_[p] > 0) writer_[p] = true;
       if (writer_[p]) {
+        if (f) out.clear();
         size_t before = out.size();
         // WriteSchemaPayload before the partition's batches when write_schema (splitter.cc:88-90)
         if (opt_.write_schema) out.insert(out.end(), schema_msg_.begin(), schema_msg_.end());
@@ -378,7 +389,7 @@ class OracleSplitter {
         if (spill_opened_[p]) {
           out.insert(out.end(), spilled_[p].begin(), spilled_[p].end());
           bytes_spilled_ += (int64_t)spilled_[p].size();
-          spilled_[p].clear();
+          std::vector<uint8_t>().swap(spilled_[p]);
         }
         for (auto& m : cached_[p]) out.insert(out.end(), m.begin(), m.end());
         cached_[p].clear();
@@ -387,18 +398,17 @@ class OracleSplitter {
         out.insert(out.end(), (uint8_t*)eos, (uint8_t*)eos + 8);
         partition_lengths_[p] = (int64_t)(out.size() - before);
         bytes_written_ += partition_lengths_[p];
+        if (f && fwrite(out.data(), 1, out.size(), f) != out.size()) {
+          fclose(f);
+          return "short write";
+        }
       } else {
         partition_lengths_[p] = 0;
       }
     }
-    if (data_file && data_file[0]) {
-      FILE* f = fopen(data_file, "wb");
-      if (!f) return std::string("cannot open data file ") + data_file;
-      if (!out.empty() && fwrite(out.data(), 1, out.size(), f) != out.size()) {
-        fclose(f);
-        return "short write";
-      }
-      fclose(f);
+    if (f) {
+      if (fclose(f) != 0) return "closing the data file failed";
+      out.clear();
     }
     if (file_bytes) *file_bytes = std::move(out);
     return "";
@@ -442,6 +452,7 @@ class OracleSplitter {
     for (int32_t r = 0; r < n; r++) {
       int32_t h = 42;
       for (int k : keys_) {
+        if (fields_[k].type == T_NULL) continue;  // no hash function (splitter.cc:1407-1408)
         const InCol& c = cols[k];
         if (c.validity && !GetBit(c.validity, r)) continue;  // null: seed passes through
         switch (fields_[k].type) {

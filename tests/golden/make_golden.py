@@ -285,7 +285,7 @@ def partitioner_cases():
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else O.reference_root()
     if not O.build_ref(ref_root):
         raise SystemExit("reference tree not found")
     recs = []

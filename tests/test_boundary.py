@@ -12,19 +12,29 @@ from gazelle_plugin_gb300 import shuffle as S
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def declared_symbols():
-    names = []
-    for fn in os.listdir(os.path.join(ROOT, "include")):
-        if fn.endswith(".h"):
-            src = open(os.path.join(ROOT, "include", fn)).read()
-            names += re.findall(r"^\w[\w\s\*]*?\b(gz_\w+)\(", src, re.M)
-    return sorted(set(names))
+def declared_symbols(header="gz_split.h"):
+    src = open(os.path.join(ROOT, "include", header)).read()
+    return sorted(set(re.findall(r"^\w[\w\s\*]*?\b(gz_\w+)\(", src, re.M)))
+
+
+def test_every_header_is_checked():
+    assert sorted(f for f in os.listdir(os.path.join(ROOT, "include")) if f.endswith(".h")) == \
+        ["gz_split.h", "gz_task.h"]
 
 
 def test_library_exports_every_declared_symbol():
     lib = S.lib()
     names = declared_symbols()
     assert "gz_split_make" in names and "gz_split_stop" in names
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_task_driver_exports_every_declared_symbol():
+    """libgztask.so, the simulated map tasks that call the C ABI (include/gz_task.h)."""
+    lib = S.task_lib()
+    names = declared_symbols("gz_task.h")
+    assert "gz_task_run" in names
     for n in names:
         assert hasattr(lib, n), n
 

@@ -136,3 +136,29 @@ def test_oracle_spill_fixed_size_matches_reference_policy():
         ro, so = r.stop(), s3.stop()
         assert ro.data == so.data and ro.bytes_spilled == so.bytes_spilled
         r.close()
+
+
+def _null_key_case():
+    """The c1 workload with a null-type field in front of it, listed first among the keys."""
+    schema = [W.Field("n", "null")] + list(W.C1_SCHEMA)
+    empty = np.zeros(0, np.uint8)
+    batches = [W.Batch(b.num_rows, [empty, empty] + list(b.buffers)) for b in W.c1_batches(3, 4, 2000)]
+    return schema, batches, [0] + [k + 1 for k in W.C1_KEYS]
+
+
+def test_oracle_null_type_key_leaves_hash_unchanged():
+    """CreateProjector adds nothing to the chain for a NullType key (splitter.cc:1407-1408)."""
+    schema, batches, keys = _null_key_case()
+    with_null = O.run_oracle(schema, batches, 8, keys)
+    without = O.run_oracle(schema, batches, 8, keys[1:])
+    assert with_null.data == without.data
+    assert (with_null.partition_lengths == without.partition_lengths).all()
+
+
+@pytest.mark.skipif(not O.RefSplitter.available(), reason="reference build absent here")
+def test_oracle_null_type_key_matches_live_reference():
+    schema, batches, keys = _null_key_case()
+    r = O.run_ref(schema, batches, 8, keys)
+    o = O.run_oracle(schema, batches, 8, keys)
+    assert r.data == o.data
+    assert (r.raw_partition_lengths == o.raw_partition_lengths).all()

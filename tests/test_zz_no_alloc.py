@@ -6,10 +6,13 @@ task's budget), or they must not let cudaMalloc / cudaFree stall the device.  Fo
 library computes a batch's partition ids and per-partition row counts with its scratch in a
 fixed 16 MiB device array of its own.
 
-Checked through the C ABI against the splitter's own partition ids (gz_split_last_pids) for the
-same batch, exactly, on calls in a row that share and reuse that array (shared-memory and
-global-memory count paths, then the first case again).  Collected last so that a run stopping at
-the first failure has run every other test first; it also passes alone in a fresh process.
+Checked through the C ABI, exactly, against the oracle's partition ids and against the
+splitter's own (gz_split_last_pids) for the same batch, on calls in a row that share and reuse
+that array (shared-memory and global-memory count paths, then the first case again, and a key
+list with a null-type key, which leaves the hash unchanged).  Around every call after the first,
+the device's free memory must not change: the call allocates nothing.  Collected last so that a
+run stopping at the first failure has run every other test first; it also passes alone in a
+fresh process.
 """
 import ctypes
 
@@ -18,6 +21,7 @@ import pytest
 
 from gazelle_plugin_gb300 import shuffle as S
 from gazelle_plugin_gb300 import workloads as W
+from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
@@ -58,6 +62,15 @@ def _splitter_pids(schema, keys, P, batch):
         w.close(h)
 
 
+def _oracle_pids(schema, keys, P, batch):
+    o = O.OracleSplitter(schema, P, keys)
+    try:
+        o.split(batch)
+        return o.last_pids(batch.num_rows)
+    finally:
+        o.close()
+
+
 def _device_keys(schema, keys, batch):
     """Key columns copied to the device; returns the ctypes array and the tensors that own it."""
     first = []
@@ -67,11 +80,15 @@ def _device_keys(schema, keys, batch):
         b += 3 if f.is_binary else 2
     hold, cols = [], (GzKeyColumn * len(keys))()
     for j, k in enumerate(keys):
+        cols[j].type = schema[k].code
+        if schema[k].type == "null":  # no buffers are read
+            cols[j].values = None
+            cols[j].validity = None
+            continue
         valid = batch.buffers[first[k]].view(np.uint8)
         vals = batch.buffers[first[k] + 1].view(np.uint8)
         dv = torch.from_numpy(vals.copy()).cuda()
         hold.append(dv)
-        cols[j].type = schema[k].code
         cols[j].values = dv.data_ptr()
         if valid.nbytes:
             dm = torch.from_numpy(valid.copy()).cuda()
@@ -87,13 +104,25 @@ def _static_call(schema, keys, P, batch):
     n = batch.num_rows
     pids16 = torch.full((max(n, 1),), -1, dtype=torch.int16, device="cuda")  # 0xFFFF: unwritten
     counts = torch.full((P,), -1, dtype=torch.int64, device="cuda")
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
     st = _entry()(0, P, cols, len(keys), n, pids16.data_ptr(), counts.data_ptr(),
                   torch.cuda.current_stream().cuda_stream)
     assert st == 0, _last_error()
     torch.cuda.synchronize()
+    free_after = torch.cuda.mem_get_info()[0]
     del hold
     got = pids16[:n].cpu().numpy().view(np.uint16)
-    return got, counts.cpu().numpy()
+    return got, counts.cpu().numpy(), free_before - free_after
+
+
+def _with_null_key():
+    """The c1 schema with a null-type field in front, listed first among the keys."""
+    schema = [W.Field("n", "null")] + list(W.C1_SCHEMA)
+    b = W.c1_batches(44, 1, 3000)[0]
+    empty = np.zeros(0, np.uint8)
+    batch = W.Batch(b.num_rows, [empty, empty] + list(b.buffers))
+    return schema, [0] + [k + 1 for k in W.C1_KEYS], batch
 
 
 CASES = [
@@ -107,13 +136,18 @@ CASES = [
 ]
 
 
-def test_static_scratch_matches_splitter_on_consecutive_calls():
-    for tag, schema, keys, P, make in CASES:
-        batch = make()
-        want = _splitter_pids(schema, keys, P, batch)
-        got, counts = _static_call(schema, keys, P, batch)
+def test_static_scratch_matches_oracle_and_splitter_on_consecutive_calls():
+    cases = [(tag, schema, keys, P, make()) for tag, schema, keys, P, make in CASES]
+    nschema, nkeys, nbatch = _with_null_key()
+    cases.append(("null-type key", nschema, nkeys, 8, nbatch))
+    for i, (tag, schema, keys, P, batch) in enumerate(cases):
+        want = _oracle_pids(schema, keys, P, batch)
+        assert np.array_equal(_splitter_pids(schema, keys, P, batch), want), tag
+        got, counts, grown = _static_call(schema, keys, P, batch)
         assert np.array_equal(got, want), tag
         assert np.array_equal(counts, np.bincount(want, minlength=P).astype(np.int64)), tag
+        if i > 0:  # the first call on the device may load the module that holds the array
+            assert grown == 0, f"{tag}: free device memory fell by {grown} bytes during the call"
 
 
 def test_static_scratch_rejects_oversized_call():
