@@ -157,7 +157,7 @@ void gz_split_default_options(GzSplitOptions* o) {
   o->buffered_write = 0;
   o->input_kind = GZ_INPUT_HOST;
   o->device = 0;
-  o->keep_output_on_device = 1;
+  o->keep_output_on_device = -1;
   o->flush_bytes = 512ll << 20;
   o->device_budget = 64ll << 30;
   o->data_file = nullptr;
@@ -622,6 +622,39 @@ GzStatus gz_debug_encode_record_batch(int64_t length, const int64_t* nodes, int3
   gz::MemorySink sink;
   int64_t body = 0;
   if (gz::WriteRecordBatchMessage(&sink, length, nm, bb, &body) < 0) return GZ_IO;
+  *out_len = (int64_t)sink.buffer().size();
+  if (*out_len > out_cap) return GZ_INVALID;
+  memcpy(out, sink.buffer().data(), sink.buffer().size());
+  return GZ_OK;
+}
+
+GzStatus gz_debug_encode_record_batch_lz4_stored(int64_t length, const int64_t* nodes, int32_t n_nodes,
+                                                const uint8_t* const* bufs, const int64_t* buf_lens,
+                                                int32_t n_bufs, uint8_t* out, int64_t out_cap,
+                                                int64_t* out_len) {
+  std::vector<gz::FieldNodeMeta> nm;
+  for (int i = 0; i < n_nodes; i++) nm.push_back(gz::FieldNodeMeta{nodes[2 * i], nodes[2 * i + 1]});
+  std::vector<std::vector<uint8_t>> temps;
+  temps.reserve(n_bufs);
+  std::vector<std::vector<gz::Chunk>> pieces(n_bufs);
+  std::vector<int64_t> lens(n_bufs, 0);
+  for (int i = 0; i < n_bufs; i++) {
+    if (buf_lens[i] <= 0) continue;  // an empty buffer stays empty
+    std::vector<gz::Lz4BlockRef> blocks;
+    for (int64_t x = 0; x < buf_lens[i]; x += 65536)
+      blocks.push_back(gz::Lz4BlockRef{bufs[i] + x, (uint32_t)std::min<int64_t>(65536, buf_lens[i] - x), true});
+    lens[i] = gz::AppendLz4Buffer(buf_lens[i], blocks, &pieces[i], &temps);
+  }
+  std::vector<uint8_t> meta;
+  int64_t body = 0;
+  gz::CompressedRecordBatchHeader(length, nm, lens, &meta, &body);
+  gz::MemorySink sink;
+  sink.Write(meta.data(), (int64_t)meta.size());
+  static const uint8_t kZ[8] = {0};
+  for (int i = 0; i < n_bufs; i++) {
+    for (const gz::Chunk& c : pieces[i]) sink.Write(c.data, c.len);
+    sink.Write(kZ, ((lens[i] + 7) & ~int64_t(7)) - lens[i]);
+  }
   *out_len = (int64_t)sink.buffer().size();
   if (*out_len > out_cap) return GZ_INVALID;
   memcpy(out, sink.buffer().data(), sink.buffer().size());

@@ -15,6 +15,7 @@ namespace gz {
 struct Chunk {
   const uint8_t* data;  // nullptr with len > 0 means `len` zero bytes
   int64_t len;
+  bool dev = false;     // `data` is device memory (or pinned host memory the device reads)
 };
 using ChunkedBuffer = std::vector<Chunk>;
 
@@ -70,6 +71,32 @@ int64_t WriteRecordBatchMessage(ByteSink* sink, int64_t length,
 void RecordBatchHeader(int64_t length, const std::vector<FieldNodeMeta>& nodes,
                        const std::vector<int64_t>& lens, std::vector<uint8_t>* out,
                        int64_t* body_length);
+
+// The same for a message whose body buffers are compressed (RecordBatch.compression set to
+// LZ4_FRAME / BUFFER); `lens` are the compressed buffer lengths (uncompressed-length prefix
+// included).
+void CompressedRecordBatchHeader(int64_t length, const std::vector<FieldNodeMeta>& nodes,
+                                 const std::vector<int64_t>& lens, std::vector<uint8_t>* out,
+                                 int64_t* body_length);
+
+// LZ4 frame format: magic, FLG (version 1, independent blocks, no checksums, no content size),
+// BD (64 KiB blocks) and the header checksum byte of those two descriptor bytes.
+constexpr uint8_t kLz4Flg = 0x60, kLz4Bd = 0x40;
+uint8_t Lz4FrameHeaderChecksum(const uint8_t* desc, int n);
+
+// One block of an LZ4 frame: `size` payload bytes at `data`; `stored`: the payload is the data
+// itself (no LZ4 sequences).
+struct Lz4BlockRef {
+  const uint8_t* data;
+  uint32_t size;
+  bool stored;
+};
+
+// Appends the bytes of one compressed IPC body buffer to `pieces`: the int64 uncompressed length,
+// then one LZ4 frame (header, the blocks with their size words, end mark).  The small byte
+// strings around the payloads are kept in a new element of `temps`.  Returns the bytes appended.
+int64_t AppendLz4Buffer(int64_t uncompressed_len, const std::vector<Lz4BlockRef>& blocks,
+                        std::vector<Chunk>* pieces, std::vector<std::vector<uint8_t>>* temps);
 
 // Size of that message without writing it.
 int64_t RecordBatchMessageSize(int64_t n_nodes, const std::vector<int64_t>& buffer_lengths,

@@ -75,6 +75,10 @@ __global__ void __launch_bounds__(kThreads) k_read_bits(const BitJob* __restrict
   }
 }
 
+__global__ void __launch_bounds__(kThreads) k_read_words(const int32_t* const* __restrict__ src, int32_t* out, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * kThreads + threadIdx.x; i < n; i += (size_t)gridDim.x * kThreads) out[i] = *src[i];
+}
+
 unsigned grid_for(uint32_t n_jobs) {
   static int sms = 0;
   if (sms == 0) {
@@ -87,6 +91,24 @@ unsigned grid_for(uint32_t n_jobs) {
 }
 
 }  // namespace
+
+cudaError_t gather_words(const int32_t* const* src, int32_t* out, size_t n, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  uint8_t* d = nullptr;
+  const size_t pb = (n * sizeof(void*) + 255) / 256 * 256;
+  cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&d), pb + n * sizeof(int32_t), st);
+  if (e != cudaSuccess) return e;
+  e = cudaMemcpyAsync(d, src, n * sizeof(void*), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    const size_t blocks = (n + kThreads - 1) / kThreads;
+    k_read_words<<<blocks < 1024 ? (unsigned)blocks : 1024u, kThreads, 0, st>>>(
+        reinterpret_cast<const int32_t* const*>(d), reinterpret_cast<int32_t*>(d + pb), n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, d + pb, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+  cudaFreeAsync(d, st);
+  return e;
+}
 
 cudaError_t launch_read_jobs(const ByteJob* bytes, uint32_t n_bytes, const OffsetJob* offs, uint32_t n_offs,
                              const BitJob* bits, uint32_t n_bits, cudaStream_t st) {

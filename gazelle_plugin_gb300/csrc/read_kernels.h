@@ -26,6 +26,10 @@ struct BitJob {  // bits [src_bit, src_bit + nbits) of src (all ones when src is
   uint64_t nbits;
 };
 
+// out[i] = *src[i] for n device addresses (host arrays; waits for nothing but the copies it
+// enqueues: the caller synchronises `st` before reading out).
+cudaError_t gather_words(const int32_t* const* src, int32_t* out, size_t n, cudaStream_t st);
+
 // Runs the three job lists on `st` (the job arrays in device memory).
 cudaError_t launch_read_jobs(const ByteJob* bytes, uint32_t n_bytes, const OffsetJob* offs, uint32_t n_offs,
                              const BitJob* bits, uint32_t n_bits, cudaStream_t st);

@@ -6,6 +6,7 @@
 #include <algorithm>
 
 #include "flatbuf.h"
+#include "lz4_kernels.h"
 #include "read_kernels.h"
 
 namespace gz {
@@ -64,6 +65,8 @@ PartitionReader::~PartitionReader() {
   if (stream_) cudaStreamSynchronize(stream_);
   for (uint8_t* p : images_)
     if (p) cudaFreeAsync(p, stream_);
+  for (uint8_t* p : arena_mem_)
+    if (p) cudaFreeAsync(p, stream_);
   if (out_mem_) cudaFreeAsync(out_mem_, stream_);
   if (stream_) {
     cudaStreamSynchronize(stream_);
@@ -74,7 +77,8 @@ PartitionReader::~PartitionReader() {
 // Walks the messages of one stream: an optional schema message, record batches, then the
 // end-of-stream marker (or the end of the bytes).  Buffer ranges are recorded relative to the
 // stream start, where the device copy keeps them.
-Status PartitionReader::ParseStream(const uint8_t* data, int64_t len, int stream, std::vector<Batch>* out) {
+Status PartitionReader::ParseStream(const uint8_t* data, int64_t len, int stream, std::vector<Batch>* out,
+                                    std::vector<FrameRef>* frames, int64_t* arena_bytes) {
   int64_t pos = 0;
   while (pos < len) {
     if (len - pos < 4) return Status::Error(GZ_INVALID, "truncated IPC stream");
@@ -112,7 +116,11 @@ Status PartitionReader::ParseStream(const uint8_t* data, int64_t len, int stream
     } else if (header_type == kHeaderRecordBatch) {
       const int64_t rb = r.Table(msg, 2);
       if (rb < 0) return Status::Error(GZ_INVALID, "record batch without header");
-      if (r.Table(rb, 3) >= 0) return Status::Error(GZ_NOT_IMPLEMENTED, "compressed record batch bodies");
+      // BodyCompression {codec, method}: LZ4_FRAME (0) and BUFFER (0) are the defaults
+      const int64_t comp = r.Table(rb, 3);
+      const bool compressed = comp >= 0;
+      if (compressed && (r.Scalar<int8_t>(comp, 0, 0) != 0 || r.Scalar<int8_t>(comp, 1, 0) != 0))
+        return Status::Error(GZ_NOT_IMPLEMENTED, "body compression other than LZ4_FRAME per buffer");
       Batch b;
       b.stream = stream;
       b.rows = r.Scalar<int64_t>(rb, 0, 0);
@@ -129,6 +137,24 @@ Status PartitionReader::ParseStream(const uint8_t* data, int64_t len, int stream
         if (off < 0 || l < 0 || off + l > body_len || (off & 7)) return false;
         out_ref->offset = body_pos + off;
         out_ref->length = l;
+        out_ref->decoded = false;
+        if (compressed && l > 0) {
+          // an int64 uncompressed length, then one LZ4 frame (-1: the bytes follow as they are)
+          if (l < 8) return false;
+          int64_t ul;
+          memcpy(&ul, data + body_pos + off, 8);
+          if (ul == -1) {
+            out_ref->offset += 8;
+            out_ref->length = l - 8;
+          } else {
+            if (ul < 0) return false;
+            frames->push_back(FrameRef{body_pos + off + 8, l - 8, *arena_bytes, ul});
+            out_ref->offset = *arena_bytes;
+            out_ref->length = ul;
+            out_ref->decoded = true;
+            *arena_bytes += Pad8(ul);
+          }
+        }
         return true;
       };
       b.cols.resize(fields_.size());
@@ -154,10 +180,12 @@ Status PartitionReader::ParseStream(const uint8_t* data, int64_t len, int stream
         if (c.values.length < need) return Status::Error(GZ_INVALID, "value buffer too short");
         if (IsBinaryType(t)) {
           if (c.offsets.length < (b.rows + 1) * 4) return Status::Error(GZ_INVALID, "offsets buffer too short");
-          memcpy(&c.o0, data + c.offsets.offset, 4);
-          memcpy(&c.o1, data + c.offsets.offset + 4 * b.rows, 4);
-          if (c.o0 < 0 || c.o1 < c.o0 || c.o1 > c.values.length)
-            return Status::Error(GZ_INVALID, "offsets exceed the characters");
+          if (!c.offsets.decoded) {  // decoded offsets are read after decoding
+            memcpy(&c.o0, data + c.offsets.offset, 4);
+            memcpy(&c.o1, data + c.offsets.offset + 4 * b.rows, 4);
+            if (c.o0 < 0 || c.o1 < c.o0 || c.o1 > c.values.length)
+              return Status::Error(GZ_INVALID, "offsets exceed the characters");
+          }
         }
       }
       if (b.rows > 0) out->push_back(std::move(b));
@@ -173,22 +201,73 @@ Status PartitionReader::AddStream(const uint8_t* data, int64_t len) {
   if (finished_) return Status::Error(GZ_INVALID, "reader already finished");
   if (len < 0 || (len > 0 && data == nullptr)) return Status::Error(GZ_INVALID, "null stream");
   std::vector<Batch> bs;
+  std::vector<FrameRef> frames;
+  int64_t arena_bytes = 0;
   const int idx = (int)images_.size();
-  Status st = ParseStream(data, len, idx, &bs);
+  Status st = ParseStream(data, len, idx, &bs, &frames, &arena_bytes);
   if (!st.ok()) return st;
   st = Cuda(cudaSetDevice(device_), "cudaSetDevice");
   if (!st.ok()) return st;
   uint8_t* d = nullptr;
+  uint8_t* arena = nullptr;
   if (!bs.empty()) {
     st = Cuda(cudaMallocAsync(reinterpret_cast<void**>(&d), AlignUp((size_t)len, 256), stream_), "cudaMallocAsync(stream)");
     if (!st.ok()) return st;
     // the caller's bytes are read before the call returns
     st = Cuda(cudaMemcpyAsync(d, data, (size_t)len, cudaMemcpyHostToDevice, stream_), "H2D stream");
     if (!st.ok()) return st;
+  }
+  images_.push_back(d);
+  arenas_.push_back(nullptr);
+  if (!frames.empty()) {
+    // compressed buffers: every LZ4 frame decoded by the device into the stream's arena
+    std::vector<Lz4Frame> jobs;
+    for (const FrameRef& f : frames)
+      jobs.push_back(Lz4Frame{nullptr, (uint64_t)f.src_len, nullptr, (uint64_t)f.dst_len});
+    const size_t jb = AlignUp(sizeof(Lz4Frame) * jobs.size(), 256);
+    st = Cuda(cudaMallocAsync(reinterpret_cast<void**>(&arena), jb + 256 + AlignUp((size_t)arena_bytes, 256), stream_),
+              "cudaMallocAsync(decode)");
+    if (!st.ok()) return st;
+    arenas_.back() = arena + jb + 256;
+    for (size_t i = 0; i < jobs.size(); i++) {
+      jobs[i].src = d + frames[i].src;
+      jobs[i].dst = arenas_.back() + frames[i].dst;
+    }
+    int32_t* d_err = reinterpret_cast<int32_t*>(arena + jb);
+    int32_t err = 0;
+    st = Cuda(cudaMemcpyAsync(arena, jobs.data(), sizeof(Lz4Frame) * jobs.size(), cudaMemcpyHostToDevice, stream_), "H2D");
+    if (st.ok()) st = Cuda(cudaMemsetAsync(d_err, 0, 4, stream_), "memset");
+    if (st.ok()) st = Cuda(launch_lz4_decode(reinterpret_cast<const Lz4Frame*>(arena), (uint32_t)jobs.size(), d_err, stream_),
+                           "k_lz4_decode");
+    if (st.ok()) st = Cuda(cudaMemcpyAsync(&err, d_err, 4, cudaMemcpyDeviceToHost, stream_), "D2H");
+    // the decoded offsets bound each batch's characters
+    std::vector<const int32_t*> where;
+    std::vector<std::pair<size_t, size_t>> which;  // (batch, field)
+    for (size_t bi = 0; bi < bs.size(); bi++)
+      for (size_t f = 0; f < fields_.size(); f++) {
+        const ColRef& c = bs[bi].cols[f];
+        if (!IsBinaryType(fields_[f].type) || !c.offsets.decoded) continue;
+        const int32_t* o = reinterpret_cast<const int32_t*>(arenas_.back() + c.offsets.offset);
+        where.push_back(o);
+        where.push_back(o + bs[bi].rows);
+        which.push_back({bi, f});
+      }
+    std::vector<int32_t> ends(where.size());
+    if (st.ok() && !where.empty()) st = Cuda(gather_words(where.data(), ends.data(), where.size(), stream_), "offsets");
+    if (st.ok()) st = Cuda(cudaStreamSynchronize(stream_), "k_lz4_decode");
+    if (!st.ok()) return st;
+    if (err) return Status::Error(GZ_INVALID, "a compressed buffer is not a valid LZ4 frame of its stated length");
+    for (size_t i = 0; i < which.size(); i++) {
+      ColRef& c = bs[which[i].first].cols[which[i].second];
+      c.o0 = ends[2 * i];
+      c.o1 = ends[2 * i + 1];
+      if (c.o0 < 0 || c.o1 < c.o0 || c.o1 > c.values.length) return Status::Error(GZ_INVALID, "offsets exceed the characters");
+    }
+    arena_mem_.push_back(arena);
+  } else {
     st = Cuda(cudaStreamSynchronize(stream_), "H2D stream");
     if (!st.ok()) return st;
   }
-  images_.push_back(d);
   for (Batch& b : bs) batches_.push_back(std::move(b));
   return Status::OK();
 }
@@ -255,32 +334,31 @@ Status PartitionReader::Finish(int64_t* rows, int32_t* n_batches) {
   int64_t row = 0;
   for (size_t bi = 0; bi < batches_.size(); bi++) {
     const Batch& b = batches_[bi];
-    const uint8_t* img = images_[b.stream];
     const bool last = bi + 1 == batches_.size();
     for (size_t f = 0; f < F; f++) {
       const int t = fields_[f].type;
       if (t == GZ_TYPE_NULL) continue;
       const ColRef& c = b.cols[f];
       if (o_valid[f] != SIZE_MAX)
-        add_bits(c.validity.length ? img + c.validity.offset : nullptr,
+        add_bits(c.validity.length ? Base(c.validity, b.stream) : nullptr,
                  reinterpret_cast<uint32_t*>(out_mem_ + o_valid[f]), (uint64_t)row, (uint64_t)b.rows);
       if (t == GZ_TYPE_BOOL) {
-        add_bits(img + c.values.offset, reinterpret_cast<uint32_t*>(out_mem_ + o_val[f]), (uint64_t)row,
+        add_bits(Base(c.values, b.stream), reinterpret_cast<uint32_t*>(out_mem_ + o_val[f]), (uint64_t)row,
                  (uint64_t)b.rows);
       } else if (IsBinaryType(t)) {
         // offsets rebased onto the characters of the earlier batches; the last batch also writes
         // the final offset
-        const int32_t* src_off = reinterpret_cast<const int32_t*>(img + c.offsets.offset);
+        const int32_t* src_off = reinterpret_cast<const int32_t*>(Base(c.offsets, b.stream));
         int32_t* dst_off = reinterpret_cast<int32_t*>(out_mem_ + o_off[f]) + row;
         const int32_t add = (int32_t)(char_pos[f] - c.o0);
         const uint64_t n = (uint64_t)b.rows + (last ? 1 : 0);
         for (uint64_t x = 0; x < n; x += kChunk / 4)
           oj.push_back(OffsetJob{src_off + x, dst_off + x, (uint32_t)std::min<uint64_t>(kChunk / 4, n - x), add});
-        add_bytes(img + c.values.offset + c.o0, out_mem_ + o_val[f] + char_pos[f], (uint64_t)(c.o1 - c.o0));
+        add_bytes(Base(c.values, b.stream) + c.o0, out_mem_ + o_val[f] + char_pos[f], (uint64_t)(c.o1 - c.o0));
         char_pos[f] += c.o1 - c.o0;
       } else {
         const int w = FixedWidth(t);
-        add_bytes(img + c.values.offset, out_mem_ + o_val[f] + (size_t)row * w, (uint64_t)b.rows * w);
+        add_bytes(Base(c.values, b.stream), out_mem_ + o_val[f] + (size_t)row * w, (uint64_t)b.rows * w);
       }
     }
     row += b.rows;
@@ -302,8 +380,12 @@ Status PartitionReader::Finish(int64_t* rows, int32_t* n_batches) {
               "reader kernels");
   cudaFreeAsync(dj, stream_);
   if (!st.ok()) return st;
-  // the stream images are no longer needed
+  // the stream images and decoded buffers are no longer needed
   for (uint8_t*& p : images_) {
+    if (p) cudaFreeAsync(p, stream_);
+    p = nullptr;
+  }
+  for (uint8_t*& p : arena_mem_) {
     if (p) cudaFreeAsync(p, stream_);
     p = nullptr;
   }

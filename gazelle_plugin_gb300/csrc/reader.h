@@ -38,8 +38,12 @@ class PartitionReader {
 
  private:
   struct BufRef {
-    int64_t offset = 0;  // inside the stream's device copy
+    int64_t offset = 0;    // inside the stream's device copy, or its decode arena
     int64_t length = 0;
+    bool decoded = false;  // a compressed buffer, decoded into the arena
+  };
+  struct FrameRef {  // one compressed buffer: its LZ4 frame in the stream, its arena range
+    int64_t src = 0, src_len = 0, dst = 0, dst_len = 0;
   };
   struct ColRef {
     int64_t null_count = 0;
@@ -61,12 +65,18 @@ class PartitionReader {
 
   PartitionReader() = default;
   Status Cuda(cudaError_t e, const char* what);
-  Status ParseStream(const uint8_t* data, int64_t len, int stream, std::vector<Batch>* out);
+  Status ParseStream(const uint8_t* data, int64_t len, int stream, std::vector<Batch>* out,
+                     std::vector<FrameRef>* frames, int64_t* arena_bytes);
+  const uint8_t* Base(const BufRef& r, int stream) const {
+    return (r.decoded ? arenas_[stream] : images_[stream]) + r.offset;
+  }
 
   std::vector<Field> fields_;
   int device_ = 0;
   cudaStream_t stream_ = nullptr;
   std::vector<uint8_t*> images_;  // device copy of every stream
+  std::vector<uint8_t*> arenas_;  // decoded compressed buffers of every stream
+  std::vector<uint8_t*> arena_mem_;  // their allocations
   std::vector<Batch> batches_;
   std::vector<OutCol> out_;
   uint8_t* out_mem_ = nullptr;

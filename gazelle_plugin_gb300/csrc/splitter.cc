@@ -4,6 +4,7 @@
 #include <errno.h>
 #include <fcntl.h>
 #include <string.h>
+#include <sys/mman.h>
 #include <sys/stat.h>
 #include <sys/uio.h>
 #include <unistd.h>
@@ -13,6 +14,7 @@
 #include <numeric>
 
 #include "gz_kernels.h"
+#include "lz4_kernels.h"
 #include "host_util.h"
 #include "tune.h"
 
@@ -21,6 +23,7 @@ namespace gz {
 namespace {
 
 inline int64_t BytesForBits(int64_t n) { return (n + 7) >> 3; }
+constexpr int64_t kMapWriteBytes = 256ll << 20;  // data files from this size are written through a mapping
 inline size_t AlignUp(size_t x, size_t a) { return (x + a - 1) / a * a; }
 inline int64_t NowNs() {
   return std::chrono::duration_cast<std::chrono::nanoseconds>(
@@ -105,8 +108,9 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
   opts_ = opts;
   if (opts_.buffer_size <= 0) opts_.buffer_size = 4096;
   if (opts_.buffer_size > 32 * 1024) return Status::Error(GZ_INVALID, "buffer_size must be <= 32768");
-  if (opts_.compression != 0)
-    return Status::Error(GZ_NOT_IMPLEMENTED, "only uncompressed shuffle output is implemented");
+  if (opts_.compression == GZ_CODEC_LZ4_FRAME) codec_ = GZ_CODEC_LZ4_FRAME;
+  else if (opts_.compression != GZ_CODEC_UNCOMPRESSED)
+    return Status::Error(GZ_NOT_IMPLEMENTED, "codec " + std::to_string(opts_.compression) + " is not implemented");
   data_file_ = opts.data_file ? opts.data_file : "";
   opts_.data_file = nullptr;
   opts_.local_dirs = nullptr;
@@ -122,6 +126,11 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
       if (opts_.seg_tiles <= 0) opts_.seg_tiles = tc.seg_tiles;
     }
   }
+  // partition data of host inputs goes back to the host as passes finish (overlapping the
+  // split); of device-resident inputs it stays in HBM until Stop
+  // (with a codec it stays: the device compresses it at Stop)
+  if (opts_.keep_output_on_device < 0)
+    opts_.keep_output_on_device = opts_.input_kind == GZ_INPUT_HOST && codec_ == GZ_CODEC_UNCOMPRESSED ? 0 : 1;
   if (opts_.flush_bytes <= 0) opts_.flush_bytes = 512ll << 20;
   if (opts_.flush_bytes > (1ll << 30)) opts_.flush_bytes = 1ll << 30;
   if (opts_.seg_tiles > kMaxSegTiles) opts_.seg_tiles = kMaxSegTiles;
@@ -788,6 +797,8 @@ Status Splitter::Flush() {
     }
   }
   const size_t bits_end = o;
+  fr.bits_begin = bits_begin;
+  fr.bits_end = bits_end;
   fr.out_bytes = std::max<size_t>(o, 256);
   Status st = Cuda(cudaMallocAsync(reinterpret_cast<void**>(&fr.d_out), fr.out_bytes, stream_),
                    "cudaMallocAsync(flush output)");
@@ -1168,10 +1179,18 @@ Status Splitter::ProcessFlushes() {
 // flush outputs (CacheRecordBatch): its IPC metadata and the byte ranges of its body, padding
 // included, ready to be written (WriteIpcPayload).  Reads only, so partitions can be built in
 // parallel.
-Status Splitter::BuildSegment(int p, const Segment& s, SegMsg* msg) const {
+Status Splitter::BuildSegment(int p, const Segment& s, SegMsg* msg, bool device_view) const {
   const int P = P_;
   const int nstr = n_str_;
   const uint32_t n = s.rows;
+  // where a pass's body bytes and bit regions are read from
+  auto body_base = [&](const FlushRec& f, bool* dev) -> const uint8_t* {
+    *dev = device_view;
+    return device_view && !f.on_host ? f.d_out : f.h_out;
+  };
+  auto bit_base = [&](const FlushRec& f, size_t off) -> const uint8_t* {
+    return f.on_host ? f.h_out + off : f.h_bits + (off - f.bits_begin);
+  };
   std::vector<FieldNodeMeta> nodes;
   std::vector<ChunkedBuffer> bufs;
   std::vector<std::vector<uint8_t>>& temps = msg->temps;
@@ -1193,7 +1212,7 @@ Status Splitter::BuildSegment(int p, const Segment& s, SegMsg* msg) const {
       }
       *all_ones = false;
       const uint64_t bit0 = (uint64_t)f.vstart(P)[p] + pc.vpos0;  // multiple of 64
-      return f.h_out + off + bit0 / 8;
+      return bit_base(f, off) + bit0 / 8;
     }
     temps.emplace_back(nb, 0xff);
     uint8_t* dst = temps.back().data();
@@ -1205,7 +1224,7 @@ Status Splitter::BuildSegment(int p, const Segment& s, SegMsg* msg) const {
       const uint32_t len = pc.frow1 - pc.frow0;
       if (off != SIZE_MAX) {
         const uint64_t bit0 = (uint64_t)f.vstart(P)[p] + pc.vpos0;
-        CopyBits(f.h_out + off, bit0, dst, drow, len);
+        CopyBits(bit_base(f, off), bit0, dst, drow, len);
         any = true;
       }
       drow += len;
@@ -1246,9 +1265,10 @@ Status Splitter::BuildSegment(int p, const Segment& s, SegMsg* msg) const {
       ChunkedBuffer vals;
       for (const Piece& pc : s.pieces) {
         const FlushRec& f = flushes_[pc.flush];
-        const uint8_t* base = f.h_out + f.off_values[a];
+        bool dev;
+        const uint8_t* base = body_base(f, &dev) + f.off_values[a];
         vals.push_back(Chunk{base + ((size_t)f.pstart(P)[p] + pc.frow0) * w,
-                             (int64_t)(pc.frow1 - pc.frow0) * w});
+                             (int64_t)(pc.frow1 - pc.frow0) * w, dev});
       }
       rawb += (int64_t)n * w;
       bufs.push_back(vals);
@@ -1268,11 +1288,14 @@ Status Splitter::BuildSegment(int p, const Segment& s, SegMsg* msg) const {
       int64_t clen = 0;
       for (const Piece& pc : s.pieces) {
         const FlushRec& f = flushes_[pc.flush];
-        const uint8_t* ob = f.h_out + f.off_values[a];
-        offs.push_back(Chunk{ob + ((size_t)f.pstart(P)[p] + pc.frow0) * 4, (int64_t)(pc.frow1 - pc.frow0) * 4});
-        const uint8_t* cb = f.h_out + f.off_chars[a];
+        bool dev;
+        const uint8_t* fb = body_base(f, &dev);
+        const uint8_t* ob = fb + f.off_values[a];
+        offs.push_back(Chunk{ob + ((size_t)f.pstart(P)[p] + pc.frow0) * 4, (int64_t)(pc.frow1 - pc.frow0) * 4, dev});
+        const uint8_t* cb = fb + f.off_chars[a];
         const uint32_t c0 = pc.fb0[k], c1 = pc.fb1[k];
-        if (c1 > c0) chars.push_back(Chunk{cb + (size_t)f.cstart(P, nstr)[(size_t)k * P + p] + c0, (int64_t)(c1 - c0)});
+        if (c1 > c0)
+          chars.push_back(Chunk{cb + (size_t)f.cstart(P, nstr)[(size_t)k * P + p] + c0, (int64_t)(c1 - c0), dev});
         clen += c1 - c0;
       }
       rawb += (int64_t)(n + 1) * 4 + clen;
@@ -1281,6 +1304,12 @@ Status Splitter::BuildSegment(int p, const Segment& s, SegMsg* msg) const {
     }
   }
   msg->raw = rawb;
+  msg->rows = n;
+  if (device_view) {  // the body is encoded after the device has compressed / copied it
+    msg->nodes = std::move(nodes);
+    msg->bufs = std::move(bufs);
+    return Status::OK();
+  }
   std::vector<int64_t> lens(bufs.size(), 0);
   for (size_t i = 0; i < bufs.size(); i++)
     for (const Chunk& c : bufs[i]) lens[i] += c.len;
@@ -1380,9 +1409,19 @@ Status Splitter::Stop() {
     }
     open = Segment();
   }
+  const bool compressed = codec_ != GZ_CODEC_UNCOMPRESSED;
   const int64_t m0 = NowNs();
   for (auto& f : flushes_) {
-    st = MoveFlushToHost(f);
+    if (!compressed) {
+      st = MoveFlushToHost(f);
+    } else if (!f.on_host && f.bits_end > f.bits_begin) {
+      // the device compresses the bodies where they are; only the bit regions (null counts,
+      // bitmaps assembled on the host) come over now
+      f.h_bits = HostAlloc(f.bits_end - f.bits_begin);
+      if (!f.h_bits) return Status::Error(GZ_OOM, "pinned host memory for validity bits");
+      st = Cuda(cudaMemcpyAsync(f.h_bits, f.d_out + f.bits_begin, f.bits_end - f.bits_begin,
+                                cudaMemcpyDeviceToHost, ostream_), "D2H bits");
+    }
     if (!st.ok()) return st;
   }
   st = Cuda(cudaStreamSynchronize(ostream_), "D2H partition data");
@@ -1402,27 +1441,33 @@ Status Splitter::Stop() {
   ParallelFor((size_t)P_, [&](size_t pi) {
     const int p = (int)pi;
     const auto& segs = segments_[p];
-    if (segs.empty()) {
-      partition_lengths_[p] = 0;
-      return;
-    }
     msgs[p].resize(segs.size());
-    int64_t len = (int64_t)schema_msg.size() + 8;  // + EOS
-    int64_t raw = 0;
     for (size_t i = 0; i < segs.size(); i++) {
-      Status b = BuildSegment(p, segs[i], &msgs[p][i]);
+      Status b = BuildSegment(p, segs[i], &msgs[p][i], compressed);
       if (!b.ok()) {
         pst[p] = b;
         return;
       }
-      len += msgs[p][i].bytes;
-      raw += msgs[p][i].raw;
     }
-    partition_lengths_[p] = len;
-    raw_partition_lengths_[p] += raw;
   });
   for (int p = 0; p < P_; p++)
     if (!pst[p].ok()) return pst[p];
+  if (compressed) {
+    st = CompressBodies(&msgs);
+    if (!st.ok()) return st;
+  }
+  for (int p = 0; p < P_; p++) {
+    if (msgs[p].empty()) {
+      partition_lengths_[p] = 0;
+      continue;
+    }
+    int64_t len = (int64_t)schema_msg.size() + 8;  // + EOS
+    for (const SegMsg& m : msgs[p]) {
+      len += m.bytes;
+      raw_partition_lengths_[p] += m.raw;
+    }
+    partition_lengths_[p] = len;
+  }
   std::vector<int64_t> start(P_ + 1, 0);
   for (int p = 0; p < P_; p++) {
     start[p + 1] = start[p] + partition_lengths_[p];
@@ -1438,11 +1483,12 @@ Status Splitter::Stop() {
   const int64_t t0 = NowNs();
   int fd = -1;
   uint8_t* mem = nullptr;
+  void* mapped = nullptr;
   if (data_file_.empty()) {
     data_bytes_.assign((size_t)total, 0);
     mem = data_bytes_.data();
   } else {
-    fd = open(data_file_.c_str(), O_WRONLY | O_CREAT | O_TRUNC, 0644);
+    fd = open(data_file_.c_str(), O_RDWR | O_CREAT | O_TRUNC, 0644);
     if (fd < 0) return Status::Error(GZ_IO, "cannot open data file " + data_file_ + ": " + strerror(errno));
     struct stat sb;
     const bool regular = fstat(fd, &sb) == 0 && S_ISREG(sb.st_mode);  // not e.g. /dev/null
@@ -1450,6 +1496,13 @@ Status Splitter::Stop() {
       const std::string why = strerror(errno);
       close(fd);
       return Status::Error(GZ_IO, "cannot size data file " + data_file_ + ": " + why);
+    }
+    // Writes to one file serialise on the file's lock; a large file is mapped instead, so that
+    // the partitions are copied into it in parallel.
+    if (regular && total >= kMapWriteBytes) {
+      mapped = mmap(nullptr, (size_t)total, PROT_READ | PROT_WRITE, MAP_SHARED, fd, 0);
+      if (mapped == MAP_FAILED) mapped = nullptr;
+      else mem = static_cast<uint8_t*>(mapped);
     }
   }
   static const uint32_t kEos[2] = {0xFFFFFFFFu, 0u};  // WriteEOS (splitter.cc:166-172)
@@ -1468,6 +1521,7 @@ Status Splitter::Stop() {
   });
   bool ok = true;
   for (int p = 0; p < P_; p++) ok = ok && wrote[p];
+  if (mapped && munmap(mapped, (size_t)total) != 0) ok = false;
   if (fd >= 0 && close(fd) != 0) ok = false;
   if (!ok) return Status::Error(GZ_IO, "writing the data file failed: " + data_file_);
   total_bytes_written_ += total;
@@ -1478,6 +1532,129 @@ Status Splitter::Stop() {
   // the pinned copies are no longer needed
   ReleaseHost();
   ReleaseStaging();
+  return Status::OK();
+}
+
+Status Splitter::CompressBodies(std::vector<std::vector<SegMsg>>* msgs_p) {
+  auto& msgs = *msgs_p;
+  const int64_t threshold = opts_.batch_compress_threshold;
+  auto lz4 = [&](const SegMsg& m) { return codec_ == GZ_CODEC_LZ4_FRAME && (int64_t)m.rows > threshold; };
+  // 1. the device work: every device-readable body range, cut into chunks (LZ4 blocks of at
+  //    most 64 KiB for compressed batches, plain copies of at most 1 MiB for the others)
+  constexpr uint32_t kCopyChunk = 1u << 20;
+  std::vector<Lz4Chunk> chunks;
+  std::vector<std::vector<uint32_t>> first(P_);  // first chunk of each message
+  uint64_t arena_bytes = 0;
+  for (int p = 0; p < P_; p++) {
+    first[p].resize(msgs[p].size());
+    for (size_t i = 0; i < msgs[p].size(); i++) {
+      const SegMsg& m = msgs[p][i];
+      first[p][i] = (uint32_t)chunks.size();
+      const uint32_t step = lz4(m) ? kLz4MaxBlock : kCopyChunk;
+      for (const ChunkedBuffer& b : m.bufs)
+        for (const Chunk& c : b) {
+          if (!c.dev) continue;
+          for (int64_t x = 0; x < c.len; x += step) {
+            const uint32_t len = (uint32_t)std::min<int64_t>(step, c.len - x);
+            chunks.push_back(Lz4Chunk{c.data + x, len, lz4(m) ? 0u : 1u});
+            arena_bytes += AlignUp(len, 16);
+          }
+        }
+    }
+  }
+  std::vector<Lz4Block> res(chunks.size());
+  uint8_t* arena = nullptr;
+  if (!chunks.empty()) {
+    const size_t n = chunks.size();
+    const size_t scratch = (size_t)lz4_compress_warps() * kLz4Slot;
+    const size_t tab = AlignUp(sizeof(Lz4Chunk) * n, 256), rb = AlignUp(sizeof(Lz4Block) * n, 256);
+    uint8_t* d = nullptr;
+    Status st = Cuda(cudaMallocAsync(reinterpret_cast<void**>(&d), tab + rb + 256 + scratch + arena_bytes, stream_),
+                     "cudaMallocAsync(compression)");
+    if (!st.ok()) return st;
+    Lz4Chunk* d_chunks = reinterpret_cast<Lz4Chunk*>(d);
+    Lz4Block* d_res = reinterpret_cast<Lz4Block*>(d + tab);
+    unsigned long long* d_used = reinterpret_cast<unsigned long long*>(d + tab + rb);
+    uint32_t* d_next = reinterpret_cast<uint32_t*>(d + tab + rb + 8);
+    int32_t* d_err = reinterpret_cast<int32_t*>(d + tab + rb + 16);
+    uint8_t* d_scratch = d + tab + rb + 256;
+    uint8_t* d_arena = d_scratch + scratch;
+    unsigned long long used = 0;
+    int32_t err = 0;
+    st = Cuda(cudaMemcpyAsync(d_chunks, chunks.data(), sizeof(Lz4Chunk) * n, cudaMemcpyHostToDevice, stream_), "H2D chunks");
+    if (st.ok()) st = Cuda(cudaMemsetAsync(d + tab + rb, 0, 256, stream_), "memset");
+    const int64_t c0 = NowNs();
+    if (st.ok())
+      st = Cuda(launch_lz4_compress(d_chunks, (uint32_t)n, d_next, d_scratch, d_arena, d_used, arena_bytes, d_res,
+                                    d_err, stream_), "k_lz4_compress");
+    if (st.ok()) st = Cuda(cudaMemcpyAsync(res.data(), d_res, sizeof(Lz4Block) * n, cudaMemcpyDeviceToHost, stream_), "D2H");
+    if (st.ok()) st = Cuda(cudaMemcpyAsync(&used, d_used, 8, cudaMemcpyDeviceToHost, stream_), "D2H");
+    if (st.ok()) st = Cuda(cudaMemcpyAsync(&err, d_err, 4, cudaMemcpyDeviceToHost, stream_), "D2H");
+    if (st.ok()) st = Cuda(cudaStreamSynchronize(stream_), "k_lz4_compress");
+    total_compress_time_ += NowNs() - c0;
+    if (st.ok() && (err || used > arena_bytes)) st = Status::Error(GZ_CUDA, "compression arena overflow");
+    if (st.ok() && used > 0) {  // only the bytes the blocks took come to the host
+      arena = HostAlloc(used);
+      if (!arena) st = Status::Error(GZ_OOM, "pinned host memory for compressed bodies");
+      if (st.ok()) st = Cuda(cudaMemcpyAsync(arena, d_arena, used, cudaMemcpyDeviceToHost, stream_), "D2H bodies");
+      if (st.ok()) st = Cuda(cudaStreamSynchronize(stream_), "D2H bodies");
+    }
+    cudaFreeAsync(d, stream_);
+    if (!st.ok()) return st;
+  }
+  // 2. the messages: compressed buffers as uncompressed length + LZ4 frame of the chunks' blocks
+  //    (host-side ranges, e.g. assembled bitmaps, as stored blocks); the rest as plain bytes
+  static const uint8_t kZero8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  ParallelFor((size_t)P_, [&](size_t pi) {
+    const int p = (int)pi;
+    for (size_t i = 0; i < msgs[p].size(); i++) {
+      SegMsg& m = msgs[p][i];
+      const bool z = lz4(m);
+      uint32_t k = first[p][i];
+      std::vector<int64_t> lens(m.bufs.size(), 0);
+      std::vector<Chunk> body;
+      for (size_t b = 0; b < m.bufs.size(); b++) {
+        int64_t raw_len = 0;
+        for (const Chunk& c : m.bufs[b]) raw_len += c.len;
+        if (raw_len == 0) continue;  // an empty buffer stays empty
+        const size_t at = body.size();
+        if (z) {
+          std::vector<Lz4BlockRef> blocks;
+          for (const Chunk& c : m.bufs[b]) {
+            for (int64_t x = 0; x < c.len; x += kLz4MaxBlock) {
+              const uint32_t len = (uint32_t)std::min<int64_t>(kLz4MaxBlock, c.len - x);
+              if (c.dev) {
+                const Lz4Block& r = res[k++];
+                blocks.push_back(Lz4BlockRef{arena + r.pos, r.size, r.stored != 0});
+              } else {
+                blocks.push_back(Lz4BlockRef{c.data + x, len, true});
+              }
+            }
+          }
+          lens[b] = AppendLz4Buffer(raw_len, blocks, &body, &m.temps);
+        } else {
+          for (const Chunk& c : m.bufs[b]) {
+            if (!c.dev) {
+              body.push_back(c);
+              continue;
+            }
+            for (int64_t x = 0; x < c.len; x += kCopyChunk) {
+              const Lz4Block& r = res[k++];
+              body.push_back(Chunk{arena + r.pos, (int64_t)r.size});
+            }
+          }
+          lens[b] = raw_len;
+        }
+        (void)at;
+        const int64_t pad = ((lens[b] + 7) & ~int64_t(7)) - lens[b];
+        if (pad) body.push_back(Chunk{kZero8, pad});
+      }
+      if (z) CompressedRecordBatchHeader(m.rows, m.nodes, lens, &m.header, &m.body);
+      else RecordBatchHeader(m.rows, m.nodes, lens, &m.header, &m.body);
+      m.pieces = std::move(body);
+      m.bytes = (int64_t)m.header.size() + m.body;
+    }
+  });
   return Status::OK();
 }
 
@@ -1567,7 +1744,9 @@ Status Splitter::SpillFixedSize(int64_t size, int64_t* actual) {
 }
 
 Status Splitter::SetCompressType(int32_t codec) {
-  if (codec != 0) return Status::Error(GZ_NOT_IMPLEMENTED, "only uncompressed shuffle output is implemented");
+  if (codec != GZ_CODEC_UNCOMPRESSED && codec != GZ_CODEC_LZ4_FRAME)
+    return Status::Error(GZ_NOT_IMPLEMENTED, "codec " + std::to_string(codec) + " is not implemented");
+  codec_ = codec;
   return Status::OK();
 }
 

@@ -99,6 +99,8 @@ class Splitter {
     bool on_host = false;
     std::vector<size_t> off_values, off_bits, off_valid, off_chars;  // per array column, SIZE_MAX: none
     uint32_t* h_meta = nullptr;         // pinned: rows_f, pstart, vstart, bytes_f, cstart, count, emit
+    size_t bits_begin = 0, bits_end = 0;  // the bit regions (validity, bool values) in the output
+    uint8_t* h_bits = nullptr;          // pinned copy of just the bit regions (compressed Stop)
     size_t meta_words = 0;
     uint32_t emit_cap = 0;
     // [0] k_hash_count start, [1] its end, [4] k_scatter start, [3] its end (stream_); [5] plan
@@ -160,8 +162,18 @@ class Splitter {
     int64_t bytes = 0;  // header + body
     int64_t body = 0;
     int64_t raw = 0;    // its raw buffer bytes (batch_nbytes)
+    uint32_t rows = 0;
+    std::vector<FieldNodeMeta> nodes;
+    std::vector<ChunkedBuffer> bufs;  // device view: the body buffers before compression
   };
-  Status BuildSegment(int p, const Segment& s, SegMsg* msg) const;
+  // `device_view`: body ranges point at the pass outputs where they are (HBM, or pinned host
+  // memory the device reads; Chunk::dev set) for the device to compress or copy, bit regions at
+  // their host copies (h_bits); otherwise everything points at the host copies (h_out).
+  Status BuildSegment(int p, const Segment& s, SegMsg* msg, bool device_view = false) const;
+  // Compressed Stop: body ranges of every record batch through the device (LZ4 blocks for
+  // batches above batch_compress_threshold rows, plain copies for the others) into one arena,
+  // which is then copied to pinned host memory; fills every message's header and pieces.
+  Status CompressBodies(std::vector<std::vector<SegMsg>>* msgs);
   uint32_t SplitBatchSize(int32_t num_rows, const std::vector<const int32_t*>& host_offsets,
                           bool* complete);
 
@@ -174,6 +186,8 @@ class Splitter {
   int32_t pid_field_ = -1;  // range: the partition id field (0), not an output column
   uint32_t rr_sel_ = 0;     // round-robin selection at the next pass's first row
   uint32_t spin_limit_ = 0; // k_scatter wait limit (0: the kernel's default)
+  int32_t codec_ = 0;       // GzCodec of the emitted record batches
+  std::vector<PinnedBlock> arena_blocks_;  // pinned host copies of compressed bodies (Stop)
   // input field index minus this = output schema index
   int32_t out_shift() const { return pid_field_ >= 0 ? 1 : 0; }
   GzSplitOptions opts_{};

@@ -299,6 +299,17 @@ def default_options() -> GzSplitOptions:
     return o
 
 
+GZ_CODEC_UNCOMPRESSED, GZ_CODEC_LZ4_FRAME, GZ_CODEC_FASTPFOR = 0, 1, 2
+
+
+def codec_code(codec: Optional[str]) -> int:
+    """GzCodec of the JNI's codec string (GetCompressionType): "lz4" is LZ4_FRAME."""
+    if codec in (None, "", "uncompressed", "none"):
+        return GZ_CODEC_UNCOMPRESSED
+    return {"lz4": GZ_CODEC_LZ4_FRAME, "lz4_frame": GZ_CODEC_LZ4_FRAME,
+            "fastpfor": GZ_CODEC_FASTPFOR}.get(codec.lower(), 99)
+
+
 def split_options(offheapPerTask: int = 0, bufferSize: int = 4096, codec: Optional[str] = None,
                   batchCompressThreshold: int = 256, dataFile: str = "", subDirsPerLocalDir: int = 64,
                   localDirs: str = "", preferSpill: bool = True, writeSchema: bool = False,
@@ -312,7 +323,7 @@ def split_options(offheapPerTask: int = 0, bufferSize: int = 4096, codec: Option
     if subDirsPerLocalDir > 0:
         o.num_sub_dirs = subDirsPerLocalDir
     o.batch_compress_threshold = batchCompressThreshold
-    o.compression = 0 if codec in (None, "", "uncompressed", "none") else 1
+    o.compression = codec_code(codec)
     o.prefer_spill = int(preferSpill)
     o.write_schema = int(writeSchema)
     o.buffered_write = 1
@@ -411,8 +422,7 @@ class ShuffleSplitterJniWrapper:
         return out.value
 
     def setCompressType(self, splitterId: int, compressType: str) -> None:
-        codec = 0 if compressType in (None, "", "uncompressed", "none") else 1
-        _check(lib().gz_split_set_compress(splitterId, codec), splitterId)
+        _check(lib().gz_split_set_compress(splitterId, codec_code(compressType)), splitterId)
 
     def stop(self, splitterId: int, numPartitions: Optional[int] = None) -> SplitResult:
         P = numPartitions or self._partitions[splitterId]

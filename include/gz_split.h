@@ -53,6 +53,15 @@ typedef struct GzField {
   const char* name;
 } GzField;
 
+/* Codec of the emitted record batches (the JNI's codec strings "uncompressed", "lz4",
+ * "fastpfor"; GetCompressionType in jni_wrapper.cc).  Batches of at most
+ * batch_compress_threshold rows are written uncompressed (splitter.cc:586-600). */
+typedef enum GzCodec {
+  GZ_CODEC_UNCOMPRESSED = 0,
+  GZ_CODEC_LZ4_FRAME = 1,  /* Arrow IPC body compression: int64 length + one LZ4 frame per buffer */
+  GZ_CODEC_FASTPFOR = 2    /* not implemented */
+} GzCodec;
+
 /* Where Split reads its buffers from. */
 typedef enum GzInputKind {
   GZ_INPUT_HOST = 0,            /* host memory, borrowed for the call (the JNI contract) */
@@ -74,15 +83,17 @@ typedef struct GzSplitOptions {
   int32_t buffer_size;               /* rows per partition buffer, <= 32768 (default 4096) */
   int32_t num_sub_dirs;              /* spill sub-directories (default 64) */
   int32_t batch_compress_threshold;  /* default 256; compression itself is off */
-  int32_t compression;               /* 0 = uncompressed (the only codec supported) */
+  int32_t compression;               /* GzCodec (default GZ_CODEC_UNCOMPRESSED) */
   int32_t prefer_spill;              /* default 1 */
   int32_t write_schema;              /* default 1: schema message before each partition */
   int32_t buffered_write;            /* accepted for compatibility */
   int32_t input_kind;                /* GzInputKind, default GZ_INPUT_HOST */
   int32_t device;                    /* CUDA device ordinal, default 0 */
-  int32_t keep_output_on_device;     /* 1 (default): partition data stays in HBM until Stop
-                                        or until device_budget is exceeded; 0: every flush is
-                                        copied to pinned host memory as soon as it is done */
+  int32_t keep_output_on_device;     /* 1: partition data stays in HBM until Stop or until
+                                        device_budget is exceeded; 0: every device pass's
+                                        partition data is copied to pinned host memory as soon
+                                        as the pass is done; -1 (default): 0 for host inputs,
+                                        1 for device-retained inputs */
   int64_t flush_bytes;               /* input bytes gathered before one device pass
                                         (default 512 MiB, at most 1 GiB; 0: the choice
                                         gz_autotune cached for this schema, else 512 MiB) */
@@ -166,8 +177,9 @@ GzStatus gz_split_data(int64_t handle, uint8_t* dst, int64_t* out_size);
  * splitter.cc:741-756).  *actual = bytes the reference policy would release. */
 GzStatus gz_split_spill(int64_t handle, int64_t size, int64_t* actual);
 
-/* Replaces ShuffleSplitterJniWrapper.setCompressType (jni_wrapper.cc:1136-1154);
- * codec 0 (uncompressed) only, anything else is GZ_NOT_IMPLEMENTED. */
+/* Replaces ShuffleSplitterJniWrapper.setCompressType (jni_wrapper.cc:1136-1154): GzCodec
+ * UNCOMPRESSED or LZ4_FRAME (FASTPFOR is GZ_NOT_IMPLEMENTED).  Record batches are encoded at
+ * Stop, so the codec set last applies to every batch of the split. */
 GzStatus gz_split_set_compress(int64_t handle, int32_t codec);
 
 /* Replaces ShuffleSplitterJniWrapper.close (jni_wrapper.cc:1229-1234). */
@@ -366,6 +378,14 @@ GzStatus gz_debug_encode_record_batch(int64_t length, const int64_t* nodes, int3
                                       const uint8_t* const* bufs, const int64_t* buf_lens,
                                       int32_t n_bufs, uint8_t* out, int64_t out_cap,
                                       int64_t* out_len);
+
+/* The same message with LZ4_FRAME body compression, every non-empty buffer written as an
+ * uncompressed length and an LZ4 frame of stored (uncompressed) blocks of at most 64 KiB: checks
+ * the compressed message layout and the frame framing without the device compressor. */
+GzStatus gz_debug_encode_record_batch_lz4_stored(int64_t length, const int64_t* nodes, int32_t n_nodes,
+                                                const uint8_t* const* bufs, const int64_t* buf_lens,
+                                                int32_t n_bufs, uint8_t* out, int64_t out_cap,
+                                                int64_t* out_len);
 
 /* Parses an Arrow IPC Schema message and encodes it again with the splitter's schema writer (the
  * message written before each partition when write_schema is set). */

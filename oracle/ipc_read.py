@@ -70,7 +70,7 @@ def parse_stream(data: bytes, schema) -> List[Tuple[int, list]]:
         body = meta_pos + meta_len
         if htype == HEADER_RECORD_BATCH:
             rb = fb.table(msg, 2)
-            assert fb.table(rb, 3) is None, "compressed bodies"
+            compressed = fb.table(rb, 3) is not None  # BodyCompression {LZ4_FRAME, BUFFER}
             rows = fb.scalar(rb, 0, "q")
             nodes, bufs = fb.table(rb, 1), fb.table(rb, 2)
             nn, nb = fb.u32(nodes), fb.u32(bufs)
@@ -80,12 +80,43 @@ def parse_stream(data: bytes, schema) -> List[Tuple[int, list]]:
             for f, (length, nulls) in zip(schema, node_list):
                 assert length == rows
                 k = 0 if f.type == "null" else (3 if f.is_binary else 2)
-                cols.append((nulls, [data[body + o: body + o + l] for o, l in buf_list[bi:bi + k]]))
+                bufs = [data[body + o: body + o + l] for o, l in buf_list[bi:bi + k]]
+                if compressed:
+                    bufs = [_decompress(b) for b in bufs]
+                cols.append((nulls, bufs))
                 bi += k
             out.append((rows, cols))
         elif htype != HEADER_SCHEMA:
             raise ValueError(f"message type {htype}")
         pos = body + ((body_len + 7) & ~7)
+    return out
+
+
+def _decompress(b: bytes) -> bytes:
+    """A compressed body buffer: int64 uncompressed length, then one LZ4 frame (-1: raw bytes)."""
+    if not b:
+        return b
+    n = struct.unpack_from("<q", b, 0)[0]
+    if n == -1:
+        return b[8:]
+    from oracle import oracle as O
+    return O.lz4f_decompress(b[8:], n)
+
+
+def batches_compressed(data: bytes) -> List[bool]:
+    """Whether each record batch of a stream carries body compression."""
+    out, pos = [], 0
+    while pos < len(data):
+        first = struct.unpack_from("<I", data, pos)[0]
+        meta_len, meta_pos = (struct.unpack_from("<i", data, pos + 4)[0], pos + 8) if first == 0xFFFFFFFF \
+            else (first, pos + 4)
+        if meta_len == 0:
+            break
+        fb = _Flat(data[meta_pos:meta_pos + meta_len])
+        msg = fb.u32(0)
+        if fb.scalar(msg, 1, "B") == HEADER_RECORD_BATCH:
+            out.append(fb.table(fb.table(msg, 2), 3) is not None)
+        pos = meta_pos + meta_len + ((fb.scalar(msg, 3, "q") + 7) & ~7)
     return out
 
 

@@ -30,11 +30,12 @@ _I64P = ctypes.POINTER(ctypes.c_int64)
 
 
 def build_oracle(force: bool = False) -> str:
-    src = os.path.join(HERE, "split_oracle.cc")
-    if force or not os.path.exists(ORACLE_SO) or os.path.getmtime(ORACLE_SO) < max(
-            os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "spark_hash.h"))):
-        subprocess.check_call(["g++", "-std=c++17", "-O3", "-fPIC", "-shared", src,
-                               "-o", ORACLE_SO])
+    srcs = [os.path.join(HERE, f) for f in ("split_oracle.cc", "lz4_oracle.cc")]
+    deps = srcs + [os.path.join(HERE, "spark_hash.h")]
+    if force or not os.path.exists(ORACLE_SO) or os.path.getmtime(ORACLE_SO) < max(map(os.path.getmtime, deps)):
+        tmp = ORACLE_SO + f".{os.getpid()}.tmp"
+        subprocess.check_call(["g++", "-std=c++17", "-O3", "-fPIC", "-shared", *srcs, "-o", tmp])
+        os.replace(tmp, ORACLE_SO)
     return ORACLE_SO
 
 
@@ -109,6 +110,10 @@ class OracleSplitter:
             lib.gzo_hash_long.argtypes = [ctypes.c_int64, ctypes.c_int32]
             lib.gzo_murmur3_bytes.restype = ctypes.c_uint32
             lib.gzo_murmur3_bytes.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32]
+            lib.gzo_xxh32.restype = ctypes.c_uint32
+            lib.gzo_xxh32.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_uint32]
+            lib.gzo_lz4f_decompress.restype = ctypes.c_int64
+            lib.gzo_lz4f_decompress.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64]
             lib.gzo_pmod.restype = ctypes.c_int32
             lib.gzo_pmod.argtypes = [ctypes.c_int32, ctypes.c_int32]
             cls._lib = lib
@@ -302,3 +307,20 @@ def run_ref(schema, batches, num_partitions, key_cols, **opts) -> SplitOutput:
     out = s.stop()
     s.close()
     return out
+
+
+# ---------------------------------------------------------------------------------------
+# LZ4 frame decoding (oracle/lz4_oracle.cc)
+def xxh32(data: bytes, seed: int = 0) -> int:
+    b = np.frombuffer(data, np.uint8)
+    return OracleSplitter.lib().gzo_xxh32(b.ctypes.data if b.nbytes else None, b.nbytes, seed)
+
+
+def lz4f_decompress(frame: bytes, size: int) -> bytes:
+    """Decodes one LZ4 frame that holds `size` bytes; raises on a malformed frame."""
+    src = np.frombuffer(frame, np.uint8)
+    dst = np.zeros(max(size, 1), np.uint8)
+    n = OracleSplitter.lib().gzo_lz4f_decompress(src.ctypes.data, src.nbytes, dst.ctypes.data, size)
+    if n != size:
+        raise ValueError(f"bad LZ4 frame (decoded {n} of {size} bytes)")
+    return dst[:size].tobytes()

@@ -360,3 +360,17 @@ def test_errors_are_reported_not_crashed():
     w.split(h, b.num_rows, addrs, sizes)
     w.stop(h)
     w.close(h)
+
+
+@pytest.mark.gpu
+def test_large_data_file_written_through_mapping(tmp_path):
+    """A data file of 256 MiB or more is written through a memory mapping (partitions copied in
+    in parallel); its bytes equal the in-memory data of the same split."""
+    batches = W.c2_batches(77, 400, 4096)  # ~290 MB of partition data
+    path = str(tmp_path / "data")
+    res_f, _ = S.split_batches(W.C2_SCHEMA, batches, W.C2_PARTITIONS, W.C2_KEYS, dataFile=path)
+    res_m, data = S.split_batches(W.C2_SCHEMA, batches, W.C2_PARTITIONS, W.C2_KEYS)
+    assert len(data) >= 256 << 20
+    with open(path, "rb") as f:
+        assert f.read() == data
+    assert np.array_equal(res_f.partitionLengths, res_m.partitionLengths)

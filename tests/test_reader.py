@@ -113,11 +113,24 @@ def _check(schema, streams):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("write_schema", [False, True])
-def test_gpu_reader_matches_oracle_on_oracle_streams(write_schema):
-    outs = map_outputs(W.C1_SCHEMA, W.C1_KEYS, 8, [4, 5, 6], c1_make, write_schema=write_schema, buffer_size=700)
+def test_gpu_reader_matches_oracle_on_oracle_streams():
+    outs = map_outputs(W.C1_SCHEMA, W.C1_KEYS, 8, [4, 5, 6], c1_make, buffer_size=700)
     for p in range(8):
         _check(W.C1_SCHEMA, streams_of(outs, p))
+
+
+@pytest.mark.gpu
+def test_gpu_reader_streams_with_schema_message():
+    """The splitter's streams with write_schema: a schema message before each partition's batches."""
+    from gazelle_plugin_gb300 import shuffle as S
+    P = 8
+    outs = []
+    for seed in (11, 12):
+        res, data = S.split_batches(W.C1_SCHEMA, c1_make(seed), P, W.C1_KEYS, writeSchema=True, bufferSize=900)
+        starts = np.concatenate([[0], np.cumsum(np.asarray(res.partitionLengths))])
+        outs.append([data[starts[p]:starts[p + 1]] for p in range(P)])
+    for p in range(P):
+        _check(W.C1_SCHEMA, [o[p] for o in outs])
 
 
 @pytest.mark.gpu
