@@ -454,12 +454,13 @@ def _prefix_batch(batch, schema, r: int):
 
 
 def run_batched(seed: int = 3, n_batches: int = 512, window: int = 64, tune_batches: int = 64):
-    """Config 4: 512 uneven batches, each task = (schema, partitions); plain = every Split its own
-    device pass, waited for; batched = the stream cut into windows of `window` batches, each
-    task's batches of a window handed over in one splitBatches call, and each task's batches
-    fused into device passes whose size (and segment length) the autotuner chose for the task's
-    schema from its first `tune_batches` batches (outside the timed region); the tasks' passes
-    overlap on the GPU."""
+    """Config 4: 512 uneven batches, each task = (schema, partitions).  plain = the drop-in as it
+    ships: one split call per batch with the default options (deferred passes, no wait per
+    call); batched = the stream cut into windows of `window` batches, each task's batches of a
+    window handed over in one splitBatches call, and each task's batches fused into device passes
+    whose size (and segment length) the autotuner chose for the task's schema from its first
+    `tune_batches` batches (outside the timed region).  Both run until every task's device work
+    is done; the tasks' passes overlap on the GPU in both."""
     from gazelle_plugin_gb300 import shuffle as S
     from gazelle_plugin_gb300 import workloads as W
     pool = _mixed_pool(seed)
@@ -490,12 +491,11 @@ def run_batched(seed: int = 3, n_batches: int = 512, window: int = 64, tune_batc
                 schema, keys = W.C4_SCHEMAS[si]
                 hs[(si, P)] = w.make(S.NativePartitioning("hash", P, None, keys, list(schema)),
                                      writeSchema=False, dataFile="/dev/null",
-                                     flush_bytes=1 if plain else 0, seg_tiles=0)
+                                     **({} if plain else dict(flush_bytes=0, seg_tiles=0)))
         t0 = time.perf_counter()
         if plain:
             for (si, P, b), (a, z) in zip(calls, bufs):
                 w.split(hs[(si, P)], b.num_rows, a, z)
-                w.sync(hs[(si, P)])
         else:
             for w0 in range(0, len(calls), window):
                 groups = {}
@@ -658,26 +658,46 @@ def run_served(seed: int = 4, n_tasks: int = 32, rate: float = 4000.0, gb_per_ta
         return lat, dt, out
 
     def plain(paced: bool):
+        """The drop-in as an executor calls it: each task on its own thread (a task slot) makes
+        its split calls itself, at their arrival times; a call's latency ends when split returns
+        (its inputs read, its rows queued for the device), the same point as a served call's.
+        Each thread then waits for its task's device work, as the served form's syncs do."""
         hs = [w.make(S.NativePartitioning("hash", P, None, W.C4_SCHEMAS[si][1], list(W.C4_SCHEMAS[si][0])),
-                     **dict(opts, flush_bytes=1)) for si, P in specs]
-        lat = []
-        t0 = time.perf_counter()
-        for t, k, si, r in calls:
-            if paced:
-                d = t0 + t - time.perf_counter()
-                if d > 0:
-                    time.sleep(d)
-            b = batch(si, r)
-            a, z = b.addrs_sizes()
-            w.split(hs[k], r, a, z)
+                     **opts) for si, P in specs]
+        per_task = [[] for _ in specs]
+        for c in calls:
+            per_task[c[1]].append(c)
+        lats = [[] for _ in specs]
+        start = threading.Barrier(len(specs) + 1)
+        t0 = [0.0]
+
+        def task(k):
+            start.wait()
+            for t, _, si, r in per_task[k]:
+                if paced:
+                    d = t0[0] + t - time.perf_counter()
+                    if d > 0:
+                        time.sleep(d)
+                arrive = t0[0] + t if paced else time.perf_counter()
+                b = batch(si, r)
+                a, z = b.addrs_sizes()
+                w.split(hs[k], r, a, z)
+                lats[k].append((time.perf_counter() - arrive) * 1e9)
             w.sync(hs[k])
-            lat.append((time.perf_counter() - t0 - (t if paced else 0.0)) * 1e9)
-        dt = time.perf_counter() - t0
+
+        ths = [threading.Thread(target=task, args=(k,)) for k in range(len(specs))]
+        for th in ths:
+            th.start()
+        t0[0] = time.perf_counter()
+        start.wait()
+        for th in ths:
+            th.join()
+        dt = time.perf_counter() - t0[0]
         out = 0
         for k, h in enumerate(hs):
             out += int(w.stop(h, specs[k][1]).rawPartitionLengths.sum())
             w.close(h)
-        return lat, dt, out
+        return [x for l in lats for x in l], dt, out
 
     def pct(v, q):
         return float(np.percentile(np.asarray(v, np.float64), q)) / 1e6
@@ -695,7 +715,9 @@ def run_served(seed: int = 4, n_tasks: int = 32, rate: float = 4000.0, gb_per_ta
                          f"3 schemas x P in {{64,200,1024}}, stop after {gb_per_task:g} GB input per task, "
                          f"spill threshold {threshold >> 20} MiB, HBM budget {budget >> 30} GiB, "
                          f"{slots} serving workers"),
-            "latency": "per Split call, submission (paced at its arrival time) to completion",
+            "latency": ("per Split call, its arrival time to the point where its inputs are read and its "
+                        "rows queued for the device (served: the ticket completes; plain: split returns)"),
+            "plain_path": "each task on its own thread calling split itself (the drop-in as an executor calls it)",
             "capacity": "the same calls submitted without pacing",
             "calls": len(calls), "input_bytes": in_bytes, "partition_bytes": res.pop("partition_bytes"),
             "served": res["served"], "plain": res["plain"],

@@ -31,7 +31,7 @@ constexpr int kScatterThreads = 256;
 constexpr int kPlanThreads = 1024;
 constexpr int kMaxBatchesPerFlush = 4096;
 
-enum KeyKind : int32_t { KEY_I32 = 0, KEY_I64 = 1, KEY_I8 = 2, KEY_I16 = 3, KEY_BOOL = 4 };
+enum KeyKind : int32_t { KEY_I32 = 0, KEY_I64 = 1, KEY_I8 = 2, KEY_I16 = 3, KEY_BOOL = 4, KEY_STR = 5 };
 // Splitter::Make short names (native-sql-engine/cpp/src/shuffle/splitter.cc:190-208):
 // "hash" (HashSplitter), "rr" and "single" (RoundRobinSplitter, single = 1 partition),
 // "range" (FallbackRangeSplitter: int32 ids in schema field 0, key_col[0] = 0)

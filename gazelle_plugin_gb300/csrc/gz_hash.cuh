@@ -39,6 +39,23 @@ __device__ __forceinline__ int32_t hash_long(int64_t v, int32_t seed) {
   return (int32_t)fmix32(h1, 8);
 }
 
+// Spark Murmur3_x86_32.hashUnsafeBytes (the utf8 key hash): 4-byte little-endian blocks, then
+// every remaining byte, sign-extended, as a block of its own; finalised with the byte length.
+// The blocks are funnel-shifted out of aligned words; the second word of a pair always holds a
+// byte of the string, so no word past the string's last aligned word is read.
+__device__ __forceinline__ int32_t hash_bytes(const uint8_t* p, int32_t len, int32_t seed) {
+  uint32_t h1 = (uint32_t)seed;
+  const int32_t aligned = len & ~3;
+  const uint32_t* base = reinterpret_cast<const uint32_t*>(reinterpret_cast<uintptr_t>(p) & ~uintptr_t(3));
+  const uint32_t sh = (uint32_t)(reinterpret_cast<uintptr_t>(p) & 3) * 8;
+  for (int32_t i = 0; i < aligned; i += 4) {
+    const uint32_t k = sh ? __funnelshift_r(base[i >> 2], base[(i >> 2) + 1], sh) : base[i >> 2];
+    h1 = mix_h1(h1, mix_k1(k));
+  }
+  for (int32_t i = aligned; i < len; i++) h1 = mix_h1(h1, mix_k1((uint32_t)(int32_t)(int8_t)p[i]));
+  return (int32_t)fmix32(h1, (uint32_t)len);
+}
+
 // Spark pmod(h, P) without a hardware divide: Lemire, Kaser & Kurz, "Faster remainder by
 // direct computation" (2019): a mod d = hi64((M * a) mod 2^64 * d) with M = floor(2^64-1 / d) + 1.
 __device__ __forceinline__ uint32_t fastmod_u32(uint32_t a, uint32_t d, unsigned long long M) {

@@ -182,6 +182,9 @@ __global__ void __launch_bounds__(kHashThreads) k_hash_count(const SchemaDesc sd
       v[1] = a0.y;
       v[2] = a0.z;
       v[3] = a0.w;
+    } else if (kind == KEY_STR) {
+#pragma unroll
+      for (int u = 0; u < kHashRows; u++) v[u] = 0;  // hashed below from the offsets
     } else {
 #pragma unroll
       for (int u = 0; u < kHashRows; u++) {
@@ -202,6 +205,21 @@ __global__ void __launch_bounds__(kHashThreads) k_hash_count(const SchemaDesc sd
     }
 #pragma unroll
     for (int u = 0; u < kHashRows; u++) valid[u] = c.validity == nullptr || get_bit(c.validity, rr[u]);
+    if (kind == KEY_STR) {
+      // utf8 key: offsets were checked against the characters by Split (host inputs) or are the
+      // caller's device buffers
+#pragma unroll
+      for (int u = 0; u < kHashRows; u++) {
+        if (!valid[u] || !act[u]) continue;
+        const int32_t o0 = c.offsets[rr[u]], o1 = c.offsets[rr[u] + 1];
+        if (o0 < 0 || o1 < o0 || (uint64_t)o1 > c.values_bytes) {
+          bad = true;
+          continue;
+        }
+        h[u] = hash_bytes(c.values + o0, o1 - o0, h[u]);
+      }
+      continue;
+    }
 #pragma unroll
     for (int u = 0; u < kHashRows; u++)  // null: seed passes
       if (valid[u]) h[u] = kind == KEY_I64 ? hash_long(v[u], h[u]) : hash_int((int32_t)v[u], h[u]);

@@ -213,6 +213,7 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
       case GZ_TYPE_INT16: kind = KEY_I16; break;
       case GZ_TYPE_INT32: case GZ_TYPE_FLOAT32: case GZ_TYPE_DATE32: kind = KEY_I32; break;
       case GZ_TYPE_INT64: case GZ_TYPE_FLOAT64: kind = KEY_I64; break;
+      case GZ_TYPE_STRING: kind = KEY_STR; break;  // hashbuf_spark (splitter.cc:1424-1427)
       default:
         return Status::Error(GZ_NOT_IMPLEMENTED,
                              "hash key type has no Spark-compatible hash in the GPU splitter");
@@ -1758,24 +1759,77 @@ Status Splitter::CompressedSize(int32_t num_rows, const int64_t* addrs, const in
     return Status::Error(GZ_NOT_IMPLEMENTED, "CompressedSize reads host buffers");
   const uint32_t nr = (uint32_t)std::max(num_rows, 0);
   auto pad8 = [](int64_t x) { return (x + 7) & ~int64_t(7); };
-  int64_t body = 0;
+  // the body buffers as the IPC writer lays them out (validity only with nulls)
+  std::vector<std::pair<const uint8_t*, int64_t>> bufs;
   for (size_t f = 0; f < fields_.size(); f++) {
     const int t = fields_[f].type;
     if (t == GZ_TYPE_NULL) continue;
     const int b0 = field_buf0_[f];
-    if (addrs[b0] != 0 && sizes[b0] > 0 && nr > 0) {
-      const int64_t z = CountZeros(reinterpret_cast<const uint8_t*>(addrs[b0]), nr);
-      if (z > 0) body += pad8(BytesForBits(nr));
-    }
+    const uint8_t* vb = reinterpret_cast<const uint8_t*>(addrs[b0]);
+    bufs.push_back({vb, addrs[b0] != 0 && sizes[b0] > 0 && nr > 0 && CountZeros(vb, nr) > 0 ? BytesForBits(nr) : 0});
     if (IsBinary(t)) {
       const int32_t* off = reinterpret_cast<const int32_t*>(addrs[b0 + 1]);
-      body += pad8((int64_t)(nr + 1) * 4);
-      if (nr > 0 && off) body += pad8(off[nr] - off[0]);
-    } else if (t == GZ_TYPE_BOOL) {
-      body += pad8(BytesForBits(nr));
+      bufs.push_back({reinterpret_cast<const uint8_t*>(off), (int64_t)(nr + 1) * 4});
+      const int64_t c0 = nr > 0 && off ? off[0] : 0, c1 = nr > 0 && off ? off[nr] : 0;
+      bufs.push_back({reinterpret_cast<const uint8_t*>(addrs[b0 + 2]) + c0, c1 - c0});
     } else {
-      body += pad8((int64_t)nr * ByteWidth(t));
+      bufs.push_back({reinterpret_cast<const uint8_t*>(addrs[b0 + 1]),
+                      t == GZ_TYPE_BOOL ? BytesForBits(nr) : (int64_t)nr * ByteWidth(t)});
     }
+  }
+  int64_t body = 0;
+  if (codec_ == GZ_CODEC_UNCOMPRESSED || nr == 0) {
+    for (auto& b : bufs) body += pad8(b.second);
+    *out = body;
+    return Status::OK();
+  }
+  // LZ4_FRAME (GetRecordBatchPayload with the codec, splitter.cc:358-369): the buffers compressed
+  // by the device; each non-empty one costs its uncompressed length (8 bytes), the frame header
+  // (7), a size word per block and the end mark (4)
+  Status st = Cuda(cudaSetDevice(device_), "cudaSetDevice");
+  if (!st.ok()) return st;
+  int64_t total = 0;
+  for (auto& b : bufs) total += (int64_t)AlignUp((size_t)b.second, 16);
+  std::vector<Lz4Chunk> chunks;
+  const size_t scratch = (size_t)lz4_compress_warps() * kLz4Slot;
+  uint8_t* d = nullptr;
+  const size_t nch = (size_t)(total / kLz4MaxBlock) + bufs.size() + 1;
+  const size_t tab = AlignUp(sizeof(Lz4Chunk) * nch, 256), rb = AlignUp(sizeof(Lz4Block) * nch, 256);
+  st = Cuda(cudaMallocAsync(reinterpret_cast<void**>(&d), tab + rb + 256 + scratch + 2 * (size_t)total + 256, stream_),
+            "cudaMallocAsync(compressed size)");
+  if (!st.ok()) return st;
+  uint8_t* d_in = d + tab + rb + 256 + scratch;
+  uint8_t* d_arena = d_in + total;
+  int64_t at = 0;
+  for (auto& b : bufs) {
+    if (b.second <= 0) continue;
+    if (st.ok()) st = Cuda(cudaMemcpyAsync(d_in + at, b.first, (size_t)b.second, cudaMemcpyHostToDevice, stream_), "H2D");
+    for (int64_t x = 0; x < b.second; x += kLz4MaxBlock)
+      chunks.push_back(Lz4Chunk{d_in + at + x, (uint32_t)std::min<int64_t>(kLz4MaxBlock, b.second - x), 0u});
+    at += (int64_t)AlignUp((size_t)b.second, 16);
+  }
+  std::vector<Lz4Block> res(chunks.size());
+  int32_t err = 0;
+  if (st.ok()) st = Cuda(cudaMemcpyAsync(d, chunks.data(), sizeof(Lz4Chunk) * chunks.size(), cudaMemcpyHostToDevice, stream_), "H2D");
+  if (st.ok()) st = Cuda(cudaMemsetAsync(d + tab + rb, 0, 256, stream_), "memset");
+  if (st.ok())
+    st = Cuda(launch_lz4_compress(reinterpret_cast<Lz4Chunk*>(d), (uint32_t)chunks.size(),
+                                  reinterpret_cast<uint32_t*>(d + tab + rb + 8), d + tab + rb + 256, d_arena,
+                                  reinterpret_cast<unsigned long long*>(d + tab + rb), (unsigned long long)total + 256,
+                                  reinterpret_cast<Lz4Block*>(d + tab), reinterpret_cast<int32_t*>(d + tab + rb + 16), stream_),
+              "k_lz4_compress");
+  if (st.ok()) st = Cuda(cudaMemcpyAsync(res.data(), d + tab, sizeof(Lz4Block) * res.size(), cudaMemcpyDeviceToHost, stream_), "D2H");
+  if (st.ok()) st = Cuda(cudaMemcpyAsync(&err, d + tab + rb + 16, 4, cudaMemcpyDeviceToHost, stream_), "D2H");
+  if (st.ok()) st = Cuda(cudaStreamSynchronize(stream_), "k_lz4_compress");
+  cudaFreeAsync(d, stream_);
+  if (!st.ok()) return st;
+  if (err) return Status::Error(GZ_CUDA, "compression arena overflow");
+  size_t k = 0;
+  for (auto& b : bufs) {
+    if (b.second <= 0) continue;
+    int64_t len = 8 + 7 + 4;
+    for (int64_t x = 0; x < b.second; x += kLz4MaxBlock) len += 4 + res[k++].size;
+    body += pad8(len);
   }
   *out = body;
   return Status::OK();

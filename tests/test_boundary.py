@@ -196,6 +196,8 @@ def test_make_rejects_bad_arguments_before_touching_the_device():
     assert make("hash", 0, c1, [0]) == S.GZ_INVALID
     assert make("hash", 65537, c1, [0]) == S.GZ_INVALID
     assert make("rr", 4, c1, [], buffer_size=40000) == S.GZ_INVALID
-    assert make("hash", 4, c1, [3]) == S.GZ_NOT_IMPLEMENTED  # utf8 key: no Spark-compatible hash here
+    c1b = c1 + [W.Field("b", "binary"), W.Field("d", "decimal128")]
+    assert make("hash", 4, c1b, [4]) == S.GZ_NOT_IMPLEMENTED  # binary key: no Spark-compatible hash here
+    assert make("hash", 4, c1b, [5]) == S.GZ_NOT_IMPLEMENTED  # decimal key: neither
     assert make("hash", 4, c1, [9]) == S.GZ_INVALID          # key column out of range
     assert make("hash", 4, c1, [0], null_keys=True) == S.GZ_INVALID

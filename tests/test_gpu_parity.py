@@ -344,8 +344,8 @@ def test_errors_are_reported_not_crashed():
     assert e.value.status == S.GZ_NOT_IMPLEMENTED
     with pytest.raises(S.SplitterError):
         w.make(S.NativePartitioning("hash", 0, None, [0], list(W.C1_SCHEMA)))
-    with pytest.raises(S.SplitterError):
-        w.make(S.NativePartitioning("hash", 4, None, [3], list(W.C1_SCHEMA)))  # utf8 key
+    with pytest.raises(S.SplitterError):  # binary key: no Spark-compatible hash
+        w.make(S.NativePartitioning("hash", 4, None, [4], list(W.C1_SCHEMA) + [W.Field("b", "binary")]))
     h = w.make(S.NativePartitioning("hash", 4, None, [0], list(W.C1_SCHEMA)), writeSchema=False)
     b = W.c1_batches(0, 1, 100)[0]
     addrs, sizes = b.addrs_sizes()
@@ -374,3 +374,33 @@ def test_large_data_file_written_through_mapping(tmp_path):
     with open(path, "rb") as f:
         assert f.read() == data
     assert np.array_equal(res_f.partitionLengths, res_m.partitionLengths)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", range(4))
+def test_utf8_hash_keys_vs_oracle(seed):
+    """utf8 key columns (the reference's hashbuf_spark, restated as Spark's hashUnsafeBytes),
+    alone and chained with an int key, with null keys and empty strings, over strings of every
+    length mod 4 and alignment phase."""
+    rng = np.random.default_rng(900 + seed)
+    schema = [W.Field("s", "utf8"), W.Field("k", "int32"), W.Field("v", "int64"), W.Field("t", "utf8")]
+    keys = [[0], [0, 1], [3, 1, 0], [1, 3]][seed]
+    batches = [W.random_batch(rng, schema, int(rng.integers(500, 5000)), 0.15) for _ in range(4)]
+    # bytes >= 0x80 too: the tail bytes of a string are hashed sign-extended
+    hi = bytes(range(1, 256))
+    for b in batches[::2]:
+        b.buffers[0:3] = W._column(rng, schema[0], b.num_rows, None, 0.1, (0, 23, hi))
+    P = [7, 64, 200, 1000][seed]
+    want = O.run_oracle(schema, batches, P, keys)
+    res, data = S.split_batches(schema, batches, P, keys, writeSchema=False)
+    assert data == want.data
+    w = S.ShuffleSplitterJniWrapper()
+    h = w.make(S.NativePartitioning("hash", P, None, keys, schema), writeSchema=False)
+    o = O.OracleSplitter(schema, P, keys)
+    for b in batches:
+        a, z = b.addrs_sizes()
+        w.split(h, b.num_rows, a, z)
+        o.split(b)
+        assert np.array_equal(w.lastPids(h, b.num_rows), o.last_pids(b.num_rows))
+    w.close(h)
+    o.close()

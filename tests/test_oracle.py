@@ -162,3 +162,21 @@ def test_oracle_null_type_key_matches_live_reference():
     o = O.run_oracle(schema, batches, 8, keys)
     assert r.data == o.data
     assert (r.raw_partition_lengths == o.raw_partition_lengths).all()
+
+
+@pytest.mark.skipif(not O.RefSplitter.available(), reason="reference build absent here")
+def test_oracle_utf8_keys_match_live_reference():
+    """utf8 hash keys: the reference's hashbuf_spark has no body in the reference tree; both the
+    oracle and the reference build's gandiva stand-in restate Spark's hashUnsafeBytes, so this
+    checks the chain, nulls and tail-byte handling end to end, not the fork's body."""
+    rng = np.random.default_rng(77)
+    schema = [W.Field("s", "utf8"), W.Field("k", "int32"), W.Field("v", "int64")]
+    hi = bytes(range(1, 256))
+    for trial in range(6):
+        batches = [W.random_batch(rng, schema, int(rng.integers(100, 2000)), 0.2) for _ in range(3)]
+        for b in batches[::2]:
+            b.buffers[0:3] = W._column(rng, schema[0], b.num_rows, None, 0.1, (0, 23, hi))
+        keys = [[0], [0, 1], [1, 0]][trial % 3]
+        r = O.run_ref(schema, batches, 16, keys)
+        o = O.run_oracle(schema, batches, 16, keys)
+        assert r.data == o.data, trial
