@@ -242,6 +242,37 @@ def digests(paths):
         return list(ex.map(S.digest_file, paths))
 
 
+def read_back(sch, paths, lengths, partitions=None):
+    """The reduce side: every partition's streams of all map outputs (the task files, memory
+    mapped: page-cache bytes, as a shuffle fetch leaves them) read into device columns by the
+    CUDA reader, one partition at a time.  GB/s = (stream bytes + column bytes) / time."""
+    from gazelle_plugin_gb300 import shuffle as S
+    maps = [np.memmap(p, dtype=np.uint8, mode="r") for p in paths]
+    starts = [np.concatenate([[0], np.cumsum(l)]) for l in lengths]
+    P = lengths[0].shape[0]
+    parts = range(P) if partitions is None else partitions
+    in_bytes = out_bytes = 0
+    t0 = time.perf_counter()
+    for p in parts:
+        r = S.PartitionReader(list(sch))
+        for m, st in zip(maps, starts):
+            if st[p + 1] > st[p]:
+                r.addStream(m[st[p]:st[p + 1]])
+                in_bytes += int(st[p + 1] - st[p])
+        rows, _ = r.finish()
+        for f in range(len(sch)):
+            c = r.column(f)
+            out_bytes += c.values_bytes + (c.length + 1) * 4 * (c.offsets is not None) + \
+                ((c.length + 7) // 8 if c.validity else 0)
+        r.close()
+    dt = time.perf_counter() - t0
+    del maps
+    return {"value": (in_bytes + out_bytes) / dt / 1e9, "unit": "GB/s", "seconds": dt,
+            "stream_bytes": in_bytes, "column_bytes": out_bytes, "partitions": len(parts),
+            "what": ("each partition's streams of all map outputs (memory-mapped data files) into one "
+                     "set of device columns: host parse, one copy per stream, device concatenation")}
+
+
 def oracle_tasks(sch, keys, partitioner, rows, haddrs, sizes, n_tasks: int, ddir: str, digest: bool = False):
     """The CPU splitter as map tasks: `n_tasks` oracle splitters on their own threads, each over a
     contiguous range of the batches (the same ranges the GPU tasks take), split then Stop writing
@@ -456,8 +487,9 @@ def _prefix_batch(batch, schema, r: int):
 def run_batched(seed: int = 3, n_batches: int = 512, window: int = 64, tune_batches: int = 64):
     """Config 4: 512 uneven batches, each task = (schema, partitions).  plain = the drop-in as it
     ships: one split call per batch with the default options (deferred passes, no wait per
-    call); batched = the stream cut into windows of `window` batches, each task's batches of a
-    window handed over in one splitBatches call, and each task's batches fused into device passes
+    call); batched = the stream cut into windows of `window` batches, all tasks' batches of a
+    window handed over in one splitGroup call (every task's host reads in flight together), and
+    each task's batches fused into device passes
     whose size (and segment length) the autotuner chose for the task's schema from its first
     `tune_batches` batches (outside the timed region).  Both run until every task's device work
     is done; the tasks' passes overlap on the GPU in both."""
@@ -501,9 +533,10 @@ def run_batched(seed: int = 3, n_batches: int = 512, window: int = 64, tune_batc
                 groups = {}
                 for i in range(w0, min(w0 + window, len(calls))):
                     groups.setdefault(calls[i][:2], []).append(i)
-                for key, idx in groups.items():
-                    w.splitBatches(hs[key], [calls[i][2].num_rows for i in idx],
-                                   np.stack([bufs[i][0] for i in idx]), np.stack([bufs[i][1] for i in idx]))
+                keys = list(groups)
+                w.splitGroup([hs[k] for k in keys], [[calls[i][2].num_rows for i in groups[k]] for k in keys],
+                             [np.stack([bufs[i][0] for i in groups[k]]) for k in keys],
+                             [np.stack([bufs[i][1] for i in groups[k]]) for k in keys])
         for h in hs.values():
             w.sync(h)
         dt = time.perf_counter() - t0
@@ -843,11 +876,26 @@ def run_gpu(args):
                 barrier()
             gpu_files = digests(task_files(ddir, tasks))
             gpu_lengths = runs[-1]["partition_lengths"]
+            read = None if args.no_read else read_back(sch, task_files(ddir, tasks), gpu_lengths)
             remove_dir(ddir)
             ddir = scratch_dir()
             one = S.run_map_tasks(part, rows, haddrs, sizes, 1, ddir, **e2e_opts)
             remove_dir(ddir)
             ddir = scratch_dir()
+            lz4 = None
+            if not args.no_lz4:
+                z_opts = dict(e2e_opts, codec="lz4")
+                S.run_map_tasks(part, rows, haddrs, sizes, tasks, ddir, **z_opts)  # warm-up
+                zr = S.run_map_tasks(part, rows, haddrs, sizes, tasks, ddir, **z_opts)
+                z_alg = zr["input_bytes"] + zr["raw_partition_bytes"]
+                lz4 = {"value": z_alg / zr["wall_s"] / 1e9, "unit": "GB/s", "tasks": tasks,
+                       "wall_s": zr["wall_s"], "split_s_max": zr["split_s_max"], "stop_s_max": zr["stop_s_max"],
+                       "bytes_written": zr["bytes_written"],
+                       "compression_ratio": zr["raw_partition_bytes"] / max(zr["bytes_written"], 1),
+                       "what": ("the e2e run with LZ4_FRAME: record batches above 256 rows compressed by the "
+                                "device at Stop; metric bytes as for e2e (uncompressed sizes)")}
+                remove_dir(ddir)
+                ddir = scratch_dir()
             e_t = reduce_over_ranks(sum(r["wall_s"] for r in runs), "max")
             e_alg = runs[-1]["input_bytes"] + runs[-1]["raw_partition_bytes"]
             e2e = {"value": reduce_over_ranks(float(e_alg), "sum") * args.steps / e_t / 1e9, "unit": "GB/s",
@@ -861,6 +909,8 @@ def run_gpu(args):
                    "split_s_max": statistics.mean(r["split_s_max"] for r in runs),
                    "stop_s_max": statistics.mean(r["stop_s_max"] for r in runs),
                    "bytes_written_per_step": runs[-1]["bytes_written"],
+                   "lz4": lz4,
+                   "read": read,
                    "one_task": {"value": (one["input_bytes"] + one["raw_partition_bytes"]) / one["wall_s"] / 1e9,
                                 "unit": "GB/s", "wall_s": one["wall_s"], "split_s": one["split_s_max"],
                                 "stop_s": one["stop_s_max"]},
@@ -937,6 +987,8 @@ def main():
     ap.add_argument("--traffic-per-launch", type=float, default=None)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-read", action="store_true", help="skip the reduce-side read line")
+    ap.add_argument("--no-lz4", action="store_true", help="skip the LZ4_FRAME e2e line")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched and served forms")
     ap.add_argument("--served-gb-per-task", type=float, default=2.0)
     ap.add_argument("--partitioner", default="hash", choices=["hash", "rr", "range"],

@@ -222,6 +222,38 @@ GzStatus gz_split_split_batches(int64_t handle, int32_t n_batches, const int32_t
   return Report(e.get(), e->splitter->SplitBatches(n_batches, rows, buf_addrs, buf_sizes, n_bufs));
 }
 
+GzStatus gz_split_split_group(int32_t n_tasks, const int64_t* handles, const int32_t* n_batches,
+                              const int32_t* rows, const int64_t* buf_addrs, const int64_t* buf_sizes,
+                              const int32_t* n_bufs) {
+  if (n_tasks < 0 || (n_tasks > 0 && (!handles || !n_batches || !rows || !buf_addrs || !buf_sizes || !n_bufs))) {
+    t_make_error = "gz_split_split_group: null argument";
+    return GZ_INVALID;
+  }
+  std::vector<std::shared_ptr<Entry>> es;
+  std::vector<gz::Splitter*> ts;
+  for (int i = 0; i < n_tasks; i++) {
+    auto e = Lookup(handles[i]);
+    if (!e) {
+      t_make_error = "Invalid splitter id " + std::to_string(handles[i]);
+      return GZ_INVALID;
+    }
+    for (int j = 0; j < i; j++)
+      if (handles[j] == handles[i]) {
+        t_make_error = "gz_split_split_group: a task appears twice";
+        return GZ_INVALID;
+      }
+    es.push_back(e);
+    ts.push_back(e->splitter.get());
+  }
+  int failed = -1;
+  gz::Status st = gz::SplitGroup(ts, n_batches, rows, buf_addrs, buf_sizes, n_bufs, &failed);
+  if (!st.ok()) {
+    if (failed >= 0) es[failed]->last_error = st.msg;
+    t_make_error = "task " + std::to_string(failed) + ": " + st.msg;
+  }
+  return st.code;
+}
+
 GzStatus gz_split_sync(int64_t handle) {
   auto e = Lookup(handle);
   if (!e) return GZ_INVALID;

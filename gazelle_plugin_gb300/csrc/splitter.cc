@@ -414,11 +414,17 @@ Status Splitter::Split(int32_t num_rows, const int64_t* addrs, const int64_t* si
 
 Status Splitter::SplitBatches(int32_t n_batches, const int32_t* rows, const int64_t* addrs,
                               const int64_t* sizes, int32_t n) {
+  Status st = SplitMany(n_batches, rows, addrs, sizes, n);
+  Status fin = FinishHostReads();
+  return st.ok() ? fin : st;
+}
+
+Status Splitter::SplitMany(int32_t n_batches, const int32_t* rows, const int64_t* addrs, const int64_t* sizes,
+                           int32_t n) {
   Status st;
   for (int32_t i = 0; i < n_batches && st.ok(); i++)
     st = SplitOne(rows[i], addrs + (size_t)i * n, sizes + (size_t)i * n, n);
-  Status fin = FinishHostReads();
-  return st.ok() ? fin : st;
+  return st;
 }
 
 // Launches k_gather over the descriptors queued since the last launch.
@@ -434,14 +440,51 @@ Status Splitter::LaunchGather() {
 // Waits until every queued host read has landed in device staging; afterwards the caller's
 // host buffers are no longer needed and the descriptor ring starts over.
 Status Splitter::FinishHostReads() {
+  Status st = StartHostReads();
+  return st.ok() ? WaitHostReads() : st;
+}
+
+// Launches the queued host reads and marks their end; WaitHostReads waits for that mark.
+Status Splitter::StartHostReads() {
   if (!direct_ || jobs_end_ == 0) return Status::OK();
   Status st = LaunchGather();
   if (!st.ok()) return st;
   st = Cuda(cudaEventRecord(gather_ev_, cstream_), "event");
   if (!st.ok()) return st;
-  st = Cuda(cudaEventSynchronize(gather_ev_), "host reads");
+  reads_marked_ = true;
+  return Status::OK();
+}
+
+Status Splitter::WaitHostReads() {
+  if (!reads_marked_) return Status::OK();
+  reads_marked_ = false;
+  Status st = Cuda(cudaEventSynchronize(gather_ev_), "host reads");
   if (!st.ok()) return st;
   jobs_begin_ = jobs_end_ = 0;
+  return Status::OK();
+}
+
+Status SplitGroup(const std::vector<Splitter*>& tasks, const int32_t* n_batches, const int32_t* rows,
+                  const int64_t* addrs, const int64_t* sizes, const int32_t* n_bufs, int* failed) {
+  // every task's batches are gathered and its host reads started before any task waits, so the
+  // tasks' reads are in flight together
+  std::vector<Status> st(tasks.size());
+  size_t r = 0, a = 0;
+  for (size_t i = 0; i < tasks.size(); i++) {
+    st[i] = tasks[i]->SplitMany(n_batches[i], rows + r, addrs + a, sizes + a, n_bufs[i]);
+    if (st[i].ok()) st[i] = tasks[i]->StartHostReads();
+    r += (size_t)n_batches[i];
+    a += (size_t)n_batches[i] * (size_t)n_bufs[i];
+  }
+  for (size_t i = 0; i < tasks.size(); i++) {
+    Status w = tasks[i]->WaitHostReads();
+    if (st[i].ok()) st[i] = w;
+  }
+  for (size_t i = 0; i < tasks.size(); i++)
+    if (!st[i].ok()) {
+      *failed = (int)i;
+      return st[i];
+    }
   return Status::OK();
 }
 

@@ -53,6 +53,12 @@ class Splitter {
   // read when it returns (also on error).
   Status SplitBatches(int32_t n_batches, const int32_t* rows, const int64_t* addrs,
                       const int64_t* sizes, int32_t n);
+  // SplitBatches without waiting for the host reads: the caller calls StartHostReads and then
+  // WaitHostReads before it releases the buffers (SplitGroup below).
+  Status SplitMany(int32_t n_batches, const int32_t* rows, const int64_t* addrs, const int64_t* sizes,
+                   int32_t n);
+  Status StartHostReads();
+  Status WaitHostReads();
   Status CompressedSize(int32_t num_rows, const int64_t* addrs, const int64_t* sizes, int32_t n,
                         int64_t* out);
   Status Stop();
@@ -149,6 +155,7 @@ class Splitter {
   Status SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t* sizes, int32_t n);
   Status LaunchGather();
   Status FinishHostReads();
+  bool reads_marked_ = false;  // gather_ev_ marks host reads not yet waited for
   Status PinnedMeta(size_t bytes, uint32_t** out);
   Status Flush();
   Status SyncAndCheck();
@@ -293,5 +300,11 @@ class Splitter {
   std::vector<int64_t> partition_lengths_, raw_partition_lengths_;
   std::vector<uint8_t> data_bytes_;
 };
+
+// Split calls of several tasks at once (task i: n_batches[i] batches of n_bufs[i] buffers, its
+// rows / addresses / sizes following the previous task's): every task's host reads are started
+// before any is waited for.  *failed: the first task whose call failed.
+Status SplitGroup(const std::vector<Splitter*>& tasks, const int32_t* n_batches, const int32_t* rows,
+                  const int64_t* addrs, const int64_t* sizes, const int32_t* n_bufs, int* failed);
 
 }  // namespace gz

@@ -106,6 +106,9 @@ def lib() -> ctypes.CDLL:
         L.gz_split_split_batches.restype = ctypes.c_int
         L.gz_split_split_batches.argtypes = [ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p,
                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]
+        L.gz_split_split_group.restype = ctypes.c_int
+        L.gz_split_split_group.argtypes = [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         L.gz_split_sync.restype = ctypes.c_int
         L.gz_split_sync.argtypes = [ctypes.c_int64]
         L.gz_split_stop.restype = ctypes.c_int
@@ -462,6 +465,20 @@ class ShuffleSplitterJniWrapper:
         _check(lib().gz_split_split_batches(splitterId, len(rows), rows.ctypes.data,
                                             addrs.ctypes.data, sizes.ctypes.data, addrs.shape[1]),
                splitterId)
+
+    def splitGroup(self, splitterIds, rows, bufAddrs, bufSizes) -> None:
+        """Split calls of several tasks at once: task i gets rows[i] (array of row counts) with
+        bufAddrs[i] / bufSizes[i] (arrays [batches, buffers]); every task's host reads are in
+        flight together."""
+        h = np.ascontiguousarray(splitterIds, dtype=np.int64)
+        nb = np.array([len(r) for r in rows], np.int32)
+        nbuf = np.array([np.asarray(a).shape[1] if len(r) else 0 for r, a in zip(rows, bufAddrs)], np.int32)
+        r = np.ascontiguousarray(np.concatenate([np.asarray(x, np.int32) for x in rows]) if len(rows) else
+                                 np.zeros(0, np.int32))
+        a = np.ascontiguousarray(np.concatenate([np.asarray(x, np.int64).reshape(-1) for x in bufAddrs]))
+        z = np.ascontiguousarray(np.concatenate([np.asarray(x, np.int64).reshape(-1) for x in bufSizes]))
+        _check(lib().gz_split_split_group(len(h), h.ctypes.data, nb.ctypes.data, r.ctypes.data, a.ctypes.data,
+                                          z.ctypes.data, nbuf.ctypes.data))
 
     def sync(self, splitterId: int) -> None:
         _check(lib().gz_split_sync(splitterId), splitterId)

@@ -160,6 +160,16 @@ GzStatus gz_split_split(int64_t handle, int32_t num_rows, const int64_t* buf_add
 GzStatus gz_split_split_batches(int64_t handle, int32_t n_batches, const int32_t* rows,
                                 const int64_t* buf_addrs, const int64_t* buf_sizes, int32_t n_bufs);
 
+/* gz_split_split_batches for several tasks (different splitters, schemas and partition counts)
+ * in one call: task i (handles[i]) gets n_batches[i] batches of n_bufs[i] buffers; the rows,
+ * addresses and sizes of the tasks follow one another in `rows`, `buf_addrs`, `buf_sizes`.  All
+ * tasks' host reads are started before any is waited for, so they are in flight together; host
+ * inputs are read when the call returns.  Errors: gz_last_error(0, ...) names the failing task.
+ * No reference counterpart (the batched form's window of calls). */
+GzStatus gz_split_split_group(int32_t n_tasks, const int64_t* handles, const int32_t* n_batches,
+                              const int32_t* rows, const int64_t* buf_addrs, const int64_t* buf_sizes,
+                              const int32_t* n_bufs);
+
 /* Runs the device pass over the batches gathered so far and waits for all device work of
  * this handle: afterwards every split batch is in its partition buffers, as after a
  * reference Split call returns.  No reference counterpart (reference Split is synchronous). */

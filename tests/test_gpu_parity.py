@@ -404,3 +404,24 @@ def test_utf8_hash_keys_vs_oracle(seed):
         assert np.array_equal(w.lastPids(h, b.num_rows), o.last_pids(b.num_rows))
     w.close(h)
     o.close()
+
+
+@pytest.mark.gpu
+def test_split_group_of_tasks_equals_per_task_calls():
+    """gz_split_split_group: batches of three tasks (three schemas, three partition counts) in one
+    call per window give each task the bytes of splitting its own batches one by one (oracle)."""
+    rng = np.random.default_rng(5)
+    specs = [(W.C1_SCHEMA, W.C1_KEYS, 8), (W.C2_SCHEMA, W.C2_KEYS, 200), (W.C4_SCHEMA_3, W.C4_KEYS_3, 64)]
+    batches = [[W.c4_batch(rng, si, int(rng.integers(500, 9000))) for _ in range(7)] for si in range(3)]
+    w = S.ShuffleSplitterJniWrapper()
+    hs = [w.make(S.NativePartitioning("hash", P, None, keys, list(sch)), writeSchema=False, flush_bytes=1 << 20)
+          for sch, keys, P in specs]
+    for lo in range(0, 7, 3):
+        win = [b[lo:lo + 3] for b in batches]
+        w.splitGroup(hs, [[b.num_rows for b in x] for x in win],
+                     [np.stack([b.addrs_sizes()[0] for b in x]) for x in win],
+                     [np.stack([b.addrs_sizes()[1] for b in x]) for x in win])
+    for (sch, keys, P), h, bs in zip(specs, hs, batches):
+        w.stop(h, P)
+        assert w.data(h) == O.run_oracle(sch, bs, P, keys).data
+        w.close(h)
