@@ -84,6 +84,7 @@ __device__ uint32_t compress_block(const uint8_t* src, uint32_t n, uint16_t* tab
   const uint32_t* base = reinterpret_cast<const uint32_t*>(reinterpret_cast<uintptr_t>(src) & ~uintptr_t(3));
   const uint32_t sh0 = (uint32_t)(reinterpret_cast<uintptr_t>(src) & 3);
   uint32_t o = 0, anchor = 0, p = 0;
+  uint32_t misses = 0;  // windows in a row without a match
   if (n >= 13) {
     for (uint32_t i = lane; i < (1u << kHashLog); i += 32) table[i] = kEmpty;
     __syncwarp();
@@ -102,9 +103,14 @@ __device__ uint32_t compress_block(const uint8_t* src, uint32_t n, uint16_t* tab
       if (m == 0) {
         if (valid) table[h] = (uint16_t)q;
         __syncwarp();
-        p += 32;
+        // acceleration (as LZ4's fast mode): the longer no match turns up, the further the next
+        // window jumps, the positions in between staying literals; incompressible data costs a
+        // fraction of a full scan
+        misses++;
+        p += 32u << min(misses >> 3, 4u);
         continue;
       }
+      misses = 0;
       const uint32_t f = __ffs(m) - 1;
       if (valid && lane <= f) table[h] = (uint16_t)q;  // positions up to the match start only
       const uint32_t mq = p + f;
@@ -176,7 +182,14 @@ k_lz4_compress(const Lz4Chunk* __restrict__ chunks, uint32_t n_chunks, uint32_t*
           reinterpret_cast<uint32_t*>(d)[i] = __ldg(reinterpret_cast<const uint32_t*>(ch.src) + i);
         for (uint32_t i = (nv << 2) + lane_id(); i < n; i += 32) d[i] = __ldg(ch.src + i);
       } else {
-        for (uint32_t i = lane_id(); i < n; i += 32) d[i] = __ldg(ch.src + i);
+        // unaligned source: aligned destination words, each a funnel shift of two aligned source
+        // words (both hold bytes of the chunk), then the last bytes one by one
+        const uint32_t* base = reinterpret_cast<const uint32_t*>(a & ~uintptr_t(3));
+        const uint32_t sh = (uint32_t)(a & 3) * 8;
+        const uint32_t nv = n >> 2;
+        for (uint32_t i = lane_id(); i < nv; i += 32)
+          reinterpret_cast<uint32_t*>(d)[i] = __funnelshift_r(__ldg(base + i), __ldg(base + i + 1), sh);
+        for (uint32_t i = (nv << 2) + lane_id(); i < n; i += 32) d[i] = __ldg(ch.src + i);
       }
     } else {
       const uint32_t nv = size >> 4;

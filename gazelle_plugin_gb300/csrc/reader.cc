@@ -6,6 +6,8 @@
 #include <algorithm>
 
 #include "flatbuf.h"
+#include "gz_kernels.h"
+#include "host_util.h"
 #include "lz4_kernels.h"
 #include "read_kernels.h"
 
@@ -56,6 +58,10 @@ Status PartitionReader::Make(std::vector<Field> fields, int device, std::unique_
   if (!st.ok()) return st;
   st = r->Cuda(cudaStreamCreateWithFlags(&r->stream_, cudaStreamNonBlocking), "cudaStreamCreate");
   if (!st.ok()) return st;
+  int pageable = 0, host_tables = 0;
+  cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device);
+  cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device);
+  r->direct_ = pageable != 0 && host_tables != 0;
   r->out_.assign(r->fields_.size(), OutCol());
   *out = std::move(r);
   return Status::OK();
@@ -72,6 +78,7 @@ PartitionReader::~PartitionReader() {
     cudaStreamSynchronize(stream_);
     cudaStreamDestroy(stream_);
   }
+  PinnedRelease(PinnedBlock{reinterpret_cast<uint8_t*>(jobs_), jobs_bytes_});
 }
 
 // Walks the messages of one stream: an optional schema message, record batches, then the
@@ -213,8 +220,25 @@ Status PartitionReader::AddStream(const uint8_t* data, int64_t len) {
   if (!bs.empty()) {
     st = Cuda(cudaMallocAsync(reinterpret_cast<void**>(&d), AlignUp((size_t)len, 256), stream_), "cudaMallocAsync(stream)");
     if (!st.ok()) return st;
-    // the caller's bytes are read before the call returns
-    st = Cuda(cudaMemcpyAsync(d, data, (size_t)len, cudaMemcpyHostToDevice, stream_), "H2D stream");
+    // the caller's bytes are read before the call returns: by the device itself where it walks
+    // the host page tables (many CTAs reading 256 KiB pieces over the coherent link), else by a copy
+    if (direct_) {
+      const size_t piece = 256u << 10;
+      const size_t n = ((size_t)len + piece - 1) / piece;
+      if (jobs_cap_ < n) {
+        PinnedRelease(PinnedBlock{reinterpret_cast<uint8_t*>(jobs_), jobs_bytes_});
+        const PinnedBlock b = PinnedAcquire(sizeof(HostCopy) * n);
+        if (!b.ptr) return Status::Error(GZ_OOM, "pinned host memory for copy descriptors");
+        jobs_ = reinterpret_cast<HostCopy*>(b.ptr);
+        jobs_bytes_ = b.cap;
+        jobs_cap_ = b.cap / sizeof(HostCopy);
+      }
+      for (size_t i = 0; i < n; i++)
+        jobs_[i] = HostCopy{data + i * piece, d + i * piece, std::min<uint64_t>(piece, (uint64_t)len - i * piece)};
+      st = Cuda(launch_gather(jobs_, (uint32_t)n, stream_), "k_gather");
+    } else {
+      st = Cuda(cudaMemcpyAsync(d, data, (size_t)len, cudaMemcpyHostToDevice, stream_), "H2D stream");
+    }
     if (!st.ok()) return st;
   }
   images_.push_back(d);

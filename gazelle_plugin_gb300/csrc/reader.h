@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "../../include/gz_split.h"
+#include "gz_engine.cuh"
 #include "schema_ipc.h"
 #include "splitter.h"  // Status
 
@@ -77,6 +78,9 @@ class PartitionReader {
   std::vector<uint8_t*> images_;  // device copy of every stream
   std::vector<uint8_t*> arenas_;  // decoded compressed buffers of every stream
   std::vector<uint8_t*> arena_mem_;  // their allocations
+  bool direct_ = false;        // the device reads pageable host memory (coherent link)
+  HostCopy* jobs_ = nullptr;   // pinned descriptors of the device's reads of a stream
+  size_t jobs_bytes_ = 0, jobs_cap_ = 0;
   std::vector<Batch> batches_;
   std::vector<OutCol> out_;
   uint8_t* out_mem_ = nullptr;
