@@ -385,7 +385,7 @@ GzStatus gz_reader_column(int64_t handle, int32_t field, GzDeviceColumn* out) {
   return ReportReader(r.get(), r->reader->Column(field, out));
 }
 
-GzStatus gz_reader_column_to_host(int64_t handle, int32_t field, uint8_t* validity, int32_t* offsets,
+GzStatus gz_reader_column_to_host(int64_t handle, int32_t field, uint8_t* validity, void* offsets,
                                   uint8_t* values) {
   auto r = LookupReader(handle);
   if (!r) return GZ_INVALID;

@@ -54,13 +54,14 @@ struct SchemaDesc {
   int32_t key_kind[kMaxKeys];
   int32_t arr_col[kMaxCols];    // schema index of array column a
   int32_t arr_kind[kMaxCols];   // ColKind
-  int32_t arr_width[kMaxCols];  // value bytes of a fixed column
+  int32_t arr_width[kMaxCols];  // value bytes of a fixed column; offset bytes (4 / 8) of a binary one
   int32_t arr_str[kMaxCols];    // binary ordinal k of a binary column, -1 otherwise
   int32_t order[kMaxCols];      // order in which k_scatter processes the array columns
 };
 
-// Device addresses of one input column of one batch.  offsets only for binary columns;
-// validity == nullptr means an empty validity buffer (no nulls).
+// Device addresses of one input column of one batch.  offsets only for binary columns (int32,
+// or int64 for large binary columns: arr_width 8); validity == nullptr means an empty validity
+// buffer (no nulls).
 struct ColPtr {
   const uint8_t* validity;
   const int32_t* offsets;
@@ -154,7 +155,7 @@ struct FlushDesc {
   unsigned long long* ihn;  // [n_batches] input_has_null_ after the batch
 
   // outputs of this flush, indexed by array column
-  uint8_t* out_values[kMaxCols];   // fixed: n_rows * width; binary: n_rows int32 end offsets
+  uint8_t* out_values[kMaxCols];   // fixed: n_rows * width; binary: n_rows end offsets (arr_width bytes)
   uint32_t* out_bits[kMaxCols];    // bool values, same bit layout as validity
   uint32_t* out_valid[kMaxCols];   // validity words, 0xff-filled; nullptr: no nulls in flush
   uint8_t* out_chars[kMaxCols];    // binary bytes

@@ -251,9 +251,25 @@ __global__ void __launch_bounds__(kHashThreads) k_hash_count(const SchemaDesc sd
   }
   for (int k = 0; k < nstr; k++) {
     const ColPtr c = s_str[k];
-    // o[u] = offsets[r0 + min(u, m)]: row u < m spans o[u] .. o[u + 1]
-    int32_t o[kHashRows + 1];
-    if (whole && (reinterpret_cast<uintptr_t>(c.offsets) & 15) == 0) {
+    // o[u] = offsets[r0 + min(u, m)]: row u < m spans o[u] .. o[u + 1]; 64-bit offsets of
+    // large binary columns are read as such and checked like the 32-bit ones
+    int64_t o[kHashRows + 1];
+    const bool aligned = (reinterpret_cast<uintptr_t>(c.offsets) & 15) == 0;
+    if (sd.arr_width[sd.n_fixed + k] == 8) {
+      const int64_t* o64 = reinterpret_cast<const int64_t*>(c.offsets);
+      if (whole && aligned) {
+        const longlong2 a0 = reinterpret_cast<const longlong2*>(o64)[r0 >> 1];
+        const longlong2 a1 = reinterpret_cast<const longlong2*>(o64)[(r0 >> 1) + 1];
+        o[0] = a0.x;
+        o[1] = a0.y;
+        o[2] = a1.x;
+        o[3] = a1.y;
+        o[4] = o64[r0 + kHashRows];
+      } else {
+#pragma unroll
+        for (int u = 0; u <= kHashRows; u++) o[u] = o64[r0 + min((uint32_t)u, m)];
+      }
+    } else if (whole && aligned) {
       const int4 a0 = reinterpret_cast<const int4*>(c.offsets)[r0 >> 2];
       o[0] = a0.x;
       o[1] = a0.y;
@@ -278,7 +294,13 @@ __global__ void __launch_bounds__(kHashThreads) k_hash_count(const SchemaDesc sd
   if (threadIdx.x < nstr) {
     const ColPtr c = s_str[threadIdx.x];
     const size_t ct = ((size_t)tile.tile0 + t0 / kTileRows) * nstr + threadIdx.x;
-    fd.crange[ct] = make_int2(c.offsets[tile.row0 + t0], c.offsets[tile.row0 + t1]);
+    // (valid offsets of either width are below 2^31: a batch's characters are at most that)
+    if (sd.arr_width[sd.n_fixed + threadIdx.x] == 8) {
+      const int64_t* o64 = reinterpret_cast<const int64_t*>(c.offsets);
+      fd.crange[ct] = make_int2((int32_t)o64[tile.row0 + t0], (int32_t)o64[tile.row0 + t1]);
+    } else {
+      fd.crange[ct] = make_int2(c.offsets[tile.row0 + t0], c.offsets[tile.row0 + t1]);
+    }
   }
   }
   if (bad) atomicOr(fd.err, kErrBadOffsets);  // k_scatter then copies nothing
@@ -1060,9 +1082,9 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
         } else if (kind == COL_BOOL) {
           vsrc = c.values + (row0 >> 3);
           vbytes = (uint32_t)(n + 7) >> 3;
-        } else if (kind == COL_BINARY) {
-          vsrc = reinterpret_cast<const uint8_t*>(c.offsets + row0);
-          vbytes = (uint32_t)(n + 1) * 4;
+        } else if (kind == COL_BINARY) {  // offsets of 4 or 8 bytes (arr_width)
+          vsrc = reinterpret_cast<const uint8_t*>(c.offsets) + (size_t)row0 * sd.arr_width[a];
+          vbytes = (uint32_t)(n + 1) * sd.arr_width[a];
         }
         const uint8_t* bsrc = nullptr;
         uint32_t bbytes = 0;
@@ -1115,7 +1137,7 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
     const uint8_t* stg = slot_base;  // staged values / bits / offsets, at the source's phase
     if (kind == COL_FIXED && w <= 8) stg = staged_ptr(slot_base, c.values + (size_t)row0 * w);
     else if (kind == COL_BOOL) stg = staged_ptr(slot_base, c.values + (row0 >> 3));
-    else if (kind == COL_BINARY) stg = staged_ptr(slot_base, reinterpret_cast<const uint8_t*>(c.offsets + row0));
+    else if (kind == COL_BINARY) stg = staged_ptr(slot_base, reinterpret_cast<const uint8_t*>(c.offsets) + (size_t)row0 * w);
     const bool vwork = c.validity != nullptr && s_nc[a] != 0 && fd.out_valid[a] != nullptr;
     const uint32_t vb = vwork ? smem_addr(staged_ptr(slot_base + kStageBytes, c.validity + (row0 >> 3))) : 0u;
     s_ct[i] = make_uint4((uint32_t)(stg - ssm), vb,
@@ -1252,7 +1274,10 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
         // read only the slot (in bounds whether or not its copy arrived), and after the first
         // barrier the block's state, the same in every thread, decides whether the rest runs
         const ColPtr c = s_col[a];
-        const int32_t* oin = reinterpret_cast<const int32_t*>(stg);  // offsets of rows row0..row0+n
+        // offsets of rows row0..row0+n, 4 or 8 bytes each (valid ones are below 2^31 either way)
+        const bool off64 = ((ct.z >> 8) & 255u) == 8;
+        const int32_t* oin = reinterpret_cast<const int32_t*>(stg);
+        const int64_t* oin64 = reinterpret_cast<const int64_t*>(stg);
         // lengths of the owned positions; exclusive prefix over the tile = the lengths of all
         // earlier rows u' < u of positions + this row's prefix, one fused warp scan per row u
         uint32_t len[kRowsPerThread], pre[kRowsPerThread], so[kRowsPerThread];  // so: source offset
@@ -1263,8 +1288,13 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
           so[u] = 0;
           if (j < n) {
             const int r = ps[j];
-            so[u] = (uint32_t)oin[r];
-            len[u] = (uint32_t)oin[r + 1] - so[u];
+            if (off64) {
+              so[u] = (uint32_t)oin64[r];
+              len[u] = (uint32_t)oin64[r + 1] - so[u];
+            } else {
+              so[u] = (uint32_t)oin[r];
+              len[u] = (uint32_t)oin[r + 1] - so[u];
+            }
           }
           pre[u] = len[u];
         }
@@ -1331,9 +1361,15 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
               cd[u] = rt1[q] + pre[u];
             }
           }
+          if (off64) {
 #pragma unroll
-          for (int u = 0; u < kRowsPerThread; u++)
-            if (threadIdx.x + u * kConsumers < n) ooff[d[u]] = (int32_t)v[u];
+            for (int u = 0; u < kRowsPerThread; u++)
+              if (threadIdx.x + u * kConsumers < n) reinterpret_cast<int64_t*>(ooff)[d[u]] = (int64_t)v[u];
+          } else {
+#pragma unroll
+            for (int u = 0; u < kRowsPerThread; u++)
+              if (threadIdx.x + u * kConsumers < n) ooff[d[u]] = (int32_t)v[u];
+          }
         }
         const int k = (int)(ct.z >> 24);
         if (chars) {

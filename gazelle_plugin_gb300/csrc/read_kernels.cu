@@ -2,7 +2,8 @@
 // IPC streams, already in HBM, concatenated into one set of Arrow columns.  Three job lists, each
 // job at most a few hundred KB so that one CTA per job keeps every SM busy:
 //   byte jobs   values of fixed-width columns and characters of binary columns, copied
-//   offset jobs binary offsets rebased: out[i] = in[i] - in[0] + (the batch's first character)
+//   offset jobs binary offsets (int32, or int64 of the large types) rebased:
+//               out[i] = in[i] - in[0] + (the batch's first character)
 //   bit jobs    validity / bool bits moved to their row in the output (OR into zeroed words;
 //               a batch without a validity buffer contributes ones)
 #include <cuda_runtime.h>
@@ -44,7 +45,16 @@ __global__ void __launch_bounds__(kThreads) k_read_bytes(const ByteJob* __restri
 __global__ void __launch_bounds__(kThreads) k_read_offsets(const OffsetJob* __restrict__ jobs, uint32_t n_jobs) {
   for (uint32_t b = blockIdx.x; b < n_jobs; b += gridDim.x) {
     const OffsetJob job = jobs[b];
-    for (uint32_t i = threadIdx.x; i < job.n; i += kThreads) job.dst[i] = job.src[i] + job.add;
+    if (job.wide) {
+      const int64_t* src = static_cast<const int64_t*>(job.src);
+      int64_t* dst = static_cast<int64_t*>(job.dst);
+      for (uint32_t i = threadIdx.x; i < job.n; i += kThreads) dst[i] = src[i] + job.add;
+    } else {
+      const int32_t* src = static_cast<const int32_t*>(job.src);
+      int32_t* dst = static_cast<int32_t*>(job.dst);
+      const int32_t add = (int32_t)job.add;
+      for (uint32_t i = threadIdx.x; i < job.n; i += kThreads) dst[i] = src[i] + add;
+    }
   }
 }
 

@@ -11,11 +11,12 @@ struct ByteJob {  // bytes [src, src + bytes) to dst
   uint64_t bytes;
 };
 
-struct OffsetJob {  // dst[i] = src[i] + add, i < n
-  const int32_t* src;
-  int32_t* dst;
+struct OffsetJob {  // dst[i] = src[i] + add, i < n; int32 offsets, or int64 when wide
+  const void* src;
+  void* dst;
   uint32_t n;
-  int32_t add;
+  uint32_t wide;
+  int64_t add;
 };
 
 struct BitJob {  // bits [src_bit, src_bit + nbits) of src (all ones when src is null) ORed into dst at dst_bit

@@ -18,7 +18,20 @@ namespace {
 inline int64_t Pad8(int64_t n) { return (n + 7) & ~int64_t(7); }
 inline size_t AlignUp(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
-bool IsBinaryType(int t) { return t == GZ_TYPE_STRING || t == GZ_TYPE_BINARY; }
+bool IsLargeBinaryType(int t) { return t == GZ_TYPE_LARGE_STRING || t == GZ_TYPE_LARGE_BINARY; }
+bool IsBinaryType(int t) { return t == GZ_TYPE_STRING || t == GZ_TYPE_BINARY || IsLargeBinaryType(t); }
+int OffsetWidth(int t) { return IsLargeBinaryType(t) ? 8 : 4; }
+// Offset r of a little-endian offsets buffer of width w
+int64_t ReadOffset(const uint8_t* p, int w, int64_t r) {
+  if (w == 8) {
+    int64_t v;
+    memcpy(&v, p + 8 * r, 8);
+    return v;
+  }
+  int32_t v;
+  memcpy(&v, p + 4 * r, 4);
+  return v;
+}
 
 int FixedWidth(int t) {
   switch (t) {
@@ -186,10 +199,11 @@ Status PartitionReader::ParseStream(const uint8_t* data, int64_t len, int stream
                              : IsBinaryType(t) ? 0 : b.rows * FixedWidth(t);
         if (c.values.length < need) return Status::Error(GZ_INVALID, "value buffer too short");
         if (IsBinaryType(t)) {
-          if (c.offsets.length < (b.rows + 1) * 4) return Status::Error(GZ_INVALID, "offsets buffer too short");
+          const int ow = OffsetWidth(t);
+          if (c.offsets.length < (b.rows + 1) * ow) return Status::Error(GZ_INVALID, "offsets buffer too short");
           if (!c.offsets.decoded) {  // decoded offsets are read after decoding
-            memcpy(&c.o0, data + c.offsets.offset, 4);
-            memcpy(&c.o1, data + c.offsets.offset + 4 * b.rows, 4);
+            c.o0 = ReadOffset(data + c.offsets.offset, ow, 0);
+            c.o1 = ReadOffset(data + c.offsets.offset, ow, b.rows);
             if (c.o0 < 0 || c.o1 < c.o0 || c.o1 > c.values.length)
               return Status::Error(GZ_INVALID, "offsets exceed the characters");
           }
@@ -264,7 +278,8 @@ Status PartitionReader::AddStream(const uint8_t* data, int64_t len) {
     if (st.ok()) st = Cuda(launch_lz4_decode(reinterpret_cast<const Lz4Frame*>(arena), (uint32_t)jobs.size(), d_err, stream_),
                            "k_lz4_decode");
     if (st.ok()) st = Cuda(cudaMemcpyAsync(&err, d_err, 4, cudaMemcpyDeviceToHost, stream_), "D2H");
-    // the decoded offsets bound each batch's characters
+    // the decoded offsets bound each batch's characters: for each, the 4-byte words of its first
+    // and last offset (low word, then high word of a 64-bit one)
     std::vector<const int32_t*> where;
     std::vector<std::pair<size_t, size_t>> which;  // (batch, field)
     for (size_t bi = 0; bi < bs.size(); bi++)
@@ -272,8 +287,15 @@ Status PartitionReader::AddStream(const uint8_t* data, int64_t len) {
         const ColRef& c = bs[bi].cols[f];
         if (!IsBinaryType(fields_[f].type) || !c.offsets.decoded) continue;
         const int32_t* o = reinterpret_cast<const int32_t*>(arenas_.back() + c.offsets.offset);
-        where.push_back(o);
-        where.push_back(o + bs[bi].rows);
+        if (IsLargeBinaryType(fields_[f].type)) {
+          where.push_back(o);
+          where.push_back(o + 1);
+          where.push_back(o + 2 * bs[bi].rows);
+          where.push_back(o + 2 * bs[bi].rows + 1);
+        } else {
+          where.push_back(o);
+          where.push_back(o + bs[bi].rows);
+        }
         which.push_back({bi, f});
       }
     std::vector<int32_t> ends(where.size());
@@ -281,10 +303,18 @@ Status PartitionReader::AddStream(const uint8_t* data, int64_t len) {
     if (st.ok()) st = Cuda(cudaStreamSynchronize(stream_), "k_lz4_decode");
     if (!st.ok()) return st;
     if (err) return Status::Error(GZ_INVALID, "a compressed buffer is not a valid LZ4 frame of its stated length");
+    size_t e = 0;
     for (size_t i = 0; i < which.size(); i++) {
       ColRef& c = bs[which[i].first].cols[which[i].second];
-      c.o0 = ends[2 * i];
-      c.o1 = ends[2 * i + 1];
+      if (IsLargeBinaryType(fields_[which[i].second].type)) {
+        c.o0 = (int64_t)((uint64_t)(uint32_t)ends[e] | (uint64_t)(uint32_t)ends[e + 1] << 32);
+        c.o1 = (int64_t)((uint64_t)(uint32_t)ends[e + 2] | (uint64_t)(uint32_t)ends[e + 3] << 32);
+        e += 4;
+      } else {
+        c.o0 = ends[e];
+        c.o1 = ends[e + 1];
+        e += 2;
+      }
       if (c.o0 < 0 || c.o1 < c.o0 || c.o1 > c.values.length) return Status::Error(GZ_INVALID, "offsets exceed the characters");
     }
     arena_mem_.push_back(arena);
@@ -321,14 +351,15 @@ Status PartitionReader::Finish(int64_t* rows, int32_t* n_batches) {
       oc.null_count += b.cols[f].null_count;
       if (IsBinaryType(t)) chars[f] += b.cols[f].o1 - b.cols[f].o0;
     }
-    if (chars[f] >= (1ll << 31)) return Status::Error(GZ_INVALID, "more than 2^31 - 1 characters in one column");
+    if (chars[f] >= (1ll << 31) && !IsLargeBinaryType(t))
+      return Status::Error(GZ_INVALID, "more than 2^31 - 1 characters in one column");
     if (oc.null_count > 0) {
       o_valid[f] = total;
       total += bit_bytes;
     }
     if (IsBinaryType(t)) {
       o_off[f] = total;
-      total += AlignUp((size_t)(R + 1) * 4, 256);
+      total += AlignUp((size_t)(R + 1) * OffsetWidth(t), 256);
     }
     o_val[f] = total;
     total += t == GZ_TYPE_BOOL ? bit_bytes
@@ -372,12 +403,14 @@ Status PartitionReader::Finish(int64_t* rows, int32_t* n_batches) {
       } else if (IsBinaryType(t)) {
         // offsets rebased onto the characters of the earlier batches; the last batch also writes
         // the final offset
-        const int32_t* src_off = reinterpret_cast<const int32_t*>(Base(c.offsets, b.stream));
-        int32_t* dst_off = reinterpret_cast<int32_t*>(out_mem_ + o_off[f]) + row;
-        const int32_t add = (int32_t)(char_pos[f] - c.o0);
+        const int ow = OffsetWidth(t);
+        const uint8_t* src_off = Base(c.offsets, b.stream);
+        uint8_t* dst_off = out_mem_ + o_off[f] + (size_t)row * ow;
+        const int64_t add = char_pos[f] - c.o0;
         const uint64_t n = (uint64_t)b.rows + (last ? 1 : 0);
         for (uint64_t x = 0; x < n; x += kChunk / 4)
-          oj.push_back(OffsetJob{src_off + x, dst_off + x, (uint32_t)std::min<uint64_t>(kChunk / 4, n - x), add});
+          oj.push_back(OffsetJob{src_off + x * ow, dst_off + x * ow, (uint32_t)std::min<uint64_t>(kChunk / 4, n - x),
+                                 ow == 8 ? 1u : 0u, add});
         add_bytes(Base(c.values, b.stream) + c.o0, out_mem_ + o_val[f] + char_pos[f], (uint64_t)(c.o1 - c.o0));
         char_pos[f] += c.o1 - c.o0;
       } else {
@@ -420,7 +453,7 @@ Status PartitionReader::Finish(int64_t* rows, int32_t* n_batches) {
     const int t = fields_[f].type;
     if (t == GZ_TYPE_NULL) continue;
     if (o_valid[f] != SIZE_MAX) oc.validity = out_mem_ + o_valid[f];
-    if (o_off[f] != SIZE_MAX) oc.offsets = reinterpret_cast<int32_t*>(out_mem_ + o_off[f]);
+    if (o_off[f] != SIZE_MAX) oc.offsets = out_mem_ + o_off[f];
     oc.values = out_mem_ + o_val[f];
     oc.values_bytes = t == GZ_TYPE_BOOL ? (R + 7) / 8 : IsBinaryType(t) ? chars[f] : R * FixedWidth(t);
   }
@@ -446,7 +479,7 @@ Status PartitionReader::Column(int field, GzDeviceColumn* out) const {
   return Status::OK();
 }
 
-Status PartitionReader::ColumnToHost(int field, uint8_t* validity, int32_t* offsets, uint8_t* values) {
+Status PartitionReader::ColumnToHost(int field, uint8_t* validity, void* offsets, uint8_t* values) {
   GzDeviceColumn c;
   Status st = Column(field, &c);
   if (!st.ok()) return st;
@@ -457,7 +490,8 @@ Status PartitionReader::ColumnToHost(int field, uint8_t* validity, int32_t* offs
     if (!st.ok()) return st;
   }
   if (offsets && c.offsets) {
-    st = Cuda(cudaMemcpyAsync(offsets, c.offsets, (size_t)(c.length + 1) * 4, cudaMemcpyDeviceToHost, stream_), "D2H");
+    st = Cuda(cudaMemcpyAsync(offsets, c.offsets, (size_t)(c.length + 1) * OffsetWidth(c.type), cudaMemcpyDeviceToHost,
+                              stream_), "D2H");
     if (!st.ok()) return st;
   }
   if (values && c.values && c.values_bytes > 0) {

@@ -35,7 +35,7 @@ class PartitionReader {
   // Concatenates every batch added so far into device columns; waits for the device.
   Status Finish(int64_t* rows, int32_t* batches);
   Status Column(int field, GzDeviceColumn* out) const;
-  Status ColumnToHost(int field, uint8_t* validity, int32_t* offsets, uint8_t* values);
+  Status ColumnToHost(int field, uint8_t* validity, void* offsets, uint8_t* values);
 
  private:
   struct BufRef {
@@ -49,7 +49,7 @@ class PartitionReader {
   struct ColRef {
     int64_t null_count = 0;
     BufRef validity, offsets, values;
-    int32_t o0 = 0, o1 = 0;  // binary: first and last offset (the batch's characters)
+    int64_t o0 = 0, o1 = 0;  // binary: first and last offset (the batch's characters)
   };
   struct Batch {
     int stream = 0;
@@ -59,7 +59,7 @@ class PartitionReader {
   struct OutCol {
     int64_t null_count = 0;
     uint8_t* validity = nullptr;
-    int32_t* offsets = nullptr;
+    uint8_t* offsets = nullptr;  // int32 or int64 (large types) offsets
     uint8_t* values = nullptr;
     int64_t values_bytes = 0;
   };

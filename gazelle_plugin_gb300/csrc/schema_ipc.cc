@@ -82,6 +82,8 @@ bool ParseSchemaIpc(const uint8_t* data, int64_t len, std::vector<Field>* out, s
       }
       case 4: f.type = GZ_TYPE_BINARY; break;
       case 5: f.type = GZ_TYPE_STRING; break;
+      case 19: f.type = GZ_TYPE_LARGE_BINARY; break;
+      case 20: f.type = GZ_TYPE_LARGE_STRING; break;
       case 6: f.type = GZ_TYPE_BOOL; break;
       case 7: {
         int32_t bw = tp >= 0 ? r.Scalar<int32_t>(tp, 2, 128) : 128;
@@ -253,6 +255,8 @@ uint8_t TypeTable(Builder& b, const Field& f, uint32_t* table) {
     case GZ_TYPE_FLOAT64: *table = floating(2); return 3;
     case GZ_TYPE_BINARY: *table = empty(); return 4;
     case GZ_TYPE_STRING: *table = empty(); return 5;
+    case GZ_TYPE_LARGE_BINARY: *table = empty(); return 19;  // Schema.fbs Type.LargeBinary
+    case GZ_TYPE_LARGE_STRING: *table = empty(); return 20;  // Type.LargeUtf8
     case GZ_TYPE_DECIMAL128:  // Decimal { precision, scale, bitWidth = 128 }
       b.StartTable();
       b.AddScalar<int32_t>(8, 128, 128);

@@ -43,7 +43,23 @@ int ByteWidth(int t) {
     default: return 0;
   }
 }
-inline bool IsBinary(int t) { return t == GZ_TYPE_STRING || t == GZ_TYPE_BINARY; }
+inline bool IsBinary(int t) {
+  return t == GZ_TYPE_STRING || t == GZ_TYPE_BINARY || t == GZ_TYPE_LARGE_STRING || t == GZ_TYPE_LARGE_BINARY;
+}
+// Bytes of one offset of a binary column: int32, or int64 for LargeBinary / LargeString
+// (splitter.cc:480-516, 626-629, 1291-1299)
+inline int OffW(int t) { return t == GZ_TYPE_LARGE_STRING || t == GZ_TYPE_LARGE_BINARY ? 8 : 4; }
+// Offset r of an offsets buffer of width w, as int64
+inline int64_t OffAt(const uint8_t* off, int w, size_t r) {
+  if (w == 8) {
+    int64_t v;
+    memcpy(&v, off + r * 8, 8);
+    return v;
+  }
+  int32_t v;
+  memcpy(&v, off + r * 4, 4);
+  return v;
+}
 
 // Copies `nbits` bits from src (starting at bit `sbit`) to dst (starting at bit `dbit`);
 // dst bits outside the range are left as they are.
@@ -171,7 +187,7 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
     const int t = fields_[ci].type;
     sd_.arr_col[a] = ci;
     sd_.arr_kind[a] = IsBinary(t) ? COL_BINARY : t == GZ_TYPE_BOOL ? COL_BOOL : COL_FIXED;
-    sd_.arr_width[a] = ByteWidth(t);
+    sd_.arr_width[a] = IsBinary(t) ? OffW(t) : ByteWidth(t);  // binary: offset bytes
     sd_.arr_str[a] = a >= fixed_cnt_ ? a - fixed_cnt_ : -1;
     // compared as an index of the output schema (the range partitioner's ids are not in it)
     if (ci - out_shift() < fixed_cnt_) sd_.quirk_mask |= 1ull << a;
@@ -347,11 +363,14 @@ Splitter::~Splitter() {
 
 // CalculateSplitBatchSize (splitter.cc:800-853).  `host_offsets` (may hold nullptr) are the
 // batch's offset buffers per binary column, readable on the host.
-uint32_t Splitter::SplitBatchSize(int32_t num_rows, const std::vector<const int32_t*>& host_offsets,
+uint32_t Splitter::SplitBatchSize(int32_t num_rows, const std::vector<const uint8_t*>& host_offsets,
                                   bool* complete) {
   for (int k = 0; k < n_str_; k++) {
     if (empirical_[k] == 0 && host_offsets[k] != nullptr && num_rows > 0) {
-      const uint64_t len = (uint64_t)(uint32_t)(host_offsets[k][num_rows] - host_offsets[k][0]);
+      // the character bytes of the batch: int32 offsets subtract as int32, int64 as int64
+      const int w = sd_.arr_width[fixed_cnt_ + k];
+      const int64_t d = OffAt(host_offsets[k], w, (size_t)num_rows) - OffAt(host_offsets[k], w, 0);
+      const uint64_t len = w == 8 ? (uint64_t)d : (uint64_t)(uint32_t)(int32_t)d;
       empirical_[k] = len % num_rows == 0 ? len / num_rows : len / num_rows + 1;
     }
   }
@@ -530,19 +549,25 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
     if (IsBinary(t)) {
       const int vi = b0 + 2;
       need_[vi] = Need{nullptr, 0};
-      const size_t ob = (size_t)(nr + 1) * 4;
+      const int ow = OffW(t);
+      const size_t ob = (size_t)(nr + 1) * ow;
       if (addrs[b0 + 1] == 0 || (size_t)sizes[b0 + 1] < ob)
         return Status::Error(GZ_INVALID, "offsets buffer too small");
       need_[b0 + 1] = Need{reinterpret_cast<const uint8_t*>(addrs[b0 + 1]), ob};
       const int k = a - fixed_cnt_;
       size_t cb = (size_t)std::max<int64_t>(sizes[vi], 0);
+      // the device engine keeps byte positions in 32 bits: a 64-bit-offset column's batch may
+      // not address more characters than a 32-bit one can
+      if (ow == 8 && sizes[vi] > (int64_t)INT32_MAX)
+        return Status::Error(GZ_NOT_IMPLEMENTED, "a large binary column batch with more than 2^31 - 1 character bytes");
       if (host_in) {
-        const int32_t* off = reinterpret_cast<const int32_t*>(addrs[b0 + 1]);
+        const uint8_t* off = reinterpret_cast<const uint8_t*>(addrs[b0 + 1]);
         host_off_[k] = off;
-        if (off[nr] < off[0] || off[0] < 0 || (int64_t)off[nr] > sizes[vi])
+        const int64_t o0 = OffAt(off, ow, 0), o1 = OffAt(off, ow, nr);
+        if (o1 < o0 || o0 < 0 || o1 > sizes[vi])
           return Status::Error(GZ_INVALID, "offsets exceed the value buffer");
-        cb = (size_t)off[nr];
-        char_scratch_[k] = (uint64_t)(off[nr] - off[0]);
+        cb = (size_t)o1;
+        char_scratch_[k] = (uint64_t)(o1 - o0);
       } else {
         char_scratch_[k] = (uint64_t)cb;
       }
@@ -572,11 +597,13 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
       if (!st.ok()) return st;
       for (int k = 0; k < n_str_; k++) {
         const int f = array_idx_[fixed_cnt_ + k];
-        const int32_t* doff = reinterpret_cast<const int32_t*>(addrs[field_buf0_[f] + 1]);
-        dev_off_[k].assign(nr + 1, 0);
-        st = Cuda(cudaMemcpy(&dev_off_[k][0], doff, 4, cudaMemcpyDeviceToHost), "read offsets");
+        const int ow = sd_.arr_width[fixed_cnt_ + k];
+        const uint8_t* doff = reinterpret_cast<const uint8_t*>(addrs[field_buf0_[f] + 1]);
+        dev_off_[k].assign((size_t)(nr + 1) * ow, 0);
+        st = Cuda(cudaMemcpy(&dev_off_[k][0], doff, ow, cudaMemcpyDeviceToHost), "read offsets");
         if (!st.ok()) return st;
-        st = Cuda(cudaMemcpy(&dev_off_[k][nr], doff + nr, 4, cudaMemcpyDeviceToHost), "read offsets");
+        st = Cuda(cudaMemcpy(&dev_off_[k][(size_t)nr * ow], doff + (size_t)nr * ow, ow, cudaMemcpyDeviceToHost),
+                  "read offsets");
         if (!st.ok()) return st;
         host_off_[k] = dev_off_[k].data();
       }
@@ -646,7 +673,7 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
           if (direct_) {
             // same 16-byte phase as the source when that keeps the elements aligned
             const uintptr_t sp = reinterpret_cast<uintptr_t>(nd.src);
-            const uintptr_t elem = j == 0 ? 1 : IsBinary(t) ? (j == 1 ? 4 : 1)
+            const uintptr_t elem = j == 0 ? 1 : IsBinary(t) ? (j == 1 ? (uintptr_t)OffW(t) : 1)
                                  : t == GZ_TYPE_BOOL ? 1 : (uintptr_t)ByteWidth(t);
             if (sp % elem == 0) phase = sp & 15;
             h_jobs_[jobs_end_++] = HostCopy{nd.src, d_stage_[cur_] + used_ + phase, nd.bytes};
@@ -689,8 +716,8 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
           cp.offsets = reinterpret_cast<const int32_t*>(addrs[b0 + 1]);
           cp.values = reinterpret_cast<const uint8_t*>(addrs[b0 + 2]);
           cp.values_bytes = (uint64_t)std::max<int64_t>(sizes[b0 + 2], 0);
-          if (reinterpret_cast<uintptr_t>(cp.offsets) % 4)
-            return Status::Error(GZ_INVALID, "device offsets buffer must be 4-byte aligned");
+          if (reinterpret_cast<uintptr_t>(cp.offsets) % (uintptr_t)OffW(t))
+            return Status::Error(GZ_INVALID, "device offsets buffer must be aligned to its offset width");
         } else {
           cp.values = need_[b0 + 1].src;
           const int w = t == GZ_TYPE_BOOL ? 1 : ByteWidth(t);
@@ -822,7 +849,7 @@ Status Splitter::Flush() {
       o += AlignUp((size_t)R * sd_.arr_width[a], 256);
     } else if (kind == COL_BINARY) {
       fr.off_values[a] = o;
-      o += AlignUp((size_t)R * 4, 256);
+      o += AlignUp((size_t)R * sd_.arr_width[a], 256);  // end offsets, 4 or 8 bytes
       uint64_t cb = 0;
       for (uint32_t b = 0; b < NB; b++) cb += pending_chars_[(size_t)b * n_str_ + sd_.arr_str[a]];
       fr.off_chars[a] = o;
@@ -1240,7 +1267,7 @@ Status Splitter::BuildSegment(int p, const Segment& s, SegMsg* msg, bool device_
   std::vector<std::vector<uint8_t>>& temps = msg->temps;
   temps.clear();
   temps.reserve(2 * fields_.size());
-  static const uint8_t kZero4[4] = {0, 0, 0, 0};
+  static const uint8_t kZero8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   int64_t rawb = 0;
 
   // bits of a per-flush bit region (validity or bool values) for this segment
@@ -1328,21 +1355,22 @@ Status Splitter::BuildSegment(int p, const Segment& s, SegMsg* msg, bool device_
     } else {
       const int k = sd_.arr_str[a];
       ChunkedBuffer offs, chars;
-      offs.push_back(Chunk{kZero4, 4});
+      const int ow = sd_.arr_width[a];  // offset bytes
+      offs.push_back(Chunk{kZero8, ow});
       int64_t clen = 0;
       for (const Piece& pc : s.pieces) {
         const FlushRec& f = flushes_[pc.flush];
         bool dev;
         const uint8_t* fb = body_base(f, &dev);
         const uint8_t* ob = fb + f.off_values[a];
-        offs.push_back(Chunk{ob + ((size_t)f.pstart(P)[p] + pc.frow0) * 4, (int64_t)(pc.frow1 - pc.frow0) * 4, dev});
+        offs.push_back(Chunk{ob + ((size_t)f.pstart(P)[p] + pc.frow0) * ow, (int64_t)(pc.frow1 - pc.frow0) * ow, dev});
         const uint8_t* cb = fb + f.off_chars[a];
         const uint32_t c0 = pc.fb0[k], c1 = pc.fb1[k];
         if (c1 > c0)
           chars.push_back(Chunk{cb + (size_t)f.cstart(P, nstr)[(size_t)k * P + p] + c0, (int64_t)(c1 - c0), dev});
         clen += c1 - c0;
       }
-      rawb += (int64_t)(n + 1) * 4 + clen;
+      rawb += (int64_t)(n + 1) * ow + clen;
       bufs.push_back(offs);
       bufs.push_back(chars);
     }
@@ -1359,7 +1387,6 @@ Status Splitter::BuildSegment(int p, const Segment& s, SegMsg* msg, bool device_
     for (const Chunk& c : bufs[i]) lens[i] += c.len;
   RecordBatchHeader(n, nodes, lens, &msg->header, &msg->body);
   // the body: every buffer's chunks, then zeros up to its 8-byte boundary
-  static const uint8_t kZero8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   msg->pieces.clear();
   for (size_t i = 0; i < bufs.size(); i++) {
     for (const Chunk& c : bufs[i])
@@ -1811,9 +1838,10 @@ Status Splitter::CompressedSize(int32_t num_rows, const int64_t* addrs, const in
     const uint8_t* vb = reinterpret_cast<const uint8_t*>(addrs[b0]);
     bufs.push_back({vb, addrs[b0] != 0 && sizes[b0] > 0 && nr > 0 && CountZeros(vb, nr) > 0 ? BytesForBits(nr) : 0});
     if (IsBinary(t)) {
-      const int32_t* off = reinterpret_cast<const int32_t*>(addrs[b0 + 1]);
-      bufs.push_back({reinterpret_cast<const uint8_t*>(off), (int64_t)(nr + 1) * 4});
-      const int64_t c0 = nr > 0 && off ? off[0] : 0, c1 = nr > 0 && off ? off[nr] : 0;
+      const int ow = OffW(t);
+      const uint8_t* off = reinterpret_cast<const uint8_t*>(addrs[b0 + 1]);
+      bufs.push_back({off, (int64_t)(nr + 1) * ow});
+      const int64_t c0 = nr > 0 && off ? OffAt(off, ow, 0) : 0, c1 = nr > 0 && off ? OffAt(off, ow, nr) : 0;
       bufs.push_back({reinterpret_cast<const uint8_t*>(addrs[b0 + 2]) + c0, c1 - c0});
     } else {
       bufs.push_back({reinterpret_cast<const uint8_t*>(addrs[b0 + 1]),

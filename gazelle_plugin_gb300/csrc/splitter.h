@@ -181,7 +181,7 @@ class Splitter {
   // batches above batch_compress_threshold rows, plain copies for the others) into one arena,
   // which is then copied to pinned host memory; fills every message's header and pieces.
   Status CompressBodies(std::vector<std::vector<SegMsg>>* msgs);
-  uint32_t SplitBatchSize(int32_t num_rows, const std::vector<const int32_t*>& host_offsets,
+  uint32_t SplitBatchSize(int32_t num_rows, const std::vector<const uint8_t*>& host_offsets,
                           bool* complete);
 
   // schema
@@ -268,7 +268,7 @@ class Splitter {
   std::vector<PinnedBlock> meta_chunks_;
   std::vector<PinnedBlock> host_chunks_;  // pinned host partition data of moved passes
   size_t meta_chunk_cap_ = 0, meta_used_ = 0;
-  std::vector<std::vector<int32_t>> dev_off_;  // offset ends read from device inputs
+  std::vector<std::vector<uint8_t>> dev_off_;  // offset ends read from device inputs (offset-width bytes)
   bool seen_rows_ = false;
 
   std::vector<PendingBatch> pending_;
@@ -277,7 +277,7 @@ class Splitter {
   uint64_t pending_bytes_ = 0;
   size_t pending_tiles_ = 0;
   std::vector<Need> need_;                // per-call scratch
-  std::vector<const int32_t*> host_off_;
+  std::vector<const uint8_t*> host_off_;  // offsets of each binary column readable on the host
   std::vector<uint64_t> char_scratch_;
   std::vector<CopyJob> jobs_;
   size_t spilled_to_host_bytes_ = 0;

@@ -649,7 +649,7 @@ class PartitionReader:
         """(validity bytes or None, offsets or None, values bytes) of a concatenated column."""
         c = self.column(field)
         valid = np.zeros((c.length + 7) // 8, np.uint8) if c.validity else None
-        offs = np.zeros(c.length + 1, np.int32) if c.offsets else None
+        offs = np.zeros(c.length + 1, np.int64 if c.type in (21, 22) else np.int32) if c.offsets else None
         vals = np.zeros(c.values_bytes, np.uint8)
         _check(lib().gz_reader_column_to_host(self.h, field, valid.ctypes.data if valid is not None else None,
                                               offs.ctypes.data if offs is not None else None,

@@ -31,6 +31,7 @@ TYPE_CODES = {
     "float16": 6, "int32": 7, "uint32": 8, "float32": 9, "date32": 10, "time32": 11,
     "int64": 12, "uint64": 13, "float64": 14, "date64": 15, "time64": 16,
     "timestamp": 17, "decimal128": 18, "utf8": 19, "binary": 20,
+    "large_utf8": 21, "large_binary": 22,
 }
 BYTE_WIDTH = {
     "int8": 1, "uint8": 1, "int16": 2, "uint16": 2, "float16": 2, "int32": 4,
@@ -57,7 +58,12 @@ class Field:
 
     @property
     def is_binary(self) -> bool:
-        return self.type in ("utf8", "binary")
+        return self.type in ("utf8", "binary", "large_utf8", "large_binary")
+
+    @property
+    def offset_dtype(self):
+        """Offsets of a binary field: int32, int64 for the large types."""
+        return np.int64 if self.type.startswith("large_") else np.int32
 
     @property
     def params(self):
@@ -89,11 +95,11 @@ def pack_validity(valid: np.ndarray) -> np.ndarray:
     return np.packbits(valid.astype(np.uint8), bitorder="little")
 
 
-def _strings(rng, n, lo, hi, alphabet: bytes, valid):
+def _strings(rng, n, lo, hi, alphabet: bytes, valid, offset_dtype=np.int32):
     lens = rng.integers(lo, hi + 1, size=n).astype(np.int32)
     if valid is not None:
         lens = np.where(valid, lens, 0).astype(np.int32)
-    offsets = np.zeros(n + 1, np.int32)
+    offsets = np.zeros(n + 1, offset_dtype)
     np.cumsum(lens, out=offsets[1:])
     alpha = np.frombuffer(alphabet, np.uint8)
     chars = alpha[rng.integers(0, len(alpha), size=int(offsets[-1]))]
@@ -106,7 +112,7 @@ def _column(rng, field: Field, n: int, values: np.ndarray | None, null_frac: flo
     vbuf = pack_validity(valid)
     if field.is_binary:
         lo, hi, alphabet = str_spec
-        offsets, chars = _strings(rng, n, lo, hi, alphabet, valid)
+        offsets, chars = _strings(rng, n, lo, hi, alphabet, valid, field.offset_dtype)
         return [vbuf, offsets.view(np.uint8), chars]
     if field.type == "bool":
         bits = values.astype(bool)

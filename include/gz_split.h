@@ -38,7 +38,10 @@ typedef enum GzType {
   GZ_TYPE_UINT32 = 8, GZ_TYPE_FLOAT32 = 9, GZ_TYPE_DATE32 = 10, GZ_TYPE_TIME32 = 11,
   GZ_TYPE_INT64 = 12, GZ_TYPE_UINT64 = 13, GZ_TYPE_FLOAT64 = 14, GZ_TYPE_DATE64 = 15,
   GZ_TYPE_TIME64 = 16, GZ_TYPE_TIMESTAMP = 17, GZ_TYPE_DECIMAL128 = 18,
-  GZ_TYPE_STRING = 19, GZ_TYPE_BINARY = 20
+  GZ_TYPE_STRING = 19, GZ_TYPE_BINARY = 20,
+  /* 64-bit offsets (SplitBinaryType<LargeBinaryType::offset_type>, splitter.cc:1291-1299):
+   * payload columns only; one batch's column may hold at most 2^31 - 1 character bytes */
+  GZ_TYPE_LARGE_STRING = 21, GZ_TYPE_LARGE_BINARY = 22
 } GzType;
 
 /* One schema field.  `unit`: time/timestamp unit (0 s, 1 ms, 2 us, 3 ns); `precision` /
@@ -345,7 +348,8 @@ typedef struct GzDeviceColumn {
   int64_t length;          /* rows */
   int64_t null_count;
   const uint8_t* validity; /* LSB-first bitmap, (length + 7) / 8 bytes; NULL: no nulls */
-  const int32_t* offsets;  /* binary / utf8: length + 1 offsets from 0; NULL otherwise */
+  const void* offsets;     /* binary / utf8: length + 1 int32 offsets from 0 (int64 for the large
+                            * types); NULL otherwise */
   const uint8_t* values;   /* fixed width: length * width bytes; bool: bitmap; binary: characters */
   int64_t values_bytes;
 } GzDeviceColumn;
@@ -371,9 +375,9 @@ GzStatus gz_reader_finish(int64_t handle, int64_t* out_rows, int32_t* out_batche
 GzStatus gz_reader_column(int64_t handle, int32_t field, GzDeviceColumn* out);
 
 /* Copies the concatenated column of `field` to host memory: `validity` ((length + 7) / 8 bytes;
- * skipped when NULL or when the column has no nulls), `offsets` (length + 1 int32, binary only),
- * `values` (values_bytes bytes).  Waits for the copies. */
-GzStatus gz_reader_column_to_host(int64_t handle, int32_t field, uint8_t* validity, int32_t* offsets,
+ * skipped when NULL or when the column has no nulls), `offsets` (length + 1 offsets of the
+ * column's offset width, binary only), `values` (values_bytes bytes).  Waits for the copies. */
+GzStatus gz_reader_column_to_host(int64_t handle, int32_t field, uint8_t* validity, void* offsets,
                                   uint8_t* values);
 
 /* Frees the reader and its device columns. */

@@ -126,8 +126,8 @@ def _bits(buf: bytes, n: int) -> np.ndarray:
 
 def read_partition(schema, streams: Sequence[bytes]):
     """Concatenation of the record batches of `streams`, in order: (rows, per field (validity
-    bits as a bool array or None when the column has no nulls, int32 offsets or None, values as
-    bytes; bool values as a bool array))."""
+    bits as a bool array or None when the column has no nulls, offsets (int32, int64 for the
+    large types) or None, values as bytes; bool values as a bool array))."""
     batches = [b for s in streams for b in parse_stream(s, schema)]
     rows = sum(r for r, _ in batches)
     cols = []
@@ -144,11 +144,12 @@ def read_partition(schema, streams: Sequence[bytes]):
             vals = np.concatenate([_bits(c[fi][1][1], r) for r, c in batches]) if batches else np.zeros(0, bool)
             cols.append((valid, None, vals))
         elif f.is_binary:
-            offs, chars, base = [np.zeros(1, np.int32)], [], 0
+            odt = f.offset_dtype  # int32, int64 for the large types
+            offs, chars, base = [np.zeros(1, odt)], [], 0
             for r, c in batches:
-                o = np.frombuffer(c[fi][1][1], np.int32)[:r + 1]
+                o = np.frombuffer(c[fi][1][1], odt)[:r + 1]
                 chars.append(c[fi][1][2][o[0]:o[r]])
-                offs.append((o[1:] - o[0] + base).astype(np.int32))
+                offs.append((o[1:] - o[0] + base).astype(odt))
                 base += int(o[r] - o[0])
             cols.append((valid, np.concatenate(offs), b"".join(chars)))
         else:

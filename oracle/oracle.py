@@ -196,7 +196,8 @@ def to_pyarrow_schema(schema):
          "date32": pa.date32(), "time32": pa.time32("ms"), "int64": pa.int64(),
          "uint64": pa.uint64(), "float64": pa.float64(), "date64": pa.date64(),
          "time64": pa.time64("us"), "timestamp": pa.timestamp("us"),
-         "decimal128": pa.decimal128(30, 2), "utf8": pa.string(), "binary": pa.binary()}
+         "decimal128": pa.decimal128(30, 2), "utf8": pa.string(), "binary": pa.binary(),
+         "large_utf8": pa.large_string(), "large_binary": pa.large_binary()}
     units = ["s", "ms", "us", "ns"]
 
     def typ(f):

@@ -48,6 +48,7 @@ enum TypeCode {
   T_HALF_FLOAT = 6, T_INT32 = 7, T_UINT32 = 8, T_FLOAT32 = 9, T_DATE32 = 10,
   T_TIME32 = 11, T_INT64 = 12, T_UINT64 = 13, T_FLOAT64 = 14, T_DATE64 = 15,
   T_TIME64 = 16, T_TIMESTAMP = 17, T_DECIMAL128 = 18, T_STRING = 19, T_BINARY = 20,
+  T_LARGE_STRING = 21, T_LARGE_BINARY = 22,
 };
 
 int ByteWidth(int t) {
@@ -61,7 +62,13 @@ int ByteWidth(int t) {
     default: return 0;
   }
 }
-bool IsBinary(int t) { return t == T_STRING || t == T_BINARY; }
+bool IsBinary(int t) { return t == T_STRING || t == T_BINARY || t == T_LARGE_STRING || t == T_LARGE_BINARY; }
+// Bytes of one offset: int32 (BinaryType / StringType) or int64 (LargeBinaryType /
+// LargeStringType, SplitBinaryType<int64_t>, splitter.cc:1291-1299).
+int OffW(int t) { return t == T_LARGE_STRING || t == T_LARGE_BINARY ? 8 : 4; }
+int64_t OffAt(const uint8_t* off, int w, int64_t r) {
+  return w == 8 ? reinterpret_cast<const int64_t*>(off)[r] : (int64_t)reinterpret_cast<const int32_t*>(off)[r];
+}
 
 int64_t BytesForBits(int64_t n) { return (n + 7) / 8; }
 int64_t Pad8(int64_t n) { return (n + 7) & ~int64_t(7); }
@@ -243,7 +250,7 @@ struct PartBufs {
   bool has_validity = false;
   std::vector<uint8_t> validity;  // capacity bytes, 0xff filled
   std::vector<uint8_t> values;    // fixed: cap * width; bool: bitmap
-  std::vector<int32_t> offsets;   // binary: cap + 1
+  std::vector<int64_t> offsets;   // binary: cap + 1 (written out at the column's offset width)
   std::vector<uint8_t> chars;     // binary values (grows)
   int64_t chars_used = 0;
 };
@@ -499,8 +506,9 @@ class OracleSplitter {
       if (e == 0) {
         const InCol& c = cols[array_idx_[a]];
         if (c.offsets) {
-          const int32_t* off = (const int32_t*)c.offsets;
-          uint64_t len = (uint64_t)(uint32_t)(off[n] - off[0]);
+          const int w = OffW(fields_[array_idx_[a]].type);
+          const uint64_t len = w == 8 ? (uint64_t)(OffAt(c.offsets, 8, n) - OffAt(c.offsets, 8, 0))
+                                      : (uint64_t)(uint32_t)(int32_t)(OffAt(c.offsets, 4, n) - OffAt(c.offsets, 4, 0));
           e = len % n == 0 ? len / n : len / n + 1;
         }
       }
@@ -569,9 +577,20 @@ class OracleSplitter {
       body.push_back(nulls > 0 ? BodyBuf{b.validity.data(), BytesForBits(n)} : BodyBuf{nullptr, 0});
       if (IsBinary(t)) {
         int64_t vlen = b.offsets[n];
-        body.push_back({(const uint8_t*)b.offsets.data(), (int64_t)(n + 1) * 4});
+        const int w = OffW(t);
+        keep.emplace_back((size_t)(n + 1) * w);
+        uint8_t* ob = keep.back().data();
+        for (uint32_t i = 0; i <= n; i++) {
+          if (w == 8) {
+            memcpy(ob + (size_t)i * 8, &b.offsets[i], 8);
+          } else {
+            const int32_t o = (int32_t)b.offsets[i];
+            memcpy(ob + (size_t)i * 4, &o, 4);
+          }
+        }
+        body.push_back({ob, (int64_t)(n + 1) * w});
         body.push_back({b.chars.data(), vlen});
-        raw += (int64_t)(n + 1) * 4 + vlen;
+        raw += (int64_t)(n + 1) * w + vlen;
       } else {
         int64_t vlen = t == T_BOOL ? BytesForBits(n) : (int64_t)n * ByteWidth(t);
         body.push_back({b.values.data(), vlen});
@@ -679,13 +698,14 @@ class OracleSplitter {
         PartBufs& b = bufs_[a][p];
         if (c.null_count > 0 && !GetBit(c.validity, r)) ClearBit(b.validity.data(), d);
         if (IsBinary(t)) {
-          const int32_t* off = (const int32_t*)c.offsets;
-          int32_t len = off[r + 1] - off[r];
+          const int w = OffW(t);
+          const int64_t o0 = OffAt(c.offsets, w, r);
+          const int64_t len = OffAt(c.offsets, w, r + 1) - o0;
           if ((int64_t)b.chars.size() < b.chars_used + len)
             b.chars.resize(std::max<int64_t>(b.chars_used + len, b.chars.size() * 3 / 2 + 64));
-          memcpy(b.chars.data() + b.chars_used, c.values + off[r], len);
+          memcpy(b.chars.data() + b.chars_used, c.values + o0, len);
           b.chars_used += len;
-          b.offsets[d + 1] = (int32_t)b.chars_used;
+          b.offsets[d + 1] = w == 8 ? b.chars_used : (int64_t)(int32_t)b.chars_used;
         } else if (t == T_BOOL) {
           if (!GetBit(c.values, r)) ClearBit(b.values.data(), d);
           else b.values[d >> 3] |= (uint8_t)(1u << (d & 7));

@@ -2,7 +2,9 @@
 
 Run in a checkout where the reference sources and pyarrow are present:
 
-    python tests/golden/make_golden.py [/path/to/gazelle_plugin]
+    python tests/golden/make_golden.py [/path/to/gazelle_plugin] [--only=large]
+
+(--only=large rewrites large_binary.json alone.)
 
 It compiles the reference Splitter (oracle/ref/Makefile -> oracle/_ref/) and runs it on
 seeded inputs from gazelle_plugin_gb300.workloads, recording for every case the SHA-256 of
@@ -20,6 +22,13 @@ Configurations on which the reference has undefined behaviour are excluded: with
 prefer_spill, a reallocation (new size > capacity) reads partition_buffers_ after
 CacheRecordBatch cleared it (splitter.cc:907-909, 766-773), which happens whenever a
 partition receives more rows in one batch than its buffer holds or offheap_per_task > 0.
+
+large_binary.json holds schemas with large_utf8 / large_binary columns (64-bit offsets).  The
+reference sizes their offset buffers through one `sizeof_binary_offset` variable per call that
+a 32-bit binary column sets and a later 64-bit one does not reset (splitter.cc:476-485,
+619-632): a 64-bit column after a 32-bit one gets a half-size offsets buffer and is cut with
+32-bit reads.  These cases put every 64-bit column before every 32-bit one, where the
+reference is well defined.
 """
 from __future__ import annotations
 
@@ -139,9 +148,47 @@ def random_case(seed):
     return schema, batches, P, keys, opts
 
 
+def large_case(seed):
+    """Schema, batches, P, keys and options of a `large_<n>` case: an int key, 0-3 fixed-width
+    columns, 1-3 large_utf8 / large_binary columns and 0-2 utf8 / binary columns, the binary
+    ones in schema order large first, interleaved at random with the others."""
+    rng = np.random.default_rng(seed)
+    others = [W.Field("k", str(rng.choice(["int32", "int64"])), bool(rng.random() < 0.5))]
+    others += [W.Field(f"f{i}", str(rng.choice(["int16", "int32", "int64", "float64", "bool"])))
+               for i in range(int(rng.integers(0, 4)))]
+    binary = [W.Field(f"L{i}", str(rng.choice(["large_utf8", "large_binary"])))
+              for i in range(int(rng.integers(1, 4)))]
+    binary += [W.Field(f"s{i}", str(rng.choice(["utf8", "binary"]))) for i in range(int(rng.integers(0, 3)))]
+    pick = rng.permutation(len(others) + len(binary)) < len(others)  # True: an `others` slot
+    oi, bi, schema = iter(others), iter(binary), []
+    for is_other in pick:
+        schema.append(next(oi) if is_other else next(bi))
+    keys = [i for i, f in enumerate(schema) if f.name == "k"]
+    P = int(rng.choice([1, 3, 16, 200]))
+    bsz = int(rng.choice([16, 100, 4096]))
+    ps = bool(rng.random() < 0.6)
+    opts = {"buffer_size": bsz, "prefer_spill": ps,
+            "offheap_per_task": 0 if ps else int(rng.choice([0, 1 << 16]))}
+    nullf = float(rng.choice([0.0, 0.05, 0.5]))
+    batches = [W.random_batch(rng, schema, int(rng.integers(1, bsz + 1)), nullf)
+               for _ in range(int(rng.integers(1, 8)))]
+    return schema, batches, P, keys, opts
+
+
+def large_cases():
+    for seed in range(16):
+        schema, batches, P, keys, opts = large_case(4000 + seed)
+        yield (f"large_{seed}", schema, batches, P, keys, opts, {"workload": "large", "seed": 4000 + seed})
+    schema, batches, P, keys, opts = large_case(4100)
+    yield ("large_write_schema", schema, batches, P, keys, dict(opts, write_schema=True),
+           {"workload": "large", "seed": 4100})
+
+
 def regenerate(case):
     """Inputs of a recorded case, rebuilt from its generator description."""
     g = case["gen"]
+    if g["workload"] == "large":
+        return large_case(g["seed"])[1]
     if g["workload"] == "c1":
         return W.c1_batches(g["seed"], g["num_batches"], g["rows"])
     if g["workload"] == "c2":
@@ -284,10 +331,24 @@ def partitioner_cases():
             yield (f"random_{seed}_rr", "rr", P, opts, g)
 
 
+def write_large():
+    recs = []
+    for name, schema, batches, P, keys, opts, gen in large_cases():
+        recs.append(record(name, schema, batches, P, keys, opts, gen))
+        print(name, recs[-1]["data_sha256"][:16])
+    with open(os.path.join(HERE, "large_binary.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py", "cases": recs}, f, indent=1)
+
+
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else O.reference_root()
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    ref_root = args[0] if args else O.reference_root()
     if not O.build_ref(ref_root):
         raise SystemExit("reference tree not found")
+    if "--only=large" in sys.argv:
+        write_large()
+        return
+    write_large()
     recs = []
     for name, schema, batches, P, keys, opts, gen in cases():
         recs.append(record(name, schema, batches, P, keys, opts, gen))
