@@ -673,7 +673,7 @@ __device__ __forceinline__ void csync() { group_sync<kConsumers, 1>(); }
 constexpr int kSortIters = kTileRows / (kW * 32);  // 32-row groups per warp
 __device__ void radix_pass(const uint16_t* kin, const uint16_t* pin, uint16_t* kout,
                            uint16_t* pout, int n, int shift, int ndig, uint16_t* wcnt, uint32_t* off,
-                           uint32_t* scratch) {
+                           uint32_t* scratch, uint32_t* first = nullptr) {
   // ndig: digit values that occur (keys < P), so only kW * ndig counters are transposed / scanned
   const int w = threadIdx.x >> 5;
   const int seg = ((n + kW * 32 - 1) / (kW * 32)) * 32;
@@ -706,6 +706,10 @@ __device__ void radix_pass(const uint16_t* kin, const uint16_t* pin, uint16_t* k
   }
   csync();
   block_exscan<kConsumers, 1>(off, kW * ndig, scratch);
+  if (first != nullptr) {  // first sorted position of every digit (its warp-0 offset), then n
+    for (int d = threadIdx.x; d <= ndig; d += kConsumers) first[d] = d < ndig ? off[d * kW] : (uint32_t)n;
+    csync();  // read before the scatter below moves the offsets
+  }
 #pragma unroll
   for (int it = 0; it < kSortIters; it++) {
     const int c = it * 32;
@@ -1145,50 +1149,78 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
                              ((uint32_t)vwork << 17) | ((uint32_t)(kind == COL_BINARY ? sd.arr_str[a] : 0) << 24),
                          (uint32_t)a);
   }
+  // destination row / validity bit of a partition's first row in the tile: its segment offset
+  // from the plan + rows from the segment's earlier tiles
+  const size_t tp = (size_t)tile.seg * P;
+  const bool has_pre = tile.tseg > 0;
+  // Up to 256 partitions (one radix pass): thread p reads partition p's entries now, so the
+  // loads are in flight during the sort, and the sort itself gives each partition's first sorted
+  // position (no scan for the run starts).
+  const bool small = P <= 256;
+  uint32_t t_ps = 0, t_cnt = 0, t_pre = 0, t_vs = 0, t_vp = 0;
+  if (small && (int)threadIdx.x < P) {
+    const int p = threadIdx.x;
+    t_ps = fd.pstart[p];
+    t_cnt = fd.cnt[tp + p];
+    t_pre = has_pre ? fd.tilepre[(size_t)blockIdx.x * P + p] : 0u;
+    t_vs = fd.vstart[p];
+    t_vp = fd.vpos[tp + p];
+  }
   for (int j = threadIdx.x; j < n; j += kConsumers) {
     kA[j] = fd.pids[tile.frow0 + j];
     pA[j] = (uint16_t)j;
   }
   csync();
-  radix_pass(kA, pA, kB, pB, n, 0, min(P, 256), wcnt, roff, scratch);
+  uint32_t* first = nm2;  // [P + 1] (nm2 is free until the run metadata of the binary columns)
+  radix_pass(kA, pA, kB, pB, n, 0, min(P, 256), wcnt, roff, scratch, small ? first : nullptr);
   uint16_t* ks = kB;
   uint16_t* ps = pB;
   uint32_t* dstrow = reinterpret_cast<uint32_t*>(kA);  // kA,pA are free after one pass
-  if (P > 256) {
+  if (!small) {
     radix_pass(kB, pB, kA, pA, n, 8, ((P - 1) >> 8) + 1, wcnt, roff, scratch);
     ks = kA;
     ps = pA;
     dstrow = reinterpret_cast<uint32_t*>(kB);
   }
 
-  // run starts: rs[j] = first sorted position with the same partition id
-  {
-    const int per = (n + kConsumers - 1) / kConsumers;
-    const int lo = threadIdx.x * per;
-    const int hi = min(lo + per, n);
-    uint32_t mx = 0;
-    for (int j = lo; j < hi; j++)
-      if (j == 0 || ks[j] != ks[j - 1]) mx = j;
-    uint32_t carry = block_exmax<kConsumers, 1>(mx, scratch);
-    for (int j = lo; j < hi; j++) {
-      if (j == 0 || ks[j] != ks[j - 1]) carry = j;
-      rs[j] = (uint16_t)carry;
+  // run starts: rs[j] = first sorted position with the same partition id; S / rt1 at a run
+  // start: the run's destination row / validity bit minus that position
+  if (small) {
+    if ((int)threadIdx.x < P) {
+      const int p = threadIdx.x;
+      const uint32_t f = first[p];
+      if (first[p + 1] > f) {  // partition p has rows in this tile
+        S[f] = t_ps + t_cnt + t_pre - f;
+        rt1[f] = t_vs + t_vp + t_pre - f;
+      }
     }
-  }
-  csync();
-  // destination row / validity bit: one metadata lookup per run, kept at the run start
-  // segment offset from the plan + rows from the segment's earlier tiles
-  const size_t tp = (size_t)tile.seg * P;
-  const bool has_pre = tile.tseg > 0;
-  for (int j = threadIdx.x; j < n; j += kConsumers) {
-    if (rs[j] == j) {
-      const int p = ks[j];
-      const uint32_t before = has_pre ? fd.tilepre[(size_t)blockIdx.x * P + p] : 0u;
-      S[j] = fd.pstart[p] + fd.cnt[tp + p] + before - (uint32_t)j;
-      rt1[j] = fd.vstart[p] + fd.vpos[tp + p] + before - (uint32_t)j;
+    for (int j = threadIdx.x; j < n; j += kConsumers) rs[j] = (uint16_t)first[ks[j]];
+    csync();
+  } else {
+    {
+      const int per = (n + kConsumers - 1) / kConsumers;
+      const int lo = threadIdx.x * per;
+      const int hi = min(lo + per, n);
+      uint32_t mx = 0;
+      for (int j = lo; j < hi; j++)
+        if (j == 0 || ks[j] != ks[j - 1]) mx = j;
+      uint32_t carry = block_exmax<kConsumers, 1>(mx, scratch);
+      for (int j = lo; j < hi; j++) {
+        if (j == 0 || ks[j] != ks[j - 1]) carry = j;
+        rs[j] = (uint16_t)carry;
+      }
     }
+    csync();
+    for (int j = threadIdx.x; j < n; j += kConsumers) {
+      if (rs[j] == j) {
+        const int p = ks[j];
+        const uint32_t before = has_pre ? fd.tilepre[(size_t)blockIdx.x * P + p] : 0u;
+        S[j] = fd.pstart[p] + fd.cnt[tp + p] + before - (uint32_t)j;
+        rt1[j] = fd.vstart[p] + fd.vpos[tp + p] + before - (uint32_t)j;
+      }
+    }
+    csync();
   }
-  csync();
   for (int j = threadIdx.x; j < n; j += kConsumers) {
     dstrow[j] = S[rs[j]] + (uint32_t)j;
     dbs[ps[j]] = rt1[rs[j]] + (uint32_t)j;
