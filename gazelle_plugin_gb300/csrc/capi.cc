@@ -162,6 +162,7 @@ void gz_split_default_options(GzSplitOptions* o) {
   o->device_budget = 64ll << 30;
   o->data_file = nullptr;
   o->local_dirs = nullptr;
+  o->host_budget = 0;
 }
 
 GzStatus gz_split_make(const char* short_name, int32_t num_partitions, const uint8_t* schema_ipc,
@@ -409,6 +410,13 @@ GzStatus gz_split_stats(int64_t handle, int64_t* out8) {
   auto e = Lookup(handle);
   if (!e || !out8) return GZ_INVALID;
   e->splitter->Stats(out8);
+  return GZ_OK;
+}
+
+GzStatus gz_split_disk_spill(int64_t handle, int64_t* out3) {
+  auto e = Lookup(handle);
+  if (!e || !out3) return GZ_INVALID;
+  e->splitter->DiskSpillStats(out3);
   return GZ_OK;
 }
 

@@ -3,6 +3,7 @@
 
 #include <errno.h>
 #include <fcntl.h>
+#include <stdio.h>
 #include <string.h>
 #include <sys/mman.h>
 #include <sys/stat.h>
@@ -10,6 +11,7 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <numeric>
 
@@ -128,6 +130,22 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
   else if (opts_.compression != GZ_CODEC_UNCOMPRESSED)
     return Status::Error(GZ_NOT_IMPLEMENTED, "codec " + std::to_string(opts_.compression) + " is not implemented");
   data_file_ = opts.data_file ? opts.data_file : "";
+  // spill dirs (the JNI's localDirs, the reference's NATIVESQL_SPARK_LOCAL_DIRS): comma
+  // separated, empty entries skipped (GetConfiguredLocalDirs, utils.h:64-88)
+  if (opts.local_dirs) {
+    std::string all = opts.local_dirs;
+    size_t at = 0;
+    while (at <= all.size()) {
+      const size_t comma = std::min(all.find(',', at), all.size());
+      if (comma > at) spill_dirs_.push_back(all.substr(at, comma - at));
+      at = comma + 1;
+    }
+  }
+  sub_dir_sel_.assign(spill_dirs_.size(), 0);
+  if (opts_.num_sub_dirs <= 0) opts_.num_sub_dirs = 64;
+  if (opts_.host_budget < 0) return Status::Error(GZ_INVALID, "host_budget must be >= 0");
+  if (opts_.host_budget > 0 && spill_dirs_.empty())
+    return Status::Error(GZ_INVALID, "host_budget needs local_dirs to spill to");
   opts_.data_file = nullptr;
   opts_.local_dirs = nullptr;
   if ((int)fields.size() > kMaxSchemaCols) return Status::Error(GZ_NOT_IMPLEMENTED, "too many fields");
@@ -1107,7 +1125,7 @@ Status Splitter::MoveOutputs() {
       if (!st.ok()) return st;
     }
   }
-  return Status::OK();
+  return KeepHostBudget();
 }
 
 // Queues the k_scatter of the last flushed pass on stream_, after that pass's plan and metadata
@@ -1158,7 +1176,98 @@ Status Splitter::MoveFlushToHost(FlushRec& f) {
   f.on_host = true;
   resident_bytes_ -= f.out_bytes;
   spilled_to_host_bytes_ += f.out_bytes;
+  host_resident_ += f.out_bytes;
   return Status::OK();
+}
+
+// A spill file: temp_shuffle_<32 hex digits> in <local dir>/<sub dir as 2 hex digits>, the dirs
+// and each dir's sub-directories taken in turn (NextSpilledFileDir, splitter.cc:1346-1353;
+// GetSpilledShuffleFileDir / CreateTempShuffleFile, utils.h:55-62, 90-115).
+std::string Splitter::NextSpillPath() {
+  const std::string& dir = spill_dirs_[dir_sel_];
+  char sub[16];
+  snprintf(sub, sizeof(sub), "%02x", sub_dir_sel_[dir_sel_]);
+  sub_dir_sel_[dir_sel_] = (sub_dir_sel_[dir_sel_] + 1) % opts_.num_sub_dirs;
+  dir_sel_ = (dir_sel_ + 1) % (int)spill_dirs_.size();
+  const std::string d = dir + "/" + sub;
+  mkdir(dir.c_str(), 0777);  // existing dirs are fine; a real failure shows at open
+  mkdir(d.c_str(), 0777);
+  static std::atomic<uint64_t> seq{0};
+  const uint64_t a = (uint64_t)NowNs() ^ ((uint64_t)getpid() << 32), b = seq.fetch_add(1) * 0x9E3779B97F4A7C15ull;
+  char name[64];
+  snprintf(name, sizeof(name), "temp_shuffle_%016llx%016llx", (unsigned long long)a, (unsigned long long)b);
+  return d + "/" + name;
+}
+
+// Writes a moved pass's bytes to a new local-dir file, maps it read-only in place of the pinned
+// block and gives the block back to the pool; Stop reads the pass through the mapping.
+Status Splitter::MoveFlushToFile(FlushRec& f) {
+  Status st = Cuda(cudaStreamSynchronize(ostream_), "D2H partition data");  // the bytes have landed
+  if (!st.ok()) return st;
+  std::string path;
+  int fd = -1;
+  for (int tries = 0; tries < 8 && fd < 0; tries++) {
+    path = NextSpillPath();
+    fd = open(path.c_str(), O_RDWR | O_CREAT | O_EXCL | O_CLOEXEC, 0600);
+  }
+  if (fd < 0) return Status::Error(GZ_IO, "cannot create spill file " + path + ": " + strerror(errno));
+  constexpr size_t kPiece = 64u << 20;
+  const size_t pieces = (f.out_bytes + kPiece - 1) / kPiece;
+  std::atomic<int> err{0};
+  ParallelFor(pieces, [&](size_t i) {
+    size_t off = i * kPiece;
+    const size_t end = std::min(off + kPiece, f.out_bytes);
+    while (off < end && err.load() == 0) {
+      const ssize_t w = pwrite(fd, f.h_out + off, end - off, (off_t)off);
+      if (w <= 0) {
+        if (w < 0 && errno == EINTR) continue;
+        err.store(w < 0 ? errno : EIO);
+        break;
+      }
+      off += (size_t)w;
+    }
+  });
+  void* m = MAP_FAILED;
+  if (err.load() == 0 && f.out_bytes > 0) m = mmap(nullptr, f.out_bytes, PROT_READ, MAP_SHARED, fd, 0);
+  const int e = err.load() ? err.load() : errno;
+  close(fd);
+  if (m == MAP_FAILED) {
+    unlink(path.c_str());
+    return Status::Error(GZ_IO, "spill file " + path + ": " + strerror(e));
+  }
+  for (size_t i = 0; i < host_chunks_.size(); i++) {
+    if (host_chunks_[i].ptr == f.h_out) {
+      PinnedRelease(host_chunks_[i]);
+      host_chunks_.erase(host_chunks_.begin() + (long)i);
+      break;
+    }
+  }
+  f.h_out = static_cast<uint8_t*>(m);
+  f.on_file = true;
+  f.spill_path = path;
+  host_resident_ -= f.out_bytes;
+  disk_files_++;
+  disk_files_now_++;
+  disk_bytes_ += (int64_t)f.out_bytes;
+  return Status::OK();
+}
+
+Status Splitter::KeepHostBudget() {
+  if (opts_.host_budget <= 0) return Status::OK();
+  for (auto& f : flushes_) {
+    if (host_resident_ <= (size_t)opts_.host_budget) break;
+    if (f.on_host && !f.on_file && f.h_out != nullptr && f.out_bytes > 0) {
+      Status st = MoveFlushToFile(f);
+      if (!st.ok()) return st;
+    }
+  }
+  return Status::OK();
+}
+
+void Splitter::DiskSpillStats(int64_t* out3) const {
+  out3[0] = disk_files_;
+  out3[1] = disk_bytes_;
+  out3[2] = disk_files_now_;
 }
 
 Status Splitter::SyncAndCheck() {
@@ -1741,7 +1850,16 @@ uint8_t* Splitter::HostAlloc(size_t bytes) {
 void Splitter::ReleaseHost() {
   for (auto& b : host_chunks_) PinnedRelease(b);
   host_chunks_.clear();
-  for (auto& f : flushes_) f.h_out = nullptr;
+  for (auto& f : flushes_) {
+    if (f.on_file) {  // the pass's local-dir file: unmapped and deleted
+      munmap(f.h_out, f.out_bytes);
+      unlink(f.spill_path.c_str());
+      f.on_file = false;
+      disk_files_now_--;
+    }
+    f.h_out = nullptr;
+  }
+  host_resident_ = 0;
 }
 
 // After Stop nothing more is split: staging and scratch go back (all streams are idle).
@@ -1776,6 +1894,8 @@ Status Splitter::SpillFixedSize(int64_t size, int64_t* actual) {
     if (!st.ok()) return st;
   }
   st = Cuda(cudaStreamSynchronize(ostream_), "D2H partition data");
+  if (!st.ok()) return st;
+  st = KeepHostBudget();
   if (!st.ok()) return st;
   // SpillLargestPartition up to 5 times (splitter.cc:741-799): largest cached body bytes
   int64_t cur = 0;

@@ -71,6 +71,8 @@ class Splitter {
   // Runs the pending device pass and waits for all device work of the batches split so far.
   Status Sync();
   void Stats(int64_t* out8) const;
+  // [0] local-dir files written, [1] their bytes, [2] files present now
+  void DiskSpillStats(int64_t* out3) const;
 
   int64_t TotalBytesWritten() const { return total_bytes_written_; }
   int64_t TotalBytesSpilled() const { return total_bytes_spilled_; }
@@ -101,8 +103,11 @@ class Splitter {
     uint32_t n_batches = 0;
     uint8_t* d_out = nullptr;           // device outputs (nullptr once moved to host)
     size_t out_bytes = 0;
-    uint8_t* h_out = nullptr;           // pinned host copy of the outputs (in host_chunks_)
+    uint8_t* h_out = nullptr;           // pinned host copy of the outputs (in host_chunks_), or
+                                        // the read-only mapping of its local-dir file
     bool on_host = false;
+    bool on_file = false;               // h_out maps spill_path (past host_budget)
+    std::string spill_path;
     std::vector<size_t> off_values, off_bits, off_valid, off_chars;  // per array column, SIZE_MAX: none
     uint32_t* h_meta = nullptr;         // pinned: rows_f, pstart, vstart, bytes_f, cstart, count, emit
     size_t bits_begin = 0, bits_end = 0;  // the bit regions (validity, bool values) in the output
@@ -241,6 +246,15 @@ class Splitter {
   Status LaunchPendingScatter();
   Status Drain();  // Flush, then queue the pending k_scatter
   Status MoveOutputs();
+  // Past host_budget, the oldest passes in pinned host memory go to local-dir files.
+  Status KeepHostBudget();
+  Status MoveFlushToFile(FlushRec& f);
+  std::string NextSpillPath();
+  std::vector<std::string> spill_dirs_;  // local_dirs, split at commas
+  std::vector<int> sub_dir_sel_;         // next sub-directory of each dir
+  int dir_sel_ = 0;
+  size_t host_resident_ = 0;             // pinned host bytes of moved passes
+  int64_t disk_files_ = 0, disk_bytes_ = 0, disk_files_now_ = 0;
 
   // staging (host inputs): double-buffered device buffers, filled by k_gather (direct_) or
   // by H2D copies of pinned host twins

@@ -52,6 +52,7 @@ class GzSplitOptions(ctypes.Structure):
         ("local_dirs", ctypes.c_char_p),
         ("host_read", ctypes.c_int32),
         ("seg_tiles", ctypes.c_int32),
+        ("host_budget", ctypes.c_int64),
     ]
 
 
@@ -492,6 +493,12 @@ class ShuffleSplitterJniWrapper:
         emitted record batches]."""
         out = (ctypes.c_int64 * 8)()
         _check(lib().gz_split_stats(splitterId, out), splitterId)
+        return list(out)
+
+    def diskSpill(self, splitterId: int) -> List[int]:
+        """Local-dir spill files (host_budget): [files written, their bytes, files present now]."""
+        out = (ctypes.c_int64 * 3)()
+        _check(lib().gz_split_disk_spill(splitterId, out), splitterId)
         return list(out)
 
     def kernelTimes(self, splitterId: int) -> List[float]:

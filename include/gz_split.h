@@ -103,12 +103,17 @@ typedef struct GzSplitOptions {
   int64_t device_budget;             /* HBM bytes for resident partition data before it is
                                         moved to pinned host memory (default 64 GiB) */
   const char* data_file;             /* written at Stop; NULL/"" keeps the bytes in memory */
-  const char* local_dirs;            /* comma separated spill dirs (unused: spills go to
-                                        pinned host memory) */
+  const char* local_dirs;            /* comma separated spill dirs (the executor's local dirs):
+                                        partition data past host_budget goes to temp_shuffle_*
+                                        files in their num_sub_dirs sub-directories */
   int32_t host_read;                 /* GzHostRead, default GZ_HOST_READ_AUTO */
   int32_t seg_tiles;                 /* 1024-row tiles per k_hash_count segment, 1..32;
                                         0 (default): the gz_autotune choice for this schema,
                                         else 4..32 growing with num_partitions */
+  int64_t host_budget;               /* pinned host bytes of partition data a splitter keeps
+                                        before its oldest passes move to files under local_dirs
+                                        (read back through a mapping at Stop, deleted after it);
+                                        0 (default): no limit */
 } GzSplitOptions;
 
 /* SplitResult (native-sql-engine/core/src/main/java/com/intel/oap/vectorized/SplitResult.java:21-39).
@@ -214,6 +219,10 @@ GzStatus gz_split_kernel_times(int64_t handle, double* out4);
  * HBM, [5] batches split, [6] rows split, [7] emitted record batches (after Stop, else -1).
  * No reference counterpart. */
 GzStatus gz_split_stats(int64_t handle, int64_t* out8);
+
+/* Local-dir spill files of this handle (host_budget): [0] files written, [1] their bytes,
+ * [2] files present now (they are deleted once Stop has read them).  No reference counterpart. */
+GzStatus gz_split_disk_spill(int64_t handle, int64_t* out3);
 
 /* ---- Autotuner (no reference counterpart) ---------------------------------------------
  * The device pass has two run-time knobs: flush_bytes (its size) and seg_tiles (the segment
