@@ -134,6 +134,7 @@ std::vector<gz::Field> FieldsFrom(const GzField* fields, int32_t n_fields) {
     f.precision = fields[i].precision;
     f.scale = fields[i].scale;
     f.unit = fields[i].unit;
+    f.elem = fields[i].elem_type;
     f.name = fields[i].name ? fields[i].name : "";
     fs.push_back(f);
   }
@@ -391,6 +392,12 @@ GzStatus gz_reader_column_to_host(int64_t handle, int32_t field, uint8_t* validi
   auto r = LookupReader(handle);
   if (!r) return GZ_INVALID;
   return ReportReader(r.get(), r->reader->ColumnToHost(field, validity, offsets, values));
+}
+
+GzStatus gz_reader_elem_validity_to_host(int64_t handle, int32_t field, uint8_t* out) {
+  auto r = LookupReader(handle);
+  if (!r) return GZ_INVALID;
+  return ReportReader(r.get(), r->reader->ElemValidityToHost(field, out));
 }
 
 GzStatus gz_reader_close(int64_t handle) {

@@ -57,6 +57,10 @@ struct SchemaDesc {
   int32_t arr_width[kMaxCols];  // value bytes of a fixed column; offset bytes (4 / 8) of a binary one
   int32_t arr_str[kMaxCols];    // binary ordinal k of a binary column, -1 otherwise
   int32_t order[kMaxCols];      // order in which k_scatter processes the array columns
+  // list columns (binary-like, after the binary ones): their "characters" are the element
+  // values, a row's byte length is its element count << arr_shift, and a null row has none
+  int32_t arr_shift[kMaxCols];
+  uint64_t list_mask;           // array columns that are lists
 };
 
 // Device addresses of one input column of one batch.  offsets only for binary columns (int32,
@@ -67,6 +71,7 @@ struct ColPtr {
   const int32_t* offsets;
   const uint8_t* values;
   uint64_t values_bytes;  // readable bytes at `values` (binary columns: offsets are checked)
+  const uint8_t* child_validity;  // list: the elements' validity bitmap; nullptr: none
 };
 
 // One input buffer the device copies out of host memory (a coherent host-device link lets
@@ -158,7 +163,9 @@ struct FlushDesc {
   uint8_t* out_values[kMaxCols];   // fixed: n_rows * width; binary: n_rows end offsets (arr_width bytes)
   uint32_t* out_bits[kMaxCols];    // bool values, same bit layout as validity
   uint32_t* out_valid[kMaxCols];   // validity words, 0xff-filled; nullptr: no nulls in flush
-  uint8_t* out_chars[kMaxCols];    // binary bytes
+  uint8_t* out_chars[kMaxCols];    // binary bytes (list: element values)
+  uint32_t* out_cvalid[kMaxCols];  // list: element validity bits at the element's position in
+                                   // out_chars, 0xff-filled; nullptr: no element nulls in flush
 
   // persistent partition state (the reference's per-pid buffer bookkeeping)
   uint32_t* st_cap;               // partition_buffer_size_

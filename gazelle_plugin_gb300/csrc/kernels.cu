@@ -106,6 +106,8 @@ constexpr int kHashThreads = 256;
 constexpr int kHashRows = kTileRows / kHashThreads;  // rows of a tile per thread
 static_assert(kHashRows * kHashThreads == kTileRows, "hash rows per thread");
 
+// kLists: the schema has list columns (instantiated apart so the other schemas' code is unchanged)
+template <bool kLists>
 __global__ void __launch_bounds__(kHashThreads) k_hash_count(const SchemaDesc sd, const FlushDesc fd) {
   extern __shared__ uint32_t smem[];
   __shared__ ColPtr s_key[kMaxKeys];
@@ -280,13 +282,18 @@ __global__ void __launch_bounds__(kHashThreads) k_hash_count(const SchemaDesc sd
 #pragma unroll
       for (int u = 0; u <= kHashRows; u++) o[u] = c.offsets[r0 + min((uint32_t)u, m)];
     }
+    // a list column: element offsets, elements of 1 << shift bytes, a null row has none
+    const int ak = sd.n_fixed + k;
+    const int shift = kLists ? sd.arr_shift[ak] : 0;
+    const bool list = kLists && ((sd.list_mask >> ak) & 1ull);
 #pragma unroll
     for (int u = 0; u < kHashRows; u++) {
-      uint32_t len = (uint32_t)(o[u + 1] - o[u]);
-      if (act[u] && (o[u] < 0 || o[u + 1] < o[u] || (uint64_t)o[u + 1] > c.values_bytes)) {
+      uint32_t len = (uint32_t)(o[u + 1] - o[u]) << shift;
+      if (act[u] && (o[u] < 0 || o[u + 1] < o[u] || ((uint64_t)o[u + 1] << shift) > c.values_bytes)) {
         bad = true;
         len = 0;
       }
+      if (list && c.validity != nullptr && !get_bit(c.validity, rr[u])) len = 0;
       if (act[u] && len) atomicAdd(&BH[k * P + p[u]], len);
     }
   }
@@ -295,11 +302,12 @@ __global__ void __launch_bounds__(kHashThreads) k_hash_count(const SchemaDesc sd
     const ColPtr c = s_str[threadIdx.x];
     const size_t ct = ((size_t)tile.tile0 + t0 / kTileRows) * nstr + threadIdx.x;
     // (valid offsets of either width are below 2^31: a batch's characters are at most that)
+    const int sh = kLists ? sd.arr_shift[sd.n_fixed + threadIdx.x] : 0;  // list: element bytes
     if (sd.arr_width[sd.n_fixed + threadIdx.x] == 8) {
       const int64_t* o64 = reinterpret_cast<const int64_t*>(c.offsets);
       fd.crange[ct] = make_int2((int32_t)o64[tile.row0 + t0], (int32_t)o64[tile.row0 + t1]);
     } else {
-      fd.crange[ct] = make_int2(c.offsets[tile.row0 + t0], c.offsets[tile.row0 + t1]);
+      fd.crange[ct] = make_int2(c.offsets[tile.row0 + t0] << sh, c.offsets[tile.row0 + t1] << sh);
     }
   }
   }
@@ -980,8 +988,29 @@ __device__ __forceinline__ void scatter_zero_bits(uint32_t* words, uint32_t bits
   }
 }
 
+// A list row's element validity: the zeros among source bits [e0, e0 + m) of `src` cleared at
+// destination bits [d0, d0 + m) of `dst` (0xff-filled words), source read 32 bits at a time
+// byte by byte (only bytes holding those bits).  Out of line: list columns only.
+__device__ __noinline__ void clear_null_elements(uint32_t* dst, uint32_t d0, const uint8_t* src, uint32_t e0,
+                                                 uint32_t m) {
+  for (uint32_t x = 0; x < m; x += 32) {
+    const uint32_t nb = min(32u, m - x);
+    const uint32_t b = e0 + x;  // first source bit
+    uint64_t w = 0;
+    for (uint32_t y = b >> 3; y <= (b + nb - 1) >> 3; y++) w |= (uint64_t)src[y] << (8 * (y - (b >> 3)));
+    uint32_t zeros = ~(uint32_t)(w >> (b & 7)) & (nb == 32 ? 0xffffffffu : (1u << nb) - 1u);
+    while (zeros) {
+      const uint32_t db = d0 + x + (uint32_t)(__ffs(zeros) - 1);
+      zeros &= zeros - 1;
+      atomicAnd(dst + (db >> 5), ~(1u << (db & 31)));
+    }
+  }
+}
+
 }  // namespace
 
+// kLists: the schema has list columns (instantiated apart so the other schemas' code is unchanged)
+template <bool kLists>
 __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc sd, const FlushDesc fd) {
   extern __shared__ __align__(128) uint8_t ssm[];
   __shared__ uint32_t scratch[33];
@@ -1310,6 +1339,10 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
         const bool off64 = ((ct.z >> 8) & 255u) == 8;
         const int32_t* oin = reinterpret_cast<const int32_t*>(stg);
         const int64_t* oin64 = reinterpret_cast<const int64_t*>(stg);
+        // a list column: element offsets, elements of 1 << shift bytes; a null row has none
+        const int shift = kLists ? sd.arr_shift[a] : 0;
+        const bool list = kLists && ((sd.list_mask >> a) & 1ull);
+        const uint32_t lvb = list && ((ct.z >> 17) & 1u) ? ct.y : 0u;  // staged row validity
         // lengths of the owned positions; exclusive prefix over the tile = the lengths of all
         // earlier rows u' < u of positions + this row's prefix, one fused warp scan per row u
         uint32_t len[kRowsPerThread], pre[kRowsPerThread], so[kRowsPerThread];  // so: source offset
@@ -1324,8 +1357,9 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
               so[u] = (uint32_t)oin64[r];
               len[u] = (uint32_t)oin64[r + 1] - so[u];
             } else {
-              so[u] = (uint32_t)oin[r];
-              len[u] = (uint32_t)oin[r + 1] - so[u];
+              so[u] = (uint32_t)oin[r] << shift;
+              len[u] = ((uint32_t)oin[r + 1] << shift) - so[u];
+              if (lvb && !((lds8(lvb + (r >> 3)) >> (r & 7)) & 1u)) len[u] = 0;
             }
           }
           pre[u] = len[u];
@@ -1400,7 +1434,7 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
           } else {
 #pragma unroll
             for (int u = 0; u < kRowsPerThread; u++)
-              if (threadIdx.x + u * kConsumers < n) ooff[d[u]] = (int32_t)v[u];
+              if (threadIdx.x + u * kConsumers < n) ooff[d[u]] = (int32_t)(v[u] >> shift);
           }
         }
         const int k = (int)(ct.z >> 24);
@@ -1419,6 +1453,17 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
           for (int u = 0; u < kRowsPerThread; u++) {
             const int j = threadIdx.x + u * kConsumers;
             if (j < n) copy_string(ochars + cd[u], c.values + so[u], len[u], buf_lo, buf_hi);
+          }
+        }
+        // a list column's element validity: the null elements of each row cleared at their
+        // destination element (bits start 0xff), read 32 at a time from the batch's bitmap
+        if constexpr (kLists) {
+          if (list && c.child_validity != nullptr && fd.out_cvalid[a] != nullptr) {
+#pragma unroll
+            for (int u = 0; u < kRowsPerThread; u++)
+              if (threadIdx.x + u * kConsumers < n && len[u])
+                clear_null_elements(fd.out_cvalid[a], cd[u] >> shift, c.child_validity, so[u] >> shift,
+                                    len[u] >> shift);
           }
         }
         }
@@ -1482,11 +1527,14 @@ __global__ void __launch_bounds__(256) k_gather(const HostCopy* __restrict__ job
 // launch helpers
 cudaError_t launch_hash_count(const SchemaDesc& sd, const FlushDesc& fd, cudaStream_t st) {
   const size_t sm = fd.hist_in_smem ? sizeof(uint32_t) * sd.P * (1 + sd.n_str) : 0;
+  const bool lists = sd.list_mask != 0;
   if (sm > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(k_hash_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaError_t e = lists ? cudaFuncSetAttribute(k_hash_count<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)
+                          : cudaFuncSetAttribute(k_hash_count<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
   }
-  k_hash_count<<<fd.n_segs, kHashThreads, sm, st>>>(sd, fd);
+  if (lists) k_hash_count<true><<<fd.n_segs, kHashThreads, sm, st>>>(sd, fd);
+  else k_hash_count<false><<<fd.n_segs, kHashThreads, sm, st>>>(sd, fd);
   return cudaGetLastError();
 }
 
@@ -1534,11 +1582,13 @@ cudaError_t launch_scatter(const SchemaDesc& sd, const FlushDesc& fd, cudaStream
   const size_t sm = scatter_smem_bytes();
   static bool attr_set = false;
   if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(k_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaError_t e = cudaFuncSetAttribute(k_scatter<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_scatter<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  k_scatter<<<fd.n_tiles, kScatterBlock, sm, st>>>(sd, fd);
+  if (sd.list_mask) k_scatter<true><<<fd.n_tiles, kScatterBlock, sm, st>>>(sd, fd);
+  else k_scatter<false><<<fd.n_tiles, kScatterBlock, sm, st>>>(sd, fd);
   return cudaGetLastError();
 }
 

@@ -21,6 +21,8 @@ inline size_t AlignUp(size_t x, size_t a) { return (x + a - 1) / a * a; }
 bool IsLargeBinaryType(int t) { return t == GZ_TYPE_LARGE_STRING || t == GZ_TYPE_LARGE_BINARY; }
 bool IsBinaryType(int t) { return t == GZ_TYPE_STRING || t == GZ_TYPE_BINARY || IsLargeBinaryType(t); }
 int OffsetWidth(int t) { return IsLargeBinaryType(t) ? 8 : 4; }
+// Types whose batches carry int32 / int64 offsets: binary ones and lists (int32 element offsets)
+bool HasOffsets(int t) { return IsBinaryType(t) || t == GZ_TYPE_LIST; }
 // Offset r of a little-endian offsets buffer of width w
 int64_t ReadOffset(const uint8_t* p, int w, int64_t r) {
   if (w == 8) {
@@ -62,7 +64,9 @@ Status PartitionReader::Cuda(cudaError_t e, const char* what) {
 Status PartitionReader::Make(std::vector<Field> fields, int device, std::unique_ptr<PartitionReader>* out) {
   std::unique_ptr<PartitionReader> r(new PartitionReader());
   for (const Field& f : fields) {
-    if (f.type != GZ_TYPE_NULL && f.type != GZ_TYPE_BOOL && !IsBinaryType(f.type) && FixedWidth(f.type) == 0)
+    if (f.type == GZ_TYPE_LIST ? FixedWidth(f.elem) == 0
+                               : f.type != GZ_TYPE_NULL && f.type != GZ_TYPE_BOOL && !IsBinaryType(f.type) &&
+                                     FixedWidth(f.type) == 0)
       return Status::Error(GZ_NOT_IMPLEMENTED, "field type not implemented by the reader");
   }
   r->fields_ = std::move(fields);
@@ -189,6 +193,30 @@ Status PartitionReader::ParseStream(const uint8_t* data, int64_t len, int stream
         c.null_count = nn;
         const int t = fields_[f].type;
         if (t == GZ_TYPE_NULL) continue;  // no buffers
+        if (t == GZ_TYPE_LIST) {
+          // the element node follows the list's; buffers [validity, offsets, element validity, values]
+          int64_t cl, cn;
+          if (node >= n_nodes || !r.Get(nodes + 4 + 16 * (int64_t)node, &cl) ||
+              !r.Get(nodes + 4 + 16 * (int64_t)node + 8, &cn))
+            return Status::Error(GZ_INVALID, "list without an element node");
+          node++;
+          c.child_nulls = cn;
+          if (!(next_buf(&c.validity) && next_buf(&c.offsets) && next_buf(&c.cvalidity) && next_buf(&c.values)))
+            return Status::Error(GZ_INVALID, "bad buffer list in a record batch");
+          if ((nn > 0 && c.validity.length < (b.rows + 7) / 8) || (cn > 0 && c.cvalidity.length < (cl + 7) / 8))
+            return Status::Error(GZ_INVALID, "validity buffer too short");
+          if (nn == 0) c.validity.length = 0;
+          if (cn == 0) c.cvalidity.length = 0;
+          if (c.offsets.length < (b.rows + 1) * 4) return Status::Error(GZ_INVALID, "offsets buffer too short");
+          const int w = FixedWidth(fields_[f].elem);
+          if (!c.offsets.decoded) {
+            c.o0 = ReadOffset(data + c.offsets.offset, 4, 0);
+            c.o1 = ReadOffset(data + c.offsets.offset, 4, b.rows);
+            if (c.o0 < 0 || c.o1 < c.o0 || c.o1 * w > c.values.length || c.o1 - c.o0 != cl)
+              return Status::Error(GZ_INVALID, "list offsets exceed the elements");
+          }
+          continue;
+        }
         bool ok = next_buf(&c.validity);
         if (IsBinaryType(t)) ok = ok && next_buf(&c.offsets);
         ok = ok && next_buf(&c.values);
@@ -285,7 +313,7 @@ Status PartitionReader::AddStream(const uint8_t* data, int64_t len) {
     for (size_t bi = 0; bi < bs.size(); bi++)
       for (size_t f = 0; f < fields_.size(); f++) {
         const ColRef& c = bs[bi].cols[f];
-        if (!IsBinaryType(fields_[f].type) || !c.offsets.decoded) continue;
+        if (!HasOffsets(fields_[f].type) || !c.offsets.decoded) continue;
         const int32_t* o = reinterpret_cast<const int32_t*>(arenas_.back() + c.offsets.offset);
         if (IsLargeBinaryType(fields_[f].type)) {
           where.push_back(o);
@@ -315,7 +343,8 @@ Status PartitionReader::AddStream(const uint8_t* data, int64_t len) {
         c.o1 = ends[e + 1];
         e += 2;
       }
-      if (c.o0 < 0 || c.o1 < c.o0 || c.o1 > c.values.length) return Status::Error(GZ_INVALID, "offsets exceed the characters");
+      const int64_t w = fields_[which[i].second].type == GZ_TYPE_LIST ? FixedWidth(fields_[which[i].second].elem) : 1;
+      if (c.o0 < 0 || c.o1 < c.o0 || c.o1 * w > c.values.length) return Status::Error(GZ_INVALID, "offsets exceed the characters");
     }
     arena_mem_.push_back(arena);
   } else {
@@ -335,8 +364,8 @@ Status PartitionReader::Finish(int64_t* rows, int32_t* n_batches) {
   for (const Batch& b : batches_) R += b.rows;
   if (R >= (1ll << 31)) return Status::Error(GZ_INVALID, "more than 2^31 - 1 rows in one partition");
   // output layout: per field validity (when some batch has nulls), offsets, values / characters
-  std::vector<size_t> o_valid(F, SIZE_MAX), o_off(F, SIZE_MAX), o_val(F, SIZE_MAX);
-  std::vector<int64_t> chars(F, 0);
+  std::vector<size_t> o_valid(F, SIZE_MAX), o_off(F, SIZE_MAX), o_val(F, SIZE_MAX), o_cvalid(F, SIZE_MAX);
+  std::vector<int64_t> chars(F, 0);  // binary: characters; list: elements
   size_t total = 0;
   const size_t bit_bytes = AlignUp((size_t)((R + 31) / 32) * 4, 256);
   for (size_t f = 0; f < F; f++) {
@@ -349,7 +378,8 @@ Status PartitionReader::Finish(int64_t* rows, int32_t* n_batches) {
     }
     for (const Batch& b : batches_) {
       oc.null_count += b.cols[f].null_count;
-      if (IsBinaryType(t)) chars[f] += b.cols[f].o1 - b.cols[f].o0;
+      oc.child_null_count += b.cols[f].child_nulls;
+      if (HasOffsets(t)) chars[f] += b.cols[f].o1 - b.cols[f].o0;
     }
     if (chars[f] >= (1ll << 31) && !IsLargeBinaryType(t))
       return Status::Error(GZ_INVALID, "more than 2^31 - 1 characters in one column");
@@ -357,14 +387,19 @@ Status PartitionReader::Finish(int64_t* rows, int32_t* n_batches) {
       o_valid[f] = total;
       total += bit_bytes;
     }
-    if (IsBinaryType(t)) {
+    if (HasOffsets(t)) {
       o_off[f] = total;
       total += AlignUp((size_t)(R + 1) * OffsetWidth(t), 256);
+    }
+    if (t == GZ_TYPE_LIST && oc.child_null_count > 0) {
+      o_cvalid[f] = total;
+      total += AlignUp((size_t)((chars[f] + 31) / 32) * 4, 256);
     }
     o_val[f] = total;
     total += t == GZ_TYPE_BOOL ? bit_bytes
              : IsBinaryType(t) ? AlignUp((size_t)chars[f] + 16, 256)
-                               : AlignUp((size_t)R * FixedWidth(t), 256);
+             : t == GZ_TYPE_LIST ? AlignUp((size_t)chars[f] * FixedWidth(fields_[f].elem), 256)
+                                 : AlignUp((size_t)R * FixedWidth(t), 256);
   }
   total = std::max<size_t>(total, 256);
   st = Cuda(cudaMallocAsync(reinterpret_cast<void**>(&out_mem_), total, stream_), "cudaMallocAsync(columns)");
@@ -413,6 +448,26 @@ Status PartitionReader::Finish(int64_t* rows, int32_t* n_batches) {
                                  ow == 8 ? 1u : 0u, add});
         add_bytes(Base(c.values, b.stream) + c.o0, out_mem_ + o_val[f] + char_pos[f], (uint64_t)(c.o1 - c.o0));
         char_pos[f] += c.o1 - c.o0;
+      } else if (t == GZ_TYPE_LIST) {
+        // offsets rebased onto the elements of the earlier batches; the elements' values and
+        // validity bits moved to their position (a batch without element nulls adds ones)
+        const uint8_t* src_off = Base(c.offsets, b.stream);
+        uint8_t* dst_off = out_mem_ + o_off[f] + (size_t)row * 4;
+        const uint64_t n = (uint64_t)b.rows + (last ? 1 : 0);
+        for (uint64_t x = 0; x < n; x += kChunk / 4)
+          oj.push_back(OffsetJob{src_off + x * 4, dst_off + x * 4, (uint32_t)std::min<uint64_t>(kChunk / 4, n - x), 0u,
+                                 char_pos[f] - c.o0});
+        const int w = FixedWidth(fields_[f].elem);
+        add_bytes(Base(c.values, b.stream) + c.o0 * w, out_mem_ + o_val[f] + char_pos[f] * w,
+                  (uint64_t)(c.o1 - c.o0) * w);
+        if (o_cvalid[f] != SIZE_MAX && c.o1 > c.o0) {
+          const uint8_t* cv = c.cvalidity.length ? Base(c.cvalidity, b.stream) : nullptr;
+          for (uint64_t x = 0; x < (uint64_t)(c.o1 - c.o0); x += kBitChunk)
+            tj.push_back(BitJob{reinterpret_cast<const uint32_t*>(cv), reinterpret_cast<uint32_t*>(out_mem_ + o_cvalid[f]),
+                                cv ? (uint64_t)c.o0 + x : 0, (uint64_t)char_pos[f] + x,
+                                std::min<uint64_t>(kBitChunk, (uint64_t)(c.o1 - c.o0) - x)});
+        }
+        char_pos[f] += c.o1 - c.o0;
       } else {
         const int w = FixedWidth(t);
         add_bytes(Base(c.values, b.stream), out_mem_ + o_val[f] + (size_t)row * w, (uint64_t)b.rows * w);
@@ -455,7 +510,12 @@ Status PartitionReader::Finish(int64_t* rows, int32_t* n_batches) {
     if (o_valid[f] != SIZE_MAX) oc.validity = out_mem_ + o_valid[f];
     if (o_off[f] != SIZE_MAX) oc.offsets = out_mem_ + o_off[f];
     oc.values = out_mem_ + o_val[f];
-    oc.values_bytes = t == GZ_TYPE_BOOL ? (R + 7) / 8 : IsBinaryType(t) ? chars[f] : R * FixedWidth(t);
+    oc.values_bytes = t == GZ_TYPE_BOOL ? (R + 7) / 8 : IsBinaryType(t) ? chars[f]
+                      : t == GZ_TYPE_LIST ? chars[f] * FixedWidth(fields_[f].elem) : R * FixedWidth(t);
+    if (t == GZ_TYPE_LIST) {
+      oc.child_length = chars[f];
+      if (o_cvalid[f] != SIZE_MAX) oc.child_validity = out_mem_ + o_cvalid[f];
+    }
   }
   rows_ = R;
   finished_ = true;
@@ -476,7 +536,23 @@ Status PartitionReader::Column(int field, GzDeviceColumn* out) const {
   out->offsets = c.offsets;
   out->values = c.values;
   out->values_bytes = c.values_bytes;
+  out->child_validity = c.child_validity;
+  out->child_length = c.child_length;
+  out->child_null_count = c.child_null_count;
   return Status::OK();
+}
+
+Status PartitionReader::ElemValidityToHost(int field, uint8_t* out) {
+  GzDeviceColumn c;
+  Status st = Column(field, &c);
+  if (!st.ok()) return st;
+  if (!out || !c.child_validity) return Status::OK();
+  st = Cuda(cudaSetDevice(device_), "cudaSetDevice");
+  if (!st.ok()) return st;
+  st = Cuda(cudaMemcpyAsync(out, c.child_validity, (size_t)(c.child_length + 7) / 8, cudaMemcpyDeviceToHost, stream_),
+            "D2H");
+  if (!st.ok()) return st;
+  return Cuda(cudaStreamSynchronize(stream_), "D2H");
 }
 
 Status PartitionReader::ColumnToHost(int field, uint8_t* validity, void* offsets, uint8_t* values) {

@@ -36,6 +36,7 @@ class PartitionReader {
   Status Finish(int64_t* rows, int32_t* batches);
   Status Column(int field, GzDeviceColumn* out) const;
   Status ColumnToHost(int field, uint8_t* validity, void* offsets, uint8_t* values);
+  Status ElemValidityToHost(int field, uint8_t* out);
 
  private:
   struct BufRef {
@@ -49,7 +50,9 @@ class PartitionReader {
   struct ColRef {
     int64_t null_count = 0;
     BufRef validity, offsets, values;
-    int64_t o0 = 0, o1 = 0;  // binary: first and last offset (the batch's characters)
+    int64_t o0 = 0, o1 = 0;  // binary: first and last offset (the batch's characters; list: elements)
+    BufRef cvalidity;        // list: element validity
+    int64_t child_nulls = 0;
   };
   struct Batch {
     int stream = 0;
@@ -62,6 +65,8 @@ class PartitionReader {
     uint8_t* offsets = nullptr;  // int32 or int64 (large types) offsets
     uint8_t* values = nullptr;
     int64_t values_bytes = 0;
+    uint8_t* child_validity = nullptr;  // list: element validity
+    int64_t child_length = 0, child_null_count = 0;
   };
 
   PartitionReader() = default;

@@ -61,6 +61,23 @@ bool ParseSchemaIpc(const uint8_t* data, int64_t len, std::vector<Field>* out, s
     f.nullable = r.Scalar<uint8_t>(ft, 1, 0) != 0;
     uint8_t tt = r.Scalar<uint8_t>(ft, 2, 0);
     int64_t tp = r.Table(ft, 3);
+    const bool list = tt == 12;
+    if (list) {  // List: its one child field is the element (its type is decoded below)
+      int64_t ch = r.Table(ft, 5);
+      uint32_t nch = 0;
+      if (ch < 0 || !r.Get(ch, &nch) || nch != 1) {
+        *err = "list field without one element field";
+        return false;
+      }
+      const int64_t et = r.Deref(ch + 4);
+      if (et < 0 || !r.String(et, 0, &f.elem_name)) {
+        *err = "bad list element field";
+        return false;
+      }
+      f.elem_nullable = r.Scalar<uint8_t>(et, 1, 0) != 0;
+      tt = r.Scalar<uint8_t>(et, 2, 0);
+      tp = r.Table(et, 3);
+    }
     switch (tt) {
       case 1: f.type = GZ_TYPE_NULL; break;
       case 2: {
@@ -115,6 +132,14 @@ bool ParseSchemaIpc(const uint8_t* data, int64_t len, std::vector<Field>* out, s
       default:
         *err = "field type " + std::to_string(tt) + " is not implemented by the GPU splitter";
         return false;
+    }
+    if (list) {
+      if (f.type == GZ_TYPE_NULL || f.type == GZ_TYPE_BOOL || f.type >= GZ_TYPE_STRING) {
+        *err = "list elements of a fixed-width type only";
+        return false;
+      }
+      f.elem = f.type;
+      f.type = GZ_TYPE_LIST;
     }
     out->push_back(f);
   }
@@ -257,6 +282,7 @@ uint8_t TypeTable(Builder& b, const Field& f, uint32_t* table) {
     case GZ_TYPE_STRING: *table = empty(); return 5;
     case GZ_TYPE_LARGE_BINARY: *table = empty(); return 19;  // Schema.fbs Type.LargeBinary
     case GZ_TYPE_LARGE_STRING: *table = empty(); return 20;  // Type.LargeUtf8
+    case GZ_TYPE_LIST: *table = empty(); return 12;           // Type.List (its element: a child field)
     case GZ_TYPE_DECIMAL128:  // Decimal { precision, scale, bitWidth = 128 }
       b.StartTable();
       b.AddScalar<int32_t>(8, 128, 128);
@@ -291,22 +317,42 @@ uint8_t TypeTable(Builder& b, const Field& f, uint32_t* table) {
 
 }  // namespace
 
+namespace {
+
+// One Field table: a list's element field first (its own Field table), then the type, the name,
+// the children vector and the Field table itself.
+uint32_t FieldTable(Builder& b, const Field& f) {
+  std::vector<uint32_t> kids;
+  if (f.type == GZ_TYPE_LIST) {
+    Field e;
+    e.type = f.elem;
+    e.nullable = f.elem_nullable;
+    e.precision = f.precision;
+    e.scale = f.scale;
+    e.unit = f.unit;
+    e.timezone = f.timezone;
+    e.name = f.elem_name;
+    kids.push_back(FieldTable(b, e));
+  }
+  uint32_t type_table = 0;
+  const uint8_t tag = TypeTable(b, f, &type_table);  // type first, then name, then children
+  const uint32_t name = b.String(f.name);
+  const uint32_t children = b.OffsetVector(kids);
+  b.StartTable();  // Field { name, nullable, type_type, type, dictionary, children, custom_metadata }
+  b.AddOffset(14, children);
+  b.AddOffset(10, type_table);
+  b.AddOffset(4, name);
+  b.AddScalar<uint8_t>(8, tag, 0);
+  b.AddScalar<uint8_t>(6, f.nullable ? 1 : 0, 0);
+  return b.EndTable();
+}
+
+}  // namespace
+
 std::vector<uint8_t> EncodeSchemaMessage(const std::vector<Field>& fields) {
   Builder b;
   std::vector<uint32_t> offs;
-  for (const Field& f : fields) {
-    uint32_t type_table = 0;
-    const uint8_t tag = TypeTable(b, f, &type_table);  // type first, then name, then children
-    const uint32_t name = b.String(f.name);
-    const uint32_t children = b.OffsetVector({});
-    b.StartTable();  // Field { name, nullable, type_type, type, dictionary, children, custom_metadata }
-    b.AddOffset(14, children);
-    b.AddOffset(10, type_table);
-    b.AddOffset(4, name);
-    b.AddScalar<uint8_t>(8, tag, 0);
-    b.AddScalar<uint8_t>(6, f.nullable ? 1 : 0, 0);
-    offs.push_back(b.EndTable());
-  }
+  for (const Field& f : fields) offs.push_back(FieldTable(b, f));
   const uint32_t vec = b.OffsetVector(offs);
   b.StartTable();  // Schema { endianness = Little, fields, custom_metadata, features }
   b.AddOffset(6, vec);

@@ -14,6 +14,10 @@ struct Field {
   int unit = 0;
   std::string name;
   std::string timezone;  // timestamp only; empty: none
+  // list: the element field (a fixed-width type; its precision / scale / unit are the ones above)
+  int elem = 0;
+  std::string elem_name = "item";
+  bool elem_nullable = true;
 };
 
 // Parses an Arrow IPC Schema message (encapsulated or legacy framing).

@@ -169,21 +169,29 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
   if (opts_.flush_bytes > (1ll << 30)) opts_.flush_bytes = 1ll << 30;
   if (opts_.seg_tiles > kMaxSegTiles) opts_.seg_tiles = kMaxSegTiles;
 
-  // Splitter::Init column classification (splitter.cc:246-269)
-  std::vector<int32_t> bin;
+  // Splitter::Init column classification (splitter.cc:246-269); list columns
+  // (list_array_idx_, :254-258) follow the binary ones here, outside the buffer policy's columns
+  std::vector<int32_t> bin, lists;
   field_array_.assign(fields_.size(), -1);
   for (size_t i = 0; i < fields_.size(); i++) {
     const int t = fields_[i].type;
     if ((int)i == pid_field_) continue;  // not an output column
     if (IsBinary(t)) bin.push_back((int32_t)i);
     else if (t == GZ_TYPE_NULL) continue;
-    else if (t == GZ_TYPE_BOOL || ByteWidth(t) > 0) array_idx_.push_back((int32_t)i);
+    else if (t == GZ_TYPE_LIST) {
+      if (ByteWidth(fields_[i].elem) <= 0)
+        return Status::Error(GZ_NOT_IMPLEMENTED, "list columns of fixed-width elements only");
+      lists.push_back((int32_t)i);
+    } else if (t == GZ_TYPE_BOOL || ByteWidth(t) > 0) array_idx_.push_back((int32_t)i);
     else return Status::Error(GZ_NOT_IMPLEMENTED, "field type not implemented in ColumnarShuffle");
   }
   fixed_cnt_ = (int32_t)array_idx_.size();
   array_idx_.insert(array_idx_.end(), bin.begin(), bin.end());
+  n_bin_ = (int32_t)bin.size();
+  n_policy_ = (int32_t)array_idx_.size();
+  array_idx_.insert(array_idx_.end(), lists.begin(), lists.end());
   n_array_ = (int32_t)array_idx_.size();
-  n_str_ = (int32_t)bin.size();
+  n_str_ = (int32_t)(bin.size() + lists.size());
   if (n_array_ == 0) return Status::Error(GZ_NOT_IMPLEMENTED, "schema without data columns");
   if (n_array_ > kMaxCols) return Status::Error(GZ_NOT_IMPLEMENTED, "more than 64 data columns");
   if (n_str_ > max_str_columns()) return Status::Error(GZ_NOT_IMPLEMENTED, "more than 32 binary columns");
@@ -204,11 +212,18 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
     field_array_[ci] = a;
     const int t = fields_[ci].type;
     sd_.arr_col[a] = ci;
-    sd_.arr_kind[a] = IsBinary(t) ? COL_BINARY : t == GZ_TYPE_BOOL ? COL_BOOL : COL_FIXED;
-    sd_.arr_width[a] = IsBinary(t) ? OffW(t) : ByteWidth(t);  // binary: offset bytes
+    const bool list = t == GZ_TYPE_LIST;
+    sd_.arr_kind[a] = IsBinary(t) || list ? COL_BINARY : t == GZ_TYPE_BOOL ? COL_BOOL : COL_FIXED;
+    sd_.arr_width[a] = IsBinary(t) ? OffW(t) : list ? 4 : ByteWidth(t);  // binary / list: offset bytes
     sd_.arr_str[a] = a >= fixed_cnt_ ? a - fixed_cnt_ : -1;
+    if (list) {
+      int sh = 0;
+      while ((1 << sh) < ByteWidth(fields_[ci].elem)) sh++;
+      sd_.arr_shift[a] = sh;
+      sd_.list_mask |= 1ull << a;
+    }
     // compared as an index of the output schema (the range partitioner's ids are not in it)
-    if (ci - out_shift() < fixed_cnt_) sd_.quirk_mask |= 1ull << a;
+    if (a < n_policy_ && ci - out_shift() < fixed_cnt_) sd_.quirk_mask |= 1ull << a;
   }
   // k_scatter processing order: binary columns spread evenly among the fixed ones, so the
   // characters of the next binary column stream in while fixed columns are scattered
@@ -262,10 +277,10 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
   int nb = 0;
   for (size_t i = 0; i < fields_.size(); i++) {
     field_buf0_[i] = nb;
-    nb += IsBinary(fields_[i].type) ? 3 : 2;
+    nb += fields_[i].type == GZ_TYPE_LIST ? 4 : IsBinary(fields_[i].type) ? 3 : 2;
   }
   n_bufs_expected_ = nb;
-  empirical_.assign(n_str_, 0);
+  empirical_.assign(n_bin_, 0);
 
   device_ = opts_.device;
   GzStatus dummy;
@@ -383,7 +398,7 @@ Splitter::~Splitter() {
 // batch's offset buffers per binary column, readable on the host.
 uint32_t Splitter::SplitBatchSize(int32_t num_rows, const std::vector<const uint8_t*>& host_offsets,
                                   bool* complete) {
-  for (int k = 0; k < n_str_; k++) {
+  for (int k = 0; k < n_bin_; k++) {
     if (empirical_[k] == 0 && host_offsets[k] != nullptr && num_rows > 0) {
       // the character bytes of the batch: int32 offsets subtract as int32, int64 as int64
       const int w = sd_.arr_width[fixed_cnt_ + k];
@@ -393,11 +408,11 @@ uint32_t Splitter::SplitBatchSize(int32_t num_rows, const std::vector<const uint
     }
   }
   *complete = true;
-  for (int k = 0; k < n_str_; k++)
+  for (int k = 0; k < n_bin_; k++)
     if (empirical_[k] == 0) *complete = false;
   uint32_t size_per_row = 0;
-  for (int k = 0; k < n_str_; k++) size_per_row += (uint32_t)empirical_[k];
-  for (int a = 0; a < n_array_; a++) {
+  for (int k = 0; k < n_bin_; k++) size_per_row += (uint32_t)empirical_[k];
+  for (int a = 0; a < n_policy_; a++) {
     const int ci = array_idx_[a];
     if (ci - out_shift() < fixed_cnt_) {  // an index of the output schema, as in the reference
       const int t = fields_[ci].type;
@@ -537,7 +552,7 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
   const size_t C = fields_.size();
 
   // validate and size every buffer that is read
-  uint64_t validity_mask = 0;
+  uint64_t validity_mask = 0, cvalid_mask = 0;
   size_t batch_bytes = 0;
   for (int k = 0; k < n_str_; k++) host_off_[k] = nullptr;
   for (size_t f = 0; f < C; f++) {
@@ -590,6 +605,37 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
         char_scratch_[k] = (uint64_t)cb;
       }
       if (cb > 0) need_[vi] = Need{reinterpret_cast<const uint8_t*>(addrs[vi]), cb};
+    } else if (t == GZ_TYPE_LIST) {
+      // [validity, int32 offsets, element validity, element values] (jni_common.h:190-226)
+      need_[b0 + 2] = Need{nullptr, 0};
+      need_[b0 + 3] = Need{nullptr, 0};
+      const size_t ob = (size_t)(nr + 1) * 4;
+      if (addrs[b0 + 1] == 0 || (size_t)sizes[b0 + 1] < ob)
+        return Status::Error(GZ_INVALID, "list offsets buffer too small");
+      need_[b0 + 1] = Need{reinterpret_cast<const uint8_t*>(addrs[b0 + 1]), ob};
+      const int k = a - fixed_cnt_;
+      const int w = ByteWidth(fields_[f].elem);
+      const int64_t vsz = std::max<int64_t>(sizes[b0 + 3], 0);
+      if (vsz > (int64_t)INT32_MAX)
+        return Status::Error(GZ_NOT_IMPLEMENTED, "a list column batch with more than 2^31 - 1 element bytes");
+      size_t vb = (size_t)vsz, eb = (size_t)std::max<int64_t>(sizes[b0 + 2], 0);
+      if (host_in) {
+        const int32_t* off = reinterpret_cast<const int32_t*>(addrs[b0 + 1]);
+        const int64_t o0 = off[0], o1 = off[nr];
+        if (o1 < o0 || o0 < 0 || o1 * w > vsz) return Status::Error(GZ_INVALID, "list offsets exceed the element values");
+        if (addrs[b0 + 2] != 0 && eb > 0 && (int64_t)eb < BytesForBits(o1))
+          return Status::Error(GZ_INVALID, "element validity buffer too small");
+        vb = (size_t)(o1 * w);
+        eb = eb > 0 ? (size_t)BytesForBits(o1) : 0;
+        char_scratch_[k] = (uint64_t)((o1 - o0) * w);
+      } else {
+        char_scratch_[k] = (uint64_t)vb;
+      }
+      if (addrs[b0 + 2] != 0 && eb > 0) {
+        need_[b0 + 2] = Need{reinterpret_cast<const uint8_t*>(addrs[b0 + 2]), eb};
+        cvalid_mask |= 1ull << a;
+      }
+      if (vb > 0) need_[b0 + 3] = Need{reinterpret_cast<const uint8_t*>(addrs[b0 + 3]), vb};
     } else {
       const size_t vbytes = t == GZ_TYPE_BOOL ? (size_t)BytesForBits(nr) : (size_t)nr * ByteWidth(t);
       if (addrs[b0 + 1] == 0 || (size_t)sizes[b0 + 1] < vbytes)
@@ -607,13 +653,13 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
   // from each later batch in which some partition reaches the function (splitter.cc:804-835).
   bool probe_call = false;
   std::vector<uint64_t> empirical_before;
-  if (opts_.offheap_per_task > 0 && n_str_ > 0) {
+  if (opts_.offheap_per_task > 0 && n_bin_ > 0) {
     bool missing = false;
-    for (int k = 0; k < n_str_; k++) missing |= empirical_[k] == 0;
+    for (int k = 0; k < n_bin_; k++) missing |= empirical_[k] == 0;
     if (missing && !host_in) {
       st = Cuda(cudaStreamSynchronize(stream_), "sync");
       if (!st.ok()) return st;
-      for (int k = 0; k < n_str_; k++) {
+      for (int k = 0; k < n_bin_; k++) {
         const int f = array_idx_[fixed_cnt_ + k];
         const int ow = sd_.arr_width[fixed_cnt_ + k];
         const uint8_t* doff = reinterpret_cast<const uint8_t*>(addrs[field_buf0_[f] + 1]);
@@ -683,7 +729,8 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
       if (a >= 0 || (int)f == pid_field_) {
         const int t = fields_[f].type;
         const int b0 = field_buf0_[f];
-        const int nbuf = IsBinary(t) ? 3 : 2;
+        const bool list = t == GZ_TYPE_LIST;
+        const int nbuf = list ? 4 : IsBinary(t) ? 3 : 2;
         for (int j = 0; j < nbuf; j++) {
           const Need& nd = need_[b0 + j];
           if (nd.bytes == 0) continue;
@@ -691,7 +738,9 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
           if (direct_) {
             // same 16-byte phase as the source when that keeps the elements aligned
             const uintptr_t sp = reinterpret_cast<uintptr_t>(nd.src);
-            const uintptr_t elem = j == 0 ? 1 : IsBinary(t) ? (j == 1 ? (uintptr_t)OffW(t) : 1)
+            const uintptr_t elem = j == 0 ? 1
+                                 : list ? (j == 1 ? 4 : j == 2 ? 1 : (uintptr_t)ByteWidth(fields_[f].elem))
+                                 : IsBinary(t) ? (j == 1 ? (uintptr_t)OffW(t) : 1)
                                  : t == GZ_TYPE_BOOL ? 1 : (uintptr_t)ByteWidth(t);
             if (sp % elem == 0) phase = sp & 15;
             h_jobs_[jobs_end_++] = HostCopy{nd.src, d_stage_[cur_] + used_ + phase, nd.bytes};
@@ -702,13 +751,14 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
           const uint8_t* dptr = d_stage_[cur_] + used_ + phase;
           used_ += AlignUp(phase + nd.bytes, 64);
           if (j == 0) cp.validity = dptr;
-          else if (IsBinary(t) && j == 1) cp.offsets = reinterpret_cast<const int32_t*>(dptr);
+          else if ((IsBinary(t) || list) && j == 1) cp.offsets = reinterpret_cast<const int32_t*>(dptr);
+          else if (list && j == 2) cp.child_validity = dptr;
           else {
             cp.values = dptr;
             cp.values_bytes = nd.bytes;
           }
         }
-        if (IsBinary(t) && cp.values == nullptr) cp.values = d_stage_[cur_];  // all strings empty
+        if ((IsBinary(t) || list) && cp.values == nullptr) cp.values = d_stage_[cur_];  // all empty
       }
       cols[f] = cp;
     }
@@ -736,6 +786,15 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
           cp.values_bytes = (uint64_t)std::max<int64_t>(sizes[b0 + 2], 0);
           if (reinterpret_cast<uintptr_t>(cp.offsets) % (uintptr_t)OffW(t))
             return Status::Error(GZ_INVALID, "device offsets buffer must be aligned to its offset width");
+        } else if (t == GZ_TYPE_LIST) {
+          cp.offsets = reinterpret_cast<const int32_t*>(addrs[b0 + 1]);
+          if (addrs[b0 + 2] != 0 && sizes[b0 + 2] > 0) cp.child_validity = reinterpret_cast<const uint8_t*>(addrs[b0 + 2]);
+          cp.values = reinterpret_cast<const uint8_t*>(addrs[b0 + 3]);
+          cp.values_bytes = (uint64_t)std::max<int64_t>(sizes[b0 + 3], 0);
+          if (reinterpret_cast<uintptr_t>(cp.offsets) % 4 ||
+              reinterpret_cast<uintptr_t>(cp.values) % (uintptr_t)ByteWidth(fields_[f].elem))
+            return Status::Error(GZ_INVALID, "device list buffers must be aligned to their widths");
+          if (cp.values == nullptr) cp.values = reinterpret_cast<const uint8_t*>(addrs[b0 + 1]);  // no elements
         } else {
           cp.values = need_[b0 + 1].src;
           const int w = t == GZ_TYPE_BOOL ? 1 : ByteWidth(t);
@@ -751,7 +810,7 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
   stat_input_bytes_ += (int64_t)batch_bytes;
   stat_batches_++;
   stat_rows_ += nr;
-  pending_.push_back(PendingBatch{nr, split_size, validity_mask});
+  pending_.push_back(PendingBatch{nr, split_size, validity_mask, cvalid_mask});
   if (probe_call) {
     st = Flush();
     if (!st.ok()) return st;
@@ -857,8 +916,12 @@ Status Splitter::Flush() {
   fr.off_bits.assign(A, SIZE_MAX);
   fr.off_valid.assign(A, SIZE_MAX);
   fr.off_chars.assign(A, SIZE_MAX);
-  uint64_t any_valid = 0;
-  for (auto& pb : pending_) any_valid |= pb.validity_mask;
+  fr.off_cvalid.assign(A, SIZE_MAX);
+  uint64_t any_valid = 0, any_cvalid = 0;
+  for (auto& pb : pending_) {
+    any_valid |= pb.validity_mask;
+    any_cvalid |= pb.cvalid_mask;
+  }
   size_t o = 0;
   for (int a = 0; a < A; a++) {
     const int kind = sd_.arr_kind[a];
@@ -883,6 +946,12 @@ Status Splitter::Flush() {
     if (any_valid & (1ull << a)) {
       fr.off_valid[a] = o;
       o += vwords_bytes;
+    }
+    if (any_cvalid & (1ull << a)) {  // one bit per element byte group of the column's characters
+      uint64_t cb = 0;
+      for (uint32_t b = 0; b < NB; b++) cb += pending_chars_[(size_t)b * n_str_ + sd_.arr_str[a]];
+      fr.off_cvalid[a] = o;
+      o += AlignUp((size_t)(((cb >> sd_.arr_shift[a]) + 31) / 32 * 4) + 8, 256);
     }
   }
   const size_t bits_end = o;
@@ -971,6 +1040,7 @@ Status Splitter::Flush() {
     if (fr.off_bits[a] != SIZE_MAX) fd.out_bits[a] = reinterpret_cast<uint32_t*>(fr.d_out + fr.off_bits[a]);
     if (fr.off_valid[a] != SIZE_MAX) fd.out_valid[a] = reinterpret_cast<uint32_t*>(fr.d_out + fr.off_valid[a]);
     if (fr.off_chars[a] != SIZE_MAX) fd.out_chars[a] = fr.d_out + fr.off_chars[a];
+    if (fr.off_cvalid[a] != SIZE_MAX) fd.out_cvalid[a] = reinterpret_cast<uint32_t*>(fr.d_out + fr.off_cvalid[a]);
   }
   fd.st_cap = st_cap_;
   fd.st_base = st_base_;
@@ -1418,6 +1488,60 @@ Status Splitter::BuildSegment(int p, const Segment& s, SegMsg* msg, bool device_
     const int a = field_array_[fi];
     if (a < 0) {
       nodes.push_back(FieldNodeMeta{n, n});
+      continue;
+    }
+    if ((sd_.list_mask >> a) & 1ull) {
+      // a list column, as its partition's ListBuilder finishes it (CacheRecordBatch,
+      // splitter.cc:532-545): list node and buffers [validity, offsets], then the element node
+      // and [validity, values]; each bitmap zero-padded and written only when it holds a null
+      const int k = sd_.arr_str[a];
+      const int sh = sd_.arr_shift[a];
+      int64_t lnulls = 0;
+      ChunkedBuffer lvb;
+      {
+        bool ones = true;
+        const uint8_t* bits = gather_bits(&FlushRec::off_valid, a, &ones);
+        if (!ones && (lnulls = CountZeros(bits, n)) > 0) {
+          temps.emplace_back(bits, bits + BytesForBits(n));
+          if (n & 7) temps.back().back() &= (uint8_t)((1u << (n & 7)) - 1);
+          lvb.push_back(Chunk{temps.back().data(), BytesForBits(n)});
+        }
+      }
+      ChunkedBuffer offs, vals;
+      offs.push_back(Chunk{kZero8, 4});
+      uint64_t elems = 0;
+      for (const Piece& pc : s.pieces) elems += (pc.fb1[k] - pc.fb0[k]) >> sh;
+      temps.emplace_back((size_t)BytesForBits((int64_t)elems), 0);
+      uint8_t* ev = temps.back().data();
+      uint64_t erow = 0;
+      for (const Piece& pc : s.pieces) {
+        const FlushRec& f = flushes_[pc.flush];
+        bool dev;
+        const uint8_t* fb = body_base(f, &dev);
+        offs.push_back(Chunk{fb + f.off_values[a] + ((size_t)f.pstart(P)[p] + pc.frow0) * 4,
+                             (int64_t)(pc.frow1 - pc.frow0) * 4, dev});
+        const uint32_t c0 = pc.fb0[k], c1 = pc.fb1[k];
+        const size_t cb = (size_t)f.cstart(P, nstr)[(size_t)k * P + p] + c0;
+        if (c1 > c0) vals.push_back(Chunk{fb + f.off_chars[a] + cb, (int64_t)(c1 - c0), dev});
+        const uint64_t m = (c1 - c0) >> sh;
+        if (f.off_cvalid[a] != SIZE_MAX) {
+          CopyBits(bit_base(f, f.off_cvalid[a]), cb >> sh, ev, erow, m);
+        } else {
+          for (uint64_t i = erow; i < erow + m; i++) ev[i >> 3] |= (uint8_t)(1u << (i & 7));
+        }
+        erow += m;
+      }
+      const int64_t cnulls = CountZeros(ev, (int64_t)elems);
+      ChunkedBuffer cvb;
+      if (cnulls > 0) cvb.push_back(Chunk{ev, BytesForBits((int64_t)elems)});
+      nodes.push_back(FieldNodeMeta{n, lnulls});
+      nodes.push_back(FieldNodeMeta{(int64_t)elems, cnulls});
+      bufs.push_back(lvb);
+      bufs.push_back(offs);
+      bufs.push_back(cvb);
+      bufs.push_back(vals);
+      // batch_nbytes: the list's own buffers (splitter.cc:438-453)
+      rawb += (lnulls > 0 ? BytesForBits(n) : 0) + (int64_t)(n + 1) * 4;
       continue;
     }
     const int kind = sd_.arr_kind[a];
@@ -1957,6 +2081,19 @@ Status Splitter::CompressedSize(int32_t num_rows, const int64_t* addrs, const in
     const int b0 = field_buf0_[f];
     const uint8_t* vb = reinterpret_cast<const uint8_t*>(addrs[b0]);
     bufs.push_back({vb, addrs[b0] != 0 && sizes[b0] > 0 && nr > 0 && CountZeros(vb, nr) > 0 ? BytesForBits(nr) : 0});
+    if (t == GZ_TYPE_LIST) {  // offsets, then the element array (validity only with nulls)
+      const int32_t* off = reinterpret_cast<const int32_t*>(addrs[b0 + 1]);
+      bufs.push_back({reinterpret_cast<const uint8_t*>(off), (int64_t)(nr + 1) * 4});
+      const int64_t e0 = nr > 0 && off ? off[0] : 0, e1 = nr > 0 && off ? off[nr] : 0;
+      const uint8_t* ev = reinterpret_cast<const uint8_t*>(addrs[b0 + 2]);
+      bool enull = false;
+      if (ev && sizes[b0 + 2] > 0)
+        for (int64_t e = e0; e < e1 && !enull; e++) enull = !((ev[e >> 3] >> (e & 7)) & 1);
+      bufs.push_back({ev, enull ? BytesForBits(e1 - e0) : 0});
+      const int w = ByteWidth(fields_[f].elem);
+      bufs.push_back({reinterpret_cast<const uint8_t*>(addrs[b0 + 3]) + e0 * w, (e1 - e0) * w});
+      continue;
+    }
     if (IsBinary(t)) {
       const int ow = OffW(t);
       const uint8_t* off = reinterpret_cast<const uint8_t*>(addrs[b0 + 1]);

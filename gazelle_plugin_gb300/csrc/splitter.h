@@ -91,6 +91,7 @@ class Splitter {
     uint32_t nrows;
     uint32_t split_size;
     uint64_t validity_mask;  // array columns with a validity buffer
+    uint64_t cvalid_mask;    // list columns with an element validity buffer
   };
   struct Need {
     const uint8_t* src;
@@ -109,6 +110,7 @@ class Splitter {
     bool on_file = false;               // h_out maps spill_path (past host_budget)
     std::string spill_path;
     std::vector<size_t> off_values, off_bits, off_valid, off_chars;  // per array column, SIZE_MAX: none
+    std::vector<size_t> off_cvalid;  // list columns: element validity bits (in the bit regions)
     uint32_t* h_meta = nullptr;         // pinned: rows_f, pstart, vstart, bytes_f, cstart, count, emit
     size_t bits_begin = 0, bits_end = 0;  // the bit regions (validity, bool values) in the output
     uint8_t* h_bits = nullptr;          // pinned copy of just the bit regions (compressed Stop)
@@ -209,7 +211,10 @@ class Splitter {
   std::vector<int32_t> field_array_;  // array column per schema field (-1 for null type)
   std::vector<int32_t> field_buf0_;   // index of the field's first buffer in the flat list
   int32_t n_bufs_expected_ = 0;
-  int32_t fixed_cnt_ = 0, n_str_ = 0, n_array_ = 0;
+  // array columns: fixed [0, fixed_cnt_), binary [fixed_cnt_, n_policy_) - the reference's
+  // array_idx_, which the buffer policy reads - then list [n_policy_, n_array_); n_str_: binary
+  // and list columns (the device's string-like columns), n_bin_: binary ones
+  int32_t fixed_cnt_ = 0, n_str_ = 0, n_array_ = 0, n_bin_ = 0, n_policy_ = 0;
   uint32_t seg_tiles_ = 1;  // tiles per k_scatter segment
   std::vector<uint64_t> empirical_;  // binary_array_empirical_size_
 

@@ -63,7 +63,7 @@ class GzField(ctypes.Structure):
         ("precision", ctypes.c_int32),
         ("scale", ctypes.c_int32),
         ("unit", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("elem_type", ctypes.c_int32),
         ("name", ctypes.c_char_p),
     ]
 
@@ -145,6 +145,8 @@ def lib() -> ctypes.CDLL:
         L.gz_reader_column_to_host.restype = ctypes.c_int
         L.gz_reader_column_to_host.argtypes = [ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
                                                ctypes.c_void_p]
+        L.gz_reader_elem_validity_to_host.restype = ctypes.c_int
+        L.gz_reader_elem_validity_to_host.argtypes = [ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p]
         L.gz_reader_close.restype = ctypes.c_int
         L.gz_reader_close.argtypes = [ctypes.c_int64]
         L.gz_serve_start.restype = ctypes.c_int
@@ -287,6 +289,9 @@ class GzDeviceColumn(ctypes.Structure):
         ("offsets", ctypes.c_void_p),
         ("values", ctypes.c_void_p),
         ("values_bytes", ctypes.c_int64),
+        ("child_validity", ctypes.c_void_p),
+        ("child_length", ctypes.c_int64),
+        ("child_null_count", ctypes.c_int64),
     ]
 
 
@@ -340,12 +345,16 @@ def split_options(offheapPerTask: int = 0, bufferSize: int = 4096, codec: Option
 
 
 def _fields(schema):
+    from . import workloads as W
     arr = (GzField * len(schema))()
     names = [f.name.encode() for f in schema]
     for i, f in enumerate(schema):
         arr[i].type = f.code
         arr[i].nullable = int(f.nullable)
         arr[i].precision, arr[i].scale, arr[i].unit = f.params
+        if f.is_list:
+            arr[i].elem_type = W.TYPE_CODES[f.elem]
+            arr[i].precision, arr[i].scale, arr[i].unit = W.Field("item", f.elem).params
         arr[i].name = names[i]
     return arr, names
 
@@ -662,6 +671,15 @@ class PartitionReader:
                                               offs.ctypes.data if offs is not None else None,
                                               vals.ctypes.data if vals.nbytes else None))
         return valid, offs, vals
+
+    def element_validity_to_host(self, field: int):
+        """A list column's element validity bytes, or None without a null element."""
+        c = self.column(field)
+        if not c.child_validity:
+            return None
+        out = np.zeros((c.child_length + 7) // 8, np.uint8)
+        _check(lib().gz_reader_elem_validity_to_host(self.h, field, out.ctypes.data))
+        return out
 
     def close(self) -> None:
         if self.h:

@@ -21,7 +21,7 @@ slot; a null fixed-width cell keeps its generated value):
 from __future__ import annotations
 
 import dataclasses
-from typing import List, Sequence
+from typing import List, Optional, Sequence
 
 import numpy as np
 
@@ -31,7 +31,7 @@ TYPE_CODES = {
     "float16": 6, "int32": 7, "uint32": 8, "float32": 9, "date32": 10, "time32": 11,
     "int64": 12, "uint64": 13, "float64": 14, "date64": 15, "time64": 16,
     "timestamp": 17, "decimal128": 18, "utf8": 19, "binary": 20,
-    "large_utf8": 21, "large_binary": 22,
+    "large_utf8": 21, "large_binary": 22, "list": 23,
 }
 BYTE_WIDTH = {
     "int8": 1, "uint8": 1, "int16": 2, "uint16": 2, "float16": 2, "int32": 4,
@@ -51,10 +51,21 @@ class Field:
     name: str
     type: str
     nullable: bool = True
+    elem: Optional[str] = None  # list: the element type (fixed width; elements nullable)
 
     @property
     def code(self) -> int:
         return TYPE_CODES[self.type]
+
+    @property
+    def is_list(self) -> bool:
+        return self.type == "list"
+
+    @property
+    def buffer_count(self) -> int:
+        """Entries of the field in a batch's flat buffer list: [validity, (offsets), values];
+        a list: [validity, offsets, element validity, element values]."""
+        return 4 if self.is_list else 3 if self.is_binary else 2
 
     @property
     def is_binary(self) -> bool:
@@ -242,6 +253,33 @@ def c4_batch(rng, schema_index: int, n: int) -> Batch:
     if schema_index == 1:
         return c2_batch(rng, n)
     return c4_schema3_batch(rng, n)
+
+
+def list_column(rng, field: Field, n: int, null_frac: float, elem_null_frac: float, max_len: int,
+                values=None) -> List[np.ndarray]:
+    """Buffers of a list column of `n` rows: lengths U{0..max_len} (0 for a null row), elements
+    of field.elem drawn like a flat column's (or taken from `values`), element nulls i.i.d."""
+    valid = rng.random(n) >= null_frac if null_frac > 0 else np.ones(n, bool)
+    lens = np.where(valid, rng.integers(0, max_len + 1, size=n), 0).astype(np.int32)
+    offsets = np.zeros(n + 1, np.int32)
+    np.cumsum(lens, out=offsets[1:])
+    m = int(offsets[-1])
+    ef = Field("item", field.elem)
+    if values is None:
+        if field.elem == "decimal128":
+            values = rng.integers(0, 2**63, size=2 * m, dtype=np.uint64)
+        elif field.elem in ("float16", "float32", "float64"):
+            values = rng.standard_normal(m) * 1e3
+        else:
+            w = BYTE_WIDTH[field.elem]
+            hi = 2 ** (8 * w - 1) if w < 8 else 2**62
+            values = rng.integers(-hi if field.elem[0] != "u" else 0, hi, size=m)
+    evalid = rng.random(m) >= elem_null_frac if elem_null_frac > 0 else np.ones(m, bool)
+    if field.elem == "decimal128":
+        vals = np.ascontiguousarray(np.asarray(values, np.uint64)).view(np.uint8)
+    else:
+        vals = np.ascontiguousarray(np.asarray(values).astype(NUMPY_DTYPE[ef.type])).view(np.uint8)
+    return [pack_validity(valid), offsets.view(np.uint8), pack_validity(evalid), vals]
 
 
 def c4_rows(rng, size=None):

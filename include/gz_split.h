@@ -41,7 +41,11 @@ typedef enum GzType {
   GZ_TYPE_STRING = 19, GZ_TYPE_BINARY = 20,
   /* 64-bit offsets (SplitBinaryType<LargeBinaryType::offset_type>, splitter.cc:1291-1299):
    * payload columns only; one batch's column may hold at most 2^31 - 1 character bytes */
-  GZ_TYPE_LARGE_STRING = 21, GZ_TYPE_LARGE_BINARY = 22
+  GZ_TYPE_LARGE_STRING = 21, GZ_TYPE_LARGE_BINARY = 22,
+  /* list of fixed-width elements (SplitListArray / AppendList, splitter.cc:1322-1344): a payload
+   * column whose element type is GzField.elem_type; buffers [validity, int32 offsets, element
+   * validity, element values] */
+  GZ_TYPE_LIST = 23
 } GzType;
 
 /* One schema field.  `unit`: time/timestamp unit (0 s, 1 ms, 2 us, 3 ns); `precision` /
@@ -52,7 +56,8 @@ typedef struct GzField {
   int32_t precision;
   int32_t scale;
   int32_t unit;
-  int32_t reserved;
+  int32_t elem_type;  /* GZ_TYPE_LIST: the element type (fixed width; precision / scale / unit
+                         then describe the element, named "item" and nullable) */
   const char* name;
 } GzField;
 
@@ -359,8 +364,12 @@ typedef struct GzDeviceColumn {
   const uint8_t* validity; /* LSB-first bitmap, (length + 7) / 8 bytes; NULL: no nulls */
   const void* offsets;     /* binary / utf8: length + 1 int32 offsets from 0 (int64 for the large
                             * types); NULL otherwise */
-  const uint8_t* values;   /* fixed width: length * width bytes; bool: bitmap; binary: characters */
+  const uint8_t* values;   /* fixed width: length * width bytes; bool: bitmap; binary: characters;
+                            * list: the element values */
   int64_t values_bytes;
+  const uint8_t* child_validity;  /* list: element validity bitmap; NULL: no null element */
+  int64_t child_length;           /* list: elements */
+  int64_t child_null_count;
 } GzDeviceColumn;
 
 /* A reader for partitions of `schema_ipc` (an encapsulated Arrow IPC Schema message, as
@@ -388,6 +397,10 @@ GzStatus gz_reader_column(int64_t handle, int32_t field, GzDeviceColumn* out);
  * column's offset width, binary only), `values` (values_bytes bytes).  Waits for the copies. */
 GzStatus gz_reader_column_to_host(int64_t handle, int32_t field, uint8_t* validity, void* offsets,
                                   uint8_t* values);
+
+/* A list column's element validity ((child_length + 7) / 8 bytes) to host memory; nothing when
+ * the column has no null element.  Waits for the copy. */
+GzStatus gz_reader_elem_validity_to_host(int64_t handle, int32_t field, uint8_t* out);
 
 /* Frees the reader and its device columns. */
 GzStatus gz_reader_close(int64_t handle);

@@ -76,14 +76,20 @@ def parse_stream(data: bytes, schema) -> List[Tuple[int, list]]:
             nn, nb = fb.u32(nodes), fb.u32(bufs)
             node_list = [struct.unpack_from("<qq", fb.b, nodes + 4 + 16 * i) for i in range(nn)]
             buf_list = [struct.unpack_from("<qq", fb.b, bufs + 4 + 16 * i) for i in range(nb)]
-            cols, bi = [], 0
-            for f, (length, nulls) in zip(schema, node_list):
+            cols, bi, ni = [], 0, 0
+            for f in schema:
+                length, nulls = node_list[ni]
+                ni += 1
                 assert length == rows
-                k = 0 if f.type == "null" else (3 if f.is_binary else 2)
+                child_nulls = None
+                if f.is_list:  # the element node follows the list's
+                    child_nulls = node_list[ni][1]
+                    ni += 1
+                k = 0 if f.type == "null" else f.buffer_count
                 bufs = [data[body + o: body + o + l] for o, l in buf_list[bi:bi + k]]
                 if compressed:
                     bufs = [_decompress(b) for b in bufs]
-                cols.append((nulls, bufs))
+                cols.append((nulls, bufs) if child_nulls is None else (nulls, bufs, child_nulls))
                 bi += k
             out.append((rows, cols))
         elif htype != HEADER_SCHEMA:
@@ -143,6 +149,20 @@ def read_partition(schema, streams: Sequence[bytes]):
         if f.type == "bool":
             vals = np.concatenate([_bits(c[fi][1][1], r) for r, c in batches]) if batches else np.zeros(0, bool)
             cols.append((valid, None, vals))
+        elif f.is_list:  # (validity, offsets, (element validity or None, element values))
+            w = BYTE_WIDTH[f.elem]
+            offs, vals, evalid, base = [np.zeros(1, np.int32)], [], [], 0
+            any_null = any(c[fi][2] for _, c in batches)
+            for r, c in batches:
+                o = np.frombuffer(c[fi][1][1], np.int32)[:r + 1]
+                m = int(o[r] - o[0])
+                vals.append(c[fi][1][3][o[0] * w:o[r] * w])
+                offs.append((o[1:] - o[0] + base).astype(np.int32))
+                if any_null:
+                    evalid.append(_bits(c[fi][1][2], int(o[r]))[o[0]:] if c[fi][2] else np.ones(m, bool))
+                base += m
+            ev = (np.concatenate(evalid) if evalid else np.zeros(0, bool)) if any_null else None
+            cols.append((valid, np.concatenate(offs), (ev, b"".join(vals))))
         elif f.is_binary:
             odt = f.offset_dtype  # int32, int64 for the large types
             offs, chars, base = [np.zeros(1, odt)], [], 0

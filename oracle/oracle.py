@@ -123,7 +123,9 @@ class OracleSplitter:
                  offheap_per_task: int = 0, buffer_size: int = 4096, prefer_spill: bool = True,
                  write_schema: bool = False, short_name: str = "hash"):
         self.P = 1 if short_name == "single" else num_partitions
-        types = np.array([f.code for f in schema], np.int32)
+        # a list field's code carries its element type above the low byte
+        types = np.array([f.code | ((f.__class__("e", f.elem).code << 8) if f.is_list else 0) for f in schema],
+                         np.int32)
         keys = np.array(key_cols, np.int32)
         err = ctypes.create_string_buffer(512)
         self.h = self.lib().gzo_make(short_name.encode(), types.ctypes.data, len(types),
@@ -201,6 +203,8 @@ def to_pyarrow_schema(schema):
     units = ["s", "ms", "us", "ns"]
 
     def typ(f):
+        if f.is_list:  # Arrow's default list element field: "item", nullable
+            return pa.list_(pa.field("item", typ(type(f)("item", f.elem)), True))
         prec, scale, unit = f.params
         if f.type == "decimal128":
             return pa.decimal128(prec, scale)

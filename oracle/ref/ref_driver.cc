@@ -35,6 +35,49 @@ void SetErr(const arrow::Status& s, char* err, int errlen) {
   }
 }
 
+// One array of `type` from the flat buffer list at *idx, in the JNI's order (jni_common.h:
+// 308-382 MakeArrayData): [validity, (offsets), values] for flat types, [validity, offsets,
+// <child buffers>] for list / large_list.  num_rows < 0: taken from the offsets (a child).
+arrow::Status WrapArray(const std::shared_ptr<arrow::DataType>& type, int64_t num_rows,
+                        const std::vector<std::shared_ptr<arrow::Buffer>>& bufs, int* idx,
+                        std::shared_ptr<arrow::ArrayData>* out) {
+  const int n = (int)bufs.size();
+  if (type->id() == arrow::Type::NA) {
+    if (*idx + 2 > n) return arrow::Status::Invalid("insufficient number of buffers");
+    *idx += 2;
+    *out = arrow::ArrayData::Make(type, num_rows, {nullptr}, num_rows);
+    return arrow::Status::OK();
+  }
+  std::vector<std::shared_ptr<arrow::Buffer>> ab;
+  if (*idx >= n) return arrow::Status::Invalid("insufficient number of buffers");
+  int64_t null_count = bufs[*idx]->size() == 0 ? 0 : arrow::kUnknownNullCount;
+  ab.push_back(bufs[(*idx)++]);
+  if (type->id() == arrow::Type::LIST || type->id() == arrow::Type::LARGE_LIST) {
+    if (*idx >= n) return arrow::Status::Invalid("insufficient number of buffers");
+    const int ow = type->id() == arrow::Type::LIST ? 4 : 8;
+    if (num_rows < 0) num_rows = bufs[*idx]->size() / ow - 1;
+    ab.push_back(bufs[(*idx)++]);
+    std::shared_ptr<arrow::ArrayData> child;
+    ARROW_RETURN_NOT_OK(WrapArray(type->field(0)->type(), -1, bufs, idx, &child));
+    *out = arrow::ArrayData::Make(type, num_rows, std::move(ab), {child}, null_count);
+    return arrow::Status::OK();
+  }
+  if (arrow::is_binary_like(type->id()) || arrow::is_large_binary_like(type->id())) {
+    if (*idx >= n) return arrow::Status::Invalid("insufficient number of buffers");
+    const int ow = arrow::is_binary_like(type->id()) ? 4 : 8;
+    if (num_rows < 0) num_rows = bufs[*idx]->size() / ow - 1;
+    ab.push_back(bufs[(*idx)++]);
+  }
+  if (*idx >= n) return arrow::Status::Invalid("insufficient number of buffers");
+  if (num_rows < 0) {
+    const int bw = arrow::bit_width(type->id());
+    num_rows = bw > 0 ? bufs[*idx]->size() * 8 / bw : 0;
+  }
+  ab.push_back(bufs[(*idx)++]);
+  *out = arrow::ArrayData::Make(type, num_rows, std::move(ab), null_count);
+  return arrow::Status::OK();
+}
+
 arrow::Status WrapBatch(const std::shared_ptr<arrow::Schema>& schema, int32_t num_rows,
                         const int64_t* addrs, const int64_t* sizes, int32_t n,
                         std::shared_ptr<arrow::RecordBatch>* out) {
@@ -50,25 +93,9 @@ arrow::Status WrapBatch(const std::shared_ptr<arrow::Schema>& schema, int32_t nu
   std::vector<std::shared_ptr<arrow::ArrayData>> arrays;
   int idx = 0;
   for (int f = 0; f < schema->num_fields(); f++) {
-    auto type = schema->field(f)->type();
-    if (type->id() == arrow::Type::NA) {
-      // the JNI generic branch consumes [validity, values] for a null-type field too
-      if (idx + 2 > n) return arrow::Status::Invalid("insufficient number of buffers");
-      idx += 2;
-      arrays.push_back(arrow::ArrayData::Make(type, num_rows, {nullptr}, num_rows));
-      continue;
-    }
-    std::vector<std::shared_ptr<arrow::Buffer>> ab;
-    if (idx >= n) return arrow::Status::Invalid("insufficient number of buffers");
-    int64_t null_count = bufs[idx]->size() == 0 ? 0 : arrow::kUnknownNullCount;
-    ab.push_back(bufs[idx++]);
-    if (arrow::is_binary_like(type->id()) || arrow::is_large_binary_like(type->id())) {
-      if (idx >= n) return arrow::Status::Invalid("insufficient number of buffers");
-      ab.push_back(bufs[idx++]);
-    }
-    if (idx >= n) return arrow::Status::Invalid("insufficient number of buffers");
-    ab.push_back(bufs[idx++]);
-    arrays.push_back(arrow::ArrayData::Make(type, num_rows, std::move(ab), null_count));
+    std::shared_ptr<arrow::ArrayData> a;
+    ARROW_RETURN_NOT_OK(WrapArray(schema->field(f)->type(), num_rows, bufs, &idx, &a));
+    arrays.push_back(std::move(a));
   }
   *out = arrow::RecordBatch::Make(schema, num_rows, std::move(arrays));
   return arrow::Status::OK();

@@ -48,7 +48,7 @@ enum TypeCode {
   T_HALF_FLOAT = 6, T_INT32 = 7, T_UINT32 = 8, T_FLOAT32 = 9, T_DATE32 = 10,
   T_TIME32 = 11, T_INT64 = 12, T_UINT64 = 13, T_FLOAT64 = 14, T_DATE64 = 15,
   T_TIME64 = 16, T_TIMESTAMP = 17, T_DECIMAL128 = 18, T_STRING = 19, T_BINARY = 20,
-  T_LARGE_STRING = 21, T_LARGE_BINARY = 22,
+  T_LARGE_STRING = 21, T_LARGE_BINARY = 22, T_LIST = 23,
 };
 
 int ByteWidth(int t) {
@@ -224,14 +224,30 @@ std::vector<uint8_t> EncodeRecordBatch(int64_t length,
 struct Field {
   int type;
   std::string name;
+  int elem = 0;  // list: the element type (fixed width)
 };
 
 struct InCol {
   const uint8_t* validity = nullptr;  // nullptr when the validity buffer is empty
   const uint8_t* offsets = nullptr;
-  const uint8_t* values = nullptr;
+  const uint8_t* values = nullptr;    // list: the element values
+  const uint8_t* child_validity = nullptr;  // list: the elements' validity (nullptr: none)
   int64_t null_count = 0;
 };
+
+// One partition's list builder (partition_list_builders_, splitter.cc:292-296, 664-674): rows
+// appended with ListBuilder::AppendArraySlice (AppendList, splitter.cc:1335-1344) - a null row
+// adds no elements - and finished by CacheRecordBatch (splitter.cc:532-545).  Bitmaps are
+// zero-padded like an Arrow builder's; each is written only when it holds a null.
+struct ListBuf {
+  std::vector<uint8_t> valid, cvalid, cvals;
+  std::vector<int32_t> offs{0};
+  int64_t rows = 0, nulls = 0, elems = 0, cnulls = 0;
+};
+inline void PutBit(std::vector<uint8_t>& v, int64_t i, bool b) {
+  if ((int64_t)v.size() * 8 <= i) v.resize((size_t)(i / 8 + 1), 0);
+  if (b) v[(size_t)(i >> 3)] |= (uint8_t)(1u << (i & 7));
+}
 
 // Splitter::Make short names (splitter.cc:190-208); "single" is round-robin over one partition.
 enum Mode { M_HASH = 0, M_RR = 1, M_RANGE = 2 };
@@ -276,6 +292,10 @@ class OracleSplitter {
       int t = fields_[i].type;
       if (IsBinary(t)) bin.push_back(i);
       else if (t == T_NULL) continue;
+      else if (t == T_LIST) {  // list_array_idx_ (splitter.cc:254-258), elements of fixed width
+        if (ByteWidth(fields_[i].elem) <= 0) return "list element type not supported";
+        list_idx_.push_back(i);
+      }
       else if (t == T_BOOL || ByteWidth(t) > 0) array_idx_.push_back(i);
       else return "unsupported field type";
     }
@@ -292,6 +312,7 @@ class OracleSplitter {
     }
     int A = (int)array_idx_.size();
     bufs_.assign(A, std::vector<PartBufs>(P_));
+    lists_.assign(list_idx_.size(), std::vector<ListBuf>(P_));
     input_has_null_.assign(A, false);
     empirical_.assign(A - fixed_cnt_, 0);
     cap_.assign(P_, 0);
@@ -333,9 +354,14 @@ class OracleSplitter {
       InCol c;
       if (sizes[idx] > 0 && addrs[idx] != 0) c.validity = (const uint8_t*)addrs[idx];
       idx++;
-      if (IsBinary(fields_[f].type)) {
+      if (IsBinary(fields_[f].type) || fields_[f].type == T_LIST) {
         if (idx >= nbuf) return "insufficient number of buffers";
         c.offsets = (const uint8_t*)addrs[idx++];
+      }
+      if (fields_[f].type == T_LIST) {  // [validity, offsets, element validity, element values]
+        if (idx >= nbuf) return "insufficient number of buffers";
+        if (sizes[idx] > 0 && addrs[idx] != 0) c.child_validity = (const uint8_t*)addrs[idx];
+        idx++;
       }
       if (idx >= nbuf) return "insufficient number of buffers";
       c.values = (const uint8_t*)addrs[idx++];
@@ -559,11 +585,26 @@ class OracleSplitter {
     std::vector<BodyBuf> body;
     std::vector<std::vector<uint8_t>> keep;
     int64_t raw = 0;
-    int fixed_i = 0, bin_i = 0;
+    int fixed_i = 0, bin_i = 0, list_i = 0;
     for (size_t f = 0; f < fields_.size(); f++) {
       int t = fields_[f].type;
       if (t == T_NULL) {
         nodes.push_back({n, n});
+        continue;
+      }
+      if (t == T_LIST) {  // builder->Finish (splitter.cc:534-545): list node, then its element node
+        ListBuf& b = lists_[list_i++][p];
+        const int w = ByteWidth(fields_[f].elem);
+        b.valid.resize((size_t)BytesForBits(n), 0);
+        b.cvalid.resize((size_t)BytesForBits(b.elems), 0);
+        nodes.push_back({n, b.nulls});
+        body.push_back(b.nulls > 0 ? BodyBuf{b.valid.data(), BytesForBits(n)} : BodyBuf{nullptr, 0});
+        body.push_back({(const uint8_t*)b.offs.data(), (int64_t)(n + 1) * 4});
+        nodes.push_back({b.elems, b.cnulls});
+        body.push_back(b.cnulls > 0 ? BodyBuf{b.cvalid.data(), BytesForBits(b.elems)} : BodyBuf{nullptr, 0});
+        body.push_back({b.cvals.data(), b.elems * w});
+        // batch_nbytes counts the list's own buffers (splitter.cc:438-453)
+        raw += (b.nulls > 0 ? BytesForBits(n) : 0) + (int64_t)(n + 1) * 4;
         continue;
       }
       int a = IsBinary(t) ? fixed_cnt_ + bin_i++ : fixed_i++;
@@ -603,6 +644,7 @@ class OracleSplitter {
     cached_size_[p] += body_len;
     cached_[p].push_back(std::move(msg));
     base_[p] = 0;
+    for (auto& l : lists_) l[p] = ListBuf();
     int A = (int)array_idx_.size();
     for (int a = 0; a < A; a++) {
       PartBufs& b = bufs_[a][p];
@@ -724,6 +766,31 @@ class OracleSplitter {
         }
       }
     }
+    // SplitListArray (splitter.cc:1322-1333): every row to its partition's builder
+    for (size_t li = 0; li < list_idx_.size(); li++) {
+      const InCol& c = cols[list_idx_[li]];
+      const int w = ByteWidth(fields_[list_idx_[li]].elem);
+      const int32_t* off = (const int32_t*)c.offsets;
+      for (int32_t r = 0; r < n; r++) {
+        ListBuf& b = lists_[li][pid_[r]];
+        const bool valid = c.null_count == 0 || GetBit(c.validity, r);
+        PutBit(b.valid, b.rows, valid);
+        b.rows++;
+        if (!valid) {
+          b.nulls++;
+          b.offs.push_back(b.offs.back());
+          continue;
+        }
+        for (int32_t e = off[r]; e < off[r + 1]; e++) {
+          const bool cv = c.child_validity == nullptr || GetBit(c.child_validity, e);
+          PutBit(b.cvalid, b.elems, cv);
+          b.cnulls += !cv;
+          b.cvals.insert(b.cvals.end(), c.values + (size_t)e * w, c.values + (size_t)(e + 1) * w);
+          b.elems++;
+        }
+        b.offs.push_back(b.offs.back() + (off[r + 1] - off[r]));
+      }
+    }
     for (int p = 0; p < P_; p++) base_[p] += cnt_[p];
     return "";
   }
@@ -734,6 +801,8 @@ class OracleSplitter {
   Options opt_;
   std::vector<uint8_t> schema_msg_;
   std::vector<int> array_idx_;
+  std::vector<int> list_idx_;
+  std::vector<std::vector<ListBuf>> lists_;  // [list column][partition]
   int fixed_cnt_ = 0;
   std::vector<std::vector<PartBufs>> bufs_;
   std::vector<bool> input_has_null_;
@@ -774,7 +843,8 @@ void* gzo_make(const char* mode, const int32_t* types, int32_t nf, int32_t num_p
                const int32_t* keys, int32_t n_keys, int64_t offheap_per_task, int32_t buffer_size,
                int32_t prefer_spill, char* err, int errlen) {
   std::vector<Field> fields;
-  for (int i = 0; i < nf; i++) fields.push_back({types[i], "f" + std::to_string(i)});
+  // a list field's code carries its element type above the low byte
+  for (int i = 0; i < nf; i++) fields.push_back({types[i] & 0xff, "f" + std::to_string(i), types[i] >> 8});
   Options o;
   const std::string m = mode ? mode : "hash";
   if (m == "hash") o.mode = M_HASH;

@@ -2,9 +2,9 @@
 
 Run in a checkout where the reference sources and pyarrow are present:
 
-    python tests/golden/make_golden.py [/path/to/gazelle_plugin] [--only=large]
+    python tests/golden/make_golden.py [/path/to/gazelle_plugin] [--only=large|--only=list]
 
-(--only=large rewrites large_binary.json alone.)
+(--only=large / --only=list rewrite large_binary.json / list_columns.json alone.)
 
 It compiles the reference Splitter (oracle/ref/Makefile -> oracle/_ref/) and runs it on
 seeded inputs from gazelle_plugin_gb300.workloads, recording for every case the SHA-256 of
@@ -70,7 +70,7 @@ def record(name, schema, batches, P, keys, opts, gen, short_name="hash"):
         **rec,
         "name": name,
         "gen": gen,
-        "schema": [[f.name, f.type, f.nullable] for f in schema],
+        "schema": [[f.name, f.type, f.nullable] + ([f.elem] if f.is_list else []) for f in schema],
         "num_partitions": P,
         "keys": [int(k) for k in keys],
         "options": opts,
@@ -175,6 +175,48 @@ def large_case(seed):
     return schema, batches, P, keys, opts
 
 
+LIST_ELEMS = ["int8", "int16", "int32", "int64", "float32", "float64", "date32", "decimal128", "timestamp"]
+
+
+def list_case(seed):
+    """Schema, batches, P, keys and options of a `list_<n>` case: an int key, 0-2 fixed-width
+    columns, 1-3 list columns of fixed-width elements (list and element nulls, or none, or no
+    validity buffers) and 0-1 utf8 column, in random order."""
+    rng = np.random.default_rng(seed)
+    fields = [W.Field("k", str(rng.choice(["int32", "int64"])), False)]
+    fields += [W.Field(f"f{i}", str(rng.choice(["int32", "float64", "bool"]))) for i in range(int(rng.integers(0, 3)))]
+    fields += [W.Field(f"L{i}", "list", True, str(rng.choice(LIST_ELEMS))) for i in range(int(rng.integers(1, 4)))]
+    fields += [W.Field("s", "utf8")] * int(rng.integers(0, 2))
+    schema = [fields[i] for i in rng.permutation(len(fields))]
+    keys = [i for i, f in enumerate(schema) if f.name == "k"]
+    P = int(rng.choice([1, 3, 16, 200]))
+    bsz = int(rng.choice([8, 100, 4096]))
+    ps = bool(rng.random() < 0.6)
+    opts = {"buffer_size": bsz, "prefer_spill": ps,
+            "offheap_per_task": 0 if ps else int(rng.choice([0, 1 << 16]))}
+    batches = []
+    for _ in range(int(rng.integers(1, 6))):
+        n = int(rng.integers(1, bsz + 1))
+        bufs = []
+        for f in schema:
+            if f.is_list:
+                bufs += W.list_column(rng, f, n, float(rng.choice([0.0, 0.1, 0.4])),
+                                      float(rng.choice([0.0, 0.05, 0.5])), int(rng.choice([0, 3, 12])))
+            else:
+                bufs += W.random_batch(rng, [f], n, 0.1).buffers
+        batches.append(W.Batch(n, bufs))
+    return schema, batches, P, keys, opts
+
+
+def list_cases():
+    for seed in range(16):
+        schema, batches, P, keys, opts = list_case(5000 + seed)
+        yield (f"list_{seed}", schema, batches, P, keys, opts, {"workload": "list", "seed": 5000 + seed})
+    schema, batches, P, keys, opts = list_case(5100)
+    yield ("list_write_schema", schema, batches, P, keys, dict(opts, write_schema=True),
+           {"workload": "list", "seed": 5100})
+
+
 def large_cases():
     for seed in range(16):
         schema, batches, P, keys, opts = large_case(4000 + seed)
@@ -189,6 +231,8 @@ def regenerate(case):
     g = case["gen"]
     if g["workload"] == "large":
         return large_case(g["seed"])[1]
+    if g["workload"] == "list":
+        return list_case(g["seed"])[1]
     if g["workload"] == "c1":
         return W.c1_batches(g["seed"], g["num_batches"], g["rows"])
     if g["workload"] == "c2":
@@ -331,13 +375,17 @@ def partitioner_cases():
             yield (f"random_{seed}_rr", "rr", P, opts, g)
 
 
-def write_large():
+def write_cases(cases, file_name):
     recs = []
-    for name, schema, batches, P, keys, opts, gen in large_cases():
+    for name, schema, batches, P, keys, opts, gen in cases:
         recs.append(record(name, schema, batches, P, keys, opts, gen))
         print(name, recs[-1]["data_sha256"][:16])
-    with open(os.path.join(HERE, "large_binary.json"), "w") as f:
+    with open(os.path.join(HERE, file_name), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py", "cases": recs}, f, indent=1)
+
+
+def write_large():
+    write_cases(large_cases(), "large_binary.json")
 
 
 def main():
@@ -348,7 +396,11 @@ def main():
     if "--only=large" in sys.argv:
         write_large()
         return
+    if "--only=list" in sys.argv:
+        write_cases(list_cases(), "list_columns.json")
+        return
     write_large()
+    write_cases(list_cases(), "list_columns.json")
     recs = []
     for name, schema, batches, P, keys, opts, gen in cases():
         recs.append(record(name, schema, batches, P, keys, opts, gen))

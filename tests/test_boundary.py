@@ -128,15 +128,18 @@ def test_schema_ipc_parser():
     pa = pytest.importorskip("pyarrow")
     from oracle.oracle import to_pyarrow_schema
     from gazelle_plugin_gb300 import workloads as W
-    schema = [W.Field(f"c{i}", t, i % 2 == 0) for i, t in enumerate(W.TYPE_CODES)]
+    schema = [W.Field(f"c{i}", t, i % 2 == 0, "int64" if t == "list" else None)
+              for i, t in enumerate(W.TYPE_CODES)]
     st, types, nulls = parse_schema(to_pyarrow_schema(schema).serialize().to_pybytes())
     assert st == 0
     expect = [f.code for f in schema]
     # time32/time64/date64/timestamp round-trip through their Arrow units
     assert types == expect
     assert nulls == [int(f.nullable) for f in schema]
-    st, _, _ = parse_schema(pa.schema([pa.field("l", pa.list_(pa.int32()))]).serialize().to_pybytes())
-    assert st != 0
+    # lists of fixed-width elements only: nested lists and lists of strings are refused
+    for t in (pa.list_(pa.list_(pa.int32())), pa.list_(pa.utf8()), pa.struct([pa.field("a", pa.int32())])):
+        st, _, _ = parse_schema(pa.schema([pa.field("l", t)]).serialize().to_pybytes())
+        assert st != 0, t
 
 
 def test_schema_message_matches_arrow_writer():
@@ -155,7 +158,9 @@ def test_schema_message_matches_arrow_writer():
              pa.timestamp("s"), pa.timestamp("ms"), pa.timestamp("us"), pa.timestamp("ns"),
              pa.timestamp("us", tz="UTC"), pa.timestamp("ns", tz="America/New_York"),
              pa.decimal128(10, 2), pa.decimal128(38, 0), pa.decimal128(1, 0), pa.utf8(),
-             pa.binary(), pa.null()]
+             pa.binary(), pa.null(), pa.large_utf8(), pa.large_binary(),
+             pa.list_(pa.int32()), pa.list_(pa.float64()), pa.list_(pa.field("element", pa.int64(), False)),
+             pa.list_(pa.decimal128(12, 3)), pa.list_(pa.timestamp("us", tz="UTC")), pa.list_(pa.date32())]
     rnd = random.Random(7)
     out = np.zeros(1 << 16, np.uint8)
     n = ctypes.c_int64(0)
