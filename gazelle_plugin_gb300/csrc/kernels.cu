@@ -682,7 +682,7 @@ constexpr int kSortIters = kTileRows / (kW * 32);  // 32-row groups per warp
 __device__ void radix_pass(const uint16_t* kin, const uint16_t* pin, uint16_t* kout,
                            uint16_t* pout, int n, int shift, int ndig, uint16_t* wcnt, uint32_t* off,
                            uint32_t* scratch, uint32_t* first = nullptr) {
-  // ndig: digit values that occur (keys < P), so only kW * ndig counters are transposed / scanned
+  // ndig: digit values that occur (keys < P), so only kW * ndig counters are scanned
   const int w = threadIdx.x >> 5;
   const int seg = ((n + kW * 32 - 1) / (kW * 32)) * 32;
   for (int i = threadIdx.x; i < kW * 256; i += kConsumers) wcnt[i] = 0;
@@ -708,15 +708,40 @@ __device__ void radix_pass(const uint16_t* kin, const uint16_t* pin, uint16_t* k
     __syncwarp();
   }
   csync();
-  for (int i = threadIdx.x; i < kW * ndig; i += kConsumers) {
-    const int d = i / kW, ww = i % kW;
-    off[i] = wcnt[ww * 256 + d];
-  }
-  csync();
-  block_exscan<kConsumers, 1>(off, kW * ndig, scratch);
-  if (first != nullptr) {  // first sorted position of every digit (its warp-0 offset), then n
-    for (int d = threadIdx.x; d <= ndig; d += kConsumers) first[d] = d < ndig ? off[d * kW] : (uint32_t)n;
-    csync();  // read before the scatter below moves the offsets
+  // One digit per thread (ndig <= 256 threads): its count in each warp, an exclusive scan of the
+  // digit totals over the block (one barrier), then its offset in each warp's part of the
+  // output; `first` gets each digit's first sorted position, then n.
+  {
+    static_assert(kConsumers >= 256, "a thread per digit");
+    const int d = threadIdx.x;
+    uint32_t cw[kW];
+    uint32_t tot = 0;
+#pragma unroll
+    for (int ww = 0; ww < kW; ww++) {
+      cw[ww] = d < ndig ? wcnt[ww * 256 + d] : 0u;
+      tot += cw[ww];
+    }
+    uint32_t x = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFull, x, o);
+      if ((int)lane_id() >= o) x += y;
+    }
+    if (lane_id() == 31) scratch[w] = x;
+    csync();
+    uint32_t base = x - tot;
+    for (int ww = 0; ww < w; ww++) base += scratch[ww];
+    if (d < ndig) {
+      uint32_t run = base;
+#pragma unroll
+      for (int ww = 0; ww < kW; ww++) {
+        off[d * kW + ww] = run;
+        run += cw[ww];
+      }
+      if (first != nullptr) first[d] = base;
+    }
+    if (first != nullptr && d == 0) first[ndig] = (uint32_t)n;
+    csync();  // the offsets are complete before the scatter below moves them
   }
 #pragma unroll
   for (int it = 0; it < kSortIters; it++) {
@@ -1260,6 +1285,11 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
   // run that starts at an owned position) is copied asynchronously into nm0/nm1/nm2 one binary
   // column ahead, so its latency is hidden behind the columns processed in between; only the
   // owning thread reads it back.
+  // Up to 256 partitions: thread p loads partition p's values instead (nmP[0..3][p]); after they
+  // land the same thread turns them into the column's bases, so no other thread reads them.
+  uint32_t* nmP = nm3;                 // [4][256] (nm3 is free after the destinations)
+  uint32_t* baseP = rt0;               // [2 column parities][2][256] offset / character bases
+  uint32_t* wexP = rt1;                // [2][256] prefix inside its 32-row block at the run start
   auto load_run_meta = [&](int i_from) {
     for (int i = i_from; i < A; i++) {
       const int a = sd.order[i];
@@ -1268,6 +1298,17 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
       const size_t tk = ((size_t)tile.seg * nstr + k) * P;
       const size_t tb = ((size_t)blockIdx.x * nstr + k) * P;
       const uint32_t* cst = fd.cstart + (size_t)k * P;
+      if (small) {
+        const int p = threadIdx.x;
+        if (p < P) {
+          cp_async4(&nmP[p], &fd.sbyte[tk + p]);
+          cp_async4(&nmP[256 + p], &fd.bcnt[tk + p]);
+          cp_async4(&nmP[512 + p], &cst[p]);
+          if (has_pre) cp_async4(&nmP[768 + p], &fd.tilebpre[tb + p]);
+        }
+        cp_async_commit();
+        return;
+      }
 #pragma unroll
       for (int u = 0; u < kRowsPerThread; u++) {
         const int j = threadIdx.x + u * kConsumers;
@@ -1373,13 +1414,34 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
           }
         }
         const int w = threadIdx.x >> 5;
-        uint32_t* tot = wtot[nbin & 1];  // the previous binary column's totals may still be read
+        const int bb = nbin & 1;
+        uint32_t* tot = wtot[bb];  // the previous binary column's totals may still be read
         if (lane_id() == 31) {
 #pragma unroll
           for (int u = 0; u < kRowsPerThread; u++) tot[u * kW + w] = pre[u];
         }
+        if (small) {
+          // before the one barrier of the column: partition p's bases (thread p, from its own
+          // loads), the next binary column's loads, and at each run start the prefix inside its
+          // 32-row block (every thread has finished the reads of these buffers two binary
+          // columns back: it has passed the previous binary column's barrier)
+          cp_async_wait_all();
+          if ((int)threadIdx.x < P) {
+            const int p = threadIdx.x;
+            const uint32_t before = has_pre ? nmP[768 + p] : 0u;  // bytes from the segment's earlier tiles
+            baseP[bb * 512 + p] = nmP[p] + before;
+            baseP[bb * 512 + 256 + p] = nmP[512 + p] + nmP[256 + p] + before;
+          }
+          load_run_meta(i + 1);
+#pragma unroll
+          for (int u = 0; u < kRowsPerThread; u++) {
+            const int j = threadIdx.x + u * kConsumers;
+            if (j < n && rs[j] == j) wexP[bb * 256 + ks[j]] = pre[u] - len[u];
+          }
+        }
         csync();
         const bool run = !*vbad;
+        uint32_t excl = 0;
         if (run) {
           // the warp totals in (row, warp) order, one per lane: their exclusive scan is what all
           // earlier rows and this row's earlier warps hold (every warp scans them itself)
@@ -1391,25 +1453,27 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
             const uint32_t y = __shfl_up_sync(kFull, incl, o);
             if ((int)lane_id() >= o) incl += y;
           }
-          const uint32_t excl = incl - sv;
+          excl = incl - sv;
 #pragma unroll
           for (int u = 0; u < kRowsPerThread; u++) pre[u] = __shfl_sync(kFull, excl, u * kW + w) + pre[u] - len[u];
-          // run tables at the run starts: destination of the run's first string and its offset
-          // inside the partition's segment, both relative to the tile prefix (every thread has
-          // finished the previous binary column's reads of them: it passed the barrier above)
-          cp_async_wait_all();
+          if (!small) {
+            // run tables at the run starts: destination of the run's first string and its offset
+            // inside the partition's segment, both relative to the tile prefix (every thread has
+            // finished the previous binary column's reads of them: it passed the barrier above)
+            cp_async_wait_all();
 #pragma unroll
-          for (int u = 0; u < kRowsPerThread; u++) {
-            const int j = threadIdx.x + u * kConsumers;
-            if (j < n && rs[j] == j) {
-              const uint32_t before = has_pre ? nm3[j] : 0u;  // bytes from the segment's earlier tiles
-              rt0[j] = nm0[j] + before - pre[u];
-              rt1[j] = nm2[j] + nm1[j] + before - pre[u];
+            for (int u = 0; u < kRowsPerThread; u++) {
+              const int j = threadIdx.x + u * kConsumers;
+              if (j < n && rs[j] == j) {
+                const uint32_t before = has_pre ? nm3[j] : 0u;  // bytes from the segment's earlier tiles
+                rt0[j] = nm0[j] + before - pre[u];
+                rt1[j] = nm2[j] + nm1[j] + before - pre[u];
+              }
             }
+            load_run_meta(i + 1);
           }
-          load_run_meta(i + 1);
         }
-        csync();
+        if (!small) csync();
         nbin++;
         if (run) {
         int32_t* ooff = reinterpret_cast<int32_t*>(fd.out_values[a]);
@@ -1420,7 +1484,19 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
 #pragma unroll
           for (int u = 0; u < kRowsPerThread; u++) {
             const int j = threadIdx.x + u * kConsumers;
-            if (j < n) {
+            if (small) {
+              // the run start q's tile prefix: its block's exclusive prefix (lane u_q * kW + w_q
+              // of every warp's scan) + the prefix inside the block published before the barrier
+              const uint32_t q = j < n ? rs[j] : 0u;
+              const uint32_t blk = __shfl_sync(kFull, excl, (int)((q >> 8) * kW + ((q & 255u) >> 5)));
+              if (j < n) {
+                const int p = ks[j];
+                const uint32_t rel = pre[u] - blk - wexP[bb * 256 + p];  // bytes of the run before row j
+                d[u] = dstrow[j];
+                v[u] = baseP[bb * 512 + p] + rel + len[u];
+                cd[u] = baseP[bb * 512 + 256 + p] + rel;
+              }
+            } else if (j < n) {
               const int q = rs[j];
               d[u] = dstrow[j];
               v[u] = rt0[q] + pre[u] + len[u];
