@@ -61,6 +61,8 @@ struct SchemaDesc {
   // values, a row's byte length is its element count << arr_shift, and a null row has none
   int32_t arr_shift[kMaxCols];
   uint64_t list_mask;           // array columns that are lists
+  uint64_t listbit_mask;        // lists of bool elements: one bit each; their "characters" are the
+                                // element indices and out_chars is a bit region (0xff-filled)
 };
 
 // Device addresses of one input column of one batch.  offsets only for binary columns (int32,

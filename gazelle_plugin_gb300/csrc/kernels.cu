@@ -286,10 +286,12 @@ __global__ void __launch_bounds__(kHashThreads) k_hash_count(const SchemaDesc sd
     const int ak = sd.n_fixed + k;
     const int shift = kLists ? sd.arr_shift[ak] : 0;
     const bool list = kLists && ((sd.list_mask >> ak) & 1ull);
+    // readable elements: bytes, or bits of a list of bool elements
+    const uint64_t cap = kLists && ((sd.listbit_mask >> ak) & 1ull) ? c.values_bytes * 8 : c.values_bytes;
 #pragma unroll
     for (int u = 0; u < kHashRows; u++) {
       uint32_t len = (uint32_t)(o[u + 1] - o[u]) << shift;
-      if (act[u] && (o[u] < 0 || o[u + 1] < o[u] || ((uint64_t)o[u + 1] << shift) > c.values_bytes)) {
+      if (act[u] && (o[u] < 0 || o[u + 1] < o[u] || ((uint64_t)o[u + 1] << shift) > cap)) {
         bad = true;
         len = 0;
       }
@@ -1109,7 +1111,10 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
     const int32_t len = s_cr[k].y - s_cr[k].x;
     return len > 0 && len <= kCharStage;
   };
-  auto staged_binary = [&](int a) { return sd.arr_kind[a] == COL_BINARY && chars_staged(sd.arr_str[a]); };
+  // (the element bits of a list of bool elements are not staged: they are read from global memory)
+  auto staged_binary = [&](int a) {
+    return sd.arr_kind[a] == COL_BINARY && !(kLists && ((sd.listbit_mask >> a) & 1ull)) && chars_staged(sd.arr_str[a]);
+  };
 
   // Polls of a wait for data or for a free slot before the block gives up (a test lowers it to
   // make the waits run out); waits for copies already in flight always use kSpinLimit.
@@ -1514,7 +1519,14 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
           }
         }
         const int k = (int)(ct.z >> 24);
-        if (chars) {
+        if (kLists && ((sd.listbit_mask >> a) & 1ull)) {
+          // bool elements: each row's element bits [so, so + len) to the bit region at cd (its
+          // words start 0xff: the false ones are cleared)
+#pragma unroll
+          for (int u = 0; u < kRowsPerThread; u++)
+            if (threadIdx.x + u * kConsumers < n && len[u])
+              clear_null_elements(reinterpret_cast<uint32_t*>(ochars), cd[u], c.values, so[u], len[u]);
+        } else if (chars) {
           // shared address of byte 0 of the column (offsets index from there)
           const uint32_t cbase = smem_addr(staged_ptr(cstage, c.values + s_cr[k].x)) - (uint32_t)s_cr[k].x;
 #pragma unroll

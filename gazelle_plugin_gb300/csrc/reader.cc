@@ -64,7 +64,7 @@ Status PartitionReader::Cuda(cudaError_t e, const char* what) {
 Status PartitionReader::Make(std::vector<Field> fields, int device, std::unique_ptr<PartitionReader>* out) {
   std::unique_ptr<PartitionReader> r(new PartitionReader());
   for (const Field& f : fields) {
-    if (f.type == GZ_TYPE_LIST ? FixedWidth(f.elem) == 0
+    if (f.type == GZ_TYPE_LIST ? FixedWidth(f.elem) == 0 && f.elem != GZ_TYPE_BOOL
                                : f.type != GZ_TYPE_NULL && f.type != GZ_TYPE_BOOL && !IsBinaryType(f.type) &&
                                      FixedWidth(f.type) == 0)
       return Status::Error(GZ_NOT_IMPLEMENTED, "field type not implemented by the reader");
@@ -208,11 +208,11 @@ Status PartitionReader::ParseStream(const uint8_t* data, int64_t len, int stream
           if (nn == 0) c.validity.length = 0;
           if (cn == 0) c.cvalidity.length = 0;
           if (c.offsets.length < (b.rows + 1) * 4) return Status::Error(GZ_INVALID, "offsets buffer too short");
-          const int w = FixedWidth(fields_[f].elem);
+          const int w = FixedWidth(fields_[f].elem);  // 0: bool elements (bits)
           if (!c.offsets.decoded) {
             c.o0 = ReadOffset(data + c.offsets.offset, 4, 0);
             c.o1 = ReadOffset(data + c.offsets.offset, 4, b.rows);
-            if (c.o0 < 0 || c.o1 < c.o0 || c.o1 * w > c.values.length || c.o1 - c.o0 != cl)
+            if (c.o0 < 0 || c.o1 < c.o0 || (w ? c.o1 * w : (c.o1 + 7) / 8) > c.values.length || c.o1 - c.o0 != cl)
               return Status::Error(GZ_INVALID, "list offsets exceed the elements");
           }
           continue;
@@ -344,7 +344,8 @@ Status PartitionReader::AddStream(const uint8_t* data, int64_t len) {
         e += 2;
       }
       const int64_t w = fields_[which[i].second].type == GZ_TYPE_LIST ? FixedWidth(fields_[which[i].second].elem) : 1;
-      if (c.o0 < 0 || c.o1 < c.o0 || c.o1 * w > c.values.length) return Status::Error(GZ_INVALID, "offsets exceed the characters");
+      if (c.o0 < 0 || c.o1 < c.o0 || (w ? c.o1 * w : (c.o1 + 7) / 8) > c.values.length)
+        return Status::Error(GZ_INVALID, "offsets exceed the characters");
     }
     arena_mem_.push_back(arena);
   } else {
@@ -398,7 +399,8 @@ Status PartitionReader::Finish(int64_t* rows, int32_t* n_batches) {
     o_val[f] = total;
     total += t == GZ_TYPE_BOOL ? bit_bytes
              : IsBinaryType(t) ? AlignUp((size_t)chars[f] + 16, 256)
-             : t == GZ_TYPE_LIST ? AlignUp((size_t)chars[f] * FixedWidth(fields_[f].elem), 256)
+             : t == GZ_TYPE_LIST ? (fields_[f].elem == GZ_TYPE_BOOL ? AlignUp((size_t)((chars[f] + 31) / 32) * 4, 256)
+                                                                    : AlignUp((size_t)chars[f] * FixedWidth(fields_[f].elem), 256))
                                  : AlignUp((size_t)R * FixedWidth(t), 256);
   }
   total = std::max<size_t>(total, 256);
@@ -458,8 +460,15 @@ Status PartitionReader::Finish(int64_t* rows, int32_t* n_batches) {
           oj.push_back(OffsetJob{src_off + x * 4, dst_off + x * 4, (uint32_t)std::min<uint64_t>(kChunk / 4, n - x), 0u,
                                  char_pos[f] - c.o0});
         const int w = FixedWidth(fields_[f].elem);
-        add_bytes(Base(c.values, b.stream) + c.o0 * w, out_mem_ + o_val[f] + char_pos[f] * w,
-                  (uint64_t)(c.o1 - c.o0) * w);
+        if (w == 0) {  // bool elements: bits [o0, o1) to bit char_pos
+          for (uint64_t x = 0; x < (uint64_t)(c.o1 - c.o0); x += kBitChunk)
+            tj.push_back(BitJob{reinterpret_cast<const uint32_t*>(Base(c.values, b.stream)),
+                                reinterpret_cast<uint32_t*>(out_mem_ + o_val[f]), (uint64_t)c.o0 + x,
+                                (uint64_t)char_pos[f] + x, std::min<uint64_t>(kBitChunk, (uint64_t)(c.o1 - c.o0) - x)});
+        } else {
+          add_bytes(Base(c.values, b.stream) + c.o0 * w, out_mem_ + o_val[f] + char_pos[f] * w,
+                    (uint64_t)(c.o1 - c.o0) * w);
+        }
         if (o_cvalid[f] != SIZE_MAX && c.o1 > c.o0) {
           const uint8_t* cv = c.cvalidity.length ? Base(c.cvalidity, b.stream) : nullptr;
           for (uint64_t x = 0; x < (uint64_t)(c.o1 - c.o0); x += kBitChunk)
@@ -511,7 +520,9 @@ Status PartitionReader::Finish(int64_t* rows, int32_t* n_batches) {
     if (o_off[f] != SIZE_MAX) oc.offsets = out_mem_ + o_off[f];
     oc.values = out_mem_ + o_val[f];
     oc.values_bytes = t == GZ_TYPE_BOOL ? (R + 7) / 8 : IsBinaryType(t) ? chars[f]
-                      : t == GZ_TYPE_LIST ? chars[f] * FixedWidth(fields_[f].elem) : R * FixedWidth(t);
+                      : t == GZ_TYPE_LIST ? (fields_[f].elem == GZ_TYPE_BOOL ? (chars[f] + 7) / 8
+                                                                             : chars[f] * FixedWidth(fields_[f].elem))
+                                          : R * FixedWidth(t);
     if (t == GZ_TYPE_LIST) {
       oc.child_length = chars[f];
       if (o_cvalid[f] != SIZE_MAX) oc.child_validity = out_mem_ + o_cvalid[f];

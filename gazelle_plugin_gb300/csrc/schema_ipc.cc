@@ -134,8 +134,8 @@ bool ParseSchemaIpc(const uint8_t* data, int64_t len, std::vector<Field>* out, s
         return false;
     }
     if (list) {
-      if (f.type == GZ_TYPE_NULL || f.type == GZ_TYPE_BOOL || f.type >= GZ_TYPE_STRING) {
-        *err = "list elements of a fixed-width type only";
+      if (f.type == GZ_TYPE_NULL || f.type >= GZ_TYPE_STRING) {
+        *err = "list elements of a fixed-width or bool type only";
         return false;
       }
       f.elem = f.type;

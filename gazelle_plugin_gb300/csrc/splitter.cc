@@ -179,8 +179,8 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
     if (IsBinary(t)) bin.push_back((int32_t)i);
     else if (t == GZ_TYPE_NULL) continue;
     else if (t == GZ_TYPE_LIST) {
-      if (ByteWidth(fields_[i].elem) <= 0)
-        return Status::Error(GZ_NOT_IMPLEMENTED, "list columns of fixed-width elements only");
+      if (ByteWidth(fields_[i].elem) <= 0 && fields_[i].elem != GZ_TYPE_BOOL)
+        return Status::Error(GZ_NOT_IMPLEMENTED, "list columns of fixed-width or bool elements only");
       lists.push_back((int32_t)i);
     } else if (t == GZ_TYPE_BOOL || ByteWidth(t) > 0) array_idx_.push_back((int32_t)i);
     else return Status::Error(GZ_NOT_IMPLEMENTED, "field type not implemented in ColumnarShuffle");
@@ -221,6 +221,7 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
       while ((1 << sh) < ByteWidth(fields_[ci].elem)) sh++;
       sd_.arr_shift[a] = sh;
       sd_.list_mask |= 1ull << a;
+      if (fields_[ci].elem == GZ_TYPE_BOOL) sd_.listbit_mask |= 1ull << a;
     }
     // compared as an index of the output schema (the range partitioner's ids are not in it)
     if (a < n_policy_ && ci - out_shift() < fixed_cnt_) sd_.quirk_mask |= 1ull << a;
@@ -614,7 +615,7 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
         return Status::Error(GZ_INVALID, "list offsets buffer too small");
       need_[b0 + 1] = Need{reinterpret_cast<const uint8_t*>(addrs[b0 + 1]), ob};
       const int k = a - fixed_cnt_;
-      const int w = ByteWidth(fields_[f].elem);
+      const int w = ByteWidth(fields_[f].elem);  // 0: bool elements, one bit each
       const int64_t vsz = std::max<int64_t>(sizes[b0 + 3], 0);
       if (vsz > (int64_t)INT32_MAX)
         return Status::Error(GZ_NOT_IMPLEMENTED, "a list column batch with more than 2^31 - 1 element bytes");
@@ -622,14 +623,15 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
       if (host_in) {
         const int32_t* off = reinterpret_cast<const int32_t*>(addrs[b0 + 1]);
         const int64_t o0 = off[0], o1 = off[nr];
-        if (o1 < o0 || o0 < 0 || o1 * w > vsz) return Status::Error(GZ_INVALID, "list offsets exceed the element values");
+        if (o1 < o0 || o0 < 0 || (w ? o1 * w : BytesForBits(o1)) > vsz)
+          return Status::Error(GZ_INVALID, "list offsets exceed the element values");
         if (addrs[b0 + 2] != 0 && eb > 0 && (int64_t)eb < BytesForBits(o1))
           return Status::Error(GZ_INVALID, "element validity buffer too small");
-        vb = (size_t)(o1 * w);
+        vb = (size_t)(w ? o1 * w : BytesForBits(o1));
         eb = eb > 0 ? (size_t)BytesForBits(o1) : 0;
-        char_scratch_[k] = (uint64_t)((o1 - o0) * w);
+        char_scratch_[k] = (uint64_t)((o1 - o0) * std::max(w, 1));  // bool elements: one "byte" each
       } else {
-        char_scratch_[k] = (uint64_t)vb;
+        char_scratch_[k] = (uint64_t)(w ? vb : vb * 8);
       }
       if (addrs[b0 + 2] != 0 && eb > 0) {
         need_[b0 + 2] = Need{reinterpret_cast<const uint8_t*>(addrs[b0 + 2]), eb};
@@ -739,7 +741,7 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
             // same 16-byte phase as the source when that keeps the elements aligned
             const uintptr_t sp = reinterpret_cast<uintptr_t>(nd.src);
             const uintptr_t elem = j == 0 ? 1
-                                 : list ? (j == 1 ? 4 : j == 2 ? 1 : (uintptr_t)ByteWidth(fields_[f].elem))
+                                 : list ? (j == 1 ? 4 : j == 2 ? 1 : (uintptr_t)std::max(1, ByteWidth(fields_[f].elem)))
                                  : IsBinary(t) ? (j == 1 ? (uintptr_t)OffW(t) : 1)
                                  : t == GZ_TYPE_BOOL ? 1 : (uintptr_t)ByteWidth(t);
             if (sp % elem == 0) phase = sp & 15;
@@ -792,7 +794,7 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
           cp.values = reinterpret_cast<const uint8_t*>(addrs[b0 + 3]);
           cp.values_bytes = (uint64_t)std::max<int64_t>(sizes[b0 + 3], 0);
           if (reinterpret_cast<uintptr_t>(cp.offsets) % 4 ||
-              reinterpret_cast<uintptr_t>(cp.values) % (uintptr_t)ByteWidth(fields_[f].elem))
+              reinterpret_cast<uintptr_t>(cp.values) % (uintptr_t)std::max(1, ByteWidth(fields_[f].elem)))
             return Status::Error(GZ_INVALID, "device list buffers must be aligned to their widths");
           if (cp.values == nullptr) cp.values = reinterpret_cast<const uint8_t*>(addrs[b0 + 1]);  // no elements
         } else {
@@ -931,6 +933,7 @@ Status Splitter::Flush() {
     } else if (kind == COL_BINARY) {
       fr.off_values[a] = o;
       o += AlignUp((size_t)R * sd_.arr_width[a], 256);  // end offsets, 4 or 8 bytes
+      if ((sd_.listbit_mask >> a) & 1ull) continue;     // bool elements: a bit region, below
       uint64_t cb = 0;
       for (uint32_t b = 0; b < NB; b++) cb += pending_chars_[(size_t)b * n_str_ + sd_.arr_str[a]];
       fr.off_chars[a] = o;
@@ -946,6 +949,12 @@ Status Splitter::Flush() {
     if (any_valid & (1ull << a)) {
       fr.off_valid[a] = o;
       o += vwords_bytes;
+    }
+    if ((sd_.listbit_mask >> a) & 1ull) {  // a list of bool elements: one bit per element
+      uint64_t cb = 0;
+      for (uint32_t b = 0; b < NB; b++) cb += pending_chars_[(size_t)b * n_str_ + sd_.arr_str[a]];
+      fr.off_chars[a] = o;
+      o += AlignUp((size_t)((cb + 31) / 32 * 4) + 8, 256);
     }
     if (any_cvalid & (1ull << a)) {  // one bit per element byte group of the column's characters
       uint64_t cb = 0;
@@ -1513,6 +1522,12 @@ Status Splitter::BuildSegment(int p, const Segment& s, SegMsg* msg, bool device_
       for (const Piece& pc : s.pieces) elems += (pc.fb1[k] - pc.fb0[k]) >> sh;
       temps.emplace_back((size_t)BytesForBits((int64_t)elems), 0);
       uint8_t* ev = temps.back().data();
+      const bool bitvals = (sd_.listbit_mask >> a) & 1ull;  // bool elements: gathered bits
+      uint8_t* bv = nullptr;
+      if (bitvals) {
+        temps.emplace_back((size_t)BytesForBits((int64_t)elems), 0);
+        bv = temps.back().data();
+      }
       uint64_t erow = 0;
       for (const Piece& pc : s.pieces) {
         const FlushRec& f = flushes_[pc.flush];
@@ -1522,8 +1537,9 @@ Status Splitter::BuildSegment(int p, const Segment& s, SegMsg* msg, bool device_
                              (int64_t)(pc.frow1 - pc.frow0) * 4, dev});
         const uint32_t c0 = pc.fb0[k], c1 = pc.fb1[k];
         const size_t cb = (size_t)f.cstart(P, nstr)[(size_t)k * P + p] + c0;
-        if (c1 > c0) vals.push_back(Chunk{fb + f.off_chars[a] + cb, (int64_t)(c1 - c0), dev});
         const uint64_t m = (c1 - c0) >> sh;
+        if (bitvals) CopyBits(bit_base(f, f.off_chars[a]), cb, bv, erow, m);
+        else if (c1 > c0) vals.push_back(Chunk{fb + f.off_chars[a] + cb, (int64_t)(c1 - c0), dev});
         if (f.off_cvalid[a] != SIZE_MAX) {
           CopyBits(bit_base(f, f.off_cvalid[a]), cb >> sh, ev, erow, m);
         } else {
@@ -1531,6 +1547,7 @@ Status Splitter::BuildSegment(int p, const Segment& s, SegMsg* msg, bool device_
         }
         erow += m;
       }
+      if (bitvals) vals.push_back(Chunk{bv, BytesForBits((int64_t)elems)});
       const int64_t cnulls = CountZeros(ev, (int64_t)elems);
       ChunkedBuffer cvb;
       if (cnulls > 0) cvb.push_back(Chunk{ev, BytesForBits((int64_t)elems)});
@@ -2091,7 +2108,8 @@ Status Splitter::CompressedSize(int32_t num_rows, const int64_t* addrs, const in
         for (int64_t e = e0; e < e1 && !enull; e++) enull = !((ev[e >> 3] >> (e & 7)) & 1);
       bufs.push_back({ev, enull ? BytesForBits(e1 - e0) : 0});
       const int w = ByteWidth(fields_[f].elem);
-      bufs.push_back({reinterpret_cast<const uint8_t*>(addrs[b0 + 3]) + e0 * w, (e1 - e0) * w});
+      if (w == 0) bufs.push_back({reinterpret_cast<const uint8_t*>(addrs[b0 + 3]) + e0 / 8, BytesForBits(e1 - e0)});
+      else bufs.push_back({reinterpret_cast<const uint8_t*>(addrs[b0 + 3]) + e0 * w, (e1 - e0) * w});
       continue;
     }
     if (IsBinary(t)) {

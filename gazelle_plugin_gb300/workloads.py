@@ -258,7 +258,8 @@ def c4_batch(rng, schema_index: int, n: int) -> Batch:
 def list_column(rng, field: Field, n: int, null_frac: float, elem_null_frac: float, max_len: int,
                 values=None) -> List[np.ndarray]:
     """Buffers of a list column of `n` rows: lengths U{0..max_len} (0 for a null row), elements
-    of field.elem drawn like a flat column's (or taken from `values`), element nulls i.i.d."""
+    of field.elem drawn like a flat column's (or taken from `values`; bool elements bit-packed),
+    element nulls i.i.d."""
     valid = rng.random(n) >= null_frac if null_frac > 0 else np.ones(n, bool)
     lens = np.where(valid, rng.integers(0, max_len + 1, size=n), 0).astype(np.int32)
     offsets = np.zeros(n + 1, np.int32)
@@ -270,12 +271,16 @@ def list_column(rng, field: Field, n: int, null_frac: float, elem_null_frac: flo
             values = rng.integers(0, 2**63, size=2 * m, dtype=np.uint64)
         elif field.elem in ("float16", "float32", "float64"):
             values = rng.standard_normal(m) * 1e3
+        elif field.elem == "bool":
+            values = rng.integers(0, 2, size=m)
         else:
             w = BYTE_WIDTH[field.elem]
             hi = 2 ** (8 * w - 1) if w < 8 else 2**62
             values = rng.integers(-hi if field.elem[0] != "u" else 0, hi, size=m)
     evalid = rng.random(m) >= elem_null_frac if elem_null_frac > 0 else np.ones(m, bool)
-    if field.elem == "decimal128":
+    if field.elem == "bool":
+        vals = np.packbits((np.asarray(values) % 2).astype(np.uint8), bitorder="little")
+    elif field.elem == "decimal128":
         vals = np.ascontiguousarray(np.asarray(values, np.uint64)).view(np.uint8)
     else:
         vals = np.ascontiguousarray(np.asarray(values).astype(NUMPY_DTYPE[ef.type])).view(np.uint8)

@@ -150,6 +150,20 @@ def read_partition(schema, streams: Sequence[bytes]):
             vals = np.concatenate([_bits(c[fi][1][1], r) for r, c in batches]) if batches else np.zeros(0, bool)
             cols.append((valid, None, vals))
         elif f.is_list:  # (validity, offsets, (element validity or None, element values))
+            if f.elem == "bool":  # element values as a bool array
+                offs, vals, evalid, base = [np.zeros(1, np.int32)], [], [], 0
+                any_null = any(c[fi][2] for _, c in batches)
+                for r, c in batches:
+                    o = np.frombuffer(c[fi][1][1], np.int32)[:r + 1]
+                    m = int(o[r] - o[0])
+                    vals.append(_bits(c[fi][1][3], int(o[r]))[o[0]:])
+                    offs.append((o[1:] - o[0] + base).astype(np.int32))
+                    if any_null:
+                        evalid.append(_bits(c[fi][1][2], int(o[r]))[o[0]:] if c[fi][2] else np.ones(m, bool))
+                    base += m
+                ev = (np.concatenate(evalid) if evalid else np.zeros(0, bool)) if any_null else None
+                cols.append((valid, np.concatenate(offs), (ev, np.concatenate(vals) if vals else np.zeros(0, bool))))
+                continue
             w = BYTE_WIDTH[f.elem]
             offs, vals, evalid, base = [np.zeros(1, np.int32)], [], [], 0
             any_null = any(c[fi][2] for _, c in batches)

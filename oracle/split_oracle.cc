@@ -292,8 +292,8 @@ class OracleSplitter {
       int t = fields_[i].type;
       if (IsBinary(t)) bin.push_back(i);
       else if (t == T_NULL) continue;
-      else if (t == T_LIST) {  // list_array_idx_ (splitter.cc:254-258), elements of fixed width
-        if (ByteWidth(fields_[i].elem) <= 0) return "list element type not supported";
+      else if (t == T_LIST) {  // list_array_idx_ (splitter.cc:254-258), fixed-width or bool elements
+        if (ByteWidth(fields_[i].elem) <= 0 && fields_[i].elem != T_BOOL) return "list element type not supported";
         list_idx_.push_back(i);
       }
       else if (t == T_BOOL || ByteWidth(t) > 0) array_idx_.push_back(i);
@@ -597,12 +597,13 @@ class OracleSplitter {
         const int w = ByteWidth(fields_[f].elem);
         b.valid.resize((size_t)BytesForBits(n), 0);
         b.cvalid.resize((size_t)BytesForBits(b.elems), 0);
+        if (w == 0) b.cvals.resize((size_t)BytesForBits(b.elems), 0);
         nodes.push_back({n, b.nulls});
         body.push_back(b.nulls > 0 ? BodyBuf{b.valid.data(), BytesForBits(n)} : BodyBuf{nullptr, 0});
         body.push_back({(const uint8_t*)b.offs.data(), (int64_t)(n + 1) * 4});
         nodes.push_back({b.elems, b.cnulls});
         body.push_back(b.cnulls > 0 ? BodyBuf{b.cvalid.data(), BytesForBits(b.elems)} : BodyBuf{nullptr, 0});
-        body.push_back({b.cvals.data(), b.elems * w});
+        body.push_back({b.cvals.data(), w == 0 ? BytesForBits(b.elems) : b.elems * w});
         // batch_nbytes counts the list's own buffers (splitter.cc:438-453)
         raw += (b.nulls > 0 ? BytesForBits(n) : 0) + (int64_t)(n + 1) * 4;
         continue;
@@ -769,7 +770,7 @@ class OracleSplitter {
     // SplitListArray (splitter.cc:1322-1333): every row to its partition's builder
     for (size_t li = 0; li < list_idx_.size(); li++) {
       const InCol& c = cols[list_idx_[li]];
-      const int w = ByteWidth(fields_[list_idx_[li]].elem);
+      const int w = ByteWidth(fields_[list_idx_[li]].elem);  // 0: bool elements, one bit each
       const int32_t* off = (const int32_t*)c.offsets;
       for (int32_t r = 0; r < n; r++) {
         ListBuf& b = lists_[li][pid_[r]];
@@ -785,7 +786,8 @@ class OracleSplitter {
           const bool cv = c.child_validity == nullptr || GetBit(c.child_validity, e);
           PutBit(b.cvalid, b.elems, cv);
           b.cnulls += !cv;
-          b.cvals.insert(b.cvals.end(), c.values + (size_t)e * w, c.values + (size_t)(e + 1) * w);
+          if (w == 0) PutBit(b.cvals, b.elems, GetBit(c.values, e));
+          else b.cvals.insert(b.cvals.end(), c.values + (size_t)e * w, c.values + (size_t)(e + 1) * w);
           b.elems++;
         }
         b.offs.push_back(b.offs.back() + (off[r + 1] - off[r]));

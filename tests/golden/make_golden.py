@@ -175,10 +175,11 @@ def large_case(seed):
     return schema, batches, P, keys, opts
 
 
-LIST_ELEMS = ["int8", "int16", "int32", "int64", "float32", "float64", "date32", "decimal128", "timestamp"]
+LIST_ELEMS = ["int8", "int16", "int32", "int64", "float32", "float64", "date32", "decimal128", "timestamp",
+              "bool"]
 
 
-def list_case(seed):
+def list_case(seed, force_elem=None):
     """Schema, batches, P, keys and options of a `list_<n>` case: an int key, 0-2 fixed-width
     columns, 1-3 list columns of fixed-width elements (list and element nulls, or none, or no
     validity buffers) and 0-1 utf8 column, in random order."""
@@ -186,6 +187,8 @@ def list_case(seed):
     fields = [W.Field("k", str(rng.choice(["int32", "int64"])), False)]
     fields += [W.Field(f"f{i}", str(rng.choice(["int32", "float64", "bool"]))) for i in range(int(rng.integers(0, 3)))]
     fields += [W.Field(f"L{i}", "list", True, str(rng.choice(LIST_ELEMS))) for i in range(int(rng.integers(1, 4)))]
+    if force_elem:  # the first list column's elements
+        fields = [W.Field(f.name, f.type, f.nullable, force_elem) if f.name == "L0" else f for f in fields]
     fields += [W.Field("s", "utf8")] * int(rng.integers(0, 2))
     schema = [fields[i] for i in rng.permutation(len(fields))]
     keys = [i for i, f in enumerate(schema) if f.name == "k"]
@@ -215,6 +218,10 @@ def list_cases():
     schema, batches, P, keys, opts = list_case(5100)
     yield ("list_write_schema", schema, batches, P, keys, dict(opts, write_schema=True),
            {"workload": "list", "seed": 5100})
+    for seed in range(4):
+        schema, batches, P, keys, opts = list_case(5200 + seed, "bool")
+        yield (f"list_bool_{seed}", schema, batches, P, keys, opts,
+               {"workload": "list", "seed": 5200 + seed, "force_elem": "bool"})
 
 
 def large_cases():
@@ -232,7 +239,7 @@ def regenerate(case):
     if g["workload"] == "large":
         return large_case(g["seed"])[1]
     if g["workload"] == "list":
-        return list_case(g["seed"])[1]
+        return list_case(g["seed"], g.get("force_elem"))[1]
     if g["workload"] == "c1":
         return W.c1_batches(g["seed"], g["num_batches"], g["rows"])
     if g["workload"] == "c2":

@@ -38,11 +38,11 @@ def test_oracle_matches_reference_list_columns(case):
 
 
 def _wide(seed, nb=6, rows=4096, elem_nulls=0.05):
-    """An int64 key, an int32, list<int32>, list<float64>, list<decimal128>, a utf8."""
+    """An int64 key, an int32, list<int32>, list<float64>, list<decimal128>, a utf8, list<bool>."""
     rng = np.random.default_rng(seed)
     schema = [W.Field("k", "int64", False), W.Field("i", "int32"), W.Field("a", "list", True, "int32"),
               W.Field("b", "list", True, "float64"), W.Field("d", "list", True, "decimal128"),
-              W.Field("s", "utf8")]
+              W.Field("s", "utf8"), W.Field("q", "list", True, "bool")]
     out = []
     for _ in range(nb):
         bufs = W._column(rng, schema[0], rows, rng.integers(0, 1 << 40, size=rows), 0.0)
@@ -51,6 +51,7 @@ def _wide(seed, nb=6, rows=4096, elem_nulls=0.05):
         bufs += W.list_column(rng, schema[3], rows, 0.0, 0.0, 3)
         bufs += W.list_column(rng, schema[4], rows, 0.3, elem_nulls, 2)
         bufs += W._column(rng, schema[5], rows, None, 0.05, (0, 12, W.AZ))
+        bufs += W.list_column(rng, schema[6], rows, 0.1, elem_nulls, 37)
         out.append(W.Batch(rows, bufs))
     return schema, out
 
@@ -211,6 +212,10 @@ def test_oracle_reader_concatenates_list_columns_like_arrow():
             assert (evalid is None) == (child.null_count == 0)
             if evalid is not None:
                 assert np.array_equal(evalid, child.is_valid().to_numpy(zero_copy_only=False))
+            if f.elem == "bool":
+                bits = np.unpackbits(np.frombuffer(child.buffers()[1], np.uint8), bitorder="little")
+                assert np.array_equal(vals, bits[child.offset:child.offset + len(child)].astype(bool))
+                continue
             w = W.BYTE_WIDTH[f.elem]
             assert vals == child.buffers()[1].to_pybytes()[child.offset * w:(child.offset + len(child)) * w]
 
@@ -249,5 +254,7 @@ def test_gpu_reader_list_columns(codec):
                     assert ge.tobytes() == R.pack_bits(evalid)
             elif f.is_binary:
                 assert np.array_equal(go, offs)
+            if f.is_list and f.elem == "bool":
+                vals = R.pack_bits(vals)
             assert gvals.tobytes() == vals
         r.close()
