@@ -21,7 +21,7 @@ slot; a null fixed-width cell keeps its generated value):
 from __future__ import annotations
 
 import dataclasses
-from typing import List, Optional, Sequence
+from typing import List, Optional, Sequence, Tuple
 
 import numpy as np
 
@@ -31,7 +31,8 @@ TYPE_CODES = {
     "float16": 6, "int32": 7, "uint32": 8, "float32": 9, "date32": 10, "time32": 11,
     "int64": 12, "uint64": 13, "float64": 14, "date64": 15, "time64": 16,
     "timestamp": 17, "decimal128": 18, "utf8": 19, "binary": 20,
-    "large_utf8": 21, "large_binary": 22, "list": 23,
+    "large_utf8": 21, "large_binary": 22, "list": 23, "large_list": 24, "struct": 25,
+    "map": 26,
 }
 BYTE_WIDTH = {
     "int8": 1, "uint8": 1, "int16": 2, "uint16": 2, "float16": 2, "int32": 4,
@@ -51,7 +52,10 @@ class Field:
     name: str
     type: str
     nullable: bool = True
-    elem: Optional[str] = None  # list: the element type (fixed width; elements nullable)
+    elem: Optional[str] = None  # list: the element type (fixed width or bool; elements nullable)
+    # nested types: a list / large_list's element field, a map's key and value fields (the
+    # entries struct between them is implicit), a struct's fields
+    children: Tuple["Field", ...] = ()
 
     @property
     def code(self) -> int:
@@ -59,12 +63,40 @@ class Field:
 
     @property
     def is_list(self) -> bool:
-        return self.type == "list"
+        """A list of fixed-width or bool elements given by `elem`."""
+        return self.type == "list" and not self.children
+
+    @property
+    def is_nested(self) -> bool:
+        """Any other list, large_list, struct or map (children given by `children`)."""
+        return self.type in ("large_list", "struct", "map") or (self.type == "list" and bool(self.children))
+
+    @property
+    def kids(self) -> Tuple["Field", ...]:
+        if self.is_list:
+            return (Field("item", self.elem, True),)
+        return self.children
+
+    def type_nodes(self) -> List[int]:
+        """The field's type tree in pre-order, each node's code with its child count above the
+        low byte (a map's entries struct included)."""
+        kids = self.kids
+        if self.type == "map":
+            kids = (Field("entries", "struct", False, children=self.children),)
+        out = [self.code | (len(kids) << 8)]
+        for k in kids:
+            out += k.type_nodes()
+        return out
 
     @property
     def buffer_count(self) -> int:
         """Entries of the field in a batch's flat buffer list: [validity, (offsets), values];
-        a list: [validity, offsets, element validity, element values]."""
+        a list: [validity, offsets, element validity, element values]; nested types depth
+        first as the JNI's MakeArrayData reads them: [validity, (offsets)] then the children's
+        (a map's entries struct adds its validity entry)."""
+        if self.is_nested:
+            own = 1 if self.type == "struct" else 2
+            return own + (self.type == "map") + sum(k.buffer_count for k in self.kids)
         return 4 if self.is_list else 3 if self.is_binary else 2
 
     @property
@@ -138,6 +170,7 @@ C1_SCHEMA = [Field("k", "int32", False), Field("v1", "int64"), Field("v2", "floa
 C1_KEYS = [0]
 C1_PARTITIONS = 8
 AZ = b"abcdefghijklmnopqrstuvwxyz"
+AZ_BYTES = np.frombuffer(AZ, np.uint8)
 
 
 def c1_batch(rng, n: int = 4096) -> Batch:
@@ -285,6 +318,54 @@ def list_column(rng, field: Field, n: int, null_frac: float, elem_null_frac: flo
     else:
         vals = np.ascontiguousarray(np.asarray(values).astype(NUMPY_DTYPE[ef.type])).view(np.uint8)
     return [pack_validity(valid), offsets.view(np.uint8), pack_validity(evalid), vals]
+
+
+def nested_column(rng, field: Field, n: int, null_frac: float = 0.1, max_len: int = 4,
+                  top: bool = True, spans: bool = False) -> List[np.ndarray]:
+    """Buffers of `n` entries of a field of any nesting, depth first (MakeArrayData order).
+    Entries are null with probability null_frac (never a map key); list / map lengths
+    U{0..max_len}, strings 0-7 letters.  A null list / map / string entry holds no elements,
+    except with `spans` at the top level (or under top-level structs), where it keeps a
+    non-empty range that the split must drop."""
+    valid = rng.random(n) >= null_frac if (null_frac > 0 and field.nullable) else np.ones(n, bool)
+    vbuf = pack_validity(valid)
+    t = field.type
+
+    def lengths(hi):
+        lens = rng.integers(0, hi + 1, size=n)
+        return lens if (spans and top) else np.where(valid, lens, 0)
+
+    if t in ("list", "large_list", "map"):
+        offs = np.zeros(n + 1, np.int64 if t == "large_list" else np.int32)
+        np.cumsum(lengths(max_len), out=offs[1:])
+        m = int(offs[-1])
+        out = [vbuf, offs.view(np.uint8)]
+        if t == "map":
+            key, val = field.kids
+            out.append(np.zeros(0, np.uint8))  # the entries struct: no validity
+            out += nested_column(rng, key, m, 0.0, max_len, False)
+            out += nested_column(rng, val, m, null_frac, max_len, False)
+        else:
+            out += nested_column(rng, field.kids[0], m, null_frac, max_len, False)
+        return out
+    if t == "struct":
+        out = [vbuf]
+        for k in field.kids:
+            out += nested_column(rng, k, n, null_frac, max_len, top, spans)
+        return out
+    if field.is_binary:
+        offs = np.zeros(n + 1, field.offset_dtype)
+        np.cumsum(lengths(7), out=offs[1:])
+        chars = AZ_BYTES[rng.integers(0, 26, size=int(offs[-1]))]
+        return [vbuf, offs.view(np.uint8), chars.astype(np.uint8)]
+    if t == "bool":
+        return [vbuf, np.packbits(rng.integers(0, 2, size=n).astype(np.uint8), bitorder="little")]
+    if t == "decimal128":
+        return [vbuf, rng.integers(0, 2**63, size=2 * n, dtype=np.uint64).view(np.uint8)]
+    w = BYTE_WIDTH[t]
+    hi = 2 ** (8 * w - 1) if w < 8 else 2**62
+    v = rng.integers(-hi if t[0] != "u" else 0, hi, size=n).astype(NUMPY_DTYPE[t])
+    return [vbuf, v.view(np.uint8)]
 
 
 def c4_rows(rng, size=None):

@@ -123,12 +123,11 @@ class OracleSplitter:
                  offheap_per_task: int = 0, buffer_size: int = 4096, prefer_spill: bool = True,
                  write_schema: bool = False, short_name: str = "hash"):
         self.P = 1 if short_name == "single" else num_partitions
-        # a list field's code carries its element type above the low byte
-        types = np.array([f.code | ((f.__class__("e", f.elem).code << 8) if f.is_list else 0) for f in schema],
-                         np.int32)
+        # the fields' type trees in pre-order (child counts above the low byte)
+        types = np.array([c for f in schema for c in f.type_nodes()], np.int32)
         keys = np.array(key_cols, np.int32)
         err = ctypes.create_string_buffer(512)
-        self.h = self.lib().gzo_make(short_name.encode(), types.ctypes.data, len(types),
+        self.h = self.lib().gzo_make(short_name.encode(), types.ctypes.data, len(schema),
                                      num_partitions, keys.ctypes.data, len(keys),
                                      offheap_per_task, buffer_size, int(prefer_spill), err, 512)
         if not self.h:
@@ -202,9 +201,18 @@ def to_pyarrow_schema(schema):
          "large_utf8": pa.large_string(), "large_binary": pa.large_binary()}
     units = ["s", "ms", "us", "ns"]
 
+    def fld(k):
+        return pa.field(k.name, typ(k), k.nullable)
+
     def typ(f):
-        if f.is_list:  # Arrow's default list element field: "item", nullable
-            return pa.list_(pa.field("item", typ(type(f)("item", f.elem)), True))
+        if f.type == "list":  # a simple list's element field: Arrow's default "item", nullable
+            return pa.list_(fld(f.kids[0]))
+        if f.type == "large_list":
+            return pa.large_list(fld(f.kids[0]))
+        if f.type == "struct":
+            return pa.struct([fld(k) for k in f.kids])
+        if f.type == "map":
+            return pa.map_(typ(f.kids[0]), fld(f.kids[1]))
         prec, scale, unit = f.params
         if f.type == "decimal128":
             return pa.decimal128(prec, scale)

@@ -36,8 +36,9 @@ void SetErr(const arrow::Status& s, char* err, int errlen) {
 }
 
 // One array of `type` from the flat buffer list at *idx, in the JNI's order (jni_common.h:
-// 308-382 MakeArrayData): [validity, (offsets), values] for flat types, [validity, offsets,
-// <child buffers>] for list / large_list.  num_rows < 0: taken from the offsets (a child).
+// 186-382 MakeArrayData): [validity, (offsets), values] for flat types, [validity, offsets,
+// <child buffers>] for list / large_list / map, [validity, <field buffers>] for struct.
+// num_rows < 0: taken from the offsets, the first field or the values (a child).
 arrow::Status WrapArray(const std::shared_ptr<arrow::DataType>& type, int64_t num_rows,
                         const std::vector<std::shared_ptr<arrow::Buffer>>& bufs, int* idx,
                         std::shared_ptr<arrow::ArrayData>* out) {
@@ -52,6 +53,34 @@ arrow::Status WrapArray(const std::shared_ptr<arrow::DataType>& type, int64_t nu
   if (*idx >= n) return arrow::Status::Invalid("insufficient number of buffers");
   int64_t null_count = bufs[*idx]->size() == 0 ? 0 : arrow::kUnknownNullCount;
   ab.push_back(bufs[(*idx)++]);
+  if (type->id() == arrow::Type::STRUCT) {  // [validity] then each field's buffers
+    std::vector<std::shared_ptr<arrow::ArrayData>> kids;
+    for (int k = 0; k < type->num_fields(); k++) {
+      std::shared_ptr<arrow::ArrayData> child;
+      ARROW_RETURN_NOT_OK(WrapArray(type->field(k)->type(), -1, bufs, idx, &child));
+      kids.push_back(std::move(child));
+    }
+    if (num_rows < 0) num_rows = kids.empty() ? 0 : kids[0]->length;
+    *out = arrow::ArrayData::Make(type, num_rows, std::move(ab), std::move(kids), null_count);
+    return arrow::Status::OK();
+  }
+  if (type->id() == arrow::Type::MAP) {  // [validity, offsets] then the entries struct's
+    if (*idx >= n) return arrow::Status::Invalid("insufficient number of buffers");
+    if (num_rows < 0) num_rows = bufs[*idx]->size() / 4 - 1;
+    ab.push_back(bufs[(*idx)++]);
+    std::shared_ptr<arrow::ArrayData> child;
+    ARROW_RETURN_NOT_OK(WrapArray(type->field(0)->type(), -1, bufs, idx, &child));
+    if (child->null_count == arrow::kUnknownNullCount) {  // the entries' validity is dropped
+      child->buffers.at(0) = nullptr;
+      child->null_count = 0;
+    }
+    if (child->child_data.size() != 2) return arrow::Status::Invalid("Map array child array should have two fields");
+    if (child->child_data[0]->null_count == arrow::kUnknownNullCount &&
+        child->child_data[0]->GetNullCount() != 0)
+      return arrow::Status::Invalid("Map array keys array should have no nulls");
+    *out = arrow::ArrayData::Make(type, num_rows, std::move(ab), {child}, null_count);
+    return arrow::Status::OK();
+  }
   if (type->id() == arrow::Type::LIST || type->id() == arrow::Type::LARGE_LIST) {
     if (*idx >= n) return arrow::Status::Invalid("insufficient number of buffers");
     const int ow = type->id() == arrow::Type::LIST ? 4 : 8;

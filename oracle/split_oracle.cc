@@ -16,6 +16,7 @@
  *   Split{FixedWidthValue,Validity,Binary}Buffer / SplitBoolType                 splitter.cc:939-1303
  *   CacheRecordBatch (slice, raw size, IPC payload)                              splitter.cc:438-608
  *   SpillPartition / SpillLargestPartition / SpillFixedSize                      splitter.cc:741-799
+ *   nested columns (list / large_list / map / struct) through Arrow builders       splitter.cc:1322-1344
  *   Stop / WriteCachedRecordBatchAndClose / EOS                                  splitter.cc:84-172,395-437
  * Arrow IPC framing restates the Arrow C++ writer (continuation token, int32 metadata
  * length padded to 8, flatbuffer Message{RecordBatch}, 8-byte padded body; a validity
@@ -31,6 +32,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <functional>
 #include <memory>
 #include <numeric>
 #include <string>
@@ -48,8 +50,10 @@ enum TypeCode {
   T_HALF_FLOAT = 6, T_INT32 = 7, T_UINT32 = 8, T_FLOAT32 = 9, T_DATE32 = 10,
   T_TIME32 = 11, T_INT64 = 12, T_UINT64 = 13, T_FLOAT64 = 14, T_DATE64 = 15,
   T_TIME64 = 16, T_TIMESTAMP = 17, T_DECIMAL128 = 18, T_STRING = 19, T_BINARY = 20,
-  T_LARGE_STRING = 21, T_LARGE_BINARY = 22, T_LIST = 23,
+  T_LARGE_STRING = 21, T_LARGE_BINARY = 22, T_LIST = 23, T_LARGE_LIST = 24, T_STRUCT = 25,
+  T_MAP = 26,
 };
+bool IsNested(int t) { return t == T_LIST || t == T_LARGE_LIST || t == T_STRUCT || t == T_MAP; }
 
 int ByteWidth(int t) {
   switch (t) {
@@ -221,32 +225,201 @@ std::vector<uint8_t> EncodeRecordBatch(int64_t length,
   return out;
 }
 
+// A schema field; nested types carry their children: list / large_list one (the element),
+// map one (the entries struct of key and value), struct its fields.
 struct Field {
   int type;
   std::string name;
-  int elem = 0;  // list: the element type (fixed width)
+  std::vector<Field> kids;
 };
 
-struct InCol {
+// One input array (jni_common.h:186-300 MakeArrayData): buffers of the node, children below.
+struct InNode {
   const uint8_t* validity = nullptr;  // nullptr when the validity buffer is empty
-  const uint8_t* offsets = nullptr;
-  const uint8_t* values = nullptr;    // list: the element values
-  const uint8_t* child_validity = nullptr;  // list: the elements' validity (nullptr: none)
-  int64_t null_count = 0;
+  const uint8_t* offsets = nullptr;   // binary / list / map
+  const uint8_t* values = nullptr;    // fixed width, bool bits, binary characters
+  int64_t null_count = 0;             // top level: counted; children: unused
+  std::vector<InNode> kids;
 };
+using InCol = InNode;
 
-// One partition's list builder (partition_list_builders_, splitter.cc:292-296, 664-674): rows
-// appended with ListBuilder::AppendArraySlice (AppendList, splitter.cc:1335-1344) - a null row
-// adds no elements - and finished by CacheRecordBatch (splitter.cc:532-545).  Bitmaps are
-// zero-padded like an Arrow builder's; each is written only when it holds a null.
-struct ListBuf {
-  std::vector<uint8_t> valid, cvalid, cvals;
-  std::vector<int32_t> offs{0};
-  int64_t rows = 0, nulls = 0, elems = 0, cnulls = 0;
-};
 inline void PutBit(std::vector<uint8_t>& v, int64_t i, bool b) {
   if ((int64_t)v.size() * 8 <= i) v.resize((size_t)(i / 8 + 1), 0);
   if (b) v[(size_t)(i >> 3)] |= (uint8_t)(1u << (i & 7));
+}
+
+// One partition's builder of a nested column (partition_list_builders_, splitter.cc:292-296,
+// 664-674), filled by AppendArraySlice one row at a time (AppendList, splitter.cc:1335-1344)
+// with the Arrow builders' semantics:
+//   list / large_list / map: a null entry appends no elements, a valid one its slice;
+//   struct: every child appends the same slice, null entries included;
+//   binary: a null entry appends no bytes; fixed width and bool: values copied under nulls.
+// A map's entries struct is all valid (its builder is sized from the keys).  Finish writes the
+// nodes in pre-order with [validity, (offsets), (values)] each, a bitmap only when it holds a
+// null, zero-padded like an Arrow builder's.
+struct NodeBuf {
+  std::vector<uint8_t> valid, data;
+  std::vector<int64_t> offs{0};
+  int64_t len = 0, nulls = 0, nbits = 0;
+  std::vector<NodeBuf> kids;
+};
+
+void InitNode(const Field& t, NodeBuf* b) {
+  *b = NodeBuf();
+  b->kids.resize(t.kids.size());
+  for (size_t i = 0; i < t.kids.size(); i++) InitNode(t.kids[i], &b->kids[i]);
+}
+
+void AppendValidity(NodeBuf* b, const uint8_t* validity, int64_t off, int64_t len) {
+  for (int64_t i = 0; i < len; i++) {
+    const bool v = validity == nullptr || GetBit(validity, off + i);
+    PutBit(b->valid, b->len + i, v);
+    b->nulls += !v;
+  }
+}
+
+void AppendSlice(const Field& t, NodeBuf* b, const InNode& in, int64_t off, int64_t len) {
+  if (t.type == T_STRUCT) {
+    for (size_t k = 0; k < t.kids.size(); k++) AppendSlice(t.kids[k], &b->kids[k], in.kids[k], off, len);
+    AppendValidity(b, in.validity, off, len);
+    b->len += len;
+    return;
+  }
+  if (t.type == T_LIST || t.type == T_LARGE_LIST || t.type == T_MAP) {
+    const int ow = t.type == T_LARGE_LIST ? 8 : 4;
+    for (int64_t r = off; r < off + len; r++) {
+      const bool v = in.validity == nullptr || GetBit(in.validity, r);
+      PutBit(b->valid, b->len, v);
+      b->nulls += !v;
+      b->len++;
+      int64_t size = 0;
+      if (v) {
+        const int64_t o0 = OffAt(in.offsets, ow, r);
+        size = OffAt(in.offsets, ow, r + 1) - o0;
+        if (t.type == T_MAP) {  // MapBuilder: keys and items, the entries struct sized after them
+          const Field& e = t.kids[0];
+          NodeBuf& eb = b->kids[0];
+          AppendSlice(e.kids[0], &eb.kids[0], in.kids[0].kids[0], o0, size);
+          AppendSlice(e.kids[1], &eb.kids[1], in.kids[0].kids[1], o0, size);
+          AppendValidity(&eb, nullptr, 0, size);
+          eb.len += size;
+        } else {
+          AppendSlice(t.kids[0], &b->kids[0], in.kids[0], o0, size);
+        }
+      }
+      b->offs.push_back(b->offs.back() + size);
+    }
+    return;
+  }
+  if (IsBinary(t.type)) {
+    const int ow = OffW(t.type);
+    for (int64_t r = off; r < off + len; r++) {
+      const bool v = in.validity == nullptr || GetBit(in.validity, r);
+      PutBit(b->valid, b->len, v);
+      b->nulls += !v;
+      b->len++;
+      if (v) {
+        const int64_t o0 = OffAt(in.offsets, ow, r), o1 = OffAt(in.offsets, ow, r + 1);
+        b->data.insert(b->data.end(), in.values + o0, in.values + o1);
+      }
+      b->offs.push_back((int64_t)b->data.size());
+    }
+    return;
+  }
+  AppendValidity(b, in.validity, off, len);
+  if (t.type == T_BOOL) {
+    for (int64_t i = 0; i < len; i++) PutBit(b->data, b->nbits++, GetBit(in.values, off + i));
+  } else {
+    const int w = ByteWidth(t.type);
+    b->data.insert(b->data.end(), in.values + off * w, in.values + (off + len) * w);
+  }
+  b->len += len;
+}
+
+// Builder Finish: nodes and body buffers in pre-order; `keep` holds the assembled buffers.
+void FinishNode(const Field& t, NodeBuf* b, std::vector<std::pair<int64_t, int64_t>>* nodes,
+                std::vector<std::pair<const uint8_t*, int64_t>>* body, std::vector<std::vector<uint8_t>>* keep) {
+  const int64_t n = b->len;
+  b->valid.resize((size_t)BytesForBits(n), 0);
+  nodes->push_back({n, b->nulls});
+  body->push_back(b->nulls > 0 ? std::make_pair((const uint8_t*)b->valid.data(), BytesForBits(n))
+                               : std::make_pair((const uint8_t*)nullptr, (int64_t)0));
+  const bool offs = t.type == T_LIST || t.type == T_LARGE_LIST || t.type == T_MAP || IsBinary(t.type);
+  if (offs) {
+    const int ow = t.type == T_LARGE_LIST || t.type == T_LARGE_STRING || t.type == T_LARGE_BINARY ? 8 : 4;
+    keep->emplace_back((size_t)(n + 1) * ow);
+    uint8_t* o = keep->back().data();
+    for (int64_t i = 0; i <= n; i++) {
+      if (ow == 8) {
+        memcpy(o + i * 8, &b->offs[i], 8);
+      } else {
+        const int32_t v = (int32_t)b->offs[i];
+        memcpy(o + i * 4, &v, 4);
+      }
+    }
+    body->push_back({o, (int64_t)(n + 1) * ow});
+  }
+  if (IsBinary(t.type) || ByteWidth(t.type) > 0) {
+    body->push_back({b->data.data(), (int64_t)b->data.size()});
+  } else if (t.type == T_BOOL) {
+    b->data.resize((size_t)BytesForBits(n), 0);
+    body->push_back({b->data.data(), BytesForBits(n)});
+  }
+  for (size_t k = 0; k < t.kids.size(); k++) FinishNode(t.kids[k], &b->kids[k], nodes, body, keep);
+}
+
+// batch_nbytes (splitter.cc:438-453): the top-level array's own buffers only.
+int64_t OwnBytes(const Field& t, const NodeBuf& b) {
+  const int64_t n = b.len;
+  int64_t r = b.nulls > 0 ? BytesForBits(n) : 0;
+  if (t.type == T_LIST || t.type == T_MAP) r += (n + 1) * 4;
+  if (t.type == T_LARGE_LIST) r += (n + 1) * 8;
+  return r;
+}
+
+// Types a nested column may hold (anything but null below the top).
+bool NestedSupported(const Field& t) {
+  if (t.type == T_NULL) return false;
+  if (t.type == T_MAP && (t.kids.size() != 1 || t.kids[0].type != T_STRUCT || t.kids[0].kids.size() != 2))
+    return false;
+  if ((t.type == T_LIST || t.type == T_LARGE_LIST) && t.kids.size() != 1) return false;
+  if (t.type == T_STRUCT && t.kids.empty()) return false;
+  if (!IsNested(t.type) && !t.kids.empty()) return false;
+  if (!IsNested(t.type) && !IsBinary(t.type) && t.type != T_BOOL && ByteWidth(t.type) == 0) return false;
+  for (const Field& k : t.kids)
+    if (!NestedSupported(k)) return false;
+  return true;
+}
+
+// MakeArrayData (jni_common.h:186-300): one array from the flat buffer list at *idx.
+std::string ParseNode(const Field& t, const int64_t* addrs, const int64_t* sizes, int nbuf, int* idx,
+                      InNode* out) {
+  auto take = [&](bool* empty) -> const uint8_t* {
+    const int i = (*idx)++;
+    *empty = sizes[i] == 0 || addrs[i] == 0;
+    return (const uint8_t*)addrs[i];
+  };
+  bool empty;
+  if (*idx >= nbuf) return "insufficient number of buffers";
+  const uint8_t* v = take(&empty);
+  out->validity = empty ? nullptr : v;
+  if (t.type == T_LIST || t.type == T_LARGE_LIST || t.type == T_MAP || IsBinary(t.type)) {
+    if (*idx >= nbuf) return "insufficient number of buffers";
+    out->offsets = take(&empty);
+  }
+  if (t.type == T_STRUCT || t.type == T_LIST || t.type == T_LARGE_LIST || t.type == T_MAP) {
+    out->kids.resize(t.kids.size());
+    for (size_t k = 0; k < t.kids.size(); k++) {
+      std::string e = ParseNode(t.kids[k], addrs, sizes, nbuf, idx, &out->kids[k]);
+      if (!e.empty()) return e;
+    }
+    // the map's entries struct: its validity is dropped (jni_common.h:284-288)
+    if (t.type == T_MAP) out->kids[0].validity = nullptr;
+    return "";
+  }
+  if (*idx >= nbuf) return "insufficient number of buffers";
+  out->values = take(&empty);
+  return "";
 }
 
 // Splitter::Make short names (splitter.cc:190-208); "single" is round-robin over one partition.
@@ -292,8 +465,8 @@ class OracleSplitter {
       int t = fields_[i].type;
       if (IsBinary(t)) bin.push_back(i);
       else if (t == T_NULL) continue;
-      else if (t == T_LIST) {  // list_array_idx_ (splitter.cc:254-258), fixed-width or bool elements
-        if (ByteWidth(fields_[i].elem) <= 0 && fields_[i].elem != T_BOOL) return "list element type not supported";
+      else if (IsNested(t)) {  // list_array_idx_ (splitter.cc:254-258)
+        if (!NestedSupported(fields_[i])) return "nested type not supported";
         list_idx_.push_back(i);
       }
       else if (t == T_BOOL || ByteWidth(t) > 0) array_idx_.push_back(i);
@@ -312,7 +485,9 @@ class OracleSplitter {
     }
     int A = (int)array_idx_.size();
     bufs_.assign(A, std::vector<PartBufs>(P_));
-    lists_.assign(list_idx_.size(), std::vector<ListBuf>(P_));
+    lists_.assign(list_idx_.size(), std::vector<NodeBuf>(P_));
+    for (size_t li = 0; li < list_idx_.size(); li++)
+      for (int p = 0; p < P_; p++) InitNode(fields_[list_idx_[li]], &lists_[li][p]);
     input_has_null_.assign(A, false);
     empirical_.assign(A - fixed_cnt_, 0);
     cap_.assign(P_, 0);
@@ -350,21 +525,9 @@ class OracleSplitter {
         idx += 2;
         continue;
       }
-      if (idx >= nbuf) return "insufficient number of buffers";
       InCol c;
-      if (sizes[idx] > 0 && addrs[idx] != 0) c.validity = (const uint8_t*)addrs[idx];
-      idx++;
-      if (IsBinary(fields_[f].type) || fields_[f].type == T_LIST) {
-        if (idx >= nbuf) return "insufficient number of buffers";
-        c.offsets = (const uint8_t*)addrs[idx++];
-      }
-      if (fields_[f].type == T_LIST) {  // [validity, offsets, element validity, element values]
-        if (idx >= nbuf) return "insufficient number of buffers";
-        if (sizes[idx] > 0 && addrs[idx] != 0) c.child_validity = (const uint8_t*)addrs[idx];
-        idx++;
-      }
-      if (idx >= nbuf) return "insufficient number of buffers";
-      c.values = (const uint8_t*)addrs[idx++];
+      std::string pe = ParseNode(fields_[f], addrs, sizes, nbuf, &idx, &c);
+      if (!pe.empty()) return pe;
       if (c.validity) {
         int64_t valid = 0;
         for (int64_t i = 0; i < n; i++) valid += GetBit(c.validity, i);
@@ -592,20 +755,12 @@ class OracleSplitter {
         nodes.push_back({n, n});
         continue;
       }
-      if (t == T_LIST) {  // builder->Finish (splitter.cc:534-545): list node, then its element node
-        ListBuf& b = lists_[list_i++][p];
-        const int w = ByteWidth(fields_[f].elem);
-        b.valid.resize((size_t)BytesForBits(n), 0);
-        b.cvalid.resize((size_t)BytesForBits(b.elems), 0);
-        if (w == 0) b.cvals.resize((size_t)BytesForBits(b.elems), 0);
-        nodes.push_back({n, b.nulls});
-        body.push_back(b.nulls > 0 ? BodyBuf{b.valid.data(), BytesForBits(n)} : BodyBuf{nullptr, 0});
-        body.push_back({(const uint8_t*)b.offs.data(), (int64_t)(n + 1) * 4});
-        nodes.push_back({b.elems, b.cnulls});
-        body.push_back(b.cnulls > 0 ? BodyBuf{b.cvalid.data(), BytesForBits(b.elems)} : BodyBuf{nullptr, 0});
-        body.push_back({b.cvals.data(), w == 0 ? BytesForBits(b.elems) : b.elems * w});
-        // batch_nbytes counts the list's own buffers (splitter.cc:438-453)
-        raw += (b.nulls > 0 ? BytesForBits(n) : 0) + (int64_t)(n + 1) * 4;
+      if (IsNested(t)) {  // builder->Finish (splitter.cc:532-545)
+        NodeBuf& b = lists_[list_i++][p];
+        std::vector<std::pair<const uint8_t*, int64_t>> bb;
+        FinishNode(fields_[f], &b, &nodes, &bb, &keep);
+        for (auto& x : bb) body.push_back(BodyBuf{x.first, x.second});
+        raw += OwnBytes(fields_[f], b);  // batch_nbytes: the column's own buffers
         continue;
       }
       int a = IsBinary(t) ? fixed_cnt_ + bin_i++ : fixed_i++;
@@ -645,7 +800,7 @@ class OracleSplitter {
     cached_size_[p] += body_len;
     cached_[p].push_back(std::move(msg));
     base_[p] = 0;
-    for (auto& l : lists_) l[p] = ListBuf();
+    for (size_t li = 0; li < list_idx_.size(); li++) InitNode(fields_[list_idx_[li]], &lists_[li][p]);
     int A = (int)array_idx_.size();
     for (int a = 0; a < A; a++) {
       PartBufs& b = bufs_[a][p];
@@ -770,28 +925,8 @@ class OracleSplitter {
     // SplitListArray (splitter.cc:1322-1333): every row to its partition's builder
     for (size_t li = 0; li < list_idx_.size(); li++) {
       const InCol& c = cols[list_idx_[li]];
-      const int w = ByteWidth(fields_[list_idx_[li]].elem);  // 0: bool elements, one bit each
-      const int32_t* off = (const int32_t*)c.offsets;
-      for (int32_t r = 0; r < n; r++) {
-        ListBuf& b = lists_[li][pid_[r]];
-        const bool valid = c.null_count == 0 || GetBit(c.validity, r);
-        PutBit(b.valid, b.rows, valid);
-        b.rows++;
-        if (!valid) {
-          b.nulls++;
-          b.offs.push_back(b.offs.back());
-          continue;
-        }
-        for (int32_t e = off[r]; e < off[r + 1]; e++) {
-          const bool cv = c.child_validity == nullptr || GetBit(c.child_validity, e);
-          PutBit(b.cvalid, b.elems, cv);
-          b.cnulls += !cv;
-          if (w == 0) PutBit(b.cvals, b.elems, GetBit(c.values, e));
-          else b.cvals.insert(b.cvals.end(), c.values + (size_t)e * w, c.values + (size_t)(e + 1) * w);
-          b.elems++;
-        }
-        b.offs.push_back(b.offs.back() + (off[r + 1] - off[r]));
-      }
+      const Field& t = fields_[list_idx_[li]];
+      for (int32_t r = 0; r < n; r++) AppendSlice(t, &lists_[li][pid_[r]], c, r, 1);
     }
     for (int p = 0; p < P_; p++) base_[p] += cnt_[p];
     return "";
@@ -804,7 +939,7 @@ class OracleSplitter {
   std::vector<uint8_t> schema_msg_;
   std::vector<int> array_idx_;
   std::vector<int> list_idx_;
-  std::vector<std::vector<ListBuf>> lists_;  // [list column][partition]
+  std::vector<std::vector<NodeBuf>> lists_;  // [nested column][partition]
   int fixed_cnt_ = 0;
   std::vector<std::vector<PartBufs>> bufs_;
   std::vector<bool> input_has_null_;
@@ -844,9 +979,16 @@ extern "C" {
 void* gzo_make(const char* mode, const int32_t* types, int32_t nf, int32_t num_partitions,
                const int32_t* keys, int32_t n_keys, int64_t offheap_per_task, int32_t buffer_size,
                int32_t prefer_spill, char* err, int errlen) {
+  // types: the fields in pre-order, each code with its child count above the low byte
   std::vector<Field> fields;
-  // a list field's code carries its element type above the low byte
-  for (int i = 0; i < nf; i++) fields.push_back({types[i] & 0xff, "f" + std::to_string(i), types[i] >> 8});
+  int at = 0;
+  std::function<Field(std::string)> node = [&](std::string name) {
+    Field f{types[at] & 0xff, std::move(name), {}};
+    const int nk = (types[at++] >> 8) & 0xff;
+    for (int k = 0; k < nk; k++) f.kids.push_back(node("c" + std::to_string(k)));
+    return f;
+  };
+  for (int i = 0; i < nf; i++) fields.push_back(node("f" + std::to_string(i)));
   Options o;
   const std::string m = mode ? mode : "hash";
   if (m == "hash") o.mode = M_HASH;

@@ -2,9 +2,10 @@
 
 Run in a checkout where the reference sources and pyarrow are present:
 
-    python tests/golden/make_golden.py [/path/to/gazelle_plugin] [--only=large|--only=list]
+    python tests/golden/make_golden.py [/path/to/gazelle_plugin] [--only=large|list|nested]
 
-(--only=large / --only=list rewrite large_binary.json / list_columns.json alone.)
+(--only=large / list / nested rewrite large_binary.json / list_columns.json /
+nested_columns.json alone.)
 
 It compiles the reference Splitter (oracle/ref/Makefile -> oracle/_ref/) and runs it on
 seeded inputs from gazelle_plugin_gb300.workloads, recording for every case the SHA-256 of
@@ -62,6 +63,19 @@ def input_digest(batches) -> str:
     return h.hexdigest()
 
 
+def field_json(f):
+    """[name, type, nullable] (+ [elem] for a simple list, + [None, [children]] when nested)."""
+    if f.is_nested:
+        return [f.name, f.type, f.nullable, None, [field_json(k) for k in f.children]]
+    return [f.name, f.type, f.nullable] + ([f.elem] if f.is_list else [])
+
+
+def field_from_json(x):
+    if len(x) > 4:
+        return W.Field(x[0], x[1], x[2], None, tuple(field_from_json(k) for k in x[4]))
+    return W.Field(*x)
+
+
 def record(name, schema, batches, P, keys, opts, gen, short_name="hash"):
     out = O.run_ref(schema, batches, P, keys, short_name=short_name, **opts)
     P = len(out.partition_lengths)
@@ -70,7 +84,7 @@ def record(name, schema, batches, P, keys, opts, gen, short_name="hash"):
         **rec,
         "name": name,
         "gen": gen,
-        "schema": [[f.name, f.type, f.nullable] + ([f.elem] if f.is_list else []) for f in schema],
+        "schema": [field_json(f) for f in schema],
         "num_partitions": P,
         "keys": [int(k) for k in keys],
         "options": opts,
@@ -224,6 +238,75 @@ def list_cases():
                {"workload": "list", "seed": 5200 + seed, "force_elem": "bool"})
 
 
+def _F(name, t, nullable=True, elem=None, *kids):
+    return W.Field(name, t, nullable, elem, tuple(kids))
+
+
+# nested column shapes: the reference unit tests' (shuffle_split_test.cc:509-1060) and more
+NESTED_SHAPES = [
+    lambda n: _F(n, "list", True, None, _F("item", "utf8")),
+    lambda n: _F(n, "list", True, None, _F("item", "list", True, "int32")),
+    lambda n: _F(n, "large_list", True, None, _F("item", "list", True, None, _F("item", "utf8"))),
+    lambda n: _F(n, "large_list", True, None, _F("item", "list", True, "int32")),
+    lambda n: _F(n, "list", True, None, _F("item", "struct", True, None, _F("a", "int32"), _F("b", "utf8"))),
+    lambda n: _F(n, "list", True, None, _F("item", "map", True, None, _F("key", "utf8", False), _F("value", "utf8"))),
+    lambda n: _F(n, "struct", True, None, _F("a", "list", True, "int32"), _F("b", "utf8")),
+    lambda n: _F(n, "map", True, None, _F("key", "utf8", False), _F("value", "utf8")),
+    lambda n: _F(n, "struct", True, None, _F("a", "int32"), _F("b", "bool"), _F("c", "decimal128"),
+                 _F("d", "large_utf8")),
+    lambda n: _F(n, "list", True, None, _F("item", "large_binary")),
+    lambda n: _F(n, "map", True, None, _F("key", "int32", False), _F("value", "list", True, "float64")),
+    lambda n: _F(n, "struct", True, None, _F("s", "struct", True, None, _F("a", "int16"), _F("b", "utf8")),
+                 _F("t", "bool")),
+    lambda n: _F(n, "list", True, None, _F("item", "list", True, None, _F("item", "list", True, "bool"))),
+]
+
+
+def nested_case(seed):
+    """Schema, batches, P, keys and options of a `nested_<n>` case: an int key, 0-1 fixed-width
+    and 0-1 simple list columns and 1-3 nested columns (list / large_list / map / struct of any
+    depth) in random order; entries null at 0-40% at every level, with null top-level entries
+    keeping non-empty ranges in half the cases."""
+    rng = np.random.default_rng(seed)
+    fields = [W.Field("k", str(rng.choice(["int32", "int64"])), False)]
+    fields += [W.Field("f", str(rng.choice(["int32", "float64", "bool"])))] * int(rng.integers(0, 2))
+    fields += [W.Field("L", "list", True, "int64")] * int(rng.integers(0, 2))
+    fields += [NESTED_SHAPES[int(rng.integers(0, len(NESTED_SHAPES)))](f"N{i}")
+               for i in range(int(rng.integers(1, 4)))]
+    schema = [fields[i] for i in rng.permutation(len(fields))]
+    keys = [i for i, f in enumerate(schema) if f.name == "k"]
+    P = int(rng.choice([1, 3, 16, 200]))
+    bsz = int(rng.choice([8, 100, 4096]))
+    ps = bool(rng.random() < 0.6)
+    opts = {"buffer_size": bsz, "prefer_spill": ps,
+            "offheap_per_task": 0 if ps else int(rng.choice([0, 1 << 16]))}
+    spans = bool(rng.random() < 0.5)
+    batches = []
+    for _ in range(int(rng.integers(1, 6))):
+        n = int(rng.integers(1, bsz + 1))
+        bufs = []
+        for f in schema:
+            if f.is_nested:
+                bufs += W.nested_column(rng, f, n, float(rng.choice([0.0, 0.1, 0.4])),
+                                        int(rng.choice([0, 2, 5])), True, spans)
+            elif f.is_list:
+                bufs += W.list_column(rng, f, n, 0.1, 0.1, 4)
+            else:
+                bufs += W.random_batch(rng, [f], n, 0.1).buffers
+        batches.append(W.Batch(n, bufs))
+    return schema, batches, P, keys, opts
+
+
+def nested_cases():
+    for seed in range(24):
+        schema, batches, P, keys, opts = nested_case(6000 + seed)
+        yield (f"nested_{seed}", schema, batches, P, keys, opts, {"workload": "nested", "seed": 6000 + seed})
+    for seed in range(2):
+        schema, batches, P, keys, opts = nested_case(6100 + seed)
+        yield (f"nested_write_schema_{seed}", schema, batches, P, keys, dict(opts, write_schema=True),
+               {"workload": "nested", "seed": 6100 + seed})
+
+
 def large_cases():
     for seed in range(16):
         schema, batches, P, keys, opts = large_case(4000 + seed)
@@ -240,6 +323,8 @@ def regenerate(case):
         return large_case(g["seed"])[1]
     if g["workload"] == "list":
         return list_case(g["seed"], g.get("force_elem"))[1]
+    if g["workload"] == "nested":
+        return nested_case(g["seed"])[1]
     if g["workload"] == "c1":
         return W.c1_batches(g["seed"], g["num_batches"], g["rows"])
     if g["workload"] == "c2":
@@ -406,8 +491,12 @@ def main():
     if "--only=list" in sys.argv:
         write_cases(list_cases(), "list_columns.json")
         return
+    if "--only=nested" in sys.argv:
+        write_cases(nested_cases(), "nested_columns.json")
+        return
     write_large()
     write_cases(list_cases(), "list_columns.json")
+    write_cases(nested_cases(), "nested_columns.json")
     recs = []
     for name, schema, batches, P, keys, opts, gen in cases():
         recs.append(record(name, schema, batches, P, keys, opts, gen))

@@ -129,7 +129,7 @@ def test_schema_ipc_parser():
     from oracle.oracle import to_pyarrow_schema
     from gazelle_plugin_gb300 import workloads as W
     schema = [W.Field(f"c{i}", t, i % 2 == 0, "int64" if t == "list" else None)
-              for i, t in enumerate(W.TYPE_CODES)]
+              for i, t in enumerate(W.TYPE_CODES) if t not in ("large_list", "struct", "map")]
     st, types, nulls = parse_schema(to_pyarrow_schema(schema).serialize().to_pybytes())
     assert st == 0
     expect = [f.code for f in schema]
