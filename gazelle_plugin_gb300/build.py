@@ -18,7 +18,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgzsplit.so")
 TASK_LIB = os.path.join(HERE, "libgztask.so")  # simulated map tasks calling the C ABI
 
-SOURCES = ["kernels.cu", "splitter.cc", "ipc.cc", "schema_ipc.cc", "capi.cc", "host_util.cc",
+SOURCES = ["kernels.cu", "splitter.cc", "splitter_nested.cc", "ipc.cc", "schema_ipc.cc", "capi.cc", "host_util.cc",
            "hash_static.cu", "serve.cc", "tune.cc", "reader.cc", "read_kernels.cu", "lz4_kernels.cu"]
 NOT_IN_LIB = {"task_driver.cc"}  # built into libgztask.so
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]

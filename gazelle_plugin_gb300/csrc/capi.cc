@@ -125,19 +125,48 @@ GzStatus MakeReader(std::vector<gz::Field> fields, int32_t device, int64_t* out_
   return GZ_OK;
 }
 
+// A GzField tree as the splitter's Field: a map's key and value go under an "entries" struct
+// (Arrow's map layout), and a list whose one child is a fixed-width or bool leaf takes the simple
+// form (elem) that the schema parser also gives it.
+gz::Field FieldFrom(const GzField& g, int depth) {
+  gz::Field f;
+  f.type = g.type;
+  f.nullable = g.nullable != 0;
+  f.precision = g.precision;
+  f.scale = g.scale;
+  f.unit = g.unit;
+  f.elem = g.elem_type;
+  f.name = g.name ? g.name : "";
+  if (g.n_children <= 0 || g.children == nullptr || depth > 16) return f;
+  std::vector<gz::Field> kids;
+  for (int k = 0; k < g.n_children; k++) kids.push_back(FieldFrom(g.children[k], depth + 1));
+  if (f.type == GZ_TYPE_MAP) {
+    gz::Field e;
+    e.type = GZ_TYPE_STRUCT;
+    e.name = "entries";
+    e.nullable = false;
+    e.children = std::move(kids);
+    f.children.push_back(std::move(e));
+    return f;
+  }
+  if (f.type == GZ_TYPE_LIST && kids.size() == 1 && !kids[0].nested() &&
+      (kids[0].type == GZ_TYPE_BOOL || (kids[0].type != GZ_TYPE_NULL && kids[0].type < GZ_TYPE_STRING))) {
+    const gz::Field& e = kids[0];
+    f.elem = e.type;
+    f.elem_name = e.name;
+    f.elem_nullable = e.nullable;
+    f.precision = e.precision;
+    f.scale = e.scale;
+    f.unit = e.unit;
+    return f;
+  }
+  f.children = std::move(kids);
+  return f;
+}
+
 std::vector<gz::Field> FieldsFrom(const GzField* fields, int32_t n_fields) {
   std::vector<gz::Field> fs;
-  for (int i = 0; i < n_fields; i++) {
-    gz::Field f;
-    f.type = fields[i].type;
-    f.nullable = fields[i].nullable != 0;
-    f.precision = fields[i].precision;
-    f.scale = fields[i].scale;
-    f.unit = fields[i].unit;
-    f.elem = fields[i].elem_type;
-    f.name = fields[i].name ? fields[i].name : "";
-    fs.push_back(f);
-  }
+  for (int i = 0; i < n_fields; i++) fs.push_back(FieldFrom(fields[i], 0));
   return fs;
 }
 

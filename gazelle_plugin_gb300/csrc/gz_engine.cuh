@@ -63,6 +63,8 @@ struct SchemaDesc {
   uint64_t list_mask;           // array columns that are lists
   uint64_t listbit_mask;        // lists of bool elements: one bit each; their "characters" are the
                                 // element indices and out_chars is a bit region (0xff-filled)
+  uint64_t nopay_mask;          // list-like columns whose elements carry no values (struct entries:
+                                // their element validity only; also in listbit_mask)
 };
 
 // Device addresses of one input column of one batch.  offsets only for binary columns (int32,
@@ -89,6 +91,25 @@ constexpr int32_t kErrEmitOverflow = 1;
 constexpr int32_t kErrBadOffsets = 2;
 constexpr int32_t kErrTimeout = 4;  // a bounded wait in a kernel gave up
 constexpr int32_t kErrBadPid = 8;   // a range partition id is negative or >= P
+constexpr int32_t kErrNestSpan = 16;  // a null entry inside a nested column holds elements
+
+// One array k_nest_prep computes for a batch of a nested column.
+//   compose: out[r] = off[depth-1][ ... off[1][off[0][r]] ... ] for r < n (int32 out; every index
+//            checked against the entries of the array it reads, lim[d]);
+//   lengths: out[i] = valid(i) ? off[0][i + 1] - off[0][i] : 0 for i < n; with `inner` a null
+//            entry holding elements is an error (kErrNestSpan).
+constexpr int kMaxNestChain = 6;
+struct NestJob {
+  uint32_t kind;   // 0 compose, 1 lengths
+  uint32_t n;
+  uint32_t depth;
+  uint32_t inner;
+  const void* off[kMaxNestChain];
+  uint64_t lim[kMaxNestChain];   // readable entries of off[d]; lengths: lim[1] validity bits
+  uint32_t wide[kMaxNestChain];  // 1: int64 offsets
+  const uint8_t* validity;       // lengths: the entries' validity (nullptr: all valid)
+  int32_t* out;
+};
 
 struct BatchDesc {
   uint32_t nrows;

@@ -100,7 +100,7 @@ __device__ uint32_t block_exmax(uint32_t v, uint32_t* scratch) {
 
 // =======================================================================================
 // k_hash_count: one CTA per segment (<= seg_tiles * kTileRows rows of one batch).
-constexpr int kMaxStrPlan = 32;
+constexpr int kMaxStrPlan = kMaxCols;  // binary, list and nested-stream columns
 
 constexpr int kHashThreads = 256;
 constexpr int kHashRows = kTileRows / kHashThreads;  // rows of a tile per thread
@@ -1521,11 +1521,13 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
         const int k = (int)(ct.z >> 24);
         if (kLists && ((sd.listbit_mask >> a) & 1ull)) {
           // bool elements: each row's element bits [so, so + len) to the bit region at cd (its
-          // words start 0xff: the false ones are cleared)
+          // words start 0xff: the false ones are cleared); struct entries carry no values
+          if (!((sd.nopay_mask >> a) & 1ull)) {
 #pragma unroll
-          for (int u = 0; u < kRowsPerThread; u++)
-            if (threadIdx.x + u * kConsumers < n && len[u])
-              clear_null_elements(reinterpret_cast<uint32_t*>(ochars), cd[u], c.values, so[u], len[u]);
+            for (int u = 0; u < kRowsPerThread; u++)
+              if (threadIdx.x + u * kConsumers < n && len[u])
+                clear_null_elements(reinterpret_cast<uint32_t*>(ochars), cd[u], c.values, so[u], len[u]);
+          }
         } else if (chars) {
           // shared address of byte 0 of the column (offsets index from there)
           const uint32_t cbase = smem_addr(staged_ptr(cstage, c.values + s_cr[k].x)) - (uint32_t)s_cr[k].x;
@@ -1612,6 +1614,64 @@ __global__ void __launch_bounds__(256) k_gather(const HostCopy* __restrict__ job
 }
 
 // =======================================================================================
+// k_nest_prep: the per-batch arrays of nested columns - row ranges composed through the offsets
+// of every list / map on a node's path, and the lengths of binary / list / map entries - one
+// job per block, striding.  Every read is checked against the entries of the array it reads;
+// a failed check writes 0 and raises kErrBadOffsets (the pass then copies nothing).
+__global__ void __launch_bounds__(256) k_nest_prep(const NestJob* __restrict__ jobs, uint32_t n_jobs,
+                                                   int32_t* err) {
+  for (uint32_t j = blockIdx.x; j < n_jobs; j += gridDim.x) {
+    const NestJob& job = jobs[j];
+    bool bad = false, span = false;
+    if (job.kind == 0) {
+      for (uint32_t r = threadIdx.x; r < job.n; r += blockDim.x) {
+        int64_t x = r;
+        for (uint32_t d = 0; d < job.depth; d++) {
+          if (x < 0 || (uint64_t)x >= job.lim[d]) {
+            bad = true;
+            x = 0;
+            break;
+          }
+          x = job.wide[d] ? static_cast<const int64_t*>(job.off[d])[x] : (int64_t) static_cast<const int32_t*>(job.off[d])[x];
+        }
+        if (x < 0 || x > INT32_MAX) {
+          bad = true;
+          x = 0;
+        }
+        job.out[r] = (int32_t)x;
+      }
+    } else {
+      for (uint32_t i = threadIdx.x; i < job.n; i += blockDim.x) {
+        int64_t len = 0;
+        if ((uint64_t)i + 1 < job.lim[0]) {
+          len = job.wide[0] ? static_cast<const int64_t*>(job.off[0])[i + 1] - static_cast<const int64_t*>(job.off[0])[i]
+                            : (int64_t) static_cast<const int32_t*>(job.off[0])[i + 1] -
+                                  static_cast<const int32_t*>(job.off[0])[i];
+        } else {
+          bad = true;
+        }
+        if (len < 0 || len > INT32_MAX) {
+          bad = true;
+          len = 0;
+        }
+        if (job.validity != nullptr) {
+          if (i >= job.lim[1]) {  // beyond the validity buffer
+            bad = true;
+            len = 0;
+          } else if (!((job.validity[i >> 3] >> (i & 7)) & 1)) {
+            if (len != 0 && job.inner) span = true;
+            len = 0;
+          }
+        }
+        job.out[i] = (int32_t)len;
+      }
+    }
+    if (bad) atomicOr(err, kErrBadOffsets);
+    if (span) atomicOr(err, kErrNestSpan);
+  }
+}
+
+// =======================================================================================
 // launch helpers
 cudaError_t launch_hash_count(const SchemaDesc& sd, const FlushDesc& fd, cudaStream_t st) {
   const size_t sm = fd.hist_in_smem ? sizeof(uint32_t) * sd.P * (1 + sd.n_str) : 0;
@@ -1641,6 +1701,12 @@ cudaError_t launch_plan(const SchemaDesc& sd, const FlushDesc& fd, cudaStream_t 
     if (e != cudaSuccess) return e;
   }
   k_plan_scan<<<1, kPlanThreads, 0, st>>>(sd, fd);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_nest_prep(const NestJob* jobs, uint32_t n_jobs, int32_t* err, cudaStream_t st) {
+  if (n_jobs == 0) return cudaSuccess;
+  k_nest_prep<<<n_jobs < 1216u ? n_jobs : 1216u, 256, 0, st>>>(jobs, n_jobs, err);
   return cudaGetLastError();
 }
 

@@ -64,6 +64,8 @@ Status PartitionReader::Cuda(cudaError_t e, const char* what) {
 Status PartitionReader::Make(std::vector<Field> fields, int device, std::unique_ptr<PartitionReader>* out) {
   std::unique_ptr<PartitionReader> r(new PartitionReader());
   for (const Field& f : fields) {
+    if (f.nested() || f.type == GZ_TYPE_LARGE_LIST || f.type == GZ_TYPE_STRUCT || f.type == GZ_TYPE_MAP)
+      return Status::Error(GZ_NOT_IMPLEMENTED, "nested fields are not implemented by the reader");
     if (f.type == GZ_TYPE_LIST ? FixedWidth(f.elem) == 0 && f.elem != GZ_TYPE_BOOL
                                : f.type != GZ_TYPE_NULL && f.type != GZ_TYPE_BOOL && !IsBinaryType(f.type) &&
                                      FixedWidth(f.type) == 0)

@@ -11,7 +11,137 @@
 #include "flatbuf.h"
 
 namespace gz {
+namespace {
 
+// One Field table (and its children, for nested types).  A list whose element is a fixed-width
+// or bool leaf keeps the simple form (elem, no children).
+bool DecodeField(FlatReader& r, int64_t ft, int depth, Field* out, std::string* err) {
+  if (depth > 16) {
+    *err = "nesting too deep";
+    return false;
+  }
+  Field f;
+  if (!r.String(ft, 0, &f.name)) {
+    *err = "bad field name";
+    return false;
+  }
+  f.nullable = r.Scalar<uint8_t>(ft, 1, 0) != 0;
+  uint8_t tt = r.Scalar<uint8_t>(ft, 2, 0);
+  int64_t tp = r.Table(ft, 3);
+  if (tt == 12 || tt == 13 || tt == 17 || tt == 21) {  // List, Struct_, Map, LargeList
+    int64_t ch = r.Table(ft, 5);
+    uint32_t nch = 0;
+    if (ch >= 0 && !r.Get(ch, &nch)) {
+      *err = "bad children vector";
+      return false;
+    }
+    for (uint32_t k = 0; k < nch; k++) {
+      const int64_t ct = r.Deref(ch + 4 + 4 * (int64_t)k);
+      Field c;
+      if (ct < 0 || !DecodeField(r, ct, depth + 1, &c, err)) {
+        if (err->empty()) *err = "bad child field";
+        return false;
+      }
+      f.children.push_back(std::move(c));
+    }
+    if ((tt == 12 || tt == 21) && nch != 1) {
+      *err = "list field without one element field";
+      return false;
+    }
+    if (tt == 13 && nch == 0) {
+      *err = "struct field without fields";
+      return false;
+    }
+    if (tt == 17) {
+      if (nch != 1 || f.children[0].type != GZ_TYPE_STRUCT || f.children[0].children.size() != 2) {
+        *err = "map field without an entries struct of key and value";
+        return false;
+      }
+      f.keys_sorted = tp >= 0 && r.Scalar<uint8_t>(tp, 0, 0) != 0;
+    }
+    for (const Field& c : f.children)
+      if (c.type == GZ_TYPE_NULL) {
+        *err = "null-type fields inside nested types are not implemented by the GPU splitter";
+        return false;
+      }
+    f.type = tt == 12 ? GZ_TYPE_LIST : tt == 13 ? GZ_TYPE_STRUCT : tt == 17 ? GZ_TYPE_MAP : GZ_TYPE_LARGE_LIST;
+    if (tt == 12) {
+      const Field& e = f.children[0];
+      if (!e.nested() && (e.type == GZ_TYPE_BOOL || (e.type != GZ_TYPE_NULL && e.type < GZ_TYPE_STRING))) {
+        // the simple form
+        f.elem = e.type;
+        f.elem_name = e.name;
+        f.elem_nullable = e.nullable;
+        f.precision = e.precision;
+        f.scale = e.scale;
+        f.unit = e.unit;
+        f.timezone = e.timezone;
+        f.children.clear();
+      }
+    }
+    *out = std::move(f);
+    return true;
+  }
+  switch (tt) {
+    case 1: f.type = GZ_TYPE_NULL; break;
+    case 2: {
+      int32_t bw = tp >= 0 ? r.Scalar<int32_t>(tp, 0, 0) : 0;
+      bool sg = tp >= 0 && r.Scalar<uint8_t>(tp, 1, 0) != 0;
+      switch (bw) {
+        case 8: f.type = sg ? GZ_TYPE_INT8 : GZ_TYPE_UINT8; break;
+        case 16: f.type = sg ? GZ_TYPE_INT16 : GZ_TYPE_UINT16; break;
+        case 32: f.type = sg ? GZ_TYPE_INT32 : GZ_TYPE_UINT32; break;
+        case 64: f.type = sg ? GZ_TYPE_INT64 : GZ_TYPE_UINT64; break;
+        default: *err = "bad integer width"; return false;
+      }
+      break;
+    }
+    case 3: {
+      int16_t prec = tp >= 0 ? r.Scalar<int16_t>(tp, 0, 0) : 0;
+      f.type = prec == 0 ? GZ_TYPE_HALF_FLOAT : prec == 1 ? GZ_TYPE_FLOAT32 : GZ_TYPE_FLOAT64;
+      break;
+    }
+    case 4: f.type = GZ_TYPE_BINARY; break;
+    case 5: f.type = GZ_TYPE_STRING; break;
+    case 19: f.type = GZ_TYPE_LARGE_BINARY; break;
+    case 20: f.type = GZ_TYPE_LARGE_STRING; break;
+    case 6: f.type = GZ_TYPE_BOOL; break;
+    case 7: {
+      int32_t bw = tp >= 0 ? r.Scalar<int32_t>(tp, 2, 128) : 128;
+      if (bw != 128) {
+        *err = "only decimal128 is supported";
+        return false;
+      }
+      f.type = GZ_TYPE_DECIMAL128;
+      f.precision = tp >= 0 ? r.Scalar<int32_t>(tp, 0, 0) : 0;
+      f.scale = tp >= 0 ? r.Scalar<int32_t>(tp, 1, 0) : 0;
+      break;
+    }
+    case 8: {
+      int16_t unit = tp >= 0 ? r.Scalar<int16_t>(tp, 0, 1) : 1;
+      f.type = unit == 0 ? GZ_TYPE_DATE32 : GZ_TYPE_DATE64;
+      break;
+    }
+    case 9: {
+      f.unit = tp >= 0 ? r.Scalar<int16_t>(tp, 0, 1) : 1;
+      int32_t bw = tp >= 0 ? r.Scalar<int32_t>(tp, 1, 32) : 32;
+      f.type = bw == 64 ? GZ_TYPE_TIME64 : GZ_TYPE_TIME32;
+      break;
+    }
+    case 10:
+      f.type = GZ_TYPE_TIMESTAMP;
+      f.unit = tp >= 0 ? r.Scalar<int16_t>(tp, 0, 0) : 0;
+      if (tp >= 0) r.String(tp, 1, &f.timezone);
+      break;
+    default:
+      *err = "field type " + std::to_string(tt) + " is not implemented by the GPU splitter";
+      return false;
+  }
+  *out = std::move(f);
+  return true;
+}
+
+}  // namespace
 
 bool ParseSchemaIpc(const uint8_t* data, int64_t len, std::vector<Field>* out, std::string* err) {
   if (data == nullptr || len < 8) {
@@ -54,93 +184,7 @@ bool ParseSchemaIpc(const uint8_t* data, int64_t len, std::vector<Field>* out, s
       return false;
     }
     Field f;
-    if (!r.String(ft, 0, &f.name)) {
-      *err = "bad field name";
-      return false;
-    }
-    f.nullable = r.Scalar<uint8_t>(ft, 1, 0) != 0;
-    uint8_t tt = r.Scalar<uint8_t>(ft, 2, 0);
-    int64_t tp = r.Table(ft, 3);
-    const bool list = tt == 12;
-    if (list) {  // List: its one child field is the element (its type is decoded below)
-      int64_t ch = r.Table(ft, 5);
-      uint32_t nch = 0;
-      if (ch < 0 || !r.Get(ch, &nch) || nch != 1) {
-        *err = "list field without one element field";
-        return false;
-      }
-      const int64_t et = r.Deref(ch + 4);
-      if (et < 0 || !r.String(et, 0, &f.elem_name)) {
-        *err = "bad list element field";
-        return false;
-      }
-      f.elem_nullable = r.Scalar<uint8_t>(et, 1, 0) != 0;
-      tt = r.Scalar<uint8_t>(et, 2, 0);
-      tp = r.Table(et, 3);
-    }
-    switch (tt) {
-      case 1: f.type = GZ_TYPE_NULL; break;
-      case 2: {
-        int32_t bw = tp >= 0 ? r.Scalar<int32_t>(tp, 0, 0) : 0;
-        bool sg = tp >= 0 && r.Scalar<uint8_t>(tp, 1, 0) != 0;
-        switch (bw) {
-          case 8: f.type = sg ? GZ_TYPE_INT8 : GZ_TYPE_UINT8; break;
-          case 16: f.type = sg ? GZ_TYPE_INT16 : GZ_TYPE_UINT16; break;
-          case 32: f.type = sg ? GZ_TYPE_INT32 : GZ_TYPE_UINT32; break;
-          case 64: f.type = sg ? GZ_TYPE_INT64 : GZ_TYPE_UINT64; break;
-          default: *err = "bad integer width"; return false;
-        }
-        break;
-      }
-      case 3: {
-        int16_t prec = tp >= 0 ? r.Scalar<int16_t>(tp, 0, 0) : 0;
-        f.type = prec == 0 ? GZ_TYPE_HALF_FLOAT : prec == 1 ? GZ_TYPE_FLOAT32 : GZ_TYPE_FLOAT64;
-        break;
-      }
-      case 4: f.type = GZ_TYPE_BINARY; break;
-      case 5: f.type = GZ_TYPE_STRING; break;
-      case 19: f.type = GZ_TYPE_LARGE_BINARY; break;
-      case 20: f.type = GZ_TYPE_LARGE_STRING; break;
-      case 6: f.type = GZ_TYPE_BOOL; break;
-      case 7: {
-        int32_t bw = tp >= 0 ? r.Scalar<int32_t>(tp, 2, 128) : 128;
-        if (bw != 128) {
-          *err = "only decimal128 is supported";
-          return false;
-        }
-        f.type = GZ_TYPE_DECIMAL128;
-        f.precision = tp >= 0 ? r.Scalar<int32_t>(tp, 0, 0) : 0;
-        f.scale = tp >= 0 ? r.Scalar<int32_t>(tp, 1, 0) : 0;
-        break;
-      }
-      case 8: {
-        int16_t unit = tp >= 0 ? r.Scalar<int16_t>(tp, 0, 1) : 1;
-        f.type = unit == 0 ? GZ_TYPE_DATE32 : GZ_TYPE_DATE64;
-        break;
-      }
-      case 9: {
-        f.unit = tp >= 0 ? r.Scalar<int16_t>(tp, 0, 1) : 1;
-        int32_t bw = tp >= 0 ? r.Scalar<int32_t>(tp, 1, 32) : 32;
-        f.type = bw == 64 ? GZ_TYPE_TIME64 : GZ_TYPE_TIME32;
-        break;
-      }
-      case 10:
-        f.type = GZ_TYPE_TIMESTAMP;
-        f.unit = tp >= 0 ? r.Scalar<int16_t>(tp, 0, 0) : 0;
-        if (tp >= 0) r.String(tp, 1, &f.timezone);
-        break;
-      default:
-        *err = "field type " + std::to_string(tt) + " is not implemented by the GPU splitter";
-        return false;
-    }
-    if (list) {
-      if (f.type == GZ_TYPE_NULL || f.type >= GZ_TYPE_STRING) {
-        *err = "list elements of a fixed-width or bool type only";
-        return false;
-      }
-      f.elem = f.type;
-      f.type = GZ_TYPE_LIST;
-    }
+    if (!DecodeField(r, ft, 0, &f, err)) return false;
     out->push_back(f);
   }
   return true;
@@ -283,6 +327,13 @@ uint8_t TypeTable(Builder& b, const Field& f, uint32_t* table) {
     case GZ_TYPE_LARGE_BINARY: *table = empty(); return 19;  // Schema.fbs Type.LargeBinary
     case GZ_TYPE_LARGE_STRING: *table = empty(); return 20;  // Type.LargeUtf8
     case GZ_TYPE_LIST: *table = empty(); return 12;           // Type.List (its element: a child field)
+    case GZ_TYPE_LARGE_LIST: *table = empty(); return 21;     // Type.LargeList
+    case GZ_TYPE_STRUCT: *table = empty(); return 13;         // Type.Struct_ (its fields: children)
+    case GZ_TYPE_MAP:                                         // Type.Map { keysSorted }
+      b.StartTable();
+      b.AddScalar<uint8_t>(4, f.keys_sorted ? 1 : 0, 0);
+      *table = b.EndTable();
+      return 17;
     case GZ_TYPE_DECIMAL128:  // Decimal { precision, scale, bitWidth = 128 }
       b.StartTable();
       b.AddScalar<int32_t>(8, 128, 128);
@@ -319,11 +370,13 @@ uint8_t TypeTable(Builder& b, const Field& f, uint32_t* table) {
 
 namespace {
 
-// One Field table: a list's element field first (its own Field table), then the type, the name,
-// the children vector and the Field table itself.
+// One Field table: the children first (a list's element field, a map's entries, a struct's
+// fields: each its own Field table), then the type, the name, the children vector and the Field
+// table itself.
 uint32_t FieldTable(Builder& b, const Field& f) {
   std::vector<uint32_t> kids;
-  if (f.type == GZ_TYPE_LIST) {
+  for (const Field& c : f.children) kids.push_back(FieldTable(b, c));
+  if (f.type == GZ_TYPE_LIST && !f.nested()) {
     Field e;
     e.type = f.elem;
     e.nullable = f.elem_nullable;

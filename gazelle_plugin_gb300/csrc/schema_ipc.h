@@ -14,10 +14,16 @@ struct Field {
   int unit = 0;
   std::string name;
   std::string timezone;  // timestamp only; empty: none
-  // list: the element field (a fixed-width type; its precision / scale / unit are the ones above)
+  // a list of fixed-width or bool elements ("simple list", no children): the element field
+  // (its precision / scale / unit are the ones above)
   int elem = 0;
   std::string elem_name = "item";
   bool elem_nullable = true;
+  // nested types (list / large_list / map / struct with `children`): a list's element field,
+  // a map's entries struct (whose children are the key and the value), a struct's fields
+  std::vector<Field> children;
+  bool keys_sorted = false;  // map
+  bool nested() const { return !children.empty(); }
 };
 
 // Parses an Arrow IPC Schema message (encapsulated or legacy framing).

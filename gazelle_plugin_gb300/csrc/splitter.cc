@@ -18,68 +18,18 @@
 #include "gz_kernels.h"
 #include "lz4_kernels.h"
 #include "host_util.h"
+#include "split_util.h"
 #include "tune.h"
 
 namespace gz {
 
 namespace {
 
-inline int64_t BytesForBits(int64_t n) { return (n + 7) >> 3; }
 constexpr int64_t kMapWriteBytes = 256ll << 20;  // data files from this size are written through a mapping
-inline size_t AlignUp(size_t x, size_t a) { return (x + a - 1) / a * a; }
 inline int64_t NowNs() {
   return std::chrono::duration_cast<std::chrono::nanoseconds>(
              std::chrono::steady_clock::now().time_since_epoch())
       .count();
-}
-
-int ByteWidth(int t) {
-  switch (t) {
-    case GZ_TYPE_INT8: case GZ_TYPE_UINT8: return 1;
-    case GZ_TYPE_INT16: case GZ_TYPE_UINT16: case GZ_TYPE_HALF_FLOAT: return 2;
-    case GZ_TYPE_INT32: case GZ_TYPE_UINT32: case GZ_TYPE_FLOAT32: case GZ_TYPE_DATE32:
-    case GZ_TYPE_TIME32: return 4;
-    case GZ_TYPE_INT64: case GZ_TYPE_UINT64: case GZ_TYPE_FLOAT64: case GZ_TYPE_DATE64:
-    case GZ_TYPE_TIME64: case GZ_TYPE_TIMESTAMP: return 8;
-    case GZ_TYPE_DECIMAL128: return 16;
-    default: return 0;
-  }
-}
-inline bool IsBinary(int t) {
-  return t == GZ_TYPE_STRING || t == GZ_TYPE_BINARY || t == GZ_TYPE_LARGE_STRING || t == GZ_TYPE_LARGE_BINARY;
-}
-// Bytes of one offset of a binary column: int32, or int64 for LargeBinary / LargeString
-// (splitter.cc:480-516, 626-629, 1291-1299)
-inline int OffW(int t) { return t == GZ_TYPE_LARGE_STRING || t == GZ_TYPE_LARGE_BINARY ? 8 : 4; }
-// Offset r of an offsets buffer of width w, as int64
-inline int64_t OffAt(const uint8_t* off, int w, size_t r) {
-  if (w == 8) {
-    int64_t v;
-    memcpy(&v, off + r * 8, 8);
-    return v;
-  }
-  int32_t v;
-  memcpy(&v, off + r * 4, 4);
-  return v;
-}
-
-// Copies `nbits` bits from src (starting at bit `sbit`) to dst (starting at bit `dbit`);
-// dst bits outside the range are left as they are.
-void CopyBits(const uint8_t* src, uint64_t sbit, uint8_t* dst, uint64_t dbit, uint64_t nbits) {
-  for (uint64_t i = 0; i < nbits; i++) {
-    const uint64_t s = sbit + i, d = dbit + i;
-    const uint8_t b = (src[s >> 3] >> (s & 7)) & 1;
-    if (b) dst[d >> 3] |= (uint8_t)(1u << (d & 7));
-    else dst[d >> 3] &= (uint8_t)~(1u << (d & 7));
-  }
-}
-
-int64_t CountZeros(const uint8_t* bits, int64_t n) {
-  int64_t ones = 0;
-  int64_t full = n >> 3;
-  for (int64_t i = 0; i < full; i++) ones += __builtin_popcount(bits[i]);
-  for (int64_t i = full * 8; i < n; i++) ones += (bits[i >> 3] >> (i & 7)) & 1;
-  return n - ones;
 }
 
 }  // namespace
@@ -178,7 +128,10 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
     if ((int)i == pid_field_) continue;  // not an output column
     if (IsBinary(t)) bin.push_back((int32_t)i);
     else if (t == GZ_TYPE_NULL) continue;
-    else if (t == GZ_TYPE_LIST) {
+    else if (fields_[i].nested() || t == GZ_TYPE_LARGE_LIST || t == GZ_TYPE_STRUCT || t == GZ_TYPE_MAP) {
+      if (!fields_[i].nested()) return Status::Error(GZ_INVALID, "nested field without child fields");
+      continue;  // streams, planned below
+    } else if (t == GZ_TYPE_LIST) {
       if (ByteWidth(fields_[i].elem) <= 0 && fields_[i].elem != GZ_TYPE_BOOL)
         return Status::Error(GZ_NOT_IMPLEMENTED, "list columns of fixed-width or bool elements only");
       lists.push_back((int32_t)i);
@@ -190,16 +143,22 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
   n_bin_ = (int32_t)bin.size();
   n_policy_ = (int32_t)array_idx_.size();
   array_idx_.insert(array_idx_.end(), lists.begin(), lists.end());
+  first_stream_ = (int32_t)array_idx_.size();
+  n_slots_ = (int32_t)fields_.size();
+  {
+    Status ps = PlanNested();  // appends the nested columns' streams to array_idx_
+    if (!ps.ok()) return ps;
+  }
   n_array_ = (int32_t)array_idx_.size();
-  n_str_ = (int32_t)(bin.size() + lists.size());
+  n_str_ = (int32_t)(bin.size() + lists.size() + streams_.size());
   if (n_array_ == 0) return Status::Error(GZ_NOT_IMPLEMENTED, "schema without data columns");
   if (n_array_ > kMaxCols) return Status::Error(GZ_NOT_IMPLEMENTED, "more than 64 data columns");
-  if (n_str_ > max_str_columns()) return Status::Error(GZ_NOT_IMPLEMENTED, "more than 32 binary columns");
+  if (n_str_ > max_str_columns()) return Status::Error(GZ_NOT_IMPLEMENTED, "more than 64 binary, list and nested-stream columns");
   if ((int)keys_.size() > kMaxKeys) return Status::Error(GZ_NOT_IMPLEMENTED, "more than 8 hash keys");
 
   memset(&sd_, 0, sizeof(sd_));
   sd_.P = P_;
-  sd_.n_cols = (int32_t)fields_.size();
+  sd_.n_cols = n_slots_;
   sd_.n_array = n_array_;
   sd_.n_fixed = fixed_cnt_;
   sd_.n_str = n_str_;
@@ -209,6 +168,30 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
   sd_.pmod_magic = P_ > 1 ? UINT64_MAX / (uint64_t)P_ + 1 : 0;
   for (int a = 0; a < n_array_; a++) {
     const int ci = array_idx_[a];
+    if (a >= first_stream_) {  // a nested column's stream: list-like, rows from its slot
+      const Stream& sm = streams_[a - first_stream_];
+      if (field_array_[ci] < 0) field_array_[ci] = a;
+      sd_.arr_col[a] = sm.slot;
+      sd_.arr_kind[a] = COL_BINARY;
+      sd_.arr_width[a] = 4;
+      sd_.arr_str[a] = a - fixed_cnt_;
+      sd_.list_mask |= 1ull << a;
+      const NestNode& nd = nest_[sm.plan].nodes[sm.node];
+      int sh = 0;
+      if (sm.chars) {
+        sh = 0;
+      } else if (sm.payload == PAY_VALUES) {
+        while ((1 << sh) < nd.width) sh++;
+      } else if (sm.payload == PAY_LENGTHS) {
+        sh = 2;
+        lenpay_mask_ |= 1ull << a;
+      } else {
+        sd_.listbit_mask |= 1ull << a;
+        if (sm.payload == PAY_NONE) sd_.nopay_mask |= 1ull << a;
+      }
+      sd_.arr_shift[a] = sh;
+      continue;
+    }
     field_array_[ci] = a;
     const int t = fields_[ci].type;
     sd_.arr_col[a] = ci;
@@ -273,14 +256,19 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
     nk++;
   }
   sd_.n_keys = nk;
-  // JNI buffer layout (jni_common.h:308-382): [validity, (offsets), values] per field
+  // JNI buffer layout (jni_common.h:186-382): [validity, (offsets), values] per field, nested
+  // fields depth first
   field_buf0_.resize(fields_.size());
   int nb = 0;
   for (size_t i = 0; i < fields_.size(); i++) {
     field_buf0_[i] = nb;
-    nb += fields_[i].type == GZ_TYPE_LIST ? 4 : IsBinary(fields_[i].type) ? 3 : 2;
+    nb += fields_[i].nested() ? NestedBufferCount(fields_[i])
+          : fields_[i].type == GZ_TYPE_LIST ? 4 : IsBinary(fields_[i].type) ? 3 : 2;
   }
   n_bufs_expected_ = nb;
+  for (NestPlan& np : nest_)
+    for (NestNode& nd : np.nodes) nd.buf += field_buf0_[np.field];
+  dptr_.assign(n_bufs_expected_ + 1, nullptr);
   empirical_.assign(n_bin_, 0);
 
   device_ = opts_.device;
@@ -387,6 +375,11 @@ Splitter::~Splitter() {
     if (d_scratch_[i]) cudaFreeAsync(d_scratch_[i], stream_);
   }
   if (d_state_) cudaFreeAsync(d_state_, stream_);
+  if (d_iota_ || !old_iota_.empty()) {
+    if (stream_) cudaStreamSynchronize(stream_);
+    if (d_iota_) cudaFree(d_iota_);
+    for (int32_t* o : old_iota_) cudaFree(o);
+  }
   PinnedRelease(PinnedBlock{reinterpret_cast<uint8_t*>(h_jobs_), h_jobs_bytes_});
   if (gather_ev_) cudaEventDestroy(gather_ev_);
   if (pstream_) cudaStreamDestroy(pstream_);
@@ -550,13 +543,14 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
   if (!st.ok()) return st;
   const bool host_in = opts_.input_kind == GZ_INPUT_HOST;
   const uint32_t nr = (uint32_t)num_rows;
-  const size_t C = fields_.size();
+  const size_t C = (size_t)n_slots_;  // ColPtr slots: the fields, then the nested streams
+  const size_t nf = fields_.size();
 
   // validate and size every buffer that is read
   uint64_t validity_mask = 0, cvalid_mask = 0;
   size_t batch_bytes = 0;
   for (int k = 0; k < n_str_; k++) host_off_[k] = nullptr;
-  for (size_t f = 0; f < C; f++) {
+  for (size_t f = 0; f < nf; f++) {
     const int b0 = field_buf0_[f];
     need_[b0] = Need{nullptr, 0};
     need_[b0 + 1] = Need{nullptr, 0};
@@ -574,6 +568,25 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
     const int a = field_array_[f];
     if (a < 0) continue;  // null type: buffers ignored
     const int t = fields_[f].type;
+    if (fields_[f].nested()) {
+      // every buffer of the field goes to the device whole; its streams' validity buffers (their
+      // row masks and element validity) decide which bit regions the pass allocates
+      const int nb = NestedBufferCount(fields_[f]);
+      for (int j = b0; j < b0 + nb; j++)
+        need_[j] = addrs[j] != 0 && sizes[j] > 0 ? Need{reinterpret_cast<const uint8_t*>(addrs[j]), (size_t)sizes[j]}
+                                                 : Need{nullptr, 0};
+      for (size_t si = 0; si < streams_.size(); si++) {
+        const Stream& sm = streams_[si];
+        const NestPlan& np = nest_[sm.plan];
+        if (np.field != (int)f) continue;
+        const NestNode& nd = np.nodes[sm.node];
+        const int maskn = sm.chars ? (nd.ident ? sm.node : nd.mask) : nd.mask;
+        const bool entries = nd.parent >= 0 && np.nodes[nd.parent].type == GZ_TYPE_MAP;
+        if (maskn >= 0 && need_[np.nodes[maskn].buf].bytes) validity_mask |= 1ull << (first_stream_ + si);
+        if (!sm.chars && !entries && need_[nd.buf].bytes) cvalid_mask |= 1ull << (first_stream_ + si);
+      }
+      continue;
+    }
     if (addrs[b0] != 0 && sizes[b0] > 0) {
       const size_t vb = (size_t)BytesForBits(nr);
       if ((size_t)sizes[b0] < vb) return Status::Error(GZ_INVALID, "validity buffer too small");
@@ -685,9 +698,10 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
 
   // make room in the current flush group
   const size_t NB1 = pending_.size() + 1;
+  const size_t jobs_one = sizeof(NestJob) * 2 * streams_.size();  // derived arrays of a batch, at most
   const size_t tables_need = AlignUp(sizeof(BatchDesc) * NB1, 256) +
                              2 * AlignUp(sizeof(TileDesc) * (pending_tiles_ + ntiles), 256) +
-                             AlignUp(sizeof(ColPtr) * NB1 * C, 256) + 256;
+                             AlignUp(sizeof(ColPtr) * NB1 * C, 256) + AlignUp(jobs_one * NB1, 256) + 256;
   // (a batch whose call flag is read back has to be alone in its device pass: the earlier
   // batches go first, before this one is staged, so each pass reads its own staging buffer)
   if (!pending_.empty() &&
@@ -707,7 +721,7 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
   }
   if (host_in) {
     const size_t tables_one = AlignUp(sizeof(BatchDesc), 256) + 2 * AlignUp(sizeof(TileDesc) * ntiles, 256) +
-                              AlignUp(sizeof(ColPtr) * C, 256) + 256;
+                              AlignUp(sizeof(ColPtr) * C, 256) + AlignUp(jobs_one, 256) + 256;
     st = EnsureStaging(batch_bytes + (direct_ ? phase_slack : tables_one));
     if (!st.ok()) return st;
     if (pending_.empty() && stage_busy_[cur_]) {
@@ -726,25 +740,28 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
     jobs_.clear();
     size_t copy_bytes = 0;
     for (size_t f = 0; f < C; f++) {
-      ColPtr cp{nullptr, nullptr, nullptr, 0};
-      const int a = field_array_[f];
+      ColPtr cp{nullptr, nullptr, nullptr, 0, nullptr};
+      const int a = f < nf ? field_array_[f] : -1;
       if (a >= 0 || (int)f == pid_field_) {
         const int t = fields_[f].type;
         const int b0 = field_buf0_[f];
-        const bool list = t == GZ_TYPE_LIST;
-        const int nbuf = list ? 4 : IsBinary(t) ? 3 : 2;
+        const bool nested = fields_[f].nested();
+        const bool list = t == GZ_TYPE_LIST && !nested;
+        const int nbuf = nested ? NestedBufferCount(fields_[f]) : list ? 4 : IsBinary(t) ? 3 : 2;
         for (int j = 0; j < nbuf; j++) {
           const Need& nd = need_[b0 + j];
+          if (nested) dptr_[b0 + j] = nullptr;
           if (nd.bytes == 0) continue;
           size_t phase = 0;
           if (direct_) {
-            // same 16-byte phase as the source when that keeps the elements aligned
+            // same 16-byte phase as the source when that keeps the elements aligned (a nested
+            // field's buffers stay 64-byte aligned: their element widths vary by node)
             const uintptr_t sp = reinterpret_cast<uintptr_t>(nd.src);
             const uintptr_t elem = j == 0 ? 1
                                  : list ? (j == 1 ? 4 : j == 2 ? 1 : (uintptr_t)std::max(1, ByteWidth(fields_[f].elem)))
                                  : IsBinary(t) ? (j == 1 ? (uintptr_t)OffW(t) : 1)
                                  : t == GZ_TYPE_BOOL ? 1 : (uintptr_t)ByteWidth(t);
-            if (sp % elem == 0) phase = sp & 15;
+            if (!nested && sp % elem == 0) phase = sp & 15;
             h_jobs_[jobs_end_++] = HostCopy{nd.src, d_stage_[cur_] + used_ + phase, nd.bytes};
           } else {
             jobs_.push_back(CopyJob{h_stage_[cur_] + used_, nd.src, nd.bytes});
@@ -752,6 +769,10 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
           copy_bytes += nd.bytes;
           const uint8_t* dptr = d_stage_[cur_] + used_ + phase;
           used_ += AlignUp(phase + nd.bytes, 64);
+          if (nested) {  // read through the field's streams (StageNested)
+            dptr_[b0 + j] = dptr;
+            continue;
+          }
           if (j == 0) cp.validity = dptr;
           else if ((IsBinary(t) || list) && j == 1) cp.offsets = reinterpret_cast<const int32_t*>(dptr);
           else if (list && j == 2) cp.child_validity = dptr;
@@ -776,11 +797,17 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
     }
   } else {
     for (size_t f = 0; f < C; f++) {
-      ColPtr cp{nullptr, nullptr, nullptr, 0};
-      const int a = field_array_[f];
+      ColPtr cp{nullptr, nullptr, nullptr, 0, nullptr};
+      const int a = f < nf ? field_array_[f] : -1;
       if (a >= 0 || (int)f == pid_field_) {
         const int t = fields_[f].type;
         const int b0 = field_buf0_[f];
+        if (fields_[f].nested()) {  // read through the field's streams (StageNested)
+          const int nb = NestedBufferCount(fields_[f]);
+          for (int j = b0; j < b0 + nb; j++) dptr_[j] = need_[j].bytes ? need_[j].src : nullptr;
+          cols[f] = cp;
+          continue;
+        }
         if (need_[b0].bytes) cp.validity = need_[b0].src;
         if (IsBinary(t)) {
           cp.offsets = reinterpret_cast<const int32_t*>(addrs[b0 + 1]);
@@ -805,6 +832,15 @@ Status Splitter::SplitOne(int32_t num_rows, const int64_t* addrs, const int64_t*
         }
       }
       cols[f] = cp;
+    }
+  }
+  if (!streams_.empty()) {
+    st = StageNested(nr, addrs, sizes, dptr_.data(), cols, host_in);
+    if (!st.ok()) return st;
+    const size_t b = pending_.size();
+    for (size_t si = 0; si < streams_.size(); si++) {
+      const int k = first_stream_ + (int)si - fixed_cnt_;
+      pending_chars_[b * n_str_ + k] = char_scratch_[k];
     }
   }
   pending_bytes_ += batch_bytes;
@@ -862,7 +898,7 @@ Status Splitter::Flush() {
   if (pending_.empty()) return Status::OK();
   const bool host_in = opts_.input_kind == GZ_INPUT_HOST;
   const uint32_t NB = (uint32_t)pending_.size();
-  const size_t C = fields_.size();
+  const size_t C = (size_t)n_slots_;
   const int P = P_;
   const int nstr = n_str_;
   const int A = n_array_;
@@ -934,6 +970,7 @@ Status Splitter::Flush() {
       fr.off_values[a] = o;
       o += AlignUp((size_t)R * sd_.arr_width[a], 256);  // end offsets, 4 or 8 bytes
       if ((sd_.listbit_mask >> a) & 1ull) continue;     // bool elements: a bit region, below
+      if ((lenpay_mask_ >> a) & 1ull) continue;         // lengths: beside the bit regions, below
       uint64_t cb = 0;
       for (uint32_t b = 0; b < NB; b++) cb += pending_chars_[(size_t)b * n_str_ + sd_.arr_str[a]];
       fr.off_chars[a] = o;
@@ -950,7 +987,13 @@ Status Splitter::Flush() {
       fr.off_valid[a] = o;
       o += vwords_bytes;
     }
-    if ((sd_.listbit_mask >> a) & 1ull) {  // a list of bool elements: one bit per element
+    if ((lenpay_mask_ >> a) & 1ull) {  // entries' lengths: read on the host at Stop, as bits are
+      uint64_t cb = 0;
+      for (uint32_t b = 0; b < NB; b++) cb += pending_chars_[(size_t)b * n_str_ + sd_.arr_str[a]];
+      fr.off_chars[a] = o;
+      o += AlignUp((size_t)cb + 16, 256);
+    }
+    if (((sd_.listbit_mask & ~sd_.nopay_mask) >> a) & 1ull) {  // a list of bool elements: one bit per element
       uint64_t cb = 0;
       for (uint32_t b = 0; b < NB; b++) cb += pending_chars_[(size_t)b * n_str_ + sd_.arr_str[a]];
       fr.off_chars[a] = o;
@@ -1000,11 +1043,22 @@ Status Splitter::Flush() {
   const size_t s_vbits = take((size_t)P * 4);
   const size_t meta_words = (3 + 2 * (size_t)nstr) * P + 1 + (size_t)emit_cap * (kEmitFixedWords + nstr);
   const size_t s_meta = take(meta_words * 4);  // rows_f, pstart, vstart, bytes_f, cstart, count, emits
+  // nested columns' derived arrays (k_nest_prep) and their jobs
+  std::vector<size_t> der_at(pending_derived_.size(), 0);
+  size_t der_bytes = 0, n_jobs = 0;
+  for (size_t i = 0; i < pending_derived_.size(); i++) {
+    if (pending_derived_[i].same_as >= 0) continue;
+    der_at[i] = der_bytes;
+    der_bytes += AlignUp(pending_derived_[i].bytes, 256);
+    n_jobs++;
+  }
+  const size_t s_der = der_bytes ? take(der_bytes) : 0;
   const size_t tb_batches = AlignUp(sizeof(BatchDesc) * NB, 256);
   const size_t tb_tiles = AlignUp(sizeof(SegDesc) * T, 256);
   const size_t tb_cols = AlignUp(sizeof(ColPtr) * NB * C, 256);
   const size_t tb_tdesc = AlignUp(sizeof(TileDesc) * NT, 256);
-  const size_t tb_total = tb_batches + tb_tiles + tb_cols + tb_tdesc;
+  const size_t tb_jobs = AlignUp(sizeof(NestJob) * n_jobs, 256);
+  const size_t tb_total = tb_batches + tb_tiles + tb_cols + tb_tdesc + tb_jobs;
   const bool staged_tables = host_in && !direct_;  // tables travel with the pinned staging copy
   const size_t s_tab = staged_tables ? 0 : take(tb_total);
   // this pass's scratch buffer: stream_ already runs this pass's work after the k_scatter that
@@ -1090,6 +1144,22 @@ Status Splitter::Flush() {
     htab = h_tables_[ti];
     dtab = nullptr;
   }
+  // derived arrays: in this pass's scratch, pointed at from their slots; jobs after the tiles
+  {
+    NestJob* hj = reinterpret_cast<NestJob*>(htab + tb_batches + tb_tiles + tb_cols + tb_tdesc);
+    size_t j = 0;
+    for (size_t i = 0; i < pending_derived_.size(); i++) {
+      PendingDerived& pd = pending_derived_[i];
+      const size_t src = pd.same_as >= 0 ? (size_t)pd.same_as : i;
+      int32_t* arr = reinterpret_cast<int32_t*>(S + s_der + der_at[src]);
+      ColPtr& cp = pending_cols_[(size_t)pd.batch * C + pd.slot];
+      if (pd.values) cp.values = reinterpret_cast<const uint8_t*>(arr);
+      else cp.offsets = arr;
+      if (pd.same_as >= 0) continue;
+      pd.job.out = arr;
+      hj[j++] = pd.job;
+    }
+  }
   memcpy(htab, batches.data(), sizeof(BatchDesc) * NB);
   memcpy(htab + tb_batches, segs.data(), sizeof(SegDesc) * T);
   ColPtr* hc = reinterpret_cast<ColPtr*>(htab + tb_batches + tb_tiles);
@@ -1139,6 +1209,12 @@ Status Splitter::Flush() {
     st = Cuda(cudaEventCreate(&e), "cudaEventCreate");
     if (!st.ok()) return st;
   }
+  if (n_jobs) {  // the nested columns' row ranges and lengths, before anything reads them
+    st = Cuda(launch_nest_prep(reinterpret_cast<const NestJob*>(dtab + tb_batches + tb_tiles + tb_cols + tb_tdesc),
+                               (uint32_t)n_jobs, d_err_, stream_),
+              "k_nest_prep");
+    if (!st.ok()) return st;
+  }
   cudaEventRecord(fr.ev[0], stream_);
   st = Cuda(launch_hash_count(sd_, fd, stream_), "k_hash_count");
   if (!st.ok()) return st;
@@ -1184,6 +1260,7 @@ Status Splitter::Flush() {
   pending_.clear();
   pending_cols_.clear();
   pending_chars_.clear();
+  pending_derived_.clear();
   pending_bytes_ = 0;
   pending_tiles_ = 0;
   if (host_in) {
@@ -1366,6 +1443,9 @@ Status Splitter::SyncAndCheck() {
     return Status::Error(GZ_INVALID, "binary offsets are decreasing or exceed the value buffer");
   if (err & kErrBadPid)
     return Status::Error(GZ_INVALID, "a partition id is negative or not less than num_partitions");
+  if (err & kErrNestSpan)
+    return Status::Error(GZ_NOT_IMPLEMENTED,
+                         "a null list, map or string entry inside a nested column holds elements");
   if (err) return Status::Error(GZ_CUDA, "device emission list overflow");
   for (; timed_flushes_ < flushes_.size() && flushes_[timed_flushes_].launched; timed_flushes_++) {
     FlushRec& f = flushes_[timed_flushes_];
@@ -1497,6 +1577,11 @@ Status Splitter::BuildSegment(int p, const Segment& s, SegMsg* msg, bool device_
     const int a = field_array_[fi];
     if (a < 0) {
       nodes.push_back(FieldNodeMeta{n, n});
+      continue;
+    }
+    if (fields_[fi].nested()) {  // its builder's output (splitter.cc:532-545), rebuilt from its streams
+      for (const NestPlan& np : nest_)
+        if (np.field == (int)fi) BuildNested(p, s, np, 0, &nodes, &bufs, &temps, device_view, &rawb);
       continue;
     }
     if ((sd_.list_mask >> a) & 1ull) {
@@ -2092,10 +2177,16 @@ Status Splitter::CompressedSize(int32_t num_rows, const int64_t* addrs, const in
   auto pad8 = [](int64_t x) { return (x + 7) & ~int64_t(7); };
   // the body buffers as the IPC writer lays them out (validity only with nulls)
   std::vector<std::pair<const uint8_t*, int64_t>> bufs;
+  std::vector<std::vector<uint8_t>> temps;
   for (size_t f = 0; f < fields_.size(); f++) {
     const int t = fields_[f].type;
     if (t == GZ_TYPE_NULL) continue;
     const int b0 = field_buf0_[f];
+    if (fields_[f].nested()) {
+      for (const NestPlan& np : nest_)
+        if (np.field == (int)f) NestedBodyBuffers(np, 0, 0, nr, addrs, sizes, &bufs, &temps);
+      continue;
+    }
     const uint8_t* vb = reinterpret_cast<const uint8_t*>(addrs[b0]);
     bufs.push_back({vb, addrs[b0] != 0 && sizes[b0] > 0 && nr > 0 && CountZeros(vb, nr) > 0 ? BytesForBits(nr) : 0});
     if (t == GZ_TYPE_LIST) {  // offsets, then the element array (validity only with nulls)

@@ -40,6 +40,9 @@ struct Status {
   }
 };
 
+// Entries of a nested field in a batch's flat buffer list (MakeArrayData's depth-first order).
+int NestedBufferCount(const Field& f);
+
 class Splitter {
  public:
   static Status Make(const std::string& short_name, std::vector<Field> fields, int32_t P,
@@ -93,6 +96,57 @@ class Splitter {
     uint64_t validity_mask;  // array columns with a validity buffer
     uint64_t cvalid_mask;    // list columns with an element validity buffer
   };
+
+  // Nested columns (list / large_list / map / struct other than a list of fixed-width or bool
+  // elements, list_array_idx_ in the reference).  A top-level row selects one contiguous range
+  // of entries at every node of the column's type tree: the rows themselves at the top and
+  // under structs, the children's entries [offsets[lo], offsets[hi]) under a list or map.  Each
+  // node's entries reach the device as a "stream": a list-like array column (after the binary
+  // and simple list ones) whose row offsets are those ranges (the node's offsets composed along
+  // its path, computed by k_nest_prep; the rows themselves through an identity array), whose
+  // element validity is the node's validity and whose elements carry the node's payload: fixed
+  // width values, bool bits, the entries' lengths (binary, list and map nodes: their offsets are
+  // rebuilt from them at Stop) or nothing (struct).  A binary node's characters are one more
+  // stream.  A top-level list or map is merged with its child's stream (its own validity and
+  // offsets are that stream's row validity and offsets), as simple lists are.
+ public:
+  enum StreamPayload { PAY_VALUES = 0, PAY_BITS = 1, PAY_LENGTHS = 2, PAY_NONE = 3 };
+  struct NestNode {
+    int type = 0;
+    int width = 0;          // element bytes of a fixed-width leaf
+    int buf = 0;            // its first buffer in the batch's flat list
+    int parent = -1;
+    std::vector<int> kids;  // node indices (pre-order)
+    bool ident = false;     // its entries are the rows
+    bool inner = false;     // below a list or map: a null entry must hold no elements
+    int mask = -1;          // node whose validity empties the rows of its streams (a list / map
+                            // whose entries are rows)
+    std::vector<int> chain; // nodes whose offsets compose its row ranges, outermost first
+    int stream = -1;        // array column of its entries (-1: none, e.g. a map's entries struct)
+    int chars = -1;         // binary node: array column of its characters
+  };
+  struct NestPlan {
+    int field = -1;
+    std::vector<NestNode> nodes;  // pre-order; nodes[0] is the field
+    bool root_list = false;       // nodes[0] (list / large_list / map) shares its child's stream
+  };
+  struct Stream {  // one array column of a nested field
+    int plan = 0, node = 0;
+    bool chars = false;  // the node's characters
+    int payload = PAY_NONE;
+    int slot = 0;        // its ColPtr slot
+  };
+  // an array computed on the device per batch (k_nest_prep) and pointed at from a ColPtr
+  struct PendingDerived {
+    uint32_t batch;
+    int slot;
+    bool values;    // the slot's values (lengths) rather than its offsets (composed ranges)
+    NestJob job;    // out filled at Flush
+    size_t bytes;
+    int same_as;    // >= 0: the slot points at that earlier entry's array (same composed ranges)
+  };
+
+ private:
   struct Need {
     const uint8_t* src;
     size_t bytes;
@@ -190,6 +244,30 @@ class Splitter {
   Status CompressBodies(std::vector<std::vector<SegMsg>>* msgs);
   uint32_t SplitBatchSize(int32_t num_rows, const std::vector<const uint8_t*>& host_offsets,
                           bool* complete);
+
+  // nested columns
+  Status PlanNested();
+  void PlanNode(NestPlan& np, const Field& f, int parent, int* buf);
+  Status StageNested(uint32_t nr, const int64_t* addrs, const int64_t* sizes, const uint8_t* const* dptr,
+                     ColPtr* cols, bool host_in);
+  Status EnsureIota(uint32_t rows);
+  // Stop: the nested field's nodes and body buffers of one record batch
+  void BuildNested(int p, const Segment& s, const NestPlan& np, int node, std::vector<FieldNodeMeta>* nodes,
+                   std::vector<ChunkedBuffer>* bufs, std::vector<std::vector<uint8_t>>* temps, bool device_view,
+                   int64_t* raw) const;
+  void NestedBodyBuffers(const NestPlan& np, int node, int64_t off, int64_t len, const int64_t* addrs,
+                         const int64_t* sizes, std::vector<std::pair<const uint8_t*, int64_t>>* bufs,
+                         std::vector<std::vector<uint8_t>>* temps) const;
+  std::vector<NestPlan> nest_;
+  std::vector<Stream> streams_;  // streams_[a - first_stream_] for array column a
+  int first_stream_ = 0;
+  int n_slots_ = 0;              // ColPtr slots per batch: the fields, then one per stream
+  uint64_t lenpay_mask_ = 0;     // streams whose elements are lengths (kept with the bit regions)
+  std::vector<PendingDerived> pending_derived_;
+  std::vector<const uint8_t*> dptr_;  // per-call scratch: device address of every input buffer
+  int32_t* d_iota_ = nullptr;    // 0, 1, 2, ...: the row ranges of streams whose entries are rows
+  uint32_t iota_cap_ = 0;
+  std::vector<int32_t*> old_iota_;
 
   // schema
   std::vector<Field> fields_;  // the input schema (the range partitioner's id field included)

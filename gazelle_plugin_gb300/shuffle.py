@@ -65,6 +65,8 @@ class GzField(ctypes.Structure):
         ("unit", ctypes.c_int32),
         ("elem_type", ctypes.c_int32),
         ("name", ctypes.c_char_p),
+        ("n_children", ctypes.c_int32),
+        ("children", ctypes.c_void_p),
     ]
 
 
@@ -345,9 +347,11 @@ def split_options(offheapPerTask: int = 0, bufferSize: int = 4096, codec: Option
 
 
 def _fields(schema):
+    """A GzField array of the schema (children of nested fields in arrays of their own) and the
+    objects that must stay alive with it."""
     from . import workloads as W
     arr = (GzField * len(schema))()
-    names = [f.name.encode() for f in schema]
+    keep = [arr]
     for i, f in enumerate(schema):
         arr[i].type = f.code
         arr[i].nullable = int(f.nullable)
@@ -355,8 +359,15 @@ def _fields(schema):
         if f.is_list:
             arr[i].elem_type = W.TYPE_CODES[f.elem]
             arr[i].precision, arr[i].scale, arr[i].unit = W.Field("item", f.elem).params
-        arr[i].name = names[i]
-    return arr, names
+        if f.is_nested:
+            kids, kkeep = _fields(list(f.kids))
+            keep.append(kkeep)
+            arr[i].n_children = len(f.kids)
+            arr[i].children = ctypes.addressof(kids)
+        name = f.name.encode()
+        keep.append(name)
+        arr[i].name = name
+    return arr, keep
 
 
 @dataclasses.dataclass

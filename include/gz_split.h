@@ -42,10 +42,15 @@ typedef enum GzType {
   /* 64-bit offsets (SplitBinaryType<LargeBinaryType::offset_type>, splitter.cc:1291-1299):
    * payload columns only; one batch's column may hold at most 2^31 - 1 character bytes */
   GZ_TYPE_LARGE_STRING = 21, GZ_TYPE_LARGE_BINARY = 22,
-  /* list of fixed-width elements (SplitListArray / AppendList, splitter.cc:1322-1344): a payload
-   * column whose element type is GzField.elem_type; buffers [validity, int32 offsets, element
-   * validity, element values] */
-  GZ_TYPE_LIST = 23
+  /* list (SplitListArray / AppendList, splitter.cc:1322-1344; payload columns only): of
+   * fixed-width or bool elements given by GzField.elem_type, buffers [validity, int32 offsets,
+   * element validity, element values]; or with one child field of any type */
+  GZ_TYPE_LIST = 23,
+  /* nested payload columns with child fields (jni_common.h:186-300 reads their buffers depth
+   * first: [validity, (offsets)] then each child's): large_list (int64 offsets; one child),
+   * struct (its fields), map (two children, key and value; the entries struct between them takes
+   * one buffer entry, its validity, which is ignored) */
+  GZ_TYPE_LARGE_LIST = 24, GZ_TYPE_STRUCT = 25, GZ_TYPE_MAP = 26
 } GzType;
 
 /* One schema field.  `unit`: time/timestamp unit (0 s, 1 ms, 2 us, 3 ns); `precision` /
@@ -56,9 +61,12 @@ typedef struct GzField {
   int32_t precision;
   int32_t scale;
   int32_t unit;
-  int32_t elem_type;  /* GZ_TYPE_LIST: the element type (fixed width; precision / scale / unit
-                         then describe the element, named "item" and nullable) */
+  int32_t elem_type;  /* GZ_TYPE_LIST without children: the element type (fixed width or bool;
+                         precision / scale / unit then describe the element, named "item" and
+                         nullable) */
   const char* name;
+  int32_t n_children;              /* nested types: child fields (a map: key, then value) */
+  const struct GzField* children;
 } GzField;
 
 /* Codec of the emitted record batches (the JNI's codec strings "uncompressed", "lz4",

@@ -98,6 +98,35 @@ def parse_stream(data: bytes, schema) -> List[Tuple[int, list]]:
     return out
 
 
+def parse_stream_raw(data: bytes) -> List[Tuple[int, list, list]]:
+    """Record batches of one stream without a schema: [(rows, [(length, null_count) per node],
+    [buffer bytes, decompressed])]."""
+    out = []
+    pos, n = 0, len(data)
+    while pos < n:
+        first = struct.unpack_from("<I", data, pos)[0]
+        if first == 0xFFFFFFFF:
+            meta_len, meta_pos = struct.unpack_from("<i", data, pos + 4)[0], pos + 8
+        else:
+            meta_len, meta_pos = first, pos + 4
+        if meta_len == 0:
+            break
+        fb = _Flat(data[meta_pos:meta_pos + meta_len])
+        msg = fb.u32(0)
+        body_len = fb.scalar(msg, 3, "q")
+        body = meta_pos + meta_len
+        if fb.scalar(msg, 1, "B") == HEADER_RECORD_BATCH:
+            rb = fb.table(msg, 2)
+            compressed = fb.table(rb, 3) is not None
+            nodes, bufs = fb.table(rb, 1), fb.table(rb, 2)
+            node_list = [struct.unpack_from("<qq", fb.b, nodes + 4 + 16 * i) for i in range(fb.u32(nodes))]
+            raw = [data[body + o: body + o + l]
+                   for o, l in (struct.unpack_from("<qq", fb.b, bufs + 4 + 16 * i) for i in range(fb.u32(bufs)))]
+            out.append((fb.scalar(rb, 0, "q"), node_list, [_decompress(b) for b in raw] if compressed else raw))
+        pos = body + ((body_len + 7) & ~7)
+    return out
+
+
 def _decompress(b: bytes) -> bytes:
     """A compressed body buffer: int64 uncompressed length, then one LZ4 frame (-1: raw bytes)."""
     if not b:

@@ -80,6 +80,10 @@ def record(name, schema, batches, P, keys, opts, gen, short_name="hash"):
     out = O.run_ref(schema, batches, P, keys, short_name=short_name, **opts)
     P = len(out.partition_lengths)
     rec = {"short_name": short_name} if short_name != "hash" else {}
+    if gen.get("workload") == "nested":  # Splitter::CompressedSize of each input batch (uncompressed)
+        r = O.RefSplitter(schema, P, keys, short_name=short_name, **opts)
+        rec["body_lengths"] = [int(r.compressed_size(b)) for b in batches]
+        r.close()
     return {
         **rec,
         "name": name,

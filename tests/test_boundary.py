@@ -136,8 +136,15 @@ def test_schema_ipc_parser():
     # time32/time64/date64/timestamp round-trip through their Arrow units
     assert types == expect
     assert nulls == [int(f.nullable) for f in schema]
-    # lists of fixed-width elements only: nested lists and lists of strings are refused
-    for t in (pa.list_(pa.list_(pa.int32())), pa.list_(pa.utf8()), pa.struct([pa.field("a", pa.int32())])):
+    # nested types of any depth parse (their top-level type codes are reported)
+    for t, code in ((pa.list_(pa.list_(pa.int32())), 23), (pa.list_(pa.utf8()), 23),
+                    (pa.struct([pa.field("a", pa.int32())]), 25), (pa.large_list(pa.int8()), 24),
+                    (pa.map_(pa.utf8(), pa.list_(pa.bool_())), 26)):
+        st, types, _ = parse_schema(pa.schema([pa.field("l", t)]).serialize().to_pybytes())
+        assert st == 0 and types == [code], t
+    # null children, empty structs and other nested types are refused
+    for t in (pa.list_(pa.null()), pa.struct([]), pa.list_(pa.int32(), 3),
+              pa.struct([pa.field("u", pa.dense_union([pa.field("x", pa.int8())]))])):
         st, _, _ = parse_schema(pa.schema([pa.field("l", t)]).serialize().to_pybytes())
         assert st != 0, t
 
@@ -160,7 +167,13 @@ def test_schema_message_matches_arrow_writer():
              pa.decimal128(10, 2), pa.decimal128(38, 0), pa.decimal128(1, 0), pa.utf8(),
              pa.binary(), pa.null(), pa.large_utf8(), pa.large_binary(),
              pa.list_(pa.int32()), pa.list_(pa.float64()), pa.list_(pa.field("element", pa.int64(), False)),
-             pa.list_(pa.decimal128(12, 3)), pa.list_(pa.timestamp("us", tz="UTC")), pa.list_(pa.date32())]
+             pa.list_(pa.decimal128(12, 3)), pa.list_(pa.timestamp("us", tz="UTC")), pa.list_(pa.date32()),
+             # nested types
+             pa.list_(pa.utf8()), pa.list_(pa.list_(pa.int32())), pa.large_list(pa.list_(pa.utf8())),
+             pa.list_(pa.struct([pa.field("a", pa.int32()), pa.field("b", pa.utf8(), False)])),
+             pa.list_(pa.map_(pa.utf8(), pa.utf8())), pa.map_(pa.int32(), pa.list_(pa.float64())),
+             pa.map_(pa.utf8(), pa.utf8(), keys_sorted=True), pa.large_list(pa.bool_()),
+             pa.struct([pa.field("a", pa.list_(pa.int32())), pa.field("s", pa.struct([pa.field("t", pa.bool_())]))])]
     rnd = random.Random(7)
     out = np.zeros(1 << 16, np.uint8)
     n = ctypes.c_int64(0)

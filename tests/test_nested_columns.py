@@ -103,3 +103,127 @@ def test_oracle_refuses_unsupported_nested_types():
                 F("n", "struct", True, None, ())):
         with pytest.raises(ValueError):
             O.OracleSplitter([F("k", "int32", False), bad], 4, [0])
+
+
+# ---------------------------------------------------------------------------------------- GPU
+def _all_shapes(seed, nb=4, rows=3000, spans=True):
+    """An int64 key and one column of every nested shape of the fixtures."""
+    rng = np.random.default_rng(seed)
+    schema = [W.Field("k", "int64", False)] + [G.NESTED_SHAPES[i](f"N{i}") for i in range(len(G.NESTED_SHAPES))]
+    batches = []
+    for _ in range(nb):
+        n = int(rng.integers(rows // 2, rows + 1))
+        bufs = W._column(rng, schema[0], n, rng.integers(0, 1 << 40, size=n), 0.0)
+        for f in schema[1:]:
+            bufs += W.nested_column(rng, f, n, 0.15, 4, True, spans)
+        batches.append(W.Batch(n, bufs))
+    return schema, batches
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", NESTED, ids=[c["name"] for c in NESTED])
+def test_gpu_nested_columns_golden(case):
+    """The fixture's data file, lengths and spills; and every batch's body length under no codec
+    (split with firstRecordBatch: Splitter::CompressedSize, splitter.cc:358-369)."""
+    from gazelle_plugin_gb300 import shuffle as S
+    o = case["options"]
+    w = S.ShuffleSplitterJniWrapper()
+    h = w.make(S.NativePartitioning("hash", case["num_partitions"], None, case["keys"], _schema(case)),
+               bufferSize=o.get("buffer_size", 4096), preferSpill=o.get("prefer_spill", True),
+               offheapPerTask=o.get("offheap_per_task", 0), writeSchema=o.get("write_schema", False))
+    try:
+        bodies = []
+        for b in G.regenerate(case):
+            a, z = b.addrs_sizes()
+            bodies.append(w.split(h, b.num_rows, a, z, True))
+            w.split(h, b.num_rows, a, z)
+        res = w.stop(h)
+        data = w.data(h)
+    finally:
+        w.close(h)
+    assert bodies == case["body_lengths"]
+    assert list(res.partitionLengths) == case["partition_lengths"]
+    assert list(res.rawPartitionLengths) == case["raw_partition_lengths"]
+    assert res.totalBytesSpilled == case["bytes_spilled"]
+    assert hashlib.sha256(data).hexdigest() == case["data_sha256"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("P", [1, 7, 200, 3000])
+def test_gpu_nested_columns_vs_oracle(P):
+    from gazelle_plugin_gb300 import shuffle as S
+    schema, batches = _all_shapes(80 + P)
+    res, data = S.split_batches(schema, batches, P, [0], writeSchema=False)
+    ref = O.run_oracle(schema, batches, P, [0])
+    assert data == ref.data
+    assert np.array_equal(res.partitionLengths, ref.partition_lengths)
+    assert np.array_equal(res.rawPartitionLengths, ref.raw_partition_lengths)
+
+
+@pytest.mark.gpu
+def test_gpu_nested_columns_device_resident_many_passes():
+    torch = pytest.importorskip("torch")
+    from gazelle_plugin_gb300 import shuffle as S
+    schema, batches = _all_shapes(91, nb=10)
+    keep = []
+    w = S.ShuffleSplitterJniWrapper()
+    h = w.make(S.NativePartitioning("hash", 64, None, [0], list(schema)), writeSchema=False,
+               input_kind=S.GZ_INPUT_DEVICE_RETAINED, flush_bytes=1 << 18)
+    for b in batches:
+        ts = [torch.from_numpy(x.copy()).cuda() if x.nbytes else torch.zeros(0, dtype=torch.uint8).cuda()
+              for x in b.buffers]
+        keep += ts
+        w.split(h, b.num_rows, [t.data_ptr() if t.numel() else 0 for t in ts], [t.numel() for t in ts])
+    assert w.stats(h)[0] >= 3
+    res = w.stop(h)
+    data = w.data(h)
+    w.close(h)
+    ref = O.run_oracle(schema, batches, 64, [0])
+    assert data == ref.data
+    assert np.array_equal(res.rawPartitionLengths, ref.raw_partition_lengths)
+
+
+@pytest.mark.gpu
+def test_gpu_nested_columns_lz4():
+    from gazelle_plugin_gb300 import shuffle as S
+    from oracle import ipc_read as R
+    schema, batches = _all_shapes(93, nb=3)
+    P = 12
+    res_u, data_u = S.split_batches(schema, batches, P, [0], writeSchema=False)
+    res_z, data_z = S.split_batches(schema, batches, P, [0], writeSchema=False, codec="lz4")
+    assert np.array_equal(res_u.rawPartitionLengths, res_z.rawPartitionLengths)
+    su = np.concatenate([[0], np.cumsum(np.asarray(res_u.partitionLengths))])
+    sz = np.concatenate([[0], np.cumsum(np.asarray(res_z.partitionLengths))])
+    for p in range(P):
+        assert R.parse_stream_raw(data_u[su[p]:su[p + 1]]) == R.parse_stream_raw(data_z[sz[p]:sz[p + 1]])
+
+
+@pytest.mark.gpu
+def test_gpu_nested_rejections():
+    """A null entry below a list holding elements (its builder would drop them) and nested keys
+    are refused; the reader does not read nested fields."""
+    from gazelle_plugin_gb300 import shuffle as S
+    F = W.Field
+    lst = F("a", "list", True, None, (F("item", "list", True, "int32"),))
+    schema = [F("k", "int32", False), lst]
+    w = S.ShuffleSplitterJniWrapper()
+    with pytest.raises(S.SplitterError) as e:
+        w.make(S.NativePartitioning("hash", 4, None, [1], list(schema)), writeSchema=False)
+    assert e.value.status == S.GZ_NOT_IMPLEMENTED
+    h = w.make(S.NativePartitioning("hash", 4, None, [0], list(schema)), writeSchema=False)
+    keys = np.arange(2, dtype=np.int32)
+    offs = np.array([0, 1, 2], np.int32)              # each row: one inner list
+    inner_valid = np.array([0b01], np.uint8)          # the second inner list is null ...
+    inner_offs = np.array([0, 1, 3], np.int32)        # ... and holds two elements
+    vals = np.arange(3, dtype=np.int32)
+    bufs = [np.zeros(0, np.uint8), keys, np.zeros(0, np.uint8), offs, inner_valid, inner_offs,
+            np.zeros(0, np.uint8), vals]
+    addrs = [b.ctypes.data if b.nbytes else 0 for b in bufs]
+    with pytest.raises(S.SplitterError) as e:
+        w.split(h, 2, addrs, [b.nbytes for b in bufs])
+        w.stop(h)
+    assert e.value.status == S.GZ_NOT_IMPLEMENTED
+    w.close(h)
+    with pytest.raises(S.SplitterError) as e:
+        S.PartitionReader(list(schema))
+    assert e.value.status == S.GZ_NOT_IMPLEMENTED
