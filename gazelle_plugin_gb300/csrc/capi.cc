@@ -429,6 +429,28 @@ GzStatus gz_reader_elem_validity_to_host(int64_t handle, int32_t field, uint8_t*
   return ReportReader(r.get(), r->reader->ElemValidityToHost(field, out));
 }
 
+GzStatus gz_reader_node_count(int64_t handle, int32_t field, int32_t* out_nodes) {
+  auto r = LookupReader(handle);
+  if (!r || !out_nodes) return GZ_INVALID;
+  const int n = r->reader->NodeCount(field);
+  if (n <= 0) return ReportReader(r.get(), gz::Status::Error(GZ_INVALID, "field out of range"));
+  *out_nodes = n;
+  return GZ_OK;
+}
+
+GzStatus gz_reader_node(int64_t handle, int32_t field, int32_t node, GzDeviceColumn* out) {
+  auto r = LookupReader(handle);
+  if (!r || !out) return GZ_INVALID;
+  return ReportReader(r.get(), r->reader->Node(field, node, out));
+}
+
+GzStatus gz_reader_node_to_host(int64_t handle, int32_t field, int32_t node, uint8_t* validity, void* offsets,
+                                uint8_t* values) {
+  auto r = LookupReader(handle);
+  if (!r) return GZ_INVALID;
+  return ReportReader(r.get(), r->reader->NodeToHost(field, node, validity, offsets, values));
+}
+
 GzStatus gz_reader_close(int64_t handle) {
   std::lock_guard<std::mutex> lk(g_mu);
   g_readers.erase(handle);

@@ -4,6 +4,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <functional>
 
 #include "flatbuf.h"
 #include "gz_kernels.h"
@@ -48,6 +49,15 @@ int FixedWidth(int t) {
   }
 }
 
+bool ListLikeType(int t) { return t == GZ_TYPE_LIST || t == GZ_TYPE_LARGE_LIST || t == GZ_TYPE_MAP; }
+bool NestedField(const Field& f) {
+  return f.nested() || f.type == GZ_TYPE_LARGE_LIST || f.type == GZ_TYPE_STRUCT || f.type == GZ_TYPE_MAP;
+}
+// offset bytes of a node with offsets
+int NodeOffsetWidth(int t) { return t == GZ_TYPE_LARGE_LIST || IsLargeBinaryType(t) ? 8 : 4; }
+// the body buffers of one node: [validity] + offsets (list / map / binary) + values (leaves)
+int NodeBuffers(int t) { return t == GZ_TYPE_STRUCT ? 1 : ListLikeType(t) ? 2 : IsBinaryType(t) ? 3 : 2; }
+
 // Arrow IPC metadata (Message.fbs / Schema.fbs): Message {version, header_type, header,
 // bodyLength}; RecordBatch {length, nodes: [FieldNode{length, null_count}], buffers:
 // [Buffer{offset, length}], compression: BodyCompression{codec, method}}.
@@ -63,9 +73,32 @@ Status PartitionReader::Cuda(cudaError_t e, const char* what) {
 
 Status PartitionReader::Make(std::vector<Field> fields, int device, std::unique_ptr<PartitionReader>* out) {
   std::unique_ptr<PartitionReader> r(new PartitionReader());
-  for (const Field& f : fields) {
-    if (f.nested() || f.type == GZ_TYPE_LARGE_LIST || f.type == GZ_TYPE_STRUCT || f.type == GZ_TYPE_MAP)
-      return Status::Error(GZ_NOT_IMPLEMENTED, "nested fields are not implemented by the reader");
+  r->tree_.assign(fields.size(), {});
+  for (size_t i = 0; i < fields.size(); i++) {
+    const Field& f = fields[i];
+    if (NestedField(f)) {
+      if (!f.nested()) return Status::Error(GZ_INVALID, "nested field without child fields");
+      // pre-order type tree; a simple list below becomes a list node and its element leaf
+      std::vector<RNode>& tree = r->tree_[i];
+      bool ok = true;
+      std::function<void(const Field&, int)> add = [&](const Field& g, int parent) {
+        const int idx = (int)tree.size();
+        tree.push_back(RNode{g.type, FixedWidth(g.type), parent, {}});
+        if (parent >= 0) tree[parent].kids.push_back(idx);
+        if (g.type == GZ_TYPE_LIST && !g.nested()) {
+          Field e;
+          e.type = g.elem;
+          add(e, idx);
+          return;
+        }
+        const bool leaf_ok = IsBinaryType(g.type) || g.type == GZ_TYPE_BOOL || FixedWidth(g.type) > 0;
+        if (g.children.empty() ? !leaf_ok : !(ListLikeType(g.type) || g.type == GZ_TYPE_STRUCT)) ok = false;
+        for (const Field& c : g.children) add(c, idx);
+      };
+      add(f, -1);
+      if (!ok) return Status::Error(GZ_NOT_IMPLEMENTED, "nested field type not implemented by the reader");
+      continue;
+    }
     if (f.type == GZ_TYPE_LIST ? FixedWidth(f.elem) == 0 && f.elem != GZ_TYPE_BOOL
                                : f.type != GZ_TYPE_NULL && f.type != GZ_TYPE_BOOL && !IsBinaryType(f.type) &&
                                      FixedWidth(f.type) == 0)
@@ -195,6 +228,44 @@ Status PartitionReader::ParseStream(const uint8_t* data, int64_t len, int stream
         c.null_count = nn;
         const int t = fields_[f].type;
         if (t == GZ_TYPE_NULL) continue;  // no buffers
+        if (!tree_[f].empty()) {  // a nested field: every node in pre-order with its buffers
+          const std::vector<RNode>& tree = tree_[f];
+          c.nodes.resize(tree.size());
+          for (size_t q = 0; q < tree.size(); q++) {
+            NodeRef& nr = c.nodes[q];
+            if (q == 0) {
+              nr.length = nl;
+              nr.null_count = nn;
+            } else {
+              if (node >= n_nodes || !r.Get(nodes + 4 + 16 * (int64_t)node, &nr.length) ||
+                  !r.Get(nodes + 4 + 16 * (int64_t)node + 8, &nr.null_count))
+                return Status::Error(GZ_INVALID, "record batch has too few field nodes");
+              node++;
+            }
+            const int qt = tree[q].type;
+            bool ok = next_buf(&nr.validity);
+            if (ListLikeType(qt) || IsBinaryType(qt)) ok = ok && next_buf(&nr.offsets);
+            if (qt != GZ_TYPE_STRUCT && !ListLikeType(qt)) ok = ok && next_buf(&nr.values);
+            if (!ok) return Status::Error(GZ_INVALID, "bad buffer list in a record batch");
+            if (nr.length < 0 || nr.null_count < 0 || nr.null_count > nr.length || nr.length >= (1ll << 31))
+              return Status::Error(GZ_INVALID, "bad field node");
+            if (nr.null_count > 0 && nr.validity.length < (nr.length + 7) / 8)
+              return Status::Error(GZ_INVALID, "validity buffer too short");
+            if (nr.null_count == 0) nr.validity.length = 0;
+            if (ListLikeType(qt) || IsBinaryType(qt)) {
+              const int ow = NodeOffsetWidth(qt);
+              if (nr.offsets.length < (nr.length + 1) * ow) return Status::Error(GZ_INVALID, "offsets buffer too short");
+              if (!nr.offsets.decoded) {  // decoded offsets are read after decoding
+                nr.o0 = ReadOffset(data + nr.offsets.offset, ow, 0);
+                nr.o1 = ReadOffset(data + nr.offsets.offset, ow, nr.length);
+              }
+            } else if (qt != GZ_TYPE_STRUCT) {
+              const int64_t need = qt == GZ_TYPE_BOOL ? (nr.length + 7) / 8 : nr.length * tree[q].width;
+              if (nr.values.length < need) return Status::Error(GZ_INVALID, "value buffer too short");
+            }
+          }
+          continue;
+        }
         if (t == GZ_TYPE_LIST) {
           // the element node follows the list's; buffers [validity, offsets, element validity, values]
           int64_t cl, cn;
@@ -308,52 +379,86 @@ Status PartitionReader::AddStream(const uint8_t* data, int64_t len) {
     if (st.ok()) st = Cuda(launch_lz4_decode(reinterpret_cast<const Lz4Frame*>(arena), (uint32_t)jobs.size(), d_err, stream_),
                            "k_lz4_decode");
     if (st.ok()) st = Cuda(cudaMemcpyAsync(&err, d_err, 4, cudaMemcpyDeviceToHost, stream_), "D2H");
-    // the decoded offsets bound each batch's characters: for each, the 4-byte words of its first
-    // and last offset (low word, then high word of a 64-bit one)
+    // the decoded offsets bound each batch's characters (and a nested node's child entries): for
+    // each, the 4-byte words of its first and last offset (low word, then high word of a 64-bit one)
     std::vector<const int32_t*> where;
     std::vector<std::pair<size_t, size_t>> which;  // (batch, field)
+    std::vector<std::pair<NodeRef*, int>> nested;  // a nested node and its offset width
+    auto queue_ends = [&](const int32_t* o, int64_t n, int ow) {
+      for (int end = 0; end < 2; end++) {
+        const int64_t at = end ? n : 0;
+        where.push_back(o + at * (ow / 4));
+        if (ow == 8) where.push_back(o + at * 2 + 1);
+      }
+    };
     for (size_t bi = 0; bi < bs.size(); bi++)
       for (size_t f = 0; f < fields_.size(); f++) {
-        const ColRef& c = bs[bi].cols[f];
+        ColRef& c = bs[bi].cols[f];
+        if (!tree_[f].empty()) continue;
         if (!HasOffsets(fields_[f].type) || !c.offsets.decoded) continue;
         const int32_t* o = reinterpret_cast<const int32_t*>(arenas_.back() + c.offsets.offset);
-        if (IsLargeBinaryType(fields_[f].type)) {
-          where.push_back(o);
-          where.push_back(o + 1);
-          where.push_back(o + 2 * bs[bi].rows);
-          where.push_back(o + 2 * bs[bi].rows + 1);
-        } else {
-          where.push_back(o);
-          where.push_back(o + bs[bi].rows);
-        }
+        queue_ends(o, bs[bi].rows, IsLargeBinaryType(fields_[f].type) ? 8 : 4);
         which.push_back({bi, f});
       }
+    for (size_t bi = 0; bi < bs.size(); bi++)
+      for (size_t f = 0; f < fields_.size(); f++)
+        for (size_t q = 0; q < tree_[f].size(); q++) {
+          NodeRef& nr = bs[bi].cols[f].nodes[q];
+          if (!nr.offsets.decoded) continue;
+          const int ow = NodeOffsetWidth(tree_[f][q].type);
+          queue_ends(reinterpret_cast<const int32_t*>(arenas_.back() + nr.offsets.offset), nr.length, ow);
+          nested.push_back({&nr, ow});
+        }
     std::vector<int32_t> ends(where.size());
     if (st.ok() && !where.empty()) st = Cuda(gather_words(where.data(), ends.data(), where.size(), stream_), "offsets");
     if (st.ok()) st = Cuda(cudaStreamSynchronize(stream_), "k_lz4_decode");
     if (!st.ok()) return st;
     if (err) return Status::Error(GZ_INVALID, "a compressed buffer is not a valid LZ4 frame of its stated length");
     size_t e = 0;
+    auto word = [&](int ow) -> int64_t {
+      const int64_t v = ow == 8 ? (int64_t)((uint64_t)(uint32_t)ends[e] | (uint64_t)(uint32_t)ends[e + 1] << 32)
+                                : (int64_t)ends[e];
+      e += ow / 4;
+      return v;
+    };
     for (size_t i = 0; i < which.size(); i++) {
       ColRef& c = bs[which[i].first].cols[which[i].second];
-      if (IsLargeBinaryType(fields_[which[i].second].type)) {
-        c.o0 = (int64_t)((uint64_t)(uint32_t)ends[e] | (uint64_t)(uint32_t)ends[e + 1] << 32);
-        c.o1 = (int64_t)((uint64_t)(uint32_t)ends[e + 2] | (uint64_t)(uint32_t)ends[e + 3] << 32);
-        e += 4;
-      } else {
-        c.o0 = ends[e];
-        c.o1 = ends[e + 1];
-        e += 2;
-      }
+      const int ow = IsLargeBinaryType(fields_[which[i].second].type) ? 8 : 4;
+      c.o0 = word(ow);
+      c.o1 = word(ow);
       const int64_t w = fields_[which[i].second].type == GZ_TYPE_LIST ? FixedWidth(fields_[which[i].second].elem) : 1;
       if (c.o0 < 0 || c.o1 < c.o0 || (w ? c.o1 * w : (c.o1 + 7) / 8) > c.values.length)
         return Status::Error(GZ_INVALID, "offsets exceed the characters");
+    }
+    for (auto& x : nested) {
+      x.first->o0 = word(x.second);
+      x.first->o1 = word(x.second);
     }
     arena_mem_.push_back(arena);
   } else {
     st = Cuda(cudaStreamSynchronize(stream_), "H2D stream");
     if (!st.ok()) return st;
   }
+  // nested fields: list / map children hold exactly the parent's entries from 0 (as Arrow's
+  // builders and IPC writer leave them), struct children the struct's, characters lie inside
+  // their buffer
+  for (const Batch& b : bs)
+    for (size_t f = 0; f < fields_.size(); f++)
+      for (size_t q = 0; q < tree_[f].size(); q++) {
+        const RNode& tn = tree_[f][q];
+        const NodeRef& nr = b.cols[f].nodes[q];
+        if (ListLikeType(tn.type)) {
+          if (nr.o0 != 0 || nr.o1 != b.cols[f].nodes[tn.kids[0]].length)
+            return Status::Error(GZ_NOT_IMPLEMENTED, "nested offsets that do not span their child from 0");
+        } else if (IsBinaryType(tn.type)) {
+          if (nr.o0 < 0 || nr.o1 < nr.o0 || nr.o1 > nr.values.length)
+            return Status::Error(GZ_INVALID, "offsets exceed the characters");
+        } else if (tn.type == GZ_TYPE_STRUCT) {
+          for (int k : tn.kids)
+            if (b.cols[f].nodes[k].length != nr.length)
+              return Status::Error(GZ_INVALID, "struct child length differs from the struct's");
+        }
+      }
   for (Batch& b : bs) batches_.push_back(std::move(b));
   return Status::OK();
 }
@@ -371,10 +476,53 @@ Status PartitionReader::Finish(int64_t* rows, int32_t* n_batches) {
   std::vector<int64_t> chars(F, 0);  // binary: characters; list: elements
   size_t total = 0;
   const size_t bit_bytes = AlignUp((size_t)((R + 31) / 32) * 4, 256);
+  // nested fields, per node: entries, nulls, characters (binary) and where its buffers go
+  struct NodeLayout {
+    int64_t length = 0, nulls = 0, chars = 0;
+    size_t valid = SIZE_MAX, off = SIZE_MAX, val = SIZE_MAX;
+  };
+  std::vector<std::vector<NodeLayout>> nl(F);
+  for (size_t f = 0; f < F; f++) {
+    const std::vector<RNode>& tree = tree_[f];
+    if (tree.empty()) continue;
+    nl[f].resize(tree.size());
+    for (const Batch& b : batches_)
+      for (size_t q = 0; q < tree.size(); q++) {
+        const NodeRef& nr = b.cols[f].nodes[q];
+        nl[f][q].length += nr.length;
+        nl[f][q].nulls += nr.null_count;
+        if (IsBinaryType(tree[q].type)) nl[f][q].chars += nr.o1 - nr.o0;
+      }
+    for (size_t q = 0; q < tree.size(); q++) {
+      NodeLayout& L = nl[f][q];
+      const int t = tree[q].type;
+      if (L.length >= (1ll << 31) || (L.chars >= (1ll << 31) && !IsLargeBinaryType(t)))
+        return Status::Error(GZ_INVALID, "more than 2^31 - 1 entries in one nested node");
+      if (L.nulls > 0) {
+        L.valid = total;
+        total += AlignUp((size_t)((L.length + 31) / 32) * 4, 256);
+      }
+      if (ListLikeType(t) || IsBinaryType(t)) {
+        L.off = total;
+        total += AlignUp((size_t)(L.length + 1) * NodeOffsetWidth(t), 256);
+      }
+      if (IsBinaryType(t)) {
+        L.val = total;
+        total += AlignUp((size_t)L.chars + 16, 256);
+      } else if (t == GZ_TYPE_BOOL) {
+        L.val = total;
+        total += AlignUp((size_t)((L.length + 31) / 32) * 4, 256);
+      } else if (t != GZ_TYPE_STRUCT && !ListLikeType(t)) {
+        L.val = total;
+        total += AlignUp((size_t)L.length * tree[q].width, 256);
+      }
+    }
+  }
   for (size_t f = 0; f < F; f++) {
     const int t = fields_[f].type;
     OutCol& oc = out_[f];
     oc = OutCol();
+    if (!tree_[f].empty()) continue;
     if (t == GZ_TYPE_NULL) {
       oc.null_count = R;
       continue;
@@ -425,6 +573,11 @@ Status PartitionReader::Finish(int64_t* rows, int32_t* n_batches) {
       tj.push_back(BitJob{reinterpret_cast<const uint32_t*>(src), dst, src ? x : 0, dst_bit + x, std::min(kBitChunk, n - x)});
   };
   std::vector<int64_t> char_pos(F, 0);
+  std::vector<std::vector<int64_t>> npos(F), ncpos(F);  // nested: entries / characters so far per node
+  for (size_t f = 0; f < F; f++) {
+    npos[f].assign(tree_[f].size(), 0);
+    ncpos[f].assign(tree_[f].size(), 0);
+  }
   int64_t row = 0;
   for (size_t bi = 0; bi < batches_.size(); bi++) {
     const Batch& b = batches_[bi];
@@ -433,6 +586,42 @@ Status PartitionReader::Finish(int64_t* rows, int32_t* n_batches) {
       const int t = fields_[f].type;
       if (t == GZ_TYPE_NULL) continue;
       const ColRef& c = b.cols[f];
+      if (!tree_[f].empty()) {
+        // every node: validity bits at its entries so far, offsets rebased onto its child's
+        // entries (or characters) so far, values / bits / characters appended
+        const std::vector<RNode>& tree = tree_[f];
+        for (size_t q = 0; q < tree.size(); q++) {
+          const NodeRef& nr = c.nodes[q];
+          const NodeLayout& L = nl[f][q];
+          const int qt = tree[q].type;
+          const uint64_t at = (uint64_t)npos[f][q];
+          if (L.valid != SIZE_MAX && nr.length > 0)
+            add_bits(nr.validity.length ? Base(nr.validity, b.stream) : nullptr,
+                     reinterpret_cast<uint32_t*>(out_mem_ + L.valid), at, (uint64_t)nr.length);
+          if (ListLikeType(qt) || IsBinaryType(qt)) {
+            const int ow = NodeOffsetWidth(qt);
+            const int64_t base = IsBinaryType(qt) ? ncpos[f][q] : npos[f][tree[q].kids[0]];
+            const uint8_t* src_off = Base(nr.offsets, b.stream);
+            uint8_t* dst_off = out_mem_ + L.off + at * ow;
+            const uint64_t n = (uint64_t)nr.length + (last ? 1 : 0);
+            for (uint64_t x = 0; x < n; x += kChunk / 4)
+              oj.push_back(OffsetJob{src_off + x * ow, dst_off + x * ow, (uint32_t)std::min<uint64_t>(kChunk / 4, n - x),
+                                     ow == 8 ? 1u : 0u, base - nr.o0});
+          }
+          if (IsBinaryType(qt)) {
+            add_bytes(Base(nr.values, b.stream) + nr.o0, out_mem_ + L.val + ncpos[f][q], (uint64_t)(nr.o1 - nr.o0));
+            ncpos[f][q] += nr.o1 - nr.o0;
+          } else if (qt == GZ_TYPE_BOOL) {
+            if (nr.length > 0)
+              add_bits(Base(nr.values, b.stream), reinterpret_cast<uint32_t*>(out_mem_ + L.val), at, (uint64_t)nr.length);
+          } else if (qt != GZ_TYPE_STRUCT && !ListLikeType(qt)) {
+            add_bytes(Base(nr.values, b.stream), out_mem_ + L.val + at * tree[q].width,
+                      (uint64_t)nr.length * tree[q].width);
+          }
+        }
+        for (size_t q = 0; q < tree.size(); q++) npos[f][q] += c.nodes[q].length;
+        continue;
+      }
       if (o_valid[f] != SIZE_MAX)
         add_bits(c.validity.length ? Base(c.validity, b.stream) : nullptr,
                  reinterpret_cast<uint32_t*>(out_mem_ + o_valid[f]), (uint64_t)row, (uint64_t)b.rows);
@@ -514,10 +703,27 @@ Status PartitionReader::Finish(int64_t* rows, int32_t* n_batches) {
   }
   st = Cuda(cudaStreamSynchronize(stream_), "reader kernels");
   if (!st.ok()) return st;
+  out_nodes_.assign(F, {});
+  for (size_t f = 0; f < F; f++) {
+    for (size_t q = 0; q < tree_[f].size(); q++) {
+      const NodeLayout& L = nl[f][q];
+      const int qt = tree_[f][q].type;
+      OutNode on;
+      on.type = qt;
+      on.length = L.length;
+      on.null_count = L.nulls;
+      if (L.valid != SIZE_MAX) on.validity = out_mem_ + L.valid;
+      if (L.off != SIZE_MAX) on.offsets = out_mem_ + L.off;
+      if (L.val != SIZE_MAX) on.values = out_mem_ + L.val;
+      on.values_bytes = IsBinaryType(qt) ? L.chars : qt == GZ_TYPE_BOOL ? (L.length + 7) / 8
+                        : L.val != SIZE_MAX ? L.length * tree_[f][q].width : 0;
+      out_nodes_[f].push_back(on);
+    }
+  }
   for (size_t f = 0; f < F; f++) {
     OutCol& oc = out_[f];
     const int t = fields_[f].type;
-    if (t == GZ_TYPE_NULL) continue;
+    if (t == GZ_TYPE_NULL || !tree_[f].empty()) continue;
     if (o_valid[f] != SIZE_MAX) oc.validity = out_mem_ + o_valid[f];
     if (o_off[f] != SIZE_MAX) oc.offsets = out_mem_ + o_off[f];
     oc.values = out_mem_ + o_val[f];
@@ -540,6 +746,7 @@ Status PartitionReader::Finish(int64_t* rows, int32_t* n_batches) {
 Status PartitionReader::Column(int field, GzDeviceColumn* out) const {
   if (!finished_) return Status::Error(GZ_INVALID, "reader not finished");
   if (field < 0 || field >= (int)fields_.size()) return Status::Error(GZ_INVALID, "field out of range");
+  if (!tree_[field].empty()) return Node(field, 0, out);
   const OutCol& c = out_[field];
   out->type = fields_[field].type;
   out->reserved = 0;
@@ -553,6 +760,66 @@ Status PartitionReader::Column(int field, GzDeviceColumn* out) const {
   out->child_length = c.child_length;
   out->child_null_count = c.child_null_count;
   return Status::OK();
+}
+
+int PartitionReader::NodeCount(int field) const {
+  if (field < 0 || field >= (int)fields_.size()) return 0;
+  if (!tree_[field].empty()) return (int)tree_[field].size();
+  return fields_[field].type == GZ_TYPE_LIST ? 2 : 1;
+}
+
+Status PartitionReader::Node(int field, int node, GzDeviceColumn* out) const {
+  if (!finished_) return Status::Error(GZ_INVALID, "reader not finished");
+  if (field < 0 || field >= (int)fields_.size()) return Status::Error(GZ_INVALID, "field out of range");
+  if (node < 0 || node >= NodeCount(field)) return Status::Error(GZ_INVALID, "node out of range");
+  memset(out, 0, sizeof(*out));
+  if (!tree_[field].empty()) {
+    const OutNode& n = out_nodes_[field][node];
+    out->type = n.type;
+    out->length = n.length;
+    out->null_count = n.null_count;
+    out->validity = n.validity;
+    out->offsets = n.offsets;
+    out->values = n.values;
+    out->values_bytes = n.values_bytes;
+    return Status::OK();
+  }
+  if (node == 0) {
+    Status st = Column(field, out);
+    if (st.ok() && fields_[field].type == GZ_TYPE_LIST) out->values = nullptr, out->values_bytes = 0;
+    return st;
+  }
+  // a simple list's elements
+  const OutCol& c = out_[field];
+  out->type = fields_[field].elem;
+  out->length = c.child_length;
+  out->null_count = c.child_null_count;
+  out->validity = c.child_validity;
+  out->values = c.values;
+  out->values_bytes = c.values_bytes;
+  return Status::OK();
+}
+
+Status PartitionReader::NodeToHost(int field, int node, uint8_t* validity, void* offsets, uint8_t* values) {
+  GzDeviceColumn c;
+  Status st = Node(field, node, &c);
+  if (!st.ok()) return st;
+  st = Cuda(cudaSetDevice(device_), "cudaSetDevice");
+  if (!st.ok()) return st;
+  if (validity && c.validity) {
+    st = Cuda(cudaMemcpyAsync(validity, c.validity, (size_t)(c.length + 7) / 8, cudaMemcpyDeviceToHost, stream_), "D2H");
+    if (!st.ok()) return st;
+  }
+  if (offsets && c.offsets) {
+    st = Cuda(cudaMemcpyAsync(offsets, c.offsets, (size_t)(c.length + 1) * NodeOffsetWidth(c.type), cudaMemcpyDeviceToHost,
+                              stream_), "D2H");
+    if (!st.ok()) return st;
+  }
+  if (values && c.values && c.values_bytes > 0) {
+    st = Cuda(cudaMemcpyAsync(values, c.values, (size_t)c.values_bytes, cudaMemcpyDeviceToHost, stream_), "D2H");
+    if (!st.ok()) return st;
+  }
+  return Cuda(cudaStreamSynchronize(stream_), "D2H");
 }
 
 Status PartitionReader::ElemValidityToHost(int field, uint8_t* out) {
@@ -579,7 +846,7 @@ Status PartitionReader::ColumnToHost(int field, uint8_t* validity, void* offsets
     if (!st.ok()) return st;
   }
   if (offsets && c.offsets) {
-    st = Cuda(cudaMemcpyAsync(offsets, c.offsets, (size_t)(c.length + 1) * OffsetWidth(c.type), cudaMemcpyDeviceToHost,
+    st = Cuda(cudaMemcpyAsync(offsets, c.offsets, (size_t)(c.length + 1) * NodeOffsetWidth(c.type), cudaMemcpyDeviceToHost,
                               stream_), "D2H");
     if (!st.ok()) return st;
   }

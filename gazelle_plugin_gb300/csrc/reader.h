@@ -37,6 +37,12 @@ class PartitionReader {
   Status Column(int field, GzDeviceColumn* out) const;
   Status ColumnToHost(int field, uint8_t* validity, void* offsets, uint8_t* values);
   Status ElemValidityToHost(int field, uint8_t* out);
+  // The nodes of a field in pre-order: 1 for flat fields, 2 for a list of fixed-width or bool
+  // elements (the list, its elements), the type tree of a nested field (a map's entries struct
+  // between the map and its key / value).
+  int NodeCount(int field) const;
+  Status Node(int field, int node, GzDeviceColumn* out) const;
+  Status NodeToHost(int field, int node, uint8_t* validity, void* offsets, uint8_t* values);
 
  private:
   struct BufRef {
@@ -47,12 +53,32 @@ class PartitionReader {
   struct FrameRef {  // one compressed buffer: its LZ4 frame in the stream, its arena range
     int64_t src = 0, src_len = 0, dst = 0, dst_len = 0;
   };
+  // one node of a nested field's record batch
+  struct NodeRef {
+    int64_t length = 0, null_count = 0;
+    BufRef validity, offsets, values;
+    int64_t o0 = 0, o1 = 0;  // first and last offset (binary: characters; list / map: child entries)
+  };
   struct ColRef {
     int64_t null_count = 0;
     BufRef validity, offsets, values;
     int64_t o0 = 0, o1 = 0;  // binary: first and last offset (the batch's characters; list: elements)
     BufRef cvalidity;        // list: element validity
     int64_t child_nulls = 0;
+    std::vector<NodeRef> nodes;  // nested field: its nodes in pre-order
+  };
+  // a nested field's type tree (pre-order)
+  struct RNode {
+    int type = 0, width = 0, parent = -1;
+    std::vector<int> kids;
+  };
+  struct OutNode {
+    int type = 0;
+    int64_t length = 0, null_count = 0;
+    uint8_t* validity = nullptr;
+    uint8_t* offsets = nullptr;
+    uint8_t* values = nullptr;
+    int64_t values_bytes = 0;
   };
   struct Batch {
     int stream = 0;
@@ -78,6 +104,8 @@ class PartitionReader {
   }
 
   std::vector<Field> fields_;
+  std::vector<std::vector<RNode>> tree_;        // per field: its nodes (nested fields only)
+  std::vector<std::vector<OutNode>> out_nodes_;  // per field: the concatenated nodes (nested fields)
   int device_ = 0;
   cudaStream_t stream_ = nullptr;
   std::vector<uint8_t*> images_;  // device copy of every stream

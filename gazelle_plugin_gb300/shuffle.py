@@ -149,6 +149,13 @@ def lib() -> ctypes.CDLL:
                                                ctypes.c_void_p]
         L.gz_reader_elem_validity_to_host.restype = ctypes.c_int
         L.gz_reader_elem_validity_to_host.argtypes = [ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p]
+        L.gz_reader_node_count.restype = ctypes.c_int
+        L.gz_reader_node_count.argtypes = [ctypes.c_int64, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
+        L.gz_reader_node.restype = ctypes.c_int
+        L.gz_reader_node.argtypes = [ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p]
+        L.gz_reader_node_to_host.restype = ctypes.c_int
+        L.gz_reader_node_to_host.argtypes = [ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,
+                                             ctypes.c_void_p, ctypes.c_void_p]
         L.gz_reader_close.restype = ctypes.c_int
         L.gz_reader_close.argtypes = [ctypes.c_int64]
         L.gz_serve_start.restype = ctypes.c_int
@@ -676,12 +683,30 @@ class PartitionReader:
         """(validity bytes or None, offsets or None, values bytes) of a concatenated column."""
         c = self.column(field)
         valid = np.zeros((c.length + 7) // 8, np.uint8) if c.validity else None
-        offs = np.zeros(c.length + 1, np.int64 if c.type in (21, 22) else np.int32) if c.offsets else None
+        offs = np.zeros(c.length + 1, np.int64 if c.type in (21, 22, 24) else np.int32) if c.offsets else None
         vals = np.zeros(c.values_bytes, np.uint8)
         _check(lib().gz_reader_column_to_host(self.h, field, valid.ctypes.data if valid is not None else None,
                                               offs.ctypes.data if offs is not None else None,
                                               vals.ctypes.data if vals.nbytes else None))
         return valid, offs, vals
+
+    def node_count(self, field: int) -> int:
+        """Nodes of a field in pre-order (gz_reader_node_count)."""
+        n = ctypes.c_int32(0)
+        _check(lib().gz_reader_node_count(self.h, field, ctypes.byref(n)))
+        return n.value
+
+    def node_to_host(self, field: int, node: int):
+        """(length, null_count, validity bytes or None, offsets or None, values bytes) of one node."""
+        c = GzDeviceColumn()
+        _check(lib().gz_reader_node(self.h, field, node, ctypes.byref(c)))
+        valid = np.zeros((c.length + 7) // 8, np.uint8) if c.validity else None
+        offs = np.zeros(c.length + 1, np.int64 if c.type in (21, 22, 24) else np.int32) if c.offsets else None
+        vals = np.zeros(c.values_bytes, np.uint8)
+        _check(lib().gz_reader_node_to_host(self.h, field, node, valid.ctypes.data if valid is not None else None,
+                                            offs.ctypes.data if offs is not None else None,
+                                            vals.ctypes.data if vals.nbytes else None))
+        return c.length, c.null_count, valid, offs, vals
 
     def element_validity_to_host(self, field: int):
         """A list column's element validity bytes, or None without a null element."""

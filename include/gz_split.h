@@ -410,6 +410,18 @@ GzStatus gz_reader_column_to_host(int64_t handle, int32_t field, uint8_t* validi
  * the column has no null element.  Waits for the copy. */
 GzStatus gz_reader_elem_validity_to_host(int64_t handle, int32_t field, uint8_t* out);
 
+/* The nodes of field `field` in pre-order (the Arrow children layout the record batches carry):
+ * 1 for a flat field, 2 for a list of fixed-width or bool elements (the list; its elements), the
+ * type tree of a nested field (a map's entries struct between the map and its key and value).
+ * Each node as a column: its entries, validity (nullptr: no nulls), offsets (list / map / binary;
+ * 64-bit for large types), values (fixed width, bool bits, characters; nullptr for list, map and
+ * struct nodes).  Reduce-side counterpart of Arrow Java's nested vectors
+ * (ArrowColumnarBatchSerializer.scala:110-240). */
+GzStatus gz_reader_node_count(int64_t handle, int32_t field, int32_t* out_nodes);
+GzStatus gz_reader_node(int64_t handle, int32_t field, int32_t node, GzDeviceColumn* out);
+GzStatus gz_reader_node_to_host(int64_t handle, int32_t field, int32_t node, uint8_t* validity, void* offsets,
+                                uint8_t* values);
+
 /* Frees the reader and its device columns. */
 GzStatus gz_reader_close(int64_t handle);
 

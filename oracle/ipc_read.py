@@ -221,6 +221,66 @@ def read_partition(schema, streams: Sequence[bytes]):
     return rows, cols
 
 
+def read_partition_nodes(schema, streams: Sequence[bytes]):
+    """Every field of a partition as its nodes in pre-order (a map's entries struct included),
+    each concatenated over all record batches of all streams: (length, null_count, validity as a
+    bool array or None when no entry is null, offsets (int32 / int64, from 0) or None, values:
+    bytes, or a bool array for bool nodes).  Offsets of a list / map start at 0 in every batch
+    (the writers' layout); binary characters are taken from the first to the last offset."""
+    from gazelle_plugin_gb300.workloads import BYTE_WIDTH as BW, TYPE_CODES
+    names = {v: k for k, v in TYPE_CODES.items()}
+    trees = [[names[c & 0xff] for c in f.type_nodes()] for f in schema]
+
+    def nbuf(t):
+        return 0 if t == "null" else 1 if t == "struct" else 2 if t in ("list", "large_list", "map") else \
+            3 if t in ("utf8", "binary", "large_utf8", "large_binary") else 2
+
+    acc = [[{"len": 0, "nulls": 0, "valid": [], "offs": [], "vals": [], "base": 0} for _ in tree] for tree in trees]
+    for s in streams:
+        for _, nodes, bufs in parse_stream_raw(s):
+            ni = bi = 0
+            for fi, tree in enumerate(trees):
+                for q, t in enumerate(tree):
+                    length, nulls = nodes[ni]
+                    ni += 1
+                    own = bufs[bi:bi + nbuf(t)]
+                    bi += nbuf(t)
+                    a = acc[fi][q]
+                    a["len"] += length
+                    a["nulls"] += nulls
+                    a["valid"].append(_bits(own[0], length) if nulls else np.ones(length, bool))
+                    if t in ("list", "large_list", "map", "utf8", "binary", "large_utf8", "large_binary"):
+                        o = np.frombuffer(own[1], np.int64 if t.startswith("large") else np.int32)[:length + 1]
+                        if not len(o):
+                            o = np.zeros(1, np.int32)
+                        a["offs"].append(o[:-1] - o[0] + a["base"])
+                        a["base"] += int(o[-1] - o[0])
+                        a["last"] = a["base"]
+                        if t not in ("list", "large_list", "map"):
+                            a["vals"].append(own[2][int(o[0]):int(o[-1])])
+                    elif t == "bool":
+                        a["vals"].append(_bits(own[1], length))
+                    elif t not in ("struct", "null"):
+                        a["vals"].append(own[1][:length * BW[t]])
+    out = []
+    for fi, tree in enumerate(trees):
+        nodes = []
+        for q, t in enumerate(tree):
+            a = acc[fi][q]
+            valid = np.concatenate(a["valid"]) if a["nulls"] else None
+            offs = None
+            if t in ("list", "large_list", "map", "utf8", "binary", "large_utf8", "large_binary"):
+                dt = np.int64 if t.startswith("large") else np.int32
+                offs = np.concatenate(a["offs"] + [np.array([a["base"]])]).astype(dt)
+            if t == "bool":
+                vals = np.concatenate(a["vals"]) if a["vals"] else np.zeros(0, bool)
+            else:
+                vals = b"".join(a["vals"])
+            nodes.append((a["len"], a["nulls"], valid, offs, vals))
+        out.append(nodes)
+    return out
+
+
 def pack_bits(v: Optional[np.ndarray]) -> Optional[bytes]:
     """An LSB-first bitmap of a bool array, zero padded (None stays None)."""
     if v is None:

@@ -201,7 +201,7 @@ def test_gpu_nested_columns_lz4():
 @pytest.mark.gpu
 def test_gpu_nested_rejections():
     """A null entry below a list holding elements (its builder would drop them) and nested keys
-    are refused; the reader does not read nested fields."""
+    are refused."""
     from gazelle_plugin_gb300 import shuffle as S
     F = W.Field
     lst = F("a", "list", True, None, (F("item", "list", True, "int32"),))
@@ -224,6 +224,104 @@ def test_gpu_nested_rejections():
         w.stop(h)
     assert e.value.status == S.GZ_NOT_IMPLEMENTED
     w.close(h)
-    with pytest.raises(S.SplitterError) as e:
-        S.PartitionReader(list(schema))
-    assert e.value.status == S.GZ_NOT_IMPLEMENTED
+
+
+# ---------------------------------------------------------------------------------------- reader
+def _arrow_nodes(pa, arr):
+    """Pre-order nodes of an Arrow array in read_partition_nodes' form."""
+    t = arr.type
+    n = len(arr)
+    nulls = arr.null_count
+    valid = arr.is_valid().to_numpy(zero_copy_only=False) if nulls else None
+    if pa.types.is_struct(t):
+        out = [(n, nulls, valid, None, b"")]
+        for i in range(t.num_fields):
+            out += _arrow_nodes(pa, arr.field(i))
+        return out
+    if pa.types.is_list(t) or pa.types.is_large_list(t) or pa.types.is_map(t):
+        o = np.asarray(arr.offsets)
+        offs = (o - o[0]).astype(np.int64 if pa.types.is_large_list(t) else np.int32)
+        child = arr.values.slice(int(o[0]), int(o[-1] - o[0]))
+        out = [(n, nulls, valid, offs, b"")]
+        if pa.types.is_map(t):  # the entries struct, then key and value
+            out.append((len(child), 0, None, None, b""))
+            out += _arrow_nodes(pa, child.field(0)) + _arrow_nodes(pa, child.field(1))
+        else:
+            out += _arrow_nodes(pa, child)
+        return out
+    if pa.types.is_binary(t) or pa.types.is_string(t) or pa.types.is_large_binary(t) or pa.types.is_large_string(t):
+        big = pa.types.is_large_binary(t) or pa.types.is_large_string(t)
+        o = np.frombuffer(arr.buffers()[1], np.int64 if big else np.int32)[arr.offset:arr.offset + n + 1]
+        data = arr.buffers()[2].to_pybytes() if arr.buffers()[2] is not None else b""
+        return [(n, nulls, valid, (o - o[0]).astype(np.int64 if big else np.int32), data[int(o[0]):int(o[-1])])]
+    if pa.types.is_boolean(t):
+        bits = np.unpackbits(np.frombuffer(arr.buffers()[1], np.uint8), bitorder="little")
+        return [(n, nulls, valid, None, bits[arr.offset:arr.offset + n].astype(bool))]
+    w = t.bit_width // 8
+    return [(n, nulls, valid, None, arr.buffers()[1].to_pybytes()[arr.offset * w:(arr.offset + n) * w])]
+
+
+def _same_nodes(a, b):
+    assert len(a) == len(b)
+    for x, y in zip(a, b):
+        assert x[0] == y[0] and x[1] == y[1]
+        assert (x[2] is None) == (y[2] is None) and (x[2] is None or np.array_equal(x[2], y[2]))
+        assert (x[3] is None) == (y[3] is None) and (x[3] is None or np.array_equal(x[3], y[3]))
+        if isinstance(x[4], np.ndarray) or isinstance(y[4], np.ndarray):
+            assert np.array_equal(np.asarray(x[4], bool), np.asarray(y[4], bool))
+        else:
+            assert x[4] == y[4]
+
+
+def test_oracle_reader_concatenates_nested_columns_like_arrow():
+    pa = pytest.importorskip("pyarrow")
+    from oracle import ipc_read as R
+    schema, _ = _all_shapes(0, nb=1, rows=10)
+    outs = [O.run_oracle(schema, _all_shapes(100 + s, nb=2, rows=400)[1], 5, [0], buffer_size=128)
+            for s in range(3)]
+    sch = O.to_pyarrow_schema(schema)
+    head = sch.serialize().to_pybytes()
+    for p in range(5):
+        streams = [o.partition_bytes(p) for o in outs]
+        got = R.read_partition_nodes(schema, streams)
+        bs = [b for s in streams if s for b in pa.ipc.open_stream(head + s)]
+        t = pa.Table.from_batches(bs, schema=sch).combine_chunks()
+        for fi in range(len(schema)):
+            col = t.column(fi).chunks[0] if t.num_rows else pa.array([], sch.field(fi).type)
+            _same_nodes(got[fi], _arrow_nodes(pa, col))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("codec", [None, "lz4"])
+def test_gpu_reader_nested_columns(codec):
+    from gazelle_plugin_gb300 import shuffle as S
+    from oracle import ipc_read as R
+    P = 9
+    outs = []
+    for seed in (111, 112, 113):
+        schema, batches = _all_shapes(seed, nb=2, rows=1500)
+        kw = {"codec": codec} if codec else {}
+        res, data = S.split_batches(schema, batches, P, [0], writeSchema=bool(seed % 2), **kw)
+        st = np.concatenate([[0], np.cumsum(np.asarray(res.partitionLengths))])
+        outs.append([data[st[p]:st[p + 1]] for p in range(P)])
+    for p in range(P):
+        streams = [o[p] for o in outs]
+        want = R.read_partition_nodes(schema, streams)
+        r = S.PartitionReader(list(schema))
+        for s in streams:
+            r.addStream(s)
+        r.finish()
+        for fi in range(len(schema)):
+            assert r.node_count(fi) == len(want[fi])
+            for q, (length, nulls, valid, offs, vals) in enumerate(want[fi]):
+                gl, gn, gv, go, gvals = r.node_to_host(fi, q)
+                assert (gl, gn) == (length, nulls), (p, fi, q)
+                assert (gv is None) == (valid is None)
+                if valid is not None:
+                    assert gv.tobytes() == R.pack_bits(valid)
+                assert (go is None) == (offs is None)
+                if offs is not None:
+                    assert np.array_equal(go, offs)
+                want_vals = R.pack_bits(vals) if isinstance(vals, np.ndarray) else vals
+                assert gvals.tobytes() == want_vals, (p, fi, q)
+        r.close()
