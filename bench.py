@@ -488,11 +488,12 @@ def run_batched(seed: int = 3, n_batches: int = 512, window: int = 64, tune_batc
     """Config 4: 512 uneven batches, each task = (schema, partitions).  plain = the drop-in as it
     ships: one split call per batch with the default options (deferred passes, no wait per
     call); batched = the stream cut into windows of `window` batches, all tasks' batches of a
-    window handed over in one splitGroup call (every task's host reads in flight together), and
+    window handed over in one splitGroup call (every task's host reads in flight together),
     each task's batches fused into device passes
     whose size (and segment length) the autotuner chose for the task's schema from its first
-    `tune_batches` batches (outside the timed region).  Both run until every task's device work
-    is done; the tasks' passes overlap on the GPU in both."""
+    `tune_batches` batches (outside the timed region), and one syncGroup at the end (every
+    task's last pass queued before any task is waited for; plain: one sync per task).  Both run
+    until every task's device work is done; the tasks' passes overlap on the GPU in both."""
     from gazelle_plugin_gb300 import shuffle as S
     from gazelle_plugin_gb300 import workloads as W
     pool = _mixed_pool(seed)
@@ -537,8 +538,11 @@ def run_batched(seed: int = 3, n_batches: int = 512, window: int = 64, tune_batc
                 w.splitGroup([hs[k] for k in keys], [[calls[i][2].num_rows for i in groups[k]] for k in keys],
                              [np.stack([bufs[i][0] for i in groups[k]]) for k in keys],
                              [np.stack([bufs[i][1] for i in groups[k]]) for k in keys])
-        for h in hs.values():
-            w.sync(h)
+        if plain:
+            for h in hs.values():
+                w.sync(h)
+        else:  # every task's last pass queued before any is waited for
+            w.syncGroup(list(hs.values()))
         dt = time.perf_counter() - t0
         out = 0
         for (si, P), h in hs.items():
@@ -547,12 +551,20 @@ def run_batched(seed: int = 3, n_batches: int = 512, window: int = 64, tune_batc
         return dt, out
 
     one(False)  # warm-up (allocations, pinned pools)
-    dt_p, out = one(True)
-    dt_b, _ = one(False)
+    # each arm 3 times, alternating; the median of each (a timed region is ~10-25 ms)
+    runs_p, runs_b = [], []
+    for _ in range(3):
+        dt_p, out = one(True)
+        runs_p.append(dt_p)
+        runs_b.append(one(False)[0])
+    dt_p, dt_b = float(np.median(runs_p)), float(np.median(runs_b))
     alg = in_bytes + out
     return {"workload": f"{n_batches} batches, rows log-uniform 1k-64k, 3 schemas x P in {{64,200,1024}}",
             "window_batches": window, "autotuned": tuned, "input_bytes": in_bytes, "partition_bytes": out,
-            "plain_gbs": alg / dt_p / 1e9, "batched_gbs": alg / dt_b / 1e9, "speedup": dt_p / dt_b}
+            "plain_gbs": alg / dt_p / 1e9, "batched_gbs": alg / dt_b / 1e9, "speedup": dt_p / dt_b,
+            "runs": "median of 3 alternating runs per arm",
+            "plain_gbs_runs": [round(alg / t / 1e9, 1) for t in runs_p],
+            "batched_gbs_runs": [round(alg / t / 1e9, 1) for t in runs_b]}
 
 
 def run_fanout(distinct: int = 256, reps: int = 12, rows: int = 32768):

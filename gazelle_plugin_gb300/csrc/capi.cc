@@ -285,6 +285,31 @@ GzStatus gz_split_split_group(int32_t n_tasks, const int64_t* handles, const int
   return st.code;
 }
 
+GzStatus gz_split_sync_group(int32_t n_tasks, const int64_t* handles) {
+  if (n_tasks < 0 || (n_tasks > 0 && !handles)) {
+    t_make_error = "gz_split_sync_group: null argument";
+    return GZ_INVALID;
+  }
+  std::vector<std::shared_ptr<Entry>> es;
+  std::vector<gz::Splitter*> ts;
+  for (int i = 0; i < n_tasks; i++) {
+    auto e = Lookup(handles[i]);
+    if (!e) {
+      t_make_error = "Invalid splitter id " + std::to_string(handles[i]);
+      return GZ_INVALID;
+    }
+    es.push_back(e);
+    ts.push_back(e->splitter.get());
+  }
+  int failed = -1;
+  gz::Status st = gz::SyncGroup(ts, &failed);
+  if (!st.ok()) {
+    if (failed >= 0) es[failed]->last_error = st.msg;
+    t_make_error = "task " + std::to_string(failed) + ": " + st.msg;
+  }
+  return st.code;
+}
+
 GzStatus gz_split_sync(int64_t handle) {
   auto e = Lookup(handle);
   if (!e) return GZ_INVALID;

@@ -2305,6 +2305,26 @@ Status Splitter::Sync() {
   return SyncAndCheck();
 }
 
+Status SyncGroup(const std::vector<Splitter*>& tasks, int* failed) {
+  // every task's last pass is queued before any task is waited for, so their tails overlap
+  for (size_t i = 0; i < tasks.size(); i++) {
+    Status st = tasks[i]->Cuda(cudaSetDevice(tasks[i]->device_), "cudaSetDevice");
+    if (st.ok()) st = tasks[i]->Drain();
+    if (!st.ok()) {
+      *failed = (int)i;
+      return st;
+    }
+  }
+  for (size_t i = 0; i < tasks.size(); i++) {
+    Status st = tasks[i]->SyncAndCheck();
+    if (!st.ok()) {
+      *failed = (int)i;
+      return st;
+    }
+  }
+  return Status::OK();
+}
+
 Status Splitter::KernelTimes(double* out4) {
   Status st = SyncAndCheck();
   if (!st.ok()) return st;

@@ -44,6 +44,8 @@ struct Status {
 int NestedBufferCount(const Field& f);
 
 class Splitter {
+  friend Status SyncGroup(const std::vector<Splitter*>& tasks, int* failed);
+
  public:
   static Status Make(const std::string& short_name, std::vector<Field> fields, int32_t P,
                      std::vector<int32_t> keys, const GzSplitOptions& opts,
@@ -403,5 +405,7 @@ class Splitter {
 // before any is waited for.  *failed: the first task whose call failed.
 Status SplitGroup(const std::vector<Splitter*>& tasks, const int32_t* n_batches, const int32_t* rows,
                   const int64_t* addrs, const int64_t* sizes, const int32_t* n_bufs, int* failed);
+// Sync of several tasks: every task's pending pass is queued before any is waited for.
+Status SyncGroup(const std::vector<Splitter*>& tasks, int* failed);
 
 }  // namespace gz

@@ -114,6 +114,8 @@ def lib() -> ctypes.CDLL:
                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         L.gz_split_sync.restype = ctypes.c_int
         L.gz_split_sync.argtypes = [ctypes.c_int64]
+        L.gz_split_sync_group.restype = ctypes.c_int
+        L.gz_split_sync_group.argtypes = [ctypes.c_int32, ctypes.c_void_p]
         L.gz_split_stop.restype = ctypes.c_int
         L.gz_split_stop.argtypes = [ctypes.c_int64, ctypes.POINTER(GzSplitResult)]
         L.gz_split_data.restype = ctypes.c_int
@@ -510,6 +512,11 @@ class ShuffleSplitterJniWrapper:
 
     def sync(self, splitterId: int) -> None:
         _check(lib().gz_split_sync(splitterId), splitterId)
+
+    def syncGroup(self, splitterIds) -> None:
+        """sync of several tasks, every task's pending pass queued before any is waited for."""
+        h = np.ascontiguousarray(splitterIds, dtype=np.int64)
+        _check(lib().gz_split_sync_group(len(h), h.ctypes.data))
 
     def setSpinLimit(self, splitterId: int, polls: int) -> None:
         """Test hook: polls of k_scatter's bounded waits in later passes (0: the default)."""

@@ -195,6 +195,9 @@ GzStatus gz_split_split_group(int32_t n_tasks, const int64_t* handles, const int
  * this handle: afterwards every split batch is in its partition buffers, as after a
  * reference Split call returns.  No reference counterpart (reference Split is synchronous). */
 GzStatus gz_split_sync(int64_t handle);
+/* gz_split_sync of several tasks: every task's pending device pass is queued before any task is
+ * waited for (their last passes and copies back overlap). */
+GzStatus gz_split_sync_group(int32_t n_tasks, const int64_t* handles);
 
 /* Replaces ShuffleSplitterJniWrapper.stop (jni_wrapper.cc:1197-1227): emits every pending
  * partition buffer, writes the data file (or keeps it in memory) and fills `out`. */

@@ -409,7 +409,8 @@ def test_utf8_hash_keys_vs_oracle(seed):
 @pytest.mark.gpu
 def test_split_group_of_tasks_equals_per_task_calls():
     """gz_split_split_group: batches of three tasks (three schemas, three partition counts) in one
-    call per window give each task the bytes of splitting its own batches one by one (oracle)."""
+    call per window, then one gz_split_sync_group, give each task the bytes of splitting its own
+    batches one by one (oracle)."""
     rng = np.random.default_rng(5)
     specs = [(W.C1_SCHEMA, W.C1_KEYS, 8), (W.C2_SCHEMA, W.C2_KEYS, 200), (W.C4_SCHEMA_3, W.C4_KEYS_3, 64)]
     batches = [[W.c4_batch(rng, si, int(rng.integers(500, 9000))) for _ in range(7)] for si in range(3)]
@@ -421,7 +422,9 @@ def test_split_group_of_tasks_equals_per_task_calls():
         w.splitGroup(hs, [[b.num_rows for b in x] for x in win],
                      [np.stack([b.addrs_sizes()[0] for b in x]) for x in win],
                      [np.stack([b.addrs_sizes()[1] for b in x]) for x in win])
+    w.syncGroup(hs)  # every task's last pass queued, then waited for
     for (sch, keys, P), h, bs in zip(specs, hs, batches):
+        assert w.stats(h)[0] >= 1
         w.stop(h, P)
         assert w.data(h) == O.run_oracle(sch, bs, P, keys).data
         w.close(h)
