@@ -976,17 +976,19 @@ __device__ __forceinline__ void copy_string_smem(uint8_t* dst, uint32_t src, uin
 constexpr int kRowsPerThread = kTileRows / kScatterThreads;
 static_assert(kRowsPerThread * kScatterThreads == kTileRows, "tile rows per thread");
 
+// One fixed-width column of the tile: value of source row sr[u] to destination row dr[u] (the
+// thread's sorted positions, held in registers for every column of the tile).
 template <typename V>
-__device__ __forceinline__ void gather_rows(V* out, const V* src, const uint16_t* ps,
-                                            const uint32_t* dstrow, int n) {
+__device__ __forceinline__ void gather_rows(V* out, const V* src, const uint32_t* sr,
+                                            const uint32_t* dr, int n) {
   V v[kRowsPerThread];
   uint32_t d[kRowsPerThread];
 #pragma unroll
   for (int u = 0; u < kRowsPerThread; u++) {
     const int j = threadIdx.x + u * kScatterThreads;
     if (j < n) {
-      d[u] = dstrow[j];
-      v[u] = src[ps[j]];
+      d[u] = dr[u];
+      v[u] = src[sr[u]];
     }
   }
 #pragma unroll
@@ -1340,6 +1342,14 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
   // barrier (a binary column's skip decision is taken after its first barrier, so it is the same
   // in all threads).
   int nbin = 0;  // binary columns done (the parity of their warp-total buffer)
+  // this thread's sorted positions: source row and destination row, held for every column
+  uint32_t r_ps[kRowsPerThread], r_d[kRowsPerThread];
+#pragma unroll
+  for (int u = 0; u < kRowsPerThread; u++) {
+    const int j = threadIdx.x + u * kConsumers;
+    r_ps[u] = j < n ? ps[j] : 0u;
+    r_d[u] = j < n ? dstrow[j] : 0u;
+  }
   for (int i = 0; i < A; i++) {
     const uint4 ct = s_ct[i];
     const int a = (int)ct.w;
@@ -1363,13 +1373,13 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
         const int w = (int)((ct.z >> 8) & 255u);
         uint8_t* out = fd.out_values[a];
         if (w == 8) {
-          gather_rows(reinterpret_cast<uint64_t*>(out), reinterpret_cast<const uint64_t*>(stg), ps, dstrow, n);
+          gather_rows(reinterpret_cast<uint64_t*>(out), reinterpret_cast<const uint64_t*>(stg), r_ps, r_d, n);
         } else if (w == 4) {
-          gather_rows(reinterpret_cast<uint32_t*>(out), reinterpret_cast<const uint32_t*>(stg), ps, dstrow, n);
+          gather_rows(reinterpret_cast<uint32_t*>(out), reinterpret_cast<const uint32_t*>(stg), r_ps, r_d, n);
         } else if (w == 2) {
-          gather_rows(reinterpret_cast<uint16_t*>(out), reinterpret_cast<const uint16_t*>(stg), ps, dstrow, n);
+          gather_rows(reinterpret_cast<uint16_t*>(out), reinterpret_cast<const uint16_t*>(stg), r_ps, r_d, n);
         } else if (w == 1) {
-          gather_rows(out, stg, ps, dstrow, n);
+          gather_rows(out, stg, r_ps, r_d, n);
         } else {  // 16-byte values are gathered straight from global memory
           const uint4* src = reinterpret_cast<const uint4*>(s_col[a].values) + row0;
           for (int j = threadIdx.x; j < n; j += kConsumers) reinterpret_cast<uint4*>(out)[dstrow[j]] = src[ps[j]];
@@ -1398,7 +1408,7 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
           len[u] = 0;
           so[u] = 0;
           if (j < n) {
-            const int r = ps[j];
+            const int r = (int)r_ps[u];
             if (off64) {
               so[u] = (uint32_t)oin64[r];
               len[u] = (uint32_t)oin64[r + 1] - so[u];
@@ -1497,13 +1507,13 @@ __global__ void __launch_bounds__(kScatterBlock, 2) k_scatter(const SchemaDesc s
               if (j < n) {
                 const int p = ks[j];
                 const uint32_t rel = pre[u] - blk - wexP[bb * 256 + p];  // bytes of the run before row j
-                d[u] = dstrow[j];
+                d[u] = r_d[u];
                 v[u] = baseP[bb * 512 + p] + rel + len[u];
                 cd[u] = baseP[bb * 512 + 256 + p] + rel;
               }
             } else if (j < n) {
               const int q = rs[j];
-              d[u] = dstrow[j];
+              d[u] = r_d[u];
               v[u] = rt0[q] + pre[u] + len[u];
               cd[u] = rt1[q] + pre[u];
             }
