@@ -161,6 +161,27 @@ def test_gpu_nested_columns_vs_oracle(P):
 
 
 @pytest.mark.gpu
+def test_gpu_nested_columns_cpu_copy_staging_many_passes():
+    """Host inputs copied by the CPU into pinned staging (GZ_HOST_READ_CPU_COPY) instead of read by
+    the device, over many passes, through the batched call."""
+    from gazelle_plugin_gb300 import shuffle as S
+    schema, batches = _all_shapes(95, nb=6)
+    w = S.ShuffleSplitterJniWrapper()
+    h = w.make(S.NativePartitioning("hash", 33, None, [0], list(schema)), writeSchema=False,
+               host_read=S.GZ_HOST_READ_CPU_COPY, flush_bytes=1 << 18)
+    for b in batches:
+        a, z = b.addrs_sizes()
+        w.splitBatches(h, [b.num_rows], a[None, :], z[None, :])
+    assert w.stats(h)[0] >= 3
+    res = w.stop(h)
+    data = w.data(h)
+    w.close(h)
+    ref = O.run_oracle(schema, batches, 33, [0])
+    assert data == ref.data
+    assert np.array_equal(res.rawPartitionLengths, ref.raw_partition_lengths)
+
+
+@pytest.mark.gpu
 def test_gpu_nested_columns_device_resident_many_passes():
     torch = pytest.importorskip("torch")
     from gazelle_plugin_gb300 import shuffle as S
