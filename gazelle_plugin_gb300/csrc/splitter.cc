@@ -335,6 +335,8 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
   for (int i = 0; i < 2; i++) {
     st = Cuda(cudaEventCreateWithFlags(&stage_ev_[i], cudaEventDisableTiming), "cudaEventCreate");
     if (!st.ok()) return st;
+  }
+  for (int i = 0; i < kTabBufs; i++) {
     st = Cuda(cudaEventCreateWithFlags(&tab_ev_[i], cudaEventDisableTiming), "cudaEventCreate");
     if (!st.ok()) return st;
   }
@@ -362,7 +364,7 @@ Splitter::~Splitter() {
   }
   ReleaseHost();
   for (auto& c : meta_chunks_) PinnedRelease(c);
-  for (int i = 0; i < 2; i++) {
+  for (int i = 0; i < kTabBufs; i++) {
     PinnedRelease(PinnedBlock{h_tables_[i], tables_cap_[i]});
     if (tab_ev_[i]) cudaEventDestroy(tab_ev_[i]);
   }
@@ -1125,7 +1127,7 @@ Status Splitter::Flush() {
     dtab = d_stage_[cur_] + used_;
     used_ += tb_total;
   } else {
-    // two pinned table buffers; wait only for the copy that last used this one
+    // a ring of pinned table buffers; wait only for the copy that last used this one
     const int ti = tab_cur_;
     if (tab_busy_[ti]) {
       st = Cuda(cudaEventSynchronize(tab_ev_[ti]), "table wait");
@@ -1184,7 +1186,7 @@ Status Splitter::Flush() {
     st = Cuda(cudaEventRecord(tab_ev_[tab_cur_], stream_), "event");
     if (!st.ok()) return st;
     tab_busy_[tab_cur_] = true;
-    tab_cur_ ^= 1;
+    tab_cur_ = (tab_cur_ + 1) % kTabBufs;
   }
   fd.batches = reinterpret_cast<const BatchDesc*>(dtab);
   fd.segs = reinterpret_cast<const SegDesc*>(dtab + tb_batches);

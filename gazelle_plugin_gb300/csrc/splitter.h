@@ -359,10 +359,13 @@ class Splitter {
   bool stage_busy_[2] = {false, false};
   int cur_ = 0;
   size_t used_ = 0;
-  uint8_t* h_tables_[2] = {nullptr, nullptr};  // pinned tables for device-retained inputs
-  size_t tables_cap_[2] = {0, 0};
-  cudaEvent_t tab_ev_[2] = {nullptr, nullptr};
-  bool tab_busy_[2] = {false, false};
+  // pinned pass tables (device-retained and device-read host inputs): a ring, so that reusing a
+  // buffer waits for a table copy kTabBufs passes back, which stream_ has long passed
+  static constexpr int kTabBufs = 8;
+  uint8_t* h_tables_[kTabBufs] = {};
+  size_t tables_cap_[kTabBufs] = {};
+  cudaEvent_t tab_ev_[kTabBufs] = {};
+  bool tab_busy_[kTabBufs] = {};
   int tab_cur_ = 0;
   std::vector<PinnedBlock> meta_chunks_;
   std::vector<PinnedBlock> host_chunks_;  // pinned host partition data of moved passes
