@@ -101,7 +101,7 @@ Status Splitter::PlanNested() {
     PlanNode(np, fields_[i], -1, &buf);
     for (const NestNode& nd : np.nodes) {
       const bool ok = nd.type == GZ_TYPE_STRUCT ? !nd.kids.empty()
-                      : ListLike(nd.type)      ? (nd.type == GZ_TYPE_MAP ? nd.kids.size() == 1 : nd.kids.size() == 1)
+                      : ListLike(nd.type)      ? nd.kids.size() == 1
                       : IsBinary(nd.type) || nd.type == GZ_TYPE_BOOL || nd.width > 0;
       if (!ok) return Status::Error(GZ_NOT_IMPLEMENTED, "nested field type not implemented in ColumnarShuffle");
       if (nd.type == GZ_TYPE_MAP) {

@@ -368,6 +368,29 @@ def nested_column(rng, field: Field, n: int, null_frac: float = 0.1, max_len: in
     return [vbuf, v.view(np.uint8)]
 
 
+NESTED_LEAVES = ["int8", "int16", "int32", "int64", "float32", "float64", "date32", "decimal128",
+                 "timestamp", "bool", "utf8", "binary", "large_utf8"]
+
+
+def random_nested_field(rng, name: str, depth: int = 0) -> Field:
+    """A random nested field: list / large_list / map / struct down to depth 3 over NESTED_LEAVES
+    (map keys: int32 or utf8, not nullable)."""
+    kind = str(rng.choice(["list", "large_list", "map", "struct"]))
+
+    def child(nm):
+        if depth >= 2 or rng.random() < 0.45:
+            return Field(nm, str(rng.choice(NESTED_LEAVES)), bool(rng.random() < 0.8))
+        return random_nested_field(rng, nm, depth + 1)
+
+    if kind == "struct":
+        kids = tuple(child(f"s{i}") for i in range(int(rng.integers(1, 4))))
+    elif kind == "map":
+        kids = (Field("key", str(rng.choice(["int32", "utf8"])), False), child("value"))
+    else:
+        kids = (child("item"),)
+    return Field(name, kind, bool(rng.random() < 0.8), None, kids)
+
+
 def c4_rows(rng, size=None):
     """Batch rows log-uniform over [1000, 65536]."""
     return np.exp(rng.uniform(np.log(1000), np.log(65536), size=size)).astype(np.int64)

@@ -36,6 +36,35 @@ def test_oracle_matches_reference_nested_columns(case):
     assert hashlib.sha256(out.data).hexdigest() == case["data_sha256"]
 
 
+def _random_case(seed, nb=3, rows=600):
+    """An int key and 1-3 random nested fields (random_nested_field), batches of random length."""
+    rng = np.random.default_rng(seed)
+    schema = [W.Field("k", "int64", False)] + [W.random_nested_field(rng, f"N{i}")
+                                                 for i in range(int(rng.integers(1, 4)))]
+    spans = bool(rng.random() < 0.5)
+    batches = []
+    for _ in range(nb):
+        n = int(rng.integers(1, rows))
+        bufs = W._column(rng, schema[0], n, rng.integers(0, 1 << 40, size=n), 0.0)
+        for f in schema[1:]:
+            bufs += W.nested_column(rng, f, n, float(rng.choice([0.0, 0.1, 0.5])), int(rng.choice([1, 3, 6])),
+                                    True, spans)
+        batches.append(W.Batch(n, bufs))
+    return schema, batches
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_oracle_matches_live_reference_on_random_nested_schemas(seed):
+    if not O.RefSplitter.available():
+        pytest.skip("reference build not available")
+    schema, batches = _random_case(7000 + seed)
+    P = [1, 5, 64][seed % 3]
+    a = O.run_oracle(schema, batches, P, [0], buffer_size=[16, 100, 4096][seed % 3])
+    b = O.run_ref(schema, batches, P, [0], buffer_size=[16, 100, 4096][seed % 3])
+    assert a.data == b.data
+    assert list(a.raw_partition_lengths) == list(b.raw_partition_lengths)
+
+
 def _arrow_array(pa, f, t, bufs, at, n):
     """The Arrow array of field f (type t) from the flat buffer list at `at`; returns it and the
     next buffer index."""
@@ -157,6 +186,19 @@ def test_gpu_nested_columns_vs_oracle(P):
     ref = O.run_oracle(schema, batches, P, [0])
     assert data == ref.data
     assert np.array_equal(res.partitionLengths, ref.partition_lengths)
+    assert np.array_equal(res.rawPartitionLengths, ref.raw_partition_lengths)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", range(12))
+def test_gpu_random_nested_schemas_vs_oracle(seed):
+    from gazelle_plugin_gb300 import shuffle as S
+    schema, batches = _random_case(7000 + seed)
+    P = [1, 5, 64][seed % 3]
+    bs = [16, 100, 4096][seed % 3]
+    res, data = S.split_batches(schema, batches, P, [0], writeSchema=False, bufferSize=bs)
+    ref = O.run_oracle(schema, batches, P, [0], buffer_size=bs)
+    assert data == ref.data
     assert np.array_equal(res.rawPartitionLengths, ref.raw_partition_lengths)
 
 
