@@ -203,6 +203,47 @@ def test_gpu_random_nested_schemas_vs_oracle(seed):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("null_frac,max_len", [(1.0, 3), (0.0, 0), (0.5, 0), (1.0, 0)])
+def test_gpu_nested_columns_all_null_and_empty(null_frac, max_len):
+    """Columns whose entries are all null, or whose lists / maps / strings are all empty (empty
+    child buffers), single-row batches among them."""
+    from gazelle_plugin_gb300 import shuffle as S
+    rng = np.random.default_rng(int(null_frac * 10) + max_len)
+    schema = [W.Field("k", "int64", False)] + [G.NESTED_SHAPES[i](f"N{i}") for i in range(len(G.NESTED_SHAPES))]
+    batches = []
+    for n in (1, 700, 1, 2500):
+        bufs = W._column(rng, schema[0], n, rng.integers(0, 1 << 40, size=n), 0.0)
+        for f in schema[1:]:
+            bufs += W.nested_column(rng, f, n, null_frac, max_len)
+        batches.append(W.Batch(n, bufs))
+    res, data = S.split_batches(schema, batches, 13, [0], writeSchema=False)
+    ref = O.run_oracle(schema, batches, 13, [0])
+    assert data == ref.data
+    assert np.array_equal(res.rawPartitionLengths, ref.raw_partition_lengths)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("short_name", ["rr", "single", "range"])
+def test_gpu_nested_columns_other_partitioners(short_name):
+    """Round-robin, single and range (int32 partition ids in field 0, not written out) with nested
+    columns beside them."""
+    from gazelle_plugin_gb300 import shuffle as S
+    schema, batches = _all_shapes(121, nb=3, rows=2000)
+    P = 9
+    if short_name == "range":
+        rng = np.random.default_rng(5)
+        schema = [W.Field("pid", "int32", False)] + schema
+        batches = [W.Batch(b.num_rows, [np.zeros(0, np.uint8),
+                                        rng.integers(0, P, size=b.num_rows).astype(np.int32).view(np.uint8)]
+                           + b.buffers) for b in batches]
+    keys = [0] if short_name == "range" else []
+    res, data = S.split_batches(schema, batches, P, keys, shortName=short_name, writeSchema=False)
+    ref = O.run_oracle(schema, batches, P, keys, short_name=short_name)
+    assert data == ref.data
+    assert np.array_equal(res.rawPartitionLengths, ref.raw_partition_lengths)
+
+
+@pytest.mark.gpu
 def test_gpu_nested_columns_cpu_copy_staging_many_passes():
     """Host inputs copied by the CPU into pinned staging (GZ_HOST_READ_CPU_COPY) instead of read by
     the device, over many passes, through the batched call."""
