@@ -4,11 +4,17 @@
 // The reference compresses each body buffer of an emitted record batch with Arrow's
 // Lz4FrameCodec (splitter.cc:311-327, 586-600) through the LZ4 library on one CPU core; the
 // buffer is written as an int64 uncompressed length followed by one LZ4 frame.  Here the
-// buffers are cut into chunks of at most 64 KiB, each compressed by one warp into one LZ4 block
-// (greedy single-candidate matching, hash table in shared memory), and the host strings the
-// blocks of a buffer into a frame (independent blocks, 64 KiB maximum block size, no
-// checksums).  The output is a valid frame for any LZ4 frame decoder; it is not the same byte
-// string the LZ4 library would produce (the codec's output is not unique).
+// buffers are cut into chunks of at most 8 KiB, each staged in shared memory and compressed by
+// one warp into one LZ4 block (greedy single-candidate matching, hash table in shared memory:
+// every read of the match search is a shared-memory read; 12 KiB of shared memory per warp, 16
+// warps per SM), and the host strings the blocks of a buffer into a frame (independent blocks,
+// 64 KiB maximum block size in the descriptor, no checksums).  The search is bound by its
+// dependent instruction chains, so its speed follows the warps per SM and the latency of its
+// reads: against 64 KiB blocks searched in global memory, the Stop compression of the wide
+// fact-table bodies runs 2.1x faster, for 1.9% more output (an 8 KiB history); 16 KiB blocks (8
+// warps per SM) were 1.0x, 8 KiB blocks with a 4096-entry table (12 warps) 1.5x.  The output is
+// a valid frame for any LZ4 frame decoder; it is not the same byte string the LZ4 library would
+// produce (the codec's output is not unique).
 //
 // Formats (published LZ4 block / frame descriptions):
 //   block    sequences of [token: literal length << 4 | match length - 4][literal length
@@ -28,7 +34,10 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kWarps = 4;  // warps per CTA
-constexpr int kHashLog = 12;
+constexpr int kHashLog = 11;
+constexpr int kCWarps = 2;                       // warps per CTA of the compressor
+constexpr uint32_t kStage = kLz4MaxBlock + 16;   // a warp's staged chunk (and a zero-padded word)
+constexpr size_t kCompressSmem = (size_t)kCWarps * (kStage + (2u << kHashLog));
 constexpr uint16_t kEmpty = 0xffff;  // no position (position 65535 never starts a match)
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31; }
@@ -60,7 +69,7 @@ __device__ uint32_t emit(uint8_t* dst, uint32_t o, const uint8_t* src, uint32_t 
   const uint32_t nl = ext_bytes(lit);
   put_ext(dst + o + 1, lit, nl);
   o += 1 + nl;
-  for (uint32_t i = lane_id(); i < lit; i += 32) dst[o + i] = __ldg(src + anchor + i);
+  for (uint32_t i = lane_id(); i < lit; i += 32) dst[o + i] = src[anchor + i];
   o += lit;
   if (off) {
     if (lane_id() == 0) {
@@ -79,10 +88,15 @@ __device__ uint32_t emit(uint8_t* dst, uint32_t o, const uint8_t* src, uint32_t 
 // looks up the last earlier position with that hash; the first lane whose candidate matches
 // starts the match, which the warp then extends 32 bytes at a time.  Table entries come only from
 // earlier windows (inserted after the lookups), so a candidate always precedes its position.
+// Little-endian 4 bytes at position q of a staged (word-aligned, shared-memory) chunk.
+__device__ __forceinline__ uint32_t read32_s(const uint32_t* sw, uint32_t q) {
+  const uint32_t w0 = sw[q >> 2];
+  return (q & 3) == 0 ? w0 : __funnelshift_r(w0, sw[(q >> 2) + 1], (q & 3) * 8);
+}
+
 __device__ uint32_t compress_block(const uint8_t* src, uint32_t n, uint16_t* table, uint8_t* dst) {
   const uint32_t lane = lane_id();
-  const uint32_t* base = reinterpret_cast<const uint32_t*>(reinterpret_cast<uintptr_t>(src) & ~uintptr_t(3));
-  const uint32_t sh0 = (uint32_t)(reinterpret_cast<uintptr_t>(src) & 3);
+  const uint32_t* sw = reinterpret_cast<const uint32_t*>(src);  // the staged chunk (word aligned)
   uint32_t o = 0, anchor = 0, p = 0;
   uint32_t misses = 0;  // windows in a row without a match
   if (n >= 13) {
@@ -93,11 +107,11 @@ __device__ uint32_t compress_block(const uint8_t* src, uint32_t n, uint16_t* tab
       const bool valid = q + 12 <= n;
       uint32_t v = 0, h = 0, cand = kEmpty;
       if (valid) {
-        v = read32(base, sh0, q);
+        v = read32_s(sw, q);
         h = hash4(v);
         cand = table[h];
       }
-      const bool ok = valid && cand != kEmpty && cand < q && read32(base, sh0, cand) == v;
+      const bool ok = valid && cand != kEmpty && cand < q && read32_s(sw, cand) == v;
       const unsigned m = __ballot_sync(kFull, ok);
       __syncwarp();
       if (m == 0) {
@@ -119,7 +133,7 @@ __device__ uint32_t compress_block(const uint8_t* src, uint32_t n, uint16_t* tab
       uint32_t len = 4;
       for (;;) {  // the match may end at n - 5 at the latest
         const uint32_t a = mq + len + lane;
-        const bool eq = a + 5 < n && __ldg(src + a) == __ldg(src + mc + len + lane);
+        const bool eq = a + 5 < n && src[a] == src[mc + len + lane];
         const unsigned ne = __ballot_sync(kFull, !eq);
         if (ne == 0) {
           len += 32;
@@ -137,13 +151,15 @@ __device__ uint32_t compress_block(const uint8_t* src, uint32_t n, uint16_t* tab
   return o;
 }
 
-__global__ void __launch_bounds__(kWarps * 32)
+__global__ void __launch_bounds__(kCWarps * 32, 8)
 k_lz4_compress(const Lz4Chunk* __restrict__ chunks, uint32_t n_chunks, uint32_t* next, uint8_t* scratch,
                uint8_t* out, unsigned long long* out_used, unsigned long long out_cap, Lz4Block* res,
                int32_t* err) {
-  __shared__ uint16_t tables[kWarps][1 << kHashLog];
+  extern __shared__ __align__(16) uint8_t csm[];
   const uint32_t warp = threadIdx.x >> 5;
-  uint8_t* slot = scratch + (size_t)(blockIdx.x * kWarps + warp) * kLz4Slot;
+  uint8_t* sbuf = csm + (size_t)warp * (kStage + (2u << kHashLog));
+  uint16_t* table = reinterpret_cast<uint16_t*>(sbuf + kStage);
+  uint8_t* slot = scratch + (size_t)(blockIdx.x * kCWarps + warp) * kLz4Slot;
   for (;;) {
     uint32_t c = 0;
     if (lane_id() == 0) c = atomicAdd(next, 1u);
@@ -153,7 +169,19 @@ k_lz4_compress(const Lz4Chunk* __restrict__ chunks, uint32_t n_chunks, uint32_t*
     const uint32_t n = ch.raw || ch.len <= kLz4MaxBlock ? ch.len : 0;  // the host cuts blocks to 64 KiB
     uint32_t size = n;
     if (!ch.raw) {
-      size = compress_block(ch.src, n, tables[warp], slot);
+      // the chunk into this warp's shared buffer (then zeros up to two words past its end)
+      const uintptr_t a = reinterpret_cast<uintptr_t>(ch.src);
+      if ((a & 15) == 0) {
+        const uint32_t nv = n >> 4;
+        for (uint32_t i = lane_id(); i < nv; i += 32)
+          reinterpret_cast<uint4*>(sbuf)[i] = __ldg(reinterpret_cast<const uint4*>(ch.src) + i);
+        for (uint32_t i = (nv << 4) + lane_id(); i < n; i += 32) sbuf[i] = __ldg(ch.src + i);
+      } else {
+        for (uint32_t i = lane_id(); i < n; i += 32) sbuf[i] = __ldg(ch.src + i);
+      }
+      if (lane_id() < 8) sbuf[n + lane_id()] = 0;
+      __syncwarp();
+      size = compress_block(sbuf, n, table, slot);
       __syncwarp();
     }
     const bool stored = size >= n;  // a plain copy, or no gain: the block is stored as it is
@@ -342,14 +370,20 @@ int sm_count() {
 
 }  // namespace
 
-uint32_t lz4_compress_warps() { return (uint32_t)sm_count() * 8 * kWarps; }
+uint32_t lz4_compress_warps() { return (uint32_t)sm_count() * 8 * kCWarps; }
 
 cudaError_t launch_lz4_compress(const Lz4Chunk* chunks, uint32_t n_chunks, uint32_t* next, uint8_t* scratch,
                                 uint8_t* out, unsigned long long* out_used, unsigned long long out_cap,
                                 Lz4Block* res, int32_t* err, cudaStream_t st) {
   if (n_chunks == 0) return cudaSuccess;
-  const uint32_t grid = lz4_compress_warps() / kWarps;
-  k_lz4_compress<<<grid, kWarps * 32, 0, st>>>(chunks, n_chunks, next, scratch, out, out_used, out_cap, res, err);
+  const uint32_t grid = lz4_compress_warps() / kCWarps;
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_lz4_compress, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCompressSmem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  k_lz4_compress<<<grid, kCWarps * 32, kCompressSmem, st>>>(chunks, n_chunks, next, scratch, out, out_used, out_cap, res, err);
   return cudaGetLastError();
 }
 

@@ -5,7 +5,7 @@
 
 namespace gz {
 
-constexpr uint32_t kLz4MaxBlock = 65536;  // bytes of input per block (the frame's 64 KiB block size)
+constexpr uint32_t kLz4MaxBlock = 8192;  // bytes of input per block (at most the frame's 64 KiB block size)
 // worst-case compressed block (all literals: token, length bytes) rounded to 16 bytes
 constexpr uint32_t kLz4Slot = ((kLz4MaxBlock + kLz4MaxBlock / 255 + 16) + 15) & ~15u;
 

@@ -1948,7 +1948,7 @@ Status Splitter::CompressBodies(std::vector<std::vector<SegMsg>>* msgs_p) {
   const int64_t threshold = opts_.batch_compress_threshold;
   auto lz4 = [&](const SegMsg& m) { return codec_ == GZ_CODEC_LZ4_FRAME && (int64_t)m.rows > threshold; };
   // 1. the device work: every device-readable body range, cut into chunks (LZ4 blocks of at
-  //    most 64 KiB for compressed batches, plain copies of at most 1 MiB for the others)
+  //    most kLz4MaxBlock bytes for compressed batches, plain copies of at most 1 MiB for the others)
   constexpr uint32_t kCopyChunk = 1u << 20;
   std::vector<Lz4Chunk> chunks;
   std::vector<std::vector<uint32_t>> first(P_);  // first chunk of each message
