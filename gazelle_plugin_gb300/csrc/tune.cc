@@ -49,12 +49,22 @@ void LoadEnvOnce(Cache& c) {
 
 }  // namespace
 
+// A field's type: its code, then a list's element type or a nested field's children in brackets.
+static std::string TypeTag(const Field& f) {
+  std::string s = std::to_string(f.type);
+  if (f.type == GZ_TYPE_LIST && !f.nested()) return s + "[" + std::to_string(f.elem) + "]";
+  if (!f.nested()) return s;
+  s += "[";
+  for (size_t i = 0; i < f.children.size(); i++) s += (i ? "," : "") + TypeTag(f.children[i]);
+  return s + "]";
+}
+
 std::string SchemaSignature(const std::string& short_name, const std::vector<Field>& fields,
                             const std::vector<int32_t>& keys, int32_t P) {
   const bool hash = short_name == "hash";
   if (short_name == "single") P = 1;  // whatever count was asked for
   std::string s = hash ? "t=" : "m=" + short_name + ";t=";
-  for (size_t i = 0; i < fields.size(); i++) s += (i ? "," : "") + std::to_string(fields[i].type);
+  for (size_t i = 0; i < fields.size(); i++) s += (i ? "," : "") + TypeTag(fields[i]);
   s += ";k=";
   for (size_t i = 0; hash && i < keys.size(); i++) s += (i ? "," : "") + std::to_string(keys[i]);
   s += ";P=" + std::to_string(P);
