@@ -127,3 +127,26 @@ def test_task_larger_than_budget_is_rejected():
         assert e.value.status == S.GZ_INVALID
     finally:
         srv.shutdown()
+
+
+def test_served_nested_tasks_equal_alone():
+    """Tasks with nested columns (list / map / struct) beside flat ones through the serving loop."""
+    from tests.golden import make_golden as G
+    rng = np.random.default_rng(17)
+    tasks = []
+    for t in range(4):
+        schema = [W.Field("k", "int64", False), G.NESTED_SHAPES[(3 * t) % len(G.NESTED_SHAPES)]("a"),
+                  G.NESTED_SHAPES[(3 * t + 1) % len(G.NESTED_SHAPES)]("b")]
+        batches = []
+        for _ in range(5):
+            n = int(rng.integers(500, 4000))
+            bufs = W._column(rng, schema[0], n, rng.integers(0, 1 << 40, size=n), 0.0)
+            for f in schema[1:]:
+                bufs += W.nested_column(rng, f, n, 0.2, 4)
+            batches.append(W.Batch(n, bufs))
+        tasks.append((schema, [0], [16, 200][t % 2], batches))
+    served, _ = _served(tasks, slots=2)
+    for (schema, keys, P, batches), (res, data) in zip(tasks, served):
+        _, want = _alone(schema, keys, P, batches)
+        assert data == want
+        assert data == O.run_oracle(schema, batches, P, keys, buffer_size=4096).data
