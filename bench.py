@@ -242,35 +242,48 @@ def digests(paths):
         return list(ex.map(S.digest_file, paths))
 
 
-def read_back(sch, paths, lengths, partitions=None):
+def read_back(sch, paths, lengths, partitions=None, tasks: int = 1):
     """The reduce side: every partition's streams of all map outputs (the task files, memory
     mapped: page-cache bytes, as a shuffle fetch leaves them) read into device columns by the
-    CUDA reader, one partition at a time.  GB/s = (stream bytes + column bytes) / time."""
+    CUDA reader, one reader per partition, `tasks` reduce tasks at once (each on its own thread,
+    as an executor's task slots run them, taking the partitions in turn).
+    GB/s = (stream bytes + column bytes) / time."""
+    from concurrent.futures import ThreadPoolExecutor
     from gazelle_plugin_gb300 import shuffle as S
     maps = [np.memmap(p, dtype=np.uint8, mode="r") for p in paths]
     starts = [np.concatenate([[0], np.cumsum(l)]) for l in lengths]
     P = lengths[0].shape[0]
-    parts = range(P) if partitions is None else partitions
-    in_bytes = out_bytes = 0
+    parts = list(range(P) if partitions is None else partitions)
+
+    def task(ps):
+        ib = ob = 0
+        for p in ps:
+            r = S.PartitionReader(list(sch))
+            for m, st in zip(maps, starts):
+                if st[p + 1] > st[p]:
+                    r.addStream(m[st[p]:st[p + 1]])
+                    ib += int(st[p + 1] - st[p])
+            r.finish()
+            for f in range(len(sch)):
+                c = r.column(f)
+                ob += c.values_bytes + (c.length + 1) * 4 * (c.offsets is not None) + \
+                    ((c.length + 7) // 8 if c.validity else 0)
+            r.close()
+        return ib, ob
+
     t0 = time.perf_counter()
-    for p in parts:
-        r = S.PartitionReader(list(sch))
-        for m, st in zip(maps, starts):
-            if st[p + 1] > st[p]:
-                r.addStream(m[st[p]:st[p + 1]])
-                in_bytes += int(st[p + 1] - st[p])
-        rows, _ = r.finish()
-        for f in range(len(sch)):
-            c = r.column(f)
-            out_bytes += c.values_bytes + (c.length + 1) * 4 * (c.offsets is not None) + \
-                ((c.length + 7) // 8 if c.validity else 0)
-        r.close()
+    with ThreadPoolExecutor(max_workers=tasks) as ex:
+        done = list(ex.map(task, [parts[i::tasks] for i in range(tasks)]))
     dt = time.perf_counter() - t0
+    in_bytes = sum(d[0] for d in done)
+    out_bytes = sum(d[1] for d in done)
     del maps
     return {"value": (in_bytes + out_bytes) / dt / 1e9, "unit": "GB/s", "seconds": dt,
             "stream_bytes": in_bytes, "column_bytes": out_bytes, "partitions": len(parts),
+            "reduce_tasks": tasks,
             "what": ("each partition's streams of all map outputs (memory-mapped data files) into one "
-                     "set of device columns: host parse, one copy per stream, device concatenation")}
+                     "set of device columns (host parse, one copy per stream, device concatenation), "
+                     f"{tasks} reduce tasks at once")}
 
 
 def oracle_tasks(sch, keys, partitioner, rows, haddrs, sizes, n_tasks: int, ddir: str, digest: bool = False):
@@ -888,7 +901,7 @@ def run_gpu(args):
                 barrier()
             gpu_files = digests(task_files(ddir, tasks))
             gpu_lengths = runs[-1]["partition_lengths"]
-            read = None if args.no_read else read_back(sch, task_files(ddir, tasks), gpu_lengths)
+            read = None if args.no_read else read_back(sch, task_files(ddir, tasks), gpu_lengths, tasks=tasks)
             remove_dir(ddir)
             ddir = scratch_dir()
             one = S.run_map_tasks(part, rows, haddrs, sizes, 1, ddir, **e2e_opts)

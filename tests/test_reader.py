@@ -148,6 +148,28 @@ def test_gpu_reader_on_cuda_splitter_streams_of_many_map_outputs():
 
 
 @pytest.mark.gpu
+def test_gpu_readers_on_concurrent_threads():
+    """Eight reduce tasks at once, each on its own thread with its own readers (as the benchmark's
+    reduce side runs them): every partition equal to the oracle's reading."""
+    from concurrent.futures import ThreadPoolExecutor
+    from gazelle_plugin_gb300 import shuffle as S
+    P = 64
+    outs = []
+    for seed in (21, 22, 23):
+        res, data = S.split_batches(W.C2_SCHEMA, c2_make(seed), P, W.C2_KEYS, writeSchema=False)
+        starts = np.concatenate([[0], np.cumsum(np.asarray(res.partitionLengths))])
+        outs.append([data[starts[p]:starts[p + 1]] for p in range(P)])
+
+    def task(ps):
+        for p in ps:
+            _check(W.C2_SCHEMA, [o[p] for o in outs])
+        return len(ps)
+
+    with ThreadPoolExecutor(max_workers=8) as ex:
+        assert sum(ex.map(task, [list(range(P))[i::8] for i in range(8)])) == P
+
+
+@pytest.mark.gpu
 def test_gpu_reader_random_schemas_bool_and_empty_streams():
     rng = np.random.default_rng(12)
     for trial in range(6):
