@@ -288,7 +288,11 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
     if (!st.ok()) return st;
     st = Cuda(cudaStreamCreateWithPriority(&stream_, cudaStreamNonBlocking, least), "cudaStreamCreate");
     if (!st.ok()) return st;
+    st = Cuda(cudaStreamCreateWithPriority(&hstream_, cudaStreamNonBlocking, least), "cudaStreamCreate");
+    if (!st.ok()) return st;
   }
+  st = Cuda(cudaEventCreateWithFlags(&hwait_ev_, cudaEventDisableTiming), "cudaEventCreate");
+  if (!st.ok()) return st;
   st = Cuda(cudaStreamCreateWithFlags(&ostream_, cudaStreamNonBlocking), "cudaStreamCreate");
   if (!st.ok()) return st;
   st = Cuda(cudaEventCreateWithFlags(&gather_ev_, cudaEventDisableTiming), "cudaEventCreate");
@@ -354,6 +358,7 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
 
 Splitter::~Splitter() {
   if (cstream_) cudaStreamSynchronize(cstream_);
+  if (hstream_) cudaStreamSynchronize(hstream_);
   if (stream_) cudaStreamSynchronize(stream_);
   if (pstream_) cudaStreamSynchronize(pstream_);
   if (ostream_) cudaStreamSynchronize(ostream_);
@@ -385,6 +390,8 @@ Splitter::~Splitter() {
   PinnedRelease(PinnedBlock{reinterpret_cast<uint8_t*>(h_jobs_), h_jobs_bytes_});
   if (gather_ev_) cudaEventDestroy(gather_ev_);
   if (pstream_) cudaStreamDestroy(pstream_);
+  if (hstream_) cudaStreamDestroy(hstream_);
+  if (hwait_ev_) cudaEventDestroy(hwait_ev_);
   if (cstream_) cudaStreamDestroy(cstream_);
   if (ostream_) cudaStreamDestroy(ostream_);
   if (stream_) cudaStreamDestroy(stream_);
@@ -428,6 +435,8 @@ Status Splitter::EnsureStaging(size_t bytes) {
   Status st = LaunchPendingScatter();
   if (!st.ok()) return st;
   st = FinishHostReads();
+  if (!st.ok()) return st;
+  st = Cuda(cudaStreamSynchronize(hstream_), "sync");
   if (!st.ok()) return st;
   st = Cuda(cudaStreamSynchronize(stream_), "sync");
   if (!st.ok()) return st;
@@ -1063,11 +1072,15 @@ Status Splitter::Flush() {
   const size_t tb_total = tb_batches + tb_tiles + tb_cols + tb_tdesc + tb_jobs;
   const bool staged_tables = host_in && !direct_;  // tables travel with the pinned staging copy
   const size_t s_tab = staged_tables ? 0 : take(tb_total);
-  // this pass's scratch buffer: stream_ already runs this pass's work after the k_scatter that
-  // last read it (queued by the previous Flush)
+  // this pass's scratch buffer: stream_ already holds the k_scatter that last read it (queued by
+  // the previous Flush), and this pass's work on hstream_ starts after what stream_ holds now
   st = EnsureScratch(so);
   if (!st.ok()) return st;
   uint8_t* S = d_scratch_[scr_cur_];
+  st = Cuda(cudaEventRecord(hwait_ev_, stream_), "event");
+  if (!st.ok()) return st;
+  st = Cuda(cudaStreamWaitEvent(hstream_, hwait_ev_, 0), "wait stream");
+  if (!st.ok()) return st;
 
   FlushDesc fd;
   memset(&fd, 0, sizeof(fd));
@@ -1168,7 +1181,7 @@ Status Splitter::Flush() {
   memcpy(hc, pending_cols_.data(), sizeof(ColPtr) * NB * C);
   memcpy(htab + tb_batches + tb_tiles + tb_cols, tiles.data(), sizeof(TileDesc) * NT);
   if (staged_tables) {
-    st = Cuda(cudaMemcpyAsync(d_stage_[cur_], h_stage_[cur_], used_, cudaMemcpyHostToDevice, stream_), "H2D");
+    st = Cuda(cudaMemcpyAsync(d_stage_[cur_], h_stage_[cur_], used_, cudaMemcpyHostToDevice, hstream_), "H2D");
     stat_h2d_bytes_ += (int64_t)used_;
     if (!st.ok()) return st;
   } else {
@@ -1177,13 +1190,13 @@ Status Splitter::Flush() {
       if (!st.ok()) return st;
       st = Cuda(cudaEventRecord(gather_ev_, cstream_), "event");
       if (!st.ok()) return st;
-      st = Cuda(cudaStreamWaitEvent(stream_, gather_ev_, 0), "wait gather");
+      st = Cuda(cudaStreamWaitEvent(hstream_, gather_ev_, 0), "wait gather");
       if (!st.ok()) return st;
     }
     dtab = S + s_tab;
-    st = Cuda(cudaMemcpyAsync(dtab, htab, tb_total, cudaMemcpyHostToDevice, stream_), "H2D tables");
+    st = Cuda(cudaMemcpyAsync(dtab, htab, tb_total, cudaMemcpyHostToDevice, hstream_), "H2D tables");
     if (!st.ok()) return st;
-    st = Cuda(cudaEventRecord(tab_ev_[tab_cur_], stream_), "event");
+    st = Cuda(cudaEventRecord(tab_ev_[tab_cur_], hstream_), "event");
     if (!st.ok()) return st;
     tab_busy_[tab_cur_] = true;
     tab_cur_ = (tab_cur_ + 1) % kTabBufs;
@@ -1193,17 +1206,17 @@ Status Splitter::Flush() {
   fd.cols = reinterpret_cast<const ColPtr*>(dtab + tb_batches + tb_tiles);
   fd.tiles = reinterpret_cast<const TileDesc*>(dtab + tb_batches + tb_tiles + tb_cols);
 
-  st = Cuda(cudaMemsetAsync(S + s_null, 0, (size_t)NB * A * 4, stream_), "memset");
+  st = Cuda(cudaMemsetAsync(S + s_null, 0, (size_t)NB * A * 4, hstream_), "memset");
   if (!st.ok()) return st;
-  st = Cuda(cudaMemsetAsync(S + s_call, 0, (size_t)NB * 4, stream_), "memset");
+  st = Cuda(cudaMemsetAsync(S + s_call, 0, (size_t)NB * 4, hstream_), "memset");
   if (!st.ok()) return st;
-  st = Cuda(cudaMemsetAsync(fd.emit_count, 0, 4, stream_), "memset");
+  st = Cuda(cudaMemsetAsync(fd.emit_count, 0, 4, hstream_), "memset");
   if (!st.ok()) return st;
   if (!fd.hist_in_smem) {
-    st = Cuda(cudaMemsetAsync(S + s_cnt, 0, TP * 4, stream_), "memset");
+    st = Cuda(cudaMemsetAsync(S + s_cnt, 0, TP * 4, hstream_), "memset");
     if (!st.ok()) return st;
     if (nstr) {
-      st = Cuda(cudaMemsetAsync(S + s_bcnt, 0, TP * nstr * 4, stream_), "memset");
+      st = Cuda(cudaMemsetAsync(S + s_bcnt, 0, TP * nstr * 4, hstream_), "memset");
       if (!st.ok()) return st;
     }
   }
@@ -1213,14 +1226,14 @@ Status Splitter::Flush() {
   }
   if (n_jobs) {  // the nested columns' row ranges and lengths, before anything reads them
     st = Cuda(launch_nest_prep(reinterpret_cast<const NestJob*>(dtab + tb_batches + tb_tiles + tb_cols + tb_tdesc),
-                               (uint32_t)n_jobs, d_err_, stream_),
+                               (uint32_t)n_jobs, d_err_, hstream_),
               "k_nest_prep");
     if (!st.ok()) return st;
   }
-  cudaEventRecord(fr.ev[0], stream_);
-  st = Cuda(launch_hash_count(sd_, fd, stream_), "k_hash_count");
+  cudaEventRecord(fr.ev[0], hstream_);
+  st = Cuda(launch_hash_count(sd_, fd, hstream_), "k_hash_count");
   if (!st.ok()) return st;
-  cudaEventRecord(fr.ev[1], stream_);
+  cudaEventRecord(fr.ev[1], hstream_);
   // the plan on pstream_, after this pass's k_hash_count (and the previous pass's plan)
   st = Cuda(cudaStreamWaitEvent(pstream_, fr.ev[1], 0), "wait k_hash_count");
   if (!st.ok()) return st;
@@ -1430,6 +1443,8 @@ void Splitter::DiskSpillStats(int64_t* out3) const {
 
 Status Splitter::SyncAndCheck() {
   Status st = Cuda(cudaStreamSynchronize(cstream_), "host reads");
+  if (!st.ok()) return st;
+  st = Cuda(cudaStreamSynchronize(hstream_), "device work");
   if (!st.ok()) return st;
   st = Cuda(cudaStreamSynchronize(stream_), "device work");
   if (!st.ok()) return st;

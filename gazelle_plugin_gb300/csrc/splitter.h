@@ -172,8 +172,8 @@ class Splitter {
     uint8_t* h_bits = nullptr;          // pinned copy of just the bit regions (compressed Stop)
     size_t meta_words = 0;
     uint32_t emit_cap = 0;
-    // [0] k_hash_count start, [1] its end, [4] k_scatter start, [3] its end (stream_); [5] plan
-    // start, [2] its end, [6] the end of the pass's work on pstream_ (plan + metadata copies)
+    // [0] k_hash_count start, [1] its end (hstream_); [4] k_scatter start, [3] its end (stream_); [5]
+    // plan start, [2] its end, [6] the end of the pass's work on pstream_ (plan + metadata copies)
     cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     bool launched = false;              // its k_scatter is queued (ev[3] recorded)
     int scratch = 0;                    // which scratch buffer the pass used
@@ -309,14 +309,17 @@ class Splitter {
   unsigned long long* st_ihn_ = nullptr;
   int32_t* d_err_ = nullptr;
   uint32_t* d_call_ = nullptr;
-  // The pass schedule: k_hash_count and k_scatter run one after the other on stream_, the plan
-  // kernels on pstream_.  With device-resident inputs a pass's k_scatter is queued only when the
-  // next pass is (or at a sync), after that pass's k_hash_count, so the plan of pass i runs beside
-  // k_hash_count of pass i + 1 and k_scatter of pass i - 1 instead of delaying stream_; with host
-  // inputs (bound by the host link) it is queued right after its own plan.  The per-pass scratch is therefore
-  // double-buffered (scr_cur_: the buffer of the next pass); stream order keeps a buffer's next
+  // The pass schedule: k_hash_count (with its pass's table copies and clears) on hstream_, the
+  // plan kernels on pstream_, k_scatter on stream_.  A pass's work on hstream_ waits for
+  // everything queued on stream_ when the pass is flushed (hwait_ev_).  With device-resident
+  // inputs a pass's k_scatter is queued only when the next pass is (or at a sync), so k_scatter of
+  // pass i runs beside k_hash_count and the plan of pass i + 1; with host inputs (bound by the
+  // host link) it is queued right after its own plan.  The per-pass scratch is therefore
+  // double-buffered (scr_cur_: the buffer of the next pass); hwait_ev_ keeps a buffer's next
   // k_hash_count behind the k_scatter that last read it.
   cudaStream_t pstream_ = nullptr;
+  cudaStream_t hstream_ = nullptr;
+  cudaEvent_t hwait_ev_ = nullptr;
   uint8_t* d_scratch_[2] = {nullptr, nullptr};
   size_t scratch_cap_[2] = {0, 0};
   int scr_cur_ = 0;
