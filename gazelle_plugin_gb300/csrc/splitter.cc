@@ -278,7 +278,8 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
   if (!st.ok()) return st;
   {
     // host reads, then the plan kernels, get the higher priorities: their few CTAs are
-    // scheduled ahead of the remaining CTAs of a running k_hash_count / k_scatter
+    // scheduled ahead of the remaining CTAs of a running k_scatter; k_hash_count gets the lowest,
+    // so it takes the SMs k_scatter leaves idle instead of delaying it
     int least = 0, greatest = 0;
     cudaDeviceGetStreamPriorityRange(&least, &greatest);
     st = Cuda(cudaStreamCreateWithPriority(&cstream_, cudaStreamNonBlocking, greatest), "cudaStreamCreate");
@@ -286,13 +287,18 @@ Status Splitter::Init(const std::string& short_name, std::vector<Field> fields, 
     st = Cuda(cudaStreamCreateWithPriority(&pstream_, cudaStreamNonBlocking, std::min(greatest + 1, least)),
               "cudaStreamCreate");
     if (!st.ok()) return st;
-    st = Cuda(cudaStreamCreateWithPriority(&stream_, cudaStreamNonBlocking, least), "cudaStreamCreate");
+    st = Cuda(cudaStreamCreateWithPriority(&stream_, cudaStreamNonBlocking, std::min(greatest + 2, least)),
+              "cudaStreamCreate");
     if (!st.ok()) return st;
     st = Cuda(cudaStreamCreateWithPriority(&hstream_, cudaStreamNonBlocking, least), "cudaStreamCreate");
     if (!st.ok()) return st;
   }
   st = Cuda(cudaEventCreateWithFlags(&hwait_ev_, cudaEventDisableTiming), "cudaEventCreate");
   if (!st.ok()) return st;
+  for (auto& e : scr_ev_) {
+    st = Cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+    if (!st.ok()) return st;
+  }
   st = Cuda(cudaStreamCreateWithFlags(&ostream_, cudaStreamNonBlocking), "cudaStreamCreate");
   if (!st.ok()) return st;
   st = Cuda(cudaEventCreateWithFlags(&gather_ev_, cudaEventDisableTiming), "cudaEventCreate");
@@ -378,8 +384,9 @@ Splitter::~Splitter() {
     if (d_stage_[i]) cudaFreeAsync(d_stage_[i], stream_);
     if (stage_ev_[i]) cudaEventDestroy(stage_ev_[i]);
   }
-  for (int i = 0; i < 2; i++) {
+  for (int i = 0; i < kScratchBufs; i++) {
     if (d_scratch_[i]) cudaFreeAsync(d_scratch_[i], stream_);
+    if (scr_ev_[i]) cudaEventDestroy(scr_ev_[i]);
   }
   if (d_state_) cudaFreeAsync(d_state_, stream_);
   if (d_iota_ || !old_iota_.empty()) {
@@ -888,9 +895,11 @@ Status Splitter::PinnedMeta(size_t bytes, uint32_t** out) {
   return Status::OK();
 }
 
-Status Splitter::EnsureScratch(size_t bytes) {
+Status Splitter::EnsureScratch(size_t bytes, bool* fresh) {
   const int i = scr_cur_;
+  *fresh = false;
   if (bytes <= scratch_cap_[i]) return Status::OK();
+  *fresh = true;
   // stream-ordered (no wait for the whole device, which other splitters may be using): the old
   // buffer is freed on stream_, which already waits for the last k_scatter that read it
   if (d_scratch_[i]) {
@@ -1073,13 +1082,18 @@ Status Splitter::Flush() {
   const bool staged_tables = host_in && !direct_;  // tables travel with the pinned staging copy
   const size_t s_tab = staged_tables ? 0 : take(tb_total);
   // this pass's scratch buffer: stream_ already holds the k_scatter that last read it (queued by
-  // the previous Flush), and this pass's work on hstream_ starts after what stream_ holds now
-  st = EnsureScratch(so);
+  // an earlier Flush); this pass's work on hstream_ starts after that k_scatter, or after all of
+  // stream_'s work so far when the buffer was (re)allocated there
+  bool fresh = false;
+  st = EnsureScratch(so, &fresh);
   if (!st.ok()) return st;
   uint8_t* S = d_scratch_[scr_cur_];
-  st = Cuda(cudaEventRecord(hwait_ev_, stream_), "event");
-  if (!st.ok()) return st;
-  st = Cuda(cudaStreamWaitEvent(hstream_, hwait_ev_, 0), "wait stream");
+  if (fresh) {
+    st = Cuda(cudaEventRecord(hwait_ev_, stream_), "event");
+    if (st.ok()) st = Cuda(cudaStreamWaitEvent(hstream_, hwait_ev_, 0), "wait stream");
+  } else if (scr_used_[scr_cur_]) {
+    st = Cuda(cudaStreamWaitEvent(hstream_, scr_ev_[scr_cur_], 0), "wait scratch");
+  }
   if (!st.ok()) return st;
 
   FlushDesc fd;
@@ -1260,7 +1274,7 @@ Status Splitter::Flush() {
   pend_.stage = cur_;
   pend_.host_in = host_in;
   fr.scratch = scr_cur_;
-  scr_cur_ ^= 1;
+  scr_cur_ = (scr_cur_ + 1) % kScratchBufs;
   // host inputs: the pass is bound by the host link, not by the device; its k_scatter goes
   // right away so its partition data can start back to the host sooner.  So does the first
   // pass's: the device has nothing else to do while the host gathers the next pass.
@@ -1312,6 +1326,9 @@ Status Splitter::LaunchPendingScatter() {
   if (!st.ok()) return st;
   cudaEventRecord(f.ev[3], stream_);
   f.launched = true;
+  st = Cuda(cudaEventRecord(scr_ev_[f.scratch], stream_), "event");
+  if (!st.ok()) return st;
+  scr_used_[f.scratch] = true;
   if (pend_.host_in) {
     st = Cuda(cudaEventRecord(stage_ev_[pend_.stage], stream_), "event");
     if (!st.ok()) return st;
@@ -2115,7 +2132,7 @@ void Splitter::ReleaseStaging() {
     stage_busy_[i] = false;
   }
   stage_cap_ = 0;
-  for (int i = 0; i < 2; i++) {
+  for (int i = 0; i < kScratchBufs; i++) {
     if (d_scratch_[i]) cudaFreeAsync(d_scratch_[i], stream_);
     d_scratch_[i] = nullptr;
     scratch_cap_[i] = 0;

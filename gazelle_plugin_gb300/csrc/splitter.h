@@ -210,7 +210,7 @@ class Splitter {
   Status Init(const std::string& short_name, std::vector<Field> fields, int32_t P,
               std::vector<int32_t> keys, const GzSplitOptions& opts);
   Status Cuda(cudaError_t e, const char* what);
-  Status EnsureScratch(size_t bytes_needed);
+  Status EnsureScratch(size_t bytes_needed, bool* fresh);
   Status EnsureStaging(size_t bytes);
   void ReleaseStaging();
   uint8_t* HostAlloc(size_t bytes);
@@ -310,18 +310,21 @@ class Splitter {
   int32_t* d_err_ = nullptr;
   uint32_t* d_call_ = nullptr;
   // The pass schedule: k_hash_count (with its pass's table copies and clears) on hstream_, the
-  // plan kernels on pstream_, k_scatter on stream_.  A pass's work on hstream_ waits for
-  // everything queued on stream_ when the pass is flushed (hwait_ev_).  With device-resident
-  // inputs a pass's k_scatter is queued only when the next pass is (or at a sync), so k_scatter of
-  // pass i runs beside k_hash_count and the plan of pass i + 1; with host inputs (bound by the
-  // host link) it is queued right after its own plan.  The per-pass scratch is therefore
-  // double-buffered (scr_cur_: the buffer of the next pass); hwait_ev_ keeps a buffer's next
-  // k_hash_count behind the k_scatter that last read it.
+  // plan kernels on pstream_, k_scatter on stream_.  With device-resident inputs a pass's
+  // k_scatter is queued only when the next pass is (or at a sync), after that pass's k_hash_count
+  // and plan; with host inputs (bound by the host link) it is queued right after its own plan.
+  // The per-pass scratch has three buffers (scr_cur_: the buffer of the next pass), so a pass's
+  // k_hash_count waits only for the k_scatter two passes back (scr_ev_) and is ready while the
+  // previous pass's k_scatter runs: stream priorities (k_gather, then the plan, then k_scatter,
+  // then k_hash_count) let its blocks take the SMs that k_scatter's last wave leaves idle.
+  static constexpr int kScratchBufs = 3;
   cudaStream_t pstream_ = nullptr;
   cudaStream_t hstream_ = nullptr;
-  cudaEvent_t hwait_ev_ = nullptr;
-  uint8_t* d_scratch_[2] = {nullptr, nullptr};
-  size_t scratch_cap_[2] = {0, 0};
+  cudaEvent_t hwait_ev_ = nullptr;                 // stream_'s work so far (a scratch buffer allocated)
+  cudaEvent_t scr_ev_[kScratchBufs] = {};          // the last k_scatter that read each buffer
+  bool scr_used_[kScratchBufs] = {};
+  uint8_t* d_scratch_[kScratchBufs] = {};
+  size_t scratch_cap_[kScratchBufs] = {};
   int scr_cur_ = 0;
   struct PendingScatter {
     bool valid = false;
