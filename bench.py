@@ -873,9 +873,9 @@ def run_gpu(args):
                                    "launch of this workload (its ratio to that launch's algorithmic "
                                    "bytes, from the committed capture summary), scaled to this run's "
                                    "average launch"),
-                "overlap": ("k_scatter of pass i runs after k_hash_count of pass i + 1 on one "
-                            "stream, beside the plan kernels of pass i + 1; its duration is the "
-                            "live one"),
+                "overlap": ("k_scatter of pass i runs beside k_hash_count and the plan kernels of "
+                            "pass i + 1 (their own streams; k_hash_count at the lowest priority); "
+                            "its duration is the live one"),
                 "launches_per_step": flushes,
                 "algorithmic_bytes_per_launch": alg_bytes / max(flushes, 1),
                 "avg_launch_ms": k_scat / max(flushes, 1)}
