@@ -276,8 +276,8 @@ def _device_batches(torch, batches):
 @pytest.mark.parametrize("flush,keep_dev,budget", [(1 << 20, 1, 64 << 30), (3 << 20, 0, 64 << 30),
                                                    (2 << 20, 1, 4 << 20)])
 def test_device_resident_inputs_many_passes(flush, keep_dev, budget):
-    # device-resident inputs: each pass's k_scatter is queued behind the next pass's
-    # k_hash_count; outputs moved to host after every pass, or past a small HBM budget
+    # device-resident inputs: each pass's k_scatter is queued when the next pass is flushed;
+    # outputs moved to host after every pass, or past a small HBM budget
     torch = pytest.importorskip("torch")
     batches = W.c2_batches(12, 24, 4096) + W.c2_batches(13, 3, 1000)
     keep, dev = _device_batches(torch, batches)
@@ -295,6 +295,33 @@ def test_device_resident_inputs_many_passes(flush, keep_dev, budget):
     w.close(h)
     ref = O.run_oracle(W.C2_SCHEMA, batches, 200, W.C2_KEYS)
     assert_same(res, data, ref)
+
+
+@pytest.mark.parametrize("input_kind", ["device", "host"])
+def test_passes_of_changing_size_reuse_and_grow_scratch(input_kind):
+    """Passes of many small batches, then of single large ones, then small again: the per-pass
+    scratch buffers (three, reused in turn while the passes before are still queued) grow in the
+    middle of the split; every byte equal to the oracle's."""
+    torch = pytest.importorskip("torch")
+    batches = (W.c2_batches(21, 30, 200) + W.c2_batches(22, 6, 4096) + W.c2_batches(23, 3, 16384) +
+               W.c2_batches(24, 20, 300) + W.c2_batches(25, 2, 16384))
+    w = S.ShuffleSplitterJniWrapper()
+    part = S.NativePartitioning("hash", 200, None, W.C2_KEYS, list(W.C2_SCHEMA))
+    if input_kind == "device":
+        keep, dev = _device_batches(torch, batches)
+        h = w.make(part, writeSchema=False, input_kind=S.GZ_INPUT_DEVICE_RETAINED, flush_bytes=1 << 20)
+        for n, addrs, sizes in dev:
+            w.split(h, n, addrs, sizes)
+    else:
+        h = w.make(part, writeSchema=False, flush_bytes=1 << 20)
+        for b in batches:
+            a, z = b.addrs_sizes()
+            w.split(h, b.num_rows, a, z)
+    assert w.stats(h)[0] >= 8
+    res = w.stop(h)
+    data = w.data(h)
+    w.close(h)
+    assert_same(res, data, O.run_oracle(W.C2_SCHEMA, batches, 200, W.C2_KEYS))
 
 
 def test_device_resident_inputs_offheap_split_size():
