@@ -226,8 +226,10 @@ GzStatus gz_split_last_pids(int64_t handle, uint16_t* out, int32_t num_rows);
 /* Message of the last error on `handle` (0: the calling thread's last make error). */
 GzStatus gz_last_error(int64_t handle, char* buf, size_t len);
 
-/* Device time (ms, CUDA events on the splitter's stream) spent in each kernel family since
- * make: [hash+count, plan+scan, scatter, total device].  Test / bench hook. */
+/* Device time (ms, CUDA events on the stream each family runs on) spent in each kernel family
+ * since make: [hash+count, plan+scan, scatter, total device].  The families of neighbouring
+ * passes run at the same time, so an event span can include other families' work.  Test /
+ * bench hook. */
 GzStatus gz_split_kernel_times(int64_t handle, double* out4);
 
 /* Counters of this handle: [0] device passes, [1] input bytes gathered, [2] bytes copied
